@@ -1,0 +1,205 @@
+"""CPU tests of the oracle: pinned against the reference's AMOS build (when the
+reference tree is present), against the committed golden fixtures, against
+scipy, and against physics identities (rotation/translation invariance, energy
+balance). No GPU."""
+import glob
+import os
+
+import numpy as np
+import pytest
+from scipy import special as sp
+from scipy.spatial.transform import Rotation
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+nm = 1e-9
+
+
+def load_cluster(O, g):
+    return O.Cluster(xyz=g["xyz"], radius=g["radius"], eps=g["eps"], mu=g["mu"],
+                     eps_sh=g["eps_sh"], nmax=int(g["nmax"]), wavelength=float(g["wavelength"]),
+                     bg_eps=complex(g["bg"][0]), bg_mu=complex(g["bg"][1]),
+                     theta=float(g["angles"][0]), phi=float(g["angles"][1]),
+                     e_theta=complex(g["pol"][0]), e_phi=complex(g["pol"][1]))
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_bessel_against_reference_amos_table(oracle):
+    g = np.load(os.path.join(GOLDEN, "bessel_amos.npz"))
+    for i, z in enumerate(g["z"]):
+        J, dJ = oracle.bessel(0, complex(z), 25)
+        H, dH = oracle.bessel(1, complex(z), 25)
+        # AMOS loses relative accuracy next to zeros of j_n; compare against the
+        # local scale of the sequence.
+        scale = np.maximum(np.abs(g["J"][i]), 1e-3 * np.max(np.abs(g["J"][i])))
+        assert np.max(np.abs(J - g["J"][i]) / scale) < 1e-11, z
+        assert np.max(np.abs(H - g["H"][i]) / np.abs(g["H"][i])) < 1e-12, z
+        assert np.max(np.abs(dH[1:] - g["dH"][i][1:]) / np.abs(g["dH"][i][1:])) < 1e-12, z
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/srcAna/amos.c"),
+                    reason="reference tree absent (GPU box): AMOS pin runs where it exists")
+def test_bessel_against_live_amos(oracle):
+    oracle.build(ref=True)
+    rng = np.random.default_rng(3)
+    zs = list(rng.uniform(0.05, 90, 20)) + list(rng.uniform(0.1, 8, 10) + 1j * rng.uniform(0, 3, 10))
+    for z in zs:
+        z = complex(z)
+        oracle.use_amos(False)
+        a, _ = oracle.bessel(1, z, 24)
+        oracle.use_amos(True)
+        b, _ = oracle.bessel(1, z, 24)
+        oracle.use_amos(False)
+        assert rel(a, b) < 1e-12
+
+
+def test_bessel_against_scipy(oracle):
+    n = np.arange(21)
+    for z in (0.3, 2.0, 9.7, 44.0):
+        J, dJ = oracle.bessel(0, complex(z), 20)
+        H, _ = oracle.bessel(1, complex(z), 20)
+        assert rel(J, sp.spherical_jn(n, z)) < 1e-13
+        assert rel(dJ[:-1], sp.spherical_jn(n, z, derivative=True)[:-1]) < 1e-12
+        assert rel(H, sp.spherical_jn(n, z) + 1j * sp.spherical_yn(n, z)) < 1e-13
+    # real-axis fix-up of Bessel.h: zero imaginary part for real arguments
+    J, _ = oracle.bessel(0, 3.0 + 0j, 8)
+    assert np.all(J.imag == 0)
+    # zero-argument branch
+    J, dJ = oracle.bessel(0, 0j, 4)
+    assert J[0] == 1 and np.all(J[1:] == 0) and np.all(dJ == 0)
+
+
+def test_spherical_harmonics_against_scipy(oracle):
+    rng = np.random.default_rng(0)
+    for n in range(0, 25):
+        for m in range(-n, n + 1):
+            t, p = rng.uniform(0.01, np.pi - 0.01), rng.uniform(-np.pi, np.pi)
+            y = oracle.ynm(n, m, t, p)
+            ys = sp.sph_harm_y(n, m, t, p)
+            assert abs(y - ys) <= 1e-12 * max(abs(ys), 1e-3)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))))
+def test_golden_fixture(oracle, path):
+    if path.endswith("bessel_amos.npz"):
+        pytest.skip("bessel table")
+    g = np.load(path)
+    cl = load_cluster(oracle, g)
+    pr = oracle.Problem(cl)
+    assert rel(pr.inc_coeffs(), g["inc"]) < 1e-12
+    for j in range(cl.n_spheres):
+        assert rel(pr.tmatrix(j), g["T"][j]) < 1e-11
+        assert rel(pr.tmatrix(j, sh=True), g["T_sh"][j]) < 1e-11
+    k, _ = pr.wave_numbers()
+    A, B = oracle.coupling(g["rel"], k, cl.nmax, True)
+    assert rel(A, g["A_irr"]) < 1e-11 and rel(B, g["B_irr"]) < 1e-11
+    A, B = oracle.coupling(g["rel"], k, cl.nmax, False)
+    assert rel(A, g["A_reg"]) < 1e-11 and rel(B, g["B_reg"]) < 1e-11
+    Q = pr.source_vector()
+    assert rel(Q, g["Q"]) < 1e-11
+    S = pr.scattering_matrix()
+    P = cl.P
+    blk = (slice(0, 2 * P), slice(2 * P, 4 * P)) if cl.n_spheres > 1 else (slice(0, 2 * P),) * 2
+    assert rel(S[blk], g["S_block"]) < 1e-11
+    assert rel(pr.scattering_matrix(sh=True)[blk], g["S_sh_block"]) < 1e-11
+    # Solution-level quantities: the fixture's Bessel values come from AMOS
+    # (accurate to ~2e-15 here) and the oracle's from recurrences (~2e-16); the
+    # solve amplifies that by the condition number of S (~1e5 for C0's
+    # high-index spheres), hence 5e-10 rather than 1e-10 at this level.
+    X = oracle.lu_solve(S, Q)
+    assert rel(X, g["X_sca"]) < 5e-10
+    # Internal coefficients are X_sca times Iaux, whose high-order entries are
+    # large (1/psi_n); errors are measured against that propagated scale.
+    ia = np.concatenate([pr.iaux(j) for j in range(cl.n_spheres)])
+    scale = np.abs(ia) * np.max(np.abs(g["X_sca"]))
+    assert np.max(np.abs(pr.internal(X) - g["X_int"]) / scale) < 5e-10
+    xs = pr.cross_sections(X)
+    assert np.max(np.abs(xs - g["xsec"]) / np.abs(g["xsec"])) < 5e-10
+    E, H = pr.near_field(X, pr.internal(X), g["points"])
+    assert rel(E, g["E"]) < 5e-10 and rel(H, g["H"]) < 5e-10
+
+
+def _solve(O, xyz, kdir, pol, nmax=5, eps=(2.0 + 0.1j) ** 2, radius=90 * nm):
+    th = np.arccos(kdir[2])
+    ph = np.arctan2(kdir[1], kdir[0])
+    eth = np.array([np.cos(th) * np.cos(ph), np.cos(th) * np.sin(ph), -np.sin(th)])
+    eph = np.array([-np.sin(ph), np.cos(ph), 0.0])
+    cl = O.Cluster(xyz=xyz, radius=radius, eps=eps, nmax=nmax, wavelength=650 * nm, theta=th,
+                   phi=ph, e_theta=pol @ eth, e_phi=pol @ eph)
+    return O.Problem(cl).wavelength_solve("lu")[0]
+
+
+def test_rotation_invariance_of_extinction(oracle):
+    """Rotating spheres, incidence and polarisation together leaves C_ext and
+    C_abs unchanged: pins the irregular and regular translation coefficients,
+    the spherical harmonics and the T-matrices jointly."""
+    pos = np.array([[0, 0, 0], [220, 30, -40], [-60, 210, 90]]) * nm
+    k0 = np.array([0.3, -0.5, 0.8])
+    k0 /= np.linalg.norm(k0)
+    e0 = np.cross(k0, [0, 0, 1.0])
+    e0 /= np.linalg.norm(e0)
+    base = _solve(oracle, pos, k0, e0)
+    R = Rotation.from_euler("zyz", [1.2, -0.3, 2.0]).as_matrix()
+    rot = _solve(oracle, pos @ R.T, R @ k0, R @ e0)
+    assert abs(rot[0] - base[0]) / abs(base[0]) < 1e-12
+    assert abs(rot[3] - base[3]) / abs(base[3]) < 1e-12
+
+
+def test_translation_convergence_single_sphere(oracle):
+    k0 = np.array([0.3, -0.5, 0.8])
+    k0 /= np.linalg.norm(k0)
+    e0 = np.cross(k0, [0, 0, 1.0])
+    e0 /= np.linalg.norm(e0)
+    a = _solve(oracle, np.zeros((1, 3)), k0, e0, nmax=12)
+    b = _solve(oracle, np.array([[80 * nm, -50 * nm, 60 * nm]]), k0, e0, nmax=12)
+    assert abs(b[0] - a[0]) / abs(a[0]) < 1e-11
+
+
+def test_single_sphere_energy_balance(oracle):
+    cl = oracle.Cluster(xyz=[[0, 0, 0]], radius=100 * nm, eps=(3.5 + 0.01j) ** 2, nmax=6,
+                        wavelength=600 * nm)
+    xs = oracle.Problem(cl).wavelength_solve("lu")[0]
+    assert abs(xs[0] - xs[1] - xs[3]) / xs[0] < 1e-12
+
+
+def test_axial_incidence_parity_trap(oracle):
+    """Incidence exactly along +z: the reference nudges theta after reflecting
+    negative m, so its x-polarised wave expands as i * y-polarised. The oracle
+    reproduces that (VIGdVIG, AuxCoefficients.cpp:217-240)."""
+    cl = oracle.Cluster(xyz=[[900 * nm, 0, 0]], radius=10 * nm, eps=2.0, nmax=12,
+                        wavelength=600 * nm)
+    pr = oracle.Problem(cl)
+    p = np.array([[30 * nm, 20 * nm, -50 * nm]])
+    E, _ = pr.near_field(np.zeros(pr.n), np.zeros(pr.n), p)
+    k = 2 * np.pi / (600 * nm)
+    expect = 1j * np.array([0, 1, 0]) * np.exp(1j * k * p[0, 2])
+    assert np.max(np.abs(E[0] - expect)) < 1e-4  # the 1e-6 theta nudge itself
+
+
+def test_gmres_matches_lu(oracle):
+    g = np.load(os.path.join(GOLDEN, "metal5.npz"))
+    pr = oracle.Problem(load_cluster(oracle, g))
+    S, Q = pr.scattering_matrix(), pr.source_vector()
+    x, it, rr = oracle.gmres(S, Q, tol=1e-13, maxit=400, restarts=3)
+    assert rr <= 1e-13 and it > 0
+    assert rel(x, oracle.lu_solve(S, Q)) < 1e-10
+
+
+def test_overlap_rejected(oracle):
+    cl = oracle.Cluster(xyz=[[0, 0, 0], [0, 0, 150 * nm]], radius=100 * nm, eps=2.0, nmax=2,
+                        wavelength=600 * nm)
+    with pytest.raises(RuntimeError, match="overlaps"):
+        oracle.Problem(cl)
+
+
+def test_thread_count_does_not_change_results(oracle):
+    g = np.load(os.path.join(GOLDEN, "diel3.npz"))
+    pr = oracle.Problem(load_cluster(oracle, g))
+    oracle.set_threads(1)
+    a = pr.wavelength_solve("lu")[0]
+    oracle.set_threads(4)
+    b = pr.wavelength_solve("lu")[0]
+    oracle.set_threads(1)
+    assert np.array_equal(a, b)
