@@ -1,0 +1,167 @@
+/*
+ * liboptimet_gpu: GB300 (sm_103a) implementation of OPTIMET-3D's multiple-
+ * scattering T-matrix hot path for clusters of spheres, behind a C ABI.
+ *
+ * Plain pointers and sizes only. Complex numbers are interleaved (re, im)
+ * doubles; vectors follow OPTIMET's layout: per sphere a TE block of P
+ * harmonics then a TM block, P = nMax (nMax + 2), harmonic p = n(n+1) - m - 1;
+ * matrices are column-major. Lengths are metres, angles radians.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the OPTIMET-3D source tree).
+ */
+#ifndef OPTIMET_GPU_H
+#define OPTIMET_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference throws std::runtime_error in these cases. */
+#define OM_OK 0
+#define OM_ERR_INVALID 1          /* bad argument (null, size, mixed nMax: PreconditionedMatrix.cpp:1161-1165) */
+#define OM_ERR_OVERLAP 2          /* overlapping spheres (Geometry.cpp:39-51) */
+#define OM_ERR_CUDA 3             /* CUDA runtime failure */
+#define OM_ERR_BUDGET 4           /* device-memory budget of the context exceeded */
+#define OM_ERR_NOT_CONVERGED 5    /* iterative solve stopped above tolerance */
+#define OM_ERR_SINGULAR 6         /* zero pivot in the LU factorisation (ScalapackSolver.cpp:76-77) */
+#define OM_ERR_STATE 7            /* call out of order (e.g. solve before assemble) */
+
+/* Harmonic selector */
+#define OM_FF 0                   /* fundamental frequency */
+#define OM_SH 1                   /* second harmonic (2 omega, eps_SH) */
+
+/* Storage precision of the scattering matrix */
+#define OM_C128 0                 /* complex FP64 */
+#define OM_C64 1                  /* complex FP32 (precision form) */
+
+/* Solve methods (Solver roles of the reference) */
+#define OM_SOLVE_LU 0             /* dense LU, partial pivoting: ScalapackSolver pzgesv role */
+#define OM_SOLVE_GMRES 1          /* restarted GMRES: MatrixBelosSolver / Gmres_Zcomp role */
+#define OM_SOLVE_FGMRES_MIXED 2   /* FP64 outer FGMRES around FP32 inner GMRES on the C64 matrix */
+#define OM_SOLVE_LU_MIXED 3       /* FP32 LU + FP64 iterative refinement */
+
+typedef struct om_context om_context;
+typedef struct om_problem om_problem;
+
+typedef struct {
+  double x, y, z;        /* centre (XML <cartesian> times 1e-9) */
+  double radius;         /* <properties radius> times 1e-9 */
+  double eps_r[2];       /* relative permittivity at the fundamental */
+  double mu_r[2];        /* relative permeability */
+  double eps_r_sh[2];    /* relative permittivity at the second harmonic (<epsilon_SH>) */
+  int nmax;              /* <harmonics nmax>; equal for all spheres */
+  int reserved;
+} om_sphere;
+
+typedef struct {
+  double eps_r[2];       /* background relative permittivity (<background>) */
+  double mu_r[2];
+} om_medium;
+
+typedef struct {
+  double wavelength;     /* <wavelength value> times 1e-9 */
+  double theta, phi;     /* <propagation>, radians */
+  double e_theta[2];     /* <polarization Etheta> */
+  double e_phi[2];       /* <polarization Ephi> */
+  int sh;                /* <SHsources condition="yes"> */
+  int reserved;
+} om_plane_wave;
+
+typedef struct {
+  int method;            /* OM_SOLVE_* */
+  int max_iter;          /* Krylov dimension per restart cycle */
+  int restarts;          /* restart cycles */
+  int inner_iter;        /* inner FP32 GMRES iterations per outer step (mixed) */
+  double tol;            /* relative residual ||b - S x|| / ||b|| */
+  double inner_tol;      /* inner relative tolerance (mixed) */
+} om_solve_options;
+
+typedef struct {
+  int iterations;        /* Krylov iterations (outer for the mixed form) */
+  int inner_iterations;  /* total inner FP32 iterations (mixed) */
+  double rel_residual;   /* final FP64 relative residual */
+  double seconds;        /* device time of the solve */
+} om_solve_stats;
+
+/* Device context: one GPU, one stream, a device-memory budget (0 = no limit).
+ * Replaces the process-level state of mpi::init / scalapack::Context
+ * (srcAna/mpi/Session.cpp:38-64, srcAna/scalapack/Context.h:32-169). */
+int om_context_create(int device, size_t budget_bytes, om_context **out);
+void om_context_destroy(om_context *ctx);
+const char *om_context_last_error(const om_context *ctx);
+/* Number of kernels the last call on this context launched. */
+int om_context_last_launches(const om_context *ctx);
+/* Wait for all work queued on the context's stream (calls are asynchronous
+ * with respect to the host unless they return data). */
+int om_context_synchronize(om_context *ctx);
+
+/* Geometry + Excitation for one cluster at one wavelength. Mirrors
+ * simulation_input (Reader.cpp:55-101,585-663,782-834): spheres are stored in
+ * spherical coordinates, overlap is rejected, the plane wave is expanded
+ * (Excitation::populate, Excitation.cpp:48-75). */
+int om_problem_create(om_context *ctx, const om_sphere *spheres, int n_spheres,
+                      const om_medium *background, const om_plane_wave *wave,
+                      om_problem **out);
+void om_problem_destroy(om_problem *pr);
+/* Excitation::updateWavelength (Excitation.cpp:132-137) + Geometry::update. */
+int om_problem_set_wavelength(om_problem *pr, double wavelength);
+/* Number of unknowns 2 P N (AbstractSolver::scattering_size, Solver.h:118-121). */
+long om_problem_size(const om_problem *pr);
+
+/* Coupling(relR, waveK, nMax, regular) (Coupling.h:29-41, Coupling.cpp:80-87):
+ * A ("diagonal") and B ("offdiagonal"), P x P column-major, for `count`
+ * displacements rel_xyz[3*count] (Cartesian, metres). `regular` keeps the
+ * reference's inverted meaning: 1 -> Hankel (irregular), 0 -> Bessel. */
+int om_coupling(om_context *ctx, const double *rel_xyz, int count, double k_re, double k_im,
+                int nmax, int regular, double *A, double *B);
+
+/* Diagonal T-matrices, N x 2P (Scatterer::getTLocal / getTLocalSH,
+ * Scatterer.cpp:39-161). */
+int om_tmatrix(om_problem *pr, int harmonic, double *T);
+/* Plane-wave coefficients [a_p | b_p], 2P (Excitation::dataIncAp/Bp). */
+int om_incident_coefficients(om_problem *pr, double *ab);
+
+/* preconditioned_scattering_matrix[SH] (PreconditionedMatrix.cpp:350-400,555-610,
+ * 1137-1184): S_ii = I, S_ij = -T_i [A^T B^T; B^T A^T](r_i - r_j), kept on the
+ * device in the requested precision. */
+int om_assemble(om_problem *pr, int harmonic, int precision);
+/* Copy the assembled matrix to the host (complex128, column-major n x n). */
+int om_copy_matrix(om_problem *pr, int harmonic, double *S);
+/* source_vector (PreconditionedMatrix.cpp:1327-1345): Q_i = T_i IncLocal_i.
+ * Q may be NULL (kept on the device). */
+int om_source_vector(om_problem *pr, double *Q);
+/* AbstractSolver::solve for the fundamental (PreconditionedMatrixSolver.h:45-79,
+ * ScalapackSolver.cpp:54-130, MatrixBelosSolver.cpp:26-104), followed by
+ * convertInternal (Solver.cpp:57-77). */
+int om_solve(om_problem *pr, const om_solve_options *opts, om_solve_stats *stats);
+/* Solve S x = b for a caller-supplied right-hand side with the assembled matrix. */
+int om_solve_rhs(om_problem *pr, int harmonic, const om_solve_options *opts, const double *b,
+                 double *x, om_solve_stats *stats);
+/* Scattered and internal coefficients (n each; either may be NULL). */
+int om_get_coefficients(om_problem *pr, double *X_sca, double *X_int);
+/* Result::getExtinctionCrossSection, getScatteringCrossSection,
+ * getAbsorptionCrossSection (Result.cpp:541-631):
+ * out = {C_ext, C_sca, C_ext - C_sca (the scan's absorption column,
+ * Simulation.cpp:659), C_abs from the Mie factors (Geometry.cpp:86-145)}. */
+int om_cross_sections(om_problem *pr, double out[4]);
+/* Result::getEHFields at Cartesian points (Result.cpp:74-301), fundamental,
+ * Cartesian components: E, H are 3 complex per point. */
+int om_near_field(om_problem *pr, const double *xyz, int npts, double *E, double *H);
+
+/* One wavelength-solve from host buffers to host buffers: problem set-up,
+ * source vector, FF assembly, solve, internal coefficients, cross sections
+ * (the body of Simulation::scan_wavelengths' loop, Simulation.cpp:643-674).
+ * X_sca / X_int may be NULL. */
+int om_wavelength_solve(om_context *ctx, const om_sphere *spheres, int n_spheres,
+                        const om_medium *background, const om_plane_wave *wave,
+                        const om_solve_options *opts, int precision, double xsec[4],
+                        double *X_sca, double *X_int, om_solve_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPTIMET_GPU_H */

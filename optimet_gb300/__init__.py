@@ -1,0 +1,292 @@
+"""optimet_gb300: GB300-native OPTIMET-3D sphere path (T-matrix multiple
+scattering) behind the C ABI of include/optimet_gpu.h.
+
+Low level: ``Context``, ``Problem``, ``coupling`` and ``wavelength_solve`` wrap
+the C entry points one to one. The reference's own interface (Geometry,
+Scatterer, Excitation, solver.factory, Result, simulation_input) is mirrored
+in :mod:`optimet_gb300.optimet`.
+
+The library must be built for sm_103a (``python -m optimet_gb300.build``);
+there is no CPU fallback: loading fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboptimet_gpu.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "optimet_gpu.h")
+
+OK, ERR_INVALID, ERR_OVERLAP, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_SINGULAR, ERR_STATE = range(8)
+FF, SH = 0, 1
+C128, C64 = 0, 1
+SOLVE_LU, SOLVE_GMRES, SOLVE_FGMRES_MIXED, SOLVE_LU_MIXED = 0, 1, 2, 3
+
+ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_OVERLAP: "overlapping spheres",
+               ERR_CUDA: "CUDA failure", ERR_BUDGET: "device-memory budget exceeded",
+               ERR_NOT_CONVERGED: "not converged", ERR_SINGULAR: "singular matrix",
+               ERR_STATE: "call out of order"}
+
+
+class OptimetError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Sphere(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("radius", C.c_double),
+                ("eps_r", C.c_double * 2), ("mu_r", C.c_double * 2), ("eps_r_sh", C.c_double * 2),
+                ("nmax", C.c_int), ("reserved", C.c_int)]
+
+
+class Medium(C.Structure):
+    _fields_ = [("eps_r", C.c_double * 2), ("mu_r", C.c_double * 2)]
+
+
+class PlaneWave(C.Structure):
+    _fields_ = [("wavelength", C.c_double), ("theta", C.c_double), ("phi", C.c_double),
+                ("e_theta", C.c_double * 2), ("e_phi", C.c_double * 2), ("sh", C.c_int),
+                ("reserved", C.c_int)]
+
+
+class SolveOptions(C.Structure):
+    _fields_ = [("method", C.c_int), ("max_iter", C.c_int), ("restarts", C.c_int),
+                ("inner_iter", C.c_int), ("tol", C.c_double), ("inner_tol", C.c_double)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("inner_iterations", C.c_int),
+                ("rel_residual", C.c_double), ("seconds", C.c_double)]
+
+
+_lib = None
+_dp = C.POINTER(C.c_double)
+
+
+def lib():
+    """Load liboptimet_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run `python -m optimet_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        vp, pvp = C.c_void_p, C.POINTER(C.c_void_p)
+        L.om_context_create.argtypes = [C.c_int, C.c_size_t, pvp]
+        L.om_context_destroy.argtypes = [vp]
+        L.om_context_last_error.argtypes = [vp]
+        L.om_context_last_error.restype = C.c_char_p
+        L.om_context_last_launches.argtypes = [vp]
+        L.om_context_synchronize.argtypes = [vp]
+        L.om_problem_create.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
+                                        C.POINTER(PlaneWave), pvp]
+        L.om_problem_destroy.argtypes = [vp]
+        L.om_problem_set_wavelength.argtypes = [vp, C.c_double]
+        L.om_problem_size.argtypes = [vp]
+        L.om_problem_size.restype = C.c_long
+        L.om_coupling.argtypes = [vp, _dp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, _dp, _dp]
+        L.om_tmatrix.argtypes = [vp, C.c_int, _dp]
+        L.om_incident_coefficients.argtypes = [vp, _dp]
+        L.om_assemble.argtypes = [vp, C.c_int, C.c_int]
+        L.om_copy_matrix.argtypes = [vp, C.c_int, _dp]
+        L.om_source_vector.argtypes = [vp, _dp]
+        L.om_solve.argtypes = [vp, C.POINTER(SolveOptions), C.POINTER(SolveStats)]
+        L.om_solve_rhs.argtypes = [vp, C.c_int, C.POINTER(SolveOptions), _dp, _dp,
+                                   C.POINTER(SolveStats)]
+        L.om_get_coefficients.argtypes = [vp, _dp, _dp]
+        L.om_cross_sections.argtypes = [vp, _dp]
+        L.om_near_field.argtypes = [vp, _dp, C.c_int, _dp, _dp]
+        L.om_wavelength_solve.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
+                                          C.POINTER(PlaneWave), C.POINTER(SolveOptions), C.c_int,
+                                          _dp, _dp, _dp, C.POINTER(SolveStats)]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def options(method=SOLVE_GMRES, tol=1e-10, max_iter=200, restarts=10, inner_iter=40,
+            inner_tol=1e-4) -> SolveOptions:
+    return SolveOptions(method, max_iter, restarts, inner_iter, tol, inner_tol)
+
+
+class Context:
+    """One GPU, one stream, an optional device-memory budget in bytes."""
+
+    def __init__(self, device: int = 0, budget: int = 0):
+        h = C.c_void_p()
+        rc = lib().om_context_create(device, budget, C.byref(h))
+        if rc:
+            raise OptimetError(rc, "cannot create a CUDA context on device %d" % device)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().om_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def check(self, rc):
+        if rc not in (OK,):
+            raise OptimetError(rc, lib().om_context_last_error(self.h).decode())
+        return rc
+
+    def synchronize(self):
+        self.check(lib().om_context_synchronize(self.h))
+
+    @property
+    def last_launches(self) -> int:
+        return lib().om_context_last_launches(self.h)
+
+
+def spheres_array(xyz, radius, eps, nmax, mu=None, eps_sh=None):
+    xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = xyz.shape[0]
+    radius = np.broadcast_to(np.asarray(radius, dtype=np.float64), (n,))
+    eps = np.broadcast_to(np.asarray(eps, dtype=np.complex128), (n,))
+    mu = np.broadcast_to(np.asarray(1.0 if mu is None else mu, dtype=np.complex128), (n,))
+    eps_sh = eps if eps_sh is None else np.broadcast_to(np.asarray(eps_sh, dtype=np.complex128), (n,))
+    arr = (Sphere * n)()
+    for i in range(n):
+        s = arr[i]
+        s.x, s.y, s.z = xyz[i]
+        s.radius = radius[i]
+        s.eps_r[0], s.eps_r[1] = eps[i].real, eps[i].imag
+        s.mu_r[0], s.mu_r[1] = mu[i].real, mu[i].imag
+        s.eps_r_sh[0], s.eps_r_sh[1] = eps_sh[i].real, eps_sh[i].imag
+        s.nmax = int(nmax)
+    return arr
+
+
+def medium(eps=1.0, mu=1.0) -> Medium:
+    eps, mu = complex(eps), complex(mu)
+    return Medium((C.c_double * 2)(eps.real, eps.imag), (C.c_double * 2)(mu.real, mu.imag))
+
+
+def plane_wave(wavelength, theta=0.0, phi=0.0, e_theta=1.0, e_phi=0.0, sh=False) -> PlaneWave:
+    et, ep = complex(e_theta), complex(e_phi)
+    return PlaneWave(wavelength, theta, phi, (C.c_double * 2)(et.real, et.imag),
+                     (C.c_double * 2)(ep.real, ep.imag), int(sh), 0)
+
+
+class Problem:
+    """Geometry + Excitation of one cluster at one wavelength, device resident."""
+
+    def __init__(self, ctx: Context, spheres, bg: Medium | None, wave: PlaneWave):
+        self.ctx = ctx
+        h = C.c_void_p()
+        self._keep = (spheres, bg, wave)
+        rc = lib().om_problem_create(ctx.h, spheres, len(spheres),
+                                     None if bg is None else C.byref(bg), C.byref(wave), C.byref(h))
+        ctx.check(rc)
+        self.h = h
+        self.n = lib().om_problem_size(h)
+        self.nmax = spheres[0].nmax
+        self.P = self.nmax * (self.nmax + 2)
+        self.N = len(spheres)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().om_problem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_wavelength(self, wavelength):
+        self.ctx.check(lib().om_problem_set_wavelength(self.h, wavelength))
+
+    def tmatrix(self, harmonic=FF):
+        out = np.zeros((self.N, 2 * self.P), np.complex128)
+        self.ctx.check(lib().om_tmatrix(self.h, harmonic, _p(out)))
+        return out
+
+    def incident_coefficients(self):
+        out = np.zeros(2 * self.P, np.complex128)
+        self.ctx.check(lib().om_incident_coefficients(self.h, _p(out)))
+        return out
+
+    def assemble(self, harmonic=FF, precision=C128):
+        self.ctx.check(lib().om_assemble(self.h, harmonic, precision))
+
+    def matrix(self, harmonic=FF):
+        S = np.zeros((self.n, self.n), np.complex128, order="F")
+        self.ctx.check(lib().om_copy_matrix(self.h, harmonic, _p(S)))
+        return S
+
+    def source_vector(self, copy=True):
+        Q = np.zeros(self.n, np.complex128) if copy else None
+        self.ctx.check(lib().om_source_vector(self.h, _p(Q)))
+        return Q
+
+    def solve(self, opts: SolveOptions | None = None, allow_unconverged=False) -> SolveStats:
+        st = SolveStats()
+        rc = lib().om_solve(self.h, C.byref(opts or options()), C.byref(st))
+        if not (allow_unconverged and rc == ERR_NOT_CONVERGED):
+            self.ctx.check(rc)
+        return st
+
+    def solve_rhs(self, b, harmonic=FF, opts: SolveOptions | None = None):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros_like(b)
+        st = SolveStats()
+        self.ctx.check(lib().om_solve_rhs(self.h, harmonic, C.byref(opts or options()), _p(b),
+                                          _p(x), C.byref(st)))
+        return x, st
+
+    def coefficients(self):
+        xs = np.zeros(self.n, np.complex128)
+        xi = np.zeros(self.n, np.complex128)
+        self.ctx.check(lib().om_get_coefficients(self.h, _p(xs), _p(xi)))
+        return xs, xi
+
+    def cross_sections(self):
+        out = np.zeros(4)
+        self.ctx.check(lib().om_cross_sections(self.h, _p(out)))
+        return out
+
+    def near_field(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        E = np.zeros((xyz.shape[0], 3), np.complex128)
+        H = np.zeros_like(E)
+        self.ctx.check(lib().om_near_field(self.h, _p(xyz), xyz.shape[0], _p(E), _p(H)))
+        return E, H
+
+
+def coupling(ctx: Context, rel_xyz, k: complex, nmax: int, regular: bool):
+    """Coupling(relR, waveK, nMax, regular) for one or many Cartesian displacements."""
+    rel = np.ascontiguousarray(rel_xyz, dtype=np.float64).reshape(-1, 3)
+    P = nmax * (nmax + 2)
+    A = np.zeros((rel.shape[0], P, P), np.complex128)
+    B = np.zeros_like(A)
+    ctx.check(lib().om_coupling(ctx.h, _p(rel), rel.shape[0], complex(k).real, complex(k).imag,
+                                nmax, int(regular), _p(A), _p(B)))
+    # (count, col, row) in memory -> (count, row, col)
+    return A.transpose(0, 2, 1), B.transpose(0, 2, 1)
+
+
+def wavelength_solve(ctx: Context, spheres, bg, wave, opts=None, precision=C128, want_coeffs=False):
+    n = 2 * spheres[0].nmax * (spheres[0].nmax + 2) * len(spheres)
+    xsec = np.zeros(4)
+    xs = np.zeros(n, np.complex128) if want_coeffs else None
+    xi = np.zeros(n, np.complex128) if want_coeffs else None
+    st = SolveStats()
+    rc = lib().om_wavelength_solve(ctx.h, spheres, len(spheres), None if bg is None else C.byref(bg),
+                                   C.byref(wave), C.byref(opts or options()), precision, _p(xsec),
+                                   _p(xs), _p(xi), C.byref(st))
+    ctx.check(rc)
+    return xsec, xs, xi, st
+
+
+def declared_symbols():
+    """Entry points declared in include/optimet_gpu.h."""
+    import re
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(om_[a-z0-9_]+)\s*\(", text)))

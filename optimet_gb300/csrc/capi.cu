@@ -1,0 +1,726 @@
+// C ABI of liboptimet_gpu: host-side model set-up (the Reader / Geometry /
+// Excitation state of OPTIMET-3D), device-memory ownership and the call
+// sequence of one wavelength-solve.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "om_internal.h"
+
+using om::cplx;
+using om::zd;
+
+namespace {
+
+// srcAna/constants.cpp:19-41
+const double kPi = 3.14159265358979323846;
+const double kC = 299792458;
+const double kMu0 = 4.0 * kPi * 1e-7;
+const double kEps0 = 1.0 / (kMu0 * kC * kC);
+
+zd Z(cplx c) { return om::mk(c.real(), c.imag()); }
+
+int cuda_fail(om_context *ctx, cudaError_t e, const char *what) {
+  ctx->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return OM_ERR_CUDA;
+}
+
+int check_launch(om_context *ctx, const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess)
+    return cuda_fail(ctx, e, what);
+  return OM_OK;
+}
+
+template <typename T> int dev_alloc(om_context *ctx, T **p, size_t count) {
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  if(ctx->budget && ctx->used + bytes > ctx->budget) {
+    ctx->err = "device-memory budget exceeded (" + std::to_string(ctx->used + bytes) + " > " +
+               std::to_string(ctx->budget) + " bytes)";
+    return OM_ERR_BUDGET;
+  }
+  cudaError_t e = cudaMalloc((void **)p, bytes);
+  if(e != cudaSuccess) {
+    cudaGetLastError();
+    ctx->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return OM_ERR_BUDGET;
+  }
+  ctx->used += bytes;
+  return OM_OK;
+}
+
+template <typename T> void dev_free(om_context *ctx, T *&p, size_t count) {
+  if(p) {
+    cudaFree(p);
+    ctx->used -= std::max<size_t>(count, 1) * sizeof(T);
+    p = nullptr;
+  }
+}
+
+void to_sph(double x, double y, double z, double *o) { om::to_spherical(x, y, z, o, o + 1, o + 2); }
+
+// The per-wavelength scalars: Excitation (Excitation.cpp:31-45,132-137),
+// per-sphere wave numbers (Scatterer.cpp:39-161, Result.cpp:206-213).
+int update_wave(om_problem *pr) {
+  om_context *ctx = pr->ctx;
+  const cplx eps_b = pr->bg_eps_r * kEps0, mu_b = pr->bg_mu_r * kMu0;
+  const double k0 = 2 * kPi / pr->lambda;  // vKInc.rrr
+  pr->waveK = k0 * std::sqrt(pr->bg_eps_r * pr->bg_mu_r);
+  pr->omega = kC * k0;
+  pr->iZ = cplx(0.0, -1.0) / std::sqrt(mu_b / eps_b);
+  const double w = pr->omega;
+  const cplx waveK_0 = w * std::sqrt(kEps0 * kMu0);
+  std::vector<om::SphereScalars> sc(pr->N);
+  std::vector<zd> kin(pr->N), izin(pr->N);
+  for(int i = 0; i < pr->N; ++i) {
+    const cplx eps_s = pr->eps_r[i] * kEps0, mu_s = pr->mu_r[i] * kMu0;
+    const cplx eps_sh = pr->eps_r_sh[i] * kEps0;
+    const cplx k_s = w * std::sqrt(eps_s * mu_s);
+    const cplx k_b = w * std::sqrt(eps_b * mu_b);
+    const cplx k_s2 = 2.0 * w * std::sqrt(eps_sh * mu_s);
+    const cplx k_b2 = 2.0 * w * std::sqrt(eps_b * mu_b);
+    om::SphereScalars &s = sc[i];
+    s.rho = Z(k_s / k_b);
+    s.r0 = Z(k_b * pr->radius[i]);
+    s.mu_sob = Z(mu_s / mu_b);
+    s.mu_j = Z(mu_s);
+    s.mu_0 = Z(mu_b);
+    s.rho_sh = Z(k_s2 / k_b2);
+    s.r0_sh = Z(k_b2 * pr->radius[i]);
+    s.mu_sob_sh = Z(mu_s / mu_b);
+    kin[i] = Z(waveK_0 * std::sqrt(pr->eps_r[i] * pr->mu_r[i]));
+    izin[i] = Z(cplx(0.0, -1.0) / std::sqrt(mu_s / eps_s));
+  }
+  cudaMemcpyAsync(pr->d_scal, sc.data(), sizeof(om::SphereScalars) * pr->N, cudaMemcpyHostToDevice,
+                  ctx->stream);
+  cudaMemcpyAsync(pr->d_kin, kin.data(), sizeof(zd) * pr->N, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(pr->d_izin, izin.data(), sizeof(zd) * pr->N, cudaMemcpyHostToDevice, ctx->stream);
+  om::launch_sphere_terms(pr);
+  // Einc = toProjection((0, theta, phi), (0, E_theta, E_phi)) (Reader.cpp:815-827)
+  const double st = std::sin(pr->theta), ct = std::cos(pr->theta), sp = std::sin(pr->phi),
+               cp = std::cos(pr->phi);
+  const cplx Et = pr->e_theta, Ep = pr->e_phi;
+  const cplx ex = ct * cp * Et - sp * Ep, ey = ct * sp * Et + cp * Ep, ez = -st * Et;
+  const double einc[6] = {ex.real(), ex.imag(), ey.real(), ey.imag(), ez.real(), ez.imag()};
+  om::launch_incident(pr, einc);
+  // the incident-field vector must reach the device before the host buffer dies
+  cudaStreamSynchronize(ctx->stream);
+  pr->have_source = false;
+  pr->have_solution = false;
+  pr->S_prec[0] = pr->S_prec[1] = -1;
+  return check_launch(ctx, "per-sphere / incident kernels");
+}
+
+void free_problem(om_problem *pr) {
+  om_context *ctx = pr->ctx;
+  const size_t N = pr->N, P = pr->P, n = pr->n, nm = 2 * (pr->nmax + 1);
+  dev_free(ctx, pr->d_cart, 3 * N);
+  dev_free(ctx, pr->d_radius, N);
+  dev_free(ctx, pr->d_kin, N);
+  dev_free(ctx, pr->d_izin, N);
+  dev_free(ctx, pr->d_scal, N);
+  dev_free(ctx, pr->d_T, N * nm);
+  dev_free(ctx, pr->d_Tsh, N * nm);
+  dev_free(ctx, pr->d_iaux, N * nm);
+  dev_free(ctx, pr->d_cabs, N * nm);
+  dev_free(ctx, pr->d_inc, 2 * P);
+  dev_free(ctx, pr->d_incloc, n);
+  dev_free(ctx, pr->d_wsca, N * P);
+  dev_free(ctx, pr->d_Q, n);
+  dev_free(ctx, pr->d_X, n);
+  dev_free(ctx, pr->d_Xint, n);
+  dev_free(ctx, pr->d_xsec, 16);
+  for(int h = 0; h < 2; ++h) {
+    if(pr->d_S[h]) {
+      cudaFree(pr->d_S[h]);
+      ctx->used -= sizeof(double2) * n * n;
+      pr->d_S[h] = nullptr;
+    }
+    if(pr->d_S32[h]) {
+      cudaFree(pr->d_S32[h]);
+      ctx->used -= sizeof(float2) * n * n;
+      pr->d_S32[h] = nullptr;
+    }
+  }
+}
+
+int make_problem(om_context *ctx, const om_sphere *spheres, int n_spheres, const om_medium *bg,
+                 const om_plane_wave *wave, om_problem **out) {
+  if(!ctx || !out)
+    return OM_ERR_INVALID;
+  *out = nullptr;
+  if(!spheres || n_spheres < 1 || !wave) {
+    ctx->err = "need at least one sphere and a plane wave";
+    return OM_ERR_INVALID;
+  }
+  const int nmax = spheres[0].nmax;
+  for(int i = 0; i < n_spheres; ++i)
+    if(spheres[i].nmax != nmax) {
+      ctx->err = "All objects must have same number of harmonics";
+      return OM_ERR_INVALID;
+    }
+  if(nmax < 1 || nmax > om::kMaxNmax) {
+    ctx->err = "nmax must be in [1, " + std::to_string(om::kMaxNmax) + "]";
+    return OM_ERR_INVALID;
+  }
+  if(!(wave->wavelength > 0)) {
+    ctx->err = "wavelength must be positive";
+    return OM_ERR_INVALID;
+  }
+  om_problem *pr = new(std::nothrow) om_problem();
+  if(!pr)
+    return OM_ERR_INVALID;
+  pr->ctx = ctx;
+  pr->N = n_spheres;
+  pr->nmax = nmax;
+  pr->P = om::pmax(nmax);
+  pr->n = 2L * pr->P * n_spheres;
+  for(int i = 0; i < n_spheres; ++i) {
+    const om_sphere &s = spheres[i];
+    if(!(s.radius > 0)) {
+      ctx->err = "sphere " + std::to_string(i) + " has no positive radius";
+      delete pr;
+      return OM_ERR_INVALID;
+    }
+    double sp[3];
+    to_sph(s.x, s.y, s.z, sp);
+    // Geometry::pushObject (Geometry.cpp:39-51)
+    for(int j = 0; j < i; ++j) {
+      double a[3], b[3];
+      om::to_cartesian(pr->sph[3 * j], pr->sph[3 * j + 1], pr->sph[3 * j + 2], a, a + 1, a + 2);
+      om::to_cartesian(sp[0], sp[1], sp[2], b, b + 1, b + 2);
+      double d = std::sqrt(std::pow(b[0] - a[0], 2.0) + std::pow(b[1] - a[1], 2.0) +
+                           std::pow(b[2] - a[2], 2.0));
+      if(d <= s.radius + pr->radius[j]) {
+        ctx->err = "The sphere at index " + std::to_string(i) + " overlaps with the one at index " +
+                   std::to_string(j);
+        delete pr;
+        return OM_ERR_OVERLAP;
+      }
+    }
+    pr->sph.insert(pr->sph.end(), sp, sp + 3);
+    double c[3];
+    om::to_cartesian(sp[0], sp[1], sp[2], c, c + 1, c + 2);
+    pr->cart.insert(pr->cart.end(), c, c + 3);
+    pr->radius.push_back(s.radius);
+    pr->eps_r.push_back(cplx(s.eps_r[0], s.eps_r[1]));
+    pr->mu_r.push_back(cplx(s.mu_r[0], s.mu_r[1]));
+    pr->eps_r_sh.push_back(cplx(s.eps_r_sh[0], s.eps_r_sh[1]));
+  }
+  pr->bg_eps_r = bg ? cplx(bg->eps_r[0], bg->eps_r[1]) : cplx(1.0, 0.0);
+  pr->bg_mu_r = bg ? cplx(bg->mu_r[0], bg->mu_r[1]) : cplx(1.0, 0.0);
+  pr->lambda = wave->wavelength;
+  pr->theta = wave->theta;
+  pr->phi = wave->phi;
+  pr->e_theta = cplx(wave->e_theta[0], wave->e_theta[1]);
+  pr->e_phi = cplx(wave->e_phi[0], wave->e_phi[1]);
+  pr->sh = wave->sh;
+  const size_t N = pr->N, P = pr->P, n = pr->n, nm = 2 * (nmax + 1);
+  int rc = OM_OK;
+  if(!rc) rc = dev_alloc(ctx, &pr->d_cart, 3 * N);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_radius, N);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_kin, N);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_izin, N);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_scal, N);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_T, N * nm);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_Tsh, N * nm);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_iaux, N * nm);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_cabs, N * nm);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_inc, 2 * P);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_incloc, n);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_wsca, N * P);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_Q, n);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_X, n);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_Xint, n);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_xsec, 16);
+  if(rc) {
+    free_problem(pr);
+    delete pr;
+    return rc;
+  }
+  cudaMemcpyAsync(pr->d_cart, pr->cart.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice,
+                  ctx->stream);
+  cudaMemcpyAsync(pr->d_radius, pr->radius.data(), sizeof(double) * N, cudaMemcpyHostToDevice,
+                  ctx->stream);
+  rc = update_wave(pr);
+  if(rc) {
+    free_problem(pr);
+    delete pr;
+    return rc;
+  }
+  *out = pr;
+  return OM_OK;
+}
+
+int ensure_matrix(om_problem *pr, int harmonic, int precision) {
+  om_context *ctx = pr->ctx;
+  const size_t nn = (size_t)pr->n * pr->n;
+  if(!pr->d_S[harmonic]) {
+    double2 *p = nullptr;
+    int rc = dev_alloc(ctx, &p, nn);
+    if(rc)
+      return rc;
+    pr->d_S[harmonic] = p;
+  }
+  if(precision == OM_C64 && !pr->d_S32[harmonic]) {
+    float2 *p = nullptr;
+    int rc = dev_alloc(ctx, &p, nn);
+    if(rc)
+      return rc;
+    pr->d_S32[harmonic] = p;
+  }
+  return OM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int om_context_create(int device, size_t budget_bytes, om_context **out) {
+  if(!out)
+    return OM_ERR_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if(cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    return OM_ERR_CUDA;
+  }
+  if(cudaSetDevice(device) != cudaSuccess)
+    return OM_ERR_CUDA;
+  om_context *ctx = new(std::nothrow) om_context();
+  if(!ctx)
+    return OM_ERR_INVALID;
+  ctx->device = device;
+  ctx->budget = budget_bytes;
+  if(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return OM_ERR_CUDA;
+  }
+  *out = ctx;
+  return OM_OK;
+}
+
+void om_context_destroy(om_context *ctx) {
+  if(!ctx)
+    return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for(auto &t : ctx->tables) {
+    cudaFree(t.rec);
+    cudaFree(t.qf);
+    cudaFree(t.pf);
+  }
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *om_context_last_error(const om_context *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int om_context_last_launches(const om_context *ctx) { return ctx ? ctx->last_launches : 0; }
+
+int om_context_synchronize(om_context *ctx) {
+  if(!ctx)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  return e == cudaSuccess ? OM_OK : cuda_fail(ctx, e, "synchronize");
+}
+
+int om_problem_create(om_context *ctx, const om_sphere *spheres, int n_spheres,
+                      const om_medium *background, const om_plane_wave *wave, om_problem **out) {
+  if(!ctx)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  try {
+    return make_problem(ctx, spheres, n_spheres, background, wave, out);
+  } catch(std::exception &e) {
+    ctx->err = e.what();
+    return OM_ERR_CUDA;
+  }
+}
+
+void om_problem_destroy(om_problem *pr) {
+  if(!pr)
+    return;
+  cudaSetDevice(pr->ctx->device);
+  cudaStreamSynchronize(pr->ctx->stream);
+  free_problem(pr);
+  delete pr;
+}
+
+long om_problem_size(const om_problem *pr) { return pr ? pr->n : 0; }
+
+int om_problem_set_wavelength(om_problem *pr, double wavelength) {
+  if(!pr || !(wavelength > 0))
+    return OM_ERR_INVALID;
+  cudaSetDevice(pr->ctx->device);
+  pr->ctx->last_launches = 0;
+  pr->lambda = wavelength;
+  return update_wave(pr);
+}
+
+int om_coupling(om_context *ctx, const double *rel_xyz, int count, double k_re, double k_im,
+                int nmax, int regular, double *A, double *B) {
+  if(!ctx || !rel_xyz || count < 1 || !A || !B || nmax < 1 || nmax > om::kMaxNmax)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  const size_t P = om::pmax(nmax);
+  double *d_rel = nullptr;
+  zd *d_A = nullptr, *d_B = nullptr;
+  int rc = dev_alloc(ctx, &d_rel, 3 * (size_t)count);
+  if(!rc) rc = dev_alloc(ctx, &d_A, P * P * count);
+  if(!rc) rc = dev_alloc(ctx, &d_B, P * P * count);
+  if(!rc) {
+    // the reference takes a Spherical displacement; mirror its Cartesian round trip
+    std::vector<double> rel(3 * (size_t)count);
+    for(int e = 0; e < count; ++e) {
+      double s[3];
+      to_sph(rel_xyz[3 * e], rel_xyz[3 * e + 1], rel_xyz[3 * e + 2], s);
+      om::to_cartesian(s[0], s[1], s[2], &rel[3 * e], &rel[3 * e + 1], &rel[3 * e + 2]);
+    }
+    cudaMemcpyAsync(d_rel, rel.data(), sizeof(double) * rel.size(), cudaMemcpyHostToDevice,
+                    ctx->stream);
+    try {
+      om::launch_coupling(ctx, d_rel, count, om::mk(k_re, k_im), nmax, regular ? 1 : 0, d_A, d_B);
+      rc = check_launch(ctx, "coupling kernel");
+    } catch(std::exception &ex) {
+      ctx->err = ex.what();
+      rc = OM_ERR_CUDA;
+    }
+    if(!rc) {
+      cudaMemcpyAsync(A, d_A, sizeof(zd) * P * P * count, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaMemcpyAsync(B, d_B, sizeof(zd) * P * P * count, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if(e != cudaSuccess)
+        rc = cuda_fail(ctx, e, "coupling");
+    }
+  }
+  dev_free(ctx, d_rel, 3 * (size_t)count);
+  dev_free(ctx, d_A, P * P * count);
+  dev_free(ctx, d_B, P * P * count);
+  return rc;
+}
+
+int om_tmatrix(om_problem *pr, int harmonic, double *T) {
+  if(!pr || !T || (harmonic != OM_FF && harmonic != OM_SH))
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  cudaSetDevice(ctx->device);
+  const int nm = 2 * (pr->nmax + 1);
+  std::vector<zd> h((size_t)pr->N * nm);
+  cudaMemcpyAsync(h.data(), harmonic == OM_SH ? pr->d_Tsh : pr->d_T, sizeof(zd) * h.size(),
+                  cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if(e != cudaSuccess)
+    return cuda_fail(ctx, e, "tmatrix");
+  // expand to the reference's 2P diagonal (Scatterer.cpp:86-95)
+  zd *out = reinterpret_cast<zd *>(T);
+  for(int i = 0; i < pr->N; ++i)
+    for(int p = 0; p < pr->P; ++p) {
+      int n = (int)std::sqrt(p + 1.0);
+      out[(size_t)i * 2 * pr->P + p] = h[(size_t)i * nm + 2 * n];
+      out[(size_t)i * 2 * pr->P + pr->P + p] = h[(size_t)i * nm + 2 * n + 1];
+    }
+  return OM_OK;
+}
+
+int om_incident_coefficients(om_problem *pr, double *ab) {
+  if(!pr || !ab)
+    return OM_ERR_INVALID;
+  cudaSetDevice(pr->ctx->device);
+  cudaMemcpyAsync(ab, pr->d_inc, sizeof(zd) * 2 * pr->P, cudaMemcpyDeviceToHost, pr->ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(pr->ctx->stream);
+  return e == cudaSuccess ? OM_OK : cuda_fail(pr->ctx, e, "incident coefficients");
+}
+
+int om_assemble(om_problem *pr, int harmonic, int precision) {
+  if(!pr || (harmonic != OM_FF && harmonic != OM_SH) ||
+     (precision != OM_C128 && precision != OM_C64))
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  int rc = ensure_matrix(pr, harmonic, precision);
+  if(rc)
+    return rc;
+  try {
+    om::launch_assemble(pr, harmonic, precision);
+  } catch(std::exception &e) {
+    ctx->err = e.what();
+    return OM_ERR_CUDA;
+  }
+  rc = check_launch(ctx, "assembly kernel");
+  if(rc)
+    return rc;
+  pr->S_prec[harmonic] = precision;
+  if(harmonic == OM_FF)
+    pr->have_solution = false;
+  return OM_OK;
+}
+
+int om_copy_matrix(om_problem *pr, int harmonic, double *S) {
+  if(!pr || !S || (harmonic != OM_FF && harmonic != OM_SH))
+    return OM_ERR_INVALID;
+  if(pr->S_prec[harmonic] < 0) {
+    pr->ctx->err = "matrix not assembled";
+    return OM_ERR_STATE;
+  }
+  cudaSetDevice(pr->ctx->device);
+  cudaMemcpyAsync(S, pr->d_S[harmonic], sizeof(double2) * (size_t)pr->n * pr->n,
+                  cudaMemcpyDeviceToHost, pr->ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(pr->ctx->stream);
+  return e == cudaSuccess ? OM_OK : cuda_fail(pr->ctx, e, "copy matrix");
+}
+
+int om_source_vector(om_problem *pr, double *Q) {
+  if(!pr)
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  try {
+    om::launch_source(pr);
+  } catch(std::exception &e) {
+    ctx->err = e.what();
+    return OM_ERR_CUDA;
+  }
+  int rc = check_launch(ctx, "source kernel");
+  if(rc)
+    return rc;
+  pr->have_source = true;
+  if(Q) {
+    cudaMemcpyAsync(Q, pr->d_Q, sizeof(zd) * pr->n, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if(e != cudaSuccess)
+      return cuda_fail(ctx, e, "source vector");
+  }
+  return OM_OK;
+}
+
+static int solve_impl(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
+                      double2 *x, om_solve_stats *st) {
+  om_context *ctx = pr->ctx;
+  if(pr->S_prec[harmonic] < 0) {
+    ctx->err = "matrix not assembled";
+    return OM_ERR_STATE;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, ctx->stream);
+  int rc;
+  switch(o->method) {
+  case OM_SOLVE_LU:
+    rc = om::solve_lu_rhs(pr, harmonic, b, x, st);
+    break;
+  case OM_SOLVE_GMRES:
+    rc = om::solve_gmres_rhs(pr, harmonic, o, b, x, st);
+    break;
+  case OM_SOLVE_FGMRES_MIXED:
+    if(!pr->d_S32[harmonic] || pr->S_prec[harmonic] != OM_C64) {
+      ctx->err = "mixed solve needs the matrix assembled with OM_C64";
+      rc = OM_ERR_STATE;
+    } else
+      rc = om::solve_fgmres_rhs(pr, harmonic, o, (const float2 *)pr->d_S32[harmonic], b, x, st);
+    break;
+  default:
+    ctx->err = "unknown solve method";
+    rc = OM_ERR_INVALID;
+  }
+  cudaEventRecord(e1, ctx->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if(st)
+    st->seconds = ms * 1e-3;
+  if(!rc)
+    rc = check_launch(ctx, "solve");
+  return rc;
+}
+
+int om_solve(om_problem *pr, const om_solve_options *opts, om_solve_stats *stats) {
+  if(!pr || !opts)
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  if(!pr->have_source) {
+    ctx->err = "source vector not computed";
+    return OM_ERR_STATE;
+  }
+  om_solve_stats st{};
+  int rc;
+  try {
+    rc = solve_impl(pr, OM_FF, opts, (const double2 *)pr->d_Q, (double2 *)pr->d_X, &st);
+  } catch(std::exception &e) {
+    ctx->err = e.what();
+    rc = OM_ERR_CUDA;
+  }
+  if(stats)
+    *stats = st;
+  if(rc && rc != OM_ERR_NOT_CONVERGED)
+    return rc;
+  om::launch_internal(pr);
+  int rc2 = check_launch(ctx, "internal coefficients");
+  if(rc2)
+    return rc2;
+  pr->have_solution = true;
+  return rc;
+}
+
+int om_solve_rhs(om_problem *pr, int harmonic, const om_solve_options *opts, const double *b,
+                 double *x, om_solve_stats *stats) {
+  if(!pr || !opts || !b || !x || (harmonic != OM_FF && harmonic != OM_SH))
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  double2 *db = nullptr, *dx = nullptr;
+  int rc = dev_alloc(ctx, &db, pr->n);
+  if(!rc)
+    rc = dev_alloc(ctx, &dx, pr->n);
+  om_solve_stats st{};
+  if(!rc) {
+    cudaMemcpyAsync(db, b, sizeof(double2) * pr->n, cudaMemcpyHostToDevice, ctx->stream);
+    try {
+      rc = solve_impl(pr, harmonic, opts, db, dx, &st);
+    } catch(std::exception &e) {
+      ctx->err = e.what();
+      rc = OM_ERR_CUDA;
+    }
+    cudaMemcpyAsync(x, dx, sizeof(double2) * pr->n, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if(!rc && e != cudaSuccess)
+      rc = cuda_fail(ctx, e, "solve_rhs");
+  }
+  if(stats)
+    *stats = st;
+  dev_free(ctx, db, pr->n);
+  dev_free(ctx, dx, pr->n);
+  return rc;
+}
+
+int om_get_coefficients(om_problem *pr, double *X_sca, double *X_int) {
+  if(!pr)
+    return OM_ERR_INVALID;
+  if(!pr->have_solution) {
+    pr->ctx->err = "no solution";
+    return OM_ERR_STATE;
+  }
+  cudaSetDevice(pr->ctx->device);
+  if(X_sca)
+    cudaMemcpyAsync(X_sca, pr->d_X, sizeof(zd) * pr->n, cudaMemcpyDeviceToHost, pr->ctx->stream);
+  if(X_int)
+    cudaMemcpyAsync(X_int, pr->d_Xint, sizeof(zd) * pr->n, cudaMemcpyDeviceToHost,
+                    pr->ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(pr->ctx->stream);
+  return e == cudaSuccess ? OM_OK : cuda_fail(pr->ctx, e, "coefficients");
+}
+
+int om_cross_sections(om_problem *pr, double out[4]) {
+  if(!pr || !out)
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  if(!pr->have_solution) {
+    ctx->err = "no solution";
+    return OM_ERR_STATE;
+  }
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  om::launch_cross_sections(pr);
+  cudaMemcpyAsync(out, pr->d_xsec, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if(e != cudaSuccess)
+    return cuda_fail(ctx, e, "cross sections");
+  return check_launch(ctx, "cross sections");
+}
+
+int om_near_field(om_problem *pr, const double *xyz, int npts, double *E, double *H) {
+  if(!pr || !xyz || npts < 1 || !E || !H)
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  if(!pr->have_solution) {
+    ctx->err = "no solution";
+    return OM_ERR_STATE;
+  }
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  // grid points reach getEHFields as Spherical (OutputGrid.cpp:147-153) and are
+  // converted back to Cartesian inside Tools::toPoint
+  std::vector<double> pts(3 * (size_t)npts);
+  for(int i = 0; i < npts; ++i) {
+    double s[3];
+    to_sph(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], s);
+    om::to_cartesian(s[0], s[1], s[2], &pts[3 * i], &pts[3 * i + 1], &pts[3 * i + 2]);
+  }
+  double *d_xyz = nullptr;
+  zd *d_E = nullptr, *d_H = nullptr;
+  int rc = dev_alloc(ctx, &d_xyz, 3 * (size_t)npts);
+  if(!rc) rc = dev_alloc(ctx, &d_E, 3 * (size_t)npts);
+  if(!rc) rc = dev_alloc(ctx, &d_H, 3 * (size_t)npts);
+  if(!rc) {
+    cudaMemcpyAsync(d_xyz, pts.data(), sizeof(double) * pts.size(), cudaMemcpyHostToDevice,
+                    ctx->stream);
+    om::launch_near_field(pr, d_xyz, npts, d_E, d_H);
+    rc = check_launch(ctx, "near field");
+    if(!rc) {
+      cudaMemcpyAsync(E, d_E, sizeof(zd) * 3 * npts, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaMemcpyAsync(H, d_H, sizeof(zd) * 3 * npts, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if(e != cudaSuccess)
+        rc = cuda_fail(ctx, e, "near field");
+    }
+  }
+  dev_free(ctx, d_xyz, 3 * (size_t)npts);
+  dev_free(ctx, d_E, 3 * (size_t)npts);
+  dev_free(ctx, d_H, 3 * (size_t)npts);
+  return rc;
+}
+
+int om_wavelength_solve(om_context *ctx, const om_sphere *spheres, int n_spheres,
+                        const om_medium *background, const om_plane_wave *wave,
+                        const om_solve_options *opts, int precision, double xsec[4],
+                        double *X_sca, double *X_int, om_solve_stats *stats) {
+  if(!ctx || !opts || !xsec)
+    return OM_ERR_INVALID;
+  om_problem *pr = nullptr;
+  int rc = om_problem_create(ctx, spheres, n_spheres, background, wave, &pr);
+  if(rc)
+    return rc;
+  int launches = ctx->last_launches;
+  rc = om_source_vector(pr, nullptr);
+  launches += ctx->last_launches;
+  if(!rc) {
+    rc = om_assemble(pr, OM_FF, precision);
+    launches += ctx->last_launches;
+  }
+  int solve_rc = OM_OK;
+  if(!rc) {
+    solve_rc = om_solve(pr, opts, stats);
+    launches += ctx->last_launches;
+    if(solve_rc && solve_rc != OM_ERR_NOT_CONVERGED)
+      rc = solve_rc;
+  }
+  if(!rc) {
+    rc = om_cross_sections(pr, xsec);
+    launches += ctx->last_launches;
+  }
+  if(!rc && (X_sca || X_int))
+    rc = om_get_coefficients(pr, X_sca, X_int);
+  std::string err = ctx->err;
+  om_problem_destroy(pr);
+  ctx->err = err;
+  ctx->last_launches = launches;
+  return rc ? rc : solve_rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Internal declarations shared by the CUDA translation units of liboptimet_gpu.
+#pragma once
+
+#include <complex>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "om_math.cuh"
+#include "../../include/optimet_gpu.h"
+
+namespace om {
+
+using cplx = std::complex<double>;
+
+// Geometry-independent coefficient tables for one nMax (device memory), built
+// once per context and nMax:
+//  rec   : a+, a-, b+, b- of the Stout recurrences (TranslationAdditionCoefficients.cpp:34-61)
+//          for n <= 2 nMax + 1, index 4 * (n*n + n + m) + {0,1,2,3}
+//  qfac  : per row harmonic q = (n, m): {0.5/sqrt(n(n+1)) * u1, * u2, * 2m, n, m} with
+//          u1 = sqrt((n-m)(n+m+1)), u2 = sqrt((n+m)(n-m+1)) (Coupling.cpp:30-51 factorised)
+//  pfac  : per column harmonic p = (l, k): {v1/sqrt(l(l+1)), v2/sqrt(l(l+1)), k/sqrt(l(l+1)),
+//          hB*w0, hB*w1, hB*w2, l, k} with hB = sqrt((2l+1)/((2l-1) l (l+1)))
+struct CoefTables {
+  int nmax = -1;
+  double *rec = nullptr;
+  double *qf = nullptr;
+  double *pf = nullptr;
+};
+constexpr int kQfacStride = 6;
+constexpr int kPfacStride = 8;
+
+// Per-sphere scalars computed on the host from the reference's formulas
+// (Scatterer.cpp:39-412), consumed by the T-matrix kernel.
+struct SphereScalars {
+  zd r0, rho, mu_sob, mu_j, mu_0;           // fundamental
+  zd r0_sh, rho_sh, mu_sob_sh;              // second harmonic
+};
+
+struct Arena;
+
+}  // namespace om
+
+struct om_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  size_t budget = 0;
+  size_t used = 0;
+  std::string err;
+  std::vector<om::CoefTables> tables;  // by nmax
+  int last_launches = 0;               // kernels launched by the last API call
+};
+
+struct om_problem {
+  om_context *ctx = nullptr;
+  int N = 0, nmax = 0, P = 0;
+  long n = 0;  // 2 P N
+  // host model (Reader/Geometry/Excitation state)
+  std::vector<double> sph;  // (r, theta, phi) per sphere as the XML reader stores it
+  std::vector<double> cart; // toCartesian(sph)
+  std::vector<double> radius;
+  std::vector<om::cplx> eps_r, mu_r, eps_r_sh;
+  om::cplx bg_eps_r, bg_mu_r;
+  double lambda = 0, theta = 0, phi = 0;
+  om::cplx e_theta, e_phi;
+  om::cplx waveK;
+  double omega = 0;
+  int sh = 0;
+  // device state
+  double *d_cart = nullptr;
+  double *d_radius = nullptr;
+  om::zd *d_kin = nullptr;    // per sphere: waveK_0 sqrt(eps_r mu_r) (interior wave number)
+  om::zd *d_izin = nullptr;   // per sphere: -i / sqrt(mu / eps)
+  om::cplx iZ;                // -i / sqrt(mu_b / eps_b)
+  om::SphereScalars *d_scal = nullptr;
+  om::zd *d_T = nullptr;      // N x (nmax+1) x 2 : TE, TM per n (FF)
+  om::zd *d_Tsh = nullptr;    // same at the second harmonic
+  om::zd *d_iaux = nullptr;   // N x (nmax+1) x 2
+  double *d_cabs = nullptr;   // N x (nmax+1) x 2
+  om::zd *d_inc = nullptr;    // 2P incident coefficients [a | b]
+  om::zd *d_incloc = nullptr; // n: IncLocal per sphere
+  double *d_wsca = nullptr;   // N x P: sum_p |T^reg_pq|^2 (Result.cpp:563-631)
+  om::zd *d_Q = nullptr;      // n
+  void *d_S[2] = {nullptr, nullptr};    // complex128 matrix per harmonic
+  void *d_S32[2] = {nullptr, nullptr};  // complex64 copy (precision form)
+  int S_prec[2] = {-1, -1};             // OM_C128, or OM_C64 when both copies exist
+  om::zd *d_X = nullptr, *d_Xint = nullptr;
+  double *d_xsec = nullptr;   // 4 + scratch
+  bool have_source = false, have_solution = false;
+};
+
+namespace om {
+
+// translate.cu
+const CoefTables &coef_tables(om_context *ctx, int nmax);
+void launch_sphere_terms(om_problem *pr);
+void launch_incident(om_problem *pr, const double einc[6]);
+void launch_assemble(om_problem *pr, int harmonic, int precision);
+void launch_source(om_problem *pr);
+int launch_coupling(om_context *ctx, const double *d_rel, int count, zd waveK, int nmax,
+                    int hankel, zd *d_A, zd *d_B);
+
+// field.cu
+void launch_internal(om_problem *pr);
+void launch_cross_sections(om_problem *pr);
+void launch_near_field(om_problem *pr, const double *d_xyz, int npts, zd *d_E, zd *d_H);
+
+// solve.cu
+int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_solve_stats *st);
+int solve_gmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
+                    double2 *x, om_solve_stats *st);
+int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const float2 *S32,
+                     const double2 *b, double2 *x, om_solve_stats *st);
+
+inline int blocks_for(long n, int threads) { return (int)((n + threads - 1) / threads); }
+
+}  // namespace om

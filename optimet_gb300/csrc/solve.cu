@@ -1,0 +1,878 @@
+// Dense solves of the OPTIMET scattering system on the device.
+//
+//  * LU with partial pivoting (the ScalapackSolver / pzgesv role,
+//    ScalapackSolver.cpp:54-130): right-looking, panels of kNb columns.
+//  * Restarted GMRES (the MatrixBelosSolver / Gmres_Zcomp role,
+//    MatrixBelosSolver.cpp:26-104, PreconditionedMatrix.cpp:892-985): classical
+//    Gram-Schmidt with one re-orthogonalisation pass, Givens rotations of
+//    det_approx (:1087-1133) on the host, residual |g_{k+1}| / ||b||.
+//  * Mixed precision form: FP64 outer flexible GMRES (Saad 1993) whose
+//    preconditioner is a fixed-length FP32 GMRES on the complex64 copy of S.
+// Reductions write per-block partial sums and add them in a fixed order, so
+// every solve is bitwise reproducible for a given problem.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "om_internal.h"
+
+namespace om {
+
+namespace {
+
+template <typename R> struct C2;
+template <> struct C2<double> {
+  typedef double2 T;
+};
+template <> struct C2<float> {
+  typedef float2 T;
+};
+
+template <typename V> __device__ __forceinline__ V cfma(V a, V b, V c) {  // c + a*b
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(a.y, b.x, c.y);
+  return c;
+}
+template <typename V> __device__ __forceinline__ V cfma_conj(V a, V b, V c) {  // c + conj(a)*b
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(-a.y, b.x, c.y);
+  return c;
+}
+
+constexpr int kMvThreads = 256;
+constexpr int kMvCols = 1024;  // columns per split-K chunk (x staged in shared memory)
+
+// Partial y over a chunk of columns: part[s * n + i] = sum_{j in chunk s} S[j ld + i] x[j]
+template <typename M, typename V>
+__global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld, long n, const V *x,
+                                                           V *part) {
+  __shared__ V xs[kMvCols];
+  const long i = blockIdx.x * (long)kMvThreads + threadIdx.x;
+  const long j0 = blockIdx.y * (long)kMvCols;
+  const long j1 = min(n, j0 + kMvCols);
+  for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads)
+    xs[j - j0] = x[j];
+  __syncthreads();
+  if(i >= n)
+    return;
+  V acc0, acc1;
+  acc0.x = acc0.y = acc1.x = acc1.y = 0;
+  const M *col = S + j0 * ld + i;
+  long j = j0;
+  for(; j + 3 < j1; j += 4) {
+    M s0 = col[0], s1 = col[ld], s2 = col[2 * ld], s3 = col[3 * ld];
+    V a0, a1, a2, a3;
+    a0.x = s0.x; a0.y = s0.y; a1.x = s1.x; a1.y = s1.y;
+    a2.x = s2.x; a2.y = s2.y; a3.x = s3.x; a3.y = s3.y;
+    acc0 = cfma(a0, xs[j - j0], acc0);
+    acc1 = cfma(a1, xs[j - j0 + 1], acc1);
+    acc0 = cfma(a2, xs[j - j0 + 2], acc0);
+    acc1 = cfma(a3, xs[j - j0 + 3], acc1);
+    col += 4 * ld;
+  }
+  for(; j < j1; ++j) {
+    M s0 = col[0];
+    V a0;
+    a0.x = s0.x;
+    a0.y = s0.y;
+    acc0 = cfma(a0, xs[j - j0], acc0);
+    col += ld;
+  }
+  acc0.x += acc1.x;
+  acc0.y += acc1.y;
+  part[blockIdx.y * n + i] = acc0;
+}
+
+// y = sum of partials (fixed order); if b given: y = b - sum.
+template <typename V>
+__global__ void k_matvec_reduce(const V *part, int nsplit, long n, const V *b, V *y) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  V acc = part[i];
+  for(int s = 1; s < nsplit; ++s) {
+    V v = part[s * n + i];
+    acc.x += v.x;
+    acc.y += v.y;
+  }
+  if(b) {
+    acc.x = b[i].x - acc.x;
+    acc.y = b[i].y - acc.y;
+  }
+  y[i] = acc;
+}
+
+constexpr int kDotThreads = 256;
+constexpr int kDotRows = 2048;  // rows per block of the multi-dot
+
+// part[b * (k+1) + t] = sum_{rows of block b} conj(V[:, t]) w   (t < k), and
+// part[b * (k+1) + k] = sum |w|^2 over the block.
+template <typename V>
+__global__ void __launch_bounds__(kDotThreads) k_multidot(const V *Vb, long ldv, int k, const V *w,
+                                                         long n, V *part) {
+  __shared__ V red[kDotThreads];
+  const long r0 = blockIdx.x * (long)kDotRows;
+  const long r1 = min(n, r0 + kDotRows);
+  for(int t = 0; t <= k; ++t) {
+    V acc;
+    acc.x = acc.y = 0;
+    if(t < k) {
+      const V *v = Vb + t * ldv;
+      for(long i = r0 + threadIdx.x; i < r1; i += kDotThreads)
+        acc = cfma_conj(v[i], w[i], acc);
+    } else {
+      for(long i = r0 + threadIdx.x; i < r1; i += kDotThreads) {
+        V a = w[i];
+        acc.x = fma(a.x, a.x, acc.x);
+        acc.x = fma(a.y, a.y, acc.x);
+      }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for(int s = kDotThreads / 2; s > 0; s >>= 1) {
+      if(threadIdx.x < s) {
+        red[threadIdx.x].x += red[threadIdx.x + s].x;
+        red[threadIdx.x].y += red[threadIdx.x + s].y;
+      }
+      __syncthreads();
+    }
+    if(threadIdx.x == 0)
+      part[blockIdx.x * (k + 1) + t] = red[0];
+    __syncthreads();
+  }
+}
+
+template <typename V> __global__ void k_sum_parts(const V *part, int nblk, int k1, V *out) {
+  const int t = threadIdx.x;
+  if(t >= k1)
+    return;
+  V acc = part[t];
+  for(int b = 1; b < nblk; ++b) {
+    acc.x += part[b * k1 + t].x;
+    acc.y += part[b * k1 + t].y;
+  }
+  out[t] = acc;
+}
+
+// w -= V[:, 0..k) h ; h read from device
+template <typename V>
+__global__ void k_sub_basis(const V *Vb, long ldv, int k, const V *h, V *w, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  V acc = w[i];
+  for(int t = 0; t < k; ++t) {
+    V c = h[t];
+    c.x = -c.x;
+    c.y = -c.y;
+    acc = cfma(Vb[t * ldv + i], c, acc);
+  }
+  w[i] = acc;
+}
+
+// dst = src * s (real scale) with conversion
+template <typename A, typename B> __global__ void k_scale_copy(const A *src, double s, B *dst, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  dst[i].x = src[i].x * s;
+  dst[i].y = src[i].y * s;
+}
+
+// x += sum_t y_t Z[:, t]
+template <typename V, typename Z>
+__global__ void k_add_combo(const Z *Zb, long ldz, int k, const double2 *y, V *x, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  double2 acc = make_double2(x[i].x, x[i].y);
+  for(int t = 0; t < k; ++t) {
+    Z z = Zb[t * ldz + i];
+    double2 zz = make_double2(z.x, z.y);
+    acc = cfma(zz, y[t], acc);
+  }
+  x[i].x = acc.x;
+  x[i].y = acc.y;
+}
+
+// ---------------------------------------------------------------------------
+// Krylov workspace and helpers
+// ---------------------------------------------------------------------------
+struct Work {
+  om_context *ctx;
+  long n;
+  void *buf = nullptr;
+  size_t bytes = 0;
+  ~Work() {
+    if(buf)
+      cudaFree(buf);
+  }
+  template <typename T> T *take(size_t count, size_t &off) {
+    T *p = reinterpret_cast<T *>(reinterpret_cast<char *>(buf) + off);
+    off += ((count * sizeof(T) + 255) / 256) * 256;
+    return p;
+  }
+};
+
+int alloc_work(om_context *ctx, Work &w, size_t bytes) {
+  if(ctx->budget && ctx->used + bytes > ctx->budget) {
+    ctx->err = "device-memory budget exceeded by solver workspace";
+    return OM_ERR_BUDGET;
+  }
+  if(cudaMalloc(&w.buf, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->err = "cudaMalloc failed for solver workspace";
+    return OM_ERR_BUDGET;
+  }
+  w.bytes = bytes;
+  return OM_OK;
+}
+
+template <typename M, typename V>
+void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, const V *b) {
+  const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
+  dim3 grid((unsigned)((n + kMvThreads - 1) / kMvThreads), (unsigned)nsplit);
+  k_matvec_part<M, V><<<grid, kMvThreads, 0, ctx->stream>>>(S, n, n, x, part);
+  k_matvec_reduce<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(part, nsplit, n, b, y);
+  ctx->last_launches += 2;
+}
+
+// h[0..k) = V^H w, h[k] = |w|^2, returned on the host (synchronous).
+template <typename V>
+void multidot(om_context *ctx, const V *Vb, long n, int k, const V *w, V *part, V *hd,
+              std::vector<std::complex<double>> &hh) {
+  const int nblk = (int)((n + kDotRows - 1) / kDotRows);
+  k_multidot<V><<<nblk, kDotThreads, 0, ctx->stream>>>(Vb, n, k, w, n, part);
+  k_sum_parts<V><<<1, 256 * ((k + 256) / 256), 0, ctx->stream>>>(part, nblk, k + 1, hd);
+  ctx->last_launches += 2;
+  std::vector<V> tmp(k + 1);
+  cudaMemcpyAsync(tmp.data(), hd, sizeof(V) * (k + 1), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  hh.resize(k + 1);
+  for(int t = 0; t <= k; ++t)
+    hh[t] = std::complex<double>(tmp[t].x, tmp[t].y);
+}
+
+template <typename V> void upload_h(om_context *ctx, const std::vector<std::complex<double>> &h, int k, V *hd) {
+  std::vector<V> tmp(k);
+  for(int t = 0; t < k; ++t) {
+    tmp[t].x = h[t].real();
+    tmp[t].y = h[t].imag();
+  }
+  cudaMemcpyAsync(hd, tmp.data(), sizeof(V) * k, cudaMemcpyHostToDevice, ctx->stream);
+}
+
+// Givens rotation of det_approx (PreconditionedMatrix.cpp:1102-1118)
+void givens(std::complex<double> hi1, std::complex<double> hi2, std::complex<double> &c,
+            std::complex<double> &s) {
+  if(std::abs(hi2) > std::abs(hi1)) {
+    std::complex<double> t = hi1 / hi2;
+    s = 1.0 / std::sqrt(1.0 + std::pow(std::abs(t), 2));
+    c = -t * s;
+  } else {
+    std::complex<double> t = hi2 / hi1;
+    c = 1.0 / std::sqrt(1.0 + std::pow(std::abs(t), 2));
+    s = -t * c;
+  }
+}
+
+// One Arnoldi step with CGS2: w <- w - V h (twice), returns h (k+1 entries incl. norm).
+template <typename V>
+void arnoldi_orth(om_context *ctx, const V *Vb, long n, int k, V *w, V *part, V *hd,
+                  std::vector<std::complex<double>> &h) {
+  std::vector<std::complex<double>> h1, h2;
+  multidot(ctx, Vb, n, k, w, part, hd, h1);
+  upload_h(ctx, h1, k, hd);
+  k_sub_basis<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, hd, w, n);
+  multidot(ctx, Vb, n, k, w, part, hd, h2);
+  upload_h(ctx, h2, k, hd);
+  k_sub_basis<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, hd, w, n);
+  ctx->last_launches += 2;
+  h.assign(k + 1, 0.0);
+  for(int t = 0; t < k; ++t)
+    h[t] = h1[t] + h2[t];
+  std::vector<std::complex<double>> h3;
+  multidot(ctx, Vb, n, 0, w, part, hd, h3);  // ||w|| after both passes
+  h[k] = std::sqrt(h3[0].real());
+}
+
+double vec_norm(om_context *ctx, const double2 *w, long n, double2 *part, double2 *hd) {
+  std::vector<std::complex<double>> h;
+  multidot<double2>(ctx, nullptr, n, 0, w, part, hd, h);
+  return std::sqrt(h[0].real());
+}
+
+// Restarted GMRES (right-hand side b, solution x; both FP64 device vectors).
+// Preconditioner hook: if `precond` is set, the flexible variant is used and
+// Z[:, k] = precond(V[:, k]) is stored (FGMRES).
+struct PrecondFn {
+  virtual void apply(const double2 *v, double2 *z) = 0;
+  virtual ~PrecondFn() {}
+};
+
+template <typename M>
+int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, double tol, int m,
+            int restarts, PrecondFn *pc, int *iters, double *relres) {
+  Work w;
+  w.ctx = ctx;
+  const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
+  const int nblk = (int)((n + kDotRows - 1) / kDotRows);
+  size_t bytes = sizeof(double2) * ((size_t)(m + 1) * n + (pc ? (size_t)m * n : 0) + 2 * n +
+                                    (size_t)nsplit * n + (size_t)nblk * (m + 2) + 2 * (m + 2)) +
+                 64 * 256;
+  int rc = alloc_work(ctx, w, bytes);
+  if(rc)
+    return rc;
+  size_t off = 0;
+  double2 *Vb = w.take<double2>((size_t)(m + 1) * n, off);
+  double2 *Zb = pc ? w.take<double2>((size_t)m * n, off) : nullptr;
+  double2 *r = w.take<double2>(n, off);
+  double2 *t = w.take<double2>(n, off);
+  double2 *part = w.take<double2>((size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)), off);
+  double2 *hd = w.take<double2>(m + 2, off);
+  double2 *yd = w.take<double2>(m + 2, off);
+
+  cudaMemsetAsync(x, 0, sizeof(double2) * n, ctx->stream);
+  const double bnorm = vec_norm(ctx, b, n, part, hd);
+  *iters = 0;
+  if(bnorm == 0.0) {
+    *relres = 0.0;
+    return OM_OK;
+  }
+  double err = 1.0;
+  int total = 0;
+  for(int rest = 0; rest < restarts && err > tol; ++rest) {
+    // r = b - S x
+    matvec<M, double2>(ctx, S, n, x, part, r, b);
+    double beta = vec_norm(ctx, r, n, part, hd);
+    if(beta == 0.0) {
+      err = 0.0;
+      break;
+    }
+    k_scale_copy<double2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(r, 1.0 / beta, Vb, n);
+    ctx->last_launches++;
+    std::vector<std::vector<std::complex<double>>> H;
+    std::vector<std::complex<double>> cs, sn, g(1, beta);
+    int k = 0;
+    double cur = beta / bnorm;
+    while(k < m && cur > tol) {
+      const double2 *vin = Vb + (size_t)k * n;
+      const double2 *op_in = vin;
+      if(pc) {
+        pc->apply(vin, Zb + (size_t)k * n);
+        op_in = Zb + (size_t)k * n;
+      }
+      double2 *wv = Vb + (size_t)(k + 1) * n;
+      matvec<M, double2>(ctx, S, n, op_in, part, wv, nullptr);
+      std::vector<std::complex<double>> h;
+      arnoldi_orth<double2>(ctx, Vb, n, k + 1, wv, part, hd, h);
+      const double hn = h[k + 1].real();
+      if(hn > 0.0) {
+        k_scale_copy<double2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(wv, 1.0 / hn, wv, n);
+        ctx->last_launches++;
+      }
+      for(int i = 0; i < k; ++i) {
+        std::complex<double> a = h[i], bb = h[i + 1];
+        h[i] = std::conj(cs[i]) * a + std::conj(-sn[i]) * bb;
+        h[i + 1] = sn[i] * a + cs[i] * bb;
+      }
+      std::complex<double> c, s;
+      givens(h[k], h[k + 1], c, s);
+      cs.push_back(c);
+      sn.push_back(s);
+      std::complex<double> hk = h[k], hk1 = h[k + 1];
+      h[k] = std::conj(c) * hk + std::conj(-s) * hk1;
+      h[k + 1] = s * hk + c * hk1;
+      g.push_back(0.0);
+      std::complex<double> g0 = g[k], g1 = g[k + 1];
+      g[k] = std::conj(c) * g0 + std::conj(-s) * g1;
+      g[k + 1] = s * g0 + c * g1;
+      H.push_back(h);
+      cur = std::abs(g[k + 1]) / bnorm;
+      ++k;
+      ++total;
+      if(hn == 0.0)
+        break;
+    }
+    // back substitution and update
+    std::vector<std::complex<double>> y(k);
+    for(int j = k - 1; j >= 0; --j) {
+      std::complex<double> v = g[j];
+      for(int q = j + 1; q < k; ++q)
+        v -= H[q][j] * y[q];
+      y[j] = v / H[j][j];
+    }
+    std::vector<double2> yh(k);
+    for(int j = 0; j < k; ++j)
+      yh[j] = make_double2(y[j].real(), y[j].imag());
+    cudaMemcpyAsync(yd, yh.data(), sizeof(double2) * k, cudaMemcpyHostToDevice, ctx->stream);
+    k_add_combo<double2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(pc ? Zb : Vb, n, k,
+                                                                               yd, x, n);
+    ctx->last_launches++;
+    // true residual for the stopping test of the next cycle
+    matvec<M, double2>(ctx, S, n, x, part, t, b);
+    err = vec_norm(ctx, t, n, part, hd) / bnorm;
+    cudaStreamSynchronize(ctx->stream);
+  }
+  *iters = total;
+  *relres = err;
+  return err <= tol ? OM_OK : OM_ERR_NOT_CONVERGED;
+}
+
+// FP32 GMRES of fixed maximum length on the complex64 matrix, used as the
+// flexible preconditioner: z ~= S^{-1} v (no restart, x0 = 0).
+struct InnerGmres32 : PrecondFn {
+  om_context *ctx;
+  const float2 *S;
+  long n;
+  int m;
+  double tol;
+  Work w;
+  float2 *Vb, *r, *part, *hd, *yd, *xz;
+  int total = 0;
+  InnerGmres32(om_context *c, const float2 *S_, long n_, int m_, double tol_)
+      : ctx(c), S(S_), n(n_), m(m_), tol(tol_) {
+    w.ctx = c;
+  }
+  int init() {
+    const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
+    const int nblk = (int)((n + kDotRows - 1) / kDotRows);
+    size_t bytes = sizeof(float2) * ((size_t)(m + 1) * n + 2 * n +
+                                     (size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)) +
+                                     2 * (m + 2)) +
+                   16 * 256;
+    int rc = alloc_work(ctx, w, bytes);
+    if(rc)
+      return rc;
+    size_t off = 0;
+    Vb = w.take<float2>((size_t)(m + 1) * n, off);
+    r = w.take<float2>(n, off);
+    xz = w.take<float2>(n, off);
+    part = w.take<float2>((size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)), off);
+    hd = w.take<float2>(m + 2, off);
+    yd = w.take<float2>(m + 2, off);
+    return OM_OK;
+  }
+  void apply(const double2 *v, double2 *z) override {
+    // v has unit norm (an Arnoldi vector): start from r0 = v
+    k_scale_copy<double2, float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v, 1.0, Vb, n);
+    ctx->last_launches++;
+    std::vector<std::vector<std::complex<double>>> H;
+    std::vector<std::complex<double>> cs, sn, g(1, 1.0);
+    int k = 0;
+    double cur = 1.0;
+    while(k < m && cur > tol) {
+      float2 *wv = Vb + (size_t)(k + 1) * n;
+      matvec<float2, float2>(ctx, S, n, Vb + (size_t)k * n, part, wv, nullptr);
+      std::vector<std::complex<double>> h;
+      arnoldi_orth<float2>(ctx, Vb, n, k + 1, wv, part, hd, h);
+      const double hn = h[k + 1].real();
+      if(hn > 0.0) {
+        k_scale_copy<float2, float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(wv, 1.0 / hn, wv, n);
+        ctx->last_launches++;
+      }
+      for(int i = 0; i < k; ++i) {
+        std::complex<double> a = h[i], bb = h[i + 1];
+        h[i] = std::conj(cs[i]) * a + std::conj(-sn[i]) * bb;
+        h[i + 1] = sn[i] * a + cs[i] * bb;
+      }
+      std::complex<double> c, s;
+      givens(h[k], h[k + 1], c, s);
+      cs.push_back(c);
+      sn.push_back(s);
+      std::complex<double> hk = h[k], hk1 = h[k + 1];
+      h[k] = std::conj(c) * hk + std::conj(-s) * hk1;
+      h[k + 1] = s * hk + c * hk1;
+      g.push_back(0.0);
+      std::complex<double> g0 = g[k], g1 = g[k + 1];
+      g[k] = std::conj(c) * g0 + std::conj(-s) * g1;
+      g[k + 1] = s * g0 + c * g1;
+      H.push_back(h);
+      cur = std::abs(g[k + 1]);
+      ++k;
+      ++total;
+      if(hn == 0.0)
+        break;
+    }
+    std::vector<std::complex<double>> y(k);
+    for(int j = k - 1; j >= 0; --j) {
+      std::complex<double> vv = g[j];
+      for(int q = j + 1; q < k; ++q)
+        vv -= H[q][j] * y[q];
+      y[j] = vv / H[j][j];
+    }
+    std::vector<double2> yh(k);
+    for(int j = 0; j < k; ++j)
+      yh[j] = make_double2(y[j].real(), y[j].imag());
+    cudaMemsetAsync(z, 0, sizeof(double2) * n, ctx->stream);
+    upload_y_and_combine(yh, k, z);
+  }
+  Work ybuf;
+  double2 *ydev = nullptr;
+  void upload_y_and_combine(const std::vector<double2> &yh, int k, double2 *z) {
+    if(!ydev) {
+      ybuf.ctx = ctx;
+      alloc_work(ctx, ybuf, sizeof(double2) * (m + 2));
+      ydev = reinterpret_cast<double2 *>(ybuf.buf);
+    }
+    cudaMemcpyAsync(ydev, yh.data(), sizeof(double2) * k, cudaMemcpyHostToDevice, ctx->stream);
+    k_add_combo<double2, float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, ydev, z, n);
+    ctx->last_launches++;
+    cudaStreamSynchronize(ctx->stream);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// LU with partial pivoting
+// ---------------------------------------------------------------------------
+constexpr int kNb = 32;
+
+template <typename V> __device__ __forceinline__ double mag2(V a) {
+  return (double)a.x * a.x + (double)a.y * a.y;
+}
+template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
+  V r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename V> __device__ __forceinline__ V make_neg(V a) {
+  a.x = -a.x;
+  a.y = -a.y;
+  return a;
+}
+template <typename V> __device__ __forceinline__ V crecip(V a) {
+  double d = (double)a.x * a.x + (double)a.y * a.y;
+  V r;
+  r.x = a.x / d;
+  r.y = -a.y / d;
+  return r;
+}
+
+// Unblocked LU of the panel A[k:n, k:k+nb) (one CTA); pivots to piv[k..k+nb).
+template <typename V>
+__global__ void __launch_bounds__(1024) k_lu_panel(V *A, long ld, long n, long k, int nb, int *piv,
+                                                   int *info) {
+  __shared__ double bestv[1024];
+  __shared__ long besti[1024];
+  __shared__ V pivrow[kNb];
+  const int t = threadIdx.x;
+  for(int c = 0; c < nb; ++c) {
+    const long col = k + c;
+    double bv = -1.0;
+    long bi = col;
+    for(long i = col + t; i < n; i += blockDim.x) {
+      double v = mag2(A[col * ld + i]);
+      if(v > bv) {
+        bv = v;
+        bi = i;
+      }
+    }
+    bestv[t] = bv;
+    besti[t] = bi;
+    __syncthreads();
+    for(int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if(t < s) {
+        if(bestv[t + s] > bestv[t] || (bestv[t + s] == bestv[t] && besti[t + s] < besti[t])) {
+          bestv[t] = bestv[t + s];
+          besti[t] = besti[t + s];
+        }
+      }
+      __syncthreads();
+    }
+    const long p = besti[0];
+    if(t == 0) {
+      piv[col] = (int)p;
+      if(bestv[0] <= 0.0 && *info == 0)
+        *info = (int)col + 1;
+    }
+    // swap rows col and p inside the panel
+    if(t < nb && p != col) {
+      V a = A[(k + t) * ld + col];
+      A[(k + t) * ld + col] = A[(k + t) * ld + p];
+      A[(k + t) * ld + p] = a;
+    }
+    __syncthreads();
+    if(t < nb)
+      pivrow[t] = A[(k + t) * ld + col];
+    __syncthreads();
+    if(bestv[0] > 0.0) {
+      const V inv = crecip(pivrow[c]);
+      for(long i = col + 1 + t; i < n; i += blockDim.x) {
+        V l = cmul(A[col * ld + i], inv);
+        A[col * ld + i] = l;
+        for(int j = c + 1; j < nb; ++j) {
+          V u = pivrow[j];
+          V a = A[(k + j) * ld + i];
+          a.x -= l.x * u.x - l.y * u.y;
+          a.y -= l.x * u.y + l.y * u.x;
+          A[(k + j) * ld + i] = a;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Apply the panel's row interchanges to the columns outside the panel.
+template <typename V>
+__global__ void k_lu_swap(V *A, long ld, long n, long k, int nb, const int *piv) {
+  const long j = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(j >= n || (j >= k && j < k + nb))
+    return;
+  V *col = A + j * ld;
+  for(int c = 0; c < nb; ++c) {
+    const long r = k + c, p = piv[r];
+    if(p != r) {
+      V a = col[r];
+      col[r] = col[p];
+      col[p] = a;
+    }
+  }
+}
+
+// U12 = L11^{-1} A12 (unit lower L11), one thread per column.
+template <typename V>
+__global__ void k_lu_trsm(V *A, long ld, long n, long k, int nb) {
+  __shared__ V L[kNb][kNb];
+  for(int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+    int r = idx % nb, c = idx / nb;
+    L[r][c] = A[(k + c) * ld + k + r];
+  }
+  __syncthreads();
+  const long j = k + nb + blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(j >= n)
+    return;
+  V x[kNb];
+  for(int r = 0; r < nb; ++r) {
+    V v = A[j * ld + k + r];
+    for(int s = 0; s < r; ++s) {
+      V l = L[r][s];
+      v.x -= l.x * x[s].x - l.y * x[s].y;
+      v.y -= l.x * x[s].y + l.y * x[s].x;
+    }
+    x[r] = v;
+    A[j * ld + k + r] = v;
+  }
+}
+
+// A22 -= L21 U12 over rows/cols >= k + nb; 32x32 output tiles, 256 threads.
+template <typename V>
+__global__ void __launch_bounds__(256) k_lu_gemm(V *A, long ld, long n, long k, int nb) {
+  __shared__ V Ls[32][kNb + 1];
+  __shared__ V Us[kNb][32 + 1];
+  const long r0 = k + nb + blockIdx.x * 32L, c0 = k + nb + blockIdx.y * 32L;
+  const int t = threadIdx.x;
+  for(int idx = t; idx < 32 * nb; idx += 256) {
+    int rr = idx % 32, cc = idx / 32;
+    long r = r0 + rr;
+    V z;
+    z.x = z.y = 0;
+    Ls[rr][cc] = r < n ? A[(k + cc) * ld + r] : z;
+  }
+  for(int idx = t; idx < nb * 32; idx += 256) {
+    int rr = idx % nb, cc = idx / nb;
+    long c = c0 + cc;
+    V z;
+    z.x = z.y = 0;
+    Us[rr][cc] = c < n ? A[c * ld + k + rr] : z;
+  }
+  __syncthreads();
+  const int tr = t % 32, tc = t / 32;  // 4 columns per thread: tc, tc+8, tc+16, tc+24
+  const long r = r0 + tr;
+  if(r >= n)
+    return;
+  for(int q = 0; q < 4; ++q) {
+    const int cc = tc + 8 * q;
+    const long c = c0 + cc;
+    if(c >= n)
+      continue;
+    V acc;
+    acc.x = acc.y = 0;
+    for(int s = 0; s < nb; ++s)
+      acc = cfma(Ls[tr][s], Us[s][cc], acc);
+    V a = A[c * ld + r];
+    a.x -= acc.x;
+    a.y -= acc.y;
+    A[c * ld + r] = a;
+  }
+}
+
+// b := P b (row interchanges in order)
+template <typename V> __global__ void k_lu_permute(V *b, long n, const int *piv) {
+  if(threadIdx.x != 0 || blockIdx.x != 0)
+    return;
+  for(long r = 0; r < n; ++r) {
+    long p = piv[r];
+    if(p != r) {
+      V a = b[r];
+      b[r] = b[p];
+      b[p] = a;
+    }
+  }
+}
+
+// Triangular solves, one block of kNb rows at a time.
+template <typename V>
+__global__ void k_tri_diag(const V *A, long ld, long k, int nb, V *b, int upper) {
+  if(threadIdx.x != 0)
+    return;
+  if(!upper) {
+    for(int r = 0; r < nb; ++r) {
+      V v = b[k + r];
+      for(int s = 0; s < r; ++s)
+        v = cfma(A[(k + s) * ld + k + r], make_neg(b[k + s]), v);
+      b[k + r] = v;
+    }
+  } else {
+    for(int r = nb - 1; r >= 0; --r) {
+      V v = b[k + r];
+      for(int s = r + 1; s < nb; ++s)
+        v = cfma(A[(k + s) * ld + k + r], make_neg(b[k + s]), v);
+      V d = A[(k + r) * ld + k + r];
+      b[k + r] = cmul(v, crecip(d));
+    }
+  }
+}
+
+// rows i outside [k, k+nb): b[i] -= A[i, k:k+nb) b[k:k+nb)  (below for L, above for U)
+template <typename V>
+__global__ void k_tri_update(const V *A, long ld, long k, int nb, V *b, long lo, long hi) {
+  const long i = lo + blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= hi)
+    return;
+  V v = b[i];
+  for(int s = 0; s < nb; ++s)
+    v = cfma(A[(k + s) * ld + i], make_neg(b[k + s]), v);
+  b[i] = v;
+}
+
+template <typename V>
+int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
+  cudaMemsetAsync(info, 0, sizeof(int), ctx->stream);
+  for(long k = 0; k < n; k += kNb) {
+    const int nb = (int)std::min<long>(kNb, n - k);
+    k_lu_panel<V><<<1, 1024, 0, ctx->stream>>>(A, n, n, k, nb, piv, info);
+    k_lu_swap<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, n, k, nb, piv);
+    ctx->last_launches += 2;
+    const long rest = n - k - nb;
+    if(rest > 0) {
+      k_lu_trsm<V><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, n, k, nb);
+      dim3 g((unsigned)((rest + 31) / 32), (unsigned)((rest + 31) / 32));
+      k_lu_gemm<V><<<g, 256, 0, ctx->stream>>>(A, n, n, k, nb);
+      ctx->last_launches += 2;
+    }
+  }
+  return OM_OK;
+}
+
+template <typename V> void lu_solve_vec(om_context *ctx, const V *A, long n, const int *piv, V *b) {
+  k_lu_permute<V><<<1, 32, 0, ctx->stream>>>(b, n, piv);
+  ctx->last_launches++;
+  for(long k = 0; k < n; k += kNb) {
+    const int nb = (int)std::min<long>(kNb, n - k);
+    k_tri_diag<V><<<1, 32, 0, ctx->stream>>>(A, n, k, nb, b, 0);
+    if(k + nb < n)
+      k_tri_update<V><<<blocks_for(n - k - nb, 256), 256, 0, ctx->stream>>>(A, n, k, nb, b, k + nb, n);
+    ctx->last_launches += 2;
+  }
+  for(long k = ((n - 1) / kNb) * kNb; k >= 0; k -= kNb) {
+    const int nb = (int)std::min<long>(kNb, n - k);
+    k_tri_diag<V><<<1, 32, 0, ctx->stream>>>(A, n, k, nb, b, 1);
+    if(k > 0)
+      k_tri_update<V><<<blocks_for(k, 256), 256, 0, ctx->stream>>>(A, n, k, nb, b, 0, k);
+    ctx->last_launches += 2;
+  }
+}
+
+}  // namespace
+
+// Direct solve of S X = Q for the given harmonic. The FP64 matrix is factored
+// in a copy (S stays available for residuals and repeated solves).
+int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_solve_stats *st) {
+  om_context *ctx = pr->ctx;
+  const long n = pr->n;
+  if(pr->S_prec[harmonic] != OM_C128) {
+    ctx->err = "LU solve needs the complex128 matrix";
+    return OM_ERR_STATE;
+  }
+  Work w;
+  w.ctx = ctx;
+  size_t bytes = sizeof(double2) * (size_t)n * n + sizeof(int) * (n + 1) + 1024;
+  int rc = alloc_work(ctx, w, bytes);
+  if(rc)
+    return rc;
+  size_t off = 0;
+  double2 *A = w.take<double2>((size_t)n * n, off);
+  int *piv = w.take<int>(n, off);
+  int *info = w.take<int>(1, off);
+  cudaMemcpyAsync(A, pr->d_S[harmonic], sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToDevice,
+                  ctx->stream);
+  lu_factor<double2>(ctx, A, n, piv, info);
+  cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+  lu_solve_vec<double2>(ctx, A, n, piv, x);
+  int hinfo = 0;
+  cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  if(hinfo) {
+    ctx->err = "singular matrix: zero pivot at column " + std::to_string(hinfo);
+    return OM_ERR_SINGULAR;
+  }
+  if(st) {
+    st->iterations = 0;
+    st->inner_iterations = 0;
+    st->rel_residual = 0.0;
+  }
+  return OM_OK;
+}
+
+int solve_gmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
+                    double2 *x, om_solve_stats *st) {
+  om_context *ctx = pr->ctx;
+  int it = 0;
+  double rr = 0;
+  // the complex128 matrix is always present (the precision form keeps both copies)
+  int rc = gmres64<double2>(ctx, (const double2 *)pr->d_S[harmonic], pr->n, b, x, o->tol,
+                            o->max_iter, o->restarts, nullptr, &it, &rr);
+  if(st) {
+    st->iterations = it;
+    st->inner_iterations = 0;
+    st->rel_residual = rr;
+  }
+  if(rc == OM_ERR_NOT_CONVERGED)
+    ctx->err = "GMRES did not reach the requested tolerance";
+  return rc;
+}
+
+// Precision form: FP64 outer FGMRES on the FP64 matrix (residuals), FP32
+// inner GMRES on the complex64 matrix (stored in d_S of the same harmonic's
+// mixed slot).
+int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const float2 *S32,
+                     const double2 *b, double2 *x, om_solve_stats *st) {
+  om_context *ctx = pr->ctx;
+  InnerGmres32 inner(ctx, S32, pr->n, std::max(1, o->inner_iter), o->inner_tol);
+  int rc = inner.init();
+  if(rc)
+    return rc;
+  int it = 0;
+  double rr = 0;
+  const int outer_m = std::max(1, std::min(o->max_iter, 32));
+  rc = gmres64<double2>(ctx, (const double2 *)pr->d_S[harmonic], pr->n, b, x, o->tol, outer_m,
+                        o->restarts, &inner, &it, &rr);
+  if(st) {
+    st->iterations = it;
+    st->inner_iterations = inner.total;
+    st->rel_residual = rr;
+  }
+  if(rc == OM_ERR_NOT_CONVERGED)
+    ctx->err = "FGMRES did not reach the requested tolerance";
+  return rc;
+}
+
+}  // namespace om

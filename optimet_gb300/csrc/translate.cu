@@ -1,0 +1,746 @@
+// Translation-addition coefficients, coupling blocks, scattering-matrix
+// assembly and source vector for the OPTIMET sphere path.
+//
+// One CTA per translation (an ordered sphere pair for the matrix, a sphere
+// for the source vector). Inside a CTA:
+//  1. seeds alpha(0,0,l,k) = sqrt(4 pi) (-1)^{l+k} Y_l^{-k}(theta,phi) z_l(kR) for
+//     l <= 2 nMax (TranslationAdditionCoefficients.cpp:102-111);
+//  2. the Stout recurrences (:113-124). Both the diagonal recurrence
+//     (n,n,l,k) <- (n-1,n-1,l+-1,k-1) and the off-diagonal one
+//     (n,m,l,k) <- (n-1,m,l+-1,k), (n-2,m,l,k) keep d = m - k fixed, so each
+//     "slice" d is an independent chain: one warp per chain, lanes over l,
+//     warp shuffles for the l+-1 neighbours, state in registers. Negative m
+//     comes from the conjugate-wave chains (:128-135). Results with l <= nMax
+//     go to a shared-memory table alpha[(n,m)][(l,k)];
+//  3. A and B (Coupling.cpp:30-51) are formed from that table and, for the
+//     matrix, scaled by -T_i and written as the 2P x 2P block of S
+//     (PreconditionedMatrix.cpp:369-397) with coalesced column stores.
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+
+#include "om_internal.h"
+
+namespace om {
+
+namespace {
+
+// --- host coefficient formulas (TranslationAdditionCoefficients.cpp:34-61) ---
+bool valid2(int n, int m) { return n >= 0 && std::abs(m) <= n; }
+double h_a_plus(int n, int m) {
+  if(!valid2(n, m))
+    return 0e0;
+  return -std::sqrt(static_cast<double>((n + m + 1) * (n - m + 1)) /
+                    static_cast<double>((2 * n + 1) * (2 * n + 3)));
+}
+double h_a_minus(int n, int m) {
+  if(!valid2(n, m))
+    return 0e0;
+  return std::sqrt(static_cast<double>((n + m) * (n - m)) /
+                   static_cast<double>((2 * n + 1) * (2 * n - 1)));
+}
+double h_b_plus(int n, int m) {
+  if(!valid2(n, m))
+    return 0e0;
+  return std::sqrt(static_cast<double>((n + m + 2) * (n + m + 1)) /
+                   static_cast<double>((2 * n + 1) * (2 * n + 3)));
+}
+double h_b_minus(int n, int m) {
+  if(!valid2(n, m))
+    return 0e0;
+  return std::sqrt(static_cast<double>((n - m) * (n - m - 1)) /
+                   static_cast<double>((2 * n + 1) * (2 * n - 1)));
+}
+
+enum { kAP = 0, kAM = 1, kBP = 2, kBM = 3 };
+
+// Shared-memory layout of a translation CTA (offsets in doubles).
+struct Layout {
+  int nmax, P, L, Lc, W;
+  int rec, qf, pf, leg, geo, zb, seed, tl, tab;
+  int rows_cap;
+  size_t bytes;
+};
+
+Layout make_layout(int nmax, size_t smem_limit) {
+  Layout y;
+  y.nmax = nmax;
+  y.P = pmax(nmax);
+  y.L = 2 * nmax;
+  y.Lc = 2 * nmax + 1;
+  y.W = (nmax + 1) * (nmax + 1);
+  int o = 0;
+  auto take = [&](int n) {
+    int at = o;
+    o += (n + 1) & ~1;  // keep 16-byte alignment for complex entries
+    return at;
+  };
+  y.rec = take(4 * (y.Lc + 1) * (y.Lc + 1));
+  y.qf = take(kQfacStride * y.P);
+  y.pf = take(kPfacStride * y.P);
+  y.leg = take((y.L + 1) * (y.L + 2) / 2);
+  y.geo = take(8);
+  y.zb = take(2 * 2 * (y.L + 1));
+  y.seed = take(2 * 2 * (y.L + 1) * (y.L + 1));
+  y.tl = take(2 * 2 * (nmax + 1));
+  y.tab = o;
+  size_t fixed = size_t(o) * sizeof(double);
+  size_t row_bytes = size_t(y.W) * sizeof(zd);
+  size_t avail = smem_limit > fixed ? smem_limit - fixed : 0;
+  int cap = (int)std::min<size_t>(avail / row_bytes, (size_t)y.P);
+  y.rows_cap = cap;
+  y.bytes = fixed + size_t(cap) * row_bytes;
+  return y;
+}
+
+// Chunks of whole n-levels whose rows fit the table.
+std::vector<std::pair<int, int>> make_chunks(const Layout &y) {
+  std::vector<std::pair<int, int>> out;
+  int n = 1;
+  while(n <= y.nmax) {
+    int lo = n, rows = 0;
+    while(n <= y.nmax && rows + (2 * n + 1) <= y.rows_cap) {
+      rows += 2 * n + 1;
+      ++n;
+    }
+    if(n == lo)
+      throw std::runtime_error("shared memory too small for one harmonic level");
+    out.push_back({lo, n - 1});
+  }
+  return out;
+}
+
+struct Smem {
+  double *rec, *qf, *pf, *leg, *geo;
+  zd *zb, *seed, *tl, *tab;
+};
+
+__device__ Smem smem_view(double *base, const Layout &y) {
+  Smem s;
+  s.rec = base + y.rec;
+  s.qf = base + y.qf;
+  s.pf = base + y.pf;
+  s.leg = base + y.leg;
+  s.geo = base + y.geo;
+  s.zb = reinterpret_cast<zd *>(base + y.zb);
+  s.seed = reinterpret_cast<zd *>(base + y.seed);
+  s.tl = reinterpret_cast<zd *>(base + y.tl);
+  s.tab = reinterpret_cast<zd *>(base + y.tab);
+  return s;
+}
+
+__device__ __forceinline__ double rcoef(const Smem &s, int Lc, int n, int m, int which) {
+  if(n < 0 || n > Lc || m > n || m < -n)
+    return 0.0;
+  return s.rec[4 * (n * n + n + m) + which];
+}
+
+__device__ __forceinline__ zd shfl_up1(zd v) {
+  return mk(__shfl_up_sync(0xffffffffu, v.re, 1), __shfl_up_sync(0xffffffffu, v.im, 1));
+}
+__device__ __forceinline__ zd shfl_down1(zd v) {
+  return mk(__shfl_down_sync(0xffffffffu, v.re, 1), __shfl_down_sync(0xffffffffu, v.im, 1));
+}
+
+// Copy the geometry-independent tables into shared memory.
+__device__ void load_tables(const Smem &s, const Layout &y, const double *rec, const double *qf,
+                            const double *pf) {
+  int nrec = 4 * (y.Lc + 1) * (y.Lc + 1);
+  for(int i = threadIdx.x; i < nrec; i += blockDim.x)
+    s.rec[i] = rec[i];
+  for(int i = threadIdx.x; i < kQfacStride * y.P; i += blockDim.x)
+    s.qf[i] = qf[i];
+  for(int i = threadIdx.x; i < kPfacStride * y.P; i += blockDim.x)
+    s.pf[i] = pf[i];
+}
+
+// Seeds for the positive (waveK) and conjugate-wave recurrences.
+// geo[0..2] must hold (r, theta, phi) before the call.
+__device__ void make_seeds(const Smem &s, const Layout &y, zd waveK, int hankel) {
+  const int L = y.L;
+  const int t = threadIdx.x;
+  const double r = s.geo[0], th = s.geo[1], ph = s.geo[2];
+  if(t == 0 || t == 32) {
+    zd k = (t == 0) ? waveK : (hankel ? -conj(waveK) : conj(waveK));
+    zd z = r * k;
+    zd f[kMaxOrder + 2];
+    bessel_deriv(hankel ? 1 : 0, z, L, f, nullptr);
+    zd *dst = s.zb + (t == 0 ? 0 : (L + 1));
+    for(int l = 0; l <= L; ++l)
+      dst[l] = f[l];
+  }
+  if(t >= 64 && t < 64 + L + 1) {
+    // normalised associated Legendre functions with the Condon-Shortley phase
+    const int k = t - 64;
+    const double x = cos(th), st = sin(th);
+    double v = 1.0 / sqrt(4.0 * kPi);
+    for(int i = 1; i <= k; ++i)
+      v *= -sqrt(double(2 * i + 1) / double(2 * i)) * st;
+    s.leg[k * (k + 1) / 2 + k] = v;
+    if(k + 1 <= L) {
+      double v0 = v, v1 = sqrt(double(2 * k + 3)) * x * v;
+      s.leg[(k + 1) * (k + 2) / 2 + k] = v1;
+      for(int l = k + 2; l <= L; ++l) {
+        double a = sqrt(double(4 * l * l - 1) / double(l * l - k * k));
+        double b = sqrt(double((l - 1) * (l - 1) - k * k) / double(4 * (l - 1) * (l - 1) - 1));
+        double v2 = a * (x * v1 - b * v0);
+        s.leg[l * (l + 1) / 2 + k] = v2;
+        v0 = v1;
+        v1 = v2;
+      }
+    }
+  }
+  __syncthreads();
+  const double s4pi = sqrt(4e0 * kPi);
+  for(int idx = t; idx < (L + 1) * (L + 1); idx += blockDim.x) {
+    int l = (int)sqrt((double)idx);
+    while(l * l > idx)
+      --l;
+    while((l + 1) * (l + 1) <= idx)
+      ++l;
+    int k = idx - l * l - l;  // idx = l*l + l + k
+    zd zp = s.zb[l], zn = s.zb[L + 1 + l];
+    if(l == 0) {
+      s.seed[idx] = zp;
+      s.seed[(L + 1) * (L + 1) + idx] = zn;
+      continue;
+    }
+    int am = k < 0 ? -k : k;  // |mu| with mu = -k
+    double pre = s.leg[l * (l + 1) / 2 + am];
+    double sn, cs;
+    sincos(am * ph, &sn, &cs);
+    double re = pre * cs, im = pre * sn;
+    if(k > 0) {  // mu = -k < 0: Y_l^{-|m|} = (-1)^|m| conj(Y_l^{|m|})
+      if(am & 1)
+        re = -re;
+      else
+        im = -im;
+    }
+    double factor = s4pi * (((l + k) % 2 == 0) ? 1 : -1);
+    zd fy = mk(factor * re, factor * im);
+    s.seed[idx] = fy * zp;
+    s.seed[(L + 1) * (L + 1) + idx] = fy * zn;
+  }
+  __syncthreads();
+}
+
+// The recurrence chains; stores alpha(n, m, l, k) for n in [n_lo, n_hi], l <= nMax.
+__device__ void run_chains(const Smem &s, const Layout &y, int hankel, int n_lo, int n_hi) {
+  const int nmax = y.nmax, L = y.L, Lc = y.Lc, W = y.W;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int npos = 3 * nmax + 1, nneg = 3 * nmax;
+  const int base = n_lo * n_lo - 1;  // flat(n_lo, n_lo)
+  const int l = lane;
+  for(int c = warp; c < npos + nneg; c += nwarps) {
+    const bool neg = c >= npos;
+    const int d = neg ? (c - npos) + 1 - nmax : c - nmax;
+    const zd *seed = s.seed + (neg ? (L + 1) * (L + 1) : 0);
+    zd D = mk(0.0, 0.0);
+    if(l <= L && (d < 0 ? -d : d) <= l)
+      D = seed[l * l + l - d];
+    const int mu_end = min(min(nmax, d + nmax), n_hi);
+    for(int mu = 0; mu <= mu_end; ++mu) {
+      const int kap = mu - d;
+      if(mu > 0) {
+        zd Dm = shfl_up1(D), Dp = shfl_down1(D);
+        double bp = rcoef(s, Lc, l - 1, kap - 1, kBP);
+        double bm = rcoef(s, Lc, l + 1, kap - 1, kBM);
+        double den = rcoef(s, Lc, mu - 1, mu - 1, kBP);
+        zd Dn = (Dm * bp + Dp * bm) / den;
+        D = (l <= L) ? Dn : mk(0.0, 0.0);
+      }
+      // store alpha(mu, mu, l, kap) (or its negative-m image)
+      auto store = [&](int n, zd v) {
+        if(n < n_lo || n > n_hi || l > nmax || kap > l || kap < -l)
+          return;
+        int m = mu, k = kap;
+        if(neg) {
+          if(mu == 0)
+            return;
+          m = -mu;
+          k = -kap;
+          v = conj(v);
+          int sign = hankel ? (n + m + l + k) : (k + m);
+          if(sign & 1)
+            v = -v;
+        }
+        s.tab[(flat(n, m) - base) * W + l * (l + 1) - k] = v;
+      };
+      store(mu, D);
+      zd O2 = mk(0.0, 0.0), O1 = D;
+      const double apl = rcoef(s, Lc, l - 1, kap, kAP);
+      const double aml = rcoef(s, Lc, l + 1, kap, kAM);
+      for(int n = mu + 1; n <= n_hi; ++n) {
+        zd Om = shfl_up1(O1), Op = shfl_down1(O1);
+        double amn = rcoef(s, Lc, n - 1, mu, kAM);
+        double apn = rcoef(s, Lc, n - 1, mu, kAP);
+        zd O = (-(O2 * amn) + Om * apl + Op * aml) / apn;
+        if(l > L)
+          O = mk(0.0, 0.0);
+        O2 = O1;
+        O1 = O;
+        store(n, O);
+      }
+    }
+  }
+}
+
+// A(q, p) and B(q, p) of Coupling.cpp:30-51 for q = (n, m) in the table chunk
+// starting at flat index `base`, p = (l, k).
+__device__ __forceinline__ void coupling_entry(const Smem &s, const Layout &y, int base, int q, int p,
+                                               zd &A, zd &B) {
+  const double *qf = s.qf + q * kQfacStride;
+  const double *pf = s.pf + p * kPfacStride;
+  const int n = (int)qf[3], m = (int)qf[4], l = (int)pf[6], k = (int)pf[7];
+  const int W = y.W;
+  const zd *row = s.tab + (q - base) * W;
+  const zd zero = mk(0.0, 0.0);
+  const int c0 = l * (l + 1) - k;
+  zd t0 = row[c0];
+  zd tp = (m < n && k < l) ? row[c0 - 1 - W] : zero;
+  zd tm = (m > -n && k > -l) ? row[c0 + 1 + W] : zero;
+  A = (qf[2] * pf[2]) * t0 + (qf[0] * pf[0]) * tp + (qf[1] * pf[1]) * tm;
+  const int c1 = (l - 1) * l - k;
+  const int lm = l - 1;
+  zd u0 = (k <= lm && k >= -lm) ? row[c1] : zero;
+  zd up = (m < n && k + 1 <= lm && k + 1 >= -lm) ? row[c1 - 1 - W] : zero;
+  zd um = (m > -n && k - 1 >= -lm && k - 1 <= lm) ? row[c1 + 1 + W] : zero;
+  zd sm = (qf[2] * pf[3]) * u0 + (qf[0] * pf[4]) * up - (qf[1] * pf[5]) * um;
+  B = mk(sm.im, -sm.re);  // -i * sm
+}
+
+struct AssembleArgs {
+  const double *cart;
+  const zd *T;  // N x (nmax+1) x 2
+  const double *rec, *qf, *pf;
+  int N;
+  zd waveK;
+  long ld;
+  int nchunks;
+  int2 chunks[kMaxNmax];
+};
+
+__device__ __forceinline__ void put2(double2 *S64, float2 *S32, size_t at, zd v) {
+  S64[at] = make_double2(v.re, v.im);
+  if(S32)
+    S32[at] = make_float2((float)v.re, (float)v.im);
+}
+
+// S64 always receives the complex128 block; S32 (precision form) the same
+// values rounded to complex64 from the same FP64 arithmetic.
+__global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y, double2 *S64,
+                                                  float2 *S32) {
+  extern __shared__ double smem[];
+  const int b = blockIdx.x;
+  const int j = b / a.N, i = b - j * a.N;
+  const int P = y.P;
+  const long x0 = 2L * P * i, y0 = 2L * P * j;
+  if(i == j) {
+    for(int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) {
+      int c = idx / (2 * P), r = idx - c * 2 * P;
+      put2(S64, S32, (y0 + c) * a.ld + x0 + r, mk(r == c ? 1.0 : 0.0, 0.0));
+    }
+    return;
+  }
+  Smem s = smem_view(smem, y);
+  load_tables(s, y, a.rec, a.qf, a.pf);
+  for(int t = threadIdx.x; t < 2 * (y.nmax + 1); t += blockDim.x)
+    s.tl[t] = a.T[(size_t)i * 2 * (y.nmax + 1) + t];
+  if(threadIdx.x == 0) {
+    double dx = a.cart[3 * i] - a.cart[3 * j], dy = a.cart[3 * i + 1] - a.cart[3 * j + 1],
+           dz = a.cart[3 * i + 2] - a.cart[3 * j + 2];
+    to_spherical(dx, dy, dz, &s.geo[0], &s.geo[1], &s.geo[2]);
+  }
+  __syncthreads();
+  make_seeds(s, y, a.waveK, 1);
+  for(int c = 0; c < a.nchunks; ++c) {
+    const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
+    run_chains(s, y, 1, n_lo, n_hi);
+    __syncthreads();
+    const int base = n_lo * n_lo - 1;
+    const int rows = (n_hi + 1) * (n_hi + 1) - 1 - base;
+    for(int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
+      const int qr = idx / P, p = idx - qr * P, q = base + qr;
+      zd A, B;
+      coupling_entry(s, y, base, q, p, A, B);
+      const int l = (int)s.pf[p * kPfacStride + 6];
+      const zd te = s.tl[2 * l], tm = s.tl[2 * l + 1];
+      const size_t col_te = (y0 + q) * a.ld + x0, col_tm = (y0 + P + q) * a.ld + x0;
+      put2(S64, S32, col_te + p, -(te * A));
+      put2(S64, S32, col_tm + P + p, -(tm * A));
+      put2(S64, S32, col_tm + p, -(te * B));
+      put2(S64, S32, col_te + P + p, -(tm * B));
+    }
+    __syncthreads();
+  }
+}
+
+struct SourceArgs {
+  const double *cart;
+  const zd *T;
+  const zd *inc;  // 2P
+  const double *rec, *qf, *pf;
+  zd waveK;
+  zd *incloc, *Q;
+  double *wsca;
+  int nchunks;
+  int2 chunks[kMaxNmax];
+};
+
+// getIncLocal (Excitation.cpp:79-129) + source_vector (PreconditionedMatrix.cpp:1327-1345)
+// + the per-sphere weights of getScatteringCrossSection (Result.cpp:563-631).
+__global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
+  extern __shared__ double smem[];
+  const int i = blockIdx.x;
+  const int P = y.P, t = threadIdx.x;
+  Smem s = smem_view(smem, y);
+  load_tables(s, y, a.rec, a.qf, a.pf);
+  for(int u = t; u < 2 * (y.nmax + 1); u += blockDim.x)
+    s.tl[u] = a.T[(size_t)i * 2 * (y.nmax + 1) + u];
+  if(t == 0)
+    to_spherical(a.cart[3 * i], a.cart[3 * i + 1], a.cart[3 * i + 2], &s.geo[0], &s.geo[1],
+                 &s.geo[2]);
+  __syncthreads();
+  zd te = mk(0.0, 0.0), tm = mk(0.0, 0.0);
+  double w = 0.0;
+  const bool at_origin = fabs(s.geo[0]) < 1e-10;  // Coupling.cpp:82-84: A = I, B = 0
+  if(at_origin) {
+    if(t < P) {
+      te = a.inc[t];
+      tm = a.inc[P + t];
+      w = 1.0;
+    }
+  } else {
+    make_seeds(s, y, a.waveK, 0);
+    for(int c = 0; c < a.nchunks; ++c) {
+      const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
+      run_chains(s, y, 0, n_lo, n_hi);
+      __syncthreads();
+      const int base = n_lo * n_lo - 1;
+      const int qend = (n_hi + 1) * (n_hi + 1) - 1;
+      if(t < P) {
+        for(int q = base; q < qend; ++q) {  // IncLocal[p] = sum_q A(q,p) a_q + B(q,p) b_q
+          zd A, B;
+          coupling_entry(s, y, base, q, t, A, B);
+          te = te + A * a.inc[q] + B * a.inc[P + q];
+          tm = tm + B * a.inc[q] + A * a.inc[P + q];
+        }
+      }
+      if(t >= base && t < qend) {
+        for(int p = 0; p < P; ++p) {
+          zd A, B;
+          coupling_entry(s, y, base, t, p, A, B);
+          w += norm2(A) + norm2(B);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if(t < P) {
+    const size_t o = (size_t)i * 2 * P;
+    const int l = (int)s.pf[t * kPfacStride + 6];
+    a.incloc[o + t] = te;
+    a.incloc[o + P + t] = tm;
+    a.Q[o + t] = s.tl[2 * l] * te;
+    a.Q[o + P + t] = s.tl[2 * l + 1] * tm;
+    a.wsca[(size_t)i * P + t] = w;
+  }
+}
+
+struct CouplingArgs {
+  const double *rel;  // count x 3 Cartesian
+  const double *rec, *qf, *pf;
+  zd waveK;
+  int hankel;
+  zd *A, *B;  // count x P x P
+  int nchunks;
+  int2 chunks[kMaxNmax];
+};
+
+__global__ void __launch_bounds__(256) k_coupling(CouplingArgs a, Layout y) {
+  extern __shared__ double smem[];
+  const int e = blockIdx.x, P = y.P;
+  Smem s = smem_view(smem, y);
+  zd *A = a.A + (size_t)e * P * P, *B = a.B + (size_t)e * P * P;
+  load_tables(s, y, a.rec, a.qf, a.pf);
+  if(threadIdx.x == 0)
+    to_spherical(a.rel[3 * e], a.rel[3 * e + 1], a.rel[3 * e + 2], &s.geo[0], &s.geo[1],
+                 &s.geo[2]);
+  __syncthreads();
+  if(fabs(s.geo[0]) < 1e-10) {
+    for(int idx = threadIdx.x; idx < P * P; idx += blockDim.x) {
+      A[idx] = mk((idx / P) == (idx % P) ? 1.0 : 0.0, 0.0);
+      B[idx] = mk(0.0, 0.0);
+    }
+    return;
+  }
+  make_seeds(s, y, a.waveK, a.hankel);
+  for(int c = 0; c < a.nchunks; ++c) {
+    const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
+    run_chains(s, y, a.hankel, n_lo, n_hi);
+    __syncthreads();
+    const int base = n_lo * n_lo - 1;
+    const int rows = (n_hi + 1) * (n_hi + 1) - 1 - base;
+    for(int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
+      const int qr = idx / P, p = idx - qr * P, q = base + qr;
+      zd va, vb;
+      coupling_entry(s, y, base, q, p, va, vb);
+      A[(size_t)p * P + q] = va;  // row q = (n,m), column p = (l,k)
+      B[(size_t)p * P + q] = vb;
+    }
+    __syncthreads();
+  }
+}
+
+// Per sphere and n: T-matrix (FF, SH), internal factors and the Mie
+// absorption factors (Scatterer.cpp:39-271, Geometry.cpp:86-145).
+__global__ void k_sphere_terms(const SphereScalars *sc, int N, int nmax, zd *T, zd *Tsh, zd *iaux,
+                               double *cabs_out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= N)
+    return;
+  const SphereScalars c = sc[i];
+  for(int h = 0; h < 2; ++h) {
+    const zd r0 = h ? c.r0_sh : c.r0, rho = h ? c.rho_sh : c.rho,
+             mu_sob = h ? c.mu_sob_sh : c.mu_sob;
+    zd J[kMaxNmax + 2], dJ[kMaxNmax + 2], Jr[kMaxNmax + 2], dJr[kMaxNmax + 2], H[kMaxNmax + 2],
+        dH[kMaxNmax + 2];
+    bessel_deriv(0, r0, nmax, J, dJ);
+    bessel_deriv(0, rho * r0, nmax, Jr, dJr);
+    bessel_deriv(1, r0, nmax, H, dH);
+    zd *Tout = (h ? Tsh : T) + (size_t)i * 2 * (nmax + 1);
+    Tout[0] = mk(0.0, 0.0);
+    Tout[1] = mk(0.0, 0.0);
+    for(int n = 1; n <= nmax; ++n) {
+      zd psi = r0 * J[n];
+      zd dpsi = r0 * dJ[n] + J[n];
+      zd ksi = r0 * H[n];
+      zd dksi = r0 * dH[n] + H[n];
+      zd psirho = r0 * rho * Jr[n];
+      zd dpsirho = r0 * rho * dJr[n] + Jr[n];
+      zd TE = (psi / ksi) * (mu_sob * dpsi / psi - rho * dpsirho / psirho) /
+              (rho * dpsirho / psirho - mu_sob * dksi / ksi);
+      zd TM = (psi / ksi) * (mu_sob * dpsirho / psirho - rho * dpsi / psi) /
+              (rho * dksi / ksi - mu_sob * dpsirho / psirho);
+      Tout[2 * n] = TE;
+      Tout[2 * n + 1] = TM;
+      if(h == 0) {
+        const zd mu_j = c.mu_j, mu_0 = c.mu_0, I = mk(0.0, 1.0);
+        zd ia_te = (mu_j * rho) / (mu_0 * rho * dpsirho * psi - mu_j * psirho * dpsi) * I;
+        zd ia_tm = (mu_j * rho) / (mu_j * psi * dpsirho - mu_0 * rho * psirho * dpsi) * I;
+        iaux[(size_t)i * 2 * (nmax + 1) + 2 * n] = ia_te;
+        iaux[(size_t)i * 2 * (nmax + 1) + 2 * n + 1] = ia_tm;
+        zd t1 = I * rho * mu_0 * conj(mu_j) * conj(psirho) * dpsirho;
+        double t2 = cabs(mu_j * psirho * dpsi - mu_0 * rho * dpsirho * psi);
+        t2 *= t2;
+        cabs_out[(size_t)i * 2 * (nmax + 1) + 2 * n] = t1.re / t2;
+        t1 = I * conj(rho) * mu_0 * mu_j * conj(psirho) * dpsirho;
+        t2 = cabs(mu_0 * rho * psirho * dpsi - mu_j * dpsirho * psi);
+        t2 *= t2;
+        cabs_out[(size_t)i * 2 * (nmax + 1) + 2 * n + 1] = t1.re / t2;
+      }
+    }
+  }
+}
+
+// Excitation::populate (Excitation.cpp:48-75): one thread per m.
+__global__ void k_incident(int nmax, double theta, double phi, const double *einc, zd *inc) {
+  const int t = threadIdx.x;
+  if(t > 2 * nmax)
+    return;
+  const int m = nmax - t;
+  const int P = pmax(nmax);
+  double W[kMaxNmax + 1], dW[kMaxNmax + 1];
+  vigdvig(nmax, m, theta, W, dW);
+  const double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+  const zd E0 = mk(einc[0], einc[1]), E1 = mk(einc[2], einc[3]), E2 = mk(einc[4], einc[5]);
+  const double sgn_m = (m & 1) ? -1.0 : 1.0;
+  double ps, pc;
+  sincos(-(double)m * phi, &ps, &pc);
+  const zd ph = mk(pc, ps);
+  for(int n = (m < 0 ? -m : m); n <= nmax; ++n) {
+    if(n == 0)
+      continue;
+    double A;
+    if(m == 0)
+      A = 0.0;
+    else if(fabs(theta) < 1e-10 || (fabs(theta) - kPi + 1e-10) > 0.0)
+      A = m / cos(theta) * dW[n];
+    else
+      A = m / sin(theta) * W[n];
+    // local (r, theta, phi) components of C_n and B_n, projected to Cartesian
+    const zd Cr = mk(0.0, 0.0), Ct = mk(0.0, A), Cp = mk(-dW[n], 0.0);
+    const zd Br = mk(0.0, 0.0), Bt = mk(dW[n], 0.0), Bp = mk(0.0, A);
+    zd Cx = st * cp * Cr + ct * cp * Ct - sp * Cp, Cy = st * sp * Cr + ct * sp * Ct + cp * Cp,
+       Cz = ct * Cr - st * Ct;
+    zd Bx = st * cp * Br + ct * cp * Bt - sp * Bp, By = st * sp * Br + ct * sp * Bt + cp * Bp,
+       Bz = ct * Br - st * Bt;
+    zd cdot = conj(Cx) * E0 + conj(Cy) * E1 + conj(Cz) * E2;
+    zd bdot = conj(Bx) * E0 + conj(By) * E1 + conj(Bz) * E2;
+    const double dn = sqrt((2.0 * n + 1.0) / (4.0 * kPi * (double)((unsigned long)n * (n + 1))));
+    const zd i_pow[4] = {mk(1, 0), mk(0, 1), mk(-1, 0), mk(0, -1)};
+    const zd in = i_pow[n & 3], in1 = i_pow[(n + 3) & 3];
+    const int p = flat(n, m);
+    inc[p] = 4 * kPi * sgn_m * in * dn * cdot * ph;
+    inc[P + p] = 4 * kPi * sgn_m * in1 * dn * bdot * ph;
+  }
+}
+
+size_t g_smem_limit = 0;
+
+size_t smem_limit() {
+  if(!g_smem_limit) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    g_smem_limit = std::min<size_t>((size_t)v, 200 * 1024);
+  }
+  return g_smem_limit;
+}
+
+template <typename Args> void fill_chunks(Args &a, const Layout &y) {
+  auto ch = make_chunks(y);
+  a.nchunks = (int)ch.size();
+  for(size_t c = 0; c < ch.size(); ++c)
+    a.chunks[c] = make_int2(ch[c].first, ch[c].second);
+}
+
+template <typename K> void set_smem(K kernel, size_t bytes) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+}  // namespace
+
+const CoefTables &coef_tables(om_context *ctx, int nmax) {
+  for(auto &t : ctx->tables)
+    if(t.nmax == nmax)
+      return t;
+  CoefTables t;
+  t.nmax = nmax;
+  const int Lc = 2 * nmax + 1, P = pmax(nmax);
+  std::vector<double> rec(4 * (Lc + 1) * (Lc + 1), 0.0);
+  for(int n = 0; n <= Lc; ++n)
+    for(int m = -n; m <= n; ++m) {
+      int i = n * n + n + m;
+      rec[4 * i + kAP] = h_a_plus(n, m);
+      rec[4 * i + kAM] = h_a_minus(n, m);
+      rec[4 * i + kBP] = h_b_plus(n, m);
+      rec[4 * i + kBM] = h_b_minus(n, m);
+    }
+  std::vector<double> qf(kQfacStride * P), pf(kPfacStride * P);
+  for(int n = 1; n <= nmax; ++n)
+    for(int m = -n; m <= n; ++m) {
+      int i = flat(n, m);
+      double g = 0.5 / std::sqrt(double(n * (n + 1)));
+      qf[kQfacStride * i + 0] = g * std::sqrt(double((n - m) * (n + m + 1)));
+      qf[kQfacStride * i + 1] = g * std::sqrt(double((n + m) * (n - m + 1)));
+      qf[kQfacStride * i + 2] = g * 2 * m;
+      qf[kQfacStride * i + 3] = n;
+      qf[kQfacStride * i + 4] = m;
+      qf[kQfacStride * i + 5] = g;
+      int l = n, k = m;
+      double gl = 1.0 / std::sqrt(double(l * (l + 1)));
+      double hB = std::sqrt(double(2 * l + 1) / double((2 * l - 1) * l * (l + 1)));
+      pf[kPfacStride * i + 0] = gl * std::sqrt(double((l - k) * (l + k + 1)));
+      pf[kPfacStride * i + 1] = gl * std::sqrt(double((l + k) * (l - k + 1)));
+      pf[kPfacStride * i + 2] = gl * k;
+      pf[kPfacStride * i + 3] = hB * std::sqrt(double((l - k) * (l + k)));
+      pf[kPfacStride * i + 4] = hB * std::sqrt(double((l - k) * (l - k - 1)));
+      pf[kPfacStride * i + 5] = hB * std::sqrt(double((l + k) * (l + k - 1)));
+      pf[kPfacStride * i + 6] = l;
+      pf[kPfacStride * i + 7] = k;
+    }
+  auto up = [](const std::vector<double> &v) {
+    double *d = nullptr;
+    if(cudaMalloc(&d, v.size() * sizeof(double)) != cudaSuccess)
+      throw std::runtime_error("cudaMalloc failed for coefficient tables");
+    cudaMemcpy(d, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
+    return d;
+  };
+  t.rec = up(rec);
+  t.qf = up(qf);
+  t.pf = up(pf);
+  ctx->tables.push_back(t);
+  return ctx->tables.back();
+}
+
+void launch_sphere_terms(om_problem *pr) {
+  k_sphere_terms<<<blocks_for(pr->N, 64), 64, 0, pr->ctx->stream>>>(
+      pr->d_scal, pr->N, pr->nmax, pr->d_T, pr->d_Tsh, pr->d_iaux, pr->d_cabs);
+  pr->ctx->last_launches++;
+}
+
+void launch_incident(om_problem *pr, const double einc[6]) {
+  double *d_e = nullptr;
+  // the field vector is passed through a small device buffer owned by the problem
+  d_e = pr->d_xsec + 8;
+  cudaMemcpyAsync(d_e, einc, 6 * sizeof(double), cudaMemcpyHostToDevice, pr->ctx->stream);
+  k_incident<<<1, 32, 0, pr->ctx->stream>>>(pr->nmax, pr->theta, pr->phi, d_e, pr->d_inc);
+  pr->ctx->last_launches++;
+}
+
+void launch_assemble(om_problem *pr, int harmonic, int precision) {
+  om_context *ctx = pr->ctx;
+  const CoefTables &ct = coef_tables(ctx, pr->nmax);
+  Layout y = make_layout(pr->nmax, smem_limit());
+  AssembleArgs a;
+  a.cart = pr->d_cart;
+  a.T = harmonic == OM_SH ? pr->d_Tsh : pr->d_T;
+  a.rec = ct.rec;
+  a.qf = ct.qf;
+  a.pf = ct.pf;
+  a.N = pr->N;
+  cplx k = harmonic == OM_SH ? 2.0 * pr->waveK : pr->waveK;
+  a.waveK = mk(k.real(), k.imag());
+  a.ld = pr->n;
+  fill_chunks(a, y);
+  dim3 grid(pr->N * pr->N);
+  set_smem(k_assemble, y.bytes);
+  k_assemble<<<grid, 256, y.bytes, ctx->stream>>>(
+      a, y, (double2 *)pr->d_S[harmonic],
+      precision == OM_C64 ? (float2 *)pr->d_S32[harmonic] : nullptr);
+  ctx->last_launches++;
+}
+
+void launch_source(om_problem *pr) {
+  om_context *ctx = pr->ctx;
+  const CoefTables &ct = coef_tables(ctx, pr->nmax);
+  Layout y = make_layout(pr->nmax, smem_limit());
+  SourceArgs a;
+  a.cart = pr->d_cart;
+  a.T = pr->d_T;
+  a.inc = pr->d_inc;
+  a.rec = ct.rec;
+  a.qf = ct.qf;
+  a.pf = ct.pf;
+  a.waveK = mk(pr->waveK.real(), pr->waveK.imag());
+  a.incloc = pr->d_incloc;
+  a.Q = pr->d_Q;
+  a.wsca = pr->d_wsca;
+  fill_chunks(a, y);
+  set_smem(k_source, y.bytes);
+  k_source<<<pr->N, 256, y.bytes, ctx->stream>>>(a, y);
+  ctx->last_launches++;
+}
+
+int launch_coupling(om_context *ctx, const double *d_rel, int count, zd waveK, int nmax,
+                    int hankel, zd *d_A, zd *d_B) {
+  const CoefTables &ct = coef_tables(ctx, nmax);
+  Layout y = make_layout(nmax, smem_limit());
+  CouplingArgs a;
+  a.rel = d_rel;
+  a.rec = ct.rec;
+  a.qf = ct.qf;
+  a.pf = ct.pf;
+  a.waveK = waveK;
+  a.hankel = hankel;
+  a.A = d_A;
+  a.B = d_B;
+  fill_chunks(a, y);
+  set_smem(k_coupling, y.bytes);
+  k_coupling<<<count, 256, y.bytes, ctx->stream>>>(a, y);
+  ctx->last_launches++;
+  return 0;
+}
+
+}  // namespace om

@@ -1,0 +1,176 @@
+"""GPU parity tests: the CUDA library (through its C ABI) against the CPU
+oracle on the same inputs, and against the committed golden fixtures.
+
+Tolerances: 1e-10 relative for the FP64 path (assembly entries, source vector,
+scattering coefficients, cross sections, near field); 1e-6 for the
+cross sections of the precision form against FP64."""
+import numpy as np
+import pytest
+
+from helpers import gpu_inputs, load_golden, nm, oracle_cluster, random_cluster, rel
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = ["c0", "metal5", "diel3", "single_sh"]
+
+
+@pytest.fixture(scope="module")
+def G():
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    return G
+
+
+@pytest.fixture(scope="module")
+def ctx(G):
+    c = G.Context(0)
+    yield c
+    c.close()
+
+
+def make(G, ctx, cl):
+    sp, bg, wave = gpu_inputs(G, cl)
+    return G.Problem(ctx, sp, bg, wave)
+
+
+@pytest.mark.parametrize("nmax", [1, 3, 6, 8, 12])
+@pytest.mark.parametrize("regular", [True, False])
+def test_coupling_matches_oracle(G, ctx, oracle, nmax, regular):
+    rng = np.random.default_rng(nmax)
+    rels = rng.uniform(-400, 400, size=(3, 3)) * nm
+    rels[0] = [0.0, 0.0, 250 * nm]         # on the z axis
+    k = 2 * np.pi * 1.33 / (650 * nm)
+    A, B = G.coupling(ctx, rels, k, nmax, regular)
+    for e in range(rels.shape[0]):
+        sph = oracle.to_spherical(*rels[e])
+        Ao, Bo = oracle.coupling(sph, k, nmax, regular)
+        assert rel(A[e], Ao) < 1e-10, (e, rel(A[e], Ao))
+        assert rel(B[e], Bo) < 1e-10, (e, rel(B[e], Bo))
+
+
+def test_coupling_complex_wavenumber_and_zero_displacement(G, ctx, oracle):
+    k = 2 * np.pi * (1.4 + 0.05j) / (600 * nm)
+    rels = np.array([[120 * nm, -80 * nm, 60 * nm], [0.0, 0.0, 0.0]])
+    A, B = G.coupling(ctx, rels, k, 4, True)
+    Ao, Bo = oracle.coupling(oracle.to_spherical(*rels[0]), k, 4, True)
+    assert rel(A[0], Ao) < 1e-10 and rel(B[0], Bo) < 1e-10
+    assert np.array_equal(A[1], np.eye(24)) and not np.any(B[1])
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_fixture_pipeline(G, ctx, oracle, name):
+    g = load_golden(name)
+    cl = oracle_cluster(oracle, g)
+    pr_o = oracle.Problem(cl)
+    pr = make(G, ctx, cl)
+    assert rel(pr.incident_coefficients(), pr_o.inc_coeffs()) < 1e-12
+    T = pr.tmatrix()
+    Tsh = pr.tmatrix(G.SH)
+    for j in range(cl.n_spheres):
+        assert rel(T[j], pr_o.tmatrix(j)) < 1e-12
+        assert rel(Tsh[j], pr_o.tmatrix(j, sh=True)) < 1e-12
+    Q = pr.source_vector()
+    assert rel(Q, pr_o.source_vector()) < 1e-10
+    pr.assemble(G.FF, G.C128)
+    S = pr.matrix()
+    So = pr_o.scattering_matrix()
+    assert rel(S, So) < 1e-10
+    pr.assemble(G.SH, G.C128)
+    assert rel(pr.matrix(G.SH), pr_o.scattering_matrix(sh=True)) < 1e-10
+    # direct solve (pzgesv role) against the oracle's LU on the oracle's matrix
+    pr.solve(G.options(G.SOLVE_LU))
+    xs, xi = pr.coefficients()
+    xo = oracle.lu_solve(So, pr_o.source_vector())
+    assert rel(xs, xo) < 1e-10
+    ia = np.concatenate([pr_o.iaux(j) for j in range(cl.n_spheres)])
+    assert np.max(np.abs(xi - pr_o.internal(xo)) / (np.abs(ia) * np.max(np.abs(xo)))) < 1e-10
+    xsec = pr.cross_sections()
+    xo_sec = pr_o.cross_sections(xo)
+    assert np.max(np.abs(xsec - xo_sec) / np.abs(xo_sec)) < 1e-10, (xsec, xo_sec)
+    # golden fixture (reference AMOS Bessel arithmetic), see test_oracle for the 5e-10
+    assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 5e-10
+    # near field at the fixture's points, including one interior point
+    E, H = pr.near_field(g["points"])
+    Eo, Ho = pr_o.near_field(xo, pr_o.internal(xo), g["points"])
+    assert rel(E, Eo) < 1e-10 and rel(H, Ho) < 1e-10
+
+
+def test_gmres_matches_lu(G, ctx, oracle):
+    cl = oracle_cluster(oracle, load_golden("metal5"))
+    pr = make(G, ctx, cl)
+    pr.source_vector(copy=False)
+    pr.assemble()
+    pr.solve(G.options(G.SOLVE_LU))
+    x_lu = pr.coefficients()[0]
+    xs_lu = pr.cross_sections()
+    st = pr.solve(G.options(G.SOLVE_GMRES, tol=1e-13, max_iter=120, restarts=6))
+    assert st.rel_residual <= 1e-13 and st.iterations > 0
+    assert rel(pr.coefficients()[0], x_lu) < 1e-10
+    assert np.max(np.abs(pr.cross_sections() - xs_lu) / np.abs(xs_lu)) < 1e-10
+
+
+def test_mixed_precision_form(G, ctx, oracle):
+    rng = np.random.default_rng(7)
+    xyz, rad = random_cluster(rng, 12, 900 * nm, 40 * nm, 70 * nm, 20 * nm)
+    cl = oracle.Cluster(xyz=xyz, radius=rad, eps=(2.0 + 0.05j) ** 2, nmax=5, wavelength=650 * nm,
+                        theta=0.3, phi=0.2)
+    pr = make(G, ctx, cl)
+    pr.source_vector(copy=False)
+    pr.assemble(G.FF, G.C64)
+    pr.solve(G.options(G.SOLVE_GMRES, tol=1e-12))
+    ref = pr.cross_sections()
+    st = pr.solve(G.options(G.SOLVE_FGMRES_MIXED, tol=1e-10, inner_iter=30, inner_tol=1e-5))
+    assert st.inner_iterations > 0
+    got = pr.cross_sections()
+    assert np.max(np.abs(got - ref) / np.abs(ref)) < 1e-6
+    # the complex64 copy is the FP64 matrix rounded
+    S = pr.matrix()
+    assert S.shape == (pr.n, pr.n)
+
+
+def test_axial_incidence_matches_oracle(G, ctx, oracle):
+    """theta_k = 0 exactly: the reference's nudge-after-reflection behaviour
+    must be reproduced (x-polarised input expands as i * y-polarised)."""
+    cl = oracle.Cluster(xyz=[[0, 0, -125 * nm], [0, 0, 125 * nm]], radius=100 * nm,
+                        eps=(3.5 + 0.01j) ** 2, nmax=6, wavelength=600 * nm)
+    pr = make(G, ctx, cl)
+    assert rel(pr.incident_coefficients(), oracle.Problem(cl).inc_coeffs()) < 1e-12
+
+
+def test_error_codes(G, ctx):
+    sp = G.spheres_array([[0, 0, 0], [0, 0, 150 * nm]], 100 * nm, 2.0, 3)
+    with pytest.raises(G.OptimetError) as e:
+        G.Problem(ctx, sp, None, G.plane_wave(600 * nm))
+    assert e.value.code == G.ERR_OVERLAP
+    sp = G.spheres_array([[0, 0, 0], [0, 0, 500 * nm]], 100 * nm, 2.0, 3)
+    sp[1].nmax = 4
+    with pytest.raises(G.OptimetError) as e:
+        G.Problem(ctx, sp, None, G.plane_wave(600 * nm))
+    assert e.value.code == G.ERR_INVALID
+    sp = G.spheres_array([[0, 0, 0], [0, 0, 500 * nm]], 100 * nm, 2.0, 3)
+    pr = G.Problem(ctx, sp, None, G.plane_wave(600 * nm))
+    with pytest.raises(G.OptimetError) as e:
+        pr.solve(G.options(G.SOLVE_LU))
+    assert e.value.code == G.ERR_STATE
+    small = G.Context(0, budget=1 << 20)
+    sp = G.spheres_array(np.arange(20)[:, None] * np.array([[0, 0, 300 * nm]]), 100 * nm, 2.0, 8)
+    pr2 = G.Problem(small, sp, None, G.plane_wave(600 * nm))
+    with pytest.raises(G.OptimetError) as e:
+        pr2.assemble()
+    assert e.value.code == G.ERR_BUDGET
+    pr2.close()
+    small.close()
+
+
+def test_deterministic(G, ctx, oracle):
+    cl = oracle_cluster(oracle, load_golden("diel3"))
+    outs = []
+    for _ in range(2):
+        pr = make(G, ctx, cl)
+        pr.source_vector(copy=False)
+        pr.assemble()
+        pr.solve(G.options(G.SOLVE_GMRES, tol=1e-12))
+        outs.append((pr.coefficients()[0], pr.cross_sections()))
+        pr.close()
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
