@@ -1,0 +1,399 @@
+"""Benchmark of the OPTIMET sphere path on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload c2|c1]
+
+Metric: wavelength-solves per second of the precision form (complex64
+matrix, FP32 inner GMRES inside FP64 outer FGMRES) next to the plain FP64
+form, at <= 1e-6 relative extinction-efficiency error, with per-solve
+latency percentiles. One "step" = one wavelength-solve of the whole cluster:
+per-wavelength set-up, source vector, assembly of S, solve, internal
+coefficients and the four cross sections. Successive steps scan the
+wavelength (650 nm + 0.25 nm per step) so nothing is reused between steps.
+
+Default workload (c2): N = 400 non-overlapping spheres (seeded rejection
+sampling, 20 nm gap) in a 4 um cube, radii U[40, 70] nm, refractive index
+2.0+0.05i in vacuum, nMax = 8 -> 64,000 unknowns; plane wave along +z,
+x-polarised. Synthetic data. Inputs exceed L2 (S alone is 32.8 GB complex64 +
+65.5 GB complex128), so no L2 flush is needed between steps.
+
+Multi-GPU: independent replicas (one cluster scan per rank, no collective);
+value = the sum over ranks of the wavelength-solves each completed, divided
+by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "wavelength-solves/sec mixed vs FP64 on 1 GB300 at 1e-6 Qext err; p50/p99 latency"
+UNIT = "wavelength-solves/s"
+nm = 1e-9
+
+WORKLOADS = {
+    "c2": dict(N=400, edge=4000 * nm, rmin=40 * nm, rmax=70 * nm, index=2.0 + 0.05j, host=1.0,
+               nmax=8, lam=650 * nm, seed=20260402,
+               desc="N=400 spheres, nMax=8 (64,000 unknowns), 4 um cube, radii U[40,70] nm, "
+                    "index 2.0+0.05i in vacuum, plane wave +z x-polarised, lambda 650 nm + 0.25 nm/step"),
+    "c1": dict(N=100, edge=2000 * nm, rmin=50 * nm, rmax=80 * nm, index=0.3 + 3.0j, host=1.33,
+               nmax=8, lam=650 * nm, seed=20260401,
+               desc="N=100 spheres, nMax=8 (16,000 unknowns), 2 um cube, radii U[50,80] nm, "
+                    "index 0.3+3.0i in host index 1.33, plane wave +z x-polarised, lambda 650 nm"),
+}
+
+
+def cluster(w, rank=0):
+    rng = np.random.default_rng(w["seed"] + 7919 * rank)
+    xyz, rad = [], []
+    while len(xyz) < w["N"]:
+        r = rng.uniform(w["rmin"], w["rmax"])
+        c = rng.uniform(-w["edge"] / 2 + r, w["edge"] / 2 - r, size=3)
+        if xyz:
+            d = np.linalg.norm(np.array(xyz) - c, axis=1) - np.array(rad) - r
+            if d.min() < 20 * nm:
+                continue
+        xyz.append(c)
+        rad.append(r)
+    return np.array(xyz), np.array(rad)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                "sw_power_cap"), f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def gpu_arm(args, w):
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    rank, world, local = dist_env()
+    build.build()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    ctx = G.Context(local)
+    xyz, rad = cluster(w, rank)
+    n_index = complex(w["index"])
+    sp = G.spheres_array(xyz, rad, n_index ** 2, w["nmax"])
+    bg = G.medium(complex(w["host"]) ** 2)
+    pr = G.Problem(ctx, sp, bg, G.plane_wave(w["lam"]))
+    n = pr.n
+    mixed_opts = G.options(G.SOLVE_FGMRES_MIXED, tol=1e-8, max_iter=30, restarts=4, inner_iter=80,
+                           inner_tol=1e-4)
+    fp64_opts = G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=400, restarts=6)
+
+    def step(i, mixed):
+        pr.set_wavelength(w["lam"] + 0.25 * nm * i)
+        launches = ctx.last_launches
+        pr.source_vector(copy=False)
+        launches += ctx.last_launches
+        pr.assemble(G.FF, G.C64 if mixed else G.C128)
+        launches += ctx.last_launches
+        st = pr.solve(mixed_opts if mixed else fp64_opts)
+        launches += ctx.last_launches
+        xs = pr.cross_sections()
+        launches += ctx.last_launches
+        return xs, st, launches
+
+    def barrier():
+        ctx.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- precision form (the metric's numerator) ----
+    for i in range(args.warmup):
+        step(i, True)
+    barrier()
+    ctx.timers(True)
+    lat, xs_mixed, total_launches, inner, outer = [], [], 0, 0, 0
+    with ClockSampler(local) as clk:
+        ctx.mark()
+        for i in range(args.steps):
+            xs, st, launches = step(args.warmup + i, True)
+            lat.append(ctx.mark() * 1e-3)
+            xs_mixed.append(xs)
+            total_launches += launches
+            inner += st.inner_iterations
+            outer += st.iterations
+        barrier()
+        t_mixed = float(np.sum(lat))
+    kt = ctx.timers(False)
+    clocks = clk.summary()
+
+    # ---- plain FP64 form on the same wavelengths ----
+    step(0, False)
+    barrier()
+    lat64, xs64, it64 = [], [], 0
+    ctx.timers(True)
+    k64 = max(1, min(args.steps, 3))
+    ctx.mark()
+    for i in range(k64):
+        xs, st, _ = step(args.warmup + i, False)
+        lat64.append(ctx.mark() * 1e-3)
+        xs64.append(xs)
+        it64 += st.iterations
+    barrier()
+    t_fp64 = float(np.sum(lat64))
+    kt64 = ctx.timers(False)
+
+    # Q_ext = C_ext / sum(pi a^2): the relative error equals that of C_ext
+    err = max(abs(xs_mixed[i][0] - xs64[i][0]) / abs(xs64[i][0]) for i in range(k64))
+    err_all = max(float(np.max(np.abs(xs_mixed[i] - xs64[i]) / np.abs(xs64[i]))) for i in range(k64))
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e_lat = []
+    for i in range(2 + max(1, min(args.steps, 3))):
+        wave = G.plane_wave(w["lam"] + 0.25 * nm * i)
+        ctx.synchronize()
+        s0 = time.perf_counter()
+        G.wavelength_solve(ctx, sp, bg, wave, mixed_opts, G.C64)
+        if i >= 2:
+            e2e_lat.append(time.perf_counter() - s0)
+    import ctypes
+    h2d = ctypes.sizeof(G.Sphere) * len(sp) + ctypes.sizeof(G.Medium) + \
+        ctypes.sizeof(G.PlaneWave) + ctypes.sizeof(G.SolveOptions)
+    d2h = 4 * 8 + ctypes.sizeof(G.SolveStats)
+
+    # aggregate over ranks (max time, summed work)
+    t_mixed_all, t64_all, e2e_all = t_mixed, t_fp64, float(np.mean(e2e_lat))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t_mixed, t_fp64, e2e_all], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_mixed_all, t64_all, e2e_all = [float(v) for v in tt.cpu()]
+    value = world * args.steps / t_mixed_all
+    value64 = world * k64 / t64_all
+
+    hbm, how = peaks()
+    mv_ms, mv_n = kt["matvec_c64"]
+    bytes_mv = 8.0 * n * n  # complex64 matrix streamed once per inner matvec
+    achieved = bytes_mv / (mv_ms / mv_n * 1e-3) / 1e9 if mv_n else 0.0
+    asm_ms, asm_n = kt["assemble"]
+    bytes_asm = 24.0 * n * n  # complex128 + complex64 copies written
+    mv64_ms, mv64_n = kt64["matvec_c128"]
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed_all / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 (FP32) inner + c128 (FP64) outer/assembly",
+        "data": "synthetic (seeded random clusters)",
+        "config": {"workload": args.workload + ": " + w["desc"], "unknowns": n,
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)",
+                   "solver": "FGMRES(FP64 outer, tol 1e-8) + GMRES(FP32 inner, 80 it, tol 1e-4)"},
+        "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
+                       "p99": 1e3 * float(np.percentile(lat, 99))},
+        "fp64": {"value": value64, "unit": UNIT, "steps": k64, "ms_per_step": 1e3 * t64_all / k64,
+                 "latency_ms": {"p50": 1e3 * float(np.percentile(lat64, 50)),
+                                "p99": 1e3 * float(np.percentile(lat64, 99))},
+                 "gmres_iterations": it64 / k64, "tol": 1e-10},
+        "speedup_vs_fp64": value / value64,
+        "qext_rel_err_vs_fp64": err, "xsec_max_rel_err_vs_fp64": err_all,
+        "iterations": {"outer": outer / args.steps, "inner": inner / args.steps},
+        "e2e": {"value": world / e2e_all, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "om_wavelength_solve (C ABI, host buffers, set-up + teardown included)"},
+        "roofline": {"bound": "hbm", "kernel": "k_matvec_part<float2,float2> (FP32 inner matvec)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": how + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": None,
+                     "algorithmic_bytes_per_launch": bytes_mv},
+        "kernels": {
+            "assemble_mixed": {"ms_avg": asm_ms / max(asm_n, 1), "launches": asm_n,
+                               "written_GBps": bytes_asm / (asm_ms / max(asm_n, 1) * 1e-3) / 1e9
+                               if asm_n else None, "bound": "fp64 ALU"},
+            "matvec_c64": {"ms_avg": mv_ms / max(mv_n, 1), "launches": mv_n},
+            "matvec_c128": {"ms_avg": mv64_ms / max(mv64_n, 1), "launches": mv64_n,
+                            "bound": "fp64 ALU (4 FMA per 16 B)"},
+        },
+        "gpu_launches": total_launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(w, xyz, rad, it64 / k64, threads=None, budget_s=15.0)
+    pr.close()
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return result if rank == 0 else None
+
+
+def cpu_baseline(w, xyz, rad, gmres_iters, threads=None, budget_s=15.0):
+    """The oracle (a restatement of the reference's CPU algorithm: map-cached
+    Stout recurrences, dense matvec GMRES) timed on a bounded sample of the
+    same wavelength-solve on this host, extrapolated to one full solve."""
+    from oracle import oracle as O
+    O.lib()
+    threads = threads or O.max_threads()
+    O.set_threads(threads)
+    cl = O.Cluster(xyz=xyz, radius=rad, eps=complex(w["index"]) ** 2, nmax=w["nmax"],
+                   wavelength=w["lam"], bg_eps=complex(w["host"]) ** 2)
+    pr = O.Problem(cl)
+    N, P = cl.n_spheres, cl.P
+    n = cl.n_unknowns
+    rng = np.random.default_rng(1)
+    # assembly sample: ordered pairs i != j
+    npairs = max(threads, 8)
+    t_pair = None
+    while True:
+        pairs = []
+        while len(pairs) < npairs:
+            i, j = rng.integers(0, N, 2)
+            if i != j:
+                pairs.append((i, j))
+        t0 = time.perf_counter()
+        O.assemble_pairs(pr, pairs)
+        dt = time.perf_counter() - t0
+        t_pair = dt / npairs
+        if dt > budget_s / 3 or npairs >= N * (N - 1):
+            break
+        npairs = min(N * (N - 1), 1024, int(npairs * max(2.0, (budget_s / 3) / max(dt, 1e-3))))
+        if npairs >= 1024 and dt > 0.05:
+            break
+    t_asm = t_pair * N * (N - 1)
+    # matvec sample: a block of rows of a dense complex128 matrix of the full width
+    rows = max(64, min(n, int(2e8 // (16 * n))))
+    A = (rng.standard_normal((rows, n)) + 1j * rng.standard_normal((rows, n))).astype(np.complex128)
+    A = np.asfortranarray(A)
+    x = rng.standard_normal(n) + 0j
+    O.matvec(A, x)
+    reps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s / 3:
+        O.matvec(A, x)
+        reps += 1
+    t_mv = (time.perf_counter() - t0) / reps * (n / rows)
+    t_solve = t_asm + t_mv * (gmres_iters + 2)
+    O.set_threads(1)
+    return {"value": 1.0 / t_solve, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"oracle on {threads} host threads: {npairs} sampled pair blocks "
+                       f"({t_pair * 1e3:.2f} ms/pair, x N(N-1)={N * (N - 1)}) + dense FP64 "
+                       f"matvec on {rows} of {n} rows ({t_mv * 1e3:.1f} ms/full matvec) x "
+                       f"{gmres_iters + 2:.0f} GMRES iterations; extrapolated {t_solve:.1f} s/solve"),
+            "seconds_per_solve": t_solve}
+
+
+def reference_arm(args, w):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    xyz, rad = cluster(w, 0)
+    # GMRES iteration count of the FP64 form on this workload (measured on the GPU arm)
+    iters = {"c2": 60, "c1": 57}[args.workload]
+    lat = []
+    for i in range(args.warmup + args.steps):
+        s0 = time.perf_counter()
+        cb = cpu_baseline(w, xyz, rad, iters, threads=None, budget_s=6.0)
+        if i >= args.warmup:
+            lat.append(cb["seconds_per_solve"])
+    t = float(np.mean(lat))
+    return {"metric": METRIC, "value": 1.0 / t, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64)",
+            "data": "synthetic (seeded random clusters)", "impl": "reference",
+            "config": {"workload": args.workload + ": " + w["desc"]},
+            "cpu_baseline": {"value": 1.0 / t, "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                             "sample": cb["sample"]},
+            "e2e": {"value": 1.0 / t, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+    out = reference_arm(args, w) if args.impl == "reference" else gpu_arm(args, w)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -97,6 +97,16 @@ int om_context_last_launches(const om_context *ctx);
 /* Wait for all work queued on the context's stream (calls are asynchronous
  * with respect to the host unless they return data). */
 int om_context_synchronize(om_context *ctx);
+/* Kernel timers (CUDA events on the context's stream; no counterpart in the
+ * reference, which has no profiling). Writes the totals accumulated since the
+ * previous call to out[6] = {assembly ms, assembly launches, complex128 matvec
+ * ms, launches, complex64 matvec ms, launches} (out may be NULL), resets them
+ * and switches timing on or off. */
+int om_context_timers(om_context *ctx, int enable, double *out);
+/* Record an event on the context's stream, wait for it and return in *ms the
+ * device time since the previous mark (0 for the first). Device-side step
+ * timing for benchmarks; no counterpart in the reference. */
+int om_context_mark(om_context *ctx, double *ms);
 
 /* Geometry + Excitation for one cluster at one wavelength. Mirrors
  * simulation_input (Reader.cpp:55-101,585-663,782-834): spheres are stored in

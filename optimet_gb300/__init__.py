@@ -81,6 +81,8 @@ def lib():
         L.om_context_last_error.restype = C.c_char_p
         L.om_context_last_launches.argtypes = [vp]
         L.om_context_synchronize.argtypes = [vp]
+        L.om_context_timers.argtypes = [vp, C.c_int, _dp]
+        L.om_context_mark.argtypes = [vp, _dp]
         L.om_problem_create.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
                                         C.POINTER(PlaneWave), pvp]
         L.om_problem_destroy.argtypes = [vp]
@@ -140,6 +142,19 @@ class Context:
 
     def synchronize(self):
         self.check(lib().om_context_synchronize(self.h))
+
+    def mark(self) -> float:
+        """Device milliseconds since the previous mark (CUDA events on the stream)."""
+        out = np.zeros(1)
+        self.check(lib().om_context_mark(self.h, _p(out)))
+        return float(out[0])
+
+    def timers(self, enable=True):
+        """Kernel times since the last call: dict of (milliseconds, launches)."""
+        out = np.zeros(6)
+        self.check(lib().om_context_timers(self.h, int(enable), _p(out)))
+        return {"assemble": (out[0], int(out[1])), "matvec_c128": (out[2], int(out[3])),
+                "matvec_c64": (out[4], int(out[5]))}
 
     @property
     def last_launches(self) -> int:

@@ -279,7 +279,68 @@ int ensure_matrix(om_problem *pr, int harmonic, int precision) {
 
 }  // namespace
 
+namespace om {
+void collect_timers(om_context *ctx) {
+  auto fold = [](std::vector<std::pair<cudaEvent_t, cudaEvent_t>> &v, double &t, long &n) {
+    for(auto &e : v) {
+      float ms = 0;
+      cudaEventSynchronize(e.second);
+      cudaEventElapsedTime(&ms, e.first, e.second);
+      t += ms;
+      ++n;
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+    v.clear();
+  };
+  fold(ctx->ev_mv64, ctx->t_mv64, ctx->n_mv64);
+  fold(ctx->ev_mv32, ctx->t_mv32, ctx->n_mv32);
+  fold(ctx->ev_asm, ctx->t_asm, ctx->n_asm);
+}
+}  // namespace om
+
 extern "C" {
+
+int om_context_mark(om_context *ctx, double *ms) {
+  if(!ctx)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaEvent_t e;
+  if(cudaEventCreate(&e) != cudaSuccess)
+    return cuda_fail(ctx, cudaGetLastError(), "event");
+  cudaEventRecord(e, ctx->stream);
+  cudaError_t err = cudaEventSynchronize(e);
+  if(err != cudaSuccess)
+    return cuda_fail(ctx, err, "mark");
+  float t = 0;
+  if(ctx->mark) {
+    cudaEventElapsedTime(&t, ctx->mark, e);
+    cudaEventDestroy(ctx->mark);
+  }
+  ctx->mark = e;
+  if(ms)
+    *ms = t;
+  return OM_OK;
+}
+
+int om_context_timers(om_context *ctx, int enable, double *out) {
+  if(!ctx)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  om::collect_timers(ctx);
+  if(out) {
+    out[0] = ctx->t_asm;
+    out[1] = (double)ctx->n_asm;
+    out[2] = ctx->t_mv64;
+    out[3] = (double)ctx->n_mv64;
+    out[4] = ctx->t_mv32;
+    out[5] = (double)ctx->n_mv32;
+  }
+  ctx->t_asm = ctx->t_mv64 = ctx->t_mv32 = 0;
+  ctx->n_asm = ctx->n_mv64 = ctx->n_mv32 = 0;
+  ctx->timing = enable != 0;
+  return OM_OK;
+}
 
 int om_context_create(int device, size_t budget_bytes, om_context **out) {
   if(!out)
@@ -315,6 +376,8 @@ void om_context_destroy(om_context *ctx) {
     cudaFree(t.qf);
     cudaFree(t.pf);
   }
+  if(ctx->mark)
+    cudaEventDestroy(ctx->mark);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

@@ -52,6 +52,12 @@ struct om_context {
   std::string err;
   std::vector<om::CoefTables> tables;  // by nmax
   int last_launches = 0;               // kernels launched by the last API call
+  // kernel timers (CUDA events on `stream`), reset by om_context_timers
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_mv64, ev_mv32, ev_asm;
+  double t_mv64 = 0, t_mv32 = 0, t_asm = 0;  // accumulated milliseconds
+  cudaEvent_t mark = nullptr;                // last om_context_mark event
+  long n_mv64 = 0, n_mv32 = 0, n_asm = 0;
 };
 
 struct om_problem {
@@ -116,5 +122,22 @@ int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, co
                      const double2 *b, double2 *x, om_solve_stats *st);
 
 inline int blocks_for(long n, int threads) { return (int)((n + threads - 1) / threads); }
+
+// Event pair around a launch when timing is enabled; folded by collect_timers.
+inline void timer_begin(om_context *ctx, std::vector<std::pair<cudaEvent_t, cudaEvent_t>> &v) {
+  if(!ctx->timing)
+    return;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, ctx->stream);
+  v.push_back({a, b});
+}
+inline void timer_end(om_context *ctx, std::vector<std::pair<cudaEvent_t, cudaEvent_t>> &v) {
+  if(!ctx->timing || v.empty())
+    return;
+  cudaEventRecord(v.back().second, ctx->stream);
+}
+void collect_timers(om_context *ctx);
 
 }  // namespace om

@@ -238,7 +238,10 @@ template <typename M, typename V>
 void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, const V *b) {
   const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
   dim3 grid((unsigned)((n + kMvThreads - 1) / kMvThreads), (unsigned)nsplit);
+  auto &ev = sizeof(M) == sizeof(double2) ? ctx->ev_mv64 : ctx->ev_mv32;
+  timer_begin(ctx, ev);
   k_matvec_part<M, V><<<grid, kMvThreads, 0, ctx->stream>>>(S, n, n, x, part);
+  timer_end(ctx, ev);
   k_matvec_reduce<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(part, nsplit, n, b, y);
   ctx->last_launches += 2;
 }

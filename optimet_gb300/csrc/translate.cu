@@ -52,7 +52,7 @@ double h_b_minus(int n, int m) {
                    static_cast<double>((2 * n + 1) * (2 * n - 1)));
 }
 
-enum { kAP = 0, kAM = 1, kBP = 2, kBM = 3 };
+enum { kAP = 0, kAM = 1, kBP = 2, kBM = 3, kRAP = 4, kRBP = 5, kRecStride = 6 };
 
 // Shared-memory layout of a translation CTA (offsets in doubles).
 struct Layout {
@@ -75,7 +75,7 @@ Layout make_layout(int nmax, size_t smem_limit) {
     o += (n + 1) & ~1;  // keep 16-byte alignment for complex entries
     return at;
   };
-  y.rec = take(4 * (y.Lc + 1) * (y.Lc + 1));
+  y.rec = take(kRecStride * (y.Lc + 1) * (y.Lc + 1));
   y.qf = take(kQfacStride * y.P);
   y.pf = take(kPfacStride * y.P);
   y.leg = take((y.L + 1) * (y.L + 2) / 2);
@@ -132,7 +132,7 @@ __device__ Smem smem_view(double *base, const Layout &y) {
 __device__ __forceinline__ double rcoef(const Smem &s, int Lc, int n, int m, int which) {
   if(n < 0 || n > Lc || m > n || m < -n)
     return 0.0;
-  return s.rec[4 * (n * n + n + m) + which];
+  return s.rec[kRecStride * (n * n + n + m) + which];
 }
 
 __device__ __forceinline__ zd shfl_up1(zd v) {
@@ -145,7 +145,7 @@ __device__ __forceinline__ zd shfl_down1(zd v) {
 // Copy the geometry-independent tables into shared memory.
 __device__ void load_tables(const Smem &s, const Layout &y, const double *rec, const double *qf,
                             const double *pf) {
-  int nrec = 4 * (y.Lc + 1) * (y.Lc + 1);
+  int nrec = kRecStride * (y.Lc + 1) * (y.Lc + 1);
   for(int i = threadIdx.x; i < nrec; i += blockDim.x)
     s.rec[i] = rec[i];
   for(int i = threadIdx.x; i < kQfacStride * y.P; i += blockDim.x)
@@ -225,16 +225,27 @@ __device__ void make_seeds(const Smem &s, const Layout &y, zd waveK, int hankel)
 }
 
 // The recurrence chains; stores alpha(n, m, l, k) for n in [n_lo, n_hi], l <= nMax.
-__device__ void run_chains(const Smem &s, const Layout &y, int hankel, int n_lo, int n_hi) {
+// For a real wave number the conjugate-wave chains (TranslationAdditionCoefficients.h:72-74)
+// follow from the positive ones: regular: alpha_neg = alpha_pos; irregular (Hankel
+// h_l(-x) = (-1)^l conj(h_l(x))): alpha_neg(n,m,l,k) = (-1)^{n+l} e^{2 i d phi}
+// conj(alpha_pos(n,m,l,k)), d = m - k (the recurrence keeps n + l parity and d);
+// only the positive chains then run.
+__device__ void run_chains(const Smem &s, const Layout &y, int hankel, bool real_k, int n_lo,
+                           int n_hi) {
   const int nmax = y.nmax, L = y.L, Lc = y.Lc, W = y.W;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  const int npos = 3 * nmax + 1, nneg = 3 * nmax;
+  const int npos = 3 * nmax + 1, nneg = real_k ? 0 : 3 * nmax;
   const int base = n_lo * n_lo - 1;  // flat(n_lo, n_lo)
   const int l = lane;
+  const double phi = s.geo[2];
   for(int c = warp; c < npos + nneg; c += nwarps) {
     const bool neg = c >= npos;
     const int d = neg ? (c - npos) + 1 - nmax : c - nmax;
     const zd *seed = s.seed + (neg ? (L + 1) * (L + 1) : 0);
+    // e^{-2 i d phi}: maps a positive-chain value to its negative-m image
+    double e2s, e2c;
+    sincos(-2.0 * d * phi, &e2s, &e2c);
+    const zd e2 = mk(e2c, e2s);
     zd D = mk(0.0, 0.0);
     if(l <= L && (d < 0 ? -d : d) <= l)
       D = seed[l * l + l - d];
@@ -245,26 +256,34 @@ __device__ void run_chains(const Smem &s, const Layout &y, int hankel, int n_lo,
         zd Dm = shfl_up1(D), Dp = shfl_down1(D);
         double bp = rcoef(s, Lc, l - 1, kap - 1, kBP);
         double bm = rcoef(s, Lc, l + 1, kap - 1, kBM);
-        double den = rcoef(s, Lc, mu - 1, mu - 1, kBP);
-        zd Dn = (Dm * bp + Dp * bm) / den;
+        double rden = rcoef(s, Lc, mu - 1, mu - 1, kRBP);
+        zd Dn = (Dm * bp + Dp * bm) * rden;
         D = (l <= L) ? Dn : mk(0.0, 0.0);
       }
-      // store alpha(mu, mu, l, kap) (or its negative-m image)
+      // store alpha(n, mu, l, kap) and, from the positive chains of a real
+      // wave number, the negative-m image (n, -mu, l, -kap)
       auto store = [&](int n, zd v) {
         if(n < n_lo || n > n_hi || l > nmax || kap > l || kap < -l)
           return;
-        int m = mu, k = kap;
+        if(!neg)
+          s.tab[(flat(n, mu) - base) * W + l * (l + 1) - kap] = v;
+        if(mu == 0 || (!neg && !real_k))
+          return;
+        const int m = -mu, k = -kap;
+        zd w;
         if(neg) {
-          if(mu == 0)
-            return;
-          m = -mu;
-          k = -kap;
-          v = conj(v);
-          int sign = hankel ? (n + m + l + k) : (k + m);
-          if(sign & 1)
-            v = -v;
+          w = conj(v);
+        } else if(hankel) {
+          w = e2 * v;  // conj(alpha_neg) = (-1)^{n+l} e^{-2 i d phi} alpha_pos
+          if((n + l) & 1)
+            w = -w;
+        } else {
+          w = conj(v);
         }
-        s.tab[(flat(n, m) - base) * W + l * (l + 1) - k] = v;
+        const int sign = hankel ? (n + m + l + k) : (k + m);
+        if(sign & 1)
+          w = -w;
+        s.tab[(flat(n, m) - base) * W + l * (l + 1) - k] = w;
       };
       store(mu, D);
       zd O2 = mk(0.0, 0.0), O1 = D;
@@ -273,8 +292,8 @@ __device__ void run_chains(const Smem &s, const Layout &y, int hankel, int n_lo,
       for(int n = mu + 1; n <= n_hi; ++n) {
         zd Om = shfl_up1(O1), Op = shfl_down1(O1);
         double amn = rcoef(s, Lc, n - 1, mu, kAM);
-        double apn = rcoef(s, Lc, n - 1, mu, kAP);
-        zd O = (-(O2 * amn) + Om * apl + Op * aml) / apn;
+        double rapn = rcoef(s, Lc, n - 1, mu, kRAP);
+        zd O = (-(O2 * amn) + Om * apl + Op * aml) * rapn;
         if(l > L)
           O = mk(0.0, 0.0);
         O2 = O1;
@@ -355,7 +374,7 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y, doub
   make_seeds(s, y, a.waveK, 1);
   for(int c = 0; c < a.nchunks; ++c) {
     const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
-    run_chains(s, y, 1, n_lo, n_hi);
+    run_chains(s, y, 1, a.waveK.im == 0.0, n_lo, n_hi);
     __syncthreads();
     const int base = n_lo * n_lo - 1;
     const int rows = (n_hi + 1) * (n_hi + 1) - 1 - base;
@@ -414,7 +433,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
     make_seeds(s, y, a.waveK, 0);
     for(int c = 0; c < a.nchunks; ++c) {
       const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
-      run_chains(s, y, 0, n_lo, n_hi);
+      run_chains(s, y, 0, a.waveK.im == 0.0, n_lo, n_hi);
       __syncthreads();
       const int base = n_lo * n_lo - 1;
       const int qend = (n_hi + 1) * (n_hi + 1) - 1;
@@ -477,7 +496,7 @@ __global__ void __launch_bounds__(256) k_coupling(CouplingArgs a, Layout y) {
   make_seeds(s, y, a.waveK, a.hankel);
   for(int c = 0; c < a.nchunks; ++c) {
     const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
-    run_chains(s, y, a.hankel, n_lo, n_hi);
+    run_chains(s, y, a.hankel, a.waveK.im == 0.0, n_lo, n_hi);
     __syncthreads();
     const int base = n_lo * n_lo - 1;
     const int rows = (n_hi + 1) * (n_hi + 1) - 1 - base;
@@ -618,14 +637,16 @@ const CoefTables &coef_tables(om_context *ctx, int nmax) {
   CoefTables t;
   t.nmax = nmax;
   const int Lc = 2 * nmax + 1, P = pmax(nmax);
-  std::vector<double> rec(4 * (Lc + 1) * (Lc + 1), 0.0);
+  std::vector<double> rec(kRecStride * (Lc + 1) * (Lc + 1), 0.0);
   for(int n = 0; n <= Lc; ++n)
     for(int m = -n; m <= n; ++m) {
       int i = n * n + n + m;
-      rec[4 * i + kAP] = h_a_plus(n, m);
-      rec[4 * i + kAM] = h_a_minus(n, m);
-      rec[4 * i + kBP] = h_b_plus(n, m);
-      rec[4 * i + kBM] = h_b_minus(n, m);
+      rec[kRecStride * i + kAP] = h_a_plus(n, m);
+      rec[kRecStride * i + kAM] = h_a_minus(n, m);
+      rec[kRecStride * i + kBP] = h_b_plus(n, m);
+      rec[kRecStride * i + kBM] = h_b_minus(n, m);
+      rec[kRecStride * i + kRAP] = h_a_plus(n, m) != 0.0 ? 1.0 / h_a_plus(n, m) : 0.0;
+      rec[kRecStride * i + kRBP] = h_b_plus(n, m) != 0.0 ? 1.0 / h_b_plus(n, m) : 0.0;
     }
   std::vector<double> qf(kQfacStride * P), pf(kPfacStride * P);
   for(int n = 1; n <= nmax; ++n)
@@ -696,9 +717,11 @@ void launch_assemble(om_problem *pr, int harmonic, int precision) {
   fill_chunks(a, y);
   dim3 grid(pr->N * pr->N);
   set_smem(k_assemble, y.bytes);
+  timer_begin(ctx, ctx->ev_asm);
   k_assemble<<<grid, 256, y.bytes, ctx->stream>>>(
       a, y, (double2 *)pr->d_S[harmonic],
       precision == OM_C64 ? (float2 *)pr->d_S32[harmonic] : nullptr);
+  timer_end(ctx, ctx->ev_asm);
   ctx->last_launches++;
 }
 

@@ -1287,6 +1287,59 @@ void orc_grid_points(const double *g, double *xyz) {
   }
 }
 
+// Blocks S_ij of preconditioned_scattering_matrix for a list of ordered pairs
+// (i_k, j_k): out holds count x (2P x 2P) column-major blocks. Used to time a
+// bounded sample of the assembly on the host.
+int orc_assemble_pairs(void *h, int count, const int *pairs, double *out) {
+  Problem *pr = static_cast<Problem *>(h);
+  try {
+    const int P = pmax(pr->nmax), n2 = 2 * P;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(g_threads)
+    for(int t = 0; t < count; ++t) {
+      int i = pairs[2 * t], j = pairs[2 * t + 1];
+      cplx *S = C(out) + (size_t)t * n2 * n2;
+      std::vector<cplx> T(n2), A, B;
+      tmatrix(*pr, pr->objects[i], false, T.data());
+      coupling(sph_minus(pr->objects[i].vR, pr->objects[j].vR), pr->waveK, pr->nmax, true, A, B);
+      for(int q = 0; q < P; ++q)
+        for(int p = 0; p < P; ++p) {
+          cplx a = A[size_t(p) * P + q], b = B[size_t(p) * P + q];
+          S[size_t(q) * n2 + p] = -(T[p] * a);
+          S[size_t(P + q) * n2 + P + p] = -(T[P + p] * a);
+          S[size_t(P + q) * n2 + p] = -(T[p] * b);
+          S[size_t(q) * n2 + P + p] = -(T[P + p] * b);
+        }
+    }
+    return 0;
+  } catch(std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// y = A x for a dense rows x cols column-major block (the GMRES matvec of the
+// CPU baseline, timed on a row sample).
+void orc_matvec(int rows, int cols, const double *A, const double *x, double *y) {
+  std::fill(C(y), C(y) + rows, cplx(0.0, 0.0));
+  // matvec() expects a square matrix; run the rectangular form here
+#pragma omp parallel num_threads(g_threads)
+  {
+    std::vector<cplx> loc(rows, cplx(0.0, 0.0));
+#pragma omp for schedule(static)
+    for(int j = 0; j < cols; ++j) {
+      const cplx *c = C(A) + size_t(j) * rows;
+      cplx v = C(x)[j];
+      for(int i = 0; i < rows; ++i)
+        loc[i] += c[i] * v;
+    }
+#pragma omp critical
+    {
+      for(int i = 0; i < rows; ++i)
+        C(y)[i] += loc[i];
+    }
+  }
+}
+
 // One full wavelength-solve (the unit the CPU baseline times): source vector,
 // FF assembly, solve (0 = LU, 1 = GMRES), internal coefficients, cross
 // sections. X_sca / X_int may be null.

@@ -57,12 +57,14 @@ def lib():
                                 C.POINTER(C.c_int), _dp]
         L.orc_bessel.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp]
         L.orc_ynm.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
-        L.orc_ta.argtypes = [C.c_double] * 6 + [C.c_int] * 5 + [_dp]
+        L.orc_ta.argtypes = [C.c_double] * 5 + [C.c_int] * 5 + [_dp]
         L.orc_coupling.argtypes = [C.c_double] * 5 + [C.c_int, C.c_int, _dp, _dp]
         L.orc_to_spherical.argtypes = [C.c_double] * 3 + [_dp]
         L.orc_grid_points.argtypes = [_dp, _dp]
         L.orc_use_amos.argtypes = [C.c_char_p]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_assemble_pairs.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]
+        L.orc_matvec.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -255,6 +257,30 @@ class Problem:
         if rc < 0:
             raise RuntimeError(lib().orc_last_error().decode())
         return xsec, xs, xi, it.value
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def assemble_pairs(pr: Problem, pairs):
+    """Blocks S_ij for the given (i, j) pairs (timing sample of the assembly)."""
+    pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+    n2 = 2 * pr.cl.P
+    out = np.zeros((pairs.shape[0], n2, n2), np.complex128)
+    rc = lib().orc_assemble_pairs(pr.h, pairs.shape[0], pairs.ctypes.data_as(C.POINTER(C.c_int)),
+                                  _p(out))
+    if rc:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return out
+
+
+def matvec(A, x):
+    A = np.asfortranarray(A, dtype=np.complex128)
+    x = _c(x)
+    y = np.zeros(A.shape[0], np.complex128)
+    lib().orc_matvec(A.shape[0], A.shape[1], _p(A), _p(x), _p(y))
+    return y
 
 
 def lu_solve(A, b):
