@@ -282,7 +282,11 @@ def gpu_arm(args, w):
             "assemble_mixed": {"ms_avg": asm_ms / max(asm_n, 1), "launches": asm_n,
                                "written_GBps": bytes_asm / (asm_ms / max(asm_n, 1) * 1e-3) / 1e9
                                if asm_n else None, "bound": "fp64 ALU"},
-            "matvec_c64": {"ms_avg": mv_ms / max(mv_n, 1), "launches": mv_n},
+            "matvec_c64": {"ms_avg": mv_ms / max(mv_n, 1), "launches": mv_n,
+                           "GBps": achieved, "bound": "hbm"},
+            "matvec_c64_compensated": {"ms_avg": kt["matvec_c64_df"][0] / max(kt["matvec_c64_df"][1], 1),
+                                       "launches": kt["matvec_c64_df"][1],
+                                       "GBps": bytes_mv / (kt["matvec_c64_df"][0] / max(kt["matvec_c64_df"][1], 1) * 1e-3) / 1e9 if kt["matvec_c64_df"][1] else None},
             "matvec_c128": {"ms_avg": mv64_ms / max(mv64_n, 1), "launches": mv64_n,
                             "bound": "fp64 ALU (4 FMA per 16 B)"},
         },

@@ -99,9 +99,10 @@ int om_context_last_launches(const om_context *ctx);
 int om_context_synchronize(om_context *ctx);
 /* Kernel timers (CUDA events on the context's stream; no counterpart in the
  * reference, which has no profiling). Writes the totals accumulated since the
- * previous call to out[6] = {assembly ms, assembly launches, complex128 matvec
- * ms, launches, complex64 matvec ms, launches} (out may be NULL), resets them
- * and switches timing on or off. */
+ * previous call to out[8] = {assembly ms, assembly launches, complex128 matvec
+ * ms, launches, complex64 x complex64 matvec ms, launches, complex64 x
+ * complex128 (compensated) matvec ms, launches} (out may be NULL), resets
+ * them and switches timing on or off. */
 int om_context_timers(om_context *ctx, int enable, double *out);
 /* Record an event on the context's stream, wait for it and return in *ms the
  * device time since the previous mark (0 for the first). Device-side step

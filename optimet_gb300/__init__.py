@@ -151,10 +151,10 @@ class Context:
 
     def timers(self, enable=True):
         """Kernel times since the last call: dict of (milliseconds, launches)."""
-        out = np.zeros(6)
+        out = np.zeros(8)
         self.check(lib().om_context_timers(self.h, int(enable), _p(out)))
         return {"assemble": (out[0], int(out[1])), "matvec_c128": (out[2], int(out[3])),
-                "matvec_c64": (out[4], int(out[5]))}
+                "matvec_c64": (out[4], int(out[5])), "matvec_c64_df": (out[6], int(out[7]))}
 
     @property
     def last_launches(self) -> int:

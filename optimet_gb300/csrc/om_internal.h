@@ -29,6 +29,7 @@ struct CoefTables {
   double *rec = nullptr;
   double *qf = nullptr;
   double *pf = nullptr;
+  double *legc = nullptr;  // normalised-Legendre recurrence coefficients for l <= 2 nMax
 };
 constexpr int kQfacStride = 6;
 constexpr int kPfacStride = 8;
@@ -54,10 +55,10 @@ struct om_context {
   int last_launches = 0;               // kernels launched by the last API call
   // kernel timers (CUDA events on `stream`), reset by om_context_timers
   bool timing = false;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_mv64, ev_mv32, ev_asm;
-  double t_mv64 = 0, t_mv32 = 0, t_asm = 0;  // accumulated milliseconds
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_mv64, ev_mv32, ev_mvdf, ev_asm;
+  double t_mv64 = 0, t_mv32 = 0, t_mvdf = 0, t_asm = 0;  // accumulated milliseconds
   cudaEvent_t mark = nullptr;                // last om_context_mark event
-  long n_mv64 = 0, n_mv32 = 0, n_asm = 0;
+  long n_mv64 = 0, n_mv32 = 0, n_mvdf = 0, n_asm = 0;
 };
 
 struct om_problem {
@@ -90,9 +91,9 @@ struct om_problem {
   om::zd *d_incloc = nullptr; // n: IncLocal per sphere
   double *d_wsca = nullptr;   // N x P: sum_p |T^reg_pq|^2 (Result.cpp:563-631)
   om::zd *d_Q = nullptr;      // n
-  void *d_S[2] = {nullptr, nullptr};    // complex128 matrix per harmonic
-  void *d_S32[2] = {nullptr, nullptr};  // complex64 copy (precision form)
-  int S_prec[2] = {-1, -1};             // OM_C128, or OM_C64 when both copies exist
+  void *d_S[2] = {nullptr, nullptr};    // complex128 matrix per harmonic (plain form)
+  void *d_S32[2] = {nullptr, nullptr};  // complex64 matrix per harmonic (precision form)
+  int S_prec[2] = {-1, -1};             // which of the two holds the current assembly
   om::zd *d_X = nullptr, *d_Xint = nullptr;
   double *d_xsec = nullptr;   // 4 + scratch
   bool have_source = false, have_solution = false;
@@ -118,8 +119,10 @@ void launch_near_field(om_problem *pr, const double *d_xyz, int npts, zd *d_E, z
 int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_solve_stats *st);
 int solve_gmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
                     double2 *x, om_solve_stats *st);
-int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const float2 *S32,
-                     const double2 *b, double2 *x, om_solve_stats *st);
+int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
+                     double2 *x, om_solve_stats *st);
+int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
+                       double2 *x, om_solve_stats *st);
 
 inline int blocks_for(long n, int threads) { return (int)((n + threads - 1) / threads); }
 

@@ -97,12 +97,13 @@ OM_HD void sph_j(zd z, int L1, zd *f) {
 
 OM_HD void sph_h1(zd z, int L1, zd *f) {
   zd e = cexp_i(z);
-  f[0] = mk(e.im, -e.re) / z;  // -i e / z
+  const zd rz = 1.0 / z;
+  f[0] = mk(e.im, -e.re) * rz;  // -i e / z
   if(L1 == 0)
     return;
-  f[1] = -(e * (z + mk(0.0, 1.0))) / (z * z);
+  f[1] = -(e * (z + mk(0.0, 1.0))) * (rz * rz);
   for(int n = 1; n < L1; ++n)
-    f[n + 1] = (double(2 * n + 1) / z) * f[n] - f[n - 1];
+    f[n + 1] = double(2 * n + 1) * (rz * f[n]) - f[n - 1];
 }
 
 // Values and derivatives for orders 0..L the way OPTIMET's bessel<> wrapper

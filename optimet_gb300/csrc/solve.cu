@@ -89,6 +89,66 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld,
   part[blockIdx.y * n + i] = acc0;
 }
 
+// Complex64 matrix times a complex128 vector with FP64-accurate results from
+// FP32 arithmetic (the precision form's refinement residuals): x is split as
+// x_hi + x_lo (floats); the products s * x_hi are made error-free with FMA
+// (TwoProduct) and summed in a float-float accumulator (TwoSum, Knuth); the
+// small terms (product errors and s * x_lo) go to a separate float sum. Each
+// CTA sums kMvCols columns, so the per-thread sums are short; partials are
+// combined in FP64.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ void df_add(DF &a, float p) {
+  const float s = a.hi + p;
+  const float bb = s - a.hi;
+  a.lo += (a.hi - (s - bb)) + (p - bb);
+  a.hi = s;
+}
+__global__ void __launch_bounds__(kMvThreads) k_matvec_part_df(const float2 *S, long ld, long n,
+                                                               const double2 *x, double2 *part) {
+  __shared__ float4 xs[kMvCols];
+  const long i = blockIdx.x * (long)kMvThreads + threadIdx.x;
+  const long j0 = blockIdx.y * (long)kMvCols;
+  const long j1 = min(n, j0 + kMvCols);
+  for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads) {
+    const double2 v = x[j];
+    const float hr = (float)v.x, hi = (float)v.y;
+    xs[j - j0] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+  }
+  __syncthreads();
+  if(i >= n)
+    return;
+  DF re{0.f, 0.f}, im{0.f, 0.f};
+  float er = 0.f, ei = 0.f;
+  const float2 *col = S + j0 * ld + i;
+  for(long j = j0; j < j1; ++j) {
+    const float2 a = *col;
+    const float4 v = xs[j - j0];
+    col += ld;
+    // __fmul_rn keeps the products out of FMA contraction so that the
+    // TwoProduct error terms below are exact
+    float p = __fmul_rn(a.x, v.x);
+    er += fmaf(a.x, v.x, -p);
+    df_add(re, p);
+    p = __fmul_rn(-a.y, v.y);
+    er += fmaf(-a.y, v.y, -p);
+    df_add(re, p);
+    er = fmaf(a.x, v.z, er);
+    er = fmaf(-a.y, v.w, er);
+    p = __fmul_rn(a.x, v.y);
+    ei += fmaf(a.x, v.y, -p);
+    df_add(im, p);
+    p = __fmul_rn(a.y, v.x);
+    ei += fmaf(a.y, v.x, -p);
+    df_add(im, p);
+    ei = fmaf(a.x, v.w, ei);
+    ei = fmaf(a.y, v.z, ei);
+  }
+  part[blockIdx.y * n + i] =
+      make_double2((double)re.hi + ((double)re.lo + (double)er), (double)im.hi + ((double)im.lo + (double)ei));
+}
+
 // y = sum of partials (fixed order); if b given: y = b - sum.
 template <typename V>
 __global__ void k_matvec_reduce(const V *part, int nsplit, long n, const V *b, V *y) {
@@ -238,9 +298,14 @@ template <typename M, typename V>
 void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, const V *b) {
   const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
   dim3 grid((unsigned)((n + kMvThreads - 1) / kMvThreads), (unsigned)nsplit);
-  auto &ev = sizeof(M) == sizeof(double2) ? ctx->ev_mv64 : ctx->ev_mv32;
+  constexpr bool df = sizeof(M) == sizeof(float2) && sizeof(V) == sizeof(double2);
+  auto &ev = sizeof(M) == sizeof(double2) ? ctx->ev_mv64 : (df ? ctx->ev_mvdf : ctx->ev_mv32);
   timer_begin(ctx, ev);
-  k_matvec_part<M, V><<<grid, kMvThreads, 0, ctx->stream>>>(S, n, n, x, part);
+  if constexpr(df)
+    k_matvec_part_df<<<grid, kMvThreads, 0, ctx->stream>>>((const float2 *)S, n, n,
+                                                           (const double2 *)x, (double2 *)part);
+  else
+    k_matvec_part<M, V><<<grid, kMvThreads, 0, ctx->stream>>>(S, n, n, x, part);
   timer_end(ctx, ev);
   k_matvec_reduce<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(part, nsplit, n, b, y);
   ctx->last_launches += 2;
@@ -351,9 +416,15 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
   double err = 1.0;
   int total = 0;
   for(int rest = 0; rest < restarts && err > tol; ++rest) {
-    // r = b - S x
-    matvec<M, double2>(ctx, S, n, x, part, r, b);
-    double beta = vec_norm(ctx, r, n, part, hd);
+    // r = b - S x (x = 0 on the first cycle)
+    double beta;
+    if(rest == 0) {
+      cudaMemcpyAsync(r, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+      beta = bnorm;
+    } else {
+      matvec<M, double2>(ctx, S, n, x, part, r, b);
+      beta = vec_norm(ctx, r, n, part, hd);
+    }
     if(beta == 0.0) {
       err = 0.0;
       break;
@@ -840,9 +911,13 @@ int solve_gmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, con
   om_context *ctx = pr->ctx;
   int it = 0;
   double rr = 0;
-  // the complex128 matrix is always present (the precision form keeps both copies)
-  int rc = gmres64<double2>(ctx, (const double2 *)pr->d_S[harmonic], pr->n, b, x, o->tol,
-                            o->max_iter, o->restarts, nullptr, &it, &rr);
+  int rc;
+  if(pr->S_prec[harmonic] == OM_C128)
+    rc = gmres64<double2>(ctx, (const double2 *)pr->d_S[harmonic], pr->n, b, x, o->tol,
+                          o->max_iter, o->restarts, nullptr, &it, &rr);
+  else  // FP64 GMRES on the complex64 system
+    rc = gmres64<float2>(ctx, (const float2 *)pr->d_S32[harmonic], pr->n, b, x, o->tol,
+                         o->max_iter, o->restarts, nullptr, &it, &rr);
   if(st) {
     st->iterations = it;
     st->inner_iterations = 0;
@@ -853,12 +928,13 @@ int solve_gmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, con
   return rc;
 }
 
-// Precision form: FP64 outer FGMRES on the FP64 matrix (residuals), FP32
-// inner GMRES on the complex64 matrix (stored in d_S of the same harmonic's
-// mixed slot).
-int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const float2 *S32,
-                     const double2 *b, double2 *x, om_solve_stats *st) {
+// Precision form: FP64 outer FGMRES whose residuals use the complex64 matrix
+// in FP64 arithmetic, with a fixed-length FP32 GMRES on the same matrix as the
+// flexible preconditioner.
+int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
+                     double2 *x, om_solve_stats *st) {
   om_context *ctx = pr->ctx;
+  const float2 *S32 = (const float2 *)pr->d_S32[harmonic];
   InnerGmres32 inner(ctx, S32, pr->n, std::max(1, o->inner_iter), o->inner_tol);
   int rc = inner.init();
   if(rc)
@@ -866,8 +942,7 @@ int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, co
   int it = 0;
   double rr = 0;
   const int outer_m = std::max(1, std::min(o->max_iter, 32));
-  rc = gmres64<double2>(ctx, (const double2 *)pr->d_S[harmonic], pr->n, b, x, o->tol, outer_m,
-                        o->restarts, &inner, &it, &rr);
+  rc = gmres64<float2>(ctx, S32, pr->n, b, x, o->tol, outer_m, o->restarts, &inner, &it, &rr);
   if(st) {
     st->iterations = it;
     st->inner_iterations = inner.total;
@@ -875,6 +950,69 @@ int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, co
   }
   if(rc == OM_ERR_NOT_CONVERGED)
     ctx->err = "FGMRES did not reach the requested tolerance";
+  return rc;
+}
+
+// FP32 LU of the complex64 matrix used as the preconditioner of FP64 outer
+// FGMRES (GMRES-based iterative refinement, Carson & Higham 2018): the
+// mixed-precision LU refinement role.
+struct LuPrecond32 : PrecondFn {
+  om_context *ctx;
+  long n;
+  Work w;
+  float2 *A = nullptr, *v32 = nullptr;
+  int *piv = nullptr, *info = nullptr;
+  int applied = 0;
+  LuPrecond32(om_context *c, long n_) : ctx(c), n(n_) { w.ctx = c; }
+  int init(const float2 *S32) {
+    size_t bytes = sizeof(float2) * ((size_t)n * n + n) + sizeof(int) * (n + 1) + 1024;
+    int rc = alloc_work(ctx, w, bytes);
+    if(rc)
+      return rc;
+    size_t off = 0;
+    A = w.take<float2>((size_t)n * n, off);
+    v32 = w.take<float2>(n, off);
+    piv = w.take<int>(n, off);
+    info = w.take<int>(1, off);
+    cudaMemcpyAsync(A, S32, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    lu_factor<float2>(ctx, A, n, piv, info);
+    int hinfo = 0;
+    cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    if(hinfo) {
+      ctx->err = "singular complex64 matrix: zero pivot at column " + std::to_string(hinfo);
+      return OM_ERR_SINGULAR;
+    }
+    return OM_OK;
+  }
+  void apply(const double2 *v, double2 *z) override {
+    k_scale_copy<double2, float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v, 1.0, v32, n);
+    lu_solve_vec<float2>(ctx, A, n, piv, v32);
+    k_scale_copy<float2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v32, 1.0, z, n);
+    ctx->last_launches += 2;
+    ++applied;
+  }
+};
+
+int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
+                       double2 *x, om_solve_stats *st) {
+  om_context *ctx = pr->ctx;
+  const float2 *S32 = (const float2 *)pr->d_S32[harmonic];
+  LuPrecond32 lu(ctx, pr->n);
+  int rc = lu.init(S32);
+  if(rc)
+    return rc;
+  int it = 0;
+  double rr = 0;
+  const int outer_m = std::max(1, std::min(o->max_iter, 32));
+  rc = gmres64<float2>(ctx, S32, pr->n, b, x, o->tol, outer_m, o->restarts, &lu, &it, &rr);
+  if(st) {
+    st->iterations = it;
+    st->inner_iterations = lu.applied;
+    st->rel_residual = rr;
+  }
+  if(rc == OM_ERR_NOT_CONVERGED)
+    ctx->err = "LU-preconditioned refinement did not reach the requested tolerance";
   return rc;
 }
 

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
+#include <type_traits>
 
 #include "om_internal.h"
 
@@ -57,13 +58,15 @@ enum { kAP = 0, kAM = 1, kBP = 2, kBM = 3, kRAP = 4, kRBP = 5, kRecStride = 6 };
 // Shared-memory layout of a translation CTA (offsets in doubles).
 struct Layout {
   int nmax, P, L, Lc, W;
-  int rec, qf, pf, leg, geo, zb, seed, tl, tab;
+  int rec, qf, pf, leg, legc, eph, geo, zb, seed, tl, qf32, pf32, tl32, tab;
   int rows_cap;
+  int tab_elem;  // bytes per table entry: 16 (complex128) or 8 (complex64, precision form)
   size_t bytes;
 };
 
-Layout make_layout(int nmax, size_t smem_limit) {
+Layout make_layout(int nmax, size_t smem_limit, bool mixed = false) {
   Layout y;
+  y.tab_elem = mixed ? 8 : 16;
   y.nmax = nmax;
   y.P = pmax(nmax);
   y.L = 2 * nmax;
@@ -79,13 +82,18 @@ Layout make_layout(int nmax, size_t smem_limit) {
   y.qf = take(kQfacStride * y.P);
   y.pf = take(kPfacStride * y.P);
   y.leg = take((y.L + 1) * (y.L + 2) / 2);
+  y.legc = take((y.L + 1) * (y.L + 2));
+  y.eph = take(2 * (y.L + 1));
   y.geo = take(8);
   y.zb = take(2 * 2 * (y.L + 1));
   y.seed = take(2 * 2 * (y.L + 1) * (y.L + 1));
   y.tl = take(2 * 2 * (nmax + 1));
+  y.qf32 = mixed ? take((kQfacStride * y.P + 1) / 2) : o;
+  y.pf32 = mixed ? take((kPfacStride * y.P + 1) / 2) : o;
+  y.tl32 = mixed ? take(2 * (nmax + 1)) : o;
   y.tab = o;
   size_t fixed = size_t(o) * sizeof(double);
-  size_t row_bytes = size_t(y.W) * sizeof(zd);
+  size_t row_bytes = size_t(y.W) * y.tab_elem;
   size_t avail = smem_limit > fixed ? smem_limit - fixed : 0;
   int cap = (int)std::min<size_t>(avail / row_bytes, (size_t)y.P);
   y.rows_cap = cap;
@@ -111,8 +119,10 @@ std::vector<std::pair<int, int>> make_chunks(const Layout &y) {
 }
 
 struct Smem {
-  double *rec, *qf, *pf, *leg, *geo;
-  zd *zb, *seed, *tl, *tab;
+  double *rec, *qf, *pf, *leg, *legc, *geo;
+  zd *eph, *zb, *seed, *tl, *tab;
+  float *qf32, *pf32;
+  float2 *tl32;
 };
 
 __device__ Smem smem_view(double *base, const Layout &y) {
@@ -121,7 +131,12 @@ __device__ Smem smem_view(double *base, const Layout &y) {
   s.qf = base + y.qf;
   s.pf = base + y.pf;
   s.leg = base + y.leg;
+  s.legc = base + y.legc;
+  s.eph = reinterpret_cast<zd *>(base + y.eph);
   s.geo = base + y.geo;
+  s.qf32 = reinterpret_cast<float *>(base + y.qf32);
+  s.pf32 = reinterpret_cast<float *>(base + y.pf32);
+  s.tl32 = reinterpret_cast<float2 *>(base + y.tl32);
   s.zb = reinterpret_cast<zd *>(base + y.zb);
   s.seed = reinterpret_cast<zd *>(base + y.seed);
   s.tl = reinterpret_cast<zd *>(base + y.tl);
@@ -144,10 +159,12 @@ __device__ __forceinline__ zd shfl_down1(zd v) {
 
 // Copy the geometry-independent tables into shared memory.
 __device__ void load_tables(const Smem &s, const Layout &y, const double *rec, const double *qf,
-                            const double *pf) {
+                            const double *pf, const double *legc) {
   int nrec = kRecStride * (y.Lc + 1) * (y.Lc + 1);
   for(int i = threadIdx.x; i < nrec; i += blockDim.x)
     s.rec[i] = rec[i];
+  for(int i = threadIdx.x; i < (y.L + 1) * (y.L + 2); i += blockDim.x)
+    s.legc[i] = legc[i];
   for(int i = threadIdx.x; i < kQfacStride * y.P; i += blockDim.x)
     s.qf[i] = qf[i];
   for(int i = threadIdx.x; i < kPfacStride * y.P; i += blockDim.x)
@@ -170,30 +187,37 @@ __device__ void make_seeds(const Smem &s, const Layout &y, zd waveK, int hankel)
       dst[l] = f[l];
   }
   if(t >= 64 && t < 64 + L + 1) {
-    // normalised associated Legendre functions with the Condon-Shortley phase
+    // normalised associated Legendre functions with the Condon-Shortley phase;
+    // legc holds, at l(l+1)/2 + k: {P_kk / sin^k, sqrt(2k+3)} for l = k and
+    // {a_lk, b_lk} of the three-term recurrence for l >= k + 2 (host-computed)
     const int k = t - 64;
     const double x = cos(th), st = sin(th);
-    double v = 1.0 / sqrt(4.0 * kPi);
+    double v = s.legc[2 * (k * (k + 1) / 2 + k)];
     for(int i = 1; i <= k; ++i)
-      v *= -sqrt(double(2 * i + 1) / double(2 * i)) * st;
+      v *= st;
     s.leg[k * (k + 1) / 2 + k] = v;
     if(k + 1 <= L) {
-      double v0 = v, v1 = sqrt(double(2 * k + 3)) * x * v;
+      double v0 = v, v1 = s.legc[2 * (k * (k + 1) / 2 + k) + 1] * x * v;
       s.leg[(k + 1) * (k + 2) / 2 + k] = v1;
       for(int l = k + 2; l <= L; ++l) {
-        double a = sqrt(double(4 * l * l - 1) / double(l * l - k * k));
-        double b = sqrt(double((l - 1) * (l - 1) - k * k) / double(4 * (l - 1) * (l - 1) - 1));
-        double v2 = a * (x * v1 - b * v0);
+        const double a = s.legc[2 * (l * (l + 1) / 2 + k)];
+        const double b = s.legc[2 * (l * (l + 1) / 2 + k) + 1];
+        double v2 = a * fma(x, v1, -b * v0);
         s.leg[l * (l + 1) / 2 + k] = v2;
         v0 = v1;
         v1 = v2;
       }
     }
   }
+  if(t >= 128 && t < 128 + L + 1) {
+    double sn, cs;
+    sincos((t - 128) * ph, &sn, &cs);
+    s.eph[t - 128] = mk(cs, sn);
+  }
   __syncthreads();
   const double s4pi = sqrt(4e0 * kPi);
   for(int idx = t; idx < (L + 1) * (L + 1); idx += blockDim.x) {
-    int l = (int)sqrt((double)idx);
+    int l = (int)sqrtf((float)idx);
     while(l * l > idx)
       --l;
     while((l + 1) * (l + 1) <= idx)
@@ -207,9 +231,8 @@ __device__ void make_seeds(const Smem &s, const Layout &y, zd waveK, int hankel)
     }
     int am = k < 0 ? -k : k;  // |mu| with mu = -k
     double pre = s.leg[l * (l + 1) / 2 + am];
-    double sn, cs;
-    sincos(am * ph, &sn, &cs);
-    double re = pre * cs, im = pre * sn;
+    const zd e = s.eph[am];
+    double re = pre * e.re, im = pre * e.im;
     if(k > 0) {  // mu = -k < 0: Y_l^{-|m|} = (-1)^|m| conj(Y_l^{|m|})
       if(am & 1)
         re = -re;
@@ -224,49 +247,95 @@ __device__ void make_seeds(const Smem &s, const Layout &y, zd waveK, int hankel)
   __syncthreads();
 }
 
+template <typename T> struct Tab;
+template <> struct Tab<zd> {
+  static __device__ __forceinline__ zd get(const zd *t, int i) { return t[i]; }
+  static __device__ __forceinline__ void put(zd *t, int i, zd v) { t[i] = v; }
+};
+template <> struct Tab<float2> {
+  static __device__ __forceinline__ float2 get(const float2 *t, int i) { return t[i]; }
+  static __device__ __forceinline__ void put(float2 *t, int i, zd v) {
+    t[i] = make_float2((float)v.re, (float)v.im);
+  }
+};
+
+template <int W> __device__ __forceinline__ zd shfl_up_w(zd v) {
+  return mk(__shfl_up_sync(0xffffffffu, v.re, 1, W), __shfl_up_sync(0xffffffffu, v.im, 1, W));
+}
+template <int W> __device__ __forceinline__ zd shfl_down_w(zd v) {
+  return mk(__shfl_down_sync(0xffffffffu, v.re, 1, W), __shfl_down_sync(0xffffffffu, v.im, 1, W));
+}
+
 // The recurrence chains; stores alpha(n, m, l, k) for n in [n_lo, n_hi], l <= nMax.
 // For a real wave number the conjugate-wave chains (TranslationAdditionCoefficients.h:72-74)
 // follow from the positive ones: regular: alpha_neg = alpha_pos; irregular (Hankel
 // h_l(-x) = (-1)^l conj(h_l(x))): alpha_neg(n,m,l,k) = (-1)^{n+l} e^{2 i d phi}
 // conj(alpha_pos(n,m,l,k)), d = m - k (the recurrence keeps n + l parity and d);
 // only the positive chains then run.
-__device__ void run_chains(const Smem &s, const Layout &y, int hankel, bool real_k, int n_lo,
-                           int n_hi) {
+//
+// kW = 32: one warp per chain, lane = l <= 2 nMax.
+// kW = 16 (nMax <= 8): two chains per warp, lane & 15 = l. Level n >= 1 only
+// needs l <= 2 nMax - 1 <= 15; the level-0 neighbours (l up to 16) are read
+// from the seed table. Both halves run the same (warp-uniform) loop bounds and
+// predicate their stores.
+template <int kW, typename TabT>
+__device__ void run_chains(const Smem &s, TabT *tab, const Layout &y, int hankel, bool real_k,
+                           int n_lo, int n_hi) {
   const int nmax = y.nmax, L = y.L, Lc = y.Lc, W = y.W;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int sub = threadIdx.x / kW, nsub = blockDim.x / kW;
+  const int l = threadIdx.x & (kW - 1);
   const int npos = 3 * nmax + 1, nneg = real_k ? 0 : 3 * nmax;
+  const int nchains = npos + nneg;
   const int base = n_lo * n_lo - 1;  // flat(n_lo, n_lo)
-  const int l = lane;
   const double phi = s.geo[2];
-  for(int c = warp; c < npos + nneg; c += nwarps) {
-    const bool neg = c >= npos;
-    const int d = neg ? (c - npos) + 1 - nmax : c - nmax;
+  // chains ordered d = 2 nMax .. -nMax (positive), then the conjugate-wave ones,
+  // so that neighbouring chains (paired in a warp) have equal loop lengths
+  const int rounds = (nchains + nsub - 1) / nsub;
+  for(int r = 0; r < rounds; ++r) {
+    const int c = sub + r * nsub;
+    const bool active = c < nchains;
+    const bool neg = active && c >= npos;
+    const int d = !active ? 0 : (neg ? 2 * nmax - (c - npos) : 2 * nmax - c);
     const zd *seed = s.seed + (neg ? (L + 1) * (L + 1) : 0);
-    // e^{-2 i d phi}: maps a positive-chain value to its negative-m image
+    auto seed_at = [&](int ll) {
+      return (active && ll >= 0 && ll <= L && (d < 0 ? -d : d) <= ll) ? seed[ll * ll + ll - d]
+                                                                      : mk(0.0, 0.0);
+    };
     double e2s, e2c;
     sincos(-2.0 * d * phi, &e2s, &e2c);
     const zd e2 = mk(e2c, e2s);
-    zd D = mk(0.0, 0.0);
-    if(l <= L && (d < 0 ? -d : d) <= l)
-      D = seed[l * l + l - d];
-    const int mu_end = min(min(nmax, d + nmax), n_hi);
-    for(int mu = 0; mu <= mu_end; ++mu) {
+    zd D = seed_at(l);
+    const int mu_end = active ? min(min(nmax, d + nmax), n_hi) : -1;
+    int mu_end_w = mu_end;
+    if(kW == 16)
+      mu_end_w = max(mu_end, __shfl_xor_sync(0xffffffffu, mu_end, 16));
+    for(int mu = 0; mu <= mu_end_w; ++mu) {
       const int kap = mu - d;
+      const bool live = mu <= mu_end;
       if(mu > 0) {
-        zd Dm = shfl_up1(D), Dp = shfl_down1(D);
-        double bp = rcoef(s, Lc, l - 1, kap - 1, kBP);
-        double bm = rcoef(s, Lc, l + 1, kap - 1, kBM);
-        double rden = rcoef(s, Lc, mu - 1, mu - 1, kRBP);
-        zd Dn = (Dm * bp + Dp * bm) * rden;
+        zd Dm, Dp;
+        if(kW == 16 && mu == 1) {
+          Dm = seed_at(l - 1);
+          Dp = seed_at(l + 1);
+        } else {
+          Dm = shfl_up_w<kW>(D);
+          Dp = shfl_down_w<kW>(D);
+        }
+        const double bp = rcoef(s, Lc, l - 1, kap - 1, kBP);
+        const double bm = rcoef(s, Lc, l + 1, kap - 1, kBM);
+        const double rden = rcoef(s, Lc, mu - 1, mu - 1, kRBP);
+        zd Dn;
+        Dn.re = fma(Dm.re, bp, Dp.re * bm) * rden;
+        Dn.im = fma(Dm.im, bp, Dp.im * bm) * rden;
         D = (l <= L) ? Dn : mk(0.0, 0.0);
       }
       // store alpha(n, mu, l, kap) and, from the positive chains of a real
       // wave number, the negative-m image (n, -mu, l, -kap)
       auto store = [&](int n, zd v) {
-        if(n < n_lo || n > n_hi || l > nmax || kap > l || kap < -l)
+        if(!live || n < n_lo || n > n_hi || l > nmax || kap > l || kap < -l)
           return;
         if(!neg)
-          s.tab[(flat(n, mu) - base) * W + l * (l + 1) - kap] = v;
+          Tab<TabT>::put(tab, (flat(n, mu) - base) * W + l * (l + 1) - kap, v);
         if(mu == 0 || (!neg && !real_k))
           return;
         const int m = -mu, k = -kap;
@@ -283,17 +352,26 @@ __device__ void run_chains(const Smem &s, const Layout &y, int hankel, bool real
         const int sign = hankel ? (n + m + l + k) : (k + m);
         if(sign & 1)
           w = -w;
-        s.tab[(flat(n, m) - base) * W + l * (l + 1) - k] = w;
+        Tab<TabT>::put(tab, (flat(n, m) - base) * W + l * (l + 1) - k, w);
       };
       store(mu, D);
       zd O2 = mk(0.0, 0.0), O1 = D;
       const double apl = rcoef(s, Lc, l - 1, kap, kAP);
       const double aml = rcoef(s, Lc, l + 1, kap, kAM);
       for(int n = mu + 1; n <= n_hi; ++n) {
-        zd Om = shfl_up1(O1), Op = shfl_down1(O1);
-        double amn = rcoef(s, Lc, n - 1, mu, kAM);
-        double rapn = rcoef(s, Lc, n - 1, mu, kRAP);
-        zd O = (-(O2 * amn) + Om * apl + Op * aml) * rapn;
+        zd Om, Op;
+        if(kW == 16 && n == 1) {
+          Om = seed_at(l - 1);
+          Op = seed_at(l + 1);
+        } else {
+          Om = shfl_up_w<kW>(O1);
+          Op = shfl_down_w<kW>(O1);
+        }
+        const double amn = rcoef(s, Lc, n - 1, mu, kAM);
+        const double rapn = rcoef(s, Lc, n - 1, mu, kRAP);
+        zd O;
+        O.re = fma(Om.re, apl, fma(Op.re, aml, -O2.re * amn)) * rapn;
+        O.im = fma(Om.im, apl, fma(Op.im, aml, -O2.im * amn)) * rapn;
         if(l > L)
           O = mk(0.0, 0.0);
         O2 = O1;
@@ -304,34 +382,84 @@ __device__ void run_chains(const Smem &s, const Layout &y, int hankel, bool real
   }
 }
 
+template <typename TabT>
+__device__ void chains(const Smem &s, TabT *tab, const Layout &y, int hankel, bool real_k,
+                       int n_lo, int n_hi) {
+  if(y.nmax <= 8)
+    run_chains<16, TabT>(s, tab, y, hankel, real_k, n_lo, n_hi);
+  else
+    run_chains<32, TabT>(s, tab, y, hankel, real_k, n_lo, n_hi);
+}
+
 // A(q, p) and B(q, p) of Coupling.cpp:30-51 for q = (n, m) in the table chunk
-// starting at flat index `base`, p = (l, k).
-__device__ __forceinline__ void coupling_entry(const Smem &s, const Layout &y, int base, int q, int p,
-                                               zd &A, zd &B) {
-  const double *qf = s.qf + q * kQfacStride;
-  const double *pf = s.pf + p * kPfacStride;
+// starting at flat index `base`, p = (l, k). The reference's coefficient
+// products c_i * factor are split into a row factor (qf) and a column factor (pf).
+template <typename R> struct CT {
+  R re, im;
+};
+template <typename R> __device__ __forceinline__ CT<R> ld(const zd *t, int i) {
+  return CT<R>{(R)t[i].re, (R)t[i].im};
+}
+template <typename R> __device__ __forceinline__ CT<R> ld(const float2 *t, int i) {
+  return CT<R>{(R)t[i].x, (R)t[i].y};
+}
+
+template <typename R> struct Fac;
+template <> struct Fac<double> {
+  static __device__ __forceinline__ const double *q(const Smem &s) { return s.qf; }
+  static __device__ __forceinline__ const double *p(const Smem &s) { return s.pf; }
+};
+template <> struct Fac<float> {
+  static __device__ __forceinline__ const float *q(const Smem &s) { return s.qf32; }
+  static __device__ __forceinline__ const float *p(const Smem &s) { return s.pf32; }
+};
+
+template <typename R, typename TabT>
+__device__ __forceinline__ void coupling_entry(const Smem &s, const TabT *tab, const Layout &y,
+                                               int base, int q, int p, CT<R> &A, CT<R> &B) {
+  const R *qf = Fac<R>::q(s) + q * kQfacStride;
+  const R *pf = Fac<R>::p(s) + p * kPfacStride;
   const int n = (int)qf[3], m = (int)qf[4], l = (int)pf[6], k = (int)pf[7];
   const int W = y.W;
-  const zd *row = s.tab + (q - base) * W;
-  const zd zero = mk(0.0, 0.0);
-  const int c0 = l * (l + 1) - k;
-  zd t0 = row[c0];
-  zd tp = (m < n && k < l) ? row[c0 - 1 - W] : zero;
-  zd tm = (m > -n && k > -l) ? row[c0 + 1 + W] : zero;
-  A = (qf[2] * pf[2]) * t0 + (qf[0] * pf[0]) * tp + (qf[1] * pf[1]) * tm;
-  const int c1 = (l - 1) * l - k;
+  const int row = (q - base) * W;
+  const R z = 0;
+  const int c0 = row + l * (l + 1) - k;
+  const CT<R> t0 = ld<R>(tab, c0);
+  const CT<R> tp = (m < n && k < l) ? ld<R>(tab, c0 - 1 - W) : CT<R>{z, z};
+  const CT<R> tm = (m > -n && k > -l) ? ld<R>(tab, c0 + 1 + W) : CT<R>{z, z};
+  const R f0 = qf[2] * pf[2], f1 = qf[0] * pf[0], f2 = qf[1] * pf[1];
+  A.re = fma(f0, t0.re, fma(f1, tp.re, f2 * tm.re));
+  A.im = fma(f0, t0.im, fma(f1, tp.im, f2 * tm.im));
+  const int c1 = row + (l - 1) * l - k;
   const int lm = l - 1;
-  zd u0 = (k <= lm && k >= -lm) ? row[c1] : zero;
-  zd up = (m < n && k + 1 <= lm && k + 1 >= -lm) ? row[c1 - 1 - W] : zero;
-  zd um = (m > -n && k - 1 >= -lm && k - 1 <= lm) ? row[c1 + 1 + W] : zero;
-  zd sm = (qf[2] * pf[3]) * u0 + (qf[0] * pf[4]) * up - (qf[1] * pf[5]) * um;
-  B = mk(sm.im, -sm.re);  // -i * sm
+  const CT<R> u0 = (k <= lm && k >= -lm) ? ld<R>(tab, c1) : CT<R>{z, z};
+  const CT<R> up = (m < n && k + 1 <= lm && k + 1 >= -lm) ? ld<R>(tab, c1 - 1 - W) : CT<R>{z, z};
+  const CT<R> um = (m > -n && k - 1 >= -lm && k - 1 <= lm) ? ld<R>(tab, c1 + 1 + W) : CT<R>{z, z};
+  const R g0 = qf[2] * pf[3], g1 = qf[0] * pf[4], g2 = qf[1] * pf[5];
+  const R sre = fma(g0, u0.re, fma(g1, up.re, -g2 * um.re));
+  const R sim = fma(g0, u0.im, fma(g1, up.im, -g2 * um.im));
+  B.re = sim;  // -i * s
+  B.im = -sre;
+}
+
+// zd-typed wrapper used by the source and coupling kernels (FP64 table)
+__device__ __forceinline__ void coupling_entry(const Smem &s, const Layout &y, int base, int q, int p,
+                                               zd &A, zd &B) {
+  CT<double> a, b;
+  coupling_entry<double, zd>(s, s.tab, y, base, q, p, a, b);
+  A = mk(a.re, a.im);
+  B = mk(b.re, b.im);
+}
+
+// -(t * v) for the T-matrix row scaling
+template <typename R> __device__ __forceinline__ CT<R> neg_mul(CT<R> t, CT<R> v) {
+  return CT<R>{fma(-t.re, v.re, t.im * v.im), fma(-t.re, v.im, -(t.im * v.re))};
 }
 
 struct AssembleArgs {
   const double *cart;
   const zd *T;  // N x (nmax+1) x 2
-  const double *rec, *qf, *pf;
+  const double *rec, *qf, *pf, *legc;
   int N;
   zd waveK;
   long ld;
@@ -339,16 +467,24 @@ struct AssembleArgs {
   int2 chunks[kMaxNmax];
 };
 
-__device__ __forceinline__ void put2(double2 *S64, float2 *S32, size_t at, zd v) {
-  S64[at] = make_double2(v.re, v.im);
-  if(S32)
-    S32[at] = make_float2((float)v.re, (float)v.im);
+template <typename O> __device__ __forceinline__ void put_out(O *S, size_t at, double re, double im);
+template <> __device__ __forceinline__ void put_out<double2>(double2 *S, size_t at, double re, double im) {
+  S[at] = make_double2(re, im);
+}
+template <> __device__ __forceinline__ void put_out<float2>(float2 *S, size_t at, double re, double im) {
+  S[at] = make_float2((float)re, (float)im);
 }
 
-// S64 always receives the complex128 block; S32 (precision form) the same
-// values rounded to complex64 from the same FP64 arithmetic.
-__global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y, double2 *S64,
-                                                  float2 *S32) {
+// kMixed = false: complex128 table, FP64 block forming, complex128 S.
+// kMixed = true (precision form): the recurrences still run in FP64; their
+// results are rounded into a complex64 table and the blocks are formed in FP32
+// straight into the complex64 S.
+template <bool kMixed>
+__global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
+                                                  typename std::conditional<kMixed, float2, double2>::type *S) {
+  typedef typename std::conditional<kMixed, float2, double2>::type OutT;
+  typedef typename std::conditional<kMixed, float2, zd>::type TabT;
+  typedef typename std::conditional<kMixed, float, double>::type R;
   extern __shared__ double smem[];
   const int b = blockIdx.x;
   const int j = b / a.N, i = b - j * a.N;
@@ -357,14 +493,25 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y, doub
   if(i == j) {
     for(int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) {
       int c = idx / (2 * P), r = idx - c * 2 * P;
-      put2(S64, S32, (y0 + c) * a.ld + x0 + r, mk(r == c ? 1.0 : 0.0, 0.0));
+      put_out<OutT>(S, (y0 + c) * a.ld + x0 + r, r == c ? 1.0 : 0.0, 0.0);
     }
     return;
   }
   Smem s = smem_view(smem, y);
-  load_tables(s, y, a.rec, a.qf, a.pf);
+  TabT *tab = reinterpret_cast<TabT *>(s.tab);
+  load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
   for(int t = threadIdx.x; t < 2 * (y.nmax + 1); t += blockDim.x)
     s.tl[t] = a.T[(size_t)i * 2 * (y.nmax + 1) + t];
+  if(kMixed) {
+    for(int t = threadIdx.x; t < kQfacStride * y.P; t += blockDim.x)
+      s.qf32[t] = (float)a.qf[t];
+    for(int t = threadIdx.x; t < kPfacStride * y.P; t += blockDim.x)
+      s.pf32[t] = (float)a.pf[t];
+    for(int t = threadIdx.x; t < 2 * (y.nmax + 1); t += blockDim.x) {
+      const zd v = a.T[(size_t)i * 2 * (y.nmax + 1) + t];
+      s.tl32[t] = make_float2((float)v.re, (float)v.im);
+    }
+  }
   if(threadIdx.x == 0) {
     double dx = a.cart[3 * i] - a.cart[3 * j], dy = a.cart[3 * i + 1] - a.cart[3 * j + 1],
            dz = a.cart[3 * i + 2] - a.cart[3 * j + 2];
@@ -374,21 +521,32 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y, doub
   make_seeds(s, y, a.waveK, 1);
   for(int c = 0; c < a.nchunks; ++c) {
     const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
-    run_chains(s, y, 1, a.waveK.im == 0.0, n_lo, n_hi);
+    chains<TabT>(s, tab, y, 1, a.waveK.im == 0.0, n_lo, n_hi);
     __syncthreads();
     const int base = n_lo * n_lo - 1;
     const int rows = (n_hi + 1) * (n_hi + 1) - 1 - base;
     for(int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
       const int qr = idx / P, p = idx - qr * P, q = base + qr;
-      zd A, B;
-      coupling_entry(s, y, base, q, p, A, B);
+      CT<R> A, B;
+      coupling_entry<R, TabT>(s, tab, y, base, q, p, A, B);
       const int l = (int)s.pf[p * kPfacStride + 6];
-      const zd te = s.tl[2 * l], tm = s.tl[2 * l + 1];
+      CT<R> te, tm;
+      if(kMixed) {
+        te = CT<R>{(R)s.tl32[2 * l].x, (R)s.tl32[2 * l].y};
+        tm = CT<R>{(R)s.tl32[2 * l + 1].x, (R)s.tl32[2 * l + 1].y};
+      } else {
+        te = CT<R>{(R)s.tl[2 * l].re, (R)s.tl[2 * l].im};
+        tm = CT<R>{(R)s.tl[2 * l + 1].re, (R)s.tl[2 * l + 1].im};
+      }
       const size_t col_te = (y0 + q) * a.ld + x0, col_tm = (y0 + P + q) * a.ld + x0;
-      put2(S64, S32, col_te + p, -(te * A));
-      put2(S64, S32, col_tm + P + p, -(tm * A));
-      put2(S64, S32, col_tm + p, -(te * B));
-      put2(S64, S32, col_te + P + p, -(tm * B));
+      CT<R> v = neg_mul(te, A);
+      put_out<OutT>(S, col_te + p, v.re, v.im);
+      v = neg_mul(tm, A);
+      put_out<OutT>(S, col_tm + P + p, v.re, v.im);
+      v = neg_mul(te, B);
+      put_out<OutT>(S, col_tm + p, v.re, v.im);
+      v = neg_mul(tm, B);
+      put_out<OutT>(S, col_te + P + p, v.re, v.im);
     }
     __syncthreads();
   }
@@ -398,7 +556,7 @@ struct SourceArgs {
   const double *cart;
   const zd *T;
   const zd *inc;  // 2P
-  const double *rec, *qf, *pf;
+  const double *rec, *qf, *pf, *legc;
   zd waveK;
   zd *incloc, *Q;
   double *wsca;
@@ -413,7 +571,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
   const int i = blockIdx.x;
   const int P = y.P, t = threadIdx.x;
   Smem s = smem_view(smem, y);
-  load_tables(s, y, a.rec, a.qf, a.pf);
+  load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
   for(int u = t; u < 2 * (y.nmax + 1); u += blockDim.x)
     s.tl[u] = a.T[(size_t)i * 2 * (y.nmax + 1) + u];
   if(t == 0)
@@ -433,7 +591,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
     make_seeds(s, y, a.waveK, 0);
     for(int c = 0; c < a.nchunks; ++c) {
       const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
-      run_chains(s, y, 0, a.waveK.im == 0.0, n_lo, n_hi);
+      chains<zd>(s, s.tab, y, 0, a.waveK.im == 0.0, n_lo, n_hi);
       __syncthreads();
       const int base = n_lo * n_lo - 1;
       const int qend = (n_hi + 1) * (n_hi + 1) - 1;
@@ -468,7 +626,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
 
 struct CouplingArgs {
   const double *rel;  // count x 3 Cartesian
-  const double *rec, *qf, *pf;
+  const double *rec, *qf, *pf, *legc;
   zd waveK;
   int hankel;
   zd *A, *B;  // count x P x P
@@ -481,7 +639,7 @@ __global__ void __launch_bounds__(256) k_coupling(CouplingArgs a, Layout y) {
   const int e = blockIdx.x, P = y.P;
   Smem s = smem_view(smem, y);
   zd *A = a.A + (size_t)e * P * P, *B = a.B + (size_t)e * P * P;
-  load_tables(s, y, a.rec, a.qf, a.pf);
+  load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
   if(threadIdx.x == 0)
     to_spherical(a.rel[3 * e], a.rel[3 * e + 1], a.rel[3 * e + 2], &s.geo[0], &s.geo[1],
                  &s.geo[2]);
@@ -496,7 +654,7 @@ __global__ void __launch_bounds__(256) k_coupling(CouplingArgs a, Layout y) {
   make_seeds(s, y, a.waveK, a.hankel);
   for(int c = 0; c < a.nchunks; ++c) {
     const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
-    run_chains(s, y, a.hankel, a.waveK.im == 0.0, n_lo, n_hi);
+    chains<zd>(s, s.tab, y, a.hankel, a.waveK.im == 0.0, n_lo, n_hi);
     __syncthreads();
     const int base = n_lo * n_lo - 1;
     const int rows = (n_hi + 1) * (n_hi + 1) - 1 - base;
@@ -671,6 +829,20 @@ const CoefTables &coef_tables(om_context *ctx, int nmax) {
       pf[kPfacStride * i + 6] = l;
       pf[kPfacStride * i + 7] = k;
     }
+  const int L = 2 * nmax;
+  std::vector<double> legc((L + 1) * (L + 2), 0.0);
+  for(int k = 0; k <= L; ++k) {
+    double c = 1.0 / std::sqrt(4.0 * kPi);
+    for(int i = 1; i <= k; ++i)
+      c *= -std::sqrt(double(2 * i + 1) / double(2 * i));
+    legc[2 * (k * (k + 1) / 2 + k)] = c;
+    legc[2 * (k * (k + 1) / 2 + k) + 1] = std::sqrt(double(2 * k + 3));
+    for(int l = k + 2; l <= L; ++l) {
+      legc[2 * (l * (l + 1) / 2 + k)] = std::sqrt(double(4 * l * l - 1) / double(l * l - k * k));
+      legc[2 * (l * (l + 1) / 2 + k) + 1] =
+          std::sqrt(double((l - 1) * (l - 1) - k * k) / double(4 * (l - 1) * (l - 1) - 1));
+    }
+  }
   auto up = [](const std::vector<double> &v) {
     double *d = nullptr;
     if(cudaMalloc(&d, v.size() * sizeof(double)) != cudaSuccess)
@@ -681,6 +853,7 @@ const CoefTables &coef_tables(om_context *ctx, int nmax) {
   t.rec = up(rec);
   t.qf = up(qf);
   t.pf = up(pf);
+  t.legc = up(legc);
   ctx->tables.push_back(t);
   return ctx->tables.back();
 }
@@ -703,24 +876,29 @@ void launch_incident(om_problem *pr, const double einc[6]) {
 void launch_assemble(om_problem *pr, int harmonic, int precision) {
   om_context *ctx = pr->ctx;
   const CoefTables &ct = coef_tables(ctx, pr->nmax);
-  Layout y = make_layout(pr->nmax, smem_limit());
+  const bool mixed = precision == OM_C64;
+  Layout y = make_layout(pr->nmax, smem_limit(), mixed);
   AssembleArgs a;
   a.cart = pr->d_cart;
   a.T = harmonic == OM_SH ? pr->d_Tsh : pr->d_T;
   a.rec = ct.rec;
   a.qf = ct.qf;
   a.pf = ct.pf;
+  a.legc = ct.legc;
   a.N = pr->N;
   cplx k = harmonic == OM_SH ? 2.0 * pr->waveK : pr->waveK;
   a.waveK = mk(k.real(), k.imag());
   a.ld = pr->n;
   fill_chunks(a, y);
   dim3 grid(pr->N * pr->N);
-  set_smem(k_assemble, y.bytes);
   timer_begin(ctx, ctx->ev_asm);
-  k_assemble<<<grid, 256, y.bytes, ctx->stream>>>(
-      a, y, (double2 *)pr->d_S[harmonic],
-      precision == OM_C64 ? (float2 *)pr->d_S32[harmonic] : nullptr);
+  if(mixed) {
+    set_smem(k_assemble<true>, y.bytes);
+    k_assemble<true><<<grid, 256, y.bytes, ctx->stream>>>(a, y, (float2 *)pr->d_S32[harmonic]);
+  } else {
+    set_smem(k_assemble<false>, y.bytes);
+    k_assemble<false><<<grid, 256, y.bytes, ctx->stream>>>(a, y, (double2 *)pr->d_S[harmonic]);
+  }
   timer_end(ctx, ctx->ev_asm);
   ctx->last_launches++;
 }
@@ -736,6 +914,7 @@ void launch_source(om_problem *pr) {
   a.rec = ct.rec;
   a.qf = ct.qf;
   a.pf = ct.pf;
+  a.legc = ct.legc;
   a.waveK = mk(pr->waveK.real(), pr->waveK.imag());
   a.incloc = pr->d_incloc;
   a.Q = pr->d_Q;
@@ -755,6 +934,7 @@ int launch_coupling(om_context *ctx, const double *d_rel, int count, zd waveK, i
   a.rec = ct.rec;
   a.qf = ct.qf;
   a.pf = ct.pf;
+  a.legc = ct.legc;
   a.waveK = waveK;
   a.hankel = hankel;
   a.A = d_A;

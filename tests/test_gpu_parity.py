@@ -111,22 +111,35 @@ def test_gmres_matches_lu(G, ctx, oracle):
 
 
 def test_mixed_precision_form(G, ctx, oracle):
+    """Precision form: complex64 matrix (FP64 recurrences, FP32 block forming),
+    FP64 outer FGMRES / FP32 inner GMRES, and FP32 LU + FP64 refinement; cross
+    sections within 1e-6 of the plain FP64 form."""
     rng = np.random.default_rng(7)
     xyz, rad = random_cluster(rng, 12, 900 * nm, 40 * nm, 70 * nm, 20 * nm)
     cl = oracle.Cluster(xyz=xyz, radius=rad, eps=(2.0 + 0.05j) ** 2, nmax=5, wavelength=650 * nm,
                         theta=0.3, phi=0.2)
     pr = make(G, ctx, cl)
     pr.source_vector(copy=False)
-    pr.assemble(G.FF, G.C64)
+    pr.assemble(G.FF, G.C128)
+    S64 = pr.matrix()
     pr.solve(G.options(G.SOLVE_GMRES, tol=1e-12))
     ref = pr.cross_sections()
+    pr.assemble(G.FF, G.C64)
+    S32 = pr.matrix()
+    assert rel(S32, S64) < 1e-6
     st = pr.solve(G.options(G.SOLVE_FGMRES_MIXED, tol=1e-10, inner_iter=30, inner_tol=1e-5))
-    assert st.inner_iterations > 0
+    assert st.inner_iterations > 0 and st.rel_residual <= 1e-10
     got = pr.cross_sections()
     assert np.max(np.abs(got - ref) / np.abs(ref)) < 1e-6
-    # the complex64 copy is the FP64 matrix rounded
-    S = pr.matrix()
-    assert S.shape == (pr.n, pr.n)
+    st = pr.solve(G.options(G.SOLVE_LU_MIXED, tol=1e-10))
+    assert st.rel_residual <= 1e-10
+    got_lu = pr.cross_sections()
+    assert np.max(np.abs(got_lu - ref) / np.abs(ref)) < 1e-6
+    # both mixed solvers solve the same complex64 system
+    assert np.max(np.abs(got_lu - got) / np.abs(got)) < 1e-8
+    with pytest.raises(G.OptimetError) as e:
+        pr.solve(G.options(G.SOLVE_LU))
+    assert e.value.code == G.ERR_STATE
 
 
 def test_axial_incidence_matches_oracle(G, ctx, oracle):
