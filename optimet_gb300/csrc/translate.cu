@@ -87,10 +87,10 @@ Layout make_layout(int nmax, size_t smem_limit, bool mixed = false) {
   y.geo = take(8);
   y.zb = take(2 * 2 * (y.L + 1));
   y.seed = take(2 * 2 * (y.L + 1) * (y.L + 1));
-  y.tl = take(2 * 2 * (nmax + 1));
+  y.tl = take(2 * 2 * 2 * (nmax + 1));  // T of both spheres of a pair
   y.qf32 = mixed ? take((kQfacStride * y.P + 1) / 2) : o;
   y.pf32 = mixed ? take((kPfacStride * y.P + 1) / 2) : o;
-  y.tl32 = mixed ? take(2 * (nmax + 1)) : o;
+  y.tl32 = mixed ? take(2 * 2 * (nmax + 1)) : o;
   y.tab = o;
   size_t fixed = size_t(o) * sizeof(double);
   size_t row_bytes = size_t(y.W) * y.tab_elem;
@@ -479,6 +479,12 @@ template <> __device__ __forceinline__ void put_out<float2>(float2 *S, size_t at
 // kMixed = true (precision form): the recurrences still run in FP64; their
 // results are rounded into a complex64 table and the blocks are formed in FP32
 // straight into the complex64 S.
+//
+// One CTA per unordered pair {i, j}, i < j: the table is built for
+// R = r_i - r_j and serves both S_ij and S_ji, because Y_l^m(-R) = (-1)^l Y_l^m(R)
+// and the recurrences keep the parity of n + l, so alpha(n,m,l,k; -R) =
+// (-1)^{n+l} alpha(n,m,l,k; R): A(-R) = (-1)^{n+l} A(R), B(-R) = -(-1)^{n+l} B(R).
+// The last N CTAs write the identity diagonal blocks.
 template <bool kMixed>
 __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
                                                   typename std::conditional<kMixed, float2, double2>::type *S) {
@@ -486,29 +492,39 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
   typedef typename std::conditional<kMixed, float2, zd>::type TabT;
   typedef typename std::conditional<kMixed, float, double>::type R;
   extern __shared__ double smem[];
-  const int b = blockIdx.x;
-  const int j = b / a.N, i = b - j * a.N;
+  const long npairs = (long)a.N * (a.N - 1) / 2;
+  const long b = blockIdx.x;
   const int P = y.P;
-  const long x0 = 2L * P * i, y0 = 2L * P * j;
-  if(i == j) {
+  if(b >= npairs) {
+    const int i = (int)(b - npairs);
+    const long x0 = 2L * P * i;
     for(int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) {
       int c = idx / (2 * P), r = idx - c * 2 * P;
-      put_out<OutT>(S, (y0 + c) * a.ld + x0 + r, r == c ? 1.0 : 0.0, 0.0);
+      put_out<OutT>(S, (x0 + c) * a.ld + x0 + r, r == c ? 1.0 : 0.0, 0.0);
     }
     return;
   }
+  // b -> (i, j), i < j: b = j (j - 1) / 2 + i
+  int j = (int)((1.0 + sqrt(1.0 + 8.0 * (double)b)) * 0.5);
+  while((long)j * (j - 1) / 2 > b)
+    --j;
+  while((long)(j + 1) * j / 2 <= b)
+    ++j;
+  const int i = (int)(b - (long)j * (j - 1) / 2);
+  const long xi = 2L * P * i, xj = 2L * P * j;
   Smem s = smem_view(smem, y);
   TabT *tab = reinterpret_cast<TabT *>(s.tab);
   load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
-  for(int t = threadIdx.x; t < 2 * (y.nmax + 1); t += blockDim.x)
-    s.tl[t] = a.T[(size_t)i * 2 * (y.nmax + 1) + t];
+  const int nT = 2 * (y.nmax + 1);
+  for(int t = threadIdx.x; t < 2 * nT; t += blockDim.x)  // T_i then T_j
+    s.tl[t] = a.T[(size_t)(t < nT ? i : j) * nT + (t < nT ? t : t - nT)];
   if(kMixed) {
     for(int t = threadIdx.x; t < kQfacStride * y.P; t += blockDim.x)
       s.qf32[t] = (float)a.qf[t];
     for(int t = threadIdx.x; t < kPfacStride * y.P; t += blockDim.x)
       s.pf32[t] = (float)a.pf[t];
-    for(int t = threadIdx.x; t < 2 * (y.nmax + 1); t += blockDim.x) {
-      const zd v = a.T[(size_t)i * 2 * (y.nmax + 1) + t];
+    for(int t = threadIdx.x; t < 2 * nT; t += blockDim.x) {
+      const zd v = a.T[(size_t)(t < nT ? i : j) * nT + (t < nT ? t : t - nT)];
       s.tl32[t] = make_float2((float)v.re, (float)v.im);
     }
   }
@@ -530,22 +546,46 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
       CT<R> A, B;
       coupling_entry<R, TabT>(s, tab, y, base, q, p, A, B);
       const int l = (int)s.pf[p * kPfacStride + 6];
-      CT<R> te, tm;
+      const int n = (int)s.qf[q * kQfacStride + 3];
+      CT<R> tei, tmi, tej, tmj;
       if(kMixed) {
-        te = CT<R>{(R)s.tl32[2 * l].x, (R)s.tl32[2 * l].y};
-        tm = CT<R>{(R)s.tl32[2 * l + 1].x, (R)s.tl32[2 * l + 1].y};
+        tei = CT<R>{(R)s.tl32[2 * l].x, (R)s.tl32[2 * l].y};
+        tmi = CT<R>{(R)s.tl32[2 * l + 1].x, (R)s.tl32[2 * l + 1].y};
+        tej = CT<R>{(R)s.tl32[nT + 2 * l].x, (R)s.tl32[nT + 2 * l].y};
+        tmj = CT<R>{(R)s.tl32[nT + 2 * l + 1].x, (R)s.tl32[nT + 2 * l + 1].y};
       } else {
-        te = CT<R>{(R)s.tl[2 * l].re, (R)s.tl[2 * l].im};
-        tm = CT<R>{(R)s.tl[2 * l + 1].re, (R)s.tl[2 * l + 1].im};
+        tei = CT<R>{(R)s.tl[2 * l].re, (R)s.tl[2 * l].im};
+        tmi = CT<R>{(R)s.tl[2 * l + 1].re, (R)s.tl[2 * l + 1].im};
+        tej = CT<R>{(R)s.tl[nT + 2 * l].re, (R)s.tl[nT + 2 * l].im};
+        tmj = CT<R>{(R)s.tl[nT + 2 * l + 1].re, (R)s.tl[nT + 2 * l + 1].im};
       }
-      const size_t col_te = (y0 + q) * a.ld + x0, col_tm = (y0 + P + q) * a.ld + x0;
-      CT<R> v = neg_mul(te, A);
+      // S_ij (rows of sphere i, columns of sphere j), translation r_i - r_j
+      size_t col_te = (xj + q) * a.ld + xi, col_tm = (xj + P + q) * a.ld + xi;
+      CT<R> v = neg_mul(tei, A);
       put_out<OutT>(S, col_te + p, v.re, v.im);
-      v = neg_mul(tm, A);
+      v = neg_mul(tmi, A);
       put_out<OutT>(S, col_tm + P + p, v.re, v.im);
-      v = neg_mul(te, B);
+      v = neg_mul(tei, B);
       put_out<OutT>(S, col_tm + p, v.re, v.im);
-      v = neg_mul(tm, B);
+      v = neg_mul(tmi, B);
+      put_out<OutT>(S, col_te + P + p, v.re, v.im);
+      // S_ji, translation r_j - r_i
+      if((n + l) & 1) {
+        A.re = -A.re;
+        A.im = -A.im;
+      } else {
+        B.re = -B.re;
+        B.im = -B.im;
+      }
+      col_te = (xi + q) * a.ld + xj;
+      col_tm = (xi + P + q) * a.ld + xj;
+      v = neg_mul(tej, A);
+      put_out<OutT>(S, col_te + p, v.re, v.im);
+      v = neg_mul(tmj, A);
+      put_out<OutT>(S, col_tm + P + p, v.re, v.im);
+      v = neg_mul(tej, B);
+      put_out<OutT>(S, col_tm + p, v.re, v.im);
+      v = neg_mul(tmj, B);
       put_out<OutT>(S, col_te + P + p, v.re, v.im);
     }
     __syncthreads();
@@ -890,7 +930,7 @@ void launch_assemble(om_problem *pr, int harmonic, int precision) {
   a.waveK = mk(k.real(), k.imag());
   a.ld = pr->n;
   fill_chunks(a, y);
-  dim3 grid(pr->N * pr->N);
+  dim3 grid((unsigned)((long)pr->N * (pr->N - 1) / 2 + pr->N));
   timer_begin(ctx, ctx->ev_asm);
   if(mixed) {
     set_smem(k_assemble<true>, y.bytes);
