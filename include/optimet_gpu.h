@@ -151,6 +151,23 @@ int om_solve(om_problem *pr, const om_solve_options *opts, om_solve_stats *stats
 /* Solve S x = b for a caller-supplied right-hand side with the assembled matrix. */
 int om_solve_rhs(om_problem *pr, int harmonic, const om_solve_options *opts, const double *b,
                  double *x, om_solve_stats *stats);
+/* The solve of om_solve_rhs (OM_SOLVE_GMRES only) without any device-memory
+ * allocation. No counterpart in the reference. For callers that cannot call
+ * cudaMalloc/cudaFree while they solve -- a serving loop that has given all of
+ * HBM to resident matrices and its own arena, or latency-critical host code
+ * that must not let an allocation synchronise the device. b and x are host
+ * buffers of n complex values, as for om_solve_rhs.
+ *   Limit: every device buffer of the solve (b, x, the Krylov basis of
+ *   max_iter + 1 vectors, split-K partial sums) lives in one fixed 64 MiB
+ *   array that each GPU loading the library holds until the process exits;
+ *   a request that does not fit returns OM_ERR_INVALID with the bytes it needs.
+ *   The first call on a device looks up that array's device address; make it
+ *   before any stream capture on that device.
+ *   All calls share the array and it keeps the previous call's contents (the
+ *   solution vector is cleared at the start of every call); calls that overlap
+ *   on the GPU, from any context on the same device, race. */
+int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve_options *opts,
+                         const double *b, double *x, om_solve_stats *stats);
 /* Scattered and internal coefficients (n each; either may be NULL). */
 int om_get_coefficients(om_problem *pr, double *X_sca, double *X_int);
 /* Result::getExtinctionCrossSection, getScatteringCrossSection,

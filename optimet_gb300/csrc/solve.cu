@@ -14,6 +14,8 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "om_internal.h"
@@ -1016,4 +1018,218 @@ int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, 
   return rc;
 }
 
+
+// ---------------------------------------------------------------------------
+// Solve without device allocation.
+//
+// Some callers cannot allocate device memory while they solve: a serving loop
+// that has handed all of HBM to resident matrices and an arena of its own, or
+// host code that must not call cudaMalloc/cudaFree because those calls can
+// synchronise the whole device in the middle of latency-critical work. For
+// them om_solve_rhs_noalloc runs the same restarted GMRES as om_solve_rhs but
+// keeps every device buffer it needs (right-hand side, solution, Krylov basis,
+// split-K partial sums) in the fixed array below, which every GPU that loads
+// this library holds until the process exits.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocBytes = size_t(64) << 20;  // 64 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+// Device address of g_noalloc_scratch, looked up once per device (with that
+// device current) on the first no-alloc call made on it.
+void *noalloc_scratch(om_context *ctx) {
+  static std::mutex mu;
+  static void *addr[256] = {};
+  std::lock_guard<std::mutex> lock(mu);
+  if(ctx->device < 0 || ctx->device >= 256)
+    return nullptr;
+  if(!addr[ctx->device]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if(e != cudaSuccess) {
+      ctx->err = std::string("cudaGetSymbolAddress(no-alloc scratch): ") + cudaGetErrorString(e);
+      return nullptr;
+    }
+    addr[ctx->device] = p;
+  }
+  return addr[ctx->device];
+}
+
+// Restarted GMRES (no preconditioner) on a caller-provided workspace: the
+// algorithm of gmres64 with its buffers carved from `ws` instead of allocated.
+template <typename M>
+int gmres_on_workspace(om_context *ctx, const M *S, long n, const double2 *b, double2 *x,
+                       double tol, int m, int restarts, char *ws, int *iters, double *relres) {
+  const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
+  const int nblk = (int)((n + kDotRows - 1) / kDotRows);
+  Work w;  // view only: buf is not owned
+  w.ctx = ctx;
+  size_t off = 0;
+  w.buf = ws;
+  double2 *Vb = w.take<double2>((size_t)(m + 1) * n, off);
+  double2 *r = w.take<double2>(n, off);
+  double2 *t = w.take<double2>(n, off);
+  double2 *part = w.take<double2>((size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)), off);
+  double2 *hd = w.take<double2>(m + 2, off);
+  double2 *yd = w.take<double2>(m + 2, off);
+  w.buf = nullptr;  // keep ~Work from freeing the static array
+
+  cudaMemsetAsync(x, 0, sizeof(double2) * n, ctx->stream);  // the array keeps old contents
+  const double bnorm = vec_norm(ctx, b, n, part, hd);
+  *iters = 0;
+  if(bnorm == 0.0) {
+    *relres = 0.0;
+    return OM_OK;
+  }
+  double err = 1.0;
+  int total = 0;
+  for(int rest = 0; rest < restarts && err > tol; ++rest) {
+    double beta;
+    if(rest == 0) {
+      cudaMemcpyAsync(r, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+      beta = bnorm;
+    } else {
+      matvec<M, double2>(ctx, S, n, x, part, r, b);
+      beta = vec_norm(ctx, r, n, part, hd);
+    }
+    if(beta == 0.0) {
+      err = 0.0;
+      break;
+    }
+    k_scale_copy<double2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(r, 1.0 / beta, Vb, n);
+    ctx->last_launches++;
+    std::vector<std::vector<std::complex<double>>> H;
+    std::vector<std::complex<double>> cs, sn, g(1, beta);
+    int k = 0;
+    double cur = beta / bnorm;
+    while(k < m && cur > tol) {
+      double2 *wv = Vb + (size_t)(k + 1) * n;
+      matvec<M, double2>(ctx, S, n, Vb + (size_t)k * n, part, wv, nullptr);
+      std::vector<std::complex<double>> h;
+      arnoldi_orth<double2>(ctx, Vb, n, k + 1, wv, part, hd, h);
+      const double hn = h[k + 1].real();
+      if(hn > 0.0) {
+        k_scale_copy<double2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(wv, 1.0 / hn, wv, n);
+        ctx->last_launches++;
+      }
+      for(int i = 0; i < k; ++i) {
+        std::complex<double> a = h[i], bb = h[i + 1];
+        h[i] = std::conj(cs[i]) * a + std::conj(-sn[i]) * bb;
+        h[i + 1] = sn[i] * a + cs[i] * bb;
+      }
+      std::complex<double> c, s;
+      givens(h[k], h[k + 1], c, s);
+      cs.push_back(c);
+      sn.push_back(s);
+      std::complex<double> hk = h[k], hk1 = h[k + 1];
+      h[k] = std::conj(c) * hk + std::conj(-s) * hk1;
+      h[k + 1] = s * hk + c * hk1;
+      g.push_back(0.0);
+      std::complex<double> g0 = g[k], g1 = g[k + 1];
+      g[k] = std::conj(c) * g0 + std::conj(-s) * g1;
+      g[k + 1] = s * g0 + c * g1;
+      H.push_back(h);
+      cur = std::abs(g[k + 1]) / bnorm;
+      ++k;
+      ++total;
+      if(hn == 0.0)
+        break;
+    }
+    std::vector<std::complex<double>> y(k);
+    for(int j = k - 1; j >= 0; --j) {
+      std::complex<double> v = g[j];
+      for(int q = j + 1; q < k; ++q)
+        v -= H[q][j] * y[q];
+      y[j] = v / H[j][j];
+    }
+    std::vector<double2> yh(k);
+    for(int j = 0; j < k; ++j)
+      yh[j] = make_double2(y[j].real(), y[j].imag());
+    cudaMemcpyAsync(yd, yh.data(), sizeof(double2) * k, cudaMemcpyHostToDevice, ctx->stream);
+    k_add_combo<double2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, yd, x, n);
+    ctx->last_launches++;
+    matvec<M, double2>(ctx, S, n, x, part, t, b);
+    err = vec_norm(ctx, t, n, part, hd) / bnorm;
+    cudaStreamSynchronize(ctx->stream);
+  }
+  *iters = total;
+  *relres = err;
+  return err <= tol ? OM_OK : OM_ERR_NOT_CONVERGED;
+}
+
+}  // namespace
+
+}  // namespace om
+
+extern "C" int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve_options *opts,
+                                    const double *b, double *x, om_solve_stats *stats) {
+  using namespace om;
+  if(!pr || !opts || !b || !x || (harmonic != OM_FF && harmonic != OM_SH))
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  if(opts->method != OM_SOLVE_GMRES) {
+    ctx->err = "om_solve_rhs_noalloc supports OM_SOLVE_GMRES only";
+    return OM_ERR_INVALID;
+  }
+  if(pr->S_prec[harmonic] < 0) {
+    ctx->err = "matrix not assembled";
+    return OM_ERR_STATE;
+  }
+  const long n = pr->n;
+  const int m = opts->max_iter;
+  if(m < 1 || opts->restarts < 1) {
+    ctx->err = "max_iter and restarts must be positive";
+    return OM_ERR_INVALID;
+  }
+  // bytes the solve needs: b and x, then the workspace of gmres_on_workspace
+  auto round = [](size_t v) { return ((v + 255) / 256) * 256; };
+  const size_t nsplit = (size_t)((n + kMvCols - 1) / kMvCols);
+  const size_t nblk = (size_t)((n + kDotRows - 1) / kDotRows);
+  const size_t z = sizeof(double2);
+  const size_t need = 2 * round(z * n) + round(z * (size_t)(m + 1) * n) + 2 * round(z * n) +
+                      round(z * std::max(nsplit * n, nblk * (size_t)(m + 2))) +
+                      2 * round(z * (size_t)(m + 2));
+  if(need > kNoAllocBytes) {
+    ctx->err = "problem too large for the no-alloc scratch: needs " + std::to_string(need) +
+               " bytes, the fixed array holds " + std::to_string(kNoAllocBytes) +
+               " (reduce max_iter or use om_solve_rhs)";
+    return OM_ERR_INVALID;
+  }
+  char *ws = static_cast<char *>(noalloc_scratch(ctx));
+  if(!ws)
+    return OM_ERR_CUDA;
+  double2 *db = reinterpret_cast<double2 *>(ws);
+  double2 *dx = reinterpret_cast<double2 *>(ws + round(z * n));
+  char *rest = ws + 2 * round(z * n);
+  cudaMemcpyAsync(db, b, z * n, cudaMemcpyHostToDevice, ctx->stream);
+  int it = 0;
+  double rr = 0;
+  int rc;
+  if(pr->S_prec[harmonic] == OM_C128)
+    rc = gmres_on_workspace<double2>(ctx, (const double2 *)pr->d_S[harmonic], n, db, dx, opts->tol,
+                                     m, opts->restarts, rest, &it, &rr);
+  else
+    rc = gmres_on_workspace<float2>(ctx, (const float2 *)pr->d_S32[harmonic], n, db, dx, opts->tol,
+                                    m, opts->restarts, rest, &it, &rr);
+  cudaMemcpyAsync(x, dx, z * n, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if(e != cudaSuccess) {
+    ctx->err = std::string("om_solve_rhs_noalloc: ") + cudaGetErrorString(e);
+    return OM_ERR_CUDA;
+  }
+  if(stats) {
+    stats->iterations = it;
+    stats->inner_iterations = 0;
+    stats->rel_residual = rr;
+    stats->seconds = 0.0;
+  }
+  if(rc == OM_ERR_NOT_CONVERGED)
+    ctx->err = "GMRES did not reach the requested tolerance";
+  return rc;
+}
+
+namespace om {
 }  // namespace om
