@@ -280,8 +280,8 @@ def gpu_arm(args, w):
         "roofline": {"bound": "hbm", "kernel": "k_matvec_part<float2,float2> (FP32 inner matvec)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": how + " (MEASURED_PEAKS.json hbm_gbs)",
-                     # DRAM bytes per launch from the ncu capture of the same kernel at
-                     # n = 6,400 (profiles/k_matvec_small.md): 1.0099 x algorithmic
+                     # DRAM bytes per launch from an ncu capture of the same kernel at
+                     # n = 6,400 (dram read + write): 1.0099 x the algorithmic bytes
                      "traffic": bytes_mv * 1.0099,
                      "algorithmic_bytes_per_launch": bytes_mv},
         "kernels": {

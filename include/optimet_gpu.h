@@ -52,6 +52,9 @@ typedef struct {
   double eps_r[2];       /* relative permittivity at the fundamental */
   double mu_r[2];        /* relative permeability */
   double eps_r_sh[2];    /* relative permittivity at the second harmonic (<epsilon_SH>) */
+  double ksippp[2];      /* surface chi(2), perp-perp-perp (<ksippp>) */
+  double ksiparppar[2];  /* surface chi(2), par-perp-par (<ksiparppar>) */
+  double gamma[2];       /* bulk chi(2) (<gamma>) */
   int nmax;              /* <harmonics nmax>; equal for all spheres */
   int reserved;
 } om_sphere;
@@ -179,14 +182,40 @@ int om_cross_sections(om_problem *pr, double out[4]);
  * Cartesian components: E, H are 3 complex per point. */
 int om_near_field(om_problem *pr, const double *xyz, int npts, double *E, double *H);
 
+/* Second harmonic (the SH half of PreconditionedMatrix::solve,
+ * PreconditionedMatrixSolver.h:62-78): source K and K1ana from the FF internal
+ * coefficients (source_vectorSH / source_vectorSH_K1ana, PreconditionedMatrix.cpp:
+ * 1347-1436, with the nine coupling tables of Symbol.cpp:1036-1451), solve with
+ * the SH matrix (om_assemble(pr, OM_SH, ...) first), then convertInternal_SH
+ * (Solver.cpp:95-116). Needs a fundamental solution (om_solve). */
+int om_solve_sh(om_problem *pr, const om_solve_options *opts, om_solve_stats *stats);
+/* SH source and its analytic part (K, K1ana; n each, either may be NULL) and SH
+ * scattered / internal coefficients (either may be NULL). */
+int om_get_sh_vectors(om_problem *pr, double *K, double *K1ana, double *X_sca_SH,
+                      double *X_int_SH);
+/* Result::getScatteringCrossSection_SH and getAbsorptionCrossSection_SH
+ * (Result.cpp:662-778, Symbol.cpp:358-477): out = {C_sca_SH, C_abs_SH}. */
+int om_sh_cross_sections(om_problem *pr, double out[2]);
+/* The nine SH coupling tables for nMaxS = nMax (9 x P^3 doubles, order C_10m1,
+ * C_11m1, C_00m1, C_01m1, W_m1m1, W_11, W_00, W_10, W_01; [k][p][q]),
+ * computed on the device (Geometry::Coefficients, Geometry.cpp:234-247). */
+int om_clg_tables(om_context *ctx, int nmax, double *out);
+
 /* One wavelength-solve from host buffers to host buffers: problem set-up,
  * source vector, FF assembly, solve, internal coefficients, cross sections
- * (the body of Simulation::scan_wavelengths' loop, Simulation.cpp:643-674).
+ * (the body of Simulation::scan_wavelengths' loop, Simulation.cpp:643-674,
+ * fundamental part).
  * X_sca / X_int may be NULL. */
 int om_wavelength_solve(om_context *ctx, const om_sphere *spheres, int n_spheres,
                         const om_medium *background, const om_plane_wave *wave,
                         const om_solve_options *opts, int precision, double xsec[4],
                         double *X_sca, double *X_int, om_solve_stats *stats);
+/* As om_wavelength_solve, followed, when wave->sh is set, by the SH assembly
+ * (same precision), om_solve_sh and om_sh_cross_sections into xsec_sh[2]. */
+int om_wavelength_solve_sh(om_context *ctx, const om_sphere *spheres, int n_spheres,
+                           const om_medium *background, const om_plane_wave *wave,
+                           const om_solve_options *opts, int precision, double xsec[4],
+                           double xsec_sh[2], om_solve_stats *stats);
 
 #ifdef __cplusplus
 }

@@ -40,6 +40,7 @@ class OptimetError(RuntimeError):
 class Sphere(C.Structure):
     _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("radius", C.c_double),
                 ("eps_r", C.c_double * 2), ("mu_r", C.c_double * 2), ("eps_r_sh", C.c_double * 2),
+                ("ksippp", C.c_double * 2), ("ksiparppar", C.c_double * 2), ("gamma", C.c_double * 2),
                 ("nmax", C.c_int), ("reserved", C.c_int)]
 
 
@@ -104,6 +105,13 @@ def lib():
         L.om_wavelength_solve.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
                                           C.POINTER(PlaneWave), C.POINTER(SolveOptions), C.c_int,
                                           _dp, _dp, _dp, C.POINTER(SolveStats)]
+        L.om_wavelength_solve_sh.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
+                                             C.POINTER(PlaneWave), C.POINTER(SolveOptions),
+                                             C.c_int, _dp, _dp, C.POINTER(SolveStats)]
+        L.om_solve_sh.argtypes = [vp, C.POINTER(SolveOptions), C.POINTER(SolveStats)]
+        L.om_get_sh_vectors.argtypes = [vp, _dp, _dp, _dp, _dp]
+        L.om_sh_cross_sections.argtypes = [vp, _dp]
+        L.om_clg_tables.argtypes = [vp, C.c_int, _dp]
         _lib = L
     return _lib
 
@@ -161,9 +169,11 @@ class Context:
         return lib().om_context_last_launches(self.h)
 
 
-def spheres_array(xyz, radius, eps, nmax, mu=None, eps_sh=None):
+def spheres_array(xyz, radius, eps, nmax, mu=None, eps_sh=None, ksippp=0.0, ksiparppar=0.0,
+                  gamma=0.0):
     xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
     n = xyz.shape[0]
+    chi = [np.broadcast_to(np.asarray(v, dtype=np.complex128), (n,)) for v in (ksippp, ksiparppar, gamma)]
     radius = np.broadcast_to(np.asarray(radius, dtype=np.float64), (n,))
     eps = np.broadcast_to(np.asarray(eps, dtype=np.complex128), (n,))
     mu = np.broadcast_to(np.asarray(1.0 if mu is None else mu, dtype=np.complex128), (n,))
@@ -176,6 +186,9 @@ def spheres_array(xyz, radius, eps, nmax, mu=None, eps_sh=None):
         s.eps_r[0], s.eps_r[1] = eps[i].real, eps[i].imag
         s.mu_r[0], s.mu_r[1] = mu[i].real, mu[i].imag
         s.eps_r_sh[0], s.eps_r_sh[1] = eps_sh[i].real, eps_sh[i].imag
+        s.ksippp[0], s.ksippp[1] = chi[0][i].real, chi[0][i].imag
+        s.ksiparppar[0], s.ksiparppar[1] = chi[1][i].real, chi[1][i].imag
+        s.gamma[0], s.gamma[1] = chi[2][i].real, chi[2][i].imag
         s.nmax = int(nmax)
     return arr
 
@@ -267,6 +280,24 @@ class Problem:
         self.ctx.check(lib().om_cross_sections(self.h, _p(out)))
         return out
 
+    def solve_sh(self, opts: SolveOptions | None = None) -> SolveStats:
+        """SH source, SH solve and SH internal coefficients (needs solve() and assemble(SH))."""
+        st = SolveStats()
+        self.ctx.check(lib().om_solve_sh(self.h, C.byref(opts or options()), C.byref(st)))
+        return st
+
+    def sh_vectors(self):
+        """(K, K1ana, X_sca_SH, X_int_SH)."""
+        outs = [np.zeros(self.n, np.complex128) for _ in range(4)]
+        self.ctx.check(lib().om_get_sh_vectors(self.h, *[_p(o) for o in outs]))
+        return outs
+
+    def sh_cross_sections(self):
+        """(C_sca_SH, C_abs_SH)."""
+        out = np.zeros(2)
+        self.ctx.check(lib().om_sh_cross_sections(self.h, _p(out)))
+        return out
+
     def near_field(self, xyz):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
         E = np.zeros((xyz.shape[0], 3), np.complex128)
@@ -298,6 +329,25 @@ def wavelength_solve(ctx: Context, spheres, bg, wave, opts=None, precision=C128,
                                    _p(xs), _p(xi), C.byref(st))
     ctx.check(rc)
     return xsec, xs, xi, st
+
+
+def clg_tables(ctx: Context, nmax: int) -> np.ndarray:
+    """The nine SH coupling tables computed on the device, flattened (9 P^3)."""
+    P = nmax * (nmax + 2)
+    out = np.zeros(9 * P ** 3)
+    ctx.check(lib().om_clg_tables(ctx.h, nmax, _p(out)))
+    return out
+
+
+def wavelength_solve_sh(ctx: Context, spheres, bg, wave, opts=None, precision=C128):
+    xsec = np.zeros(4)
+    xsh = np.zeros(2)
+    st = SolveStats()
+    rc = lib().om_wavelength_solve_sh(ctx.h, spheres, len(spheres), None if bg is None else C.byref(bg),
+                                      C.byref(wave), C.byref(opts or options()), precision,
+                                      _p(xsec), _p(xsh), C.byref(st))
+    ctx.check(rc)
+    return xsec, xsh, st
 
 
 def declared_symbols():

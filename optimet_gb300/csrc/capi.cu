@@ -76,6 +76,8 @@ int update_wave(om_problem *pr) {
   const double w = pr->omega;
   const cplx waveK_0 = w * std::sqrt(kEps0 * kMu0);
   std::vector<om::SphereScalars> sc(pr->N);
+  std::vector<om::ShScalars> shs(pr->N);
+  pr->eta = std::sqrt(mu_b / eps_b);
   std::vector<zd> kin(pr->N), izin(pr->N);
   for(int i = 0; i < pr->N; ++i) {
     const cplx eps_s = pr->eps_r[i] * kEps0, mu_s = pr->mu_r[i] * kMu0;
@@ -93,12 +95,35 @@ int update_wave(om_problem *pr) {
     s.rho_sh = Z(k_s2 / k_b2);
     s.r0_sh = Z(k_b2 * pr->radius[i]);
     s.mu_sob_sh = Z(mu_s / mu_b);
+    // SH outer / internal factors (Scatterer.cpp:163-412)
+    s.x_b2 = Z(k_b2 * pr->radius[i]);
+    s.x_i2 = Z(k_s2 * pr->radius[i]);
+    s.zeta = Z(std::sqrt(mu_b / eps_b) / std::sqrt(mu_s / eps_sh));
+    // SH source and absorption scalars (Symbol.cpp:155-477)
+    om::ShScalars &h = shs[i];
+    const cplx mu_0 = kMu0, eps_0 = kEps0;
+    const cplx imp = std::sqrt(mu_b / eps_b) / std::sqrt(mu_0 / eps_0);
+    const cplx waveK_01 = w * std::sqrt(eps_0 * mu_0);
+    const double R = pr->radius[i];
+    h.k1 = Z(w * std::sqrt(eps_s * mu_s));
+    h.kSH = Z(2.0 * w * std::sqrt(eps_sh * mu_s));
+    h.c_up = Z(cplx(2.0, 0.0) * cplx(0.0, 1.0) * pr->ksiparppar[i] * imp);
+    h.c_vp = Z(cplx(2.0, 0.0) * pr->ksiparppar[i] * imp);
+    h.c_g1 = Z(cplx(0.0, 1.0) * pr->ksippp[i] / waveK_01 / R);
+    h.c_g2 = Z(cplx(0.0, 1.0) * pr->gamma[i] * (eps_0 / eps_sh) / waveK_01 / R);
+    h.c_bulk = Z((-eps_0 / eps_sh) * pr->gamma[i]);
+    h.sigma = Z(-cplx(0.0, 1.0) * kEps0 * 2.0 * w * (pr->eps_r_sh[i] - 1.0));
+    h.w01 = Z(waveK_01);
+    h.R = R;
+    h.has_gamma = pr->gamma[i] != cplx(0.0, 0.0);
     kin[i] = Z(waveK_0 * std::sqrt(pr->eps_r[i] * pr->mu_r[i]));
     izin[i] = Z(cplx(0.0, -1.0) / std::sqrt(mu_s / eps_s));
   }
   cudaMemcpyAsync(pr->d_scal, sc.data(), sizeof(om::SphereScalars) * pr->N, cudaMemcpyHostToDevice,
                   ctx->stream);
   cudaMemcpyAsync(pr->d_kin, kin.data(), sizeof(zd) * pr->N, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(pr->d_shs, shs.data(), sizeof(om::ShScalars) * pr->N, cudaMemcpyHostToDevice,
+                  ctx->stream);
   cudaMemcpyAsync(pr->d_izin, izin.data(), sizeof(zd) * pr->N, cudaMemcpyHostToDevice, ctx->stream);
   om::launch_sphere_terms(pr);
   // Einc = toProjection((0, theta, phi), (0, E_theta, E_phi)) (Reader.cpp:815-827)
@@ -112,6 +137,7 @@ int update_wave(om_problem *pr) {
   cudaStreamSynchronize(ctx->stream);
   pr->have_source = false;
   pr->have_solution = false;
+  pr->have_sh = false;
   pr->S_prec[0] = pr->S_prec[1] = -1;
   return check_launch(ctx, "per-sphere / incident kernels");
 }
@@ -135,6 +161,15 @@ void free_problem(om_problem *pr) {
   dev_free(ctx, pr->d_X, n);
   dev_free(ctx, pr->d_Xint, n);
   dev_free(ctx, pr->d_xsec, 16);
+  dev_free(ctx, pr->d_shs, N);
+  dev_free(ctx, pr->d_shf, N * (nm / 2) * 8);
+  dev_free(ctx, pr->d_shvec, 3 * N * P);
+  dev_free(ctx, pr->d_K, n);
+  dev_free(ctx, pr->d_K1, n);
+  dev_free(ctx, pr->d_Xsh, n);
+  dev_free(ctx, pr->d_Xish, n);
+  dev_free(ctx, pr->d_wsh, N * P);
+  dev_free(ctx, pr->d_acs, N * P);
   for(int h = 0; h < 2; ++h) {
     if(pr->d_S[h]) {
       cudaFree(pr->d_S[h]);
@@ -211,6 +246,9 @@ int make_problem(om_context *ctx, const om_sphere *spheres, int n_spheres, const
     pr->eps_r.push_back(cplx(s.eps_r[0], s.eps_r[1]));
     pr->mu_r.push_back(cplx(s.mu_r[0], s.mu_r[1]));
     pr->eps_r_sh.push_back(cplx(s.eps_r_sh[0], s.eps_r_sh[1]));
+    pr->ksippp.push_back(cplx(s.ksippp[0], s.ksippp[1]));
+    pr->ksiparppar.push_back(cplx(s.ksiparppar[0], s.ksiparppar[1]));
+    pr->gamma.push_back(cplx(s.gamma[0], s.gamma[1]));
   }
   pr->bg_eps_r = bg ? cplx(bg->eps_r[0], bg->eps_r[1]) : cplx(1.0, 0.0);
   pr->bg_mu_r = bg ? cplx(bg->mu_r[0], bg->mu_r[1]) : cplx(1.0, 0.0);
@@ -238,6 +276,8 @@ int make_problem(om_context *ctx, const om_sphere *spheres, int n_spheres, const
   if(!rc) rc = dev_alloc(ctx, &pr->d_X, n);
   if(!rc) rc = dev_alloc(ctx, &pr->d_Xint, n);
   if(!rc) rc = dev_alloc(ctx, &pr->d_xsec, 16);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_shs, N);
+  if(!rc) rc = dev_alloc(ctx, &pr->d_shf, N * (nm / 2) * 8);
   if(rc) {
     free_problem(pr);
     delete pr;
@@ -283,6 +323,20 @@ int ensure_matrix(om_problem *pr, int harmonic, int precision) {
 }  // namespace
 
 namespace om {
+int sh_alloc(om_problem *pr) {
+  om_context *ctx = pr->ctx;
+  const size_t N = pr->N, P = pr->P, n = pr->n;
+  int rc = OM_OK;
+  if(!rc && !pr->d_shvec) rc = dev_alloc(ctx, &pr->d_shvec, 3 * N * P);
+  if(!rc && !pr->d_K) rc = dev_alloc(ctx, &pr->d_K, n);
+  if(!rc && !pr->d_K1) rc = dev_alloc(ctx, &pr->d_K1, n);
+  if(!rc && !pr->d_Xsh) rc = dev_alloc(ctx, &pr->d_Xsh, n);
+  if(!rc && !pr->d_Xish) rc = dev_alloc(ctx, &pr->d_Xish, n);
+  if(!rc && !pr->d_wsh) rc = dev_alloc(ctx, &pr->d_wsh, N * P);
+  if(!rc && !pr->d_acs) rc = dev_alloc(ctx, &pr->d_acs, N * P);
+  return rc;
+}
+
 void collect_timers(om_context *ctx) {
   auto fold = [](std::vector<std::pair<cudaEvent_t, cudaEvent_t>> &v, double &t, long &n) {
     for(auto &e : v) {
@@ -383,6 +437,8 @@ void om_context_destroy(om_context *ctx) {
     cudaFree(t.pf);
     cudaFree(t.legc);
   }
+  for(auto &t : ctx->clg)
+    cudaFree(t.second);
   if(ctx->mark)
     cudaEventDestroy(ctx->mark);
   cudaStreamDestroy(ctx->stream);
@@ -774,6 +830,146 @@ int om_near_field(om_problem *pr, const double *xyz, int npts, double *E, double
   dev_free(ctx, d_E, 3 * (size_t)npts);
   dev_free(ctx, d_H, 3 * (size_t)npts);
   return rc;
+}
+
+
+int om_solve_sh(om_problem *pr, const om_solve_options *opts, om_solve_stats *stats) {
+  if(!pr || !opts)
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  if(!pr->have_solution) {
+    ctx->err = "the SH source needs the fundamental solution (om_solve first)";
+    return OM_ERR_STATE;
+  }
+  if(pr->S_prec[OM_SH] < 0) {
+    ctx->err = "SH matrix not assembled (om_assemble with OM_SH)";
+    return OM_ERR_STATE;
+  }
+  int rc = om::sh_alloc(pr);
+  if(rc)
+    return rc;
+  om_solve_stats st{};
+  try {
+    om::launch_sh_source(pr);
+    rc = check_launch(ctx, "SH source");
+    if(!rc)
+      rc = solve_impl(pr, OM_SH, opts, (const double2 *)pr->d_K, (double2 *)pr->d_Xsh, &st);
+  } catch(std::exception &e) {
+    ctx->err = e.what();
+    rc = OM_ERR_CUDA;
+  }
+  if(stats)
+    *stats = st;
+  if(rc && rc != OM_ERR_NOT_CONVERGED)
+    return rc;
+  om::launch_sh_internal(pr);
+  int rc2 = check_launch(ctx, "SH internal coefficients");
+  if(rc2)
+    return rc2;
+  pr->have_sh = true;
+  return rc;
+}
+
+int om_get_sh_vectors(om_problem *pr, double *K, double *K1ana, double *X_sca_SH,
+                      double *X_int_SH) {
+  if(!pr)
+    return OM_ERR_INVALID;
+  if(!pr->have_sh) {
+    pr->ctx->err = "no SH solution";
+    return OM_ERR_STATE;
+  }
+  cudaSetDevice(pr->ctx->device);
+  const size_t b = sizeof(zd) * pr->n;
+  if(K) cudaMemcpyAsync(K, pr->d_K, b, cudaMemcpyDeviceToHost, pr->ctx->stream);
+  if(K1ana) cudaMemcpyAsync(K1ana, pr->d_K1, b, cudaMemcpyDeviceToHost, pr->ctx->stream);
+  if(X_sca_SH) cudaMemcpyAsync(X_sca_SH, pr->d_Xsh, b, cudaMemcpyDeviceToHost, pr->ctx->stream);
+  if(X_int_SH) cudaMemcpyAsync(X_int_SH, pr->d_Xish, b, cudaMemcpyDeviceToHost, pr->ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(pr->ctx->stream);
+  return e == cudaSuccess ? OM_OK : cuda_fail(pr->ctx, e, "SH vectors");
+}
+
+int om_sh_cross_sections(om_problem *pr, double out[2]) {
+  if(!pr || !out)
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  if(!pr->have_sh) {
+    ctx->err = "no SH solution";
+    return OM_ERR_STATE;
+  }
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  try {
+    om::launch_sh_cross_sections(pr, pr->d_xsec + 4);
+  } catch(std::exception &e) {
+    ctx->err = e.what();
+    return OM_ERR_CUDA;
+  }
+  cudaMemcpyAsync(out, pr->d_xsec + 4, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if(e != cudaSuccess)
+    return cuda_fail(ctx, e, "SH cross sections");
+  return check_launch(ctx, "SH cross sections");
+}
+
+int om_clg_tables(om_context *ctx, int nmax, double *out) {
+  if(!ctx || !out || nmax < 1 || nmax > om::kMaxNmax)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  try {
+    const double *d = om::clg_tables_dev(ctx, nmax);
+    const size_t P = om::pmax(nmax);
+    cudaMemcpyAsync(out, d, sizeof(double) * 9 * P * P * P, cudaMemcpyDeviceToHost, ctx->stream);
+  } catch(std::exception &e) {
+    ctx->err = e.what();
+    return OM_ERR_BUDGET;
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  return e == cudaSuccess ? check_launch(ctx, "tables") : cuda_fail(ctx, e, "tables");
+}
+
+int om_wavelength_solve_sh(om_context *ctx, const om_sphere *spheres, int n_spheres,
+                           const om_medium *background, const om_plane_wave *wave,
+                           const om_solve_options *opts, int precision, double xsec[4],
+                           double xsec_sh[2], om_solve_stats *stats) {
+  if(!ctx || !opts || !xsec || !wave)
+    return OM_ERR_INVALID;
+  om_problem *pr = nullptr;
+  int rc = om_problem_create(ctx, spheres, n_spheres, background, wave, &pr);
+  if(rc)
+    return rc;
+  int launches = ctx->last_launches;
+  auto step = [&](int r) {
+    launches += ctx->last_launches;
+    return r;
+  };
+  rc = step(om_source_vector(pr, nullptr));
+  if(!rc) rc = step(om_assemble(pr, OM_FF, precision));
+  int solve_rc = OM_OK;
+  if(!rc) {
+    solve_rc = step(om_solve(pr, opts, stats));
+    if(solve_rc && solve_rc != OM_ERR_NOT_CONVERGED)
+      rc = solve_rc;
+  }
+  if(!rc) rc = step(om_cross_sections(pr, xsec));
+  if(!rc && wave->sh && xsec_sh) {
+    rc = step(om_assemble(pr, OM_SH, precision));
+    if(!rc) {
+      int r2 = step(om_solve_sh(pr, opts, nullptr));
+      if(r2 && r2 != OM_ERR_NOT_CONVERGED)
+        rc = r2;
+      else if(r2)
+        solve_rc = r2;
+    }
+    if(!rc) rc = step(om_sh_cross_sections(pr, xsec_sh));
+  }
+  std::string err = ctx->err;
+  om_problem_destroy(pr);
+  ctx->err = err;
+  ctx->last_launches = launches;
+  return rc ? rc : solve_rc;
 }
 
 int om_wavelength_solve(om_context *ctx, const om_sphere *spheres, int n_spheres,

@@ -39,6 +39,20 @@ constexpr int kPfacStride = 8;
 struct SphereScalars {
   zd r0, rho, mu_sob, mu_j, mu_0;           // fundamental
   zd r0_sh, rho_sh, mu_sob_sh;              // second harmonic
+  zd x_b2, x_i2, zeta;                      // SH outer / internal factors
+};
+
+// Per-sphere scalars of the SH source and absorption (Symbol.cpp:155-477).
+struct ShScalars {
+  zd k1;          // omega sqrt(eps_j mu_j)
+  zd kSH;         // 2 omega sqrt(eps_SH mu_SH)
+  zd c_up, c_vp;  // 2 i ksiparppar imp, 2 ksiparppar imp; imp = sqrt(mu_b/eps_b)/sqrt(mu_0/eps_0)
+  zd c_g1, c_g2;  // i ksippp / waveK_01 / R, i gamma (eps_0/eps_SH) / waveK_01 / R
+  zd c_bulk;      // (-eps_0 / eps_SH) gamma
+  zd sigma;       // -i eps_0 2 omega (eps_r_SH - 1)
+  zd w01;         // waveK_01 = omega sqrt(eps_0 mu_0)
+  double R;
+  int has_gamma;
 };
 
 struct Arena;
@@ -52,6 +66,7 @@ struct om_context {
   size_t used = 0;
   std::string err;
   std::vector<om::CoefTables> tables;  // by nmax
+  std::vector<std::pair<int, double *>> clg;  // SH coupling tables by nmax
   int last_launches = 0;               // kernels launched by the last API call
   // kernel timers (CUDA events on `stream`), reset by om_context_timers
   bool timing = false;
@@ -96,6 +111,16 @@ struct om_problem {
   int S_prec[2] = {-1, -1};             // which of the two holds the current assembly
   om::zd *d_X = nullptr, *d_Xint = nullptr;
   double *d_xsec = nullptr;   // 4 + scratch
+  // second harmonic
+  std::vector<om::cplx> ksippp, ksiparppar, gamma;
+  om::ShScalars *d_shs = nullptr;
+  om::zd *d_shf = nullptr;    // N x (nmax+1) x 8: T1 TE/TM, T2 TE/TM, IauxSH1 TE/TM, IauxSH2 TE/TM
+  om::zd *d_shvec = nullptr;  // N x 3P: A_0, A_1, A_m1 vectors
+  om::zd *d_K = nullptr, *d_K1 = nullptr, *d_Xsh = nullptr, *d_Xish = nullptr;
+  double *d_wsh = nullptr;    // N x P: SH scattering weights
+  om::zd *d_acs = nullptr;    // N x P: ACSshcoeff
+  om::cplx eta;
+  bool have_sh = false;
   bool have_source = false, have_solution = false;
 };
 
@@ -107,8 +132,16 @@ void launch_sphere_terms(om_problem *pr);
 void launch_incident(om_problem *pr, const double einc[6]);
 void launch_assemble(om_problem *pr, int harmonic, int precision);
 void launch_source(om_problem *pr);
+void launch_sh_weights(om_problem *pr);
 int launch_coupling(om_context *ctx, const double *d_rel, int count, zd waveK, int nmax,
                     int hankel, zd *d_A, zd *d_B);
+
+// sh.cu
+const double *clg_tables_dev(om_context *ctx, int nmax);
+int sh_alloc(om_problem *pr);
+void launch_sh_source(om_problem *pr);
+void launch_sh_internal(om_problem *pr);
+void launch_sh_cross_sections(om_problem *pr, double *d_out2);
 
 // field.cu
 void launch_internal(om_problem *pr);

@@ -1,0 +1,424 @@
+// Second harmonic on the device: the nine coupling tables (Wigner 3j/6j/9j),
+// the SH source terms u', v', u'' and their analytic part, SH internal
+// coefficients and the SH cross sections.
+//
+// Tables: Symbol.cpp:1036-1451 (computed once per nMax and context; entries
+// with M != M1 + M2 vanish through their Clebsch-Gordan factor and are left 0).
+// Source: Symbol.cpp:155-353 with Geometry.cpp:250-310 and
+// PreconditionedMatrix.cpp:1347-1436; every bilinear form only visits the
+// (p, q) with m_q = M - m_p.
+#include <cmath>
+#include <stdexcept>
+#include <vector>
+
+#include "om_internal.h"
+
+namespace om {
+
+namespace {
+
+enum { T_C10m1, T_C11m1, T_C00m1, T_C01m1, T_Wm1m1, T_W11, T_W00, T_W10, T_W01 };
+
+// Wigner symbols from their Racah formulas (zero outside the triangle and
+// projection rules); f is a factorial table in shared memory.
+__device__ __forceinline__ bool tri(int a, int b, int c) { return c >= abs(a - b) && c <= a + b; }
+__device__ __forceinline__ double fk(const double *f, int n) { return n < 0 ? 0.0 : f[n]; }
+
+__device__ double w3j(const double *f, int j1, int j2, int j3, int m1, int m2, int m3) {
+  if(j1 < 0 || j2 < 0 || j3 < 0 || !tri(j1, j2, j3) || m1 + m2 + m3 != 0 || abs(m1) > j1 ||
+     abs(m2) > j2 || abs(m3) > j3)
+    return 0.0;
+  const double delta = sqrt(fk(f, j1 + j2 - j3) * fk(f, j1 - j2 + j3) * fk(f, -j1 + j2 + j3) /
+                            fk(f, j1 + j2 + j3 + 1));
+  const double pre = sqrt(fk(f, j1 + m1) * fk(f, j1 - m1) * fk(f, j2 + m2) * fk(f, j2 - m2) *
+                          fk(f, j3 + m3) * fk(f, j3 - m3));
+  const int kmin = max(0, max(j2 - j3 - m1, j1 - j3 + m2));
+  const int kmax = min(j1 + j2 - j3, min(j1 - m1, j2 + m2));
+  double sum = 0.0;
+  for(int k = kmin; k <= kmax; ++k) {
+    const double den = fk(f, k) * fk(f, j3 - j2 + k + m1) * fk(f, j3 - j1 + k - m2) *
+                       fk(f, j1 + j2 - j3 - k) * fk(f, j1 - k - m1) * fk(f, j2 - k + m2);
+    sum += ((k & 1) ? -1.0 : 1.0) / den;
+  }
+  return (((j1 - j2 - m3) & 1) ? -1.0 : 1.0) * delta * pre * sum;
+}
+
+__device__ __forceinline__ double tdelta(const double *f, int a, int b, int c) {
+  return sqrt(fk(f, a + b - c) * fk(f, a - b + c) * fk(f, -a + b + c) / fk(f, a + b + c + 1));
+}
+
+__device__ double w6j(const double *f, int j1, int j2, int j3, int j4, int j5, int j6) {
+  if(j1 < 0 || j2 < 0 || j3 < 0 || j4 < 0 || j5 < 0 || j6 < 0)
+    return 0.0;
+  if(!tri(j1, j2, j3) || !tri(j1, j5, j6) || !tri(j4, j2, j6) || !tri(j4, j5, j3))
+    return 0.0;
+  const int a1 = j1 + j2 + j3, a2 = j1 + j5 + j6, a3 = j4 + j2 + j6, a4 = j4 + j5 + j3;
+  const int b1 = j1 + j2 + j4 + j5, b2 = j2 + j3 + j5 + j6, b3 = j3 + j1 + j6 + j4;
+  const int tmin = max(max(a1, a2), max(a3, a4)), tmax = min(b1, min(b2, b3));
+  double sum = 0.0;
+  for(int t = tmin; t <= tmax; ++t) {
+    const double den = fk(f, t - a1) * fk(f, t - a2) * fk(f, t - a3) * fk(f, t - a4) *
+                       fk(f, b1 - t) * fk(f, b2 - t) * fk(f, b3 - t);
+    sum += ((t & 1) ? -1.0 : 1.0) * fk(f, t + 1) / den;
+  }
+  return tdelta(f, j1, j2, j3) * tdelta(f, j1, j5, j6) * tdelta(f, j4, j2, j6) *
+         tdelta(f, j4, j5, j3) * sum;
+}
+
+__device__ double w9j(const double *f, int a, int b, int c, int d, int e, int g6, int g, int h, int i) {
+  if(a < 0 || b < 0 || c < 0 || d < 0 || e < 0 || g6 < 0 || g < 0 || h < 0 || i < 0)
+    return 0.0;
+  const int xmin = max(abs(a - i), max(abs(h - d), abs(b - g6)));
+  const int xmax = min(a + i, min(h + d, b + g6));
+  double sum = 0.0;
+  for(int x = xmin; x <= xmax; ++x)
+    sum += (2 * x + 1) * w6j(f, a, d, g, h, i, x) * w6j(f, b, e, h, d, x, g6) *
+           w6j(f, c, g6, i, x, a, b);
+  return sum;
+}
+
+// Symbol.cpp:39-43 and :110-116
+__device__ double cg(const double *f, int j, int m, int j1, int m1, int j2, int m2) {
+  return (((m + j1 - j2) & 1) ? -1.0 : 1.0) * sqrt(2.0 * j + 1.0) * w3j(f, j1, j2, j, m1, m2, -m);
+}
+__device__ double Wf(const double *f, int L1, int J1, int M1, int L2, int J2, int M2, int L, int M) {
+  return (((J2 + L1 + L) & 1) ? -1.0 : 1.0) *
+         sqrt((2.0 * J1 + 1.0) * (2.0 * J2 + 1.0) * (2.0 * L1 + 1.0) * (2.0 * L2 + 1.0) /
+              (4.0 * kPi * (2.0 * L + 1.0))) *
+         w6j(f, L1, L2, L, J2, J1, 1) * cg(f, L, 0, L1, 0, L2, 0) * cg(f, L, M, J1, M1, J2, M2);
+}
+
+__device__ __forceinline__ void nm_of(int p, int &n, int &m) {
+  n = (int)sqrtf((float)(p + 1));
+  while(n * n > p + 1)
+    --n;
+  while((n + 1) * (n + 1) <= p + 1)
+    ++n;
+  m = -(p + 1) + n * (n + 1);
+}
+
+// One CTA per SH harmonic k; threads over (p, m2 fixed by M - m1, n2).
+__global__ void __launch_bounds__(256) k_clg_tables(int nmax, double *out) {
+  __shared__ double f[171];
+  if(threadIdx.x == 0) {
+    f[0] = 1.0;
+    for(int i = 1; i <= 170; ++i)
+      f[i] = f[i - 1] * i;
+  }
+  __syncthreads();
+  const int P = pmax(nmax);
+  const size_t sz = (size_t)P * P * P;
+  const int k = blockIdx.x;
+  int J, M;
+  nm_of(k, J, M);
+  const double s32 = sqrt(3.0 / 2.0 / kPi);
+  for(int idx = threadIdx.x; idx < P * P; idx += blockDim.x) {
+    const int p = idx / P, q = idx - p * P;
+    int J1, M1, J2, M2;
+    nm_of(p, J1, M1);
+    nm_of(q, J2, M2);
+    if(M != M1 + M2)
+      continue;
+    const size_t at = ((size_t)k * P + p) * P + q;
+    const double c = cg(f, J, M, J1, M1, J2, M2);
+    const double jp = sqrt(J / (2.0 * J + 1.0)), jm = sqrt((J + 1) / (2.0 * J + 1.0));
+    const double r2m = sqrt(J2 * (2.0 * J2 - 1.0)), r2p = sqrt((J2 + 1.0) * (2.0 * J2 + 3.0));
+    out[T_C10m1 * sz + at] =
+        s32 * (2.0 * J1 + 1.0) * c *
+        (r2m * w9j(f, J1, J1, 1, J2, J2 - 1, 1, J, J + 1, 1) * cg(f, J + 1, 0, J1, 0, J2 - 1, 0) * jp -
+         r2p * w9j(f, J1, J1, 1, J2, J2 + 1, 1, J, J + 1, 1) * cg(f, J + 1, 0, J1, 0, J2 + 1, 0) * jp +
+         r2m * w9j(f, J1, J1, 1, J2, J2 - 1, 1, J, J - 1, 1) * cg(f, J - 1, 0, J1, 0, J2 - 1, 0) * jm -
+         r2p * w9j(f, J1, J1, 1, J2, J2 + 1, 1, J, J - 1, 1) * cg(f, J - 1, 0, J1, 0, J2 + 1, 0) * jm);
+    const double s_mm = sqrt((J1 + 1.0) * J2 * (2.0 * J1 - 1.0) * (2.0 * J2 - 1.0));
+    const double s_mp = sqrt((J1 + 1.0) * (J2 + 1) * (2.0 * J1 - 1.0) * (2.0 * J2 + 3.0));
+    const double s_pm = sqrt((double)(J1 * J2) * (2.0 * J1 + 3.0) * (2.0 * J2 - 1.0));
+    const double s_pp = sqrt((double)(J1 * (J2 + 1)) * (2.0 * J1 + 3.0) * (2.0 * J2 + 3.0));
+    out[T_C11m1 * sz + at] =
+        s32 * c *
+        (s_mm * w9j(f, J1, J1 - 1, 1, J2, J2 - 1, 1, J, J + 1, 1) * cg(f, J + 1, 0, J1 - 1, 0, J2 - 1, 0) * jp -
+         s_mp * w9j(f, J1, J1 - 1, 1, J2, J2 + 1, 1, J, J + 1, 1) * cg(f, J + 1, 0, J1 - 1, 0, J2 + 1, 0) * jp +
+         s_pm * w9j(f, J1, J1 + 1, 1, J2, J2 - 1, 1, J, J + 1, 1) * cg(f, J + 1, 0, J1 + 1, 0, J2 - 1, 0) * jp -
+         s_pp * w9j(f, J1, J1 + 1, 1, J2, J2 + 1, 1, J, J + 1, 1) * cg(f, J + 1, 0, J1 + 1, 0, J2 + 1, 0) * jp +
+         s_mm * w9j(f, J1, J1 - 1, 1, J2, J2 - 1, 1, J, J - 1, 1) * cg(f, J - 1, 0, J1 - 1, 0, J2 - 1, 0) * jm -
+         s_mp * w9j(f, J1, J1 - 1, 1, J2, J2 + 1, 1, J, J - 1, 1) * cg(f, J - 1, 0, J1 - 1, 0, J2 + 1, 0) * jm +
+         s_pm * w9j(f, J1, J1 + 1, 1, J2, J2 - 1, 1, J, J - 1, 1) * cg(f, J - 1, 0, J1 + 1, 0, J2 - 1, 0) * jm -
+         s_pp * w9j(f, J1, J1 + 1, 1, J2, J2 + 1, 1, J, J - 1, 1) * cg(f, J - 1, 0, J1 + 1, 0, J2 + 1, 0) * jm);
+    out[T_C00m1 * sz + at] =
+        s32 * (2.0 * J1 + 1.0) * c *
+        (r2m * w9j(f, J1, J1, 1, J2, J2 - 1, 1, J, J, 1) * cg(f, J, 0, J1, 0, J2 - 1, 0) -
+         r2p * w9j(f, J1, J1, 1, J2, J2 + 1, 1, J, J, 1) * cg(f, J, 0, J1, 0, J2 + 1, 0));
+    out[T_C01m1 * sz + at] =
+        s32 * c *
+        (s_mm * w9j(f, J1, J1 - 1, 1, J2, J2 - 1, 1, J, J, 1) * cg(f, J, 0, J1 - 1, 0, J2 - 1, 0) -
+         s_mp * w9j(f, J1, J1 - 1, 1, J2, J2 + 1, 1, J, J, 1) * cg(f, J, 0, J1 - 1, 0, J2 + 1, 0) +
+         s_pm * w9j(f, J1, J1 + 1, 1, J2, J2 - 1, 1, J, J, 1) * cg(f, J, 0, J1 + 1, 0, J2 - 1, 0) -
+         s_pp * w9j(f, J1, J1 + 1, 1, J2, J2 + 1, 1, J, J, 1) * cg(f, J, 0, J1 + 1, 0, J2 + 1, 0));
+    const double a1 = sqrt(J1 / (2.0 * J1 + 1.0)), b1 = sqrt((J1 + 1) / (2.0 * J1 + 1.0));
+    const double a2 = sqrt(J2 / (2.0 * J2 + 1.0)), b2 = sqrt((J2 + 1) / (2.0 * J2 + 1.0));
+    out[T_Wm1m1 * sz + at] = a1 * a2 * Wf(f, J1 - 1, J1, M1, J2 - 1, J2, M2, J, M) +
+                             b1 * b2 * Wf(f, J1 + 1, J1, M1, J2 + 1, J2, M2, J, M) -
+                             a1 * b2 * Wf(f, J1 - 1, J1, M1, J2 + 1, J2, M2, J, M) -
+                             b1 * a2 * Wf(f, J1 + 1, J1, M1, J2 - 1, J2, M2, J, M);
+    out[T_W11 * sz + at] = b1 * b2 * Wf(f, J1 - 1, J1, M1, J2 - 1, J2, M2, J, M) +
+                           a1 * a2 * Wf(f, J1 + 1, J1, M1, J2 + 1, J2, M2, J, M) +
+                           b1 * a2 * Wf(f, J1 - 1, J1, M1, J2 + 1, J2, M2, J, M) +
+                           a1 * b2 * Wf(f, J1 + 1, J1, M1, J2 - 1, J2, M2, J, M);
+    out[T_W00 * sz + at] = Wf(f, J1, J1, M1, J2, J2, M2, J, M);
+    out[T_W10 * sz + at] = b1 * Wf(f, J1 - 1, J1, M1, J2, J2, M2, J, M) +
+                           a1 * Wf(f, J1 + 1, J1, M1, J2, J2, M2, J, M);
+    out[T_W01 * sz + at] = b2 * Wf(f, J1, J1, M1, J2 - 1, J2, M2, J, M) +
+                           a2 * Wf(f, J1, J1, M1, J2 + 1, J2, M2, J, M);
+  }
+}
+
+// Per sphere: A_0, A_1, A_m1 of Symbol.cpp:46-64 times conj(internal coefficients)
+// (the solve passes them conjugated, PreconditionedMatrixSolver.h:65-70).
+__global__ void k_sh_vectors(const ShScalars *shs, const zd *Xint, int nmax, zd *vec) {
+  const int j = blockIdx.x, P = pmax(nmax);
+  __shared__ zd J[kMaxNmax + 2], dJ[kMaxNmax + 2];
+  const ShScalars c = shs[j];
+  if(threadIdx.x == 0)
+    bessel_deriv(0, c.R * c.k1, nmax, J, dJ);
+  __syncthreads();
+  const zd I = mk(0.0, 1.0);
+  const zd rk = 1.0 / c.k1;
+  for(int p = threadIdx.x; p < P; p += blockDim.x) {
+    int n, m;
+    nm_of(p, n, m);
+    const zd cc = conj(Xint[(size_t)j * 2 * P + p]), dd = conj(Xint[(size_t)j * 2 * P + P + p]);
+    zd *v = vec + (size_t)j * 3 * P;
+    v[p] = J[n] * cc;
+    v[P + p] = I * rk * (c.k1 * dJ[n] + J[n] / c.R) * dd;
+    v[2 * P + p] = I * sqrt(n * (n + 1.0)) * (rk / c.R) * J[n] * dd;
+  }
+}
+
+// u', v', u'' per (sphere, SH harmonic) and K, K1ana (source_vectorSH, K1ana).
+__global__ void __launch_bounds__(256) k_sh_source(const ShScalars *shs, const zd *vec,
+                                                   const double *tab, const zd *shf, int nmax,
+                                                   zd *K, zd *K1) {
+  extern __shared__ zd sv[];
+  const int j = blockIdx.x, P = pmax(nmax);
+  const size_t sz = (size_t)P * P * P;
+  for(int t = threadIdx.x; t < 3 * P; t += blockDim.x)
+    sv[t] = vec[(size_t)j * 3 * P + t];
+  __syncthreads();
+  const zd *a0 = sv, *a1 = sv + P, *am1 = sv + 2 * P;
+  const ShScalars c = shs[j];
+  for(int k = threadIdx.x; k < P; k += blockDim.x) {
+    int J, M;
+    nm_of(k, J, M);
+    zd up = mk(0, 0), vp = mk(0, 0), gmn = mk(0, 0), fmn = mk(0, 0);
+    for(int p = 0; p < P; ++p) {
+      int n1, m1;
+      nm_of(p, n1, m1);
+      const int m2 = M - m1;
+      if(m2 < -nmax || m2 > nmax)
+        continue;
+      for(int n2 = max(1, abs(m2)); n2 <= nmax; ++n2) {
+        const int q = flat(n2, m2);
+        const size_t at = ((size_t)k * P + p) * P + q;
+        const zd a1am = a1[p] * am1[q], a0am = a0[p] * am1[q];
+        up = up + a1am * tab[T_C10m1 * sz + at] + a0am * tab[T_C11m1 * sz + at];
+        vp = vp + a1am * tab[T_C00m1 * sz + at] + a0am * tab[T_C01m1 * sz + at];
+        gmn = gmn + am1[p] * am1[q] * tab[T_Wm1m1 * sz + at];
+        fmn = fmn + a1[p] * a1[q] * tab[T_W11 * sz + at] + a0[p] * a0[q] * tab[T_W00 * sz + at] +
+              a1[p] * a0[q] * tab[T_W10 * sz + at] + a0[p] * a1[q] * tab[T_W01 * sz + at];
+      }
+    }
+    const double snn = sqrt((double)(J * (J + 1)));
+    const zd u1 = up * c.c_up, v1 = vp * c.c_vp;
+    const zd u2 = (c.c_g1 * snn) * gmn + (c.c_g2 * snn) * (gmn + fmn);
+    const zd *f = shf + ((size_t)j * (nmax + 1) + J) * 8;
+    const size_t o = (size_t)j * 2 * P;
+    K[o + k] = f[0] * v1;               // + T2_TE * v'' (v'' = 0, Geometry.cpp:296)
+    K[o + P + k] = f[1] * u1 + f[3] * u2;
+    K1[o + k] = mk(0.0, 0.0);           // IauxSH2_TE * v''
+    K1[o + P + k] = f[7] * u2;
+  }
+}
+
+// convertInternal_SH (Solver.cpp:95-116)
+__global__ void k_sh_internal(const zd *X, const zd *K1, const zd *shf, int nmax, long n, zd *Xi) {
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(idx >= n)
+    return;
+  const int P = pmax(nmax);
+  const long j = idx / (2 * P);
+  const int r = (int)(idx - j * 2 * P);
+  const int p = r < P ? r : r - P;
+  int nn, mm;
+  nm_of(p, nn, mm);
+  const zd f = shf[((size_t)j * (nmax + 1) + nn) * 8 + (r < P ? 4 : 5)];
+  Xi[idx] = X[idx] * f - K1[idx];
+}
+
+// ACSshcoeff (Symbol.cpp:358-477) per (sphere, SH harmonic): 4-point
+// Gauss-Legendre radial integral.
+__global__ void __launch_bounds__(256) k_sh_abs(const ShScalars *shs, const zd *Xint,
+                                                const zd *Xish, const double *tab, int nmax,
+                                                double omega, zd *acs) {
+  const int j = blockIdx.x, P = pmax(nmax);
+  const size_t sz = (size_t)P * P * P;
+  __shared__ zd d[4][kMaxNmax + 2], dd[4][kMaxNmax + 2], ddd[4][kMaxNmax + 2];
+  __shared__ zd ds[4][kMaxNmax + 2], dds[4][kMaxNmax + 2];
+  const double xi[4] = {-0.3399810435848563, 0.3399810435848563, -0.8611363115940526,
+                        0.8611363115940526};
+  const double wi[4] = {0.6521451548625461, 0.6521451548625461, 0.3478548451374538,
+                        0.3478548451374538};
+  const ShScalars c = shs[j];
+  const double R = c.R;
+  if(threadIdx.x < 4) {
+    const int g = threadIdx.x;
+    const double r = (R / 2.0) * xi[g] + R / 2.0;
+    const zd z = r * c.k1;
+    bessel_deriv(0, z, nmax, d[g], dd[g]);
+    // second derivatives (bessel3der, Bessel.h:145-245)
+    ddd[g][0] = mk(0.0, 0.0);
+    for(int i = 1; i <= nmax; ++i) {
+      ddd[g][i] = -((double(i) / z) * dd[g][i]) + (double(i) / (z * z)) * d[g][i] + dd[g][i - 1];
+      if(z.im == 0.0)
+        ddd[g][i].im = 0.0;
+    }
+    bessel_deriv(0, r * c.kSH, nmax, ds[g], dds[g]);
+  }
+  __syncthreads();
+  const zd k1 = c.k1, rk2 = 1.0 / (k1 * k1);
+  for(int k = threadIdx.x; k < P; k += blockDim.x) {
+    int J, M;
+    nm_of(k, J, M);
+    const double sn = sqrt((double)(J * (J + 1)));
+    const zd cmn = Xish[(size_t)j * 2 * P + k], dmn = Xish[(size_t)j * 2 * P + P + k];
+    zd integral = mk(0.0, 0.0);
+    for(int g = 0; g < 4; ++g) {
+      const double r = (R / 2.0) * xi[g] + R / 2.0;
+      zd Xm1 = mk(0.0, 0.0), Xp1 = mk(0.0, 0.0);
+      if(c.has_gamma) {
+        for(int p = 0; p < P; ++p) {
+          int n1, m1;
+          nm_of(p, n1, m1);
+          const int m2 = M - m1;
+          if(m2 < -nmax || m2 > nmax)
+            continue;
+          const zd c1 = Xint[(size_t)j * 2 * P + p], d1 = Xint[(size_t)j * 2 * P + P + p];
+          for(int n2 = max(1, abs(m2)); n2 <= nmax; ++n2) {
+            const int q = flat(n2, m2);
+            const size_t at = ((size_t)k * P + p) * P + q;
+            const double Wm = tab[T_Wm1m1 * sz + at], W1 = tab[T_W11 * sz + at],
+                         W0 = tab[T_W00 * sz + at];
+            const zd c2 = Xint[(size_t)j * 2 * P + q], d2 = Xint[(size_t)j * 2 * P + P + q];
+            const zd F00 = d[g][n1] * dd[g][n2];
+            const zd F11 = (k1 * dd[g][n2] + d[g][n2] / r) * (k1 * dd[g][n1] + d[g][n1] / r);
+            const zd Fm = (1.0 / (r * r)) * (d[g][n1] * d[g][n2]);
+            const zd Fd00 = d[g][n1] * dd[g][n2] * k1 + k1 * dd[g][n1] * d[g][n2];
+            const zd Fd11 =
+                ((k1 * k1) * ddd[g][n1] - (1.0 / (r * r)) * d[g][n1] + (1.0 / r) * k1 * dd[g][n1]) *
+                    (k1 * dd[g][n2] + d[g][n2] / r) +
+                ((k1 * k1) * ddd[g][n2] - (1.0 / (r * r)) * d[g][n2] + (1.0 / r) * k1 * dd[g][n2]) *
+                    (k1 * dd[g][n1] + d[g][n1] / r);
+            const zd Fdm = (1.0 / (r * r)) * (k1 * dd[g][n1] * d[g][n2] + d[g][n1] * k1 * dd[g][n2]) -
+                           (2.0 / (r * r * r)) * (d[g][n1] * d[g][n2]);
+            const double sq = sqrt((double)(n1 * n2 * (n1 + 1) * (n2 + 1)));
+            Xm1 = Xm1 + c.c_bulk * (c1 * c2 * W0 * Fd00 + d1 * d2 * rk2 * (W1 * Fd11 + Wm * sq * Fdm));
+            Xp1 = Xp1 + c.c_bulk * (c1 * c2 * W0 * sn * (1.0 / r) * F00 +
+                                    d1 * d2 * rk2 * (W1 * sn * (1.0 / r) * F11 + Wm * sq * sn * (1.0 / r) * Fm));
+          }
+        }
+      }
+      const zd w01 = c.w01;
+      const zd rkSH = 1.0 / c.kSH;
+      const zd Xm1SH = w01 * dmn * rkSH * sn * (1.0 / r) * ds[g][J];
+      const zd X0 = -(w01 * cmn * ds[g][J]);
+      const zd Xp1SH = w01 * dmn * rkSH * ((1.0 / r) * ds[g][J] + dds[g][J]);
+      const zd a = Xm1 + Xm1SH, b = Xp1 + Xp1SH;
+      integral = integral + wi[g] * (r * r) * (a * conj(a) + X0 * conj(X0) + b * conj(b));
+    }
+    acs[(size_t)j * P + k] = integral * (R / 2.0);
+  }
+}
+
+// C_sca_SH (Result.cpp:662-745) and C_abs_SH (Result.cpp:747-778): one CTA,
+// fixed-order reductions.
+__global__ void __launch_bounds__(256) k_sh_xsec(const ShScalars *shs, const zd *X, const double *w,
+                                                 const zd *acs, int N, int nmax, double arbcf,
+                                                 zd eta, double *out) {
+  __shared__ double red[2][256];
+  const int P = pmax(nmax);
+  double s = 0.0, a = 0.0;
+  for(long idx = threadIdx.x; idx < (long)N * P; idx += blockDim.x) {
+    const long j = idx / P;
+    const int p = (int)(idx - j * P);
+    s += w[j * P + p] * (norm2(X[j * 2 * P + p]) + norm2(X[j * 2 * P + P + p]));
+  }
+  for(int j = threadIdx.x; j < N; j += blockDim.x) {
+    zd sum = mk(0.0, 0.0);
+    for(int k = 0; k < P; ++k)
+      sum = sum + acs[(size_t)j * P + k];
+    a += ((2.0 * eta) * 0.5 * shs[j].sigma * sum).re;
+  }
+  red[0][threadIdx.x] = s;
+  red[1][threadIdx.x] = a;
+  __syncthreads();
+  for(int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if(threadIdx.x < st) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + st];
+      red[1][threadIdx.x] += red[1][threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) {
+    out[0] = (1.0 / (4.0 * arbcf)) * red[0][0];
+    out[1] = red[1][0];
+  }
+}
+
+}  // namespace
+
+const double *clg_tables_dev(om_context *ctx, int nmax) {
+  for(auto &t : ctx->clg)
+    if(t.first == nmax)
+      return t.second;
+  const size_t P = pmax(nmax), count = 9 * P * P * P;
+  double *d = nullptr;
+  if(ctx->budget && ctx->used + count * sizeof(double) > ctx->budget)
+    throw std::runtime_error("device-memory budget exceeded by the SH coupling tables");
+  if(cudaMalloc(&d, count * sizeof(double)) != cudaSuccess)
+    throw std::runtime_error("cudaMalloc failed for the SH coupling tables");
+  ctx->used += count * sizeof(double);
+  cudaMemsetAsync(d, 0, count * sizeof(double), ctx->stream);
+  k_clg_tables<<<(unsigned)P, 256, 0, ctx->stream>>>(nmax, d);
+  ctx->last_launches++;
+  ctx->clg.push_back({nmax, d});
+  return d;
+}
+
+void launch_sh_source(om_problem *pr) {
+  om_context *ctx = pr->ctx;
+  const double *tab = clg_tables_dev(ctx, pr->nmax);
+  const int P = pr->P;
+  k_sh_vectors<<<pr->N, 128, 0, ctx->stream>>>(pr->d_shs, pr->d_Xint, pr->nmax, pr->d_shvec);
+  k_sh_source<<<pr->N, 256, 3 * P * sizeof(zd), ctx->stream>>>(pr->d_shs, pr->d_shvec, tab,
+                                                               pr->d_shf, pr->nmax, pr->d_K,
+                                                               pr->d_K1);
+  ctx->last_launches += 2;
+}
+
+void launch_sh_internal(om_problem *pr) {
+  k_sh_internal<<<blocks_for(pr->n, 256), 256, 0, pr->ctx->stream>>>(
+      pr->d_Xsh, pr->d_K1, pr->d_shf, pr->nmax, pr->n, pr->d_Xish);
+  pr->ctx->last_launches++;
+}
+
+void launch_sh_cross_sections(om_problem *pr, double *d_out2) {
+  om_context *ctx = pr->ctx;
+  const double *tab = clg_tables_dev(ctx, pr->nmax);
+  launch_sh_weights(pr);
+  k_sh_abs<<<pr->N, 256, 0, ctx->stream>>>(pr->d_shs, pr->d_Xint, pr->d_Xish, tab, pr->nmax,
+                                           pr->omega, pr->d_acs);
+  const double arbcf = pr->bg_eps_r.real() * pr->bg_mu_r.real();
+  k_sh_xsec<<<1, 256, 0, ctx->stream>>>(pr->d_shs, pr->d_Xsh, pr->d_wsh, pr->d_acs, pr->N, pr->nmax,
+                                        arbcf, mk(pr->eta.real(), pr->eta.imag()), d_out2);
+  ctx->last_launches += 2;
+}
+
+}  // namespace om

@@ -595,6 +595,7 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
 struct SourceArgs {
   const double *cart;
   const zd *T;
+  int weights_only;  // 1: only the C_sca weights (SH cross section at 2k)
   const zd *inc;  // 2P
   const double *rec, *qf, *pf, *legc;
   zd waveK;
@@ -623,8 +624,10 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
   const bool at_origin = fabs(s.geo[0]) < 1e-10;  // Coupling.cpp:82-84: A = I, B = 0
   if(at_origin) {
     if(t < P) {
-      te = a.inc[t];
-      tm = a.inc[P + t];
+      if(!a.weights_only) {
+        te = a.inc[t];
+        tm = a.inc[P + t];
+      }
       w = 1.0;
     }
   } else {
@@ -635,7 +638,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
       __syncthreads();
       const int base = n_lo * n_lo - 1;
       const int qend = (n_hi + 1) * (n_hi + 1) - 1;
-      if(t < P) {
+      if(t < P && !a.weights_only) {
         for(int q = base; q < qend; ++q) {  // IncLocal[p] = sum_q A(q,p) a_q + B(q,p) b_q
           zd A, B;
           coupling_entry(s, y, base, q, t, A, B);
@@ -653,7 +656,9 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
       __syncthreads();
     }
   }
-  if(t < P) {
+  if(t < P && a.weights_only) {
+    a.wsca[(size_t)i * P + t] = w;
+  } else if(t < P) {
     const size_t o = (size_t)i * 2 * P;
     const int l = (int)s.pf[t * kPfacStride + 6];
     a.incloc[o + t] = te;
@@ -712,7 +717,7 @@ __global__ void __launch_bounds__(256) k_coupling(CouplingArgs a, Layout y) {
 // Per sphere and n: T-matrix (FF, SH), internal factors and the Mie
 // absorption factors (Scatterer.cpp:39-271, Geometry.cpp:86-145).
 __global__ void k_sphere_terms(const SphereScalars *sc, int N, int nmax, zd *T, zd *Tsh, zd *iaux,
-                               double *cabs_out) {
+                               double *cabs_out, zd *shf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= N)
     return;
@@ -741,6 +746,25 @@ __global__ void k_sphere_terms(const SphereScalars *sc, int N, int nmax, zd *T, 
               (rho * dksi / ksi - mu_sob * dpsirho / psirho);
       Tout[2 * n] = TE;
       Tout[2 * n + 1] = TM;
+      if(h == 1 && shf) {
+        // getTLocalSH1_outer / SH2_outer / getIauxSH1 / getIauxSH2 (Scatterer.cpp:163-412)
+        const zd x_b2 = c.x_b2, x_i2 = c.x_i2, z = c.zeta;
+        zd *f = shf + ((size_t)i * (nmax + 1) + n) * 8;
+        const zd den_te = z * ksi * dpsirho - psirho * dksi;
+        const zd den_tm = z * psirho * dksi - ksi * dpsirho;
+        f[0] = -(x_b2 * psirho) / den_te;
+        f[1] = -(x_b2 * dpsirho) / den_tm;
+        f[2] = z * x_b2 * dpsirho / den_te;
+        f[3] = z * x_b2 * psirho / den_tm;
+        const zd i1te = (-x_i2 * ksi) / (x_b2 * psirho);
+        const zd i1tm = (-x_i2 * dksi) / (x_b2 * dpsirho);
+        f[4] = i1te;
+        f[5] = i1tm;
+        const zd bnpp = (z * x_b2 * dpsirho) / den_te;
+        const zd anpp = (z * x_b2 * psirho) / den_tm;
+        f[6] = bnpp * ((-x_i2 * ksi) / (x_b2 * psirho) + (x_i2 * dksi) / (z * x_b2 * dpsirho));
+        f[7] = anpp * ((-x_i2 * dksi) / (x_b2 * dpsirho) + (x_i2 * ksi) / (z * x_b2 * psirho));
+      }
       if(h == 0) {
         const zd mu_j = c.mu_j, mu_0 = c.mu_0, I = mk(0.0, 1.0);
         zd ia_te = (mu_j * rho) / (mu_0 * rho * dpsirho * psi - mu_j * psirho * dpsi) * I;
@@ -900,7 +924,7 @@ const CoefTables &coef_tables(om_context *ctx, int nmax) {
 
 void launch_sphere_terms(om_problem *pr) {
   k_sphere_terms<<<blocks_for(pr->N, 64), 64, 0, pr->ctx->stream>>>(
-      pr->d_scal, pr->N, pr->nmax, pr->d_T, pr->d_Tsh, pr->d_iaux, pr->d_cabs);
+      pr->d_scal, pr->N, pr->nmax, pr->d_T, pr->d_Tsh, pr->d_iaux, pr->d_cabs, pr->d_shf);
   pr->ctx->last_launches++;
 }
 
@@ -959,6 +983,33 @@ void launch_source(om_problem *pr) {
   a.incloc = pr->d_incloc;
   a.Q = pr->d_Q;
   a.wsca = pr->d_wsca;
+  a.weights_only = 0;
+  fill_chunks(a, y);
+  set_smem(k_source, y.bytes);
+  k_source<<<pr->N, 256, y.bytes, ctx->stream>>>(a, y);
+  ctx->last_launches++;
+}
+
+// Per-sphere weights sum_p |T^reg_pq(2k)|^2 of getScatteringCrossSection_SH
+// (Result.cpp:662-745): the regular translation at twice the wave number.
+void launch_sh_weights(om_problem *pr) {
+  om_context *ctx = pr->ctx;
+  const CoefTables &ct = coef_tables(ctx, pr->nmax);
+  Layout y = make_layout(pr->nmax, smem_limit());
+  SourceArgs a;
+  a.cart = pr->d_cart;
+  a.T = pr->d_T;
+  a.inc = nullptr;
+  a.rec = ct.rec;
+  a.qf = ct.qf;
+  a.pf = ct.pf;
+  a.legc = ct.legc;
+  const cplx k2 = 2.0 * pr->waveK;
+  a.waveK = mk(k2.real(), k2.imag());
+  a.incloc = nullptr;
+  a.Q = nullptr;
+  a.wsca = pr->d_wsh;
+  a.weights_only = 1;
   fill_chunks(a, y);
   set_smem(k_source, y.bytes);
   k_source<<<pr->N, 256, y.bytes, ctx->stream>>>(a, y);

@@ -528,6 +528,7 @@ void aux_coefficients(Sph R, cplx waveK, bool regular, int nMax, Aux &out, bool 
 struct Medium {  // ElectroMagnetic::init_r (ElectroMagnetic.cpp:18-37)
   cplx epsilon_r, mu_r, epsilon_r_SH;
   cplx epsilon, mu, epsilon_SH, mu_SH;
+  cplx ksippp, ksiparppar, gamma;  // surface and bulk chi(2) coefficients
   void init(cplx er, cplx mr, cplx er_sh) {
     epsilon_r = er;
     mu_r = mr;
@@ -982,6 +983,372 @@ void eh_fields(const Problem &pr, const cplx *sca, const cplx *intc, Sph R, Vec3
   H = {Hi.x + Hf.x, Hi.y + Hf.y, Hi.z + Hf.z};
 }
 
+
+// ---------------------------------------------------------------------------
+// Second harmonic. Wigner symbols restated from their Racah formulas with the
+// semantics of GSL's gsl_sf_coupling_3j/6j/9j (zero outside the triangle and
+// projection rules), then the tables of Symbol.cpp:1036-1451, the source terms
+// u', v', u'' of Symbol.cpp:155-353 and their assembly (Geometry.cpp:250-310,
+// PreconditionedMatrix.cpp:1347-1436), the SH outer / internal factors
+// (Scatterer.cpp:163-412), convertInternal_SH (Solver.cpp:95-116), the SH
+// cross sections (Result.cpp:662-778, Symbol.cpp:358-477).
+// ---------------------------------------------------------------------------
+double fact(int n) {
+  static std::vector<double> f = [] {
+    std::vector<double> v(171, 1.0);
+    for(int i = 1; i <= 170; ++i)
+      v[i] = v[i - 1] * i;
+    return v;
+  }();
+  return n < 0 ? 0.0 : f[n];
+}
+bool triangle(int a, int b, int c) { return c >= std::abs(a - b) && c <= a + b; }
+
+double wigner3j(int j1, int j2, int j3, int m1, int m2, int m3) {
+  if(j1 < 0 || j2 < 0 || j3 < 0 || !triangle(j1, j2, j3) || m1 + m2 + m3 != 0 ||
+     std::abs(m1) > j1 || std::abs(m2) > j2 || std::abs(m3) > j3)
+    return 0.0;
+  double delta = std::sqrt(fact(j1 + j2 - j3) * fact(j1 - j2 + j3) * fact(-j1 + j2 + j3) /
+                           fact(j1 + j2 + j3 + 1));
+  double pre = std::sqrt(fact(j1 + m1) * fact(j1 - m1) * fact(j2 + m2) * fact(j2 - m2) *
+                         fact(j3 + m3) * fact(j3 - m3));
+  int kmin = std::max({0, j2 - j3 - m1, j1 - j3 + m2});
+  int kmax = std::min({j1 + j2 - j3, j1 - m1, j2 + m2});
+  double sum = 0.0;
+  for(int k = kmin; k <= kmax; ++k) {
+    double den = fact(k) * fact(j3 - j2 + k + m1) * fact(j3 - j1 + k - m2) * fact(j1 + j2 - j3 - k) *
+                 fact(j1 - k - m1) * fact(j2 - k + m2);
+    sum += ((k & 1) ? -1.0 : 1.0) / den;
+  }
+  int ph = j1 - j2 - m3;
+  return ((ph & 1) ? -1.0 : 1.0) * delta * pre * sum;
+}
+
+double tri_delta(int a, int b, int c) {
+  return std::sqrt(fact(a + b - c) * fact(a - b + c) * fact(-a + b + c) / fact(a + b + c + 1));
+}
+
+double wigner6j(int j1, int j2, int j3, int j4, int j5, int j6) {
+  if(j1 < 0 || j2 < 0 || j3 < 0 || j4 < 0 || j5 < 0 || j6 < 0)
+    return 0.0;
+  if(!triangle(j1, j2, j3) || !triangle(j1, j5, j6) || !triangle(j4, j2, j6) ||
+     !triangle(j4, j5, j3))
+    return 0.0;
+  int a1 = j1 + j2 + j3, a2 = j1 + j5 + j6, a3 = j4 + j2 + j6, a4 = j4 + j5 + j3;
+  int b1 = j1 + j2 + j4 + j5, b2 = j2 + j3 + j5 + j6, b3 = j3 + j1 + j6 + j4;
+  int tmin = std::max({a1, a2, a3, a4}), tmax = std::min({b1, b2, b3});
+  double sum = 0.0;
+  for(int t = tmin; t <= tmax; ++t) {
+    double den = fact(t - a1) * fact(t - a2) * fact(t - a3) * fact(t - a4) * fact(b1 - t) *
+                 fact(b2 - t) * fact(b3 - t);
+    sum += ((t & 1) ? -1.0 : 1.0) * fact(t + 1) / den;
+  }
+  return tri_delta(j1, j2, j3) * tri_delta(j1, j5, j6) * tri_delta(j4, j2, j6) *
+         tri_delta(j4, j5, j3) * sum;
+}
+
+double wigner9j(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
+  if(a < 0 || b < 0 || c < 0 || d < 0 || e < 0 || f < 0 || g < 0 || h < 0 || i < 0)
+    return 0.0;
+  int xmin = std::max({std::abs(a - i), std::abs(h - d), std::abs(b - f)});
+  int xmax = std::min({a + i, h + d, b + f});
+  double sum = 0.0;
+  for(int x = xmin; x <= xmax; ++x)
+    sum += (2 * x + 1) * wigner6j(a, d, g, h, i, x) * wigner6j(b, e, h, d, x, f) *
+           wigner6j(c, f, i, x, a, b);
+  return sum;
+}
+
+// Symbol.cpp:39-43
+double clegor(int j, int m, int j1, int m1, int j2, int m2) {
+  return std::pow(-1.0, m + j1 - j2) * std::sqrt(2.0 * j + 1.0) * wigner3j(j1, j2, j, m1, m2, -m);
+}
+// Symbol.cpp:110-116
+double Wfun(int L1, int J1, int M1, int L2, int J2, int M2, int L, int M) {
+  return std::pow(-1.0, J2 + L1 + L) *
+         std::sqrt((2.0 * J1 + 1.0) * (2.0 * J2 + 1.0) * (2.0 * L1 + 1.0) * (2.0 * L2 + 1.0) /
+                   (4.0 * kPi * (2.0 * L + 1.0))) *
+         wigner6j(L1, L2, L, J2, J1, 1) * clegor(L, 0, L1, 0, L2, 0) * clegor(L, M, J1, M1, J2, M2);
+}
+
+// The nine tables [k][p][q] (k over SH harmonics, p, q over FF harmonics).
+enum { T_C10m1, T_C11m1, T_C00m1, T_C01m1, T_Wm1m1, T_W11, T_W00, T_W10, T_W01 };
+void clg_tables(int nMax, int nMaxS, std::vector<double> &out) {
+  const int P = pmax(nMax), PS = pmax(nMaxS);
+  const size_t sz = size_t(PS) * P * P;
+  out.assign(9 * sz, 0.0);
+  auto nm = [](int p, int &n, int &m) {
+    n = (int)std::sqrt(p + 1.0);
+    m = -(p + 1) + n * (n + 1);
+  };
+  const double s32 = std::sqrt(3.0 / 2.0 / kPi);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(g_threads)
+  for(int k = 0; k < PS; ++k) {
+    int J, M;
+    nm(k, J, M);
+    for(int p = 0; p < P; ++p) {
+      int J1, M1;
+      nm(p, J1, M1);
+      for(int q = 0; q < P; ++q) {
+        int J2, M2;
+        nm(q, J2, M2);
+        if(M != M1 + M2)
+          continue;  // every table carries CleGor(J, M, J1, M1, J2, M2) = 0 here
+        const size_t at = (size_t(k) * P + p) * P + q;
+        const double cg = clegor(J, M, J1, M1, J2, M2);
+        out[T_C10m1 * sz + at] =
+            s32 * (2.0 * J1 + 1.0) * cg *
+            (std::sqrt(J2 * (2.0 * J2 - 1.0)) * wigner9j(J1, J1, 1, J2, J2 - 1, 1, J, J + 1, 1) *
+                 clegor(J + 1, 0, J1, 0, J2 - 1, 0) * std::sqrt(J / (2.0 * J + 1.0)) -
+             std::sqrt((J2 + 1.0) * (2.0 * J2 + 3.0)) * wigner9j(J1, J1, 1, J2, J2 + 1, 1, J, J + 1, 1) *
+                 clegor(J + 1, 0, J1, 0, J2 + 1, 0) * std::sqrt(J / (2.0 * J + 1.0)) +
+             std::sqrt(J2 * (2.0 * J2 - 1.0)) * wigner9j(J1, J1, 1, J2, J2 - 1, 1, J, J - 1, 1) *
+                 clegor(J - 1, 0, J1, 0, J2 - 1, 0) * std::sqrt((J + 1.0) / (2.0 * J + 1.0)) -
+             std::sqrt((J2 + 1) * (2.0 * J2 + 3.0)) * wigner9j(J1, J1, 1, J2, J2 + 1, 1, J, J - 1, 1) *
+                 clegor(J - 1, 0, J1, 0, J2 + 1, 0) * std::sqrt((J + 1) / (2.0 * J + 1.0)));
+        const double jp = std::sqrt(J / (2.0 * J + 1.0)), jm = std::sqrt((J + 1) / (2.0 * J + 1.0));
+        const double s_mm = std::sqrt((J1 + 1.0) * J2 * (2.0 * J1 - 1.0) * (2.0 * J2 - 1.0));
+        const double s_mp = std::sqrt((J1 + 1.0) * (J2 + 1) * (2.0 * J1 - 1.0) * (2.0 * J2 + 3.0));
+        const double s_pm = std::sqrt(J1 * J2 * (2.0 * J1 + 3.0) * (2.0 * J2 - 1.0));
+        const double s_pp = std::sqrt(J1 * (J2 + 1) * (2.0 * J1 + 3.0) * (2.0 * J2 + 3.0));
+        out[T_C11m1 * sz + at] =
+            s32 * cg *
+            (s_mm * wigner9j(J1, J1 - 1, 1, J2, J2 - 1, 1, J, J + 1, 1) *
+                 clegor(J + 1, 0, J1 - 1, 0, J2 - 1, 0) * jp -
+             s_mp * wigner9j(J1, J1 - 1, 1, J2, J2 + 1, 1, J, J + 1, 1) *
+                 clegor(J + 1, 0, J1 - 1, 0, J2 + 1, 0) * jp +
+             s_pm * wigner9j(J1, J1 + 1, 1, J2, J2 - 1, 1, J, J + 1, 1) *
+                 clegor(J + 1, 0, J1 + 1, 0, J2 - 1, 0) * jp -
+             s_pp * wigner9j(J1, J1 + 1, 1, J2, J2 + 1, 1, J, J + 1, 1) *
+                 clegor(J + 1, 0, J1 + 1, 0, J2 + 1, 0) * jp +
+             s_mm * wigner9j(J1, J1 - 1, 1, J2, J2 - 1, 1, J, J - 1, 1) *
+                 clegor(J - 1, 0, J1 - 1, 0, J2 - 1, 0) * jm -
+             s_mp * wigner9j(J1, J1 - 1, 1, J2, J2 + 1, 1, J, J - 1, 1) *
+                 clegor(J - 1, 0, J1 - 1, 0, J2 + 1, 0) * jm +
+             s_pm * wigner9j(J1, J1 + 1, 1, J2, J2 - 1, 1, J, J - 1, 1) *
+                 clegor(J - 1, 0, J1 + 1, 0, J2 - 1, 0) * jm -
+             s_pp * wigner9j(J1, J1 + 1, 1, J2, J2 + 1, 1, J, J - 1, 1) *
+                 clegor(J - 1, 0, J1 + 1, 0, J2 + 1, 0) * jm);
+        out[T_C00m1 * sz + at] =
+            s32 * (2.0 * J1 + 1.0) * cg *
+            (std::sqrt(J2 * (2.0 * J2 - 1.0)) * wigner9j(J1, J1, 1, J2, J2 - 1, 1, J, J, 1) *
+                 clegor(J, 0, J1, 0, J2 - 1, 0) -
+             std::sqrt((J2 + 1.0) * (2.0 * J2 + 3.0)) * wigner9j(J1, J1, 1, J2, J2 + 1, 1, J, J, 1) *
+                 clegor(J, 0, J1, 0, J2 + 1, 0));
+        out[T_C01m1 * sz + at] =
+            s32 * cg *
+            (s_mm * wigner9j(J1, J1 - 1, 1, J2, J2 - 1, 1, J, J, 1) * clegor(J, 0, J1 - 1, 0, J2 - 1, 0) -
+             std::sqrt((J1 + 1.0) * (J2 + 1.0) * (2.0 * J1 - 1.0) * (2.0 * J2 + 3.0)) *
+                 wigner9j(J1, J1 - 1, 1, J2, J2 + 1, 1, J, J, 1) * clegor(J, 0, J1 - 1, 0, J2 + 1, 0) +
+             s_pm * wigner9j(J1, J1 + 1, 1, J2, J2 - 1, 1, J, J, 1) * clegor(J, 0, J1 + 1, 0, J2 - 1, 0) -
+             s_pp * wigner9j(J1, J1 + 1, 1, J2, J2 + 1, 1, J, J, 1) * clegor(J, 0, J1 + 1, 0, J2 + 1, 0));
+        const double a1 = std::sqrt(J1 / (2.0 * J1 + 1.0)), b1 = std::sqrt((J1 + 1) / (2.0 * J1 + 1.0));
+        const double a2 = std::sqrt(J2 / (2.0 * J2 + 1.0)), b2 = std::sqrt((J2 + 1) / (2.0 * J2 + 1.0));
+        out[T_Wm1m1 * sz + at] = a1 * a2 * Wfun(J1 - 1, J1, M1, J2 - 1, J2, M2, J, M) +
+                                 b1 * b2 * Wfun(J1 + 1, J1, M1, J2 + 1, J2, M2, J, M) -
+                                 a1 * b2 * Wfun(J1 - 1, J1, M1, J2 + 1, J2, M2, J, M) -
+                                 b1 * a2 * Wfun(J1 + 1, J1, M1, J2 - 1, J2, M2, J, M);
+        out[T_W11 * sz + at] = b1 * b2 * Wfun(J1 - 1, J1, M1, J2 - 1, J2, M2, J, M) +
+                               a1 * a2 * Wfun(J1 + 1, J1, M1, J2 + 1, J2, M2, J, M) +
+                               b1 * a2 * Wfun(J1 - 1, J1, M1, J2 + 1, J2, M2, J, M) +
+                               a1 * b2 * Wfun(J1 + 1, J1, M1, J2 - 1, J2, M2, J, M);
+        out[T_W00 * sz + at] = Wfun(J1, J1, M1, J2, J2, M2, J, M);
+        out[T_W10 * sz + at] = b1 * Wfun(J1 - 1, J1, M1, J2, J2, M2, J, M) +
+                               a1 * Wfun(J1 + 1, J1, M1, J2, J2, M2, J, M);
+        out[T_W01 * sz + at] = b2 * Wfun(J1, J1, M1, J2 - 1, J2, M2, J, M) +
+                               a2 * Wfun(J1, J1, M1, J2 + 1, J2, M2, J, M);
+      }
+    }
+  }
+}
+
+// SH per-sphere factors of Scatterer.cpp:163-412, per degree n:
+// T1 (TE, TM), T2 (TE, TM), IauxSH1 (TE, TM), IauxSH2 (TE, TM).
+struct ShFactors {
+  std::vector<cplx> t1te, t1tm, t2te, t2tm, i1te, i1tm, i2te, i2tm;
+};
+ShFactors sh_factors(const Problem &pr, const Sphere &s) {
+  int nmax = pr.nmax;
+  double w = pr.omega();
+  cplx k_s = 2.0 * w * std::sqrt(s.elmag.epsilon_SH * s.elmag.mu_SH);
+  cplx k_b = 2.0 * w * std::sqrt(pr.bground.epsilon * pr.bground.mu);
+  cplx rho = k_s / k_b, r_0 = k_b * s.radius;
+  cplx x_b2 = k_b * s.radius, x_i2 = k_s * s.radius;
+  cplx zeta_b2 = std::sqrt(pr.bground.mu / pr.bground.epsilon);
+  cplx zeta_j2 = std::sqrt(s.elmag.mu_SH / s.elmag.epsilon_SH);
+  cplx z = zeta_b2 / zeta_j2;
+  auto rb = riccati(r_0, rho, nmax, true);
+  ShFactors f;
+  for(auto *v : {&f.t1te, &f.t1tm, &f.t2te, &f.t2tm, &f.i1te, &f.i1tm, &f.i2te, &f.i2tm})
+    v->assign(nmax + 1, 0.0);
+  for(int n = 1; n <= nmax; ++n) {
+    const Riccati &R = rb[n];
+    f.t1te[n] = -x_b2 * R.psirho / (z * R.ksi * R.dpsirho - R.psirho * R.dksi);
+    f.t1tm[n] = -x_b2 * R.dpsirho / (z * R.psirho * R.dksi - R.ksi * R.dpsirho);
+    f.t2te[n] = z * x_b2 * R.dpsirho / (z * R.ksi * R.dpsirho - R.psirho * R.dksi);
+    f.t2tm[n] = z * x_b2 * R.psirho / (z * R.psirho * R.dksi - R.ksi * R.dpsirho);
+    f.i1te[n] = (-x_i2 * R.ksi) / (x_b2 * R.psirho);
+    f.i1tm[n] = (-x_i2 * R.dksi) / (x_b2 * R.dpsirho);
+    cplx bnpp = (z * x_b2 * R.dpsirho) / (z * R.ksi * R.dpsirho - R.psirho * R.dksi);
+    cplx anpp = (z * x_b2 * R.psirho) / (z * R.psirho * R.dksi - R.ksi * R.dpsirho);
+    f.i2te[n] = bnpp * ((-x_i2 * R.ksi) / (x_b2 * R.psirho) + (x_i2 * R.dksi) / (z * x_b2 * R.dpsirho));
+    f.i2tm[n] = anpp * ((-x_i2 * R.dksi) / (x_b2 * R.dpsirho) + (x_i2 * R.ksi) / (z * x_b2 * R.psirho));
+  }
+  return f;
+}
+
+// u', v', u'' for one sphere (Symbol.cpp:155-353), with Xi = the FF internal
+// coefficients the reference passes in (the conjugated ones for the source).
+// out: [v' | u' | v''=0 | u''], P_S each (Geometry.cpp:250-310).
+void sh_inc_local(const Problem &pr, int j, const std::vector<double> &tab, const cplx *Xi,
+                  cplx *out) {
+  const Sphere &s = pr.objects[j];
+  const int nmax = pr.nmax, P = pmax(nmax), PS = P;
+  const size_t sz = size_t(PS) * P * P;
+  const double w = pr.omega(), R = s.radius;
+  const cplx k1 = w * std::sqrt(s.elmag.epsilon * s.elmag.mu);
+  std::vector<cplx> J, dJ;
+  bessel(kBessel, R * k1, nmax, J, dJ);
+  std::vector<cplx> a0(P), a1(P), am1(P);
+  const cplx I(0.0, 1.0);
+  for(int p = 0; p < P; ++p) {
+    int n = (int)std::sqrt(p + 1.0);
+    cplx c = Xi[size_t(j) * 2 * P + p], d = Xi[P + size_t(j) * 2 * P + p];
+    a0[p] = J[n] * c;                                                        // A_0
+    a1[p] = I * (1.0 / k1) * (k1 * dJ[n] + J[n] / R) * d;                    // A_1
+    am1[p] = I * std::sqrt(n * (n + 1.0)) * (1.0 / k1 / R) * J[n] * d;       // A_m1
+  }
+  const cplx mu_0 = kMu0, eps_0 = kEps0, mu_b = pr.bground.mu, eps_b = pr.bground.epsilon;
+  const cplx imp = std::sqrt(mu_b / eps_b) / std::sqrt(mu_0 / eps_0);
+  const cplx waveK_01 = w * std::sqrt(eps_0 * mu_0);
+  for(int k = 0; k < PS; ++k) {
+    int n = (int)std::sqrt(k + 1.0);
+    cplx up(0, 0), vp(0, 0), gmn(0, 0), fmn(0, 0);
+    for(int p = 0; p < P; ++p)
+      for(int q = 0; q < P; ++q) {
+        const size_t at = (size_t(k) * P + p) * P + q;
+        up += a1[p] * am1[q] * tab[T_C10m1 * sz + at] + a0[p] * am1[q] * tab[T_C11m1 * sz + at];
+        vp += a1[p] * am1[q] * tab[T_C00m1 * sz + at] + a0[p] * am1[q] * tab[T_C01m1 * sz + at];
+        gmn += am1[p] * am1[q] * tab[T_Wm1m1 * sz + at];
+        fmn += a1[p] * a1[q] * tab[T_W11 * sz + at] + a0[p] * a0[q] * tab[T_W00 * sz + at] +
+               a1[p] * a0[q] * tab[T_W10 * sz + at] + a0[p] * a1[q] * tab[T_W01 * sz + at];
+      }
+    out[k + P] = up * cplx(2.0, 0.0) * I * s.elmag.ksiparppar * imp;
+    out[k] = vp * cplx(2.0, 0.0) * s.elmag.ksiparppar * imp;
+    out[k + 2 * P] = 0.0;
+    out[k + 3 * P] = I * s.elmag.ksippp * std::sqrt(n * (n + 1)) * gmn / waveK_01 / R +
+                     I * s.elmag.gamma * (eps_0 / s.elmag.epsilon_SH) * std::sqrt(n * (n + 1)) *
+                         (gmn + fmn) / waveK_01 / R;
+  }
+}
+
+// Second-derivative sequence of bessel3der (Bessel.h:145-245) for j_n.
+std::vector<cplx> bessel_dd(cplx z, int L) {
+  std::vector<cplx> d, dd, ddd(L + 1, 0.0);
+  bessel(kBessel, z, L, d, dd);
+  if(std::abs(z) > kTol)
+    for(int i = 1; i <= L; ++i)
+      ddd[i] = cplx(-1.0, 0.0) * ((double)i / z) * dd[i] + ((double)i / std::pow(z, 2.0)) * d[i] +
+               dd[i - 1];
+  if(z.imag() == 0.0)
+    for(int i = 1; i <= L; ++i)
+      ddd[i] = ddd[i].real();
+  return ddd;
+}
+
+
+// K and K1ana (source_vectorSH, source_vectorSH_K1ana; PreconditionedMatrix.cpp:1347-1436)
+// from the FF internal coefficients; the solve passes them conjugated
+// (PreconditionedMatrixSolver.h:65-70).
+void sh_source(const Problem &pr, const std::vector<double> &tab, const cplx *X_int, cplx *K,
+               cplx *K1ana) {
+  const int N = (int)pr.objects.size(), P = pmax(pr.nmax);
+  std::vector<cplx> xc(size_t(N) * 2 * P);
+  for(size_t i = 0; i < xc.size(); ++i)
+    xc[i] = std::conj(X_int[i]);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(g_threads)
+  for(int j = 0; j < N; ++j) {
+    std::vector<cplx> ana(4 * P);
+    sh_inc_local(pr, j, tab, xc.data(), ana.data());
+    ShFactors f = sh_factors(pr, pr.objects[j]);
+    for(int p = 0; p < P; ++p) {
+      int n = (int)std::sqrt(p + 1.0);
+      const size_t o = size_t(j) * 2 * P;
+      K[o + p] = f.t1te[n] * ana[p] + f.t2te[n] * ana[2 * P + p];
+      K[o + P + p] = f.t1tm[n] * ana[P + p] + f.t2tm[n] * ana[3 * P + p];
+      K1ana[o + p] = f.i2te[n] * ana[2 * P + p];
+      K1ana[o + P + p] = f.i2tm[n] * ana[3 * P + p];
+    }
+  }
+}
+
+// ACSshcoeff (Symbol.cpp:358-477) for harmonic kk of sphere j.
+cplx acs_sh(const Problem &pr, int j, int kk, const std::vector<double> &tab, const cplx *Xi,
+            cplx cmnSH, cplx dmnSH) {
+  const Sphere &s = pr.objects[j];
+  const int nmax = pr.nmax, P = pmax(nmax);
+  const size_t sz = size_t(P) * P * P;
+  const int n = (int)std::sqrt(kk + 1.0);
+  const double R = s.radius, w = pr.omega();
+  const cplx eps_0 = kEps0, mu_0 = kMu0, gamma = s.elmag.gamma, eps_j2 = s.elmag.epsilon_SH,
+             mu_j2 = s.elmag.mu_SH;
+  const cplx waveK_01 = w * std::sqrt(eps_0 * mu_0);
+  const cplx k1 = w * std::sqrt(s.elmag.epsilon * s.elmag.mu);
+  const cplx kSH = 2.0 * w * std::sqrt(eps_j2 * mu_j2);
+  const double xi[4] = {-0.3399810435848563, 0.3399810435848563, -0.8611363115940526,
+                        0.8611363115940526};
+  const double wi[4] = {0.6521451548625461, 0.6521451548625461, 0.3478548451374538,
+                        0.3478548451374538};
+  cplx integral(0.0, 0.0);
+  for(int ii = 0; ii < 4; ++ii) {
+    const double r = (R / 2.0) * xi[ii] + R / 2.0;
+    std::vector<cplx> d, dd;
+    bessel(kBessel, r * k1, nmax, d, dd);
+    std::vector<cplx> ddd = bessel_dd(r * k1, nmax);
+    cplx Xm1(0, 0), Xp1(0, 0);
+    for(int p = 0; p < P; ++p) {
+      int n1 = (int)std::sqrt(p + 1.0);
+      cplx c1 = Xi[size_t(j) * 2 * P + p], d1 = Xi[P + size_t(j) * 2 * P + p];
+      for(int q = 0; q < P; ++q) {
+        int n2 = (int)std::sqrt(q + 1.0);
+        cplx c2 = Xi[size_t(j) * 2 * P + q], d2 = Xi[P + size_t(j) * 2 * P + q];
+        const size_t at = (size_t(kk) * P + p) * P + q;
+        double Wm = tab[T_Wm1m1 * sz + at], W1 = tab[T_W11 * sz + at], W0 = tab[T_W00 * sz + at];
+        if(Wm == 0.0 && W1 == 0.0 && W0 == 0.0)
+          continue;
+        cplx F00 = d[n1] * dd[n2];
+        cplx F11 = (k1 * dd[n2] + d[n2] / r) * (k1 * dd[n1] + d[n1] / r);
+        cplx Fm = (1.0 / std::pow(r, 2.0)) * (d[n1] * d[n2]);
+        cplx Fd00 = d[n1] * dd[n2] * k1 + k1 * dd[n1] * d[n2];
+        cplx Fd11 = (std::pow(k1, 2.0) * ddd[n1] - (1.0 / std::pow(r, 2.0)) * d[n1] + (1.0 / r) * k1 * dd[n1]) *
+                        (k1 * dd[n2] + d[n2] / r) +
+                    (std::pow(k1, 2.0) * ddd[n2] - (1.0 / std::pow(r, 2.0)) * d[n2] + (1.0 / r) * k1 * dd[n2]) *
+                        (k1 * dd[n1] + d[n1] / r);
+        cplx Fdm = (1.0 / std::pow(r, 2.0)) * (k1 * dd[n1] * d[n2] + d[n1] * k1 * dd[n2]) -
+                   (2.0 / std::pow(r, 3.0)) * (d[n1] * d[n2]);
+        const double sq = std::sqrt(n1 * n2 * (n1 + 1) * (n2 + 1));
+        const double sn = std::sqrt(n * (n + 1));
+        Xm1 += (-eps_0 / eps_j2) * gamma *
+               (c1 * c2 * W0 * Fd00 + d1 * d2 * (1.0 / std::pow(k1, 2.0)) * (W1 * Fd11 + Wm * sq * Fdm));
+        Xp1 += (-eps_0 / eps_j2) * gamma *
+               (c1 * c2 * W0 * sn * (1.0 / r) * F00 +
+                d1 * d2 * (1.0 / std::pow(k1, 2.0)) *
+                    (W1 * sn * (1.0 / r) * F11 + Wm * sq * sn * (1.0 / r) * Fm));
+      }
+    }
+    std::vector<cplx> ds, dds;
+    bessel(kBessel, r * kSH, nmax, ds, dds);
+    const double sn = std::sqrt(n * (n + 1));
+    cplx Xm1SH = waveK_01 * dmnSH * (1.0 / kSH) * sn * (1.0 / r) * ds[n];
+    cplx X0 = -waveK_01 * cmnSH * ds[n];
+    cplx Xp1SH = waveK_01 * dmnSH * (1.0 / kSH) * ((1.0 / r) * ds[n] + dds[n]);
+    integral = integral + wi[ii] * std::pow(r, 2.0) *
+                              ((Xm1 + Xm1SH) * std::conj(Xm1 + Xm1SH) + X0 * std::conj(X0) +
+                               (Xp1 + Xp1SH) * std::conj(Xp1 + Xp1SH));
+  }
+  return integral * (R / 2.0);
+}
+
 inline cplx *C(double *p) { return reinterpret_cast<cplx *>(p); }
 inline const cplx *C(const double *p) { return reinterpret_cast<const cplx *>(p); }
 
@@ -1082,7 +1449,7 @@ void orc_to_spherical(double x, double y, double z, double *out) {
 void *orc_problem_create(int N, const double *xyz, const double *radius, const double *eps,
                          const double *mu, const double *eps_sh, const double *bg, double lambda,
                          double theta, double phi, const double *e_theta, const double *e_phi,
-                         int nmax) {
+                         int nmax, const double *chi) {
   try {
     Problem *pr = new Problem();
     pr->nmax = nmax;
@@ -1093,6 +1460,10 @@ void *orc_problem_create(int N, const double *xyz, const double *radius, const d
       s.radius = radius[i];
       s.elmag.init(cplx(eps[2 * i], eps[2 * i + 1]), cplx(mu[2 * i], mu[2 * i + 1]),
                    cplx(eps_sh[2 * i], eps_sh[2 * i + 1]));
+      // chi: per sphere {ksippp, ksiparppar, gamma} complex (6 doubles), may be null
+      s.elmag.ksippp = chi ? cplx(chi[6 * i], chi[6 * i + 1]) : 0.0;
+      s.elmag.ksiparppar = chi ? cplx(chi[6 * i + 2], chi[6 * i + 3]) : 0.0;
+      s.elmag.gamma = chi ? cplx(chi[6 * i + 4], chi[6 * i + 5]) : 0.0;
       for(auto const &o : pr->objects)
         if(find_distance(o.vR, s.vR) <= (s.radius + o.radius)) {
           g_err = "The sphere at index " + std::to_string(i) + " overlaps with another one";
@@ -1111,6 +1482,125 @@ void *orc_problem_create(int N, const double *xyz, const double *radius, const d
   } catch(std::exception &e) {
     g_err = e.what();
     return nullptr;
+  }
+}
+
+
+// The nine SH coupling tables for nMaxS = nMax, 9 x P^3 doubles in the order
+// C_10m1, C_11m1, C_00m1, C_01m1, W_m1m1, W_11, W_00, W_10, W_01.
+void orc_clg_tables(int nmax, double *out) {
+  std::vector<double> t;
+  clg_tables(nmax, nmax, t);
+  std::memcpy(out, t.data(), sizeof(double) * t.size());
+}
+
+double orc_wigner(int kind, const int *j) {
+  if(kind == 3)
+    return wigner3j(j[0], j[1], j[2], j[3], j[4], j[5]);
+  if(kind == 6)
+    return wigner6j(j[0], j[1], j[2], j[3], j[4], j[5]);
+  return wigner9j(j[0], j[1], j[2], j[3], j[4], j[5], j[6], j[7], j[8]);
+}
+
+// SH per-sphere factors expanded to 2P each: T1_outer, T2_outer, IauxSH1, IauxSH2.
+void orc_sh_factors(void *h, int j, double *out) {
+  Problem *pr = static_cast<Problem *>(h);
+  int P = pmax(pr->nmax);
+  ShFactors f = sh_factors(*pr, pr->objects[j]);
+  cplx *o = C(out);
+  for(int p = 0; p < P; ++p) {
+    int n = (int)std::sqrt(p + 1.0);
+    o[p] = f.t1te[n];
+    o[P + p] = f.t1tm[n];
+    o[2 * P + p] = f.t2te[n];
+    o[3 * P + p] = f.t2tm[n];
+    o[4 * P + p] = f.i1te[n];
+    o[5 * P + p] = f.i1tm[n];
+    o[6 * P + p] = f.i2te[n];
+    o[7 * P + p] = f.i2tm[n];
+  }
+}
+
+// The SH half of PreconditionedMatrix::solve (PreconditionedMatrixSolver.h:62-78):
+// K, K1ana from X_int (unconjugated FF internal coefficients), LU solve with the SH
+// matrix, convertInternal_SH. tables from orc_clg_tables.
+int orc_sh_solve(void *h, const double *tables, const double *X_int, double *K, double *K1ana,
+                 double *X_sca_SH, double *X_int_SH) {
+  Problem *pr = static_cast<Problem *>(h);
+  try {
+    const int P = pmax(pr->nmax), N = (int)pr->objects.size();
+    const int n = 2 * P * N;
+    std::vector<double> tab(tables, tables + 9 * size_t(P) * P * P);
+    std::vector<cplx> k(n), k1(n), V(size_t(n) * n), x(n);
+    sh_source(*pr, tab, C(X_int), k.data(), k1.data());
+    scattering_matrix(*pr, true, V.data());
+    int rc = lu_solve(n, V.data(), k.data(), x.data());
+    if(rc)
+      return rc;
+    for(int j = 0; j < N; ++j) {
+      ShFactors f = sh_factors(*pr, pr->objects[j]);
+      for(int p = 0; p < P; ++p) {
+        int nn = (int)std::sqrt(p + 1.0);
+        size_t o = size_t(j) * 2 * P;
+        C(X_int_SH)[o + p] = x[o + p] * f.i1te[nn] - k1[o + p];
+        C(X_int_SH)[o + P + p] = x[o + P + p] * f.i1tm[nn] - k1[o + P + p];
+      }
+    }
+    std::memcpy(K, k.data(), sizeof(cplx) * n);
+    std::memcpy(K1ana, k1.data(), sizeof(cplx) * n);
+    std::memcpy(X_sca_SH, x.data(), sizeof(cplx) * n);
+    return 0;
+  } catch(std::exception &e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+// getScatteringCrossSection_SH and getAbsorptionCrossSection_SH (Result.cpp:662-778):
+// out = {C_sca_SH, C_abs_SH}. X_int is the FF internal vector of Result (unconjugated).
+int orc_sh_cross_sections(void *h, const double *tables, const double *X_int,
+                          const double *X_sca_SH, const double *X_int_SH, double *out) {
+  Problem *pr = static_cast<Problem *>(h);
+  try {
+    const int P = pmax(pr->nmax), N = (int)pr->objects.size();
+    std::vector<double> tab(tables, tables + 9 * size_t(P) * P * P);
+    double ArbCf = std::real(pr->bground.epsilon_r) * std::real(pr->bground.mu_r);
+    double temp1 = 0.0;
+    for(int j = 0; j < N; ++j) {
+      std::vector<cplx> A, B;
+      Sph Rrel = sph_minus(pr->objects[j].vR, Sph{0.0, 0.0, 0.0});
+      coupling(Rrel, 2.0 * pr->waveK, pr->nmax, false, A, B);
+      const cplx *c = C(X_sca_SH) + size_t(j) * 2 * P;
+      for(int p = 0; p < 2 * P; ++p)
+        for(int q = 0; q < 2 * P; ++q) {
+          int pp = p % P, qq = q % P;
+          bool same = (p < P) == (q < P);
+          cplx T = same ? A[size_t(pp) * P + qq] : B[size_t(pp) * P + qq];
+          temp1 += std::real(T * std::conj(c[q]) * std::conj(T) * c[q]);
+        }
+    }
+    out[0] = (1.0 / (4.0 * ArbCf)) * temp1;
+    const double w = pr->omega();
+    const cplx eta = std::sqrt(pr->bground.mu / pr->bground.epsilon);
+    std::vector<double> acc(N, 0.0);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(g_threads)
+    for(int j = 0; j < N; ++j) {
+      cplx sigma = -cplx(0.0, 1.0) * kEps0 * 2.0 * w * (pr->objects[j].elmag.epsilon_r_SH - 1.0);
+      cplx sum(0.0, 0.0);
+      for(int kk = 0; kk < P; ++kk) {
+        cplx cmn = C(X_int_SH)[size_t(j) * 2 * P + kk], dmn = C(X_int_SH)[P + size_t(j) * 2 * P + kk];
+        sum += acs_sh(*pr, j, kk, tab, C(X_int), cmn, dmn);
+      }
+      acc[j] = std::real((2.0 * eta) * 0.5 * sigma * sum);
+    }
+    double a = 0.0;
+    for(int j = 0; j < N; ++j)
+      a = a + acc[j];
+    out[1] = a;
+    return 0;
+  } catch(std::exception &e) {
+    g_err = e.what();
+    return -1;
   }
 }
 

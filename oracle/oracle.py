@@ -38,7 +38,13 @@ def lib():
         L.orc_last_error.restype = C.c_char_p
         L.orc_problem_create.restype = C.c_void_p
         L.orc_problem_create.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double,
-                                         C.c_double, C.c_double, _dp, _dp, C.c_int]
+                                         C.c_double, C.c_double, _dp, _dp, C.c_int, _dp]
+        L.orc_clg_tables.argtypes = [C.c_int, _dp]
+        L.orc_wigner.argtypes = [C.c_int, C.POINTER(C.c_int)]
+        L.orc_wigner.restype = C.c_double
+        L.orc_sh_factors.argtypes = [C.c_void_p, C.c_int, _dp]
+        L.orc_sh_solve.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.orc_sh_cross_sections.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
         for name in ("orc_problem_destroy",):
             getattr(L, name).argtypes = [C.c_void_p]
         for name in ("orc_inc_coeffs", "orc_source_vector", "orc_wave_numbers"):
@@ -139,6 +145,9 @@ class Cluster:
     phi: float = 0.0
     e_theta: complex = 1.0
     e_phi: complex = 0.0
+    ksippp: complex = 0.0      # surface chi(2) perp-perp-perp (XML <ksippp>)
+    ksiparppar: complex = 0.0  # surface chi(2) par-perp-par (XML <ksiparppar>)
+    gamma: complex = 0.0       # bulk chi(2) (XML <gamma>)
 
     def __post_init__(self):
         self.xyz = np.ascontiguousarray(self.xyz, dtype=np.float64).reshape(-1, 3)
@@ -147,6 +156,11 @@ class Cluster:
         self.eps = _c(np.broadcast_to(self.eps, (n,)))
         self.mu = _c(np.ones(n) if self.mu is None else np.broadcast_to(self.mu, (n,)))
         self.eps_sh = _c(self.eps if self.eps_sh is None else np.broadcast_to(self.eps_sh, (n,)))
+        chi = np.zeros((n, 3), np.complex128)
+        chi[:, 0] = np.broadcast_to(self.ksippp, (n,))
+        chi[:, 1] = np.broadcast_to(self.ksiparppar, (n,))
+        chi[:, 2] = np.broadcast_to(self.gamma, (n,))
+        self.chi = np.ascontiguousarray(chi)
 
     @property
     def n_spheres(self):
@@ -174,7 +188,8 @@ class Problem:
         self._keep = (bg, et, ep)
         h = L.orc_problem_create(cl.n_spheres, _p(cl.xyz), _p(cl.radius), _p(cl.eps.view(np.float64)),
                                  _p(cl.mu.view(np.float64)), _p(cl.eps_sh.view(np.float64)), _p(bg),
-                                 cl.wavelength, cl.theta, cl.phi, _p(et), _p(ep), cl.nmax)
+                                 cl.wavelength, cl.theta, cl.phi, _p(et), _p(ep), cl.nmax,
+                                 _p(cl.chi.view(np.float64)))
         if not h:
             raise RuntimeError(L.orc_last_error().decode())
         self.h = h
@@ -247,6 +262,30 @@ class Problem:
             raise RuntimeError(lib().orc_last_error().decode())
         return E, H
 
+    def sh_factors(self, j):
+        """T1_outer, T2_outer, IauxSH1, IauxSH2 of sphere j (2P each)."""
+        out = np.zeros(8 * self.cl.P, np.complex128)
+        lib().orc_sh_factors(self.h, j, _p(out))
+        return out.reshape(4, 2 * self.cl.P)
+
+    def sh_solve(self, tables, x_int):
+        """SH half of the solve: (K, K1ana, X_sca_SH, X_int_SH)."""
+        x_int = _c(x_int)
+        outs = [np.zeros(self.n, np.complex128) for _ in range(4)]
+        rc = lib().orc_sh_solve(self.h, _p(tables), _p(x_int), *[_p(o) for o in outs])
+        if rc:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return outs
+
+    def sh_cross_sections(self, tables, x_int, x_sca_sh, x_int_sh):
+        """(C_sca_SH, C_abs_SH) as Result::getScatteringCrossSection_SH / getAbsorptionCrossSection_SH."""
+        out = np.zeros(2)
+        rc = lib().orc_sh_cross_sections(self.h, _p(tables), _p(_c(x_int)), _p(_c(x_sca_sh)),
+                                         _p(_c(x_int_sh)), _p(out))
+        if rc:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return out
+
     def wavelength_solve(self, method="lu", tol=1e-10, maxit=1000, restarts=4):
         xsec = np.zeros(4)
         xs = np.zeros(self.n, np.complex128)
@@ -281,6 +320,20 @@ def matvec(A, x):
     y = np.zeros(A.shape[0], np.complex128)
     lib().orc_matvec(A.shape[0], A.shape[1], _p(A), _p(x), _p(y))
     return y
+
+
+def clg_tables(nmax: int) -> np.ndarray:
+    """The nine SH coupling tables (9, P, P, P): C_10m1, C_11m1, C_00m1, C_01m1,
+    W_m1m1, W_11, W_00, W_10, W_01, indexed [k][p][q]."""
+    P = nmax * (nmax + 2)
+    out = np.zeros(9 * P ** 3)
+    lib().orc_clg_tables(nmax, _p(out))
+    return out
+
+
+def wigner(kind: int, *js) -> float:
+    arr = (C.c_int * len(js))(*js)
+    return float(lib().orc_wigner(kind, arr))
 
 
 def lu_solve(A, b):

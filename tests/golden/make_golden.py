@@ -42,10 +42,17 @@ def cases():
     xyz, rad = random_cluster(np.random.default_rng(12), 3, 500 * nm, 40 * nm, 70 * nm, 20 * nm)
     out["diel3"] = O.Cluster(xyz=xyz, radius=rad, eps=(2.0 + 0.05j) ** 2, nmax=5,
                              wavelength=650 * nm, theta=2.0, phi=-0.7, e_theta=1.0, e_phi=0.0)
-    # Single sphere off the origin with SH permittivity, nMax=3.
+    # Single sphere off the origin with SH permittivity and surface + bulk chi(2), nMax=3.
     out["single_sh"] = O.Cluster(xyz=[[40 * nm, -30 * nm, 20 * nm]], radius=120 * nm,
                                  eps=(4.0 + 0.1j) ** 2, eps_sh=(4.2 + 0.2j) ** 2, nmax=3,
-                                 wavelength=800 * nm, theta=0.9, phi=0.2)
+                                 wavelength=800 * nm, theta=0.9, phi=0.2, ksippp=1.0,
+                                 ksiparppar=0.25, gamma=0.3)
+    # Two spheres, C3-like chi(2) (perp-perp-perp 1.0, par-perp-par 0.25, no bulk term), nMax=4.
+    out["pair_sh"] = O.Cluster(xyz=[[0, 0, 0], [180 * nm, 60 * nm, -90 * nm]], radius=[70 * nm, 90 * nm],
+                               eps=[(2.5 + 0.05j) ** 2, (3.0 + 0.02j) ** 2],
+                               eps_sh=[(2.6 + 0.06j) ** 2, (3.1 + 0.03j) ** 2], nmax=4,
+                               wavelength=700 * nm, theta=0.5, phi=-0.4, e_theta=0.8, e_phi=0.6j,
+                               ksippp=1.0, ksiparppar=0.25)
     return out
 
 
@@ -87,8 +94,18 @@ def make(name, cl):
     k, omega = pr.wave_numbers()
     A_irr, B_irr = O.coupling(rel, k, cl.nmax, True)
     A_reg, B_reg = O.coupling(rel, k, cl.nmax, False)
+    sh = {}
+    if np.any(cl.chi != 0):
+        tab = O.clg_tables(cl.nmax)
+        K, K1, Xs, Xis = pr.sh_solve(tab, Xi)
+        sh = dict(chi=cl.chi[0], K=K, K1ana=K1, X_sca_SH=Xs, X_int_SH=Xis,
+                  xsec_sh=pr.sh_cross_sections(tab, Xi, Xs, Xis),
+                  sh_factors=np.stack([pr.sh_factors(j) for j in range(N)]))
+        if cl.nmax <= 3:
+            sh["clg"] = tab
+        print(name, "SH xsec", sh["xsec_sh"])
     np.savez_compressed(
-        os.path.join(HERE, f"{name}.npz"),
+        os.path.join(HERE, f"{name}.npz"), **sh,
         xyz=cl.xyz, radius=cl.radius, eps=cl.eps, mu=cl.mu, eps_sh=cl.eps_sh,
         bg=np.array([cl.bg_eps, cl.bg_mu], np.complex128), nmax=cl.nmax,
         wavelength=cl.wavelength, angles=np.array([cl.theta, cl.phi]),

@@ -17,16 +17,19 @@ def load_golden(name):
 
 
 def oracle_cluster(O, g):
+    chi = g["chi"] if "chi" in g.files else np.zeros(3, np.complex128)
     return O.Cluster(xyz=g["xyz"], radius=g["radius"], eps=g["eps"], mu=g["mu"], eps_sh=g["eps_sh"],
                      nmax=int(g["nmax"]), wavelength=float(g["wavelength"]),
                      bg_eps=complex(g["bg"][0]), bg_mu=complex(g["bg"][1]),
                      theta=float(g["angles"][0]), phi=float(g["angles"][1]),
-                     e_theta=complex(g["pol"][0]), e_phi=complex(g["pol"][1]))
+                     e_theta=complex(g["pol"][0]), e_phi=complex(g["pol"][1]),
+                     ksippp=complex(chi[0]), ksiparppar=complex(chi[1]), gamma=complex(chi[2]))
 
 
 def gpu_inputs(G, cl):
     """(spheres, medium, wave) for the GPU library from an oracle Cluster."""
-    sp = G.spheres_array(cl.xyz, cl.radius, cl.eps, cl.nmax, mu=cl.mu, eps_sh=cl.eps_sh)
+    sp = G.spheres_array(cl.xyz, cl.radius, cl.eps, cl.nmax, mu=cl.mu, eps_sh=cl.eps_sh,
+                         ksippp=cl.chi[:, 0], ksiparppar=cl.chi[:, 1], gamma=cl.chi[:, 2])
     return sp, G.medium(cl.bg_eps, cl.bg_mu), G.plane_wave(cl.wavelength, cl.theta, cl.phi,
                                                            cl.e_theta, cl.e_phi)
 

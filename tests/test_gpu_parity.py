@@ -187,3 +187,48 @@ def test_deterministic(G, ctx, oracle):
         outs.append((pr.coefficients()[0], pr.cross_sections()))
         pr.close()
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("nmax", [3, 5])
+def test_sh_tables_match_oracle(G, ctx, oracle, nmax):
+    a = G.clg_tables(ctx, nmax)
+    b = oracle.clg_tables(nmax)
+    assert np.max(np.abs(a - b)) < 1e-13 * max(1.0, np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("name", ["single_sh", "pair_sh"])
+@pytest.mark.parametrize("method", ["lu", "gmres"])
+def test_sh_pipeline(G, ctx, oracle, name, method):
+    """SH source, SH solve, internal SH coefficients and SH cross sections
+    against the oracle (and the golden fixture)."""
+    g = load_golden(name)
+    cl = oracle_cluster(oracle, g)
+    pr = make(G, ctx, cl)
+    opts = G.options(G.SOLVE_LU) if method == "lu" else G.options(G.SOLVE_GMRES, tol=1e-13, max_iter=200)
+    pr.source_vector(copy=False)
+    pr.assemble(G.FF)
+    pr.solve(opts)
+    pr.assemble(G.SH)
+    pr.solve_sh(opts)
+    K, K1, Xs, Xis = pr.sh_vectors()
+    pr_o = oracle.Problem(cl)
+    tab = oracle.clg_tables(cl.nmax)
+    xo = oracle.lu_solve(pr_o.scattering_matrix(), pr_o.source_vector())
+    xio = pr_o.internal(xo)
+    Ko, K1o, Xso, Xiso = pr_o.sh_solve(tab, xio)
+    assert rel(K, Ko) < 1e-10 and rel(K1, K1o) < 1e-10
+    assert rel(Xs, Xso) < 1e-10 and rel(Xis, Xiso) < 1e-10
+    xs = pr.sh_cross_sections()
+    xso = pr_o.sh_cross_sections(tab, xio, Xso, Xiso)
+    assert np.max(np.abs(xs - xso) / np.abs(xso)) < 1e-10
+    assert np.max(np.abs(xs - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10
+
+
+def test_wavelength_solve_sh_entry_point(G, ctx, oracle):
+    g = load_golden("pair_sh")
+    cl = oracle_cluster(oracle, g)
+    sp, bg, wave = gpu_inputs(G, cl)
+    wave.sh = 1
+    xsec, xsh, st = G.wavelength_solve_sh(ctx, sp, bg, wave, G.options(G.SOLVE_LU))
+    assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 5e-10
+    assert np.max(np.abs(xsh - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10

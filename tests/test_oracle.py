@@ -15,11 +15,8 @@ nm = 1e-9
 
 
 def load_cluster(O, g):
-    return O.Cluster(xyz=g["xyz"], radius=g["radius"], eps=g["eps"], mu=g["mu"],
-                     eps_sh=g["eps_sh"], nmax=int(g["nmax"]), wavelength=float(g["wavelength"]),
-                     bg_eps=complex(g["bg"][0]), bg_mu=complex(g["bg"][1]),
-                     theta=float(g["angles"][0]), phi=float(g["angles"][1]),
-                     e_theta=complex(g["pol"][0]), e_phi=complex(g["pol"][1]))
+    from helpers import oracle_cluster
+    return oracle_cluster(O, g)
 
 
 def rel(a, b):
@@ -203,3 +200,92 @@ def test_thread_count_does_not_change_results(oracle):
     b = pr.wavelength_solve("lu")[0]
     oracle.set_threads(1)
     assert np.array_equal(a, b)
+
+
+def _w_table_entry_sympy(J1, M1, J2, M2, J, M, L1, L2):
+    """Symbol.cpp's W(L1, J1, M1, L2, J2, M2, L, M) from sympy's exact symbols."""
+    from sympy.physics.wigner import wigner_3j, wigner_6j
+
+    def cg(j, m, j1, m1, j2, m2):
+        return (-1.0) ** int(m + j1 - j2) * np.sqrt(2 * j + 1) * float(wigner_3j(j1, j2, j, m1, m2, -m))
+
+    return ((-1.0) ** int(J2 + L1 + J) * np.sqrt((2 * J1 + 1) * (2 * J2 + 1) * (2 * L1 + 1) * (2 * L2 + 1)
+                                             / (4 * np.pi * (2 * J + 1)))
+            * float(wigner_6j(L1, L2, J, J2, J1, 1)) * cg(J, 0, L1, 0, L2, 0) * cg(J, M, J1, M1, J2, M2))
+
+
+def test_sh_tables_against_sympy(oracle):
+    """W_00 and W_10 entries of the SH coupling tables against sympy's exact Wigner symbols."""
+    nmax = 3
+    P = nmax * (nmax + 2)
+    tab = oracle.clg_tables(nmax).reshape(9, P, P, P)
+
+    def nm(p):
+        n = int(np.sqrt(p + 1.0))
+        return n, -(p + 1) + n * (n + 1)
+
+    rng = np.random.default_rng(4)
+    checked = 0
+    for _ in range(60):
+        k, p, q = rng.integers(0, P, 3)
+        J, M = nm(k)
+        J1, M1 = nm(p)
+        J2, M2 = nm(q)
+        if M != M1 + M2:
+            assert tab[6, k, p, q] == 0.0
+            continue
+        w00 = _w_table_entry_sympy(J1, M1, J2, M2, J, M, J1, J2)
+        assert abs(tab[6, k, p, q] - w00) < 1e-13 * max(1.0, abs(w00))
+        a1, b1 = np.sqrt(J1 / (2 * J1 + 1)), np.sqrt((J1 + 1) / (2 * J1 + 1))
+        w10 = b1 * _w_table_entry_sympy(J1, M1, J2, M2, J, M, J1 - 1, J2) + \
+            a1 * _w_table_entry_sympy(J1, M1, J2, M2, J, M, J1 + 1, J2)
+        assert abs(tab[7, k, p, q] - w10) < 1e-13 * max(1.0, abs(w10))
+        checked += 1
+    assert checked > 5
+
+
+@pytest.mark.parametrize("name", ["single_sh", "pair_sh"])
+def test_sh_golden(oracle, name):
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    cl = load_cluster(oracle, g)
+    pr = oracle.Problem(cl)
+    tab = oracle.clg_tables(cl.nmax)
+    if "clg" in g.files:
+        assert np.max(np.abs(tab - g["clg"])) < 1e-13
+    for j in range(cl.n_spheres):
+        assert rel(pr.sh_factors(j), g["sh_factors"][j]) < 1e-11
+    S, Q = pr.scattering_matrix(), pr.source_vector()
+    X = oracle.lu_solve(S, Q)
+    Xi = pr.internal(X)
+    K, K1, Xs, Xis = pr.sh_solve(tab, Xi)
+    for a, b in ((K, g["K"]), (K1, g["K1ana"]), (Xs, g["X_sca_SH"]), (Xis, g["X_int_SH"])):
+        assert rel(a, b) < 5e-10
+    xs = pr.sh_cross_sections(tab, Xi, Xs, Xis)
+    assert np.max(np.abs(xs - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10
+
+
+def test_sh_single_sphere_rotation_invariance(oracle):
+    """Single sphere at the origin, surface chi(2) only: both SH cross sections
+    are rotation invariant (pins the coupling tables and the SH factors). With
+    two spheres the reference's source, built from conj(X_int), is not rotation
+    covariant, so no such identity holds there."""
+    def run(kdir, pol):
+        th = np.arccos(kdir[2])
+        ph = np.arctan2(kdir[1], kdir[0])
+        eth = np.array([np.cos(th) * np.cos(ph), np.cos(th) * np.sin(ph), -np.sin(th)])
+        eph = np.array([-np.sin(ph), np.cos(ph), 0.0])
+        cl = oracle.Cluster(xyz=np.zeros((1, 3)), radius=80 * nm, eps=(2.0 + 0.1j) ** 2,
+                            eps_sh=(2.2 + 0.15j) ** 2, nmax=4, wavelength=800 * nm, theta=th, phi=ph,
+                            e_theta=pol @ eth, e_phi=pol @ eph, ksippp=1.0, ksiparppar=0.25)
+        pr = oracle.Problem(cl)
+        _, X, Xi, _ = pr.wavelength_solve("lu")
+        tab = oracle.clg_tables(4)
+        K, K1, Xs, Xis = pr.sh_solve(tab, Xi)
+        return pr.sh_cross_sections(tab, Xi, Xs, Xis)
+    k0 = np.array([0.3, -0.5, 0.8])
+    k0 /= np.linalg.norm(k0)
+    e0 = np.cross(k0, [0, 0, 1.0])
+    e0 /= np.linalg.norm(e0)
+    R = Rotation.from_euler("zyz", [1.2, -0.3, 2.0]).as_matrix()
+    a, b = run(k0, e0), run(R @ k0, R @ e0)
+    assert np.max(np.abs(a - b) / np.abs(a)) < 1e-12
