@@ -17,6 +17,12 @@ sampling, 20 nm gap) in a 4 um cube, radii U[40, 70] nm, refractive index
 x-polarised. Synthetic data. Inputs exceed L2 (S alone is 32.8 GB complex64 +
 65.5 GB complex128), so no L2 flush is needed between steps.
 
+The headline number is the batched/served form: om_server with two slots
+(device contexts with their own streams and host threads) takes the scan's
+wavelengths in order, so one wavelength's FP64-bound assembly overlaps the
+previous wavelength's HBM-bound solve; the FP64 form is served the same way.
+The single-stream numbers of both forms are reported beside it.
+
 Multi-GPU: independent replicas (one cluster scan per rank, no collective);
 value = the sum over ranks of the wavelength-solves each completed, divided
 by the slowest rank's time.
@@ -224,30 +230,74 @@ def gpu_arm(args, w):
     err = max(abs(xs_mixed[i][0] - xs64[i][0]) / abs(xs64[i][0]) for i in range(k64))
     err_all = max(float(np.max(np.abs(xs_mixed[i] - xs64[i]) / np.abs(xs64[i]))) for i in range(k64))
 
-    # ---- end to end through the C ABI with host buffers ----
-    e2e_lat = []
-    for i in range(2 + max(1, min(args.steps, 3))):
-        wave = G.plane_wave(w["lam"] + 0.25 * nm * i)
-        ctx.synchronize()
+
+    pr.close()
+
+    # ---- batched / served form: om_server with `slots` contexts on the GPU ----
+    # Successive wavelengths of the scan run on alternating slots, so one
+    # wavelength's FP64-bound assembly overlaps the previous one's HBM-bound
+    # solve. Same requests for both forms; a slot keeps its problem resident
+    # across wavelengths (cluster_key) like the reference's scan keeps its
+    # Geometry.
+    def served(opts, precision, k, key, tuning=None, tune_count=4):
+        srv = G.Server(local, 0, args.slots)
+        lam = lambda i: G.plane_wave(w["lam"] + 0.25 * nm * i)
+        # launch tuning: the server's autotuner on warm-up requests (untimed)
+        if tuning is None:
+            tuning = srv.autotune(sp, bg, lam(0), opts, precision, 1, tune_count)
+        else:
+            srv.tune(**tuning)
+        for t in [srv.submit(sp, bg, lam(i), opts, precision, key) for i in range(args.warmup)]:
+            srv.poll(t)
+        srv.launches()
+        srv.mark()
         s0 = time.perf_counter()
-        G.wavelength_solve(ctx, sp, bg, wave, mixed_opts, G.C64)
-        if i >= 2:
-            e2e_lat.append(time.perf_counter() - s0)
+        tickets = [srv.submit(sp, bg, lam(args.warmup + i), opts, precision, key) for i in range(k)]
+        res = [srv.poll(t) for t in tickets]
+        wall = time.perf_counter() - s0
+        dev_ms = srv.mark()
+        launches = srv.launches()
+        srv.close()
+        bad = [r["status"] for r in res if r["status"] not in (G.OK,)]
+        if bad:
+            raise RuntimeError(f"served solve failed: status {bad}")
+        return dev_ms * 1e-3, wall, res, launches, tuning
+
+    barrier()
+    with ClockSampler(local) as clk_srv:
+        t_srv, _, res_srv, srv_launches, tuning = served(mixed_opts, G.C64, args.steps, 1)
+    clocks_srv = clk_srv.summary()
+    k64s = max(1, min(args.steps, 4))
+    t_srv64, _, res_srv64, _, tuning64 = served(fp64_opts, G.C128, k64s, 1, tune_count=2)
+    err_srv = max(abs(res_srv[i]["xsec"][0] - res_srv64[i]["xsec"][0]) / abs(res_srv64[i]["xsec"][0])
+                  for i in range(k64s))
+    err_srv_all = max(float(np.max(np.abs(res_srv[i]["xsec"] - res_srv64[i]["xsec"]) /
+                                   np.abs(res_srv64[i]["xsec"]))) for i in range(k64s))
+    svc = [r["service_ms"] for r in res_srv]
+    svc64 = [r["service_ms"] for r in res_srv64]
+
+    # ---- end to end through the C ABI with host buffers: every request
+    # copies its spheres and wave from the host, sets its problem up from
+    # scratch (cluster_key 0), and returns its cross sections to the host ----
+    _, wall_e2e, res_e2e, _, _ = served(mixed_opts, G.C64, args.steps, 0, tuning=tuning)
     import ctypes
     h2d = ctypes.sizeof(G.Sphere) * len(sp) + ctypes.sizeof(G.Medium) + \
         ctypes.sizeof(G.PlaneWave) + ctypes.sizeof(G.SolveOptions)
-    d2h = 4 * 8 + ctypes.sizeof(G.SolveStats)
+    d2h = ctypes.sizeof(G.Result)
 
     # aggregate over ranks (max time, summed work)
-    t_mixed_all, t64_all, e2e_all = t_mixed, t_fp64, float(np.mean(e2e_lat))
+    t_all = [t_srv, t_srv64, wall_e2e, t_mixed, t_fp64]
     if world > 1:
         import torch
         import torch.distributed as dist
-        tt = torch.tensor([t_mixed, t_fp64, e2e_all], device=f"cuda:{local}", dtype=torch.float64)
+        tt = torch.tensor(t_all, device=f"cuda:{local}", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_mixed_all, t64_all, e2e_all = [float(v) for v in tt.cpu()]
-    value = world * args.steps / t_mixed_all
-    value64 = world * k64 / t64_all
+        t_all = [float(v) for v in tt.cpu()]
+    t_srv_all, t_srv64_all, e2e_all, t_mixed_all, t64_all = t_all
+    value = world * args.steps / t_srv_all
+    value64 = world * k64s / t_srv64_all
+    value_ss = world * args.steps / t_mixed_all
+    value64_ss = world * k64 / t64_all
 
     hbm, how = peaks()
     mv_ms, mv_n = kt["matvec_c64"]
@@ -258,25 +308,39 @@ def gpu_arm(args, w):
     mv64_ms, mv64_n = kt64["matvec_c128"]
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed_all / args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_srv_all / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64 (FP32) inner + c128 (FP64) outer/assembly",
         "data": "synthetic (seeded random clusters)",
         "config": {"workload": args.workload + ": " + w["desc"], "unknowns": n,
-                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)",
-                   "solver": "FGMRES(FP64 outer, tol 1e-8) + GMRES(FP32 inner, 80 it, tol 1e-4)"},
-        "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
-                       "p99": 1e3 * float(np.percentile(lat, 99))},
-        "fp64": {"value": value64, "unit": UNIT, "steps": k64, "ms_per_step": 1e3 * t64_all / k64,
-                 "latency_ms": {"p50": 1e3 * float(np.percentile(lat64, 50)),
-                                "p99": 1e3 * float(np.percentile(lat64, 99))},
-                 "gmres_iterations": it64 / k64, "tol": 1e-10},
+                   "parallelism": f"replicas x{world}, {args.slots} serving slots per GPU",
+                   "l2": "inputs larger than L2 (no flush)",
+                   "solver": "FGMRES(FP64 outer, tol 1e-8) + GMRES(FP32 inner, 80 it, tol 1e-4)",
+                   "timing": "CUDA events on every slot's stream (om_server_mark) around the K requests",
+                   "launch_tuning": {"mixed": tuning, "fp64": tuning64,
+                                     "how": "om_server_autotune on warm-up requests"}},
+        "latency_ms": {"p50": float(np.percentile(svc, 50)), "p99": float(np.percentile(svc, 99)),
+                       "what": "per-request service time on its slot (host clock), overlapping the other slot"},
+        "fp64": {"value": value64, "unit": UNIT, "steps": k64s, "ms_per_step": 1e3 * t_srv64_all / k64s,
+                 "latency_ms": {"p50": float(np.percentile(svc64, 50)),
+                                "p99": float(np.percentile(svc64, 99))},
+                 "solver": "GMRES(FP64, tol 1e-10)", "gmres_iterations": it64 / k64},
         "speedup_vs_fp64": value / value64,
-        "qext_rel_err_vs_fp64": err, "xsec_max_rel_err_vs_fp64": err_all,
+        "qext_rel_err_vs_fp64": err_srv, "xsec_max_rel_err_vs_fp64": err_srv_all,
+        "single_stream": {
+            "mixed": {"value": value_ss, "ms_per_step": 1e3 * t_mixed_all / args.steps,
+                      "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
+                                     "p99": 1e3 * float(np.percentile(lat, 99))}},
+            "fp64": {"value": value64_ss, "ms_per_step": 1e3 * t64_all / k64,
+                     "latency_ms": {"p50": 1e3 * float(np.percentile(lat64, 50)),
+                                    "p99": 1e3 * float(np.percentile(lat64, 99))}},
+            "speedup_vs_fp64": value_ss / value64_ss,
+            "qext_rel_err_vs_fp64": err, "xsec_max_rel_err_vs_fp64": err_all},
         "iterations": {"outer": outer / args.steps, "inner": inner / args.steps},
-        "e2e": {"value": world / e2e_all, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": world * args.steps / e2e_all, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "path": "om_wavelength_solve (C ABI, host buffers, set-up + teardown included)"},
+                "path": "om_server_submit/om_server_poll (C ABI, host buffers, problem set-up "
+                        "from the host every request, host wall clock)"},
         "roofline": {"bound": "hbm", "kernel": "k_matvec_part<float2,float2> (FP32 inner matvec)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": how + " (MEASURED_PEAKS.json hbm_gbs)",
@@ -296,12 +360,13 @@ def gpu_arm(args, w):
             "matvec_c128": {"ms_avg": mv64_ms / max(mv64_n, 1), "launches": mv64_n,
                             "bound": "fp64 ALU (4 FMA per 16 B)"},
         },
-        "gpu_launches": total_launches,
-        "clocks": clocks,
+        "gpu_launches": srv_launches,
+        "gpu_launches_single_stream": total_launches,
+        "clocks": clocks_srv,
+        "clocks_single_stream": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(w, xyz, rad, it64 / k64, threads=None, budget_s=15.0)
-    pr.close()
     ctx.close()
     if world > 1:
         import torch.distributed as dist
@@ -392,7 +457,8 @@ def reference_arm(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--slots", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))

@@ -28,6 +28,7 @@ extern "C" {
 #define OM_ERR_NOT_CONVERGED 5    /* iterative solve stopped above tolerance */
 #define OM_ERR_SINGULAR 6         /* zero pivot in the LU factorisation (ScalapackSolver.cpp:76-77) */
 #define OM_ERR_STATE 7            /* call out of order (e.g. solve before assemble) */
+#define OM_PENDING 8              /* om_server_poll: the request has not finished yet */
 
 /* Harmonic selector */
 #define OM_FF 0                   /* fundamental frequency */
@@ -107,6 +108,23 @@ int om_context_synchronize(om_context *ctx);
  * complex128 (compensated) matvec ms, launches} (out may be NULL), resets
  * them and switches timing on or off. */
 int om_context_timers(om_context *ctx, int enable, double *out);
+/* Launch tuning of a context (no counterpart in the reference). Fields below
+ * zero keep the current value.
+ *   matvec_ctas_per_sm / matvec_df_ctas_per_sm: grid caps of the complex64 /
+ *     complex128 matvec and of the compensated complex64 x complex128 one, in
+ *     CTAs per SM (defaults 8 and 8; servers with several slots start at 4
+ *     and 2); the CTAs take tiles from a counter, so lower caps leave room on
+ *     each SM for another context's work.
+ *   assemble_carveout / matvec_carveout: preferred shared-memory carveout of
+ *     the assembly and matvec kernels in percent (0-100; default: the
+ *     driver's choice). The setting is per kernel for the whole process. */
+typedef struct {
+  int matvec_ctas_per_sm;
+  int matvec_df_ctas_per_sm;
+  int assemble_carveout;
+  int matvec_carveout;
+} om_tuning;
+int om_context_tune(om_context *ctx, const om_tuning *t);
 /* Record an event on the context's stream, wait for it and return in *ms the
  * device time since the previous mark (0 for the first). Device-side step
  * timing for benchmarks; no counterpart in the reference. */
@@ -122,6 +140,10 @@ int om_problem_create(om_context *ctx, const om_sphere *spheres, int n_spheres,
 void om_problem_destroy(om_problem *pr);
 /* Excitation::updateWavelength (Excitation.cpp:132-137) + Geometry::update. */
 int om_problem_set_wavelength(om_problem *pr, double wavelength);
+/* The whole plane wave at once (wavelength, direction, polarisation, SH flag):
+ * Excitation::populate (Excitation.cpp:48-75) for a new excitation of the same
+ * geometry; device buffers, including an assembled matrix's storage, are kept. */
+int om_problem_set_wave(om_problem *pr, const om_plane_wave *wave);
 /* Number of unknowns 2 P N (AbstractSolver::scattering_size, Solver.h:118-121). */
 long om_problem_size(const om_problem *pr);
 
@@ -193,6 +215,11 @@ int om_solve_sh(om_problem *pr, const om_solve_options *opts, om_solve_stats *st
  * scattered / internal coefficients (either may be NULL). */
 int om_get_sh_vectors(om_problem *pr, double *K, double *K1ana, double *X_sca_SH,
                       double *X_int_SH);
+/* Result::getEHFields, second-harmonic half, at Cartesian points
+ * (Result.cpp:166-199, 237-276, with the particular solution of
+ * Result::setFields / Geometry::COEFFpartSH, Result.cpp:906-919,
+ * Geometry.cpp:458-491): E_SH, H_SH, 3 complex per point. Needs om_solve_sh. */
+int om_near_field_sh(om_problem *pr, const double *xyz, int npts, double *E, double *H);
 /* Result::getScatteringCrossSection_SH and getAbsorptionCrossSection_SH
  * (Result.cpp:662-778, Symbol.cpp:358-477): out = {C_sca_SH, C_abs_SH}. */
 int om_sh_cross_sections(om_problem *pr, double out[2]);
@@ -216,6 +243,75 @@ int om_wavelength_solve_sh(om_context *ctx, const om_sphere *spheres, int n_sphe
                            const om_medium *background, const om_plane_wave *wave,
                            const om_solve_options *opts, int precision, double xsec[4],
                            double xsec_sh[2], om_solve_stats *stats);
+
+/* ---------------------------------------------------------------------------
+ * Serving and batching. No counterpart in the reference, whose
+ * Simulation::scan_wavelengths (Simulation.cpp:604-685) runs one
+ * wavelength-solve after another on one process.
+ *
+ * A server owns `slots` device contexts on one GPU, each driven by its own
+ * host thread and stream. Requests are taken in arrival order by the first
+ * free slot (continuous batching: a request that arrives while others run
+ * starts as soon as a slot and device memory are free, and its kernels overlap
+ * theirs on the device). Admission is against `hbm_budget` bytes: a request's
+ * device memory (matrix, Krylov basis, solver workspace) is estimated from
+ * N, nMax, the precision and the solve options, and it waits until the running
+ * and resident requests leave room; one that cannot fit even on an empty
+ * device fails with OM_ERR_BUDGET. A slot keeps its problem (matrix storage,
+ * per-sphere state) resident after a request and reuses it for the next one
+ * with the same non-zero cluster_key (a wavelength scan), releasing it under
+ * memory pressure. Results do not depend on the slot or on what else runs:
+ * every kernel reduces in a fixed order.
+ * ------------------------------------------------------------------------- */
+typedef struct om_server om_server;
+
+typedef struct {
+  const om_sphere *spheres;       /* copied by om_server_submit */
+  int n_spheres;
+  int precision;                  /* OM_C128 (plain form) or OM_C64 (precision form) */
+  om_medium background;
+  om_plane_wave wave;             /* wave.sh = 1 attaches the second-harmonic solve */
+  om_solve_options opts;          /* used for the FF and the SH solve */
+  unsigned long long cluster_key; /* non-zero: same spheres as earlier requests with this key */
+} om_request;
+
+typedef struct {
+  int status;                     /* OM_OK or the first failing call's code */
+  int slot;                       /* slot that served the request */
+  double xsec[4];                 /* as om_cross_sections */
+  double xsec_sh[2];              /* as om_sh_cross_sections (SH requests) */
+  om_solve_stats ff, sh;          /* solve statistics */
+  double queue_ms;                /* submit -> start of service (host clock) */
+  double service_ms;              /* start of service -> result */
+  double latency_ms;              /* submit -> result */
+  size_t device_bytes;            /* admission estimate */
+} om_result;
+
+int om_server_create(int device, size_t hbm_budget, int slots, om_server **out);
+/* Copies the request; returns its ticket. */
+int om_server_submit(om_server *srv, const om_request *rq, unsigned long long *ticket);
+/* OM_PENDING while the request runs (wait = 0) or blocks until it finishes
+ * (wait != 0); on completion fills *out and forgets the ticket. */
+int om_server_poll(om_server *srv, unsigned long long ticket, int wait, om_result *out);
+/* Blocks until every submitted request has finished. */
+int om_server_drain(om_server *srv);
+/* Records an event on every slot's stream, waits for them and returns in *ms
+ * the device time from the earliest event of the previous mark to the latest
+ * of this one (0 for the first). */
+int om_server_mark(om_server *srv, double *ms);
+/* om_context_tune on every slot; only while no request is outstanding. */
+int om_server_tune(om_server *srv, const om_tuning *t);
+/* Autotuner of the launch tuning: runs `count` requests like *rq (its cluster
+ * key and options, successive wavelengths from rq->wave.wavelength in steps of
+ * `step` metres) under each of a few built-in tunings (matvec grid caps,
+ * shared-memory carveouts), keeps the one with the shortest device time and
+ * returns it in *chosen (may be NULL). Results do not depend on the tuning. */
+int om_server_autotune(om_server *srv, const om_request *rq, int count, double step,
+                       om_tuning *chosen);
+/* Kernels launched by all requests finished since the previous call. */
+long om_server_launches(om_server *srv);
+const char *om_server_last_error(om_server *srv);
+void om_server_destroy(om_server *srv);
 
 #ifdef __cplusplus
 }

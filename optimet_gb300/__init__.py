@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboptimet_gpu.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "optimet_gpu.h")
 
-OK, ERR_INVALID, ERR_OVERLAP, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_SINGULAR, ERR_STATE = range(8)
+OK, ERR_INVALID, ERR_OVERLAP, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_SINGULAR, ERR_STATE, PENDING = range(9)
 FF, SH = 0, 1
 C128, C64 = 0, 1
 SOLVE_LU, SOLVE_GMRES, SOLVE_FGMRES_MIXED, SOLVE_LU_MIXED = 0, 1, 2, 3
@@ -64,6 +64,24 @@ class SolveStats(C.Structure):
                 ("rel_residual", C.c_double), ("seconds", C.c_double)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("matvec_ctas_per_sm", C.c_int), ("matvec_df_ctas_per_sm", C.c_int),
+                ("assemble_carveout", C.c_int), ("matvec_carveout", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("spheres", C.POINTER(Sphere)), ("n_spheres", C.c_int), ("precision", C.c_int),
+                ("background", Medium), ("wave", PlaneWave), ("opts", SolveOptions),
+                ("cluster_key", C.c_ulonglong)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("slot", C.c_int), ("xsec", C.c_double * 4),
+                ("xsec_sh", C.c_double * 2), ("ff", SolveStats), ("sh", SolveStats),
+                ("queue_ms", C.c_double), ("service_ms", C.c_double), ("latency_ms", C.c_double),
+                ("device_bytes", C.c_size_t)]
+
+
 _lib = None
 _dp = C.POINTER(C.c_double)
 
@@ -84,6 +102,7 @@ def lib():
         L.om_context_synchronize.argtypes = [vp]
         L.om_context_timers.argtypes = [vp, C.c_int, _dp]
         L.om_context_mark.argtypes = [vp, _dp]
+        L.om_context_tune.argtypes = [vp, C.POINTER(Tuning)]
         L.om_problem_create.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
                                         C.POINTER(PlaneWave), pvp]
         L.om_problem_destroy.argtypes = [vp]
@@ -102,6 +121,7 @@ def lib():
         L.om_get_coefficients.argtypes = [vp, _dp, _dp]
         L.om_cross_sections.argtypes = [vp, _dp]
         L.om_near_field.argtypes = [vp, _dp, C.c_int, _dp, _dp]
+        L.om_near_field_sh.argtypes = [vp, _dp, C.c_int, _dp, _dp]
         L.om_wavelength_solve.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
                                           C.POINTER(PlaneWave), C.POINTER(SolveOptions), C.c_int,
                                           _dp, _dp, _dp, C.POINTER(SolveStats)]
@@ -112,6 +132,20 @@ def lib():
         L.om_get_sh_vectors.argtypes = [vp, _dp, _dp, _dp, _dp]
         L.om_sh_cross_sections.argtypes = [vp, _dp]
         L.om_clg_tables.argtypes = [vp, C.c_int, _dp]
+        L.om_problem_set_wave.argtypes = [vp, C.POINTER(PlaneWave)]
+        L.om_server_create.argtypes = [C.c_int, C.c_size_t, C.c_int, pvp]
+        L.om_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_ulonglong)]
+        L.om_server_poll.argtypes = [vp, C.c_ulonglong, C.c_int, C.POINTER(Result)]
+        L.om_server_drain.argtypes = [vp]
+        L.om_server_tune.argtypes = [vp, C.POINTER(Tuning)]
+        L.om_server_autotune.argtypes = [vp, C.POINTER(Request), C.c_int, C.c_double,
+                                         C.POINTER(Tuning)]
+        L.om_server_mark.argtypes = [vp, _dp]
+        L.om_server_launches.argtypes = [vp]
+        L.om_server_launches.restype = C.c_long
+        L.om_server_last_error.argtypes = [vp]
+        L.om_server_last_error.restype = C.c_char_p
+        L.om_server_destroy.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -156,6 +190,12 @@ class Context:
         out = np.zeros(1)
         self.check(lib().om_context_mark(self.h, _p(out)))
         return float(out[0])
+
+    def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
+             matvec_carveout=-1):
+        """Launch tuning (om_context_tune); 0 / -1 keep the current value."""
+        t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout)
+        self.check(lib().om_context_tune(self.h, C.byref(t)))
 
     def timers(self, enable=True):
         """Kernel times since the last call: dict of (milliseconds, launches)."""
@@ -231,6 +271,9 @@ class Problem:
     def set_wavelength(self, wavelength):
         self.ctx.check(lib().om_problem_set_wavelength(self.h, wavelength))
 
+    def set_wave(self, wave: PlaneWave):
+        self.ctx.check(lib().om_problem_set_wave(self.h, C.byref(wave)))
+
     def tmatrix(self, harmonic=FF):
         out = np.zeros((self.N, 2 * self.P), np.complex128)
         self.ctx.check(lib().om_tmatrix(self.h, harmonic, _p(out)))
@@ -305,6 +348,14 @@ class Problem:
         self.ctx.check(lib().om_near_field(self.h, _p(xyz), xyz.shape[0], _p(E), _p(H)))
         return E, H
 
+    def near_field_sh(self, xyz):
+        """Second-harmonic E, H at Cartesian points (after solve_sh)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        E = np.zeros((xyz.shape[0], 3), np.complex128)
+        H = np.zeros_like(E)
+        self.ctx.check(lib().om_near_field_sh(self.h, _p(xyz), xyz.shape[0], _p(E), _p(H)))
+        return E, H
+
 
 def coupling(ctx: Context, rel_xyz, k: complex, nmax: int, regular: bool):
     """Coupling(relR, waveK, nMax, regular) for one or many Cartesian displacements."""
@@ -348,6 +399,88 @@ def wavelength_solve_sh(ctx: Context, spheres, bg, wave, opts=None, precision=C1
                                       _p(xsec), _p(xsh), C.byref(st))
     ctx.check(rc)
     return xsec, xsh, st
+
+
+class Server:
+    """Serving / batching runtime (om_server_*): `slots` contexts on one GPU
+    taking wavelength-solve requests in arrival order, admitted against an HBM
+    budget in bytes (0 = the device's free memory less 1/16)."""
+
+    def __init__(self, device: int = 0, budget: int = 0, slots: int = 2):
+        h = C.c_void_p()
+        rc = lib().om_server_create(device, budget, slots, C.byref(h))
+        if rc:
+            raise OptimetError(rc, "cannot create a server on device %d" % device)
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().om_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, spheres, bg, wave, opts=None, precision=C128, cluster_key=0) -> int:
+        rq = Request(C.cast(spheres, C.POINTER(Sphere)), len(spheres), precision, bg, wave,
+                     opts or options(), cluster_key)
+        t = C.c_ulonglong()
+        rc = lib().om_server_submit(self.h, C.byref(rq), C.byref(t))
+        if rc:
+            raise OptimetError(rc, lib().om_server_last_error(self.h).decode())
+        return t.value
+
+    def poll(self, ticket: int, wait: bool = True):
+        """None while pending (wait=False), else a dict of the result."""
+        r = Result()
+        rc = lib().om_server_poll(self.h, ticket, int(wait), C.byref(r))
+        if rc == PENDING:
+            return None
+        if rc:
+            raise OptimetError(rc, "unknown ticket %d" % ticket)
+        st = lambda s: {"iterations": s.iterations, "inner_iterations": s.inner_iterations,
+                        "rel_residual": s.rel_residual, "seconds": s.seconds}
+        return {"status": r.status, "slot": r.slot, "xsec": np.array(r.xsec[:]),
+                "xsec_sh": np.array(r.xsec_sh[:]), "ff": st(r.ff), "sh": st(r.sh),
+                "queue_ms": r.queue_ms, "service_ms": r.service_ms, "latency_ms": r.latency_ms,
+                "device_bytes": r.device_bytes}
+
+    def drain(self):
+        lib().om_server_drain(self.h)
+
+    def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
+             matvec_carveout=-1):
+        t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout)
+        rc = lib().om_server_tune(self.h, C.byref(t))
+        if rc:
+            raise OptimetError(rc, "server tune")
+
+    def mark(self) -> float:
+        out = np.zeros(1)
+        rc = lib().om_server_mark(self.h, _p(out))
+        if rc:
+            raise OptimetError(rc, "server mark")
+        return float(out[0])
+
+    def autotune(self, spheres, bg, wave, opts=None, precision=C128, cluster_key=1, count=4,
+                 step=0.25e-9):
+        """Pick the fastest built-in launch tuning for requests like this one;
+        returns it as a dict."""
+        rq = Request(C.cast(spheres, C.POINTER(Sphere)), len(spheres), precision, bg, wave,
+                     opts or options(), cluster_key)
+        t = Tuning()
+        rc = lib().om_server_autotune(self.h, C.byref(rq), count, step, C.byref(t))
+        if rc:
+            raise OptimetError(rc, lib().om_server_last_error(self.h).decode())
+        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+
+    def launches(self) -> int:
+        return int(lib().om_server_launches(self.h))
+
+    @property
+    def last_error(self) -> str:
+        return lib().om_server_last_error(self.h).decode()
 
 
 def declared_symbols():

@@ -38,28 +38,12 @@ int check_launch(om_context *ctx, const char *what) {
 }
 
 template <typename T> int dev_alloc(om_context *ctx, T **p, size_t count) {
-  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
-  if(ctx->budget && ctx->used + bytes > ctx->budget) {
-    ctx->err = "device-memory budget exceeded (" + std::to_string(ctx->used + bytes) + " > " +
-               std::to_string(ctx->budget) + " bytes)";
-    return OM_ERR_BUDGET;
-  }
-  cudaError_t e = cudaMalloc((void **)p, bytes);
-  if(e != cudaSuccess) {
-    cudaGetLastError();
-    ctx->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
-    return OM_ERR_BUDGET;
-  }
-  ctx->used += bytes;
-  return OM_OK;
+  return om::dev_malloc(ctx, (void **)p, std::max<size_t>(count, 1) * sizeof(T));
 }
 
 template <typename T> void dev_free(om_context *ctx, T *&p, size_t count) {
-  if(p) {
-    cudaFree(p);
-    ctx->used -= std::max<size_t>(count, 1) * sizeof(T);
-    p = nullptr;
-  }
+  om::dev_release(ctx, p, std::max<size_t>(count, 1) * sizeof(T));
+  p = nullptr;
 }
 
 void to_sph(double x, double y, double z, double *o) { om::to_spherical(x, y, z, o, o + 1, o + 2); }
@@ -171,16 +155,10 @@ void free_problem(om_problem *pr) {
   dev_free(ctx, pr->d_wsh, N * P);
   dev_free(ctx, pr->d_acs, N * P);
   for(int h = 0; h < 2; ++h) {
-    if(pr->d_S[h]) {
-      cudaFree(pr->d_S[h]);
-      ctx->used -= sizeof(double2) * n * n;
-      pr->d_S[h] = nullptr;
-    }
-    if(pr->d_S32[h]) {
-      cudaFree(pr->d_S32[h]);
-      ctx->used -= sizeof(float2) * n * n;
-      pr->d_S32[h] = nullptr;
-    }
+    om::dev_release(ctx, pr->d_S[h], sizeof(double2) * n * n);
+    pr->d_S[h] = nullptr;
+    om::dev_release(ctx, pr->d_S32[h], sizeof(float2) * n * n);
+    pr->d_S32[h] = nullptr;
   }
 }
 
@@ -323,6 +301,47 @@ int ensure_matrix(om_problem *pr, int harmonic, int precision) {
 }  // namespace
 
 namespace om {
+// Device memory is stream-ordered (cudaMallocAsync / cudaFreeAsync on the
+// context's stream, from the device's default pool): a release never waits
+// for other streams, so contexts that run side by side on one device (the
+// serving slots) do not serialise each other through allocation.
+int dev_malloc(om_context *ctx, void **p, size_t bytes) {
+  *p = nullptr;
+  if(ctx->budget && ctx->used + bytes > ctx->budget) {
+    ctx->err = "device-memory budget exceeded (" + std::to_string(ctx->used + bytes) + " > " +
+               std::to_string(ctx->budget) + " bytes)";
+    return OM_ERR_BUDGET;
+  }
+  cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
+  if(e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    ctx->err = std::string("cudaMallocAsync(") + std::to_string(bytes) +
+               " bytes): " + cudaGetErrorString(e);
+    return OM_ERR_BUDGET;
+  }
+  ctx->used += bytes;
+  return OM_OK;
+}
+
+void dev_release(om_context *ctx, void *p, size_t bytes) {
+  if(!p)
+    return;
+  cudaFreeAsync(p, ctx->stream);
+  ctx->used -= bytes;
+}
+
+// Drop one harmonic's matrix storage (the server frees the FF matrix before
+// the SH assembly).
+void release_matrix(om_problem *pr, int harmonic) {
+  const size_t nn = (size_t)pr->n * pr->n;
+  dev_release(pr->ctx, pr->d_S[harmonic], sizeof(double2) * nn);
+  pr->d_S[harmonic] = nullptr;
+  dev_release(pr->ctx, pr->d_S32[harmonic], sizeof(float2) * nn);
+  pr->d_S32[harmonic] = nullptr;
+  pr->S_prec[harmonic] = -1;
+}
+
 int sh_alloc(om_problem *pr) {
   om_context *ctx = pr->ctx;
   const size_t N = pr->N, P = pr->P, n = pr->n;
@@ -381,6 +400,21 @@ int om_context_mark(om_context *ctx, double *ms) {
   return OM_OK;
 }
 
+int om_context_tune(om_context *ctx, const om_tuning *t) {
+  if(!ctx || !t || t->matvec_ctas_per_sm > 64 || t->matvec_df_ctas_per_sm > 64 ||
+     t->assemble_carveout > 100 || t->matvec_carveout > 100)
+    return OM_ERR_INVALID;
+  if(t->matvec_ctas_per_sm > 0)
+    ctx->mv_ctas = t->matvec_ctas_per_sm;
+  if(t->matvec_df_ctas_per_sm > 0)
+    ctx->mv_ctas_df = t->matvec_df_ctas_per_sm;
+  if(t->assemble_carveout >= 0)
+    ctx->carve_asm = t->assemble_carveout;
+  if(t->matvec_carveout >= 0)
+    ctx->carve_mv = t->matvec_carveout;
+  return OM_OK;
+}
+
 int om_context_timers(om_context *ctx, int enable, double *out) {
   if(!ctx)
     return OM_ERR_INVALID;
@@ -418,10 +452,40 @@ int om_context_create(int device, size_t budget_bytes, om_context **out) {
     return OM_ERR_INVALID;
   ctx->device = device;
   ctx->budget = budget_bytes;
-  if(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    ctx->sm_count = 1;
+  // the context's stream at the highest priority, the assembly stream at the
+  // lowest: when contexts share the device, pending solve blocks are
+  // dispatched ahead of pending assembly blocks
+  int lo = 0, hi = 0;
+  cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  if(cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, hi) != cudaSuccess ||
+     cudaStreamCreateWithPriority(&ctx->stream_lo, cudaStreamNonBlocking, lo) != cudaSuccess ||
+     cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+     cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    if(ctx->stream) cudaStreamDestroy(ctx->stream);
+    if(ctx->stream_lo) cudaStreamDestroy(ctx->stream_lo);
     delete ctx;
     return OM_ERR_CUDA;
   }
+  if(cudaMalloc(&ctx->d_tile_counter, 256) != cudaSuccess) {
+    cudaGetLastError();
+    cudaStreamDestroy(ctx->stream);
+    cudaStreamDestroy(ctx->stream_lo);
+    cudaEventDestroy(ctx->ev_fork);
+    cudaEventDestroy(ctx->ev_join);
+    delete ctx;
+    return OM_ERR_CUDA;
+  }
+  // keep freed blocks in the default pool (process-local setting) so that
+  // repeated solves reuse them instead of returning memory to the driver
+  cudaMemPool_t pool;
+  if(cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    unsigned long long keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
   *out = ctx;
   return OM_OK;
 }
@@ -441,7 +505,16 @@ void om_context_destroy(om_context *ctx) {
     cudaFree(t.second);
   if(ctx->mark)
     cudaEventDestroy(ctx->mark);
+  cudaEventDestroy(ctx->ev_fork);
+  cudaEventDestroy(ctx->ev_join);
+  cudaFree(ctx->d_tile_counter);
+  cudaStreamDestroy(ctx->stream_lo);
   cudaStreamDestroy(ctx->stream);
+  // hand unused pool memory back (live allocations of other contexts stay)
+  cudaMemPool_t pool;
+  if(cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess)
+    cudaMemPoolTrimTo(pool, 0);
+  cudaGetLastError();
   delete ctx;
 }
 
@@ -488,6 +561,20 @@ int om_problem_set_wavelength(om_problem *pr, double wavelength) {
   cudaSetDevice(pr->ctx->device);
   pr->ctx->last_launches = 0;
   pr->lambda = wavelength;
+  return update_wave(pr);
+}
+
+int om_problem_set_wave(om_problem *pr, const om_plane_wave *wave) {
+  if(!pr || !wave || !(wave->wavelength > 0))
+    return OM_ERR_INVALID;
+  cudaSetDevice(pr->ctx->device);
+  pr->ctx->last_launches = 0;
+  pr->lambda = wave->wavelength;
+  pr->theta = wave->theta;
+  pr->phi = wave->phi;
+  pr->e_theta = cplx(wave->e_theta[0], wave->e_theta[1]);
+  pr->e_phi = cplx(wave->e_phi[0], wave->e_phi[1]);
+  pr->sh = wave->sh;
   return update_wave(pr);
 }
 
@@ -888,6 +975,71 @@ int om_get_sh_vectors(om_problem *pr, double *K, double *K1ana, double *X_sca_SH
   if(X_int_SH) cudaMemcpyAsync(X_int_SH, pr->d_Xish, b, cudaMemcpyDeviceToHost, pr->ctx->stream);
   cudaError_t e = cudaStreamSynchronize(pr->ctx->stream);
   return e == cudaSuccess ? OM_OK : cuda_fail(pr->ctx, e, "SH vectors");
+}
+
+int om_near_field_sh(om_problem *pr, const double *xyz, int npts, double *E, double *H) {
+  if(!pr || !xyz || npts < 1 || !E || !H)
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  if(!pr->have_sh) {
+    ctx->err = "no SH solution";
+    return OM_ERR_STATE;
+  }
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  std::vector<double> pts(3 * (size_t)npts);
+  for(int i = 0; i < npts; ++i) {
+    double s[3];
+    to_sph(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], s);
+    om::to_cartesian(s[0], s[1], s[2], &pts[3 * i], &pts[3 * i + 1], &pts[3 * i + 2]);
+  }
+  // Result.cpp:237-244: interior SH wave number and impedance per sphere
+  const cplx w0 = pr->omega * std::sqrt(kEps0 * kMu0);
+  std::vector<zd> kin(pr->N), izw(pr->N);
+  for(int j = 0; j < pr->N; ++j) {
+    const cplx k = cplx(2.0, 0.0) * w0 * std::sqrt(pr->eps_r_sh[j] * pr->mu_r[j]);
+    const cplx mu_sh = pr->mu_r[j] * kMu0, eps_sh = pr->eps_r_sh[j] * kEps0;
+    const cplx iz = (cplx(0.0, -1.0) / std::sqrt(mu_sh / eps_sh)) * w0;
+    kin[j] = om::mk(k.real(), k.imag());
+    izw[j] = om::mk(iz.real(), iz.imag());
+  }
+  double *d_xyz = nullptr;
+  zd *d_E = nullptr, *d_H = nullptr, *d_k = nullptr;
+  int *d_inner = nullptr;
+  const size_t np = (size_t)npts;
+  int rc = dev_alloc(ctx, &d_xyz, 3 * np);
+  if(!rc) rc = dev_alloc(ctx, &d_E, 3 * np);
+  if(!rc) rc = dev_alloc(ctx, &d_H, 3 * np);
+  if(!rc) rc = dev_alloc(ctx, &d_k, 2 * (size_t)pr->N);
+  if(!rc) rc = dev_alloc(ctx, &d_inner, np);
+  if(!rc) {
+    cudaMemcpyAsync(d_xyz, pts.data(), sizeof(double) * pts.size(), cudaMemcpyHostToDevice,
+                    ctx->stream);
+    cudaMemcpyAsync(d_k, kin.data(), sizeof(zd) * pr->N, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d_k + pr->N, izw.data(), sizeof(zd) * pr->N, cudaMemcpyHostToDevice,
+                    ctx->stream);
+    try {
+      om::launch_near_field_sh(pr, d_xyz, npts, w0, d_k, d_k + pr->N, d_inner, d_E, d_H);
+      rc = check_launch(ctx, "SH near field");
+    } catch(std::exception &e) {
+      ctx->err = e.what();
+      rc = OM_ERR_CUDA;
+    }
+    if(!rc) {
+      cudaMemcpyAsync(E, d_E, sizeof(zd) * 3 * np, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaMemcpyAsync(H, d_H, sizeof(zd) * 3 * np, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if(e != cudaSuccess)
+        rc = cuda_fail(ctx, e, "SH near field");
+    }
+  }
+  cudaStreamSynchronize(ctx->stream);
+  dev_free(ctx, d_xyz, 3 * np);
+  dev_free(ctx, d_E, 3 * np);
+  dev_free(ctx, d_H, 3 * np);
+  dev_free(ctx, d_k, 2 * (size_t)pr->N);
+  dev_free(ctx, d_inner, np);
+  return rc;
 }
 
 int om_sh_cross_sections(om_problem *pr, double out[2]) {

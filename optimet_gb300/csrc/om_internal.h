@@ -61,7 +61,15 @@ struct Arena;
 
 struct om_context {
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;     // every call's work, in order (highest priority)
+  cudaStream_t stream_lo = nullptr;  // matrix assembly, forked from / joined to `stream`
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int sm_count = 1;
+  // matvec grid caps, CTAs per SM (the kernels walk their tiles with a grid
+  // stride): below the SM's capacity so that another slot's assembly fits
+  int mv_ctas = 8, mv_ctas_df = 8;
+  unsigned long long *d_tile_counter = nullptr;  // matvec tile counter (device)
+  int carve_asm = -1, carve_mv = -1;  // preferred smem carveout (percent), -1 = driver's choice
   size_t budget = 0;
   size_t used = 0;
   std::string err;
@@ -142,6 +150,10 @@ int sh_alloc(om_problem *pr);
 void launch_sh_source(om_problem *pr);
 void launch_sh_internal(om_problem *pr);
 void launch_sh_cross_sections(om_problem *pr, double *d_out2);
+// w0 = waveK_0; d_kin / d_izw per sphere: 2 waveK_0 sqrt(eps_r_SH mu_r) and
+// waveK_0 (-i) / sqrt(mu_SH / eps_SH); d_inner: npts ints of scratch.
+void launch_near_field_sh(om_problem *pr, const double *d_xyz, int npts, cplx w0, const zd *d_kin,
+                          const zd *d_izw, int *d_inner, zd *d_E, zd *d_H);
 
 // field.cu
 void launch_internal(om_problem *pr);
@@ -156,6 +168,11 @@ int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, co
                      double2 *x, om_solve_stats *st);
 int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
                        double2 *x, om_solve_stats *st);
+
+// capi.cu: stream-ordered device memory counted against the context budget
+int dev_malloc(om_context *ctx, void **p, size_t bytes);
+void dev_release(om_context *ctx, void *p, size_t bytes);
+void release_matrix(om_problem *pr, int harmonic);
 
 inline int blocks_for(long n, int threads) { return (int)((n + threads - 1) / threads); }
 

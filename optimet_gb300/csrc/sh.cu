@@ -11,6 +11,7 @@
 #include <stdexcept>
 #include <vector>
 
+#include "om_field.cuh"
 #include "om_internal.h"
 
 namespace om {
@@ -24,7 +25,7 @@ enum { T_C10m1, T_C11m1, T_C00m1, T_C01m1, T_Wm1m1, T_W11, T_W00, T_W10, T_W01 }
 __device__ __forceinline__ bool tri(int a, int b, int c) { return c >= abs(a - b) && c <= a + b; }
 __device__ __forceinline__ double fk(const double *f, int n) { return n < 0 ? 0.0 : f[n]; }
 
-__device__ double w3j(const double *f, int j1, int j2, int j3, int m1, int m2, int m3) {
+__device__ __noinline__ double w3j(const double *f, int j1, int j2, int j3, int m1, int m2, int m3) {
   if(j1 < 0 || j2 < 0 || j3 < 0 || !tri(j1, j2, j3) || m1 + m2 + m3 != 0 || abs(m1) > j1 ||
      abs(m2) > j2 || abs(m3) > j3)
     return 0.0;
@@ -47,7 +48,7 @@ __device__ __forceinline__ double tdelta(const double *f, int a, int b, int c) {
   return sqrt(fk(f, a + b - c) * fk(f, a - b + c) * fk(f, -a + b + c) / fk(f, a + b + c + 1));
 }
 
-__device__ double w6j(const double *f, int j1, int j2, int j3, int j4, int j5, int j6) {
+__device__ __noinline__ double w6j(const double *f, int j1, int j2, int j3, int j4, int j5, int j6) {
   if(j1 < 0 || j2 < 0 || j3 < 0 || j4 < 0 || j5 < 0 || j6 < 0)
     return 0.0;
   if(!tri(j1, j2, j3) || !tri(j1, j5, j6) || !tri(j4, j2, j6) || !tri(j4, j5, j3))
@@ -65,7 +66,7 @@ __device__ double w6j(const double *f, int j1, int j2, int j3, int j4, int j5, i
          tdelta(f, j4, j5, j3) * sum;
 }
 
-__device__ double w9j(const double *f, int a, int b, int c, int d, int e, int g6, int g, int h, int i) {
+__device__ __noinline__ double w9j(const double *f, int a, int b, int c, int d, int e, int g6, int g, int h, int i) {
   if(a < 0 || b < 0 || c < 0 || d < 0 || e < 0 || g6 < 0 || g < 0 || h < 0 || i < 0)
     return 0.0;
   const int xmin = max(abs(a - i), max(abs(h - d), abs(b - g6)));
@@ -78,10 +79,10 @@ __device__ double w9j(const double *f, int a, int b, int c, int d, int e, int g6
 }
 
 // Symbol.cpp:39-43 and :110-116
-__device__ double cg(const double *f, int j, int m, int j1, int m1, int j2, int m2) {
+__device__ __noinline__ double cg(const double *f, int j, int m, int j1, int m1, int j2, int m2) {
   return (((m + j1 - j2) & 1) ? -1.0 : 1.0) * sqrt(2.0 * j + 1.0) * w3j(f, j1, j2, j, m1, m2, -m);
 }
-__device__ double Wf(const double *f, int L1, int J1, int M1, int L2, int J2, int M2, int L, int M) {
+__device__ __noinline__ double Wf(const double *f, int L1, int J1, int M1, int L2, int J2, int M2, int L, int M) {
   return (((J2 + L1 + L) & 1) ? -1.0 : 1.0) *
          sqrt((2.0 * J1 + 1.0) * (2.0 * J2 + 1.0) * (2.0 * L1 + 1.0) * (2.0 * L2 + 1.0) /
               (4.0 * kPi * (2.0 * L + 1.0))) *
@@ -253,13 +254,66 @@ __global__ void k_sh_internal(const zd *X, const zd *K1, const zd *shf, int nmax
   Xi[idx] = X[idx] * f - K1[idx];
 }
 
+// The bulk (gamma) sums CXm1 / CXp1 (Symbol.cpp:478-620) for SH harmonic k =
+// (J, M) of one sphere at radius r; xi = that sphere's FF internal
+// coefficients [c | d], d/dd/ddd = j_n(k1 r) and its first two derivatives.
+// Only the (p, q) with m_q = M - m_p are visited (the tables vanish elsewhere).
+__device__ void cx_sums(int k, int J, int M, int nmax, const zd *xi, const double *tab,
+                        const zd *d, const zd *dd, const zd *ddd, zd k1, double r, zd c_bulk,
+                        zd &Xm1, zd &Xp1) {
+  const int P = pmax(nmax);
+  const size_t sz = (size_t)P * P * P;
+  const double sn = sqrt((double)(J * (J + 1)));
+  const zd rk2 = 1.0 / (k1 * k1);
+  Xm1 = mk(0.0, 0.0);
+  Xp1 = mk(0.0, 0.0);
+  for(int p = 0; p < P; ++p) {
+    int n1, m1;
+    nm_of(p, n1, m1);
+    const int m2 = M - m1;
+    if(m2 < -nmax || m2 > nmax)
+      continue;
+    const zd c1 = xi[p], d1 = xi[P + p];
+    for(int n2 = max(1, abs(m2)); n2 <= nmax; ++n2) {
+      const int q = flat(n2, m2);
+      const size_t at = ((size_t)k * P + p) * P + q;
+      const double Wm = tab[T_Wm1m1 * sz + at], W1 = tab[T_W11 * sz + at], W0 = tab[T_W00 * sz + at];
+      const zd c2 = xi[q], d2 = xi[P + q];
+      const zd F00 = d[n1] * dd[n2];
+      const zd F11 = (k1 * dd[n2] + d[n2] / r) * (k1 * dd[n1] + d[n1] / r);
+      const zd Fm = (1.0 / (r * r)) * (d[n1] * d[n2]);
+      const zd Fd00 = d[n1] * dd[n2] * k1 + k1 * dd[n1] * d[n2];
+      const zd Fd11 = ((k1 * k1) * ddd[n1] - (1.0 / (r * r)) * d[n1] + (1.0 / r) * k1 * dd[n1]) *
+                          (k1 * dd[n2] + d[n2] / r) +
+                      ((k1 * k1) * ddd[n2] - (1.0 / (r * r)) * d[n2] + (1.0 / r) * k1 * dd[n2]) *
+                          (k1 * dd[n1] + d[n1] / r);
+      const zd Fdm = (1.0 / (r * r)) * (k1 * dd[n1] * d[n2] + d[n1] * k1 * dd[n2]) -
+                     (2.0 / (r * r * r)) * (d[n1] * d[n2]);
+      const double sq = sqrt((double)(n1 * n2 * (n1 + 1) * (n2 + 1)));
+      Xm1 = Xm1 + c_bulk * (c1 * c2 * W0 * Fd00 + d1 * d2 * rk2 * (W1 * Fd11 + Wm * sq * Fdm));
+      Xp1 = Xp1 + c_bulk * (c1 * c2 * W0 * sn * (1.0 / r) * F00 +
+                            d1 * d2 * rk2 * (W1 * sn * (1.0 / r) * F11 + Wm * sq * sn * (1.0 / r) * Fm));
+    }
+  }
+}
+
+// j_n(z), j_n'(z), j_n''(z) for n <= nmax (bessel3der, Bessel.h:145-245).
+__device__ void bessel_j012(zd z, int nmax, zd *d, zd *dd, zd *ddd) {
+  bessel_deriv(0, z, nmax, d, dd);
+  ddd[0] = mk(0.0, 0.0);
+  for(int i = 1; i <= nmax; ++i) {
+    ddd[i] = -((double(i) / z) * dd[i]) + (double(i) / (z * z)) * d[i] + dd[i - 1];
+    if(z.im == 0.0)
+      ddd[i].im = 0.0;
+  }
+}
+
 // ACSshcoeff (Symbol.cpp:358-477) per (sphere, SH harmonic): 4-point
 // Gauss-Legendre radial integral.
 __global__ void __launch_bounds__(256) k_sh_abs(const ShScalars *shs, const zd *Xint,
                                                 const zd *Xish, const double *tab, int nmax,
                                                 double omega, zd *acs) {
   const int j = blockIdx.x, P = pmax(nmax);
-  const size_t sz = (size_t)P * P * P;
   __shared__ zd d[4][kMaxNmax + 2], dd[4][kMaxNmax + 2], ddd[4][kMaxNmax + 2];
   __shared__ zd ds[4][kMaxNmax + 2], dds[4][kMaxNmax + 2];
   const double xi[4] = {-0.3399810435848563, 0.3399810435848563, -0.8611363115940526,
@@ -272,18 +326,11 @@ __global__ void __launch_bounds__(256) k_sh_abs(const ShScalars *shs, const zd *
     const int g = threadIdx.x;
     const double r = (R / 2.0) * xi[g] + R / 2.0;
     const zd z = r * c.k1;
-    bessel_deriv(0, z, nmax, d[g], dd[g]);
-    // second derivatives (bessel3der, Bessel.h:145-245)
-    ddd[g][0] = mk(0.0, 0.0);
-    for(int i = 1; i <= nmax; ++i) {
-      ddd[g][i] = -((double(i) / z) * dd[g][i]) + (double(i) / (z * z)) * d[g][i] + dd[g][i - 1];
-      if(z.im == 0.0)
-        ddd[g][i].im = 0.0;
-    }
+    bessel_j012(z, nmax, d[g], dd[g], ddd[g]);
     bessel_deriv(0, r * c.kSH, nmax, ds[g], dds[g]);
   }
   __syncthreads();
-  const zd k1 = c.k1, rk2 = 1.0 / (k1 * k1);
+  const zd k1 = c.k1;
   for(int k = threadIdx.x; k < P; k += blockDim.x) {
     int J, M;
     nm_of(k, J, M);
@@ -293,38 +340,9 @@ __global__ void __launch_bounds__(256) k_sh_abs(const ShScalars *shs, const zd *
     for(int g = 0; g < 4; ++g) {
       const double r = (R / 2.0) * xi[g] + R / 2.0;
       zd Xm1 = mk(0.0, 0.0), Xp1 = mk(0.0, 0.0);
-      if(c.has_gamma) {
-        for(int p = 0; p < P; ++p) {
-          int n1, m1;
-          nm_of(p, n1, m1);
-          const int m2 = M - m1;
-          if(m2 < -nmax || m2 > nmax)
-            continue;
-          const zd c1 = Xint[(size_t)j * 2 * P + p], d1 = Xint[(size_t)j * 2 * P + P + p];
-          for(int n2 = max(1, abs(m2)); n2 <= nmax; ++n2) {
-            const int q = flat(n2, m2);
-            const size_t at = ((size_t)k * P + p) * P + q;
-            const double Wm = tab[T_Wm1m1 * sz + at], W1 = tab[T_W11 * sz + at],
-                         W0 = tab[T_W00 * sz + at];
-            const zd c2 = Xint[(size_t)j * 2 * P + q], d2 = Xint[(size_t)j * 2 * P + P + q];
-            const zd F00 = d[g][n1] * dd[g][n2];
-            const zd F11 = (k1 * dd[g][n2] + d[g][n2] / r) * (k1 * dd[g][n1] + d[g][n1] / r);
-            const zd Fm = (1.0 / (r * r)) * (d[g][n1] * d[g][n2]);
-            const zd Fd00 = d[g][n1] * dd[g][n2] * k1 + k1 * dd[g][n1] * d[g][n2];
-            const zd Fd11 =
-                ((k1 * k1) * ddd[g][n1] - (1.0 / (r * r)) * d[g][n1] + (1.0 / r) * k1 * dd[g][n1]) *
-                    (k1 * dd[g][n2] + d[g][n2] / r) +
-                ((k1 * k1) * ddd[g][n2] - (1.0 / (r * r)) * d[g][n2] + (1.0 / r) * k1 * dd[g][n2]) *
-                    (k1 * dd[g][n1] + d[g][n1] / r);
-            const zd Fdm = (1.0 / (r * r)) * (k1 * dd[g][n1] * d[g][n2] + d[g][n1] * k1 * dd[g][n2]) -
-                           (2.0 / (r * r * r)) * (d[g][n1] * d[g][n2]);
-            const double sq = sqrt((double)(n1 * n2 * (n1 + 1) * (n2 + 1)));
-            Xm1 = Xm1 + c.c_bulk * (c1 * c2 * W0 * Fd00 + d1 * d2 * rk2 * (W1 * Fd11 + Wm * sq * Fdm));
-            Xp1 = Xp1 + c.c_bulk * (c1 * c2 * W0 * sn * (1.0 / r) * F00 +
-                                    d1 * d2 * rk2 * (W1 * sn * (1.0 / r) * F11 + Wm * sq * sn * (1.0 / r) * Fm));
-          }
-        }
-      }
+      if(c.has_gamma)
+        cx_sums(k, J, M, nmax, Xint + (size_t)j * 2 * P, tab, d[g], dd[g], ddd[g], k1, r, c.c_bulk,
+                Xm1, Xp1);
       const zd w01 = c.w01;
       const zd rkSH = 1.0 / c.kSH;
       const zd Xm1SH = w01 * dmn * rkSH * sn * (1.0 / r) * ds[g][J];
@@ -369,6 +387,124 @@ __global__ void __launch_bounds__(256) k_sh_xsec(const ShScalars *shs, const zd 
   if(threadIdx.x == 0) {
     out[0] = (1.0 / (4.0 * arbcf)) * red[0][0];
     out[1] = red[1][0];
+  }
+}
+
+struct ShFieldArgs {
+  const double *xyz;     // points, Cartesian (after the reader's spherical round trip)
+  int npts;
+  const double *cart;    // sphere centres
+  const double *radius;
+  int N, nmax;
+  const zd *Xsh, *Xish;  // SH scattered / internal coefficients
+  const zd *Xint;        // FF internal coefficients (particular solution)
+  const ShScalars *shs;
+  const double *tab;     // the nine SH coupling tables
+  zd k2b;                // 2 waveK (background, second harmonic)
+  zd iZw;                // iZ waveK_0 (background)
+  zd w0;                 // waveK_0
+  const zd *k_in;        // per sphere: 2 waveK_0 sqrt(eps_r_SH mu_r_SH)
+  const zd *iZw_in;      // per sphere: -i / sqrt(mu_SH / eps_SH) waveK_0
+  int *inner;            // per point: index of the sphere holding it, or -1
+  zd *E, *H;
+};
+
+// Result::getEHFields, second-harmonic half (Result.cpp:166-199 outside,
+// 237-276 inside), without the particular solution (k_near_field_sh_gamma).
+__global__ void __launch_bounds__(128) k_near_field_sh(ShFieldArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= a.npts)
+    return;
+  const int P = pmax(a.nmax);
+  const double px = a.xyz[3 * i], py = a.xyz[3 * i + 1], pz = a.xyz[3 * i + 2];
+  zd E[3] = {mk(0, 0), mk(0, 0), mk(0, 0)}, H[3] = {mk(0, 0), mk(0, 0), mk(0, 0)};
+  int inner = -1;
+  for(int j = 0; j < a.N; ++j) {
+    double r, t, p;
+    to_spherical(px - a.cart[3 * j], py - a.cart[3 * j + 1], pz - a.cart[3 * j + 2], &r, &t, &p);
+    if(r <= a.radius[j]) {
+      inner = j;
+      break;
+    }
+  }
+  zd el[3], hl[3];
+  if(inner < 0) {
+    for(int j = 0; j < a.N; ++j) {
+      double r, t, p;
+      to_spherical(px - a.cart[3 * j], py - a.cart[3 * j + 1], pz - a.cart[3 * j + 2], &r, &t, &p);
+      const zd *c = a.Xsh + (size_t)j * 2 * P;
+      vswf_sum(r, t, p, a.k2b, 0, a.nmax, c, c + P, el, hl);
+      project_add(t, p, el, a.w0, E);
+      project_add(t, p, hl, a.iZw, H);
+    }
+  } else {
+    double r, t, p;
+    to_spherical(px - a.cart[3 * inner], py - a.cart[3 * inner + 1], pz - a.cart[3 * inner + 2],
+                 &r, &t, &p);
+    const zd *c = a.Xish + (size_t)inner * 2 * P;
+    vswf_sum(r, t, p, a.k_in[inner], 1, a.nmax, c, c + P, el, hl);
+    project_add(t, p, el, a.w0, E);
+    project_add(t, p, hl, a.iZw_in[inner], H);
+  }
+  a.inner[i] = inner;
+  for(int q = 0; q < 3; ++q) {
+    a.E[3 * (size_t)i + q] = E[q];
+    a.H[3 * (size_t)i + q] = H[q];
+  }
+}
+
+// The particular solution inside spheres with a bulk chi(2) (gamma != 0):
+// E_SH += sum_k (Xm_k CXm1_k + Xp_k CXp1_k) (Result.cpp:260-262 with
+// Result::setFields / Geometry::COEFFpartSH, Result.cpp:906-919,
+// Geometry.cpp:458-491; Xm, Xp: AuxCoefficients.cpp:134-176). One CTA per
+// point; points outside every such sphere return at once.
+__global__ void __launch_bounds__(128) k_near_field_sh_gamma(ShFieldArgs a) {
+  const int i = blockIdx.x;
+  const int j = a.inner[i];
+  if(j < 0 || !a.shs[j].has_gamma)
+    return;
+  const int P = pmax(a.nmax), nmax = a.nmax;
+  __shared__ zd d[kMaxNmax + 2], dd[kMaxNmax + 2], ddd[kMaxNmax + 2];
+  __shared__ zd red[3][128];
+  double r, t, ph;
+  to_spherical(a.xyz[3 * i] - a.cart[3 * j], a.xyz[3 * i + 1] - a.cart[3 * j + 1],
+               a.xyz[3 * i + 2] - a.cart[3 * j + 2], &r, &t, &ph);
+  const ShScalars c = a.shs[j];
+  if(threadIdx.x == 0)
+    bessel_j012(r * c.k1, nmax, d, dd, ddd);
+  __syncthreads();
+  zd acc[3] = {mk(0, 0), mk(0, 0), mk(0, 0)};
+  const bool pole = fabs(t) < 1e-10 || (fabs(t) - kPi + 1e-10) > 0.0;
+  const double inv_trig = pole ? 1.0 / cos(t) : 1.0 / sin(t);
+  for(int k = threadIdx.x; k < P; k += blockDim.x) {
+    int J, M;
+    nm_of(k, J, M);
+    zd cxm, cxp;
+    cx_sums(k, J, M, nmax, a.Xint + (size_t)j * 2 * P, a.tab, d, dd, ddd, c.k1, r, c.c_bulk, cxm,
+            cxp);
+    double W[kMaxNmax + 1], dW[kMaxNmax + 1];
+    vigdvig(nmax, M, t, W, dW);
+    const double A = (M == 0) ? 0.0 : (pole ? M * inv_trig * dW[J] : M * inv_trig * W[J]);
+    const double dn = sqrt((2.0 * J + 1.0) / (4.0 * kPi * (double)(J * (J + 1))));
+    double sn, cs;
+    sincos(M * ph, &sn, &cs);
+    const zd cb = (((M & 1) ? -1.0 : 1.0) * dn) * mk(cs, sn);
+    const zd cx = sqrt((double)(J * (J + 1))) * cb;
+    // Xm = cx (W, 0, 0), Xp = cb (0, dW, iA), in local spherical components
+    const zd xm[3] = {cx * W[J], mk(0, 0), mk(0, 0)};
+    const zd cbA = cb * A;
+    const zd xp[3] = {mk(0, 0), cb * dW[J], mk(-cbA.im, cbA.re)};
+    project_add(t, ph, xm, cxm, acc);
+    project_add(t, ph, xp, cxp, acc);
+  }
+  for(int q = 0; q < 3; ++q)
+    red[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  if(threadIdx.x < 3) {
+    zd s = mk(0, 0);
+    for(int u = 0; u < (int)blockDim.x; ++u)
+      s = s + red[threadIdx.x][u];
+    a.E[3 * (size_t)i + threadIdx.x] = a.E[3 * (size_t)i + threadIdx.x] + s;
   }
 }
 
@@ -419,6 +555,42 @@ void launch_sh_cross_sections(om_problem *pr, double *d_out2) {
   k_sh_xsec<<<1, 256, 0, ctx->stream>>>(pr->d_shs, pr->d_Xsh, pr->d_wsh, pr->d_acs, pr->N, pr->nmax,
                                         arbcf, mk(pr->eta.real(), pr->eta.imag()), d_out2);
   ctx->last_launches += 2;
+}
+
+void launch_near_field_sh(om_problem *pr, const double *d_xyz, int npts, cplx w0, const zd *d_kin,
+                          const zd *d_izw, int *d_inner, zd *d_E, zd *d_H) {
+  om_context *ctx = pr->ctx;
+  ShFieldArgs a;
+  a.xyz = d_xyz;
+  a.npts = npts;
+  a.cart = pr->d_cart;
+  a.radius = pr->d_radius;
+  a.N = pr->N;
+  a.nmax = pr->nmax;
+  a.Xsh = pr->d_Xsh;
+  a.Xish = pr->d_Xish;
+  a.Xint = pr->d_Xint;
+  a.shs = pr->d_shs;
+  a.tab = nullptr;
+  const cplx k2b = cplx(2.0, 0.0) * pr->waveK, iZw = pr->iZ * w0;
+  a.k2b = mk(k2b.real(), k2b.imag());
+  a.iZw = mk(iZw.real(), iZw.imag());
+  a.w0 = mk(w0.real(), w0.imag());
+  a.k_in = d_kin;
+  a.iZw_in = d_izw;
+  a.inner = d_inner;
+  a.E = d_E;
+  a.H = d_H;
+  k_near_field_sh<<<blocks_for(npts, 128), 128, 0, ctx->stream>>>(a);
+  ctx->last_launches++;
+  bool gamma = false;
+  for(const auto &g : pr->gamma)
+    gamma = gamma || g != cplx(0.0, 0.0);
+  if(gamma) {
+    a.tab = clg_tables_dev(ctx, pr->nmax);
+    k_near_field_sh_gamma<<<npts, 128, 0, ctx->stream>>>(a);
+    ctx->last_launches++;
+  }
 }
 
 }  // namespace om

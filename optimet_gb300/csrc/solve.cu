@@ -50,45 +50,66 @@ template <typename V> __device__ __forceinline__ V cfma_conj(V a, V b, V c) {  /
 constexpr int kMvThreads = 256;
 constexpr int kMvCols = 1024;  // columns per split-K chunk (x staged in shared memory)
 
-// Partial y over a chunk of columns: part[s * n + i] = sum_{j in chunk s} S[j ld + i] x[j]
+// Partial y over chunks of columns: part[s * n + i] = sum_{j in chunk s} S[j ld + i] x[j].
+// A tile is kMvThreads rows x kMvCols columns; the grid is capped (a few CTAs
+// per SM) and the CTAs take tiles from a counter (*next, zeroed before the
+// launch) in column-chunk-major order, so the kernel leaves room on every SM
+// for the assembly kernel of another slot and still balances its load. Eight columns'
+// loads are issued before their FMAs; the two accumulators take alternate
+// columns.
 template <typename M, typename V>
 __global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld, long n, const V *x,
-                                                           V *part) {
+                                                           V *part, int row_tiles, long tiles,
+                                                           unsigned long long *next) {
   __shared__ V xs[kMvCols];
-  const long i = blockIdx.x * (long)kMvThreads + threadIdx.x;
-  const long j0 = blockIdx.y * (long)kMvCols;
-  const long j1 = min(n, j0 + kMvCols);
-  for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads)
-    xs[j - j0] = x[j];
-  __syncthreads();
-  if(i >= n)
-    return;
-  V acc0, acc1;
-  acc0.x = acc0.y = acc1.x = acc1.y = 0;
-  const M *col = S + j0 * ld + i;
-  long j = j0;
-  for(; j + 3 < j1; j += 4) {
-    M s0 = col[0], s1 = col[ld], s2 = col[2 * ld], s3 = col[3 * ld];
-    V a0, a1, a2, a3;
-    a0.x = s0.x; a0.y = s0.y; a1.x = s1.x; a1.y = s1.y;
-    a2.x = s2.x; a2.y = s2.y; a3.x = s3.x; a3.y = s3.y;
-    acc0 = cfma(a0, xs[j - j0], acc0);
-    acc1 = cfma(a1, xs[j - j0 + 1], acc1);
-    acc0 = cfma(a2, xs[j - j0 + 2], acc0);
-    acc1 = cfma(a3, xs[j - j0 + 3], acc1);
-    col += 4 * ld;
+  __shared__ long tile;
+  for(;;) {
+    __syncthreads();
+    if(threadIdx.x == 0)
+      tile = (long)atomicAdd(next, 1ull);
+    __syncthreads();
+    const long t = tile;
+    if(t >= tiles)
+      break;
+    const long ct = t / row_tiles, rt = t - ct * row_tiles;
+    const long i = rt * kMvThreads + threadIdx.x;
+    const long j0 = ct * kMvCols;
+    const long j1 = min(n, j0 + kMvCols);
+    for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads)
+      xs[j - j0] = x[j];
+    __syncthreads();
+    if(i >= n)
+      continue;
+    V acc0, acc1;
+    acc0.x = acc0.y = acc1.x = acc1.y = 0;
+    const M *col = S + j0 * ld + i;
+    long j = j0;
+    for(; j + 7 < j1; j += 8) {
+      M s[8];
+#pragma unroll
+      for(int u = 0; u < 8; ++u)
+        s[u] = col[u * ld];
+#pragma unroll
+      for(int u = 0; u < 8; u += 2) {
+        V a0, a1;
+        a0.x = s[u].x; a0.y = s[u].y; a1.x = s[u + 1].x; a1.y = s[u + 1].y;
+        acc0 = cfma(a0, xs[j - j0 + u], acc0);
+        acc1 = cfma(a1, xs[j - j0 + u + 1], acc1);
+      }
+      col += 8 * ld;
+    }
+    for(; j < j1; ++j) {
+      M s0 = col[0];
+      V a0;
+      a0.x = s0.x;
+      a0.y = s0.y;
+      acc0 = cfma(a0, xs[j - j0], acc0);
+      col += ld;
+    }
+    acc0.x += acc1.x;
+    acc0.y += acc1.y;
+    part[ct * n + i] = acc0;
   }
-  for(; j < j1; ++j) {
-    M s0 = col[0];
-    V a0;
-    a0.x = s0.x;
-    a0.y = s0.y;
-    acc0 = cfma(a0, xs[j - j0], acc0);
-    col += ld;
-  }
-  acc0.x += acc1.x;
-  acc0.y += acc1.y;
-  part[blockIdx.y * n + i] = acc0;
 }
 
 // Complex64 matrix times a complex128 vector with FP64-accurate results from
@@ -108,47 +129,71 @@ __device__ __forceinline__ void df_add(DF &a, float p) {
   a.hi = s;
 }
 __global__ void __launch_bounds__(kMvThreads) k_matvec_part_df(const float2 *S, long ld, long n,
-                                                               const double2 *x, double2 *part) {
+                                                               const double2 *x, double2 *part,
+                                                               int row_tiles, long tiles,
+                                                               unsigned long long *next) {
   __shared__ float4 xs[kMvCols];
-  const long i = blockIdx.x * (long)kMvThreads + threadIdx.x;
-  const long j0 = blockIdx.y * (long)kMvCols;
-  const long j1 = min(n, j0 + kMvCols);
-  for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads) {
-    const double2 v = x[j];
-    const float hr = (float)v.x, hi = (float)v.y;
-    xs[j - j0] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+  __shared__ long tile;
+  for(;;) {
+    __syncthreads();
+    if(threadIdx.x == 0)
+      tile = (long)atomicAdd(next, 1ull);
+    __syncthreads();
+    const long t = tile;
+    if(t >= tiles)
+      break;
+    const long ct = t / row_tiles, rt = t - ct * row_tiles;
+    const long i = rt * kMvThreads + threadIdx.x;
+    const long j0 = ct * kMvCols;
+    const long j1 = min(n, j0 + kMvCols);
+    for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads) {
+      const double2 v = x[j];
+      const float hr = (float)v.x, hi = (float)v.y;
+      xs[j - j0] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+    }
+    __syncthreads();
+    if(i >= n)
+      continue;
+    DF re{0.f, 0.f}, im{0.f, 0.f};
+    float er = 0.f, ei = 0.f;
+    const float2 *col = S + j0 * ld + i;
+    for(long j = j0; j < j1; j += 4) {
+      // four columns' loads in flight, then the same per-column arithmetic
+      float2 av[4];
+      const int cnt = (int)min(4L, j1 - j);
+#pragma unroll
+      for(int u = 0; u < 4; ++u)
+        av[u] = u < cnt ? col[u * ld] : make_float2(0.f, 0.f);
+#pragma unroll
+      for(int u = 0; u < 4; ++u) {
+        if(u >= cnt)
+          break;
+        const float2 a = av[u];
+        const float4 v = xs[j - j0 + u];
+        // __fmul_rn keeps the products out of FMA contraction so that the
+        // TwoProduct error terms below are exact
+        float p = __fmul_rn(a.x, v.x);
+        er += fmaf(a.x, v.x, -p);
+        df_add(re, p);
+        p = __fmul_rn(-a.y, v.y);
+        er += fmaf(-a.y, v.y, -p);
+        df_add(re, p);
+        er = fmaf(a.x, v.z, er);
+        er = fmaf(-a.y, v.w, er);
+        p = __fmul_rn(a.x, v.y);
+        ei += fmaf(a.x, v.y, -p);
+        df_add(im, p);
+        p = __fmul_rn(a.y, v.x);
+        ei += fmaf(a.y, v.x, -p);
+        df_add(im, p);
+        ei = fmaf(a.x, v.w, ei);
+        ei = fmaf(a.y, v.z, ei);
+      }
+      col += 4 * ld;
+    }
+    part[ct * n + i] = make_double2((double)re.hi + ((double)re.lo + (double)er),
+                                    (double)im.hi + ((double)im.lo + (double)ei));
   }
-  __syncthreads();
-  if(i >= n)
-    return;
-  DF re{0.f, 0.f}, im{0.f, 0.f};
-  float er = 0.f, ei = 0.f;
-  const float2 *col = S + j0 * ld + i;
-  for(long j = j0; j < j1; ++j) {
-    const float2 a = *col;
-    const float4 v = xs[j - j0];
-    col += ld;
-    // __fmul_rn keeps the products out of FMA contraction so that the
-    // TwoProduct error terms below are exact
-    float p = __fmul_rn(a.x, v.x);
-    er += fmaf(a.x, v.x, -p);
-    df_add(re, p);
-    p = __fmul_rn(-a.y, v.y);
-    er += fmaf(-a.y, v.y, -p);
-    df_add(re, p);
-    er = fmaf(a.x, v.z, er);
-    er = fmaf(-a.y, v.w, er);
-    p = __fmul_rn(a.x, v.y);
-    ei += fmaf(a.x, v.y, -p);
-    df_add(im, p);
-    p = __fmul_rn(a.y, v.x);
-    ei += fmaf(a.y, v.x, -p);
-    df_add(im, p);
-    ei = fmaf(a.x, v.w, ei);
-    ei = fmaf(a.y, v.z, ei);
-  }
-  part[blockIdx.y * n + i] =
-      make_double2((double)re.hi + ((double)re.lo + (double)er), (double)im.hi + ((double)im.lo + (double)ei));
 }
 
 // y = sum of partials (fixed order); if b given: y = b - sum.
@@ -267,13 +312,13 @@ __global__ void k_add_combo(const Z *Zb, long ldz, int k, const double2 *y, V *x
 // Krylov workspace and helpers
 // ---------------------------------------------------------------------------
 struct Work {
-  om_context *ctx;
-  long n;
+  om_context *ctx = nullptr;
+  long n = 0;
   void *buf = nullptr;
   size_t bytes = 0;
   ~Work() {
     if(buf)
-      cudaFree(buf);
+      dev_release(ctx, buf, bytes);
   }
   template <typename T> T *take(size_t count, size_t &off) {
     T *p = reinterpret_cast<T *>(reinterpret_cast<char *>(buf) + off);
@@ -283,15 +328,9 @@ struct Work {
 };
 
 int alloc_work(om_context *ctx, Work &w, size_t bytes) {
-  if(ctx->budget && ctx->used + bytes > ctx->budget) {
-    ctx->err = "device-memory budget exceeded by solver workspace";
-    return OM_ERR_BUDGET;
-  }
-  if(cudaMalloc(&w.buf, bytes) != cudaSuccess) {
-    cudaGetLastError();
-    ctx->err = "cudaMalloc failed for solver workspace";
-    return OM_ERR_BUDGET;
-  }
+  int rc = dev_malloc(ctx, &w.buf, bytes);
+  if(rc)
+    return rc;
   w.bytes = bytes;
   return OM_OK;
 }
@@ -299,15 +338,29 @@ int alloc_work(om_context *ctx, Work &w, size_t bytes) {
 template <typename M, typename V>
 void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, const V *b) {
   const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
-  dim3 grid((unsigned)((n + kMvThreads - 1) / kMvThreads), (unsigned)nsplit);
+  const int row_tiles = (int)((n + kMvThreads - 1) / kMvThreads);
+  const long tiles = (long)row_tiles * nsplit;
   constexpr bool df = sizeof(M) == sizeof(float2) && sizeof(V) == sizeof(double2);
+  const long cap = (long)ctx->sm_count * (df ? ctx->mv_ctas_df : ctx->mv_ctas);
+  const unsigned grid = (unsigned)std::max(1L, std::min(tiles, cap));
   auto &ev = sizeof(M) == sizeof(double2) ? ctx->ev_mv64 : (df ? ctx->ev_mvdf : ctx->ev_mv32);
+  if(ctx->carve_mv >= 0) {
+    if constexpr(df)
+      cudaFuncSetAttribute(k_matvec_part_df, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           ctx->carve_mv);
+    else
+      cudaFuncSetAttribute(k_matvec_part<M, V>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           ctx->carve_mv);
+  }
   timer_begin(ctx, ev);
+  cudaMemsetAsync(ctx->d_tile_counter, 0, sizeof(unsigned long long), ctx->stream);
   if constexpr(df)
     k_matvec_part_df<<<grid, kMvThreads, 0, ctx->stream>>>((const float2 *)S, n, n,
-                                                           (const double2 *)x, (double2 *)part);
+                                                           (const double2 *)x, (double2 *)part,
+                                                           row_tiles, tiles, ctx->d_tile_counter);
   else
-    k_matvec_part<M, V><<<grid, kMvThreads, 0, ctx->stream>>>(S, n, n, x, part);
+    k_matvec_part<M, V><<<grid, kMvThreads, 0, ctx->stream>>>(S, n, n, x, part, row_tiles, tiles,
+                                                              ctx->d_tile_counter);
   timer_end(ctx, ev);
   k_matvec_reduce<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(part, nsplit, n, b, y);
   ctx->last_launches += 2;

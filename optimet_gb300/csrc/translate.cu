@@ -304,6 +304,7 @@ __device__ void run_chains(const Smem &s, TabT *tab, const Layout &y, int hankel
     double e2s, e2c;
     sincos(-2.0 * d * phi, &e2s, &e2c);
     const zd e2 = mk(e2c, e2s);
+    const float2 e2f = make_float2((float)e2c, (float)e2s);
     zd D = seed_at(l);
     const int mu_end = active ? min(min(nmax, d + nmax), n_hi) : -1;
     int mu_end_w = mu_end;
@@ -330,29 +331,50 @@ __device__ void run_chains(const Smem &s, TabT *tab, const Layout &y, int hankel
         D = (l <= L) ? Dn : mk(0.0, 0.0);
       }
       // store alpha(n, mu, l, kap) and, from the positive chains of a real
-      // wave number, the negative-m image (n, -mu, l, -kap)
+      // wave number, the negative-m image (n, -mu, l, -kap). With a complex64
+      // table (precision form) the image is formed in FP32 from the rounded
+      // entry: the recurrence stays FP64, only the stored values are FP32.
       auto store = [&](int n, zd v) {
         if(!live || n < n_lo || n > n_hi || l > nmax || kap > l || kap < -l)
           return;
-        if(!neg)
-          Tab<TabT>::put(tab, (flat(n, mu) - base) * W + l * (l + 1) - kap, v);
-        if(mu == 0 || (!neg && !real_k))
-          return;
         const int m = -mu, k = -kap;
-        zd w;
-        if(neg) {
-          w = conj(v);
-        } else if(hankel) {
-          w = e2 * v;  // conj(alpha_neg) = (-1)^{n+l} e^{-2 i d phi} alpha_pos
-          if((n + l) & 1)
-            w = -w;
-        } else {
-          w = conj(v);
-        }
         const int sign = hankel ? (n + m + l + k) : (k + m);
-        if(sign & 1)
-          w = -w;
-        Tab<TabT>::put(tab, (flat(n, m) - base) * W + l * (l + 1) - k, w);
+        if constexpr(std::is_same<TabT, float2>::value) {
+          const float2 vf = make_float2((float)v.re, (float)v.im);
+          if(!neg)
+            tab[(flat(n, mu) - base) * W + l * (l + 1) - kap] = vf;
+          if(mu == 0 || (!neg && !real_k))
+            return;
+          float2 wf;
+          if(!neg && hankel) {
+            wf = make_float2(fmaf(e2f.x, vf.x, -e2f.y * vf.y), fmaf(e2f.x, vf.y, e2f.y * vf.x));
+            if((n + l) & 1)
+              wf = make_float2(-wf.x, -wf.y);
+          } else {
+            wf = make_float2(vf.x, -vf.y);
+          }
+          if(sign & 1)
+            wf = make_float2(-wf.x, -wf.y);
+          tab[(flat(n, m) - base) * W + l * (l + 1) - k] = wf;
+        } else {
+          if(!neg)
+            Tab<TabT>::put(tab, (flat(n, mu) - base) * W + l * (l + 1) - kap, v);
+          if(mu == 0 || (!neg && !real_k))
+            return;
+          zd w;
+          if(neg) {
+            w = conj(v);
+          } else if(hankel) {
+            w = e2 * v;  // conj(alpha_neg) = (-1)^{n+l} e^{-2 i d phi} alpha_pos
+            if((n + l) & 1)
+              w = -w;
+          } else {
+            w = conj(v);
+          }
+          if(sign & 1)
+            w = -w;
+          Tab<TabT>::put(tab, (flat(n, m) - base) * W + l * (l + 1) - k, w);
+        }
       };
       store(mu, D);
       zd O2 = mk(0.0, 0.0), O1 = D;
@@ -846,8 +868,10 @@ template <typename Args> void fill_chunks(Args &a, const Layout &y) {
     a.chunks[c] = make_int2(ch[c].first, ch[c].second);
 }
 
-template <typename K> void set_smem(K kernel, size_t bytes) {
+template <typename K> void set_smem(K kernel, size_t bytes, int carveout = -1) {
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if(carveout >= 0)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
 }
 
 }  // namespace
@@ -956,13 +980,19 @@ void launch_assemble(om_problem *pr, int harmonic, int precision) {
   fill_chunks(a, y);
   dim3 grid((unsigned)((long)pr->N * (pr->N - 1) / 2 + pr->N));
   timer_begin(ctx, ctx->ev_asm);
+  // the assembly runs on the context's low-priority stream, ordered after and
+  // before the work of `stream`
+  cudaEventRecord(ctx->ev_fork, ctx->stream);
+  cudaStreamWaitEvent(ctx->stream_lo, ctx->ev_fork, 0);
   if(mixed) {
-    set_smem(k_assemble<true>, y.bytes);
-    k_assemble<true><<<grid, 256, y.bytes, ctx->stream>>>(a, y, (float2 *)pr->d_S32[harmonic]);
+    set_smem(k_assemble<true>, y.bytes, ctx->carve_asm);
+    k_assemble<true><<<grid, 256, y.bytes, ctx->stream_lo>>>(a, y, (float2 *)pr->d_S32[harmonic]);
   } else {
-    set_smem(k_assemble<false>, y.bytes);
-    k_assemble<false><<<grid, 256, y.bytes, ctx->stream>>>(a, y, (double2 *)pr->d_S[harmonic]);
+    set_smem(k_assemble<false>, y.bytes, ctx->carve_asm);
+    k_assemble<false><<<grid, 256, y.bytes, ctx->stream_lo>>>(a, y, (double2 *)pr->d_S[harmonic]);
   }
+  cudaEventRecord(ctx->ev_join, ctx->stream_lo);
+  cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);
   timer_end(ctx, ctx->ev_asm);
   ctx->last_launches++;
 }

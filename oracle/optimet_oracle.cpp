@@ -466,10 +466,11 @@ void vigdvig(int nMaxI, int mI, Sph R, std::vector<double> &W, std::vector<doubl
 }
 
 struct Aux {
-  std::vector<Vec3c> M, N, B, C;
+  std::vector<Vec3c> M, N, B, C, Xm, Xp;  // Xm, Xp: the SH particular-solution functions
 };
 
-// AuxCoefficients ctor (AuxCoefficients.cpp:292-343): M, N, B, C projected to
+// AuxCoefficients ctor (AuxCoefficients.cpp:292-343): M, N, B, C, Xm, Xp
+// (compute_Xm1 / compute_Xp1, AuxCoefficients.cpp:134-176) projected to
 // Cartesian components for every p < P.
 void aux_coefficients(Sph R, cplx waveK, bool regular, int nMax, Aux &out, bool want_mn = true) {
   int P = pmax(nMax);
@@ -477,6 +478,8 @@ void aux_coefficients(Sph R, cplx waveK, bool regular, int nMax, Aux &out, bool 
   out.N.assign(P, Vec3c{});
   out.B.assign(P, Vec3c{});
   out.C.assign(P, Vec3c{});
+  out.Xm.assign(P, Vec3c{});
+  out.Xp.assign(P, Vec3c{});
   std::vector<double> dn(nMax + 1);
   dn[0] = -1000;
   for(int i = 1; i <= nMax; ++i)
@@ -518,6 +521,9 @@ void aux_coefficients(Sph R, cplx waveK, bool regular, int nMax, Aux &out, bool 
                (1.0 / Kr) * dm * dn[n] * ((nn1 * data[n] * Pn.z) + (rad * Bn.z)) * eimphi};
       out.M[p] = to_projection(R, Mn);
       out.N[p] = to_projection(R, Nn);
+      const cplx cx = dm * dn[n] * std::sqrt(nn1) * eimphi, cb = dm * dn[n] * eimphi;
+      out.Xm[p] = to_projection(R, Vec3c{cx * Pn.x, cx * Pn.y, cx * Pn.z});
+      out.Xp[p] = to_projection(R, Vec3c{cb * Bn.x, cb * Bn.y, cb * Bn.z});
     }
   }
 }
@@ -1282,16 +1288,60 @@ void sh_source(const Problem &pr, const std::vector<double> &tab, const cplx *X_
   }
 }
 
+// The bulk (gamma) sums CXm1 / CXp1 (Symbol.cpp:478-620) for SH harmonic kk of
+// sphere j at radius r, from the FF internal coefficients Xi; d, dd, ddd are
+// j_n(k1 r) and its first two derivatives. ACSshcoeff (Symbol.cpp:358-477)
+// evaluates the same sums at its quadrature radii.
+void cx_sums(const Problem &pr, int j, int kk, const std::vector<double> &tab, const cplx *Xi,
+             double r, const std::vector<cplx> &d, const std::vector<cplx> &dd,
+             const std::vector<cplx> &ddd, cplx &Xm1, cplx &Xp1) {
+  const Sphere &s = pr.objects[j];
+  const int P = pmax(pr.nmax);
+  const size_t sz = size_t(P) * P * P;
+  const int n = (int)std::sqrt(kk + 1.0);
+  const cplx eps_0 = kEps0, gamma = s.elmag.gamma, eps_j2 = s.elmag.epsilon_SH;
+  const cplx k1 = pr.omega() * std::sqrt(s.elmag.epsilon * s.elmag.mu);
+  Xm1 = Xp1 = cplx(0, 0);
+  for(int p = 0; p < P; ++p) {
+    int n1 = (int)std::sqrt(p + 1.0);
+    cplx c1 = Xi[size_t(j) * 2 * P + p], d1 = Xi[P + size_t(j) * 2 * P + p];
+    for(int q = 0; q < P; ++q) {
+      int n2 = (int)std::sqrt(q + 1.0);
+      cplx c2 = Xi[size_t(j) * 2 * P + q], d2 = Xi[P + size_t(j) * 2 * P + q];
+      const size_t at = (size_t(kk) * P + p) * P + q;
+      double Wm = tab[T_Wm1m1 * sz + at], W1 = tab[T_W11 * sz + at], W0 = tab[T_W00 * sz + at];
+      if(Wm == 0.0 && W1 == 0.0 && W0 == 0.0)
+        continue;
+      cplx F00 = d[n1] * dd[n2];
+      cplx F11 = (k1 * dd[n2] + d[n2] / r) * (k1 * dd[n1] + d[n1] / r);
+      cplx Fm = (1.0 / std::pow(r, 2.0)) * (d[n1] * d[n2]);
+      cplx Fd00 = d[n1] * dd[n2] * k1 + k1 * dd[n1] * d[n2];
+      cplx Fd11 = (std::pow(k1, 2.0) * ddd[n1] - (1.0 / std::pow(r, 2.0)) * d[n1] + (1.0 / r) * k1 * dd[n1]) *
+                      (k1 * dd[n2] + d[n2] / r) +
+                  (std::pow(k1, 2.0) * ddd[n2] - (1.0 / std::pow(r, 2.0)) * d[n2] + (1.0 / r) * k1 * dd[n2]) *
+                      (k1 * dd[n1] + d[n1] / r);
+      cplx Fdm = (1.0 / std::pow(r, 2.0)) * (k1 * dd[n1] * d[n2] + d[n1] * k1 * dd[n2]) -
+                 (2.0 / std::pow(r, 3.0)) * (d[n1] * d[n2]);
+      const double sq = std::sqrt(n1 * n2 * (n1 + 1) * (n2 + 1));
+      const double sn = std::sqrt(n * (n + 1));
+      Xm1 += (-eps_0 / eps_j2) * gamma *
+             (c1 * c2 * W0 * Fd00 + d1 * d2 * (1.0 / std::pow(k1, 2.0)) * (W1 * Fd11 + Wm * sq * Fdm));
+      Xp1 += (-eps_0 / eps_j2) * gamma *
+             (c1 * c2 * W0 * sn * (1.0 / r) * F00 +
+              d1 * d2 * (1.0 / std::pow(k1, 2.0)) *
+                  (W1 * sn * (1.0 / r) * F11 + Wm * sq * sn * (1.0 / r) * Fm));
+    }
+  }
+}
+
 // ACSshcoeff (Symbol.cpp:358-477) for harmonic kk of sphere j.
 cplx acs_sh(const Problem &pr, int j, int kk, const std::vector<double> &tab, const cplx *Xi,
             cplx cmnSH, cplx dmnSH) {
   const Sphere &s = pr.objects[j];
-  const int nmax = pr.nmax, P = pmax(nmax);
-  const size_t sz = size_t(P) * P * P;
+  const int nmax = pr.nmax;
   const int n = (int)std::sqrt(kk + 1.0);
   const double R = s.radius, w = pr.omega();
-  const cplx eps_0 = kEps0, mu_0 = kMu0, gamma = s.elmag.gamma, eps_j2 = s.elmag.epsilon_SH,
-             mu_j2 = s.elmag.mu_SH;
+  const cplx eps_0 = kEps0, mu_0 = kMu0, eps_j2 = s.elmag.epsilon_SH, mu_j2 = s.elmag.mu_SH;
   const cplx waveK_01 = w * std::sqrt(eps_0 * mu_0);
   const cplx k1 = w * std::sqrt(s.elmag.epsilon * s.elmag.mu);
   const cplx kSH = 2.0 * w * std::sqrt(eps_j2 * mu_j2);
@@ -1305,37 +1355,8 @@ cplx acs_sh(const Problem &pr, int j, int kk, const std::vector<double> &tab, co
     std::vector<cplx> d, dd;
     bessel(kBessel, r * k1, nmax, d, dd);
     std::vector<cplx> ddd = bessel_dd(r * k1, nmax);
-    cplx Xm1(0, 0), Xp1(0, 0);
-    for(int p = 0; p < P; ++p) {
-      int n1 = (int)std::sqrt(p + 1.0);
-      cplx c1 = Xi[size_t(j) * 2 * P + p], d1 = Xi[P + size_t(j) * 2 * P + p];
-      for(int q = 0; q < P; ++q) {
-        int n2 = (int)std::sqrt(q + 1.0);
-        cplx c2 = Xi[size_t(j) * 2 * P + q], d2 = Xi[P + size_t(j) * 2 * P + q];
-        const size_t at = (size_t(kk) * P + p) * P + q;
-        double Wm = tab[T_Wm1m1 * sz + at], W1 = tab[T_W11 * sz + at], W0 = tab[T_W00 * sz + at];
-        if(Wm == 0.0 && W1 == 0.0 && W0 == 0.0)
-          continue;
-        cplx F00 = d[n1] * dd[n2];
-        cplx F11 = (k1 * dd[n2] + d[n2] / r) * (k1 * dd[n1] + d[n1] / r);
-        cplx Fm = (1.0 / std::pow(r, 2.0)) * (d[n1] * d[n2]);
-        cplx Fd00 = d[n1] * dd[n2] * k1 + k1 * dd[n1] * d[n2];
-        cplx Fd11 = (std::pow(k1, 2.0) * ddd[n1] - (1.0 / std::pow(r, 2.0)) * d[n1] + (1.0 / r) * k1 * dd[n1]) *
-                        (k1 * dd[n2] + d[n2] / r) +
-                    (std::pow(k1, 2.0) * ddd[n2] - (1.0 / std::pow(r, 2.0)) * d[n2] + (1.0 / r) * k1 * dd[n2]) *
-                        (k1 * dd[n1] + d[n1] / r);
-        cplx Fdm = (1.0 / std::pow(r, 2.0)) * (k1 * dd[n1] * d[n2] + d[n1] * k1 * dd[n2]) -
-                   (2.0 / std::pow(r, 3.0)) * (d[n1] * d[n2]);
-        const double sq = std::sqrt(n1 * n2 * (n1 + 1) * (n2 + 1));
-        const double sn = std::sqrt(n * (n + 1));
-        Xm1 += (-eps_0 / eps_j2) * gamma *
-               (c1 * c2 * W0 * Fd00 + d1 * d2 * (1.0 / std::pow(k1, 2.0)) * (W1 * Fd11 + Wm * sq * Fdm));
-        Xp1 += (-eps_0 / eps_j2) * gamma *
-               (c1 * c2 * W0 * sn * (1.0 / r) * F00 +
-                d1 * d2 * (1.0 / std::pow(k1, 2.0)) *
-                    (W1 * sn * (1.0 / r) * F11 + Wm * sq * sn * (1.0 / r) * Fm));
-      }
-    }
+    cplx Xm1, Xp1;
+    cx_sums(pr, j, kk, tab, Xi, r, d, dd, ddd, Xm1, Xp1);
     std::vector<cplx> ds, dds;
     bessel(kBessel, r * kSH, nmax, ds, dds);
     const double sn = std::sqrt(n * (n + 1));
@@ -1347,6 +1368,64 @@ cplx acs_sh(const Problem &pr, int j, int kk, const std::vector<double> &tab, co
                                (Xp1 + Xp1SH) * std::conj(Xp1 + Xp1SH));
   }
   return integral * (R / 2.0);
+}
+
+// Result::getEHFields, second-harmonic half (Result.cpp:166-199 outside,
+// 237-276 inside; projection off), with the particular solution of
+// Result::setFields / Geometry::COEFFpartSH (Result.cpp:906-919,
+// Geometry.cpp:458-491): X_sca_SH / X_int_SH scaled by the vacuum wave number,
+// radiating waves at 2k outside, regular waves at 2 k0 sqrt(eps_r_SH mu_r_SH)
+// inside plus sum_p (Xm_p CXm1_p + Xp_p CXp1_p) from the FF internal
+// coefficients Xi.
+void eh_fields_sh(const Problem &pr, const std::vector<double> &tab, const cplx *Xi,
+                  const cplx *Xs, const cplx *Xis, Sph R, Vec3c &E, Vec3c &H) {
+  const int P = pmax(pr.nmax);
+  const double w = pr.omega();
+  const cplx waveK_0 = w * std::sqrt(kEps0 * kMu0);
+  const cplx iZ = cplx(0.0, -1.0) / std::sqrt(pr.bground.mu / pr.bground.epsilon);
+  Vec3c Ef{0., 0., 0.}, Hf{0., 0., 0.}, Eg{0., 0., 0.};
+  auto accs = [](Vec3c &a, const Vec3c &m, cplx cm, const Vec3c &nn, cplx cn, cplx s) {
+    a.x = a.x + (m.x * cm + nn.x * cn) * s;
+    a.y = a.y + (m.y * cm + nn.y * cn) * s;
+    a.z = a.z + (m.z * cm + nn.z * cn) * s;
+  };
+  const int in = check_inner(pr, R);
+  if(in < 0) {
+    for(size_t j = 0; j < pr.objects.size(); ++j) {
+      Sph Rrel = sph_minus(R, pr.objects[j].vR);
+      Aux a;
+      aux_coefficients(Rrel, cplx(2.0, 0.0) * pr.waveK, false, pr.nmax, a);
+      const cplx *c = Xs + j * 2 * P;
+      for(int p = 0; p < P; ++p) {
+        accs(Ef, a.M[p], c[p], a.N[p], c[P + p], waveK_0);
+        accs(Hf, a.N[p], c[p], a.M[p], c[P + p], iZ * waveK_0);
+      }
+    }
+  } else {
+    const Sphere &s = pr.objects[in];
+    Sph Rrel = sph_minus(R, s.vR);
+    std::vector<cplx> cxm(P), cxp(P);
+    const cplx k1 = w * std::sqrt(s.elmag.epsilon * s.elmag.mu);
+    std::vector<cplx> d, dd;
+    bessel(kBessel, Rrel.rrr * k1, pr.nmax, d, dd);
+    std::vector<cplx> ddd = bessel_dd(Rrel.rrr * k1, pr.nmax);
+    for(int kk = 0; kk < P; ++kk)
+      cx_sums(pr, in, kk, tab, Xi, Rrel.rrr, d, dd, ddd, cxm[kk], cxp[kk]);
+    Aux a;
+    aux_coefficients(Rrel, cplx(2.0, 0.0) * waveK_0 * std::sqrt(s.elmag.epsilon_r_SH * s.elmag.mu_r),
+                     true, pr.nmax, a);
+    const cplx iZo = cplx(0.0, -1.0) / std::sqrt(s.elmag.mu_SH / s.elmag.epsilon_SH);
+    const cplx *c = Xis + size_t(in) * 2 * P;
+    for(int p = 0; p < P; ++p) {
+      accs(Ef, a.M[p], c[p], a.N[p], c[P + p], waveK_0);
+      Eg.x = Eg.x + (a.Xm[p].x * cxm[p] + a.Xp[p].x * cxp[p]);
+      Eg.y = Eg.y + (a.Xm[p].y * cxm[p] + a.Xp[p].y * cxp[p]);
+      Eg.z = Eg.z + (a.Xm[p].z * cxm[p] + a.Xp[p].z * cxp[p]);
+      accs(Hf, a.N[p], c[p], a.M[p], c[P + p], iZo * waveK_0);
+    }
+  }
+  E = {Ef.x + Eg.x, Ef.y + Eg.y, Ef.z + Eg.z};
+  H = Hf;
 }
 
 inline cplx *C(double *p) { return reinterpret_cast<cplx *>(p); }
@@ -1734,6 +1813,34 @@ void orc_cross_sections(void *h, const double *sca_d, double *out) {
   out[1] = (1. / kr2) * s;
   out[2] = out[0] - out[1];
   out[3] = (1 / kr2) * a;
+}
+
+// Second-harmonic fields at Cartesian points (metres): E_SH, H_SH, 3 complex
+// per point; tables = the nine SH coupling tables, Xi = FF internal
+// coefficients, Xs / Xis = SH scattered / internal coefficients.
+int orc_near_field_sh(void *h, const double *tables, const double *Xi, const double *Xs,
+                      const double *Xis, int npts, const double *xyz, double *E, double *H) {
+  Problem *pr = static_cast<Problem *>(h);
+  try {
+    const int P = pmax(pr->nmax);
+    std::vector<double> tab(tables, tables + 9 * size_t(P) * P * P);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads)
+    for(int i = 0; i < npts; ++i) {
+      Sph R = to_sph({xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]});
+      Vec3c e, hh;
+      eh_fields_sh(*pr, tab, C(Xi), C(Xs), C(Xis), R, e, hh);
+      C(E)[3 * i] = e.x;
+      C(E)[3 * i + 1] = e.y;
+      C(E)[3 * i + 2] = e.z;
+      C(H)[3 * i] = hh.x;
+      C(H)[3 * i + 1] = hh.y;
+      C(H)[3 * i + 2] = hh.z;
+    }
+    return 0;
+  } catch(std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
 }
 
 // Result::getEHFields at Cartesian points (metres). E and H: 3 complex per point.

@@ -56,6 +56,7 @@ def lib():
         L.orc_internal.argtypes = [C.c_void_p, _dp, _dp]
         L.orc_cross_sections.argtypes = [C.c_void_p, _dp, _dp]
         L.orc_near_field.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _dp]
+        L.orc_near_field_sh.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp]
         L.orc_wavelength_solve.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int,
                                            _dp, _dp, _dp, C.POINTER(C.c_int)]
         L.orc_lu_solve.argtypes = [C.c_int, _dp, _dp, _dp]
@@ -259,6 +260,16 @@ class Problem:
         E = np.zeros((xyz.shape[0], 3), np.complex128)
         H = np.zeros_like(E)
         if lib().orc_near_field(self.h, _p(sca), _p(intc), xyz.shape[0], _p(xyz), _p(E), _p(H)):
+            raise RuntimeError(lib().orc_last_error().decode())
+        return E, H
+
+    def near_field_sh(self, tables, x_int, x_sca_sh, x_int_sh, xyz):
+        """Second-harmonic E, H (3 complex per point) at Cartesian points."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        E = np.zeros((xyz.shape[0], 3), np.complex128)
+        H = np.zeros_like(E)
+        if lib().orc_near_field_sh(self.h, _p(tables), _p(_c(x_int)), _p(_c(x_sca_sh)),
+                                   _p(_c(x_int_sh)), xyz.shape[0], _p(xyz), _p(E), _p(H)):
             raise RuntimeError(lib().orc_last_error().decode())
         return E, H
 

@@ -98,7 +98,8 @@ def make(name, cl):
     if np.any(cl.chi != 0):
         tab = O.clg_tables(cl.nmax)
         K, K1, Xs, Xis = pr.sh_solve(tab, Xi)
-        sh = dict(chi=cl.chi[0], K=K, K1ana=K1, X_sca_SH=Xs, X_int_SH=Xis,
+        E_sh, H_sh = pr.near_field_sh(tab, Xi, Xs, Xis, pts)
+        sh = dict(chi=cl.chi[0], K=K, K1ana=K1, X_sca_SH=Xs, X_int_SH=Xis, E_sh=E_sh, H_sh=H_sh,
                   xsec_sh=pr.sh_cross_sections(tab, Xi, Xs, Xis),
                   sh_factors=np.stack([pr.sh_factors(j) for j in range(N)]))
         if cl.nmax <= 3:

@@ -222,6 +222,10 @@ def test_sh_pipeline(G, ctx, oracle, name, method):
     xso = pr_o.sh_cross_sections(tab, xio, Xso, Xiso)
     assert np.max(np.abs(xs - xso) / np.abs(xso)) < 1e-10
     assert np.max(np.abs(xs - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10
+    E, H = pr.near_field_sh(g["points"])
+    Eo, Ho = pr_o.near_field_sh(tab, xio, Xso, Xiso, g["points"])
+    assert rel(E, Eo) < 1e-10 and rel(H, Ho) < 1e-10
+    assert rel(E, g["E_sh"]) < 5e-10 and rel(H, g["H_sh"]) < 5e-10
 
 
 def test_wavelength_solve_sh_entry_point(G, ctx, oracle):

@@ -262,6 +262,8 @@ def test_sh_golden(oracle, name):
         assert rel(a, b) < 5e-10
     xs = pr.sh_cross_sections(tab, Xi, Xs, Xis)
     assert np.max(np.abs(xs - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10
+    E, H = pr.near_field_sh(tab, Xi, Xs, Xis, g["points"])
+    assert rel(E, g["E_sh"]) < 5e-10 and rel(H, g["H_sh"]) < 5e-10
 
 
 def test_sh_single_sphere_rotation_invariance(oracle):
