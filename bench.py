@@ -454,6 +454,222 @@ def reference_arm(args, w):
                     "d2h_bytes_per_step": 0}}
 
 
+# ---------------------------------------------------------------------------
+# Batching (c3) and serving (c4) workloads: ragged requests through om_server.
+# ---------------------------------------------------------------------------
+def c1_volume_fraction():
+    """Volume fraction of the c1 cluster (N = 100, radii U[50, 80] nm, 2 um cube)."""
+    xyz, rad = cluster(WORKLOADS["c1"])
+    return float(np.sum(4.0 / 3.0 * np.pi * rad ** 3) / (2000 * nm) ** 3)
+
+
+def nmax_rule(radii, lam):
+    """nMax = clamp(ceil(x + 4 x^(1/3) + 2), 4, 12), x = 2 pi a / lambda; the
+    reference needs one nMax per cluster, so the largest over its spheres."""
+    x = 2.0 * np.pi * np.asarray(radii) / lam
+    return int(np.clip(np.ceil(x + 4.0 * np.cbrt(x) + 2.0), 4, 12).max())
+
+
+def ragged_cluster(rng, N, rmin, rmax, frac):
+    """N spheres, radii U[rmin, rmax], in the smallest cube edge that gives the
+    volume fraction `frac` (seeded rejection sampling, 20 nm gap)."""
+    rad = rng.uniform(rmin, rmax, N)
+    edge = float(np.cbrt(np.sum(4.0 / 3.0 * np.pi * rad ** 3) / frac))
+    edge = max(edge, 2.0 * rad.max() + 40 * nm)
+    while True:
+        xyz = np.zeros((N, 3))
+        ok = True
+        for k, r in enumerate(rad):
+            lim = (rad[:k] + r + 20 * nm) ** 2
+            for _ in range(1000):
+                cand = rng.uniform(-edge / 2 + r, edge / 2 - r, size=(4, 3))
+                if k == 0:
+                    xyz[0] = cand[0]
+                    break
+                diff = cand[:, None, :] - xyz[None, :k, :]
+                good = np.nonzero(((diff * diff).sum(axis=2) >= lim).all(axis=1))[0]
+                if good.size:
+                    xyz[k] = cand[good[0]]
+                    break
+            else:
+                ok = False
+                break
+        if ok:
+            return xyz, rad, edge
+        edge *= 1.1
+
+
+def c3_cases(n_clusters, n_lambda, seed=20260404):
+    """The spectral sweep: clusters of 2-64 spheres (radii U[30, 120] nm,
+    index U[1.5, 4.0] + i U[0.001, 0.1] per cluster) at wavelengths uniform in
+    [400, 900] nm; every case is the fundamental solve plus the SH solve
+    driven by the surface chi(2) (perp-perp-perp 1.0, par-perp-par 0.25)."""
+    import optimet_gb300 as G
+    rng = np.random.default_rng(seed)
+    frac = c1_volume_fraction()
+    lams = np.linspace(400 * nm, 900 * nm, 256)
+    pick = np.linspace(0, 255, n_lambda).round().astype(int)
+    cases = []
+    for c in range(n_clusters):
+        N = int(rng.integers(2, 65))
+        xyz, rad, edge = ragged_cluster(rng, N, 30 * nm, 120 * nm, frac)
+        index = complex(rng.uniform(1.5, 4.0), rng.uniform(0.001, 0.1))
+        arrays = {}
+        for li in pick:
+            lam = float(lams[li])
+            nmax = nmax_rule(rad, lam)
+            if nmax not in arrays:
+                arrays[nmax] = G.spheres_array(xyz, rad, index ** 2, nmax, ksippp=1.0,
+                                               ksiparppar=0.25)
+            cases.append(dict(sp=arrays[nmax], wave=G.plane_wave(lam, sh=True), key=c * 16 + nmax,
+                              N=N, nmax=nmax))
+    return cases
+
+
+def run_cases(G, cases, opts, precision, slots, bg, device=0, budget=0):
+    srv = G.Server(device, budget, slots)
+    # warm-up: one request per size class
+    seen = {}
+    for cs in cases:
+        seen.setdefault((cs["N"], cs["nmax"]), cs)
+    for t in [srv.submit(cs["sp"], bg, cs["wave"], opts, precision, 0) for cs in list(seen.values())[:8]]:
+        srv.poll(t)
+    srv.launches()
+    srv.mark()
+    tickets = [srv.submit(cs["sp"], bg, cs["wave"], opts, precision, cs["key"]) for cs in cases]
+    res = [srv.poll(t) for t in tickets]
+    dev_s = srv.mark() * 1e-3
+    launches = srv.launches()
+    srv.close()
+    return dev_s, res, launches
+
+
+def batch_arm(args):
+    """c3: a ragged spectral sweep through the server, precision form against
+    the FP64 form on the same cases."""
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    cases = c3_cases(args.c3_clusters, args.c3_wavelengths)
+    bg = G.medium(1.0)
+    mixed = G.options(G.SOLVE_FGMRES_MIXED, tol=1e-8, max_iter=30, restarts=4, inner_iter=60,
+                      inner_tol=1e-4)
+    fp64 = G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=300, restarts=6)
+    with ClockSampler(0) as clk:
+        t_mx, res_mx, launches = run_cases(G, cases, mixed, G.C64, args.batch_slots, bg)
+    t_64, res_64, _ = run_cases(G, cases, fp64, G.C128, args.batch_slots, bg)
+    ok = [i for i in range(len(cases)) if res_mx[i]["status"] == G.OK and res_64[i]["status"] == G.OK]
+    err = max(abs(res_mx[i]["xsec"][0] - res_64[i]["xsec"][0]) / abs(res_64[i]["xsec"][0]) for i in ok)
+    err_sh = max(float(np.max(np.abs(res_mx[i]["xsec_sh"] - res_64[i]["xsec_sh"]) /
+                              np.abs(res_64[i]["xsec_sh"]))) for i in ok)
+    svc = [r["service_ms"] for r in res_mx]
+    Ns = [cs["N"] for cs in cases]
+    nm_ = [cs["nmax"] for cs in cases]
+    return {"metric": METRIC, "value": len(cases) / t_mx, "unit": UNIT + " (FF + SH per case)",
+            "n_gpus": 1, "steps": len(cases), "warmup": 8, "ms_per_step": 1e3 * t_mx / len(cases),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64 (FP32) inner + c128 (FP64) outer/assembly", "data": "synthetic (seeded)",
+            "config": {"workload": f"c3: {args.c3_clusters} clusters x {args.c3_wavelengths} of the "
+                                   "256 wavelengths in [400, 900] nm, N U{2..64}, radii U[30,120] nm, "
+                                   "index U[1.5,4]+iU[0.001,0.1], nMax rule clamp(ceil(x+4x^(1/3)+2),4,12) "
+                                   "(max over each cluster), FF + SH (ksippp 1, ksiparppar 0.25)",
+                       "slots": args.batch_slots, "N_range": [min(Ns), max(Ns)],
+                       "nmax_range": [min(nm_), max(nm_)]},
+            "latency_ms": {"p50": float(np.percentile(svc, 50)), "p99": float(np.percentile(svc, 99))},
+            "fp64": {"value": len(cases) / t_64, "unit": UNIT},
+            "speedup_vs_fp64": t_64 / t_mx,
+            "qext_rel_err_vs_fp64": err, "sh_xsec_rel_err_vs_fp64": err_sh,
+            "failed": {"mixed": len(cases) - sum(r["status"] == G.OK for r in res_mx),
+                       "fp64": len(cases) - sum(r["status"] == G.OK for r in res_64)},
+            "statuses": {"mixed": {str(k): v for k, v in sorted(
+                             __import__("collections").Counter(r["status"] for r in res_mx).items())},
+                         "fp64": {str(k): v for k, v in sorted(
+                             __import__("collections").Counter(r["status"] for r in res_64).items())}},
+            "gpu_launches": launches, "clocks": clk.summary()}
+
+
+def c4_requests(rate, duration, seed=20260405):
+    """Poisson arrivals; N log-uniform in [1, 300]; radii, index and nMax as
+    c3; wavelength U[400, 900] nm; random linear polarisation and direction;
+    SH attached to 30% of the requests."""
+    import optimet_gb300 as G
+    rng = np.random.default_rng(seed)
+    frac = c1_volume_fraction()
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        N = int(np.clip(np.floor(np.exp(rng.uniform(0.0, np.log(301.0)))), 1, 300))
+        xyz, rad, _ = ragged_cluster(rng, N, 30 * nm, 120 * nm, frac)
+        index = complex(rng.uniform(1.5, 4.0), rng.uniform(0.001, 0.1))
+        lam = rng.uniform(400 * nm, 900 * nm)
+        nmax = nmax_rule(rad, lam)
+        sh = bool(rng.uniform() < 0.3)
+        psi = rng.uniform(0, np.pi)
+        th, ph = float(np.arccos(rng.uniform(-1, 1))), float(rng.uniform(0, 2 * np.pi))
+        sp = G.spheres_array(xyz, rad, index ** 2, nmax, ksippp=1.0 if sh else 0.0,
+                             ksiparppar=0.25 if sh else 0.0)
+        out.append(dict(t=t, sp=sp, wave=G.plane_wave(lam, th, ph, np.cos(psi), np.sin(psi), sh=sh),
+                        N=N, nmax=nmax))
+    return out
+
+
+def serve_arm(args):
+    """c4: Poisson request stream admitted against a 150 GB HBM budget."""
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    reqs = c4_requests(args.c4_rate, args.c4_seconds)
+    bg = G.medium(1.0)
+    forms = {"mixed": (G.options(G.SOLVE_FGMRES_MIXED, tol=1e-8, max_iter=30, restarts=4,
+                                 inner_iter=60, inner_tol=1e-4), G.C64),
+             "fp64": (G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=300, restarts=6), G.C128)}
+    out = {}
+    for name, (opts, prec) in forms.items():
+        srv = G.Server(0, 150 << 30, args.batch_slots)
+        for r in reqs[:4]:
+            srv.poll(srv.submit(r["sp"], bg, r["wave"], opts, prec, 0))
+        tickets = []
+        s0 = time.perf_counter()
+        with ClockSampler(0) as clk:
+            for r in reqs:
+                delay = s0 + r["t"] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append(srv.submit(r["sp"], bg, r["wave"], opts, prec, 0))
+            res = [srv.poll(t) for t in tickets]
+            wall = time.perf_counter() - s0
+        srv.close()
+        lat = np.array([r["latency_ms"] for r in res if r["status"] == G.OK])
+        out[name] = {"solves_per_s": len(lat) / wall, "offered_per_s": len(reqs) / args.c4_seconds,
+                     "latency_ms": {"p50": float(np.percentile(lat, 50)),
+                                    "p99": float(np.percentile(lat, 99)),
+                                    "p99.9": float(np.percentile(lat, 99.9))},
+                     "completed": int(len(lat)),
+                     "refused_budget": int(sum(r["status"] == G.ERR_BUDGET for r in res)),
+                     "other_failures": int(sum(r["status"] not in (G.OK, G.ERR_BUDGET) for r in res)),
+                     "service_ms_by_N": {f"{lo}-{hi}": float(np.median([r["service_ms"] for r, q in zip(res, reqs)
+                                                                        if lo <= q["N"] <= hi] or [0]))
+                                         for lo, hi in ((1, 10), (11, 30), (31, 100), (101, 300))},
+                     "wall_s": wall, "clocks": clk.summary(), "xsec": [r["xsec"][0] for r in res]}
+    both = [i for i in range(len(reqs)) if out["mixed"]["xsec"][i] and out["fp64"]["xsec"][i]]
+    err = max(abs(out["mixed"]["xsec"][i] - out["fp64"]["xsec"][i]) / abs(out["fp64"]["xsec"][i])
+              for i in both) if both else None
+    for v in out.values():
+        v.pop("xsec")
+    m = out["mixed"]
+    return {"metric": METRIC, "value": m["solves_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": len(reqs), "warmup": 4, "ms_per_step": 1e3 / m["solves_per_s"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64 (FP32) inner + c128 (FP64) outer/assembly", "data": "synthetic (seeded)",
+            "config": {"workload": f"c4: Poisson arrivals {args.c4_rate}/s for {args.c4_seconds} s, "
+                                   "N log-uniform [1,300], radii/index/nMax as c3, lambda U[400,900] nm, "
+                                   "random polarisation and direction, SH on 30%, HBM budget 150 GB",
+                       "slots": args.batch_slots},
+            "latency_ms": m["latency_ms"], "forms": out, "qext_rel_err_vs_fp64": err}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -461,12 +677,22 @@ def main():
     ap.add_argument("--slots", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "c4"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--c3-clusters", type=int, default=64)
+    ap.add_argument("--c3-wavelengths", type=int, default=16)
+    ap.add_argument("--c4-rate", type=float, default=200.0)
+    ap.add_argument("--c4-seconds", type=float, default=60.0)
+    ap.add_argument("--batch-slots", type=int, default=6, help="server slots for c3 / c4")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    w = WORKLOADS[args.workload]
-    out = reference_arm(args, w) if args.impl == "reference" else gpu_arm(args, w)
+    if args.workload == "c3":
+        out = batch_arm(args) if args.impl != "reference" else None
+    elif args.workload == "c4":
+        out = serve_arm(args) if args.impl != "reference" else None
+    else:
+        w = WORKLOADS[args.workload]
+        out = reference_arm(args, w) if args.impl == "reference" else gpu_arm(args, w)
     if out is not None:
         print(json.dumps(out))
 

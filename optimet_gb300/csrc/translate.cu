@@ -16,6 +16,7 @@
 //     matrix, scaled by -T_i and written as the 2P x 2P block of S
 //     (PreconditionedMatrix.cpp:369-397) with coalesced column stores.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <stdexcept>
 #include <type_traits>
@@ -849,16 +850,18 @@ __global__ void k_incident(int nmax, double theta, double phi, const double *ein
   }
 }
 
-size_t g_smem_limit = 0;
+std::atomic<size_t> g_smem_limit{0};
 
 size_t smem_limit() {
-  if(!g_smem_limit) {
-    int dev = 0, v = 0;
+  size_t v = g_smem_limit.load();
+  if(!v) {
+    int dev = 0, lim = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    g_smem_limit = std::min<size_t>((size_t)v, 200 * 1024);
+    cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    v = std::min<size_t>((size_t)lim, 200 * 1024);
+    g_smem_limit.store(v);
   }
-  return g_smem_limit;
+  return v;
 }
 
 template <typename Args> void fill_chunks(Args &a, const Layout &y) {
@@ -868,8 +871,13 @@ template <typename Args> void fill_chunks(Args &a, const Layout &y) {
     a.chunks[c] = make_int2(ch[c].first, ch[c].second);
 }
 
+// The dynamic shared-memory ceiling of a kernel is a process-wide attribute:
+// it is always raised to the largest layout (smem_limit), never set to one
+// launch's size, so that contexts launching the same kernel from several host
+// threads with different nMax cannot undercut each other's launches.
 template <typename K> void set_smem(K kernel, size_t bytes, int carveout = -1) {
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  (void)bytes;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit());
   if(carveout >= 0)
     cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
 }
