@@ -670,6 +670,88 @@ def serve_arm(args):
             "latency_ms": m["latency_ms"], "forms": out, "qext_rel_err_vs_fp64": err}
 
 
+def fp64_gemm_tflops():
+    """FP64 throughput measured with cuBLAS DGEMM (torch.matmul, 8192^3, best of 5)."""
+    import torch
+    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    b = torch.randn_like(a)
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    return 2.0 * 8192 ** 3 / best / 1e12
+
+
+def near_field_arm(args):
+    """c1 near field: |E|^2 on a 256 x 256 grid in the z = 0 plane (two z
+    layers at +-0.1 nm, as the reference's grid needs two steps: 131,072
+    points) around the c1 cluster after its FP64 GMRES solve."""
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    from optimet_gb300.optimet import grid_points
+    build.build()
+    w = WORKLOADS["c1"]
+    xyz, rad = cluster(w)
+    ctx = G.Context(0)
+    sp = G.spheres_array(xyz, rad, complex(w["index"]) ** 2, w["nmax"])
+    pr = G.Problem(ctx, sp, G.medium(complex(w["host"]) ** 2), G.plane_wave(w["lam"]))
+    pr.source_vector(copy=False)
+    pr.assemble(G.FF, G.C128)
+    st = pr.solve(G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=400, restarts=6))
+    params = [-1000 * nm, 1000 * nm, 256, -1000 * nm, 1000 * nm, 256, -0.1 * nm, 0.1 * nm, 2]
+    pts = grid_points(params)
+    for _ in range(args.warmup):
+        pr.near_field(pts[:8192])
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            ctx.mark()
+            E, H = pr.near_field(pts)
+            times.append(ctx.mark() * 1e-3)
+    t = float(np.median(times))
+    inside = 0
+    for c, r in zip(xyz, rad):
+        inside += int(np.sum(np.linalg.norm(pts - c, axis=1) <= r))
+    N, P = w["N"], w["nmax"] * (w["nmax"] + 2)
+    flops = 8.0 * 6 * N * P * (len(pts) - inside)  # 6 complex MAC per (point, sphere, harmonic)
+    peak = fp64_gemm_tflops()
+    res = {"metric": "near-field points/s (|E|^2, c1 grid)", "value": len(pts) / t, "unit": "points/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64)",
+           "data": "synthetic (seeded)",
+           "config": {"workload": "c1 near field: " + w["desc"] + "; grid 256 x 256 x 2 over "
+                                  "[-1, 1] um^2 at z = +-0.1 nm", "points": len(pts),
+                      "points_inside_spheres": inside, "gmres_iterations": st.iterations},
+           "max_abs_E2": float(np.max(np.sum(np.abs(E) ** 2, axis=1))),
+           "roofline": {"bound": "fp64", "achieved": flops / t / 1e12, "peak": peak, "unit": "TFLOP/s",
+                        "frac": flops / t / 1e12 / peak,
+                        "peak_source": "measured here: cuBLAS DGEMM 8192^3 (torch.matmul float64)",
+                        "algorithmic_flops": flops},
+           "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.lib()
+        O.set_threads(O.max_threads())
+        cl = O.Cluster(xyz=xyz, radius=rad, eps=complex(w["index"]) ** 2, nmax=w["nmax"],
+                       wavelength=w["lam"], bg_eps=complex(w["host"]) ** 2)
+        po = O.Problem(cl)
+        xs, xi = pr.coefficients()
+        sample = pts[:: max(1, len(pts) // 2048)]
+        s0 = time.perf_counter()
+        po.near_field(xs, xi, sample)
+        dt = time.perf_counter() - s0
+        res["cpu_baseline"] = {"value": len(sample) / dt, "unit": "points/s", "cores": O.max_threads(),
+                               "kind": "port", "sample": f"oracle eh_fields on {len(sample)} of the grid points"}
+        O.set_threads(1)
+    pr.close()
+    ctx.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -677,7 +759,7 @@ def main():
     ap.add_argument("--slots", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c1f", "c3", "c4"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--c3-clusters", type=int, default=64)
     ap.add_argument("--c3-wavelengths", type=int, default=16)
@@ -686,7 +768,9 @@ def main():
     ap.add_argument("--batch-slots", type=int, default=6, help="server slots for c3 / c4")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.workload == "c3":
+    if args.workload == "c1f":
+        out = near_field_arm(args) if args.impl != "reference" else None
+    elif args.workload == "c3":
         out = batch_arm(args) if args.impl != "reference" else None
     elif args.workload == "c4":
         out = serve_arm(args) if args.impl != "reference" else None

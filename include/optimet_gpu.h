@@ -94,6 +94,7 @@ typedef struct {
  * Replaces the process-level state of mpi::init / scalapack::Context
  * (srcAna/mpi/Session.cpp:38-64, srcAna/scalapack/Context.h:32-169). */
 int om_context_create(int device, size_t budget_bytes, om_context **out);
+/* Also destroys the problems of the context that are still alive. */
 void om_context_destroy(om_context *ctx);
 const char *om_context_last_error(const om_context *ctx);
 /* Number of kernels the last call on this context launched. */

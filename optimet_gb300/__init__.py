@@ -262,7 +262,9 @@ class Problem:
 
     def close(self):
         if getattr(self, "h", None):
-            lib().om_problem_destroy(self.h)
+            # a closed context has already destroyed its problems
+            if getattr(self.ctx, "h", None):
+                lib().om_problem_destroy(self.h)
             self.h = None
 
     def __del__(self):

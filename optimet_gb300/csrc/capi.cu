@@ -495,6 +495,9 @@ void om_context_destroy(om_context *ctx) {
     return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  // problems still alive belong to the context and go with it
+  while(!ctx->problems.empty())
+    om_problem_destroy(ctx->problems.back());
   for(auto &t : ctx->tables) {
     cudaFree(t.rec);
     cudaFree(t.qf);
@@ -537,7 +540,10 @@ int om_problem_create(om_context *ctx, const om_sphere *spheres, int n_spheres,
   cudaSetDevice(ctx->device);
   ctx->last_launches = 0;
   try {
-    return make_problem(ctx, spheres, n_spheres, background, wave, out);
+    int rc = make_problem(ctx, spheres, n_spheres, background, wave, out);
+    if(rc == OM_OK)
+      ctx->problems.push_back(*out);
+    return rc;
   } catch(std::exception &e) {
     ctx->err = e.what();
     return OM_ERR_CUDA;
@@ -547,9 +553,12 @@ int om_problem_create(om_context *ctx, const om_sphere *spheres, int n_spheres,
 void om_problem_destroy(om_problem *pr) {
   if(!pr)
     return;
-  cudaSetDevice(pr->ctx->device);
-  cudaStreamSynchronize(pr->ctx->stream);
+  om_context *ctx = pr->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
   free_problem(pr);
+  auto &v = ctx->problems;
+  v.erase(std::remove(v.begin(), v.end(), pr), v.end());
   delete pr;
 }
 

@@ -73,7 +73,16 @@ struct FieldArgs {
 
 // Result::getEHFields, fundamental frequency, Cartesian components
 // (Result.cpp:74-301) with Geometry::checkInner (Geometry.cpp:147-163).
-__global__ void __launch_bounds__(128) k_near_field(FieldArgs a) {
+// One thread per point; the CTA shares the Wigner tables and holds each
+// thread's radial factors (see vswf_point) in dynamic shared memory.
+template <int NM>
+__global__ void k_near_field(FieldArgs a) {
+  extern __shared__ double fsm[];
+  WigTab &T = *reinterpret_cast<WigTab *>(fsm);
+  zd *zs = reinterpret_cast<zd *>(fsm + sizeof(WigTab) / sizeof(double)) + threadIdx.x;
+  const int zst = blockDim.x;
+  wigtab_fill(T);
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= a.npts)
     return;
@@ -94,14 +103,14 @@ __global__ void __launch_bounds__(128) k_near_field(FieldArgs a) {
   if(inner < 0) {
     double r, t, p;
     to_spherical(px, py, pz, &r, &t, &p);
-    vswf_sum(r, t, p, a.waveK, 1, a.nmax, a.inc, a.inc + P, el, hl);
+    vswf_point<NM>(T, zs, zst, r, t, p, a.waveK, 1, a.nmax, a.inc, a.inc + P, el, hl);
     zd Ei[3] = {mk(0, 0), mk(0, 0), mk(0, 0)}, Hi[3] = {mk(0, 0), mk(0, 0), mk(0, 0)};
     project_add(t, p, el, one, Ei);
     project_add(t, p, hl, a.iZ, Hi);
     for(int j = 0; j < a.N; ++j) {
       to_spherical(px - a.cart[3 * j], py - a.cart[3 * j + 1], pz - a.cart[3 * j + 2], &r, &t, &p);
       const zd *c = a.X + (size_t)j * 2 * P;
-      vswf_sum(r, t, p, a.waveK, 0, a.nmax, c, c + P, el, hl);
+      vswf_point<NM>(T, zs, zst, r, t, p, a.waveK, 0, a.nmax, c, c + P, el, hl);
       project_add(t, p, el, one, E);
       project_add(t, p, hl, a.iZ, H);
     }
@@ -114,7 +123,7 @@ __global__ void __launch_bounds__(128) k_near_field(FieldArgs a) {
     to_spherical(px - a.cart[3 * inner], py - a.cart[3 * inner + 1], pz - a.cart[3 * inner + 2],
                  &r, &t, &p);
     const zd *c = a.Xint + (size_t)inner * 2 * P;
-    vswf_sum(r, t, p, a.k_in[inner], 1, a.nmax, c, c + P, el, hl);
+    vswf_point<NM>(T, zs, zst, r, t, p, a.k_in[inner], 1, a.nmax, c, c + P, el, hl);
     project_add(t, p, el, one, E);
     project_add(t, p, hl, a.iZ_in[inner], H);
   }
@@ -122,6 +131,13 @@ __global__ void __launch_bounds__(128) k_near_field(FieldArgs a) {
     a.E[3 * (size_t)i + q] = E[q];
     a.H[3 * (size_t)i + q] = H[q];
   }
+}
+
+template <int NM> void launch_nf(const FieldArgs &a, cudaStream_t st) {
+  const int threads = NM <= 8 ? 128 : 64;
+  const size_t smem = sizeof(WigTab) + 3 * (NM + 1) * threads * sizeof(zd);
+  cudaFuncSetAttribute(k_near_field<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_near_field<NM><<<blocks_for(a.npts, threads), threads, smem, st>>>(a);
 }
 
 }  // namespace
@@ -156,7 +172,14 @@ void launch_near_field(om_problem *pr, const double *d_xyz, int npts, zd *d_E, z
   a.iZ_in = pr->d_izin;
   a.E = d_E;
   a.H = d_H;
-  k_near_field<<<blocks_for(npts, 128), 128, 0, pr->ctx->stream>>>(a);
+  if(a.nmax <= 4)
+    launch_nf<4>(a, pr->ctx->stream);
+  else if(a.nmax <= 8)
+    launch_nf<8>(a, pr->ctx->stream);
+  else if(a.nmax <= 12)
+    launch_nf<12>(a, pr->ctx->stream);
+  else
+    launch_nf<15>(a, pr->ctx->stream);
   pr->ctx->last_launches++;
 }
 

@@ -82,6 +82,7 @@ struct om_context {
   double t_mv64 = 0, t_mv32 = 0, t_mvdf = 0, t_asm = 0;  // accumulated milliseconds
   cudaEvent_t mark = nullptr;                // last om_context_mark event
   long n_mv64 = 0, n_mv32 = 0, n_mvdf = 0, n_asm = 0;
+  std::vector<om_problem *> problems;  // live problems, destroyed with the context
 };
 
 struct om_problem {

@@ -411,7 +411,15 @@ struct ShFieldArgs {
 
 // Result::getEHFields, second-harmonic half (Result.cpp:166-199 outside,
 // 237-276 inside), without the particular solution (k_near_field_sh_gamma).
-__global__ void __launch_bounds__(128) k_near_field_sh(ShFieldArgs a) {
+// Same structure as the fundamental field kernel (vswf_point).
+template <int NM>
+__global__ void k_near_field_sh(ShFieldArgs a) {
+  extern __shared__ double fsm[];
+  WigTab &T = *reinterpret_cast<WigTab *>(fsm);
+  zd *zs = reinterpret_cast<zd *>(fsm + sizeof(WigTab) / sizeof(double)) + threadIdx.x;
+  const int zst = blockDim.x;
+  wigtab_fill(T);
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= a.npts)
     return;
@@ -433,7 +441,7 @@ __global__ void __launch_bounds__(128) k_near_field_sh(ShFieldArgs a) {
       double r, t, p;
       to_spherical(px - a.cart[3 * j], py - a.cart[3 * j + 1], pz - a.cart[3 * j + 2], &r, &t, &p);
       const zd *c = a.Xsh + (size_t)j * 2 * P;
-      vswf_sum(r, t, p, a.k2b, 0, a.nmax, c, c + P, el, hl);
+      vswf_point<NM>(T, zs, zst, r, t, p, a.k2b, 0, a.nmax, c, c + P, el, hl);
       project_add(t, p, el, a.w0, E);
       project_add(t, p, hl, a.iZw, H);
     }
@@ -442,7 +450,7 @@ __global__ void __launch_bounds__(128) k_near_field_sh(ShFieldArgs a) {
     to_spherical(px - a.cart[3 * inner], py - a.cart[3 * inner + 1], pz - a.cart[3 * inner + 2],
                  &r, &t, &p);
     const zd *c = a.Xish + (size_t)inner * 2 * P;
-    vswf_sum(r, t, p, a.k_in[inner], 1, a.nmax, c, c + P, el, hl);
+    vswf_point<NM>(T, zs, zst, r, t, p, a.k_in[inner], 1, a.nmax, c, c + P, el, hl);
     project_add(t, p, el, a.w0, E);
     project_add(t, p, hl, a.iZw_in[inner], H);
   }
@@ -451,6 +459,13 @@ __global__ void __launch_bounds__(128) k_near_field_sh(ShFieldArgs a) {
     a.E[3 * (size_t)i + q] = E[q];
     a.H[3 * (size_t)i + q] = H[q];
   }
+}
+
+template <int NM> void launch_nf_sh(const ShFieldArgs &a, cudaStream_t st) {
+  const int threads = NM <= 8 ? 128 : 64;
+  const size_t smem = sizeof(WigTab) + 3 * (NM + 1) * threads * sizeof(zd);
+  cudaFuncSetAttribute(k_near_field_sh<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_near_field_sh<NM><<<blocks_for(a.npts, threads), threads, smem, st>>>(a);
 }
 
 // The particular solution inside spheres with a bulk chi(2) (gamma != 0):
@@ -581,7 +596,14 @@ void launch_near_field_sh(om_problem *pr, const double *d_xyz, int npts, cplx w0
   a.inner = d_inner;
   a.E = d_E;
   a.H = d_H;
-  k_near_field_sh<<<blocks_for(npts, 128), 128, 0, ctx->stream>>>(a);
+  if(a.nmax <= 4)
+    launch_nf_sh<4>(a, ctx->stream);
+  else if(a.nmax <= 8)
+    launch_nf_sh<8>(a, ctx->stream);
+  else if(a.nmax <= 12)
+    launch_nf_sh<12>(a, ctx->stream);
+  else
+    launch_nf_sh<15>(a, ctx->stream);
   ctx->last_launches++;
   bool gamma = false;
   for(const auto &g : pr->gamma)

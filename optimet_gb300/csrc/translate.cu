@@ -62,10 +62,11 @@ struct Layout {
   int rec, qf, pf, leg, legc, eph, geo, zb, seed, tl, qf32, pf32, tl32, tab;
   int rows_cap;
   int tab_elem;  // bytes per table entry: 16 (complex128) or 8 (complex64, precision form)
+  int qf_global; // the factor tables qf / pf stay in global memory (large nMax)
   size_t bytes;
 };
 
-Layout make_layout(int nmax, size_t smem_limit, bool mixed = false) {
+Layout make_layout_with(int nmax, size_t smem_limit, bool mixed, bool qf_global) {
   Layout y;
   y.tab_elem = mixed ? 8 : 16;
   y.nmax = nmax;
@@ -73,6 +74,7 @@ Layout make_layout(int nmax, size_t smem_limit, bool mixed = false) {
   y.L = 2 * nmax;
   y.Lc = 2 * nmax + 1;
   y.W = (nmax + 1) * (nmax + 1);
+  y.qf_global = qf_global ? 1 : 0;
   int o = 0;
   auto take = [&](int n) {
     int at = o;
@@ -80,8 +82,8 @@ Layout make_layout(int nmax, size_t smem_limit, bool mixed = false) {
     return at;
   };
   y.rec = take(kRecStride * (y.Lc + 1) * (y.Lc + 1));
-  y.qf = take(kQfacStride * y.P);
-  y.pf = take(kPfacStride * y.P);
+  y.qf = take(qf_global ? 0 : kQfacStride * y.P);
+  y.pf = take(qf_global ? 0 : kPfacStride * y.P);
   y.leg = take((y.L + 1) * (y.L + 2) / 2);
   y.legc = take((y.L + 1) * (y.L + 2));
   y.eph = take(2 * (y.L + 1));
@@ -99,6 +101,16 @@ Layout make_layout(int nmax, size_t smem_limit, bool mixed = false) {
   int cap = (int)std::min<size_t>(avail / row_bytes, (size_t)y.P);
   y.rows_cap = cap;
   y.bytes = fixed + size_t(cap) * row_bytes;
+  return y;
+}
+
+// Shared-memory layout of the translation kernels. When the top harmonic level
+// does not fit next to the tables (nMax >= 14 in FP64), the coefficient
+// factor tables are read from global memory instead.
+Layout make_layout(int nmax, size_t smem_limit, bool mixed = false) {
+  Layout y = make_layout_with(nmax, smem_limit, mixed, false);
+  if(y.rows_cap < 2 * nmax + 1)
+    y = make_layout_with(nmax, smem_limit, mixed, true);
   return y;
 }
 
@@ -126,11 +138,11 @@ struct Smem {
   float2 *tl32;
 };
 
-__device__ Smem smem_view(double *base, const Layout &y) {
+__device__ Smem smem_view(double *base, const Layout &y, const double *gqf, const double *gpf) {
   Smem s;
   s.rec = base + y.rec;
-  s.qf = base + y.qf;
-  s.pf = base + y.pf;
+  s.qf = y.qf_global ? const_cast<double *>(gqf) : base + y.qf;
+  s.pf = y.qf_global ? const_cast<double *>(gpf) : base + y.pf;
   s.leg = base + y.leg;
   s.legc = base + y.legc;
   s.eph = reinterpret_cast<zd *>(base + y.eph);
@@ -166,6 +178,8 @@ __device__ void load_tables(const Smem &s, const Layout &y, const double *rec, c
     s.rec[i] = rec[i];
   for(int i = threadIdx.x; i < (y.L + 1) * (y.L + 2); i += blockDim.x)
     s.legc[i] = legc[i];
+  if(y.qf_global)
+    return;
   for(int i = threadIdx.x; i < kQfacStride * y.P; i += blockDim.x)
     s.qf[i] = qf[i];
   for(int i = threadIdx.x; i < kPfacStride * y.P; i += blockDim.x)
@@ -535,7 +549,7 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
     ++j;
   const int i = (int)(b - (long)j * (j - 1) / 2);
   const long xi = 2L * P * i, xj = 2L * P * j;
-  Smem s = smem_view(smem, y);
+  Smem s = smem_view(smem, y, a.qf, a.pf);
   TabT *tab = reinterpret_cast<TabT *>(s.tab);
   load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
   const int nT = 2 * (y.nmax + 1);
@@ -634,7 +648,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a, Layout y) {
   extern __shared__ double smem[];
   const int i = blockIdx.x;
   const int P = y.P, t = threadIdx.x;
-  Smem s = smem_view(smem, y);
+  Smem s = smem_view(smem, y, a.qf, a.pf);
   load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
   for(int u = t; u < 2 * (y.nmax + 1); u += blockDim.x)
     s.tl[u] = a.T[(size_t)i * 2 * (y.nmax + 1) + u];
@@ -705,7 +719,7 @@ struct CouplingArgs {
 __global__ void __launch_bounds__(256) k_coupling(CouplingArgs a, Layout y) {
   extern __shared__ double smem[];
   const int e = blockIdx.x, P = y.P;
-  Smem s = smem_view(smem, y);
+  Smem s = smem_view(smem, y, a.qf, a.pf);
   zd *A = a.A + (size_t)e * P * P, *B = a.B + (size_t)e * P * P;
   load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
   if(threadIdx.x == 0)
@@ -858,7 +872,7 @@ size_t smem_limit() {
     int dev = 0, lim = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    v = std::min<size_t>((size_t)lim, 200 * 1024);
+    v = (size_t)lim;
     g_smem_limit.store(v);
   }
   return v;

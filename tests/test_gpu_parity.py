@@ -34,7 +34,7 @@ def make(G, ctx, cl):
     return G.Problem(ctx, sp, bg, wave)
 
 
-@pytest.mark.parametrize("nmax", [1, 3, 6, 8, 12])
+@pytest.mark.parametrize("nmax", [1, 3, 6, 8, 12, 15])
 @pytest.mark.parametrize("regular", [True, False])
 def test_coupling_matches_oracle(G, ctx, oracle, nmax, regular):
     rng = np.random.default_rng(nmax)
@@ -236,3 +236,47 @@ def test_wavelength_solve_sh_entry_point(G, ctx, oracle):
     xsec, xsh, st = G.wavelength_solve_sh(ctx, sp, bg, wave, G.options(G.SOLVE_LU))
     assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 5e-10
     assert np.max(np.abs(xsh - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10
+
+
+@pytest.mark.parametrize("nmax", [10, 14, 15])
+def test_near_field_high_nmax_and_poles(G, ctx, oracle, nmax):
+    """The field kernels' large-nMax instantiations, with points on the z axis
+    of the spheres (the theta = 0 / pi branch of VIGdVIG and of the m/cos
+    theta term) and inside a sphere."""
+    cl = oracle.Cluster(xyz=[[0, 0, -150 * nm], [20 * nm, -10 * nm, 150 * nm]], radius=[60 * nm, 70 * nm],
+                        eps=[(2.5 + 0.1j) ** 2, (1.8 + 0.02j) ** 2], nmax=nmax, wavelength=500 * nm,
+                        theta=0.7, phi=0.4, e_theta=0.6, e_phi=0.8j)
+    pr = make(G, ctx, cl)
+    pr.source_vector(copy=False)
+    pr.assemble(G.FF, G.C128)
+    pr.solve(G.options(G.SOLVE_LU))
+    pr_o = oracle.Problem(cl)
+    xo = oracle.lu_solve(pr_o.scattering_matrix(), pr_o.source_vector())
+    # points on the z axis of sphere 0 or 1 (theta = 0 / pi after the nudge)
+    axis = np.array([[0, 0, -300 * nm], [0, 0, 10 * nm], [20 * nm, -10 * nm, 300 * nm],
+                     [20 * nm, -10 * nm, 40 * nm], [0, 0, -140 * nm]])
+    # (the global origin is left out: the incident expansion about it is 0/0
+    # there, in the reference as here)
+    rng = np.random.default_rng(8)
+    other = np.concatenate([[[10 * nm, 5 * nm, -160 * nm]], rng.uniform(-400 * nm, 400 * nm, size=(10, 3))])
+    # The field kernels are compared on the same coefficients (the GPU's):
+    # X_int = X_sca (.) Iaux multiplies rounding noise of the high-order X_sca by
+    # |Iaux| up to 1e20 at nMax 10-14, so interior fields of two independent
+    # solves differ far above 1e-10 (in the reference as here). Exterior fields
+    # are also compared end to end against the oracle's own solve.
+    xs_g, xi_g = pr.coefficients()
+    for pts, tol in ((other, 1e-10), (axis, 1e-8)):
+        E, H = pr.near_field(pts)
+        Eo, Ho = pr_o.near_field(xs_g, xi_g, pts)
+        # on the axis VIGdVIG divides by sin(1e-6): rounding differences of
+        # 1e-16 in its recurrence grow by ~1e6 there, in the reference too
+        assert rel(E, Eo) < tol and rel(H, Ho) < tol
+    # end to end against the oracle's own solve (nMax 10). At nMax 14-15 the
+    # field next to a 60 nm sphere is carried by high-order terms h_n(kr) X_n
+    # whose tiny X_n the two LU solves agree on only to ~1e-5 relative,
+    # although the coefficient vectors agree to 1e-11 in max norm.
+    if nmax <= 10:
+        outside = other[1:]
+        E, H = pr.near_field(outside)
+        Eo, Ho = pr_o.near_field(xo, pr_o.internal(xo), outside)
+        assert rel(E, Eo) < 1e-10 and rel(H, Ho) < 1e-10
