@@ -232,6 +232,17 @@ def gpu_arm(args, w):
 
 
     pr.close()
+    if args.single_stream:
+        ctx.close()
+        return {"metric": METRIC + " (single stream)", "value": args.steps / t_mixed,
+                "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "c64 (FP32) inner + c128 (FP64) outer/assembly",
+                "data": "synthetic (seeded random clusters)",
+                "config": {"workload": args.workload + ": " + w["desc"], "unknowns": n},
+                "fp64": {"value": k64 / t_fp64}, "kernels_ms": {k: v[0] / max(v[1], 1) for k, v in kt.items()},
+                "gpu_launches": total_launches, "clocks": clocks}
 
     # ---- batched / served form: om_server with `slots` contexts on the GPU ----
     # Successive wavelengths of the scan run on alternating slots, so one
@@ -761,6 +772,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c1f", "c3", "c4"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--single-stream", action="store_true",
+                    help="only the single-stream measurement of both forms (profiling runs)")
     ap.add_argument("--c3-clusters", type=int, default=64)
     ap.add_argument("--c3-wavelengths", type=int, default=16)
     ap.add_argument("--c4-rate", type=float, default=200.0)

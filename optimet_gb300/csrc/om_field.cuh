@@ -82,7 +82,7 @@ __device__ void vswf_point(const WigTab &T, zd *zs, int zst, double r, double th
       zd f1 = -(e * (zz + mk(0.0, 1.0))) * (rz * rz);
       for(int n = 1; n <= nmax; ++n) {
         const zd f2 = double(2 * n + 1) * (rz * f1) - f0;  // h_{n+1}
-        const zd dz = (double(n) / zz) * f1 - f2;
+        const zd dz = (double(n) * rz) * f1 - f2;
         const double dn = T.dn[n];
         Z1[n * zst] = dn * f1;
         Z2[n * zst] = (dn * (Kr * dz + f1)) * invKr;
@@ -107,11 +107,18 @@ __device__ void vswf_point(const WigTab &T, zd *zs, int zst, double r, double th
   }
   double sp, cp;
   sincos(ph, &sp, &cp);
+  const zd e1 = mk(cp, sp);
+  zd em;  // e^{i m phi}, advanced by e^{i phi} per m
+  {
+    double s0, c0;
+    sincos(-nmax * ph, &s0, &c0);
+    em = mk(c0, s0);
+  }
   for(int t = 0; t < 3; ++t) {
     eloc[t] = mk(0.0, 0.0);
     hloc[t] = mk(0.0, 0.0);
   }
-  for(int m = -nmax; m <= nmax; ++m) {
+  for(int m = -nmax; m <= nmax; ++m, em = em * e1) {
     const int am = m < 0 ? -m : m, g = m < 0;
     const double x = xs[g], isv = svi[g];
     double qm = 1.0;
@@ -167,16 +174,12 @@ __device__ void vswf_point(const WigTab &T, zd *zs, int zst, double r, double th
       }
     }
     // (-1)^m e^{i m phi}
-    double sm, cm;
-    sincos(m * ph, &sm, &cm);
-    const zd ep = ((am & 1) ? -1.0 : 1.0) * mk(cm, sm);
+    const zd ep = ((am & 1) ? -1.0 : 1.0) * em;
     for(int t = 0; t < 3; ++t) {
       eloc[t] = eloc[t] + ep * S[t];
       hloc[t] = hloc[t] + ep * S[3 + t];
     }
   }
-  (void)sp;
-  (void)cp;
 }
 
 __device__ __forceinline__ void project_add(double th, double ph, const zd v[3], zd s, zd out[3]) {
