@@ -141,6 +141,30 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(times, world, device="cpu"):
+    """Replica timing: every rank's times reduced with MAX (the slowest rank
+    sets the job's time; the work is the sum over ranks)."""
+    if world <= 1:
+        return list(times)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor(times, device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return [float(v) for v in tt.cpu()]
+
+
+def replica_value(units_per_rank, seconds, world, device="cpu"):
+    """Whole-job throughput of independent replicas: units summed over ranks
+    divided by the slowest rank's time."""
+    if world <= 1:
+        return units_per_rank / seconds
+    import torch
+    import torch.distributed as dist
+    u = torch.tensor([float(units_per_rank)], device=device, dtype=torch.float64)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(u.item()) / max_over_ranks([seconds], world, device)[0]
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -297,14 +321,8 @@ def gpu_arm(args, w):
     d2h = ctypes.sizeof(G.Result)
 
     # aggregate over ranks (max time, summed work)
-    t_all = [t_srv, t_srv64, wall_e2e, t_mixed, t_fp64]
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        tt = torch.tensor(t_all, device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_all = [float(v) for v in tt.cpu()]
-    t_srv_all, t_srv64_all, e2e_all, t_mixed_all, t64_all = t_all
+    t_srv_all, t_srv64_all, e2e_all, t_mixed_all, t64_all = max_over_ranks(
+        [t_srv, t_srv64, wall_e2e, t_mixed, t_fp64], world, f"cuda:{local}")
     value = world * args.steps / t_srv_all
     value64 = world * k64s / t_srv64_all
     value_ss = world * args.steps / t_mixed_all
