@@ -124,8 +124,15 @@ typedef struct {
   int matvec_df_ctas_per_sm;
   int assemble_carveout;
   int matvec_carveout;
+  int lu_tensor_cores;   /* complex64 LU trailing updates on the tensor cores: 1 (default) / 0 */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
+/* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, k <= 32,
+ * host buffers: the tensor-core trailing update of the complex64 LU (bf16
+ * hi/lo split products accumulated in FP32, about 17 significant bits). The
+ * role of the trailing pzgemm of pzgesv (ScalapackSolver.cpp:54-130). */
+int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, long lda,
+                     const float *B, long ldb, float *C, long ldc);
 /* Record an event on the context's stream, wait for it and return in *ms the
  * device time since the previous mark (0 for the first). Device-side step
  * timing for benchmarks; no counterpart in the reference. */

@@ -66,7 +66,8 @@ class SolveStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("matvec_ctas_per_sm", C.c_int), ("matvec_df_ctas_per_sm", C.c_int),
-                ("assemble_carveout", C.c_int), ("matvec_carveout", C.c_int)]
+                ("assemble_carveout", C.c_int), ("matvec_carveout", C.c_int),
+                ("lu_tensor_cores", C.c_int)]
 
 
 class Request(C.Structure):
@@ -84,6 +85,7 @@ class Result(C.Structure):
 
 _lib = None
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 
 
 def lib():
@@ -103,6 +105,8 @@ def lib():
         L.om_context_timers.argtypes = [vp, C.c_int, _dp]
         L.om_context_mark.argtypes = [vp, _dp]
         L.om_context_tune.argtypes = [vp, C.POINTER(Tuning)]
+        L.om_cgemm_sub_c64.argtypes = [vp, C.c_long, C.c_long, C.c_int, _fp, C.c_long, _fp,
+                                       C.c_long, _fp, C.c_long]
         L.om_problem_create.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
                                         C.POINTER(PlaneWave), pvp]
         L.om_problem_destroy.argtypes = [vp]
@@ -192,9 +196,10 @@ class Context:
         return float(out[0])
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
-             matvec_carveout=-1):
+             matvec_carveout=-1, lu_tensor_cores=-1):
         """Launch tuning (om_context_tune); 0 / -1 keep the current value."""
-        t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout)
+        t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
+                   lu_tensor_cores)
         self.check(lib().om_context_tune(self.h, C.byref(t)))
 
     def timers(self, enable=True):
@@ -384,6 +389,19 @@ def wavelength_solve(ctx: Context, spheres, bg, wave, opts=None, precision=C128,
     return xsec, xs, xi, st
 
 
+def cgemm_sub_c64(ctx: Context, A, B, C_):
+    """C - A B for complex64 A (m x k), B (k x n), C (m x n), k <= 32, on the
+    tensor cores (om_cgemm_sub_c64); returns the new C."""
+    A = np.asfortranarray(A, dtype=np.complex64)
+    B = np.asfortranarray(B, dtype=np.complex64)
+    out = np.array(C_, dtype=np.complex64, order="F")
+    m, k = A.shape
+    n = B.shape[1]
+    fp = lambda a: a.ctypes.data_as(_fp)
+    ctx.check(lib().om_cgemm_sub_c64(ctx.h, m, n, k, fp(A), m, fp(B), k, fp(out), m))
+    return out
+
+
 def clg_tables(ctx: Context, nmax: int) -> np.ndarray:
     """The nine SH coupling tables computed on the device, flattened (9 P^3)."""
     P = nmax * (nmax + 2)
@@ -452,8 +470,9 @@ class Server:
         lib().om_server_drain(self.h)
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
-             matvec_carveout=-1):
-        t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout)
+             matvec_carveout=-1, lu_tensor_cores=-1):
+        t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
+                   lu_tensor_cores)
         rc = lib().om_server_tune(self.h, C.byref(t))
         if rc:
             raise OptimetError(rc, "server tune")

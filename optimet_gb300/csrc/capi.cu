@@ -412,7 +412,50 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
     ctx->carve_asm = t->assemble_carveout;
   if(t->matvec_carveout >= 0)
     ctx->carve_mv = t->matvec_carveout;
+  if(t->lu_tensor_cores >= 0)
+    ctx->lu_tc = t->lu_tensor_cores ? 1 : 0;
   return OM_OK;
+}
+
+int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, long lda,
+                     const float *B, long ldb, float *C, long ldc) {
+  if(!ctx || !A || !B || !C || m < 1 || n < 1 || k < 1 || k > 32 || lda < m || ldb < k || ldc < m)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  float2 *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  int *derr = nullptr;
+  const size_t na = (size_t)lda * k, nbb = (size_t)ldb * n, nc = (size_t)ldc * n;
+  int rc = dev_alloc(ctx, &dA, na);
+  if(!rc) rc = dev_alloc(ctx, &dB, nbb);
+  if(!rc) rc = dev_alloc(ctx, &dC, nc);
+  if(!rc) rc = dev_alloc(ctx, &derr, 1);
+  if(!rc) {
+    cudaMemcpyAsync(dA, A, sizeof(float2) * na, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dB, B, sizeof(float2) * nbb, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dC, C, sizeof(float2) * nc, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(derr, 0, sizeof(int), ctx->stream);
+    om::launch_cgemm_sub_tc(ctx, dA, lda, dB, ldb, dC, ldc, m, n, k, derr);
+    rc = check_launch(ctx, "tensor-core update");
+    int herr = 0;
+    if(!rc) {
+      cudaMemcpyAsync(C, dC, sizeof(float2) * nc, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if(e != cudaSuccess)
+        rc = cuda_fail(ctx, e, "tensor-core update");
+      else if(herr) {
+        ctx->err = "tensor-core update timed out";
+        rc = OM_ERR_CUDA;
+      }
+    }
+  }
+  cudaStreamSynchronize(ctx->stream);
+  dev_free(ctx, dA, na);
+  dev_free(ctx, dB, nbb);
+  dev_free(ctx, dC, nc);
+  dev_free(ctx, derr, 1);
+  return rc;
 }
 
 int om_context_timers(om_context *ctx, int enable, double *out) {

@@ -70,6 +70,7 @@ struct om_context {
   int mv_ctas = 8, mv_ctas_df = 8;
   unsigned long long *d_tile_counter = nullptr;  // matvec tile counter (device)
   int carve_asm = -1, carve_mv = -1;  // preferred smem carveout (percent), -1 = driver's choice
+  int lu_tc = 1;  // complex64 LU trailing updates on the tensor cores
   size_t budget = 0;
   size_t used = 0;
   std::string err;
@@ -169,6 +170,12 @@ int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, co
                      double2 *x, om_solve_stats *st);
 int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
                        double2 *x, om_solve_stats *st);
+
+// tc_gemm.cu: C (m x n) -= A (m x k) B (k x n), k <= 32, complex64, column-major,
+// on the tensor cores (bf16 hi/lo split, FP32 accumulation); *d_err set on a
+// timed-out wait
+void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
+                         float2 *C, long ldc, long m, long n, int k, int *d_err);
 
 // capi.cu: stream-ordered device memory counted against the context budget
 int dev_malloc(om_context *ctx, void **p, size_t bytes);

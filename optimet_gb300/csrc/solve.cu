@@ -10,6 +10,7 @@
 //    preconditioner is a fixed-length FP32 GMRES on the complex64 copy of S.
 // Reductions write per-block partial sums and add them in a fixed order, so
 // every solve is bitwise reproducible for a given problem.
+#include <type_traits>
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -882,9 +883,11 @@ __global__ void k_tri_update(const V *A, long ld, long k, int nb, V *b, long lo,
   b[i] = v;
 }
 
+// info[0]: first zero pivot (1-based) or 0; info[1]: set when a tensor-core
+// trailing update timed out (complex64 only).
 template <typename V>
 int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
-  cudaMemsetAsync(info, 0, sizeof(int), ctx->stream);
+  cudaMemsetAsync(info, 0, 2 * sizeof(int), ctx->stream);
   for(long k = 0; k < n; k += kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
     k_lu_panel<V><<<1, 1024, 0, ctx->stream>>>(A, n, n, k, nb, piv, info);
@@ -893,9 +896,18 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
     const long rest = n - k - nb;
     if(rest > 0) {
       k_lu_trsm<V><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, n, k, nb);
+      ctx->last_launches++;
+      if constexpr(std::is_same<V, float2>::value) {
+        if(ctx->lu_tc && rest >= 128) {
+          const long kn = k + nb;
+          launch_cgemm_sub_tc(ctx, A + k * n + kn, n, A + kn * n + k, n, A + kn * n + kn, n, rest,
+                              rest, nb, info + 1);
+          continue;
+        }
+      }
       dim3 g((unsigned)((rest + 31) / 32), (unsigned)((rest + 31) / 32));
       k_lu_gemm<V><<<g, 256, 0, ctx->stream>>>(A, n, n, k, nb);
-      ctx->last_launches += 2;
+      ctx->last_launches++;
     }
   }
   return OM_OK;
@@ -1028,14 +1040,18 @@ struct LuPrecond32 : PrecondFn {
     A = w.take<float2>((size_t)n * n, off);
     v32 = w.take<float2>(n, off);
     piv = w.take<int>(n, off);
-    info = w.take<int>(1, off);
+    info = w.take<int>(2, off);
     cudaMemcpyAsync(A, S32, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, ctx->stream);
     lu_factor<float2>(ctx, A, n, piv, info);
-    int hinfo = 0;
-    cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    int hinfo[2] = {0, 0};
+    cudaMemcpyAsync(hinfo, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
-    if(hinfo) {
-      ctx->err = "singular complex64 matrix: zero pivot at column " + std::to_string(hinfo);
+    if(hinfo[1]) {
+      ctx->err = "tensor-core LU update timed out";
+      return OM_ERR_CUDA;
+    }
+    if(hinfo[0]) {
+      ctx->err = "singular complex64 matrix: zero pivot at column " + std::to_string(hinfo[0]);
       return OM_ERR_SINGULAR;
     }
     return OM_OK;

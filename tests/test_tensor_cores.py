@@ -1,0 +1,69 @@
+"""The tensor-core (tcgen05) complex64 trailing update of the precision form's
+LU: exact on operands that bf16 represents exactly (which pins the operand
+layout, the descriptors and the TMEM read-back), within the bf16 hi/lo split's
+accuracy on general data, and the LU-refined solve agrees with and without it."""
+import numpy as np
+import pytest
+
+from helpers import load_golden, oracle_cluster, random_cluster, nm
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G():
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    return G
+
+
+@pytest.fixture(scope="module")
+def ctx(G):
+    c = G.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 64, 32), (300, 200, 32), (257, 70, 17), (5, 3, 1)])
+def test_update_exact_on_bf16_values(G, ctx, m, n, k):
+    rng = np.random.default_rng(m + n + k)
+    A = (rng.integers(-8, 9, (m, k)) + 1j * rng.integers(-8, 9, (m, k))).astype(np.complex64)
+    B = (rng.integers(-8, 9, (k, n)) + 1j * rng.integers(-8, 9, (k, n))).astype(np.complex64)
+    C = (rng.integers(-100, 101, (m, n)) + 1j * rng.integers(-100, 101, (m, n))).astype(np.complex64)
+    out = G.cgemm_sub_c64(ctx, A, B, C)
+    ref = C.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
+    assert np.array_equal(out.astype(np.complex128), ref)
+
+
+def test_update_accuracy_general(G, ctx):
+    rng = np.random.default_rng(3)
+    m, n, k = 600, 400, 32
+    A = (rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))).astype(np.complex64)
+    B = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))).astype(np.complex64)
+    C = (rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))).astype(np.complex64)
+    out = G.cgemm_sub_c64(ctx, A, B, C)
+    ref = C.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
+    scale = np.abs(A.astype(np.complex128)) @ np.abs(B.astype(np.complex128))
+    err = np.max(np.abs(out - ref) / scale)
+    assert err < 4e-5, err   # three bf16 products: about 17 significant bits
+    assert err > 1e-9        # (and not an FP32 SIMT path in disguise)
+
+
+def test_lu_mixed_with_and_without_tensor_cores(G, ctx):
+    rng = np.random.default_rng(21)
+    xyz, rad = random_cluster(rng, 12, 900 * nm, 40 * nm, 70 * nm, 20 * nm)
+    sp = G.spheres_array(xyz, rad, (2.5 + 0.05j) ** 2, 6)   # n = 1,152
+    bg, wave = G.medium(1.0), G.plane_wave(600 * nm)
+    ref = G.wavelength_solve(ctx, sp, bg, wave, G.options(G.SOLVE_LU), G.C128)[0]
+    opts = G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4)
+    out = {}
+    for tc in (1, 0):
+        ctx.tune(lu_tensor_cores=tc)
+        xs, _, _, st = G.wavelength_solve(ctx, sp, bg, wave, opts, G.C64)
+        out[tc] = (xs, st.iterations)
+    ctx.tune(lu_tensor_cores=1)
+    for tc, (xs, it) in out.items():
+        assert np.max(np.abs(xs - ref) / np.abs(ref)) < 1e-6, (tc, xs, ref)
+    # the FP64 refinement absorbs the weaker factorisation in a few more steps
+    assert out[1][1] <= out[0][1] + 10
