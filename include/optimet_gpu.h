@@ -37,6 +37,9 @@ extern "C" {
 /* Storage precision of the scattering matrix */
 #define OM_C128 0                 /* complex FP64 */
 #define OM_C64 1                  /* complex FP32 (precision form) */
+#define OM_ACA 2                  /* complex FP64, admissible blocks ACA-compressed (GMRES only):
+                                     Scattering_matrix_ACA_FF/_SH + ACA_compression,
+                                     PreconditionedMatrix.cpp:402-551,760-890 */
 
 /* Solve methods (Solver roles of the reference) */
 #define OM_SOLVE_LU 0             /* dense LU, partial pivoting: ScalapackSolver pzgesv role */
@@ -133,6 +136,12 @@ int om_context_tune(om_context *ctx, const om_tuning *t);
  * role of the trailing pzgemm of pzgesv (ScalapackSolver.cpp:54-130). */
 int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, long lda,
                      const float *B, long ldb, float *C, long ldc);
+/* Statistics of an ACA-compressed matrix (om_assemble with OM_ACA): device
+ * bytes of the packed blocks, number of compressed / dense off-diagonal blocks,
+ * mean and largest rank (the reference prints the compressed size in MB,
+ * PreconditionedMatrix.cpp:548). */
+int om_aca_info(om_problem *pr, int harmonic, double *store_bytes, int *compressed, int *dense,
+                double *mean_rank, int *max_rank);
 /* Record an event on the context's stream, wait for it and return in *ms the
  * device time since the previous mark (0 for the first). Device-side step
  * timing for benchmarks; no counterpart in the reference. */

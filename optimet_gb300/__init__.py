@@ -22,7 +22,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "optimet_gpu.h")
 
 OK, ERR_INVALID, ERR_OVERLAP, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_SINGULAR, ERR_STATE, PENDING = range(9)
 FF, SH = 0, 1
-C128, C64 = 0, 1
+C128, C64, ACA = 0, 1, 2
 SOLVE_LU, SOLVE_GMRES, SOLVE_FGMRES_MIXED, SOLVE_LU_MIXED = 0, 1, 2, 3
 
 ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_OVERLAP: "overlapping spheres",
@@ -105,6 +105,8 @@ def lib():
         L.om_context_timers.argtypes = [vp, C.c_int, _dp]
         L.om_context_mark.argtypes = [vp, _dp]
         L.om_context_tune.argtypes = [vp, C.POINTER(Tuning)]
+        L.om_aca_info.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp,
+                                  C.POINTER(C.c_int)]
         L.om_cgemm_sub_c64.argtypes = [vp, C.c_long, C.c_long, C.c_int, _fp, C.c_long, _fp,
                                        C.c_long, _fp, C.c_long]
         L.om_problem_create.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
@@ -354,6 +356,17 @@ class Problem:
         H = np.zeros_like(E)
         self.ctx.check(lib().om_near_field(self.h, _p(xyz), xyz.shape[0], _p(E), _p(H)))
         return E, H
+
+    def aca_info(self, harmonic=FF):
+        """Packed bytes, compressed / dense block counts, mean and max rank of
+        an OM_ACA assembly."""
+        b = C.c_double()
+        nc, nd, mx = C.c_int(), C.c_int(), C.c_int()
+        mr = C.c_double()
+        self.ctx.check(lib().om_aca_info(self.h, harmonic, C.byref(b), C.byref(nc), C.byref(nd),
+                                         C.byref(mr), C.byref(mx)))
+        return {"store_bytes": b.value, "compressed": nc.value, "dense": nd.value,
+                "mean_rank": mr.value, "max_rank": mx.value}
 
     def near_field_sh(self, xyz):
         """Second-harmonic E, H at Cartesian points (after solve_sh)."""

@@ -160,6 +160,7 @@ void free_problem(om_problem *pr) {
     om::dev_release(ctx, pr->d_S32[h], sizeof(float2) * n * n);
     pr->d_S32[h] = nullptr;
   }
+  om::aca_free(pr);
 }
 
 int make_problem(om_context *ctx, const om_sphere *spheres, int n_spheres, const om_medium *bg,
@@ -707,11 +708,28 @@ int om_incident_coefficients(om_problem *pr, double *ab) {
 
 int om_assemble(om_problem *pr, int harmonic, int precision) {
   if(!pr || (harmonic != OM_FF && harmonic != OM_SH) ||
-     (precision != OM_C128 && precision != OM_C64))
+     (precision != OM_C128 && precision != OM_C64 && precision != OM_ACA))
     return OM_ERR_INVALID;
   om_context *ctx = pr->ctx;
   cudaSetDevice(ctx->device);
   ctx->last_launches = 0;
+  if(precision == OM_ACA) {
+    int rc;
+    try {
+      rc = om::aca_build(pr, harmonic);
+    } catch(std::exception &e) {
+      ctx->err = e.what();
+      rc = OM_ERR_CUDA;
+    }
+    if(!rc)
+      rc = check_launch(ctx, "ACA compression");
+    if(rc)
+      return rc;
+    pr->S_prec[harmonic] = OM_ACA;
+    if(harmonic == OM_FF)
+      pr->have_solution = false;
+    return OM_OK;
+  }
   int rc = ensure_matrix(pr, harmonic, precision);
   if(rc)
     return rc;
@@ -730,11 +748,48 @@ int om_assemble(om_problem *pr, int harmonic, int precision) {
   return OM_OK;
 }
 
+int om_aca_info(om_problem *pr, int harmonic, double *store_bytes, int *compressed, int *dense,
+                double *mean_rank, int *max_rank) {
+  if(!pr || (harmonic != OM_FF && harmonic != OM_SH))
+    return OM_ERR_INVALID;
+  om_context *ctx = pr->ctx;
+  if(pr->S_prec[harmonic] != OM_ACA) {
+    ctx->err = "matrix not assembled with OM_ACA";
+    return OM_ERR_STATE;
+  }
+  cudaSetDevice(ctx->device);
+  const size_t NN = (size_t)pr->N * pr->N;
+  std::vector<int> r(NN);
+  cudaMemcpyAsync(r.data(), pr->aca[harmonic].rank, sizeof(int) * NN, cudaMemcpyDeviceToHost,
+                  ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if(e != cudaSuccess)
+    return cuda_fail(ctx, e, "ACA info");
+  int nc = 0, nd = 0, mx = 0;
+  double sum = 0.0;
+  for(int v : r) {
+    if(v == -1)
+      ++nd;
+    else if(v >= 0) {
+      ++nc;
+      sum += v;
+      mx = std::max(mx, v);
+    }
+  }
+  if(store_bytes) *store_bytes = (double)pr->aca[harmonic].used * sizeof(double2);
+  if(compressed) *compressed = nc;
+  if(dense) *dense = nd;
+  if(mean_rank) *mean_rank = nc ? sum / nc : 0.0;
+  if(max_rank) *max_rank = mx;
+  return OM_OK;
+}
+
 int om_copy_matrix(om_problem *pr, int harmonic, double *S) {
   if(!pr || !S || (harmonic != OM_FF && harmonic != OM_SH))
     return OM_ERR_INVALID;
-  if(pr->S_prec[harmonic] < 0) {
-    pr->ctx->err = "matrix not assembled";
+  if(pr->S_prec[harmonic] < 0 || pr->S_prec[harmonic] == OM_ACA) {
+    pr->ctx->err = pr->S_prec[harmonic] < 0 ? "matrix not assembled"
+                                             : "an ACA-compressed matrix has no dense copy";
     return OM_ERR_STATE;
   }
   cudaSetDevice(pr->ctx->device);

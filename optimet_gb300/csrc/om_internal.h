@@ -57,6 +57,21 @@ struct ShScalars {
 
 struct Arena;
 
+// ACA-compressed operator of one harmonic (aca.cu)
+struct AcaData {
+  double2 *store = nullptr;  // packed blocks (complex128)
+  size_t cap = 0, used = 0;  // capacity / used, complex values
+  long long *off = nullptr;  // per ordered block (i N + j): offset in the store
+  int *rank = nullptr;       // per ordered block: rank, -1 dense, -2 identity
+  char *ctl = nullptr;       // bump offset (8 bytes) + overflow flag
+};
+struct AcaOp {
+  int N, kmax;
+  const long long *off;
+  const int *rank;
+  const double2 *store;
+};
+
 }  // namespace om
 
 struct om_context {
@@ -132,6 +147,7 @@ struct om_problem {
   om::cplx eta;
   bool have_sh = false;
   bool have_source = false, have_solution = false;
+  om::AcaData aca[2];
 };
 
 namespace om {
@@ -141,6 +157,9 @@ const CoefTables &coef_tables(om_context *ctx, int nmax);
 void launch_sphere_terms(om_problem *pr);
 void launch_incident(om_problem *pr, const double einc[6]);
 void launch_assemble(om_problem *pr, int harmonic, int precision);
+// unordered pairs pair0 .. pair0 + count - 1 (pair b = j (j - 1) / 2 + i, i < j):
+// S_ij and S_ji as 2P x 2P column-major blocks at scratch + 2 (b - pair0) (2P)^2
+void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, double2 *scratch);
 void launch_source(om_problem *pr);
 void launch_sh_weights(om_problem *pr);
 int launch_coupling(om_context *ctx, const double *d_rel, int count, zd waveK, int nmax,
@@ -176,6 +195,13 @@ int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, 
 // timed-out wait
 void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
                          float2 *C, long ldc, long m, long n, int k, int *d_err);
+
+// aca.cu
+int aca_build(om_problem *pr, int harmonic);
+void aca_free(om_problem *pr);
+AcaOp aca_op(const om_problem *pr, int harmonic);
+// y = S x, or y = b - S x when b is given
+void aca_matvec(om_context *ctx, const AcaOp &op, const double2 *x, double2 *y, const double2 *b);
 
 // capi.cu: stream-ordered device memory counted against the context budget
 int dev_malloc(om_context *ctx, void **p, size_t bytes);

@@ -440,6 +440,18 @@ struct PrecondFn {
   virtual ~PrecondFn() {}
 };
 
+// y = S x (b null) or y = b - S x for the operators GMRES runs on: a dense
+// complex128 / complex64 matrix or the ACA-compressed operator
+template <typename M>
+void op_apply(om_context *ctx, const M *S, long n, const double2 *x, double2 *part, double2 *y,
+              const double2 *b) {
+  matvec<M, double2>(ctx, S, n, x, part, y, b);
+}
+inline void op_apply(om_context *ctx, const AcaOp *S, long, const double2 *x, double2 *, double2 *y,
+                     const double2 *b) {
+  aca_matvec(ctx, *S, x, y, b);
+}
+
 template <typename M>
 int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, double tol, int m,
             int restarts, PrecondFn *pc, int *iters, double *relres) {
@@ -478,7 +490,7 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
       cudaMemcpyAsync(r, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
       beta = bnorm;
     } else {
-      matvec<M, double2>(ctx, S, n, x, part, r, b);
+      op_apply(ctx, S, n, x, part, r, b);
       beta = vec_norm(ctx, r, n, part, hd);
     }
     if(beta == 0.0) {
@@ -499,7 +511,7 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
         op_in = Zb + (size_t)k * n;
       }
       double2 *wv = Vb + (size_t)(k + 1) * n;
-      matvec<M, double2>(ctx, S, n, op_in, part, wv, nullptr);
+      op_apply(ctx, S, n, op_in, part, wv, nullptr);
       std::vector<std::complex<double>> h;
       arnoldi_orth<double2>(ctx, Vb, n, k + 1, wv, part, hd, h);
       const double hn = h[k + 1].real();
@@ -546,7 +558,7 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
                                                                                yd, x, n);
     ctx->last_launches++;
     // true residual for the stopping test of the next cycle
-    matvec<M, double2>(ctx, S, n, x, part, t, b);
+    op_apply(ctx, S, n, x, part, t, b);
     err = vec_norm(ctx, t, n, part, hd) / bnorm;
     cudaStreamSynchronize(ctx->stream);
   }
@@ -979,10 +991,13 @@ int solve_gmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, con
   int it = 0;
   double rr = 0;
   int rc;
-  if(pr->S_prec[harmonic] == OM_C128)
+  if(pr->S_prec[harmonic] == OM_C128) {
     rc = gmres64<double2>(ctx, (const double2 *)pr->d_S[harmonic], pr->n, b, x, o->tol,
                           o->max_iter, o->restarts, nullptr, &it, &rr);
-  else  // FP64 GMRES on the complex64 system
+  } else if(pr->S_prec[harmonic] == OM_ACA) {  // Gmres_Zcomp role
+    const AcaOp op = aca_op(pr, harmonic);
+    rc = gmres64<AcaOp>(ctx, &op, pr->n, b, x, o->tol, o->max_iter, o->restarts, nullptr, &it, &rr);
+  } else  // FP64 GMRES on the complex64 system
     rc = gmres64<float2>(ctx, (const float2 *)pr->d_S32[harmonic], pr->n, b, x, o->tol,
                          o->max_iter, o->restarts, nullptr, &it, &rr);
   if(st) {
@@ -1243,8 +1258,9 @@ extern "C" int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve
     ctx->err = "om_solve_rhs_noalloc supports OM_SOLVE_GMRES only";
     return OM_ERR_INVALID;
   }
-  if(pr->S_prec[harmonic] < 0) {
-    ctx->err = "matrix not assembled";
+  if(pr->S_prec[harmonic] < 0 || pr->S_prec[harmonic] == OM_ACA) {
+    ctx->err = pr->S_prec[harmonic] < 0 ? "matrix not assembled"
+                                        : "om_solve_rhs_noalloc needs a dense matrix";
     return OM_ERR_STATE;
   }
   const long n = pr->n;

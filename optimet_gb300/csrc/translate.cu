@@ -502,6 +502,11 @@ struct AssembleArgs {
   long ld;
   int nchunks;
   int2 chunks[kMaxNmax];
+  // pair-scratch mode (ACA batches): CTA b handles unordered pair pair0 + b and
+  // writes S_ij, S_ji as two consecutive 2P x 2P column-major blocks at
+  // S + 2 b (2P)^2 (ld = 2P); no identity blocks
+  int scratch;
+  long pair0;
 };
 
 template <typename O> __device__ __forceinline__ void put_out(O *S, size_t at, double re, double im);
@@ -530,9 +535,9 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
   typedef typename std::conditional<kMixed, float, double>::type R;
   extern __shared__ double smem[];
   const long npairs = (long)a.N * (a.N - 1) / 2;
-  const long b = blockIdx.x;
+  const long b = blockIdx.x + (a.scratch ? a.pair0 : 0);
   const int P = y.P;
-  if(b >= npairs) {
+  if(!a.scratch && b >= npairs) {
     const int i = (int)(b - npairs);
     const long x0 = 2L * P * i;
     for(int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) {
@@ -548,7 +553,12 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
   while((long)(j + 1) * j / 2 <= b)
     ++j;
   const int i = (int)(b - (long)j * (j - 1) / 2);
-  const long xi = 2L * P * i, xj = 2L * P * j;
+  const long xi = a.scratch ? 0 : 2L * P * i, xj = a.scratch ? 0 : 2L * P * j;
+  OutT *Sij = S, *Sji = S;
+  if(a.scratch) {
+    Sij = S + (size_t)(2 * blockIdx.x) * (4L * P * P);
+    Sji = Sij + 4L * P * P;
+  }
   Smem s = smem_view(smem, y, a.qf, a.pf);
   TabT *tab = reinterpret_cast<TabT *>(s.tab);
   load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
@@ -599,13 +609,13 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
       // S_ij (rows of sphere i, columns of sphere j), translation r_i - r_j
       size_t col_te = (xj + q) * a.ld + xi, col_tm = (xj + P + q) * a.ld + xi;
       CT<R> v = neg_mul(tei, A);
-      put_out<OutT>(S, col_te + p, v.re, v.im);
+      put_out<OutT>(Sij, col_te + p, v.re, v.im);
       v = neg_mul(tmi, A);
-      put_out<OutT>(S, col_tm + P + p, v.re, v.im);
+      put_out<OutT>(Sij, col_tm + P + p, v.re, v.im);
       v = neg_mul(tei, B);
-      put_out<OutT>(S, col_tm + p, v.re, v.im);
+      put_out<OutT>(Sij, col_tm + p, v.re, v.im);
       v = neg_mul(tmi, B);
-      put_out<OutT>(S, col_te + P + p, v.re, v.im);
+      put_out<OutT>(Sij, col_te + P + p, v.re, v.im);
       // S_ji, translation r_j - r_i
       if((n + l) & 1) {
         A.re = -A.re;
@@ -617,13 +627,13 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
       col_te = (xi + q) * a.ld + xj;
       col_tm = (xi + P + q) * a.ld + xj;
       v = neg_mul(tej, A);
-      put_out<OutT>(S, col_te + p, v.re, v.im);
+      put_out<OutT>(Sji, col_te + p, v.re, v.im);
       v = neg_mul(tmj, A);
-      put_out<OutT>(S, col_tm + P + p, v.re, v.im);
+      put_out<OutT>(Sji, col_tm + P + p, v.re, v.im);
       v = neg_mul(tej, B);
-      put_out<OutT>(S, col_tm + p, v.re, v.im);
+      put_out<OutT>(Sji, col_tm + p, v.re, v.im);
       v = neg_mul(tmj, B);
-      put_out<OutT>(S, col_te + P + p, v.re, v.im);
+      put_out<OutT>(Sji, col_te + P + p, v.re, v.im);
     }
     __syncthreads();
   }
@@ -999,6 +1009,8 @@ void launch_assemble(om_problem *pr, int harmonic, int precision) {
   cplx k = harmonic == OM_SH ? 2.0 * pr->waveK : pr->waveK;
   a.waveK = mk(k.real(), k.imag());
   a.ld = pr->n;
+  a.scratch = 0;
+  a.pair0 = 0;
   fill_chunks(a, y);
   dim3 grid((unsigned)((long)pr->N * (pr->N - 1) / 2 + pr->N));
   timer_begin(ctx, ctx->ev_asm);
@@ -1016,6 +1028,29 @@ void launch_assemble(om_problem *pr, int harmonic, int precision) {
   cudaEventRecord(ctx->ev_join, ctx->stream_lo);
   cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);
   timer_end(ctx, ctx->ev_asm);
+  ctx->last_launches++;
+}
+
+void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, double2 *scratch) {
+  om_context *ctx = pr->ctx;
+  const CoefTables &ct = coef_tables(ctx, pr->nmax);
+  Layout y = make_layout(pr->nmax, smem_limit(), false);
+  AssembleArgs a;
+  a.cart = pr->d_cart;
+  a.T = harmonic == OM_SH ? pr->d_Tsh : pr->d_T;
+  a.rec = ct.rec;
+  a.qf = ct.qf;
+  a.pf = ct.pf;
+  a.legc = ct.legc;
+  a.N = pr->N;
+  cplx k = harmonic == OM_SH ? 2.0 * pr->waveK : pr->waveK;
+  a.waveK = mk(k.real(), k.imag());
+  a.ld = 2L * pr->P;
+  a.scratch = 1;
+  a.pair0 = pair0;
+  fill_chunks(a, y);
+  set_smem(k_assemble<false>, y.bytes, ctx->carve_asm);
+  k_assemble<false><<<count, 256, y.bytes, ctx->stream>>>(a, y, scratch);
   ctx->last_launches++;
 }
 

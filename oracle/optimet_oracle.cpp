@@ -1428,6 +1428,143 @@ void eh_fields_sh(const Problem &pr, const std::vector<double> &tab, const cplx 
   H = Hf;
 }
 
+// getMaxInd (PreconditionedMatrix.cpp:869-890): first index of the strict
+// maximum of |v_i| over the indices not among K[0 .. K.size()-2] (the last
+// slot of K is the one being chosen). The reference leaves the result
+// undefined when every candidate is 0; the first candidate is returned then.
+int aca_max_ind(const std::vector<cplx> &v, const std::vector<int> &K, int kmax) {
+  double mx = 0.0;
+  int imax = -1, first = -1;
+  for(int i = 0; i < kmax; ++i) {
+    bool same = false;
+    for(size_t j = 0; j + 1 < K.size(); ++j)
+      if(i == K[j])
+        same = true;
+    if(same)
+      continue;
+    if(first < 0)
+      first = i;
+    if(std::abs(v[i]) > mx) {
+      mx = std::abs(v[i]);
+      imax = i;
+    }
+  }
+  return imax >= 0 ? imax : first;
+}
+
+// ACA_compression (PreconditionedMatrix.cpp:760-867): partially pivoted
+// adaptive cross approximation of a kmax x kmax column-major block M ~ U V,
+// eps 1e-3, first row 0, with the reference's running norm estimate (cross
+// terms over p <= k - 2 and the first k entries of the vectors). U: kmax x r
+// column-major, V: r x kmax stored row by row (V[k kmax + c]). Returns r.
+int aca_compress(const cplx *M, int kmax, std::vector<cplx> &U, std::vector<cplx> &V) {
+  const double eps = 1e-3;
+  U.assign(size_t(kmax) * kmax, cplx(0, 0));
+  V.assign(size_t(kmax) * kmax, cplx(0, 0));
+  std::vector<int> I{0}, J;
+  std::vector<cplx> row(kmax), col(kmax);
+  double norma = 0.0;
+  int rank = kmax;
+  for(int k = 0; k < kmax; ++k) {
+    const int ik = I[k];
+    for(int c = 0; c < kmax; ++c) {
+      cplx v = M[size_t(c) * kmax + ik];
+      if(k > 0) {
+        cplx sum(0.0, 0.0);
+        for(int p = 0; p <= k - 1; ++p)
+          sum += U[size_t(p) * kmax + ik] * V[size_t(p) * kmax + c];
+        v -= sum;
+      }
+      row[c] = v;
+    }
+    J.push_back(0);
+    J[k] = aca_max_ind(row, J, kmax);
+    const cplx piv = row[J[k]];
+    for(int c = 0; c < kmax; ++c)
+      V[size_t(k) * kmax + c] = row[c] / piv;
+    for(int i = 0; i < kmax; ++i) {
+      cplx v = M[size_t(J[k]) * kmax + i];
+      if(k > 0) {
+        cplx sum(0.0, 0.0);
+        for(int p = 0; p <= k - 1; ++p)
+          sum += V[size_t(p) * kmax + J[k]] * U[size_t(p) * kmax + i];
+        v -= sum;
+      }
+      col[i] = v;
+      U[size_t(k) * kmax + i] = v;
+    }
+    double cn = 0.0, rn = 0.0;
+    for(int i = 0; i < kmax; ++i) {
+      cn += std::norm(U[size_t(k) * kmax + i]);
+      rn += std::norm(V[size_t(k) * kmax + i]);
+    }
+    cn = std::sqrt(cn);
+    rn = std::sqrt(rn);
+    if(k == 0) {
+      norma = std::pow(cn, 2) * std::pow(rn, 2);
+    } else {
+      double sum = 0.0;
+      for(int p = 0; p != k - 1; ++p) {
+        cplx pom1(0.0, 0.0), pom2(0.0, 0.0);
+        for(int tt = 0; tt != k; ++tt) {
+          pom1 += U[size_t(p) * kmax + tt] * U[size_t(k) * kmax + tt];
+          pom2 += V[size_t(p) * kmax + tt] * V[size_t(k) * kmax + tt];
+        }
+        sum += std::abs(pom1) * std::abs(pom2);
+      }
+      norma = norma + std::pow(cn, 2) * std::pow(rn, 2) + 2.0 * sum;
+      if(eps * std::sqrt(norma) >= cn * rn) {
+        rank = k + 1;
+        break;
+      }
+    }
+    I.push_back(0);
+    I[k + 1] = aca_max_ind(col, I, kmax);
+  }
+  U.resize(size_t(kmax) * rank);
+  V.resize(size_t(kmax) * rank);
+  return rank;
+}
+
+// Scattering_matrix_ACA_FF / _SH (PreconditionedMatrix.cpp:462-551, 612-757)
+// written out densely: admissible blocks (distance >= 2 (a_i + a_j),
+// Tools::findDistance) replaced by their ACA product U V. ranks[i N + j]:
+// -2 diagonal, -1 dense, else the rank.
+void aca_matrix(const Problem &pr, bool sh, cplx *S, int *ranks) {
+  const int N = (int)pr.objects.size(), P = pmax(pr.nmax), n2 = 2 * P;
+  const size_t ld = size_t(n2) * N;
+  scattering_matrix(pr, sh, S);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(g_threads)
+  for(long t = 0; t < (long)N * N; ++t) {
+    const int i = (int)(t / N), j = (int)(t % N);
+    if(i == j) {
+      ranks[t] = -2;
+      continue;
+    }
+    const Sphere &a = pr.objects[i], &b = pr.objects[j];
+    const Cart ca = to_cart(a.vR), cb = to_cart(b.vR);
+    const double d = std::sqrt(std::pow(cb.x - ca.x, 2.0) + std::pow(cb.y - ca.y, 2.0) +
+                               std::pow(cb.z - ca.z, 2.0));
+    if(!(d >= 2.0 * (a.radius + b.radius))) {
+      ranks[t] = -1;
+      continue;
+    }
+    std::vector<cplx> blk(size_t(n2) * n2), U, V;
+    for(int q = 0; q < n2; ++q)
+      for(int p = 0; p < n2; ++p)
+        blk[size_t(q) * n2 + p] = S[(size_t(n2) * j + q) * ld + size_t(n2) * i + p];
+    const int r = aca_compress(blk.data(), n2, U, V);
+    ranks[t] = r;
+    for(int q = 0; q < n2; ++q)
+      for(int p = 0; p < n2; ++p) {
+        cplx v(0.0, 0.0);
+        for(int k = 0; k < r; ++k)
+          v += U[size_t(k) * n2 + p] * V[size_t(k) * n2 + q];
+        S[(size_t(n2) * j + q) * ld + size_t(n2) * i + p] = v;
+      }
+  }
+}
+
 inline cplx *C(double *p) { return reinterpret_cast<cplx *>(p); }
 inline const cplx *C(const double *p) { return reinterpret_cast<const cplx *>(p); }
 
@@ -1836,6 +1973,33 @@ int orc_near_field_sh(void *h, const double *tables, const double *Xi, const dou
       C(H)[3 * i + 1] = hh.y;
       C(H)[3 * i + 2] = hh.z;
     }
+    return 0;
+  } catch(std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// ACA_compression of one kmax x kmax column-major block: U (kmax x r), V
+// (r rows of kmax); U and V need kmax * kmax complex values of room.
+int orc_aca_block(const double *M, int kmax, double *U, double *V, int *rank) {
+  try {
+    std::vector<cplx> u, v;
+    const int r = aca_compress(C(M), kmax, u, v);
+    std::memcpy(U, u.data(), sizeof(cplx) * u.size());
+    std::memcpy(V, v.data(), sizeof(cplx) * v.size());
+    *rank = r;
+    return 0;
+  } catch(std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// The ACA-compressed scattering matrix written out densely, with the block ranks.
+int orc_aca_matrix(void *h, int sh, double *S, int *ranks) {
+  try {
+    aca_matrix(*static_cast<Problem *>(h), sh != 0, C(S), ranks);
     return 0;
   } catch(std::exception &e) {
     g_err = e.what();

@@ -57,6 +57,8 @@ def lib():
         L.orc_cross_sections.argtypes = [C.c_void_p, _dp, _dp]
         L.orc_near_field.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _dp]
         L.orc_near_field_sh.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp]
+        L.orc_aca_block.argtypes = [_dp, C.c_int, _dp, _dp, C.POINTER(C.c_int)]
+        L.orc_aca_matrix.argtypes = [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_int)]
         L.orc_wavelength_solve.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int,
                                            _dp, _dp, _dp, C.POINTER(C.c_int)]
         L.orc_lu_solve.argtypes = [C.c_int, _dp, _dp, _dp]
@@ -263,6 +265,16 @@ class Problem:
             raise RuntimeError(lib().orc_last_error().decode())
         return E, H
 
+    def aca_matrix(self, sh=False):
+        """Scattering matrix with the admissible blocks replaced by their ACA
+        products (dense), and the block ranks (N x N: -2 diagonal, -1 dense)."""
+        n = self.n
+        S = np.zeros((n, n), np.complex128, order="F")
+        ranks = np.zeros(self.cl.n_spheres ** 2, np.int32)
+        if lib().orc_aca_matrix(self.h, int(sh), _p(S), ranks.ctypes.data_as(C.POINTER(C.c_int))):
+            raise RuntimeError(lib().orc_last_error().decode())
+        return S, ranks.reshape(self.cl.n_spheres, self.cl.n_spheres)
+
     def near_field_sh(self, tables, x_int, x_sca_sh, x_int_sh, xyz):
         """Second-harmonic E, H (3 complex per point) at Cartesian points."""
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
@@ -366,6 +378,19 @@ def gmres(A, b, tol=1e-10, maxit=240, restarts=2):
     lib().orc_gmres(A.shape[0], _p(A), _p(b), _p(x), tol, maxit, restarts, C.byref(it),
                     C.byref(rr))
     return x, it.value, rr.value
+
+
+def aca_block(M):
+    """ACA_compression of one square block: (U kmax x r, V r x kmax, r)."""
+    M = np.asfortranarray(M, dtype=np.complex128)
+    k = M.shape[0]
+    U = np.zeros(k * k, np.complex128)
+    V = np.zeros(k * k, np.complex128)
+    r = C.c_int(0)
+    if lib().orc_aca_block(_p(M), k, _p(U), _p(V), C.byref(r)):
+        raise RuntimeError(lib().orc_last_error().decode())
+    r = r.value
+    return U[:k * r].reshape(r, k).T, V[:k * r].reshape(r, k), r
 
 
 def grid_points(params):
