@@ -781,6 +781,59 @@ def near_field_arm(args):
     return res
 
 
+def aca_arm(args):
+    """ACA-compressed FP64 form (the reference's ACA + Gmres_Zcomp role:
+    eps 1e-3, GMRES tol 1e-6, 240 iterations, 2 restarts) on the c2 cluster
+    and on a 1,000-sphere cluster whose dense matrix would not fit comfortably."""
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    ctx = G.Context(0)
+    opts = G.options(G.SOLVE_GMRES, tol=1e-6, max_iter=240, restarts=2)
+    out = {}
+    cases = [("c2", WORKLOADS["c2"]),
+             ("n1000", dict(WORKLOADS["c2"], N=1000, edge=6000 * nm, nmax=6, seed=20260406,
+                            desc="N=1000 spheres, nMax=6 (96,000 unknowns), 6 um cube, radii U[40,70] nm"))]
+    for name, w in cases:
+        xyz, rad = cluster(w)
+        sp = G.spheres_array(xyz, rad, complex(w["index"]) ** 2, w["nmax"])
+        pr = G.Problem(ctx, sp, G.medium(complex(w["host"]) ** 2), G.plane_wave(w["lam"]))
+        times = []
+        for i in range(args.warmup + args.steps):
+            pr.set_wavelength(w["lam"] + 0.25 * nm * i)
+            ctx.mark()
+            pr.source_vector(copy=False)
+            pr.assemble(G.FF, G.ACA)
+            t_asm = ctx.mark()
+            st = pr.solve(opts)
+            xs = pr.cross_sections()
+            t_sol = ctx.mark()
+            if i >= args.warmup:
+                times.append((t_asm, t_sol))
+        info = pr.aca_info()
+        n = pr.n
+        res = {"unknowns": n, "ms_assemble_compress": float(np.mean([t[0] for t in times])),
+               "ms_solve": float(np.mean([t[1] for t in times])), "gmres_iterations": st.iterations,
+               "store_GB": info["store_bytes"] / 1e9, "dense_c128_GB": 16.0 * n * n / 1e9,
+               "compressed_blocks": info["compressed"], "dense_blocks": info["dense"],
+               "mean_rank": info["mean_rank"], "max_rank": info["max_rank"], "xsec": list(xs)}
+        if name == "c2":
+            pr.assemble(G.FF, G.C128)
+            pr.solve(G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=400, restarts=6))
+            ref = pr.cross_sections()
+            res["qext_rel_err_vs_dense_fp64"] = abs(xs[0] - ref[0]) / abs(ref[0])
+        res["wavelength_solves_per_s"] = 1e3 / (res["ms_assemble_compress"] + res["ms_solve"])
+        out[name] = res
+        pr.close()
+    ctx.close()
+    return {"metric": "ACA-compressed wavelength-solves/s (FP64)", "value": out["c2"]["wavelength_solves_per_s"],
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / out["c2"]["wavelength_solves_per_s"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64), ACA eps 1e-3",
+            "data": "synthetic (seeded)", "config": {"workload": "aca: c2 and a 1,000-sphere cluster"},
+            "cases": out}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -788,7 +841,7 @@ def main():
     ap.add_argument("--slots", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c1f", "c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c1f", "c3", "c4", "aca"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--single-stream", action="store_true",
                     help="only the single-stream measurement of both forms (profiling runs)")
@@ -799,7 +852,9 @@ def main():
     ap.add_argument("--batch-slots", type=int, default=6, help="server slots for c3 / c4")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.workload == "c1f":
+    if args.workload == "aca":
+        out = aca_arm(args) if args.impl != "reference" else None
+    elif args.workload == "c1f":
         out = near_field_arm(args) if args.impl != "reference" else None
     elif args.workload == "c3":
         out = batch_arm(args) if args.impl != "reference" else None

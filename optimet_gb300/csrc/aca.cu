@@ -243,17 +243,14 @@ __global__ void __launch_bounds__(kAcaThreads) k_aca_blocks(AcaBuildArgs a) {
   __syncthreads();
   if(s_off + sz > a.cap)
     return;
-  // U (kmax x r, column-major) then V stored column-major as r x kmax
-  for(size_t e = threadIdx.x; e < (size_t)kmax * r; e += blockDim.x)
-    a.store[s_off + e] = U[e];
-  for(size_t e = threadIdx.x; e < (size_t)kmax * r; e += blockDim.x) {
-    const size_t q = e % r, c = e / r;
-    a.store[s_off + (size_t)kmax * r + e] = V[q * kmax + c];
-  }
+  // U (kmax x r, column-major) then V (r rows of kmax)
+  for(size_t e = threadIdx.x; e < 2 * (size_t)kmax * r; e += blockDim.x)
+    a.store[s_off + e] = e < (size_t)kmax * r ? U[e] : V[e - (size_t)kmax * r];
 }
 
 // y_i = sum_j S_ij x_j (or b_i - that sum), one CTA per block row, blocks in
-// column order: identity, dense 2P x 2P, or U (V x_j).
+// column order: identity, dense 2P x 2P, or U (V x_j) with V x_j formed by
+// one warp per row of V.
 __global__ void __launch_bounds__(kAcaThreads) k_aca_matvec(AcaOp op, const double2 *x,
                                                            const double2 *b, double2 *y) {
   extern __shared__ double msm[];
@@ -286,12 +283,20 @@ __global__ void __launch_bounds__(kAcaThreads) k_aca_matvec(AcaOp op, const doub
       }
     } else if(r > 0) {
       const double2 *U = op.store + op.off[slot];
-      const double2 *Vt = U + (size_t)kmax * r;  // r x kmax, column-major
-      for(int q = threadIdx.x; q < r; q += blockDim.x) {
+      const double2 *V = U + (size_t)kmax * r;  // r rows of kmax
+      // t = V x_j: one warp per row of V, lanes along the row, fixed-order
+      // shuffle reduction
+      const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for(int q = w; q < r; q += nw) {
         zd s = mk(0.0, 0.0);
-        for(int c = 0; c < kmax; ++c)
-          s = s + ld2(Vt, (size_t)c * r + q) * xs[c];
-        ts[q] = s;
+        for(int c = lane; c < kmax; c += 32)
+          s = s + ld2(V, (size_t)q * kmax + c) * xs[c];
+        for(int o = 16; o > 0; o >>= 1) {
+          s.re += __shfl_down_sync(0xffffffffu, s.re, o);
+          s.im += __shfl_down_sync(0xffffffffu, s.im, o);
+        }
+        if(lane == 0)
+          ts[q] = s;
       }
       __syncthreads();
       for(int u = 0; u < 2; ++u) {
