@@ -28,8 +28,8 @@ from typing import List, Optional
 
 import numpy as np
 
-from . import (C64, C128, FF, SH, SOLVE_FGMRES_MIXED, SOLVE_GMRES, SOLVE_LU, Context, Problem,
-               medium, options, plane_wave, spheres_array)
+from . import (ACA, C64, C128, FF, SH, SOLVE_FGMRES_MIXED, SOLVE_GMRES, SOLVE_LU, Context,
+               Problem, medium, options, plane_wave, spheres_array)
 from . import materials
 
 FRNM_TO_M = 1e-9  # consFrnmTom (constants.cpp)
@@ -288,7 +288,15 @@ class GpuSolver:
         self.ctx = ctx or Context(0)
         self.pr = None  # built by the first update() (the scan sets its wavelength first)
 
+    def _form(self):
+        # <ACA compression="yes">: compressed operator under Gmres_Zcomp
+        if self.precision == C128 and self.run.geometry.ACA_cond:
+            return ACA
+        return self.precision
+
     def _options(self):
+        if self._form() == ACA:  # PreconditionedMatrixSolver.h:48-51
+            return options(SOLVE_GMRES, tol=1e-6, max_iter=240, restarts=2)
         if self.precision == C64:
             return options(SOLVE_FGMRES_MIXED, tol=min(self.run.tolerance, 1e-8), max_iter=30,
                            restarts=8, inner_iter=80, inner_tol=1e-4)
@@ -324,12 +332,13 @@ class GpuSolver:
         if self.pr is None:
             self.update()
         opts = self._options()
-        self.pr.assemble(FF, self.precision)
+        form = self._form()
+        self.pr.assemble(FF, form)
         self.pr.solve(opts, allow_unconverged=False)
         X_sca, X_int = self.pr.coefficients()
         X_sca_SH = X_int_SH = None
         if self.run.excitation.SH_cond:
-            self.pr.assemble(SH, self.precision)
+            self.pr.assemble(SH, form)
             self.pr.solve_sh(opts)
             _, _, X_sca_SH, X_int_SH = self.pr.sh_vectors()
         return X_sca, X_int, X_sca_SH, X_int_SH
