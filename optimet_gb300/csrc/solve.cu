@@ -49,7 +49,21 @@ template <typename V> __device__ __forceinline__ V cfma_conj(V a, V b, V c) {  /
 }
 
 constexpr int kMvThreads = 256;
-constexpr int kMvCols = 1024;  // columns per split-K chunk (x staged in shared memory)
+constexpr int kMvCols = 1024;  // largest split-K chunk (x staged in shared memory)
+
+// Columns per split-K chunk: 1024, halved (down to 128) while the tile grid
+// would leave the GPU short of work (fewer than 4 tiles per SM).
+inline int mv_cols(const om_context *ctx, long n) {
+  int cols = kMvCols;
+  const long rows = (n + kMvThreads - 1) / kMvThreads;
+  while(cols > 128 && rows * ((n + cols - 1) / cols) < 4L * ctx->sm_count)
+    cols >>= 1;
+  return cols;
+}
+inline int mv_nsplit(const om_context *ctx, long n) {
+  const int c = mv_cols(ctx, n);
+  return (int)((n + c - 1) / c);
+}
 
 // Partial y over chunks of columns: part[s * n + i] = sum_{j in chunk s} S[j ld + i] x[j].
 // A tile is kMvThreads rows x kMvCols columns; the grid is capped (a few CTAs
@@ -61,7 +75,7 @@ constexpr int kMvCols = 1024;  // columns per split-K chunk (x staged in shared 
 template <typename M, typename V>
 __global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld, long n, const V *x,
                                                            V *part, int row_tiles, long tiles,
-                                                           unsigned long long *next) {
+                                                           unsigned long long *next, int cols) {
   __shared__ V xs[kMvCols];
   __shared__ long tile;
   for(;;) {
@@ -74,8 +88,8 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld,
       break;
     const long ct = t / row_tiles, rt = t - ct * row_tiles;
     const long i = rt * kMvThreads + threadIdx.x;
-    const long j0 = ct * kMvCols;
-    const long j1 = min(n, j0 + kMvCols);
+    const long j0 = ct * cols;
+    const long j1 = min(n, j0 + cols);
     for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads)
       xs[j - j0] = x[j];
     __syncthreads();
@@ -132,7 +146,7 @@ __device__ __forceinline__ void df_add(DF &a, float p) {
 __global__ void __launch_bounds__(kMvThreads) k_matvec_part_df(const float2 *S, long ld, long n,
                                                                const double2 *x, double2 *part,
                                                                int row_tiles, long tiles,
-                                                               unsigned long long *next) {
+                                                               unsigned long long *next, int cols) {
   __shared__ float4 xs[kMvCols];
   __shared__ long tile;
   for(;;) {
@@ -145,8 +159,8 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part_df(const float2 *S, 
       break;
     const long ct = t / row_tiles, rt = t - ct * row_tiles;
     const long i = rt * kMvThreads + threadIdx.x;
-    const long j0 = ct * kMvCols;
-    const long j1 = min(n, j0 + kMvCols);
+    const long j0 = ct * cols;
+    const long j1 = min(n, j0 + cols);
     for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads) {
       const double2 v = x[j];
       const float hr = (float)v.x, hi = (float)v.y;
@@ -338,7 +352,7 @@ int alloc_work(om_context *ctx, Work &w, size_t bytes) {
 
 template <typename M, typename V>
 void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, const V *b) {
-  const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
+  const int nsplit = mv_nsplit(ctx, n);
   const int row_tiles = (int)((n + kMvThreads - 1) / kMvThreads);
   const long tiles = (long)row_tiles * nsplit;
   constexpr bool df = sizeof(M) == sizeof(float2) && sizeof(V) == sizeof(double2);
@@ -358,10 +372,11 @@ void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, cons
   if constexpr(df)
     k_matvec_part_df<<<grid, kMvThreads, 0, ctx->stream>>>((const float2 *)S, n, n,
                                                            (const double2 *)x, (double2 *)part,
-                                                           row_tiles, tiles, ctx->d_tile_counter);
+                                                           row_tiles, tiles, ctx->d_tile_counter,
+                                                           mv_cols(ctx, n));
   else
     k_matvec_part<M, V><<<grid, kMvThreads, 0, ctx->stream>>>(S, n, n, x, part, row_tiles, tiles,
-                                                              ctx->d_tile_counter);
+                                                              ctx->d_tile_counter, mv_cols(ctx, n));
   timer_end(ctx, ev);
   k_matvec_reduce<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(part, nsplit, n, b, y);
   ctx->last_launches += 2;
@@ -383,14 +398,15 @@ void multidot(om_context *ctx, const V *Vb, long n, int k, const V *w, V *part, 
     hh[t] = std::complex<double>(tmp[t].x, tmp[t].y);
 }
 
-template <typename V> void upload_h(om_context *ctx, const std::vector<std::complex<double>> &h, int k, V *hd) {
-  std::vector<V> tmp(k);
-  for(int t = 0; t < k; ++t) {
-    tmp[t].x = h[t].real();
-    tmp[t].y = h[t].imag();
-  }
-  cudaMemcpyAsync(hd, tmp.data(), sizeof(V) * k, cudaMemcpyHostToDevice, ctx->stream);
+// the same sums left on the device (hd[0..k]), no host copy
+template <typename V>
+void multidot_dev(om_context *ctx, const V *Vb, long n, int k, const V *w, V *part, V *hd) {
+  const int nblk = (int)((n + kDotRows - 1) / kDotRows);
+  k_multidot<V><<<nblk, kDotThreads, 0, ctx->stream>>>(Vb, n, k, w, n, part);
+  k_sum_parts<V><<<1, 256 * ((k + 256) / 256), 0, ctx->stream>>>(part, nblk, k + 1, hd);
+  ctx->last_launches += 2;
 }
+
 
 // Givens rotation of det_approx (PreconditionedMatrix.cpp:1102-1118)
 void givens(std::complex<double> hi1, std::complex<double> hi2, std::complex<double> &c,
@@ -410,20 +426,24 @@ void givens(std::complex<double> hi1, std::complex<double> hi2, std::complex<dou
 template <typename V>
 void arnoldi_orth(om_context *ctx, const V *Vb, long n, int k, V *w, V *part, V *hd,
                   std::vector<std::complex<double>> &h) {
-  std::vector<std::complex<double>> h1, h2;
-  multidot(ctx, Vb, n, k, w, part, hd, h1);
-  upload_h(ctx, h1, k, hd);
-  k_sub_basis<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, hd, w, n);
-  multidot(ctx, Vb, n, k, w, part, hd, h2);
-  upload_h(ctx, h2, k, hd);
-  k_sub_basis<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, hd, w, n);
+  // hd holds (2 k + 3 entries): the projections of the two passes, then
+  // |w|^2 after both; the passes subtract with the device copies and the host
+  // reads all three once
+  V *h1 = hd, *h2 = hd + (k + 1), *h3 = hd + 2 * (k + 1);
+  multidot_dev(ctx, Vb, n, k, w, part, h1);
+  k_sub_basis<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, h1, w, n);
+  multidot_dev(ctx, Vb, n, k, w, part, h2);
+  k_sub_basis<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, h2, w, n);
+  multidot_dev(ctx, Vb, n, 0, w, part, h3);
   ctx->last_launches += 2;
+  std::vector<V> tmp(2 * (k + 1) + 1);
+  cudaMemcpyAsync(tmp.data(), hd, sizeof(V) * tmp.size(), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
   h.assign(k + 1, 0.0);
   for(int t = 0; t < k; ++t)
-    h[t] = h1[t] + h2[t];
-  std::vector<std::complex<double>> h3;
-  multidot(ctx, Vb, n, 0, w, part, hd, h3);  // ||w|| after both passes
-  h[k] = std::sqrt(h3[0].real());
+    h[t] = std::complex<double>(tmp[t].x, tmp[t].y) +
+           std::complex<double>(tmp[k + 1 + t].x, tmp[k + 1 + t].y);
+  h[k] = std::sqrt((double)tmp[2 * (k + 1)].x);
 }
 
 double vec_norm(om_context *ctx, const double2 *w, long n, double2 *part, double2 *hd) {
@@ -457,10 +477,10 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
             int restarts, PrecondFn *pc, int *iters, double *relres) {
   Work w;
   w.ctx = ctx;
-  const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
+  const int nsplit = mv_nsplit(ctx, n);
   const int nblk = (int)((n + kDotRows - 1) / kDotRows);
   size_t bytes = sizeof(double2) * ((size_t)(m + 1) * n + (pc ? (size_t)m * n : 0) + 2 * n +
-                                    (size_t)nsplit * n + (size_t)nblk * (m + 2) + 2 * (m + 2)) +
+                                    (size_t)nsplit * n + (size_t)nblk * (m + 2) + 3 * (m + 2)) +
                  64 * 256;
   int rc = alloc_work(ctx, w, bytes);
   if(rc)
@@ -471,7 +491,7 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
   double2 *r = w.take<double2>(n, off);
   double2 *t = w.take<double2>(n, off);
   double2 *part = w.take<double2>((size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)), off);
-  double2 *hd = w.take<double2>(m + 2, off);
+  double2 *hd = w.take<double2>(2 * (m + 2), off);
   double2 *yd = w.take<double2>(m + 2, off);
 
   cudaMemsetAsync(x, 0, sizeof(double2) * n, ctx->stream);
@@ -583,11 +603,11 @@ struct InnerGmres32 : PrecondFn {
     w.ctx = c;
   }
   int init() {
-    const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
+    const int nsplit = mv_nsplit(ctx, n);
     const int nblk = (int)((n + kDotRows - 1) / kDotRows);
     size_t bytes = sizeof(float2) * ((size_t)(m + 1) * n + 2 * n +
                                      (size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)) +
-                                     2 * (m + 2)) +
+                                     3 * (m + 2)) +
                    16 * 256;
     int rc = alloc_work(ctx, w, bytes);
     if(rc)
@@ -597,7 +617,7 @@ struct InnerGmres32 : PrecondFn {
     r = w.take<float2>(n, off);
     xz = w.take<float2>(n, off);
     part = w.take<float2>((size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)), off);
-    hd = w.take<float2>(m + 2, off);
+    hd = w.take<float2>(2 * (m + 2), off);
     yd = w.take<float2>(m + 2, off);
     return OM_OK;
   }
@@ -1145,7 +1165,7 @@ void *noalloc_scratch(om_context *ctx) {
 template <typename M>
 int gmres_on_workspace(om_context *ctx, const M *S, long n, const double2 *b, double2 *x,
                        double tol, int m, int restarts, char *ws, int *iters, double *relres) {
-  const int nsplit = (int)((n + kMvCols - 1) / kMvCols);
+  const int nsplit = mv_nsplit(ctx, n);
   const int nblk = (int)((n + kDotRows - 1) / kDotRows);
   Work w;  // view only: buf is not owned
   w.ctx = ctx;
@@ -1155,7 +1175,7 @@ int gmres_on_workspace(om_context *ctx, const M *S, long n, const double2 *b, do
   double2 *r = w.take<double2>(n, off);
   double2 *t = w.take<double2>(n, off);
   double2 *part = w.take<double2>((size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)), off);
-  double2 *hd = w.take<double2>(m + 2, off);
+  double2 *hd = w.take<double2>(2 * (m + 2), off);
   double2 *yd = w.take<double2>(m + 2, off);
   w.buf = nullptr;  // keep ~Work from freeing the static array
 
@@ -1271,12 +1291,12 @@ extern "C" int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve
   }
   // bytes the solve needs: b and x, then the workspace of gmres_on_workspace
   auto round = [](size_t v) { return ((v + 255) / 256) * 256; };
-  const size_t nsplit = (size_t)((n + kMvCols - 1) / kMvCols);
+  const size_t nsplit = (size_t)mv_nsplit(ctx, n);
   const size_t nblk = (size_t)((n + kDotRows - 1) / kDotRows);
   const size_t z = sizeof(double2);
   const size_t need = 2 * round(z * n) + round(z * (size_t)(m + 1) * n) + 2 * round(z * n) +
                       round(z * std::max(nsplit * n, nblk * (size_t)(m + 2))) +
-                      2 * round(z * (size_t)(m + 2));
+                      round(z * 2 * (size_t)(m + 2)) + round(z * (size_t)(m + 2));
   if(need > kNoAllocBytes) {
     ctx->err = "problem too large for the no-alloc scratch: needs " + std::to_string(need) +
                " bytes, the fixed array holds " + std::to_string(kNoAllocBytes) +
