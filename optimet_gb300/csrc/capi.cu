@@ -415,6 +415,8 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
     ctx->carve_mv = t->matvec_carveout;
   if(t->lu_tensor_cores >= 0)
     ctx->lu_tc = t->lu_tensor_cores ? 1 : 0;
+  if(t->matvec_tma >= 0)
+    ctx->mv_tma = t->matvec_tma ? 1 : 0;
   return OM_OK;
 }
 
@@ -513,7 +515,10 @@ int om_context_create(int device, size_t budget_bytes, om_context **out) {
     delete ctx;
     return OM_ERR_CUDA;
   }
-  if(cudaMalloc(&ctx->d_tile_counter, 256) != cudaSuccess) {
+  if(cudaMalloc(&ctx->d_tile_counter, 256) == cudaSuccess) {
+    ctx->d_tma_err = reinterpret_cast<int *>(ctx->d_tile_counter + 1);
+    cudaMemset(ctx->d_tile_counter, 0, 256);
+  } else {
     cudaGetLastError();
     cudaStreamDestroy(ctx->stream);
     cudaStreamDestroy(ctx->stream_lo);
@@ -884,6 +889,15 @@ static int solve_impl(om_problem *pr, int harmonic, const om_solve_options *o, c
     st->seconds = ms * 1e-3;
   if(!rc)
     rc = check_launch(ctx, "solve");
+  // a TMA matvec whose bounded wait ran out leaves a flag
+  int tma_err = 0;
+  cudaMemcpyAsync(&tma_err, ctx->d_tma_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  if(tma_err) {
+    cudaMemsetAsync(ctx->d_tma_err, 0, sizeof(int), ctx->stream);
+    ctx->err = "a TMA matrix-vector product timed out";
+    rc = OM_ERR_CUDA;
+  }
   return rc;
 }
 

@@ -84,6 +84,8 @@ struct om_context {
   // stride): below the SM's capacity so that another slot's assembly fits
   int mv_ctas = 8, mv_ctas_df = 8;
   unsigned long long *d_tile_counter = nullptr;  // matvec tile counter (device)
+  int *d_tma_err = nullptr;                      // set by a TMA matvec whose wait timed out
+  int mv_tma = 1;                                // complex64 matvecs staged by TMA
   int carve_asm = -1, carve_mv = -1;  // preferred smem carveout (percent), -1 = driver's choice
   int lu_tc = 1;  // complex64 LU trailing updates on the tensor cores
   size_t budget = 0;
@@ -202,6 +204,11 @@ void aca_free(om_problem *pr);
 AcaOp aca_op(const om_problem *pr, int harmonic);
 // y = S x, or y = b - S x when b is given
 void aca_matvec(om_context *ctx, const AcaOp &op, const double2 *x, double2 *y, const double2 *b);
+
+// tma_matvec.cu: complex64 matvec with TMA-staged matrix tiles; false when the
+// tensor map cannot be encoded
+bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const void *x, void *part, bool df,
+                       int row_tiles, long tiles, int cols, unsigned grid);
 
 // capi.cu: stream-ordered device memory counted against the context budget
 int dev_malloc(om_context *ctx, void **p, size_t bytes);

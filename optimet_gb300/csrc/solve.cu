@@ -369,7 +369,16 @@ void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, cons
   }
   timer_begin(ctx, ev);
   cudaMemsetAsync(ctx->d_tile_counter, 0, sizeof(unsigned long long), ctx->stream);
-  if constexpr(df)
+  // the inner FP32 matvec streams its tiles through TMA; the compensated one
+  // (FP32-ALU heavy) keeps the register-prefetching kernel, which measured
+  // faster (6.98 ms against 9.12 ms at n = 64,000)
+  bool done = false;
+  if constexpr(sizeof(M) == sizeof(float2) && !df)
+    if(ctx->mv_tma)
+      done = launch_matvec_tma(ctx, (const float2 *)S, n, x, part, false, row_tiles, tiles,
+                               mv_cols(ctx, n), grid);
+  if(done) {
+  } else if constexpr(df)
     k_matvec_part_df<<<grid, kMvThreads, 0, ctx->stream>>>((const float2 *)S, n, n,
                                                            (const double2 *)x, (double2 *)part,
                                                            row_tiles, tiles, ctx->d_tile_counter,

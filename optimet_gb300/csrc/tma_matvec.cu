@@ -1,0 +1,259 @@
+// Complex64 matrix-vector products with the matrix staged by the Tensor
+// Memory Accelerator: the GMRES matvecs of the precision form (the inner FP32
+// one and the compensated FP64-accurate residual one).
+//
+// Same decomposition as the plain kernels: tiles of 256 rows x `cols` columns
+// taken from a counter by a capped grid, x chunk in shared memory, one row
+// per thread, partial sums per column chunk. Here the tile's columns arrive
+// in stages of 16 columns (256 x 16 complex64 = 32 KB, one 2-D TMA box of the
+// column-major matrix) through a 4-deep ring of shared-memory buffers, each
+// with an mbarrier that the TMA completes by transaction bytes. Thread 0
+// issues the copies; after all threads have consumed a buffer it refills it
+// with the stage four ahead. Waits are bounded (error flag, no hang). The
+// arithmetic and its order per thread are those of the plain kernels, so
+// the results are bitwise the same.
+#include <cuda.h>
+
+#include <mutex>
+#include <type_traits>
+
+#include "om_internal.h"
+
+namespace om {
+
+namespace {
+
+constexpr int kTmaRows = 256, kTmaStageCols = 16, kTmaStages = 4;
+constexpr uint32_t kStageBytes = kTmaRows * kTmaStageCols * sizeof(float2);
+
+__device__ __forceinline__ uint32_t sa(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tma_load(void *dst, const CUtensorMap *tm, int row, int col,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          sa(dst)),
+      "l"(tm), "r"(row), "r"(col), "r"(sa(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void arm(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(bar)), "r"(bytes)
+               : "memory");
+}
+
+// bounded wait for the given phase parity; false on time-out
+__device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity) {
+  for(long it = 0; it < (1L << 26); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(sa(bar)), "r"(parity)
+        : "memory");
+    if(ok)
+      return true;
+  }
+  return false;
+}
+
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ void df_add(DF &a, float p) {
+  const float s = a.hi + p;
+  const float bb = s - a.hi;
+  a.lo += (a.hi - (s - bb)) + (p - bb);
+  a.hi = s;
+}
+
+template <bool kDF> struct XT;
+template <> struct XT<false> { typedef float2 type; };
+template <> struct XT<true> { typedef float4 type; };
+
+// kDF = false: part = S x (complex64 x complex64, two alternating FP32
+// accumulators as k_matvec_part); kDF = true: the compensated product of
+// k_matvec_part_df (x split into hi + lo floats, TwoProduct / TwoSum).
+template <bool kDF>
+__global__ void __launch_bounds__(kTmaRows) k_matvec_tma(const __grid_constant__ CUtensorMap tm, long n,
+                                                      const typename std::conditional<kDF, double2, float2>::type *x,
+                                                      typename std::conditional<kDF, double2, float2>::type *part,
+                                                      int row_tiles, long tiles, unsigned long long *next,
+                                                      int cols, int *err) {
+  extern __shared__ __align__(128) unsigned char tsm_[];
+  float2 *stage = reinterpret_cast<float2 *>(tsm_);  // [kTmaStages][kTmaStageCols][kTmaRows]
+  typename XT<kDF>::type *xs =
+      reinterpret_cast<typename XT<kDF>::type *>(tsm_ + kTmaStages * kStageBytes);
+  __shared__ __align__(8) uint64_t bar[kTmaStages];
+  __shared__ long tile;
+  __shared__ int fail;
+  const int t = threadIdx.x;
+  if(t == 0) {
+    for(int s = 0; s < kTmaStages; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(&bar[s])), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fail = 0;
+  }
+  __syncthreads();
+  uint32_t parity = 0;  // bit s: parity of the next completion of bar[s]
+  for(;;) {
+    __syncthreads();
+    if(t == 0)
+      tile = (long)atomicAdd(next, 1ull);
+    __syncthreads();
+    const long tl = tile;
+    if(tl >= tiles || fail)
+      break;
+    const long ct = tl / row_tiles, rt = tl - ct * row_tiles;
+    const long i = rt * kTmaRows + t;
+    const long j0 = ct * cols;
+    const long j1 = min(n, j0 + cols);
+    const int nst = (int)((j1 - j0 + kTmaStageCols - 1) / kTmaStageCols);
+    if(t == 0) {
+      for(int s = 0; s < kTmaStages && s < nst; ++s) {
+        arm(&bar[s], kStageBytes);
+        tma_load(stage + (size_t)s * kTmaStageCols * kTmaRows, &tm, (int)(rt * kTmaRows),
+                 (int)(j0 + s * kTmaStageCols), &bar[s]);
+      }
+    }
+    for(long j = j0 + t; j < j1; j += kTmaRows) {
+      if constexpr(kDF) {
+        const double2 v = x[j];
+        const float hr = (float)v.x, hi = (float)v.y;
+        xs[j - j0] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+      } else {
+        xs[j - j0] = x[j];
+      }
+    }
+    __syncthreads();
+    // accumulators (the plain kernels' order: columns in groups of eight,
+    // alternating accumulators, a tail of fewer than eight into acc0)
+    float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
+    DF re{0.f, 0.f}, im{0.f, 0.f};
+    float er = 0.f, ei = 0.f;
+    const long full8 = j0 + ((j1 - j0) / 8) * 8;
+    for(int s = 0; s < nst; ++s) {
+      const int slot = s % kTmaStages;
+      if(!fail && !wait_phase(&bar[slot], (parity >> slot) & 1u)) {
+        fail = 1;
+        if(t == 0)
+          atomicExch(err, 1);
+      }
+      parity ^= 1u << slot;
+      const float2 *sb = stage + (size_t)slot * kTmaStageCols * kTmaRows;
+      const long cb = j0 + (long)s * kTmaStageCols;
+      const int ccount = (int)min((long)kTmaStageCols, j1 - cb);
+      if(i < n && !fail) {
+        for(int c = 0; c < ccount; ++c) {
+          const float2 a = sb[c * kTmaRows + t];
+          const long j = cb + c;
+          if constexpr(kDF) {
+            const float4 v = xs[j - j0];
+            float p = __fmul_rn(a.x, v.x);
+            er += fmaf(a.x, v.x, -p);
+            df_add(re, p);
+            p = __fmul_rn(-a.y, v.y);
+            er += fmaf(-a.y, v.y, -p);
+            df_add(re, p);
+            er = fmaf(a.x, v.z, er);
+            er = fmaf(-a.y, v.w, er);
+            p = __fmul_rn(a.x, v.y);
+            ei += fmaf(a.x, v.y, -p);
+            df_add(im, p);
+            p = __fmul_rn(a.y, v.x);
+            ei += fmaf(a.y, v.x, -p);
+            df_add(im, p);
+            ei = fmaf(a.x, v.w, ei);
+            ei = fmaf(a.y, v.z, ei);
+          } else {
+            const float2 xv = xs[j - j0];
+            const bool alt = j < full8 && ((j - j0) & 1);
+            float2 acc = alt ? acc1 : acc0;
+            acc.x = fmaf(a.x, xv.x, acc.x);
+            acc.x = fmaf(-a.y, xv.y, acc.x);
+            acc.y = fmaf(a.x, xv.y, acc.y);
+            acc.y = fmaf(a.y, xv.x, acc.y);
+            if(alt)
+              acc1 = acc;
+            else
+              acc0 = acc;
+          }
+        }
+      }
+      __syncthreads();  // the buffer is free again
+      if(t == 0 && s + kTmaStages < nst && !fail) {
+        arm(&bar[slot], kStageBytes);
+        tma_load(stage + (size_t)slot * kTmaStageCols * kTmaRows, &tm, (int)(rt * kTmaRows),
+                 (int)(j0 + (long)(s + kTmaStages) * kTmaStageCols), &bar[slot]);
+      }
+    }
+    if(i < n && !fail) {
+      if constexpr(kDF) {
+        part[ct * n + i] = make_double2((double)re.hi + ((double)re.lo + (double)er),
+                                        (double)im.hi + ((double)im.lo + (double)ei));
+      } else {
+        acc0.x += acc1.x;
+        acc0.y += acc1.y;
+        part[ct * n + i] = acc0;
+      }
+    }
+  }
+}
+
+typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                             const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                             CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                             CUtensorMapFloatOOBfill);
+
+EncodeFn encode_fn() {
+  static EncodeFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+           cudaSuccess &&
+       q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeFn>(p);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+}  // namespace
+
+// Launches the TMA matvec (false when the tensor map cannot be made: the
+// caller then runs the plain kernel).
+bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const void *x, void *part, bool df,
+                       int row_tiles, long tiles, int cols, unsigned grid) {
+  EncodeFn enc = encode_fn();
+  if(!enc || (reinterpret_cast<uintptr_t>(S) & 15) || (n & 1))
+    return false;
+  alignas(64) CUtensorMap tm;
+  const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)n * sizeof(float2)};
+  const cuuint32_t box[2] = {kTmaRows, kTmaStageCols};
+  const cuuint32_t estr[2] = {1, 1};
+  if(enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<float2 *>(S), dims, strides, box, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  const size_t xbytes = (size_t)cols * (df ? sizeof(float4) : sizeof(float2));
+  const size_t smem = kTmaStages * kStageBytes + xbytes;
+  if(df) {
+    cudaFuncSetAttribute(k_matvec_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_matvec_tma<true><<<grid, kTmaRows, smem, ctx->stream>>>(
+        tm, n, (const double2 *)x, (double2 *)part, row_tiles, tiles, ctx->d_tile_counter, cols,
+        ctx->d_tma_err);
+  } else {
+    cudaFuncSetAttribute(k_matvec_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_matvec_tma<false><<<grid, kTmaRows, smem, ctx->stream>>>(
+        tm, n, (const float2 *)x, (float2 *)part, row_tiles, tiles, ctx->d_tile_counter, cols,
+        ctx->d_tma_err);
+  }
+  return true;
+}
+
+}  // namespace om

@@ -280,3 +280,25 @@ def test_near_field_high_nmax_and_poles(G, ctx, oracle, nmax):
         E, H = pr.near_field(outside)
         Eo, Ho = pr_o.near_field(xo, pr_o.internal(xo), outside)
         assert rel(E, Eo) < 1e-10 and rel(H, Ho) < 1e-10
+
+
+@pytest.mark.parametrize("N,nmax", [(7, 3), (12, 7)])
+def test_tma_matvec_bitwise_equal(G, ctx, N, nmax):
+    """The complex64 matvecs with TMA-staged tiles give the same bits as the
+    plain kernels (same per-thread arithmetic and order), through the whole
+    precision-form solve; the sizes leave partial row tiles and a column tail
+    that is not a multiple of the 16-column stage."""
+    rng = np.random.default_rng(N)
+    xyz, rad = random_cluster(rng, N, 1200 * nm, 40 * nm, 70 * nm, 20 * nm)
+    sp = G.spheres_array(xyz, rad, (2.2 + 0.05j) ** 2, nmax)
+    opts = G.options(G.SOLVE_FGMRES_MIXED, tol=1e-10, max_iter=30, restarts=4, inner_iter=40,
+                     inner_tol=1e-4)
+    out = []
+    for tma in (1, 0):
+        ctx.tune(matvec_tma=tma)
+        xs, X, _, st = G.wavelength_solve(ctx, sp, G.medium(1.0), G.plane_wave(600 * nm), opts, G.C64,
+                                          want_coeffs=True)
+        out.append((xs, X, st.iterations, st.inner_iterations))
+    ctx.tune(matvec_tma=1)
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2:] == out[1][2:]
