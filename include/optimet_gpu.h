@@ -128,7 +128,8 @@ typedef struct {
   int assemble_carveout;
   int matvec_carveout;
   int lu_tensor_cores;   /* complex64 LU trailing updates on the tensor cores: 1 (default) / 0 */
-  int matvec_tma;        /* complex64 x complex64 matvec with TMA-staged matrix tiles: 1 (default) / 0 */
+  int matvec_tma;        /* complex64 x complex64 matvec with TMA-staged matrix tiles: 1 (default for
+                            a context) / 0 (default for the slots of a server with several slots) */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, k <= 32,

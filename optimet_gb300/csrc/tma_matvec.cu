@@ -11,7 +11,10 @@
 // issues the copies; after all threads have consumed a buffer it refills it
 // with the stage four ahead. Waits are bounded (error flag, no hang). The
 // arithmetic and its order per thread are those of the plain kernels, so
-// the results are bitwise the same.
+// the results are bitwise the same. The solver dispatches the complex64 x
+// complex64 variant; the compensated variant (kDF) measured slower than the
+// register-prefetching plain kernel (its FP32 work needs more resident warps
+// than the 144 KB of buffers leave) and is kept for the tuning experiments.
 #include <cuda.h>
 
 #include <mutex>
