@@ -332,6 +332,28 @@ long om_server_launches(om_server *srv);
 const char *om_server_last_error(om_server *srv);
 void om_server_destroy(om_server *srv);
 
+/* Batched wavelength solves (the batching form): runs `count` requests on the
+ * context's stream and fills results[i] for reqs[i] (status, cross sections,
+ * solve statistics; slot = the request's slot in its batch; queue_ms = call
+ * start -> start of its batch; service_ms = its batch's time; latency_ms =
+ * call start -> its results). Requests are grouped into size classes (same
+ * precision, nMax and options; N padded up to 1, 2, 3, 4, 6, 8, 12, 16, ...)
+ * and solved in batches whose device memory stays within `arena_bytes`
+ * (0 = 40 % of the free device memory, at most 64 GiB). Per batch one
+ * assembly launch builds the FF and SH matrices of all its requests, and the
+ * systems are solved together by restarted GMRES whose steps are captured
+ * CUDA graphs (one set per size class). Supported: OM_C128 with
+ * OM_SOLVE_GMRES (restarts cycles of at most max_iter steps) and OM_C64 with
+ * OM_SOLVE_FGMRES_MIXED, run as GMRES-based iterative refinement: at most
+ * min(max_iter, 32) x restarts refinement steps, each with an FP64-accurate
+ * residual and an FP32 GMRES of at most inner_iter steps that reduces it by
+ * inner_tol. Other requests get OM_ERR_INVALID. A request's results do not
+ * depend on the batch it runs in. cluster_key is not used.
+ * Returns OM_OK unless a device error stopped the call; per-request failures
+ * (overlap, not converged, budget) are in results[i].status. */
+int om_batch_solve(om_context *ctx, const om_request *reqs, int count, size_t arena_bytes,
+                   om_result *results);
+
 #ifdef __cplusplus
 }
 #endif

@@ -152,6 +152,7 @@ def lib():
         L.om_server_last_error.argtypes = [vp]
         L.om_server_last_error.restype = C.c_char_p
         L.om_server_destroy.argtypes = [vp]
+        L.om_batch_solve.argtypes = [vp, C.POINTER(Request), C.c_int, C.c_size_t, C.POINTER(Result)]
         _lib = L
     return _lib
 
@@ -434,6 +435,33 @@ def wavelength_solve_sh(ctx: Context, spheres, bg, wave, opts=None, precision=C1
     return xsec, xsh, st
 
 
+def _result_dict(r: Result) -> dict:
+    st = lambda s: {"iterations": s.iterations, "inner_iterations": s.inner_iterations,
+                    "rel_residual": s.rel_residual, "seconds": s.seconds}
+    return {"status": r.status, "slot": r.slot, "xsec": np.array(r.xsec[:]),
+            "xsec_sh": np.array(r.xsec_sh[:]), "ff": st(r.ff), "sh": st(r.sh),
+            "queue_ms": r.queue_ms, "service_ms": r.service_ms, "latency_ms": r.latency_ms,
+            "device_bytes": r.device_bytes}
+
+
+def batch_solve(ctx: Context, requests, arena_bytes: int = 0):
+    """Batched wavelength solves (om_batch_solve). `requests`: a list of
+    (spheres, background, wave, opts, precision) tuples (a sixth element, the
+    cluster key, is accepted and ignored). Returns one result dict per request,
+    as Server.poll."""
+    n = len(requests)
+    rq = (Request * max(n, 1))()
+    keep = []
+    for i, r in enumerate(requests):
+        sp, bg, wave, opts, prec = r[:5]
+        keep.append(sp)
+        rq[i] = Request(C.cast(sp, C.POINTER(Sphere)), len(sp), prec, bg or medium(), wave,
+                        opts or options(), 0)
+    out = (Result * max(n, 1))()
+    ctx.check(lib().om_batch_solve(ctx.h, rq, n, arena_bytes, out))
+    return [_result_dict(out[i]) for i in range(n)]
+
+
 class Server:
     """Serving / batching runtime (om_server_*): `slots` contexts on one GPU
     taking wavelength-solve requests in arrival order, admitted against an HBM
@@ -472,12 +500,7 @@ class Server:
             return None
         if rc:
             raise OptimetError(rc, "unknown ticket %d" % ticket)
-        st = lambda s: {"iterations": s.iterations, "inner_iterations": s.inner_iterations,
-                        "rel_residual": s.rel_residual, "seconds": s.seconds}
-        return {"status": r.status, "slot": r.slot, "xsec": np.array(r.xsec[:]),
-                "xsec_sh": np.array(r.xsec_sh[:]), "ff": st(r.ff), "sh": st(r.sh),
-                "queue_ms": r.queue_ms, "service_ms": r.service_ms, "latency_ms": r.latency_ms,
-                "device_bytes": r.device_bytes}
+        return _result_dict(r)
 
     def drain(self):
         lib().om_server_drain(self.h)

@@ -1,0 +1,1161 @@
+// Batched wavelength solves: the batching form (om_batch_solve).
+//
+// Many requests (clusters and wavelengths of uneven N and nMax, fundamental
+// with optional second harmonic) are grouped into size classes: the same
+// precision form, nMax and solve options, and N padded up to a class size
+// (1, 2, 3, 4, 6, 8, 12, ... : steps of at most 1.5x). A class runs its
+// requests in batches of up to B slots, where B follows from the device memory
+// a slot needs. Per batch:
+//
+//  * the per-sphere state of every request (T-matrix factors, incident
+//    coefficients, source vector) is set up with the kernels of the
+//    single-request path;
+//  * ONE launch of the translation/assembly kernel builds the FF and the SH
+//    matrices of all requests of the batch (one CTA per sphere pair per
+//    matrix, `k_assemble` in batch mode);
+//  * the FF systems, then the SH systems, are solved together by restarted
+//    GMRES in lockstep: every slot runs the same Arnoldi step at the same
+//    time, a slot that has converged is masked (its kernels return at once),
+//    one matvec launch serves all slots (split-K tiles of every slot's
+//    matrix taken from one counter), and the Hessenberg/Givens updates run on
+//    the device, so that the whole iteration reads its step index and its
+//    flags from device memory;
+//  * those iterations are captured once per size class as three CUDA graphs
+//    (start of a cycle: residual, its norm, convergence test; a segment of
+//    kSegSteps Arnoldi steps; end of a cycle: back substitution and update)
+//    and replayed; the host reads two counters after each segment.
+//
+// Forms: the plain form (OM_C128 with OM_SOLVE_GMRES) is restarted GMRES on
+// the complex128 matrices; the precision form (OM_C64 with
+// OM_SOLVE_FGMRES_MIXED) is GMRES-based iterative refinement (Carson & Higham
+// 2018): each cycle takes the residual of the complex64 system in FP64-accurate
+// arithmetic (compensated products), runs FP32 Arnoldi on the complex64 matrix
+// until the residual estimate falls by inner_tol, and adds the FP64 correction.
+//
+// A slot's arithmetic does not depend on the other slots, on its position or
+// on the class it runs in (fixed split-K chunks and dot-product blocks, fixed
+// reduction orders), so a request's results are bitwise the same alone and in
+// any batch.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <map>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <vector>
+
+#include "om_internal.h"
+#include "om_krylov.cuh"
+
+namespace om {
+
+namespace {
+
+constexpr int kBT = 256;         // threads of the vector kernels; rows per matvec tile
+constexpr int kBCols = 1024;     // columns per split-K chunk
+constexpr int kBDotRows = 2048;  // rows per block of the dot products
+constexpr int kSegSteps = 8;     // Arnoldi steps per captured segment
+constexpr int kMaxSlots = 256;   // slots per batch (one thread per slot in the control kernels)
+
+// Per-slot solver state (device).
+struct Slot {
+  long n;          // unknowns; 0 = empty slot
+  const void *S;   // matrix, column-major, ld = n
+  double bnorm;    // ||b||; negative until the first cycle
+  double rho;      // ||b - S x|| at the start of the latest cycle
+  double thr;      // this cycle's stop threshold on |g_{j+1}|
+  int outer;       // still needs cycles
+  int inner;       // Arnoldi of this cycle running
+  int k;           // Arnoldi steps of this cycle
+  int xzero;       // x = 0 (the residual is b)
+  int steps;       // Arnoldi steps, all cycles
+  int cycles;      // cycles run
+  int status;      // OM_OK or OM_ERR_NOT_CONVERGED once outer = 0
+  int pad;
+};
+
+// Batch control (device).
+struct Ctl {
+  int j;        // Arnoldi step of the slots (the new basis vector is column j + 1)
+  int n_inner;  // slots whose Arnoldi runs
+  int n_outer;  // slots that still need cycles
+  int ntiles;   // matvec tiles of the current system
+};
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  // Smith's algorithm
+  if(fabs(b.x) >= fabs(b.y)) {
+    const double r = b.y / b.x, d = b.x + b.y * r;
+    return make_double2((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  }
+  const double r = b.x / b.y, d = b.x * r + b.y;
+  return make_double2((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+__device__ __forceinline__ double cabs2(double2 a) { return hypot(a.x, a.y); }
+
+// Givens rotation of det_approx (PreconditionedMatrix.cpp:1102-1118), as the
+// host solver uses it
+__device__ void givens_dev(double2 h1, double2 h2, double2 &c, double2 &s) {
+  const double a1 = cabs2(h1), a2 = cabs2(h2);
+  if(a1 == 0.0 && a2 == 0.0) {
+    c = make_double2(1.0, 0.0);
+    s = make_double2(0.0, 0.0);
+    return;
+  }
+  if(a2 > a1) {
+    const double2 t = cdiv(h1, h2);
+    const double at = cabs2(t);
+    s = make_double2(1.0 / sqrt(1.0 + at * at), 0.0);
+    c = cneg(cmul(t, s));
+  } else {
+    const double2 t = cdiv(h2, h1);
+    const double at = cabs2(t);
+    c = make_double2(1.0 / sqrt(1.0 + at * at), 0.0);
+    s = cneg(cmul(t, c));
+  }
+}
+
+template <typename V> __device__ __forceinline__ double2 to_d2(V v) { return make_double2(v.x, v.y); }
+
+// ---------------------------------------------------------------------------
+// Matrix-vector products over all slots. A tile is (slot, 256 rows, 1024
+// columns); the capped grid takes tiles from a counter (zeroed before the
+// launch). part[(s nsm + chunk) np + i] holds a chunk's partial sum.
+// ---------------------------------------------------------------------------
+
+// Arnoldi product: S_s times basis column j of slot s (slots with inner set)
+template <typename M, typename V>
+__global__ void __launch_bounds__(kBT) k_b_mv(const Slot *st, const int4 *tiles, const Ctl *ctl,
+                                             const V *Vb, long vslot, long np, int nsm, V *part,
+                                             unsigned long long *next) {
+  __shared__ V xs[kBCols];
+  __shared__ int tile;
+  const int ntiles = ctl->ntiles;
+  const int jcol = ctl->j;
+  for(;;) {
+    __syncthreads();
+    if(threadIdx.x == 0)
+      tile = (int)atomicAdd(next, 1ull);
+    __syncthreads();
+    const int t = tile;
+    if(t >= ntiles)
+      break;
+    const int4 d = tiles[t];
+    if(!st[d.x].inner)
+      continue;
+    const long n = st[d.x].n;
+    const M *S = (const M *)st[d.x].S;
+    const V *x = Vb + d.x * vslot + (long)jcol * np;
+    const long i = (long)d.y * kBT + threadIdx.x;
+    const long j0 = (long)d.z * kBCols, j1 = min(n, j0 + kBCols);
+    for(long j = j0 + threadIdx.x; j < j1; j += kBT)
+      xs[j - j0] = x[j];
+    __syncthreads();
+    if(i < n)
+      part[((long)d.x * nsm + d.z) * np + i] = mv_row<M, V>(S + j0 * n + i, n, xs, (int)(j1 - j0));
+  }
+}
+
+// Residual product: S_s x_s with x in FP64 (slots with outer set and x != 0);
+// a complex64 matrix takes the compensated FP64-accurate sums
+template <typename M>
+__global__ void __launch_bounds__(kBT) k_b_resid(const Slot *st, const int4 *tiles, const Ctl *ctl,
+                                                const double2 *x, long np, int nsm, double2 *part,
+                                                unsigned long long *next) {
+  constexpr bool kDF = std::is_same<M, float2>::value;
+  typedef typename std::conditional<kDF, float4, double2>::type XS;
+  __shared__ XS xs[kBCols];
+  __shared__ int tile;
+  const int ntiles = ctl->ntiles;
+  for(;;) {
+    __syncthreads();
+    if(threadIdx.x == 0)
+      tile = (int)atomicAdd(next, 1ull);
+    __syncthreads();
+    const int t = tile;
+    if(t >= ntiles)
+      break;
+    const int4 d = tiles[t];
+    if(!st[d.x].outer || st[d.x].xzero)
+      continue;
+    const long n = st[d.x].n;
+    const M *S = (const M *)st[d.x].S;
+    const double2 *xv = x + d.x * np;
+    const long i = (long)d.y * kBT + threadIdx.x;
+    const long j0 = (long)d.z * kBCols, j1 = min(n, j0 + kBCols);
+    for(long j = j0 + threadIdx.x; j < j1; j += kBT) {
+      if constexpr(kDF)
+        xs[j - j0] = df_split(xv[j]);
+      else
+        xs[j - j0] = xv[j];
+    }
+    __syncthreads();
+    if(i >= n)
+      continue;
+    double2 v;
+    if constexpr(kDF)
+      v = mv_row_df(S + j0 * n + i, n, xs, (int)(j1 - j0));
+    else
+      v = mv_row<double2, double2>(S + j0 * n + i, n, xs, (int)(j1 - j0));
+    part[((long)d.x * nsm + d.z) * np + i] = v;
+  }
+}
+
+// basis column j + 1 = sum of the chunks' partials (fixed order)
+template <typename V>
+__global__ void k_b_reduce_w(const Slot *st, const Ctl *ctl, const V *part, long np, int nsm, V *Vb,
+                             long vslot) {
+  const int s = blockIdx.y;
+  if(!st[s].inner)
+    return;
+  const long n = st[s].n, i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  const int ns = (int)((n + kBCols - 1) / kBCols);
+  const V *p = part + (long)s * nsm * np + i;
+  V acc = p[0];
+  for(int c = 1; c < ns; ++c) {
+    const V v = p[(long)c * np];
+    acc.x += v.x;
+    acc.y += v.y;
+  }
+  Vb[s * vslot + (long)(ctl->j + 1) * np + i] = acc;
+}
+
+// r = b - S x (r = b while x = 0)
+__global__ void k_b_reduce_r(const Slot *st, const double2 *part, long np, int nsm, const double2 *b,
+                             double2 *r) {
+  const int s = blockIdx.y;
+  if(!st[s].outer)
+    return;
+  const long n = st[s].n, i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  const double2 bv = b[s * np + i];
+  if(st[s].xzero) {
+    r[s * np + i] = bv;
+    return;
+  }
+  const int ns = (int)((n + kBCols - 1) / kBCols);
+  const double2 *p = part + (long)s * nsm * np + i;
+  double2 acc = p[0];
+  for(int c = 1; c < ns; ++c) {
+    const double2 v = p[(long)c * np];
+    acc.x += v.x;
+    acc.y += v.y;
+  }
+  r[s * np + i] = make_double2(bv.x - acc.x, bv.y - acc.y);
+}
+
+// Block partial sums over rows [blockIdx.x kBDotRows, ...) of slot blockIdx.y:
+// norm = 0: conj(v_t) . w for t = 0 .. j, w = column j + 1 (Arnoldi slots);
+// norm = 1: |w|^2 with w = column j + 1 (use_j) or column 0 (residual, outer slots).
+// dpart[((s nblk) + block) m2 + t]
+template <typename V>
+__global__ void __launch_bounds__(kBT) k_b_dot(const Slot *st, const Ctl *ctl, const V *base,
+                                              long vslot, long np, int use_j, int norm, int outer,
+                                              int nblk, int m2, V *dpart) {
+  __shared__ V red[kBT];
+  const int s = blockIdx.y;
+  if(!(outer ? st[s].outer : st[s].inner))
+    return;
+  const long n = st[s].n;
+  const long r0 = (long)blockIdx.x * kBDotRows;
+  if(r0 >= n)
+    return;
+  const long r1 = min(n, r0 + kBDotRows);
+  const int j = use_j ? ctl->j : -1;
+  const V *vs = base + s * vslot;
+  const V *w = vs + (long)(j + 1) * np;
+  const int cnt = norm ? 1 : j + 1;
+  V *out = dpart + ((long)s * nblk + blockIdx.x) * m2;
+  for(int t = 0; t < cnt; ++t) {
+    V acc;
+    acc.x = acc.y = 0;
+    if(!norm) {
+      const V *v = vs + (long)t * np;
+      for(long i = r0 + threadIdx.x; i < r1; i += kBT)
+        acc = cfma_conj(v[i], w[i], acc);
+    } else {
+      for(long i = r0 + threadIdx.x; i < r1; i += kBT) {
+        const V a = w[i];
+        acc.x = fma(a.x, a.x, acc.x);
+        acc.x = fma(a.y, a.y, acc.x);
+      }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for(int h = kBT / 2; h > 0; h >>= 1) {
+      if(threadIdx.x < h) {
+        red[threadIdx.x].x += red[threadIdx.x + h].x;
+        red[threadIdx.x].y += red[threadIdx.x + h].y;
+      }
+      __syncthreads();
+    }
+    if(threadIdx.x == 0)
+      out[t] = red[0];
+    __syncthreads();
+  }
+}
+
+// h_t = sum over blocks (fixed order) for t = 0 .. j; hacc = h (pass 0) or hacc + h (pass 1)
+template <typename V>
+__global__ void k_b_hsum(const Slot *st, const Ctl *ctl, const V *dpart, int nblk, int m2, V *hs,
+                         double2 *hacc, int pass) {
+  const int s = blockIdx.x;
+  if(!st[s].inner)
+    return;
+  const int k = ctl->j + 1;
+  const int nb = (int)((st[s].n + kBDotRows - 1) / kBDotRows);
+  for(int t = threadIdx.x; t < k; t += blockDim.x) {
+    const V *p = dpart + (long)s * nblk * m2 + t;
+    V acc = p[0];
+    for(int b = 1; b < nb; ++b) {
+      acc.x += p[(long)b * m2].x;
+      acc.y += p[(long)b * m2].y;
+    }
+    hs[s * m2 + t] = acc;
+    const double2 a = to_d2(acc);
+    hacc[s * m2 + t] = pass ? cadd(hacc[s * m2 + t], a) : a;
+  }
+}
+
+// w -= V[:, 0..j] h (w = column j + 1)
+template <typename V>
+__global__ void k_b_sub(const Slot *st, const Ctl *ctl, const V *hs, int m2, V *Vb, long vslot, long np) {
+  const int s = blockIdx.y;
+  if(!st[s].inner)
+    return;
+  const long n = st[s].n, i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  const int k = ctl->j + 1;
+  V *vs = Vb + s * vslot;
+  V acc = vs[(long)k * np + i];
+  for(int t = 0; t < k; ++t) {
+    V c = hs[s * m2 + t];
+    c.x = -c.x;
+    c.y = -c.y;
+    acc = cfma(vs[(long)t * np + i], c, acc);
+  }
+  vs[(long)k * np + i] = acc;
+}
+
+// Hessenberg column j of every Arnoldi slot: previous rotations, the new
+// rotation, the residual estimate |g_{j+1}| and the stop test; one thread
+// per slot. Then the step index advances (if any slot ran).
+template <typename V>
+__global__ void k_b_givens(Slot *st, Ctl *ctl, const V *dpart, int nblk, int m2, const double2 *hacc,
+                           double2 *Hm, double2 *cs, double2 *sn, double2 *g, double *inv, int m,
+                           int B) {
+  const int s = threadIdx.x;
+  const int j = ctl->j;
+  const int act = s < B ? st[s].inner : 0;
+  const int any = __syncthreads_count(act);
+  int still = 0;
+  if(act) {
+    Slot &sl = st[s];
+    const int nb = (int)((sl.n + kBDotRows - 1) / kBDotRows);
+    const V *p = dpart + (long)s * nblk * m2;
+    V acc = p[0];
+    for(int b = 1; b < nb; ++b) {
+      acc.x += p[(long)b * m2].x;
+      acc.y += p[(long)b * m2].y;
+    }
+    const double hn = sqrt((double)acc.x);
+    double2 *col = Hm + ((long)s * m + j) * (m + 1);
+    for(int t = 0; t <= j; ++t)
+      col[t] = hacc[s * m2 + t];
+    double2 *c_s = cs + (long)s * m, *s_s = sn + (long)s * m;
+    for(int i = 0; i < j; ++i) {
+      const double2 a = col[i], bb = col[i + 1];
+      col[i] = cadd(cmul(cconj(c_s[i]), a), cmul(cconj(cneg(s_s[i])), bb));
+      col[i + 1] = cadd(cmul(s_s[i], a), cmul(c_s[i], bb));
+    }
+    double2 c, sr;
+    const double2 hk1 = make_double2(hn, 0.0);
+    givens_dev(col[j], hk1, c, sr);
+    c_s[j] = c;
+    s_s[j] = sr;
+    const double2 hk = col[j];
+    col[j] = cadd(cmul(cconj(c), hk), cmul(cconj(cneg(sr)), hk1));
+    double2 *gs = g + (long)s * (m + 1);
+    const double2 g0 = gs[j];
+    gs[j] = cmul(cconj(c), g0);
+    gs[j + 1] = cmul(sr, g0);
+    inv[s] = hn > 0.0 ? 1.0 / hn : 0.0;
+    sl.k = j + 1;
+    sl.steps++;
+    still = !(cabs2(gs[j + 1]) <= sl.thr || hn == 0.0 || j + 1 >= m);
+    sl.inner = still;
+  }
+  const int n_in = __syncthreads_count(still);
+  if(threadIdx.x == 0 && any) {
+    ctl->j = j + 1;
+    ctl->n_inner = n_in;
+  }
+}
+
+// v_{j+1} = w / h_{j+1,j} (the step index has advanced: w = column j)
+template <typename V>
+__global__ void k_b_scale(const Slot *st, const Ctl *ctl, const double *inv, V *Vb, long vslot, long np) {
+  const int s = blockIdx.y;
+  if(!st[s].inner)
+    return;
+  const long n = st[s].n, i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  V *w = Vb + s * vslot + (long)ctl->j * np;
+  const double f = inv[s];
+  w[i].x = w[i].x * f;
+  w[i].y = w[i].y * f;
+}
+
+// Start of a cycle: rho = ||r||, the convergence test, g_0 = rho.
+__global__ void k_b_start(Slot *st, Ctl *ctl, const double2 *dpart, int nblk, int m2, double2 *g,
+                          int m, int B, double tol, double inner_rel, int max_cycles) {
+  const int s = threadIdx.x;
+  int out = 0, in = 0;
+  if(s < B) {
+    Slot &sl = st[s];
+    sl.k = 0;
+    sl.inner = 0;
+    if(sl.outer) {
+      const int nb = (int)((sl.n + kBDotRows - 1) / kBDotRows);
+      const double2 *p = dpart + (long)s * nblk * m2;
+      double acc = p[0].x;
+      for(int b = 1; b < nb; ++b)
+        acc += p[(long)b * m2].x;
+      const double rho = sqrt(acc);
+      if(sl.bnorm < 0.0)
+        sl.bnorm = rho;
+      sl.rho = rho;
+      if(sl.bnorm == 0.0 || rho <= tol * sl.bnorm) {
+        sl.outer = 0;
+        sl.status = OM_OK;
+      } else if(sl.cycles >= max_cycles) {
+        sl.outer = 0;
+        sl.status = OM_ERR_NOT_CONVERGED;
+      } else {
+        sl.inner = 1;
+        sl.thr = fmax(inner_rel * rho, tol * sl.bnorm);
+        g[(long)s * (m + 1)] = make_double2(rho, 0.0);
+      }
+      out = sl.outer;
+      in = sl.inner;
+    }
+  }
+  const int n_out = __syncthreads_count(out);
+  const int n_in = __syncthreads_count(in);
+  if(threadIdx.x == 0) {
+    ctl->j = 0;
+    ctl->n_outer = n_out;
+    ctl->n_inner = n_in;
+  }
+}
+
+// v_0 = r / rho
+template <typename V>
+__global__ void k_b_v0(const Slot *st, const double2 *r, long np, V *Vb, long vslot) {
+  const int s = blockIdx.y;
+  if(!st[s].inner)
+    return;
+  const long n = st[s].n, i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  const double f = 1.0 / st[s].rho;
+  const double2 v = r[s * np + i];
+  V o;
+  o.x = v.x * f;
+  o.y = v.y * f;
+  Vb[s * vslot + i] = o;
+}
+
+// End of a cycle: y = R^{-1} g over the slot's k steps (one thread per slot).
+__global__ void k_b_end(Slot *st, const double2 *Hm, const double2 *g, double2 *y, int m, int B) {
+  const int s = threadIdx.x;
+  if(s >= B)
+    return;
+  Slot &sl = st[s];
+  const int k = sl.k;
+  if(k == 0)
+    return;
+  const double2 *H = Hm + (long)s * m * (m + 1);
+  const double2 *gs = g + (long)s * (m + 1);
+  double2 *ys = y + (long)s * m;
+  for(int j = k - 1; j >= 0; --j) {
+    double2 v = gs[j];
+    for(int q = j + 1; q < k; ++q)
+      v = cadd(v, cneg(cmul(H[(long)q * (m + 1) + j], ys[q])));
+    ys[j] = cdiv(v, H[(long)j * (m + 1) + j]);
+  }
+  sl.cycles++;
+  sl.xzero = 0;
+}
+
+// x += sum_t y_t v_t (FP64)
+template <typename V>
+__global__ void k_b_update(const Slot *st, const V *Vb, long vslot, long np, const double2 *y, int m,
+                           double2 *x) {
+  const int s = blockIdx.y;
+  const int k = st[s].k;
+  if(k == 0)
+    return;
+  const long n = st[s].n, i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i >= n)
+    return;
+  const V *vs = Vb + s * vslot;
+  double2 acc = x[s * np + i];
+  for(int t = 0; t < k; ++t)
+    acc = cfma(to_d2(vs[(long)t * np + i]), y[(long)s * m + t], acc);
+  x[s * np + i] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// Size classes
+// ---------------------------------------------------------------------------
+
+// N padded to the class size: 1, 2, 3, 4, 6, 8, 12, 16, 24, ... (x1.5 / x1.33 steps)
+int pad_spheres(int N) {
+  int a = 1;
+  while(a < N) {
+    const int b = a < 2 ? 2 : (a & (a - 1)) == 0 ? a + a / 2 : a / 3 * 4;
+    a = b;
+  }
+  return a;
+}
+
+struct ClassKey {
+  int precision, nmax, Npad, m, max_cycles;
+  double tol, inner_rel;
+  bool operator<(const ClassKey &o) const {
+    return std::tie(precision, nmax, Npad, m, max_cycles, tol, inner_rel) <
+           std::tie(o.precision, o.nmax, o.Npad, o.m, o.max_cycles, o.tol, o.inner_rel);
+  }
+};
+
+inline size_t rup(size_t v) { return ((v + 255) / 256) * 256; }
+
+// Device and pinned host buffers of one size class, and its graphs.
+template <typename M, typename V> struct Class {
+  om_context *ctx = nullptr;
+  ClassKey key{};
+  int B = 0, m = 0, m2 = 0, nsm = 0, nblk = 0, max_tiles = 0;
+  long np = 0, vslot = 0;
+  unsigned mv_grid = 1;
+  void *buf = nullptr;
+  size_t bytes = 0;
+  Slot *st = nullptr;
+  Ctl *ctl = nullptr;
+  int4 *tiles = nullptr;
+  BatchMat *mats = nullptr;
+  M *Sff = nullptr, *Ssh = nullptr;
+  double2 *b = nullptr, *x = nullptr, *r = nullptr, *part = nullptr;
+  V *Vb = nullptr, *hs = nullptr;
+  void *dpart = nullptr;
+  double2 *hacc = nullptr, *Hm = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr;
+  double *inv = nullptr;
+  unsigned long long *counter = nullptr;
+  // pinned host mirrors
+  Slot *h_st = nullptr;
+  Ctl *h_ctl = nullptr;
+  int4 *h_tiles = nullptr;
+  BatchMat *h_mats = nullptr;
+  double *h_xsec = nullptr;  // 8 per slot: the FF and SH cross sections
+  cudaEvent_t ev_main = nullptr;        // main stream -> auxiliary streams
+  std::vector<cudaEvent_t> ev_aux;      // auxiliary streams -> main stream
+  cudaGraphExec_t g_start = nullptr, g_seg = nullptr, g_end = nullptr;
+  int k_start = 0, k_seg = 0, k_end = 0;  // kernels per replay
+
+  static size_t slot_bytes(long np, int m) {
+    const int m2 = m + 2;
+    const long nsm = (np + kBCols - 1) / kBCols, nblk = (np + kBDotRows - 1) / kBDotRows;
+    return 2 * rup(sizeof(M) * (size_t)np * np) + 3 * sizeof(double2) * np +
+           sizeof(V) * (size_t)(m + 1) * np + sizeof(double2) * (size_t)nsm * np +
+           sizeof(double2) * (size_t)nblk * m2 + sizeof(V) * m2 +
+           sizeof(double2) * ((size_t)m2 + (size_t)m * (m + 1) + 2 * (size_t)m + (m + 1) + m) +
+           sizeof(int4) * (size_t)((np + kBT - 1) / kBT) * nsm + sizeof(Slot) + 2 * sizeof(BatchMat) + 64;
+  }
+
+  int init(om_context *c, const ClassKey &k, int slots) {
+    ctx = c;
+    key = k;
+    B = slots;
+    m = k.m;
+    m2 = m + 2;
+    np = (long)rup((size_t)2 * pmax(k.nmax) * k.Npad);
+    vslot = (long)(m + 1) * np;
+    nsm = (int)((np + kBCols - 1) / kBCols);
+    nblk = (int)((np + kBDotRows - 1) / kBDotRows);
+    max_tiles = B * (int)((np + kBT - 1) / kBT) * nsm;
+    mv_grid = (unsigned)std::max(1L, std::min((long)max_tiles, (long)ctx->sm_count * 8));
+    const size_t Bz = (size_t)B;
+    size_t sz[] = {Bz * sizeof(Slot), sizeof(Ctl), sizeof(int4) * (size_t)max_tiles,
+                   2 * Bz * sizeof(BatchMat), Bz * sizeof(M) * np * np, Bz * sizeof(M) * np * np,
+                   Bz * sizeof(double2) * np, Bz * sizeof(double2) * np, Bz * sizeof(double2) * np,
+                   Bz * sizeof(double2) * nsm * np, Bz * sizeof(V) * vslot, Bz * sizeof(V) * m2,
+                   Bz * sizeof(double2) * nblk * m2, Bz * sizeof(double2) * m2,
+                   Bz * sizeof(double2) * m * (m + 1), Bz * sizeof(double2) * m,
+                   Bz * sizeof(double2) * m, Bz * sizeof(double2) * (m + 1), Bz * sizeof(double2) * m,
+                   Bz * sizeof(double), sizeof(unsigned long long)};
+    bytes = 0;
+    for(size_t v : sz)
+      bytes += rup(v);
+    int rc = dev_malloc(ctx, &buf, bytes);
+    if(rc)
+      return rc;
+    char *p = (char *)buf;
+    auto take = [&](size_t v) {
+      void *q = p;
+      p += rup(v);
+      return q;
+    };
+    int i = 0;
+    st = (Slot *)take(sz[i++]);
+    ctl = (Ctl *)take(sz[i++]);
+    tiles = (int4 *)take(sz[i++]);
+    mats = (BatchMat *)take(sz[i++]);
+    Sff = (M *)take(sz[i++]);
+    Ssh = (M *)take(sz[i++]);
+    b = (double2 *)take(sz[i++]);
+    x = (double2 *)take(sz[i++]);
+    r = (double2 *)take(sz[i++]);
+    part = (double2 *)take(sz[i++]);
+    Vb = (V *)take(sz[i++]);
+    hs = (V *)take(sz[i++]);
+    dpart = take(sz[i++]);
+    hacc = (double2 *)take(sz[i++]);
+    Hm = (double2 *)take(sz[i++]);
+    cs = (double2 *)take(sz[i++]);
+    sn = (double2 *)take(sz[i++]);
+    g = (double2 *)take(sz[i++]);
+    y = (double2 *)take(sz[i++]);
+    inv = (double *)take(sz[i++]);
+    counter = (unsigned long long *)take(sz[i++]);
+    if(cudaMallocHost(&h_st, Bz * sizeof(Slot)) != cudaSuccess ||
+       cudaMallocHost(&h_ctl, sizeof(Ctl)) != cudaSuccess ||
+       cudaMallocHost(&h_tiles, sizeof(int4) * (size_t)max_tiles) != cudaSuccess ||
+       cudaMallocHost(&h_mats, 2 * Bz * sizeof(BatchMat)) != cudaSuccess ||
+       cudaMallocHost(&h_xsec, 8 * Bz * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->err = "pinned host staging for the batch";
+      return OM_ERR_CUDA;
+    }
+    cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming);
+    ev_aux.resize(ctx->aux.size());
+    for(auto &e : ev_aux)
+      cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    return capture();
+  }
+
+  ~Class() {
+    if(g_start) cudaGraphExecDestroy(g_start);
+    if(g_seg) cudaGraphExecDestroy(g_seg);
+    if(g_end) cudaGraphExecDestroy(g_end);
+    if(buf) {
+      cudaStreamSynchronize(ctx->stream);
+      dev_release(ctx, buf, bytes);
+    }
+    if(h_st) cudaFreeHost(h_st);
+    if(h_ctl) cudaFreeHost(h_ctl);
+    if(h_tiles) cudaFreeHost(h_tiles);
+    if(h_mats) cudaFreeHost(h_mats);
+    if(h_xsec) cudaFreeHost(h_xsec);
+    if(ev_main) cudaEventDestroy(ev_main);
+    for(auto &e : ev_aux)
+      if(e) cudaEventDestroy(e);
+  }
+
+  dim3 vgrid() const { return dim3((unsigned)((np + kBT - 1) / kBT), (unsigned)B); }
+  int ctl_threads() const { return ((B + 31) / 32) * 32; }
+
+  // cycle start: r = b - S x, ||r||, the test, v_0
+  int enqueue_start(cudaStream_t s) {
+    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+    k_b_resid<M><<<mv_grid, kBT, 0, s>>>(st, tiles, ctl, x, np, nsm, part, counter);
+    k_b_reduce_r<<<vgrid(), kBT, 0, s>>>(st, part, np, nsm, b, r);
+    k_b_dot<double2><<<dim3(nblk, B), kBT, 0, s>>>(st, ctl, r, np, np, 0, 1, 1, nblk, m2,
+                                                   (double2 *)dpart);
+    k_b_start<<<1, ctl_threads(), 0, s>>>(st, ctl, (const double2 *)dpart, nblk, m2, g, m, B,
+                                          key.tol, key.inner_rel, key.max_cycles);
+    k_b_v0<V><<<vgrid(), kBT, 0, s>>>(st, r, np, Vb, vslot);
+    return 5;
+  }
+  // one Arnoldi step with CGS2 (two projection passes), the rotation, the scaling
+  int enqueue_step(cudaStream_t s) {
+    V *dp = (V *)dpart;
+    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+    k_b_mv<M, V><<<mv_grid, kBT, 0, s>>>(st, tiles, ctl, Vb, vslot, np, nsm, (V *)part, counter);
+    k_b_reduce_w<V><<<vgrid(), kBT, 0, s>>>(st, ctl, (const V *)part, np, nsm, Vb, vslot);
+    for(int pass = 0; pass < 2; ++pass) {
+      k_b_dot<V><<<dim3(nblk, B), kBT, 0, s>>>(st, ctl, Vb, vslot, np, 1, 0, 0, nblk, m2, dp);
+      k_b_hsum<V><<<B, 64, 0, s>>>(st, ctl, dp, nblk, m2, hs, hacc, pass);
+      k_b_sub<V><<<vgrid(), kBT, 0, s>>>(st, ctl, hs, m2, Vb, vslot, np);
+    }
+    k_b_dot<V><<<dim3(nblk, B), kBT, 0, s>>>(st, ctl, Vb, vslot, np, 1, 1, 0, nblk, m2, dp);
+    k_b_givens<V><<<1, ctl_threads(), 0, s>>>(st, ctl, dp, nblk, m2, hacc, Hm, cs, sn, g, inv, m, B);
+    k_b_scale<V><<<vgrid(), kBT, 0, s>>>(st, ctl, inv, Vb, vslot, np);
+    return 11;
+  }
+  int enqueue_end(cudaStream_t s) {
+    k_b_end<<<1, ctl_threads(), 0, s>>>(st, Hm, g, y, m, B);
+    k_b_update<V><<<vgrid(), kBT, 0, s>>>(st, Vb, vslot, np, y, m, x);
+    return 2;
+  }
+
+  int capture_one(cudaGraphExec_t *out, int which, int *kernels) {
+    cudaStream_t s = ctx->stream;
+    cudaGraph_t gr = nullptr;
+    if(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return OM_ERR_CUDA;
+    int k = 0;
+    if(which == 0)
+      k = enqueue_start(s);
+    else if(which == 1)
+      for(int t = 0; t < kSegSteps; ++t)
+        k += enqueue_step(s);
+    else
+      k = enqueue_end(s);
+    cudaError_t e = cudaStreamEndCapture(s, &gr);
+    if(e == cudaSuccess)
+      e = cudaGraphInstantiate(out, gr, 0);
+    if(gr)
+      cudaGraphDestroy(gr);
+    if(e != cudaSuccess) {
+      cudaGetLastError();
+      ctx->err = std::string("batch graph capture: ") + cudaGetErrorString(e);
+      return OM_ERR_CUDA;
+    }
+    *kernels = k;
+    return OM_OK;
+  }
+  int capture() {
+    int rc = capture_one(&g_start, 0, &k_start);
+    if(!rc) rc = capture_one(&g_seg, 1, &k_seg);
+    if(!rc) rc = capture_one(&g_end, 2, &k_end);
+    return rc;
+  }
+
+  int read_ctl() {
+    cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if(e != cudaSuccess) {
+      ctx->err = std::string("batched solve: ") + cudaGetErrorString(e);
+      return OM_ERR_CUDA;
+    }
+    return OM_OK;
+  }
+
+  // Solve the systems of the slots whose h_st entries are set (uploaded here):
+  // replays the graphs until no slot needs another cycle.
+  int solve(long *launches) {
+    int nt = 0;
+    for(int s = 0; s < B; ++s) {
+      const long n = h_st[s].outer ? h_st[s].n : 0;
+      const int rt = (int)((n + kBT - 1) / kBT), ct = (int)((n + kBCols - 1) / kBCols);
+      for(int c = 0; c < ct; ++c)
+        for(int q = 0; q < rt; ++q)
+          h_tiles[nt++] = make_int4(s, q, c, 0);
+    }
+    h_ctl->j = 0;
+    h_ctl->n_inner = 0;
+    h_ctl->n_outer = 0;
+    h_ctl->ntiles = nt;
+    cudaMemcpyAsync(st, h_st, sizeof(Slot) * B, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, ctx->stream);
+    if(nt)
+      cudaMemcpyAsync(tiles, h_tiles, sizeof(int4) * nt, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(x, 0, sizeof(double2) * B * np, ctx->stream);
+    // each cycle ends within m steps, and a slot runs at most max_cycles cycles
+    const long guard = (long)(key.max_cycles + 2) * (m / kSegSteps + 2) + 8;
+    long rounds = 0;
+    for(;;) {
+      cudaGraphLaunch(g_start, ctx->stream);
+      cudaGraphLaunch(g_seg, ctx->stream);
+      *launches += k_start + k_seg;
+      int rc = read_ctl();
+      if(rc)
+        return rc;
+      if(h_ctl->n_outer == 0)
+        break;
+      while(h_ctl->n_inner > 0) {
+        if(++rounds > guard) {
+          ctx->err = "batched solve: iteration guard reached";
+          return OM_ERR_CUDA;
+        }
+        cudaGraphLaunch(g_seg, ctx->stream);
+        *launches += k_seg;
+        rc = read_ctl();
+        if(rc)
+          return rc;
+      }
+      cudaGraphLaunch(g_end, ctx->stream);
+      *launches += k_end;
+      if(++rounds > guard) {
+        ctx->err = "batched solve: iteration guard reached";
+        return OM_ERR_CUDA;
+      }
+    }
+    cudaMemcpyAsync(h_st, st, sizeof(Slot) * B, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if(e != cudaSuccess) {
+      ctx->err = std::string("batched solve: ") + cudaGetErrorString(e);
+      return OM_ERR_CUDA;
+    }
+    return OM_OK;
+  }
+};
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+void fill_stats(const Slot &sl, bool mixed, double seconds, om_solve_stats *o) {
+  o->iterations = mixed ? sl.cycles : sl.steps;
+  o->inner_iterations = mixed ? sl.steps : 0;
+  o->rel_residual = sl.bnorm > 0 ? sl.rho / sl.bnorm : 0.0;
+  o->seconds = seconds;
+}
+
+// Auxiliary contexts of `ctx` (created on first use, kept with it): the
+// per-request set-up and post-processing kernels are small (one CTA per
+// sphere), so the requests of a batch spread them over kAux streams.
+constexpr int kAux = 8;
+int aux_contexts(om_context *ctx) {
+  while((int)ctx->aux.size() < kAux) {
+    om_context *a = nullptr;
+    int rc = om_context_create(ctx->device, 0, &a);
+    if(rc) {
+      ctx->err = "cannot create an auxiliary context for the batch";
+      return rc;
+    }
+    a->parent = ctx;
+    ctx->aux.push_back(a);
+  }
+  return OM_OK;
+}
+
+// Stream-order the auxiliary streams after the main stream (to_aux) or the
+// main stream after the auxiliary ones.
+void join(om_context *ctx, cudaEvent_t ev_main, const std::vector<cudaEvent_t> &ev_aux, bool to_aux) {
+  if(to_aux) {
+    cudaEventRecord(ev_main, ctx->stream);
+    for(om_context *a : ctx->aux)
+      cudaStreamWaitEvent(a->stream, ev_main, 0);
+  } else {
+    for(size_t q = 0; q < ctx->aux.size(); ++q) {
+      cudaEventRecord(ev_aux[q], ctx->aux[q]->stream);
+      cudaStreamWaitEvent(ctx->stream, ev_aux[q], 0);
+    }
+  }
+}
+
+// One batch of nb requests (indices idx[b0 ..]) of a size class; the
+// problems it creates are left in `pr` for the caller to destroy. Request s
+// lives on auxiliary context s % kAux; the batched assembly and solves run
+// on the main stream.
+template <typename M, typename V>
+int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::vector<int> &idx,
+              size_t b0, int nb, const om_request *reqs, om_result *out, double t_call,
+              std::vector<om_problem *> &pr, long *launches) {
+  const bool mixed = key.precision == OM_C64;
+  const long np = cl.np;
+  const size_t per = Class<M, V>::slot_bytes(np, key.m);
+  const double t0 = now_ms();
+  int rc = OM_OK;
+  auto actx = [&](int s) { return ctx->aux[s % kAux]; };
+  auto tracked = [&](om_context *c, auto &&fn) {
+    const int L0 = c->last_launches;
+    fn();
+    *launches += c->last_launches - L0;
+  };
+  auto fail = [&](int s, int r) {
+    om_result &res = out[idx[b0 + s]];
+    if(res.status == OM_OK || res.status == OM_ERR_NOT_CONVERGED)
+      res.status = r;
+    ctx->err = actx(s)->err;
+  };
+  // set-up: per-sphere terms, incident coefficients, source vector
+  for(int s = 0; s < nb; ++s) {
+    const om_request &rq = reqs[idx[b0 + s]];
+    om_result &res = out[idx[b0 + s]];
+    res.slot = s;
+    res.queue_ms = t0 - t_call;
+    om_context *a = actx(s);
+    int r = om_problem_create(a, rq.spheres, rq.n_spheres, &rq.background, &rq.wave, &pr[s]);
+    *launches += a->last_launches;
+    if(r) {
+      fail(s, r);
+      pr[s] = nullptr;
+      continue;
+    }
+    tracked(a, [&] { launch_source(pr[s]); });
+    pr[s]->have_source = true;
+  }
+  join(ctx, cl.ev_main, cl.ev_aux, false);
+  // one assembly launch: FF matrices in entries 0 .. B-1, SH in B .. 2B-1
+  const long per_mat = (long)key.Npad * (key.Npad + 1) / 2;
+  bool any_sh = false;
+  for(int e = 0; e < 2 * cl.B; ++e)
+    cl.h_mats[e] = BatchMat{nullptr, nullptr, nullptr, 0, mk(0.0, 0.0), 0};
+  for(int s = 0; s < nb; ++s) {
+    if(!pr[s])
+      continue;
+    const cplx k = pr[s]->waveK;
+    cl.h_mats[s] = BatchMat{pr[s]->d_cart, pr[s]->d_T, cl.Sff + (size_t)s * np * np, pr[s]->n,
+                            mk(k.real(), k.imag()), pr[s]->N};
+    if(reqs[idx[b0 + s]].wave.sh) {
+      any_sh = true;
+      const cplx k2 = 2.0 * k;
+      cl.h_mats[cl.B + s] = BatchMat{pr[s]->d_cart, pr[s]->d_Tsh, cl.Ssh + (size_t)s * np * np,
+                                     pr[s]->n, mk(k2.real(), k2.imag()), pr[s]->N};
+    }
+  }
+  const int nmats = any_sh ? 2 * cl.B : cl.B;
+  cudaMemcpyAsync(cl.mats, cl.h_mats, sizeof(BatchMat) * nmats, cudaMemcpyHostToDevice, ctx->stream);
+  tracked(ctx, [&] {
+    launch_assemble_batch(ctx, key.nmax, key.precision, cl.mats, nmats, (int)per_mat, ctx->stream);
+  });
+  // FF systems
+  for(int s = 0; s < cl.B; ++s) {
+    Slot z{};
+    z.bnorm = -1.0;
+    z.xzero = 1;
+    if(s < nb && pr[s]) {
+      z.n = pr[s]->n;
+      z.S = cl.Sff + (size_t)s * np * np;
+      z.outer = 1;
+      cudaMemcpyAsync(cl.b + (size_t)s * np, pr[s]->d_Q, sizeof(double2) * z.n,
+                      cudaMemcpyDeviceToDevice, ctx->stream);
+    }
+    cl.h_st[s] = z;
+  }
+  const double ts = now_ms();
+  rc = cl.solve(launches);
+  const double t_ff = (now_ms() - ts) * 1e-3;
+  if(rc)
+    return rc;
+  // FF results and the SH sources, on the auxiliary streams
+  join(ctx, cl.ev_main, cl.ev_aux, true);
+  std::vector<Slot> ff(cl.h_st, cl.h_st + cl.B);
+  for(int s = 0; s < nb; ++s) {
+    if(!pr[s])
+      continue;
+    om_result &res = out[idx[b0 + s]];
+    fill_stats(ff[s], mixed, t_ff, &res.ff);
+    res.status = ff[s].status;
+    om_context *a = actx(s);
+    cudaMemcpyAsync(pr[s]->d_X, cl.x + (size_t)s * np, sizeof(double2) * pr[s]->n,
+                    cudaMemcpyDeviceToDevice, a->stream);
+    tracked(a, [&] {
+      launch_internal(pr[s]);
+      launch_cross_sections(pr[s]);
+    });
+    pr[s]->have_solution = true;
+    if(reqs[idx[b0 + s]].wave.sh) {
+      int r = sh_alloc(pr[s]);
+      if(r) {
+        fail(s, r);
+        continue;
+      }
+      tracked(a, [&] { launch_sh_source(pr[s]); });
+    }
+  }
+  join(ctx, cl.ev_main, cl.ev_aux, false);
+  // SH systems
+  bool run = false;
+  for(int s = 0; s < cl.B; ++s) {
+    Slot z{};
+    z.bnorm = -1.0;
+    z.xzero = 1;
+    if(s < nb && pr[s] && reqs[idx[b0 + s]].wave.sh && pr[s]->d_K && pr[s]->d_acs) {
+      z.n = pr[s]->n;
+      z.S = cl.Ssh + (size_t)s * np * np;
+      z.outer = 1;
+      run = true;
+      cudaMemcpyAsync(cl.b + (size_t)s * np, pr[s]->d_K, sizeof(double2) * z.n,
+                      cudaMemcpyDeviceToDevice, ctx->stream);
+    }
+    cl.h_st[s] = z;
+  }
+  double t_sh = 0.0;
+  if(run) {
+    const double t1 = now_ms();
+    rc = cl.solve(launches);
+    t_sh = (now_ms() - t1) * 1e-3;
+    if(rc)
+      return rc;
+  }
+  // SH results; every request's cross sections into pinned memory
+  join(ctx, cl.ev_main, cl.ev_aux, true);
+  double *hx = cl.h_xsec;
+  for(int s = 0; s < nb; ++s) {
+    if(!pr[s])
+      continue;
+    om_context *a = actx(s);
+    if(run && cl.h_st[s].n) {
+      om_result &res = out[idx[b0 + s]];
+      fill_stats(cl.h_st[s], mixed, t_sh, &res.sh);
+      if(res.status == OM_OK)
+        res.status = cl.h_st[s].status;
+      cudaMemcpyAsync(pr[s]->d_Xsh, cl.x + (size_t)s * np, sizeof(double2) * pr[s]->n,
+                      cudaMemcpyDeviceToDevice, a->stream);
+      tracked(a, [&] {
+        launch_sh_internal(pr[s]);
+        launch_sh_cross_sections(pr[s], pr[s]->d_xsec + 4);
+      });
+      pr[s]->have_sh = true;
+    }
+    cudaMemcpyAsync(hx + 8 * s, pr[s]->d_xsec, sizeof(double) * 6, cudaMemcpyDeviceToHost, a->stream);
+  }
+  cudaError_t e = cudaSuccess;
+  for(om_context *a : ctx->aux) {
+    cudaError_t ea = cudaStreamSynchronize(a->stream);
+    if(e == cudaSuccess)
+      e = ea;
+  }
+  if(e == cudaSuccess)
+    e = cudaGetLastError();
+  const double t_end = now_ms();
+  for(int s = 0; s < nb; ++s) {
+    om_result &res = out[idx[b0 + s]];
+    if(pr[s]) {
+      for(int q = 0; q < 4; ++q)
+        res.xsec[q] = hx[8 * s + q];
+      if(reqs[idx[b0 + s]].wave.sh)
+        for(int q = 0; q < 2; ++q)
+          res.xsec_sh[q] = hx[8 * s + 4 + q];
+    }
+    res.service_ms = t_end - t0;
+    res.latency_ms = t_end - t_call;
+    res.device_bytes = per;
+  }
+  if(e != cudaSuccess) {
+    ctx->err = std::string("batch: ") + cudaGetErrorString(e);
+    return OM_ERR_CUDA;
+  }
+  return OM_OK;
+}
+
+template <typename M, typename V>
+int run_class(om_context *ctx, const ClassKey &key, const std::vector<int> &idx, const om_request *reqs,
+              om_result *out, size_t arena, double t_call, long *launches) {
+  const long np = (long)rup((size_t)2 * pmax(key.nmax) * key.Npad);
+  const size_t per = Class<M, V>::slot_bytes(np, key.m);
+  // tables the auxiliary contexts share, ready before their streams use them
+  int rc = aux_contexts(ctx);
+  if(rc)
+    return rc;
+  coef_tables(ctx, key.nmax);
+  clg_tables_dev(ctx, key.nmax);
+  cudaStreamSynchronize(ctx->stream);
+  int B = (int)std::min<size_t>({idx.size(), (size_t)kMaxSlots, std::max<size_t>(1, arena / per)});
+  Class<M, V> *cl = nullptr;
+  for(;;) {
+    cl = new Class<M, V>();
+    rc = cl->init(ctx, key, B);
+    if(!rc)
+      break;
+    delete cl;
+    cl = nullptr;
+    if(rc != OM_ERR_BUDGET || B == 1)
+      break;
+    B = (B + 1) / 2;
+  }
+  if(!cl) {
+    for(int i : idx)
+      out[i].status = rc;
+    return OM_OK;
+  }
+  for(size_t b0 = 0; b0 < idx.size() && !rc; b0 += B) {
+    const int nb = (int)std::min<size_t>(B, idx.size() - b0);
+    std::vector<om_problem *> pr(nb, nullptr);
+    rc = run_batch(ctx, key, *cl, idx, b0, nb, reqs, out, t_call, pr, launches);
+    for(om_problem *p : pr)
+      if(p)
+        om_problem_destroy(p);
+  }
+  delete cl;
+  return rc;
+}
+
+}  // namespace
+
+}  // namespace om
+
+extern "C" int om_batch_solve(om_context *ctx, const om_request *reqs, int count, size_t arena_bytes,
+                              om_result *results) {
+  using namespace om;
+  if(!ctx || (count > 0 && (!reqs || !results)) || count < 0)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  const double t_call = now_ms();
+  long launches = 0;
+  std::map<ClassKey, std::vector<int>> classes;
+  for(int i = 0; i < count; ++i) {
+    const om_request &rq = reqs[i];
+    om_result &res = results[i];
+    res = om_result{};
+    res.status = OM_OK;
+    const om_solve_options &o = rq.opts;
+    const bool plain = rq.precision == OM_C128 && o.method == OM_SOLVE_GMRES;
+    const bool mixed = rq.precision == OM_C64 && o.method == OM_SOLVE_FGMRES_MIXED;
+    if(!plain && !mixed) {
+      res.status = OM_ERR_INVALID;
+      continue;
+    }
+    if(!rq.spheres || rq.n_spheres < 1 || rq.spheres[0].nmax < 1 || rq.spheres[0].nmax > kMaxNmax ||
+       o.max_iter < 1 || o.restarts < 1 || (mixed && o.inner_iter < 1)) {
+      res.status = OM_ERR_INVALID;
+      continue;
+    }
+    ClassKey k{};
+    k.precision = rq.precision;
+    k.nmax = rq.spheres[0].nmax;
+    k.Npad = pad_spheres(rq.n_spheres);
+    k.m = mixed ? o.inner_iter : o.max_iter;
+    k.max_cycles = mixed ? std::min(o.max_iter, 32) * o.restarts : o.restarts;
+    k.tol = o.tol;
+    k.inner_rel = mixed ? o.inner_tol : 0.0;
+    classes[k].push_back(i);
+  }
+  bool bad = false;
+  for(int i = 0; i < count; ++i)
+    bad |= results[i].status == OM_ERR_INVALID;
+  if(bad)
+    ctx->err = "om_batch_solve runs OM_SOLVE_GMRES on OM_C128 and OM_SOLVE_FGMRES_MIXED on OM_C64 "
+               "requests with positive iteration counts and 1 <= nMax <= 15";
+  size_t arena = arena_bytes;
+  if(!arena) {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    arena = std::min<size_t>(fr / 5 * 2, size_t(64) << 30);
+    if(ctx->budget)
+      arena = std::min(arena, (ctx->budget - std::min(ctx->budget, ctx->used)) / 2);
+  }
+  int rc = OM_OK;
+  for(auto &kv : classes) {
+    try {
+      if(kv.first.precision == OM_C64)
+        rc = run_class<float2, float2>(ctx, kv.first, kv.second, reqs, results, arena, t_call, &launches);
+      else
+        rc = run_class<double2, double2>(ctx, kv.first, kv.second, reqs, results, arena, t_call,
+                                         &launches);
+    } catch(std::exception &e) {
+      ctx->err = e.what();
+      rc = OM_ERR_CUDA;
+    }
+    if(rc)
+      break;
+  }
+  ctx->last_launches = (int)std::min<long>(launches, 0x7fffffff);
+  return rc;
+}

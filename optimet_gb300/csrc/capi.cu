@@ -59,10 +59,17 @@ int update_wave(om_problem *pr) {
   pr->iZ = cplx(0.0, -1.0) / std::sqrt(mu_b / eps_b);
   const double w = pr->omega;
   const cplx waveK_0 = w * std::sqrt(kEps0 * kMu0);
-  std::vector<om::SphereScalars> sc(pr->N);
-  std::vector<om::ShScalars> shs(pr->N);
+  // the previous upload from these buffers must be done before they change
+  if(!pr->h_scal.empty())
+    cudaStreamSynchronize(ctx->stream);
+  std::vector<om::SphereScalars> &sc = pr->h_scal;
+  std::vector<om::ShScalars> &shs = pr->h_shs;
+  std::vector<zd> &kin = pr->h_kin, &izin = pr->h_izin;
+  sc.assign(pr->N, om::SphereScalars{});
+  shs.assign(pr->N, om::ShScalars{});
+  kin.assign(pr->N, zd{});
+  izin.assign(pr->N, zd{});
   pr->eta = std::sqrt(mu_b / eps_b);
-  std::vector<zd> kin(pr->N), izin(pr->N);
   for(int i = 0; i < pr->N; ++i) {
     const cplx eps_s = pr->eps_r[i] * kEps0, mu_s = pr->mu_r[i] * kMu0;
     const cplx eps_sh = pr->eps_r_sh[i] * kEps0;
@@ -115,10 +122,14 @@ int update_wave(om_problem *pr) {
                cp = std::cos(pr->phi);
   const cplx Et = pr->e_theta, Ep = pr->e_phi;
   const cplx ex = ct * cp * Et - sp * Ep, ey = ct * sp * Et + cp * Ep, ez = -st * Et;
-  const double einc[6] = {ex.real(), ex.imag(), ey.real(), ey.imag(), ez.real(), ez.imag()};
+  double *einc = pr->h_einc;
+  einc[0] = ex.real();
+  einc[1] = ex.imag();
+  einc[2] = ey.real();
+  einc[3] = ey.imag();
+  einc[4] = ez.real();
+  einc[5] = ez.imag();
   om::launch_incident(pr, einc);
-  // the incident-field vector must reach the device before the host buffer dies
-  cudaStreamSynchronize(ctx->stream);
   pr->have_source = false;
   pr->have_solution = false;
   pr->have_sh = false;
@@ -543,6 +554,9 @@ void om_context_destroy(om_context *ctx) {
   if(!ctx)
     return;
   cudaSetDevice(ctx->device);
+  for(om_context *a : ctx->aux)
+    om_context_destroy(a);
+  ctx->aux.clear();
   cudaStreamSynchronize(ctx->stream);
   // problems still alive belong to the context and go with it
   while(!ctx->problems.empty())

@@ -72,6 +72,19 @@ struct AcaOp {
   const double2 *store;
 };
 
+// One matrix of a batched assembly (batch.cu): the spheres' centres and
+// T-matrix factors (FF or SH), the wave number and the column-major output
+// (ld = 2 P N). N = 0 marks an unused entry.
+struct BatchMat {
+  const double *cart;
+  const zd *T;
+  void *S;
+  long ld;
+  zd waveK;
+  int N;
+};
+struct BatchClass;
+
 }  // namespace om
 
 struct om_context {
@@ -101,6 +114,10 @@ struct om_context {
   cudaEvent_t mark = nullptr;                // last om_context_mark event
   long n_mv64 = 0, n_mv32 = 0, n_mvdf = 0, n_asm = 0;
   std::vector<om_problem *> problems;  // live problems, destroyed with the context
+  // auxiliary contexts of the batched solver (streams for per-request work);
+  // a context with a parent takes its coefficient tables from the parent
+  om_context *parent = nullptr;
+  std::vector<om_context *> aux;
 };
 
 struct om_problem {
@@ -150,6 +167,12 @@ struct om_problem {
   bool have_sh = false;
   bool have_source = false, have_solution = false;
   om::AcaData aca[2];
+  // host copies of what update_wave uploads (kept until the next update, so
+  // that no asynchronous copy reads freed host memory)
+  std::vector<om::SphereScalars> h_scal;
+  std::vector<om::ShScalars> h_shs;
+  std::vector<om::zd> h_kin, h_izin;
+  double h_einc[6] = {0, 0, 0, 0, 0, 0};
 };
 
 namespace om {
@@ -162,6 +185,10 @@ void launch_assemble(om_problem *pr, int harmonic, int precision);
 // unordered pairs pair0 .. pair0 + count - 1 (pair b = j (j - 1) / 2 + i, i < j):
 // S_ij and S_ji as 2P x 2P column-major blocks at scratch + 2 (b - pair0) (2P)^2
 void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, double2 *scratch);
+// batched assembly: matrix e of the table d_mats (device) is assembled by CTAs
+// e per_mat .. (e + 1) per_mat - 1; per_mat >= N (N + 1) / 2 for every entry
+void launch_assemble_batch(om_context *ctx, int nmax, int precision, const BatchMat *d_mats,
+                           int nmats, int per_mat, cudaStream_t stream);
 void launch_source(om_problem *pr);
 void launch_sh_weights(om_problem *pr);
 int launch_coupling(om_context *ctx, const double *d_rel, int count, zd waveK, int nmax,

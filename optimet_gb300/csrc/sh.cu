@@ -526,6 +526,15 @@ __global__ void __launch_bounds__(128) k_near_field_sh_gamma(ShFieldArgs a) {
 }  // namespace
 
 const double *clg_tables_dev(om_context *ctx, int nmax) {
+  if(ctx->parent) {
+    bool cached = false;
+    for(auto &t : ctx->parent->clg)
+      cached |= t.first == nmax;
+    const double *d = clg_tables_dev(ctx->parent, nmax);
+    if(!cached)  // built on the parent's stream: finish before this context uses it
+      cudaStreamSynchronize(ctx->parent->stream);
+    return d;
+  }
   for(auto &t : ctx->clg)
     if(t.first == nmax)
       return t.second;

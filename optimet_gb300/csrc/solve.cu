@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "om_internal.h"
+#include "om_krylov.cuh"
 
 namespace om {
 
@@ -32,21 +33,6 @@ template <> struct C2<double> {
 template <> struct C2<float> {
   typedef float2 T;
 };
-
-template <typename V> __device__ __forceinline__ V cfma(V a, V b, V c) {  // c + a*b
-  c.x = fma(a.x, b.x, c.x);
-  c.x = fma(-a.y, b.y, c.x);
-  c.y = fma(a.x, b.y, c.y);
-  c.y = fma(a.y, b.x, c.y);
-  return c;
-}
-template <typename V> __device__ __forceinline__ V cfma_conj(V a, V b, V c) {  // c + conj(a)*b
-  c.x = fma(a.x, b.x, c.x);
-  c.x = fma(a.y, b.y, c.x);
-  c.y = fma(a.x, b.y, c.y);
-  c.y = fma(-a.y, b.x, c.y);
-  return c;
-}
 
 constexpr int kMvThreads = 256;
 constexpr int kMvCols = 1024;  // largest split-K chunk (x staged in shared memory)
@@ -95,35 +81,7 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld,
     __syncthreads();
     if(i >= n)
       continue;
-    V acc0, acc1;
-    acc0.x = acc0.y = acc1.x = acc1.y = 0;
-    const M *col = S + j0 * ld + i;
-    long j = j0;
-    for(; j + 7 < j1; j += 8) {
-      M s[8];
-#pragma unroll
-      for(int u = 0; u < 8; ++u)
-        s[u] = col[u * ld];
-#pragma unroll
-      for(int u = 0; u < 8; u += 2) {
-        V a0, a1;
-        a0.x = s[u].x; a0.y = s[u].y; a1.x = s[u + 1].x; a1.y = s[u + 1].y;
-        acc0 = cfma(a0, xs[j - j0 + u], acc0);
-        acc1 = cfma(a1, xs[j - j0 + u + 1], acc1);
-      }
-      col += 8 * ld;
-    }
-    for(; j < j1; ++j) {
-      M s0 = col[0];
-      V a0;
-      a0.x = s0.x;
-      a0.y = s0.y;
-      acc0 = cfma(a0, xs[j - j0], acc0);
-      col += ld;
-    }
-    acc0.x += acc1.x;
-    acc0.y += acc1.y;
-    part[ct * n + i] = acc0;
+    part[ct * n + i] = mv_row<M, V>(S + j0 * ld + i, ld, xs, (int)(j1 - j0));
   }
 }
 
@@ -134,15 +92,6 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld,
 // small terms (product errors and s * x_lo) go to a separate float sum. Each
 // CTA sums kMvCols columns, so the per-thread sums are short; partials are
 // combined in FP64.
-struct DF {
-  float hi, lo;
-};
-__device__ __forceinline__ void df_add(DF &a, float p) {
-  const float s = a.hi + p;
-  const float bb = s - a.hi;
-  a.lo += (a.hi - (s - bb)) + (p - bb);
-  a.hi = s;
-}
 __global__ void __launch_bounds__(kMvThreads) k_matvec_part_df(const float2 *S, long ld, long n,
                                                                const double2 *x, double2 *part,
                                                                int row_tiles, long tiles,
@@ -161,53 +110,12 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part_df(const float2 *S, 
     const long i = rt * kMvThreads + threadIdx.x;
     const long j0 = ct * cols;
     const long j1 = min(n, j0 + cols);
-    for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads) {
-      const double2 v = x[j];
-      const float hr = (float)v.x, hi = (float)v.y;
-      xs[j - j0] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
-    }
+    for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads)
+      xs[j - j0] = df_split(x[j]);
     __syncthreads();
     if(i >= n)
       continue;
-    DF re{0.f, 0.f}, im{0.f, 0.f};
-    float er = 0.f, ei = 0.f;
-    const float2 *col = S + j0 * ld + i;
-    for(long j = j0; j < j1; j += 4) {
-      // four columns' loads in flight, then the same per-column arithmetic
-      float2 av[4];
-      const int cnt = (int)min(4L, j1 - j);
-#pragma unroll
-      for(int u = 0; u < 4; ++u)
-        av[u] = u < cnt ? col[u * ld] : make_float2(0.f, 0.f);
-#pragma unroll
-      for(int u = 0; u < 4; ++u) {
-        if(u >= cnt)
-          break;
-        const float2 a = av[u];
-        const float4 v = xs[j - j0 + u];
-        // __fmul_rn keeps the products out of FMA contraction so that the
-        // TwoProduct error terms below are exact
-        float p = __fmul_rn(a.x, v.x);
-        er += fmaf(a.x, v.x, -p);
-        df_add(re, p);
-        p = __fmul_rn(-a.y, v.y);
-        er += fmaf(-a.y, v.y, -p);
-        df_add(re, p);
-        er = fmaf(a.x, v.z, er);
-        er = fmaf(-a.y, v.w, er);
-        p = __fmul_rn(a.x, v.y);
-        ei += fmaf(a.x, v.y, -p);
-        df_add(im, p);
-        p = __fmul_rn(a.y, v.x);
-        ei += fmaf(a.y, v.x, -p);
-        df_add(im, p);
-        ei = fmaf(a.x, v.w, ei);
-        ei = fmaf(a.y, v.z, ei);
-      }
-      col += 4 * ld;
-    }
-    part[ct * n + i] = make_double2((double)re.hi + ((double)re.lo + (double)er),
-                                    (double)im.hi + ((double)im.lo + (double)ei));
+    part[ct * n + i] = mv_row_df(S + j0 * ld + i, ld, xs, (int)(j1 - j0));
   }
 }
 

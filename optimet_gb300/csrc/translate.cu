@@ -507,6 +507,12 @@ struct AssembleArgs {
   // S + 2 b (2P)^2 (ld = 2P); no identity blocks
   int scratch;
   long pair0;
+  // batch mode (batch != nullptr): CTA b works on matrix b / per_mat of the
+  // table, local index b % per_mat (pairs, then identity blocks, then idle
+  // CTAs of the size class's padding); the table's entry replaces cart, T,
+  // N, waveK, ld and S
+  const BatchMat *batch;
+  int per_mat;
 };
 
 template <typename O> __device__ __forceinline__ void put_out(O *S, size_t at, double re, double im);
@@ -534,15 +540,32 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
   typedef typename std::conditional<kMixed, float2, zd>::type TabT;
   typedef typename std::conditional<kMixed, float, double>::type R;
   extern __shared__ double smem[];
-  const long npairs = (long)a.N * (a.N - 1) / 2;
-  const long b = blockIdx.x + (a.scratch ? a.pair0 : 0);
+  const double *cart = a.cart;
+  const zd *Tg = a.T;
+  int N = a.N;
+  zd waveK = a.waveK;
+  long ld = a.ld;
+  long b = blockIdx.x + (a.scratch ? a.pair0 : 0);
+  if(a.batch) {
+    const BatchMat &bm = a.batch[blockIdx.x / a.per_mat];
+    b = blockIdx.x % a.per_mat;
+    cart = bm.cart;
+    Tg = bm.T;
+    N = bm.N;
+    waveK = bm.waveK;
+    ld = bm.ld;
+    S = (OutT *)bm.S;
+    if(b >= (long)N * (N + 1) / 2)  // idle: padding of the size class or an empty entry
+      return;
+  }
+  const long npairs = (long)N * (N - 1) / 2;
   const int P = y.P;
   if(!a.scratch && b >= npairs) {
     const int i = (int)(b - npairs);
     const long x0 = 2L * P * i;
     for(int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) {
       int c = idx / (2 * P), r = idx - c * 2 * P;
-      put_out<OutT>(S, (x0 + c) * a.ld + x0 + r, r == c ? 1.0 : 0.0, 0.0);
+      put_out<OutT>(S, (x0 + c) * ld + x0 + r, r == c ? 1.0 : 0.0, 0.0);
     }
     return;
   }
@@ -564,27 +587,27 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
   load_tables(s, y, a.rec, a.qf, a.pf, a.legc);
   const int nT = 2 * (y.nmax + 1);
   for(int t = threadIdx.x; t < 2 * nT; t += blockDim.x)  // T_i then T_j
-    s.tl[t] = a.T[(size_t)(t < nT ? i : j) * nT + (t < nT ? t : t - nT)];
+    s.tl[t] = Tg[(size_t)(t < nT ? i : j) * nT + (t < nT ? t : t - nT)];
   if(kMixed) {
     for(int t = threadIdx.x; t < kQfacStride * y.P; t += blockDim.x)
       s.qf32[t] = (float)a.qf[t];
     for(int t = threadIdx.x; t < kPfacStride * y.P; t += blockDim.x)
       s.pf32[t] = (float)a.pf[t];
     for(int t = threadIdx.x; t < 2 * nT; t += blockDim.x) {
-      const zd v = a.T[(size_t)(t < nT ? i : j) * nT + (t < nT ? t : t - nT)];
+      const zd v = Tg[(size_t)(t < nT ? i : j) * nT + (t < nT ? t : t - nT)];
       s.tl32[t] = make_float2((float)v.re, (float)v.im);
     }
   }
   if(threadIdx.x == 0) {
-    double dx = a.cart[3 * i] - a.cart[3 * j], dy = a.cart[3 * i + 1] - a.cart[3 * j + 1],
-           dz = a.cart[3 * i + 2] - a.cart[3 * j + 2];
+    double dx = cart[3 * i] - cart[3 * j], dy = cart[3 * i + 1] - cart[3 * j + 1],
+           dz = cart[3 * i + 2] - cart[3 * j + 2];
     to_spherical(dx, dy, dz, &s.geo[0], &s.geo[1], &s.geo[2]);
   }
   __syncthreads();
-  make_seeds(s, y, a.waveK, 1);
+  make_seeds(s, y, waveK, 1);
   for(int c = 0; c < a.nchunks; ++c) {
     const int n_lo = a.chunks[c].x, n_hi = a.chunks[c].y;
-    chains<TabT>(s, tab, y, 1, a.waveK.im == 0.0, n_lo, n_hi);
+    chains<TabT>(s, tab, y, 1, waveK.im == 0.0, n_lo, n_hi);
     __syncthreads();
     const int base = n_lo * n_lo - 1;
     const int rows = (n_hi + 1) * (n_hi + 1) - 1 - base;
@@ -607,7 +630,7 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
         tmj = CT<R>{(R)s.tl[nT + 2 * l + 1].re, (R)s.tl[nT + 2 * l + 1].im};
       }
       // S_ij (rows of sphere i, columns of sphere j), translation r_i - r_j
-      size_t col_te = (xj + q) * a.ld + xi, col_tm = (xj + P + q) * a.ld + xi;
+      size_t col_te = (xj + q) * ld + xi, col_tm = (xj + P + q) * ld + xi;
       CT<R> v = neg_mul(tei, A);
       put_out<OutT>(Sij, col_te + p, v.re, v.im);
       v = neg_mul(tmi, A);
@@ -624,8 +647,8 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
         B.re = -B.re;
         B.im = -B.im;
       }
-      col_te = (xi + q) * a.ld + xj;
-      col_tm = (xi + P + q) * a.ld + xj;
+      col_te = (xi + q) * ld + xj;
+      col_tm = (xi + P + q) * ld + xj;
       v = neg_mul(tej, A);
       put_out<OutT>(Sji, col_te + p, v.re, v.im);
       v = neg_mul(tmj, A);
@@ -909,6 +932,8 @@ template <typename K> void set_smem(K kernel, size_t bytes, int carveout = -1) {
 }  // namespace
 
 const CoefTables &coef_tables(om_context *ctx, int nmax) {
+  if(ctx->parent)  // built with synchronous copies: ready for any stream
+    return coef_tables(ctx->parent, nmax);
   for(auto &t : ctx->tables)
     if(t.nmax == nmax)
       return t;
@@ -1011,6 +1036,8 @@ void launch_assemble(om_problem *pr, int harmonic, int precision) {
   a.ld = pr->n;
   a.scratch = 0;
   a.pair0 = 0;
+  a.batch = nullptr;
+  a.per_mat = 1;
   fill_chunks(a, y);
   dim3 grid((unsigned)((long)pr->N * (pr->N - 1) / 2 + pr->N));
   timer_begin(ctx, ctx->ev_asm);
@@ -1048,9 +1075,37 @@ void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, 
   a.ld = 2L * pr->P;
   a.scratch = 1;
   a.pair0 = pair0;
+  a.batch = nullptr;
+  a.per_mat = 1;
   fill_chunks(a, y);
   set_smem(k_assemble<false>, y.bytes, ctx->carve_asm);
   k_assemble<false><<<count, 256, y.bytes, ctx->stream>>>(a, y, scratch);
+  ctx->last_launches++;
+}
+
+void launch_assemble_batch(om_context *ctx, int nmax, int precision, const BatchMat *d_mats,
+                           int nmats, int per_mat, cudaStream_t stream) {
+  const CoefTables &ct = coef_tables(ctx, nmax);
+  const bool mixed = precision == OM_C64;
+  Layout y = make_layout(nmax, smem_limit(), mixed);
+  AssembleArgs a{};
+  a.rec = ct.rec;
+  a.qf = ct.qf;
+  a.pf = ct.pf;
+  a.legc = ct.legc;
+  a.scratch = 0;
+  a.pair0 = 0;
+  a.batch = d_mats;
+  a.per_mat = per_mat;
+  fill_chunks(a, y);
+  const dim3 grid((unsigned)((long)nmats * per_mat));
+  if(mixed) {
+    set_smem(k_assemble<true>, y.bytes, ctx->carve_asm);
+    k_assemble<true><<<grid, 256, y.bytes, stream>>>(a, y, nullptr);
+  } else {
+    set_smem(k_assemble<false>, y.bytes, ctx->carve_asm);
+    k_assemble<false><<<grid, 256, y.bytes, stream>>>(a, y, nullptr);
+  }
   ctx->last_launches++;
 }
 

@@ -1,0 +1,138 @@
+"""Batching form (om_batch_solve): batched results agree with the golden
+vectors of the oracle and with the single-request entry points, a request's
+results are bitwise the same alone and in any batch, and failures stay with
+the request that caused them.
+
+Tolerances: the plain form (complex128 GMRES to 1e-13) within 5e-10 of the
+golden cross sections, as the single-request entry point; both forms against
+the single-request FP64 path within 1e-10 (plain) and 1e-6 (precision form)."""
+import numpy as np
+import pytest
+
+from helpers import gpu_inputs, load_golden, nm, oracle_cluster, random_cluster, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G():
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    return G
+
+
+@pytest.fixture(scope="module")
+def ctx(G):
+    c = G.Context(0)
+    yield c
+    c.close()
+
+
+def plain(G, tol=1e-13):
+    return G.options(G.SOLVE_GMRES, tol=tol, max_iter=150, restarts=6)
+
+
+def mixed(G):
+    return G.options(G.SOLVE_FGMRES_MIXED, tol=1e-10, max_iter=30, restarts=4, inner_iter=40,
+                     inner_tol=1e-4)
+
+
+def ragged_requests(G, opts, prec, seed=11):
+    """Uneven N and nMax (several requests per size class), SH on every other
+    request, random incidence."""
+    rng = np.random.default_rng(seed)
+    specs = [(1, 4), (2, 4), (2, 4), (3, 4), (5, 4), (6, 4), (7, 5), (2, 5), (12, 4), (11, 4),
+             (9, 6), (4, 3), (16, 4), (6, 5)]
+    out = []
+    for i, (N, nmax) in enumerate(specs):
+        xyz, rad = random_cluster(rng, N, 1000 * nm, 40 * nm, 80 * nm, 20 * nm)
+        sh = i % 2 == 0
+        sp = G.spheres_array(xyz, rad, (2.2 + 0.05j) ** 2, nmax, eps_sh=(2.4 + 0.07j) ** 2,
+                             ksippp=1.0 if sh else 0.0, ksiparppar=0.25 if sh else 0.0)
+        wave = G.plane_wave(rng.uniform(500, 800) * nm, theta=rng.uniform(0, np.pi),
+                            phi=rng.uniform(-np.pi, np.pi), e_theta=0.6, e_phi=0.8j, sh=sh)
+        out.append((sp, G.medium(1.2), wave, opts, prec))
+    return out
+
+
+def test_golden_vectors_through_the_batch(G, ctx, oracle):
+    """The committed golden fixtures (oracle cross sections, FF and SH) as one
+    batched call spanning several size classes."""
+    names = ["c0", "metal5", "diel3", "single_sh", "pair_sh"]
+    reqs, gs = [], []
+    for name in names:
+        g = load_golden(name)
+        sp, bg, wave = gpu_inputs(G, oracle_cluster(oracle, g))
+        wave.sh = int("xsec_sh" in g.files)
+        reqs.append((sp, bg, wave, plain(G), G.C128))
+        gs.append(g)
+    res = G.batch_solve(ctx, reqs)
+    for name, g, r in zip(names, gs, res):
+        assert r["status"] == G.OK, name
+        assert np.max(np.abs(r["xsec"] - g["xsec"]) / np.abs(g["xsec"])) < 5e-10, name
+        if "xsec_sh" in g.files:
+            assert np.max(np.abs(r["xsec_sh"] - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10, name
+
+
+def test_plain_batch_matches_single_requests(G, ctx):
+    reqs = ragged_requests(G, plain(G), G.C128)
+    res = G.batch_solve(ctx, reqs)
+    for r, (sp, bg, wave, opts, prec) in zip(res, reqs):
+        assert r["status"] == G.OK
+        xs, xsh, _ = G.wavelength_solve_sh(ctx, sp, bg, wave, opts, prec)
+        assert rel(r["xsec"], xs) < 1e-10
+        if wave.sh:
+            assert rel(r["xsec_sh"], xsh) < 1e-10
+        assert r["ff"]["rel_residual"] <= 1e-13
+
+
+def test_precision_form_batch_within_1e6_of_fp64(G, ctx):
+    reqs = ragged_requests(G, mixed(G), G.C64)
+    res = G.batch_solve(ctx, reqs)
+    for r, (sp, bg, wave, opts, prec) in zip(res, reqs):
+        assert r["status"] == G.OK
+        xs, xsh, _ = G.wavelength_solve_sh(ctx, sp, bg, wave, plain(G), G.C128)
+        assert rel(r["xsec"], xs) < 1e-6
+        if wave.sh:
+            assert rel(r["xsec_sh"], xsh) < 1e-6
+        # refinement: a few cycles, each an FP32 Arnoldi run
+        assert 1 <= r["ff"]["iterations"] <= 8 and r["ff"]["inner_iterations"] >= 1
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_alone_equals_in_the_batch(G, ctx, form):
+    """Every kernel reduces in a fixed order per slot, so a request gives the
+    same bits alone, in a full batch, and in batches cut small by the arena."""
+    reqs = ragged_requests(G, plain(G) if form == "plain" else mixed(G),
+                           G.C128 if form == "plain" else G.C64, seed=5)
+    together = G.batch_solve(ctx, reqs)
+    tiny = G.batch_solve(ctx, reqs, arena_bytes=1 << 20)  # one request per batch
+    for i, rq in enumerate(reqs):
+        alone = G.batch_solve(ctx, [rq])[0]
+        for other in (together[i], tiny[i]):
+            assert np.array_equal(alone["xsec"], other["xsec"])
+            assert np.array_equal(alone["xsec_sh"], other["xsec_sh"])
+            assert alone["ff"]["iterations"] == other["ff"]["iterations"]
+            assert alone["sh"]["inner_iterations"] == other["sh"]["inner_iterations"]
+    assert len({r["slot"] for r in together}) > 1
+
+
+def test_failures_stay_with_their_request(G, ctx):
+    rng = np.random.default_rng(3)
+    xyz, rad = random_cluster(rng, 4, 800 * nm, 40 * nm, 60 * nm, 20 * nm)
+    good = G.spheres_array(xyz, rad, 4.0, 4)
+    overlap = G.spheres_array([[0, 0, 0], [0, 0, 50 * nm]], [40 * nm, 40 * nm], 4.0, 4)
+    w = G.plane_wave(600 * nm)
+    starved = G.options(G.SOLVE_GMRES, tol=1e-14, max_iter=2, restarts=1)
+    reqs = [(good, G.medium(), w, plain(G), G.C128),
+            (overlap, G.medium(), w, plain(G), G.C128),
+            (good, G.medium(), w, G.options(G.SOLVE_LU), G.C128),  # LU is not batched
+            (good, G.medium(), w, starved, G.C128),
+            (good, G.medium(), w, plain(G), G.C128)]
+    res = G.batch_solve(ctx, reqs)
+    assert [r["status"] for r in res] == [G.OK, G.ERR_OVERLAP, G.ERR_INVALID, G.ERR_NOT_CONVERGED,
+                                          G.OK]
+    assert np.array_equal(res[0]["xsec"], res[4]["xsec"])
+    # the unconverged request still reports its (approximate) cross sections
+    assert res[3]["ff"]["iterations"] == 2 and np.all(np.isfinite(res[3]["xsec"]))
