@@ -555,8 +555,9 @@ template <typename M, typename V> struct Class {
   Slot *st = nullptr;
   Ctl *ctl = nullptr;
   int4 *tiles = nullptr;
-  BatchMat *mats = nullptr;
-  M *Sff = nullptr, *Ssh = nullptr;
+  int nbuf = 1;                       // matrix buffers: 2 when batches overlap
+  BatchMat *mats = nullptr;           // nbuf x 2B entries
+  M *Sff[2] = {nullptr, nullptr}, *Ssh[2] = {nullptr, nullptr};
   double2 *b = nullptr, *x = nullptr, *r = nullptr, *part = nullptr;
   V *Vb = nullptr, *hs = nullptr;
   void *dpart = nullptr;
@@ -570,24 +571,27 @@ template <typename M, typename V> struct Class {
   BatchMat *h_mats = nullptr;
   double *h_xsec = nullptr;  // 8 per slot: the FF and SH cross sections
   cudaEvent_t ev_main = nullptr;        // main stream -> auxiliary streams
-  std::vector<cudaEvent_t> ev_aux;      // auxiliary streams -> main stream
+  std::vector<cudaEvent_t> ev_aux;      // auxiliary streams -> main / assembly stream
+  cudaEvent_t ev_asm[2] = {nullptr, nullptr};  // assembly of buffer i done
   cudaGraphExec_t g_start = nullptr, g_seg = nullptr, g_end = nullptr;
   int k_start = 0, k_seg = 0, k_end = 0;  // kernels per replay
 
-  static size_t slot_bytes(long np, int m) {
+  static size_t slot_bytes(long np, int m, int nbuf) {
     const int m2 = m + 2;
     const long nsm = (np + kBCols - 1) / kBCols, nblk = (np + kBDotRows - 1) / kBDotRows;
-    return 2 * rup(sizeof(M) * (size_t)np * np) + 3 * sizeof(double2) * np +
+    return 2 * nbuf * rup(sizeof(M) * (size_t)np * np) + 3 * sizeof(double2) * np +
            sizeof(V) * (size_t)(m + 1) * np + sizeof(double2) * (size_t)nsm * np +
            sizeof(double2) * (size_t)nblk * m2 + sizeof(V) * m2 +
            sizeof(double2) * ((size_t)m2 + (size_t)m * (m + 1) + 2 * (size_t)m + (m + 1) + m) +
-           sizeof(int4) * (size_t)((np + kBT - 1) / kBT) * nsm + sizeof(Slot) + 2 * sizeof(BatchMat) + 64;
+           sizeof(int4) * (size_t)((np + kBT - 1) / kBT) * nsm + sizeof(Slot) +
+           2 * nbuf * sizeof(BatchMat) + 64;
   }
 
-  int init(om_context *c, const ClassKey &k, int slots) {
+  int init(om_context *c, const ClassKey &k, int slots, int buffers) {
     ctx = c;
     key = k;
     B = slots;
+    nbuf = buffers;
     m = k.m;
     m2 = m + 2;
     np = (long)rup((size_t)2 * pmax(k.nmax) * k.Npad);
@@ -595,10 +599,13 @@ template <typename M, typename V> struct Class {
     nsm = (int)((np + kBCols - 1) / kBCols);
     nblk = (int)((np + kBDotRows - 1) / kBDotRows);
     max_tiles = B * (int)((np + kBT - 1) / kBT) * nsm;
-    mv_grid = (unsigned)std::max(1L, std::min((long)max_tiles, (long)ctx->sm_count * 8));
-    const size_t Bz = (size_t)B;
+    // overlapping batches: half the SM's CTA slots, so that two CTAs of the
+    // next batch's assembly (FP64-bound) fit beside the matvec (HBM-bound)
+    mv_grid = (unsigned)std::max(1L, std::min((long)max_tiles,
+                                              (long)ctx->sm_count * (nbuf > 1 ? 4 : 8)));
+    const size_t Bz = (size_t)B, mz = Bz * sizeof(M) * np * np;
     size_t sz[] = {Bz * sizeof(Slot), sizeof(Ctl), sizeof(int4) * (size_t)max_tiles,
-                   2 * Bz * sizeof(BatchMat), Bz * sizeof(M) * np * np, Bz * sizeof(M) * np * np,
+                   2 * Bz * nbuf * sizeof(BatchMat), mz, mz, nbuf > 1 ? mz : 0, nbuf > 1 ? mz : 0,
                    Bz * sizeof(double2) * np, Bz * sizeof(double2) * np, Bz * sizeof(double2) * np,
                    Bz * sizeof(double2) * nsm * np, Bz * sizeof(V) * vslot, Bz * sizeof(V) * m2,
                    Bz * sizeof(double2) * nblk * m2, Bz * sizeof(double2) * m2,
@@ -622,8 +629,10 @@ template <typename M, typename V> struct Class {
     ctl = (Ctl *)take(sz[i++]);
     tiles = (int4 *)take(sz[i++]);
     mats = (BatchMat *)take(sz[i++]);
-    Sff = (M *)take(sz[i++]);
-    Ssh = (M *)take(sz[i++]);
+    Sff[0] = (M *)take(sz[i++]);
+    Ssh[0] = (M *)take(sz[i++]);
+    Sff[1] = (M *)take(sz[i++]);
+    Ssh[1] = (M *)take(sz[i++]);
     b = (double2 *)take(sz[i++]);
     x = (double2 *)take(sz[i++]);
     r = (double2 *)take(sz[i++]);
@@ -642,13 +651,15 @@ template <typename M, typename V> struct Class {
     if(cudaMallocHost(&h_st, Bz * sizeof(Slot)) != cudaSuccess ||
        cudaMallocHost(&h_ctl, sizeof(Ctl)) != cudaSuccess ||
        cudaMallocHost(&h_tiles, sizeof(int4) * (size_t)max_tiles) != cudaSuccess ||
-       cudaMallocHost(&h_mats, 2 * Bz * sizeof(BatchMat)) != cudaSuccess ||
+       cudaMallocHost(&h_mats, 2 * Bz * nbuf * sizeof(BatchMat)) != cudaSuccess ||
        cudaMallocHost(&h_xsec, 8 * Bz * sizeof(double)) != cudaSuccess) {
       cudaGetLastError();
       ctx->err = "pinned host staging for the batch";
       return OM_ERR_CUDA;
     }
     cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_asm[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_asm[1], cudaEventDisableTiming);
     ev_aux.resize(ctx->aux.size());
     for(auto &e : ev_aux)
       cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
@@ -669,6 +680,8 @@ template <typename M, typename V> struct Class {
     if(h_mats) cudaFreeHost(h_mats);
     if(h_xsec) cudaFreeHost(h_xsec);
     if(ev_main) cudaEventDestroy(ev_main);
+    for(auto &e : ev_asm)
+      if(e) cudaEventDestroy(e);
     for(auto &e : ev_aux)
       if(e) cudaEventDestroy(e);
   }
@@ -858,72 +871,95 @@ void join(om_context *ctx, cudaEvent_t ev_main, const std::vector<cudaEvent_t> &
   }
 }
 
-// One batch of nb requests (indices idx[b0 ..]) of a size class; the
-// problems it creates are left in `pr` for the caller to destroy. Request s
-// lives on auxiliary context s % kAux; the batched assembly and solves run
-// on the main stream.
+// A batch between its set-up and its results.
+struct Pending {
+  std::vector<om_problem *> pr;  // per slot; null where set-up failed
+  size_t b0 = 0;                 // first request (index into the class's list)
+  int nb = 0;                    // requests
+  int buf = 0;                   // matrix buffer
+  double t0 = 0;                 // host time when its set-up started
+};
+
+// Set-up of a batch and its assembly: request s lives on auxiliary context
+// s % kAux (per-sphere terms, incident coefficients, source vector); then one
+// launch on the low-priority stream assembles the FF and SH matrices of every
+// request into matrix buffer `buf`, so that it can overlap the solves of the
+// previous batch on the main stream.
 template <typename M, typename V>
-int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::vector<int> &idx,
-              size_t b0, int nb, const om_request *reqs, om_result *out, double t_call,
-              std::vector<om_problem *> &pr, long *launches) {
+void prepare_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::vector<int> &idx,
+                   const om_request *reqs, om_result *out, double t_call, Pending &P, long *launches) {
+  const long np = cl.np;
+  P.t0 = now_ms();
+  P.pr.assign(P.nb, nullptr);
+  for(int s = 0; s < P.nb; ++s) {
+    const om_request &rq = reqs[idx[P.b0 + s]];
+    om_result &res = out[idx[P.b0 + s]];
+    res.slot = s;
+    res.queue_ms = P.t0 - t_call;
+    om_context *a = ctx->aux[s % kAux];
+    int r = om_problem_create(a, rq.spheres, rq.n_spheres, &rq.background, &rq.wave, &P.pr[s]);
+    *launches += a->last_launches;
+    if(r) {
+      res.status = r;
+      ctx->err = a->err;
+      P.pr[s] = nullptr;
+      continue;
+    }
+    const int L0 = a->last_launches;
+    launch_source(P.pr[s]);
+    *launches += a->last_launches - L0;
+    P.pr[s]->have_source = true;
+  }
+  for(size_t q = 0; q < ctx->aux.size(); ++q) {
+    cudaEventRecord(cl.ev_aux[q], ctx->aux[q]->stream);
+    cudaStreamWaitEvent(ctx->stream_lo, cl.ev_aux[q], 0);
+  }
+  // FF matrices in entries 0 .. B-1, SH in B .. 2B-1 of this buffer's table
+  BatchMat *hm = cl.h_mats + (size_t)2 * cl.B * P.buf;
+  for(int e = 0; e < 2 * cl.B; ++e)
+    hm[e] = BatchMat{nullptr, nullptr, nullptr, 0, mk(0.0, 0.0), 0};
+  bool any_sh = false;
+  for(int s = 0; s < P.nb; ++s) {
+    om_problem *p = P.pr[s];
+    if(!p)
+      continue;
+    const cplx k = p->waveK;
+    hm[s] = BatchMat{p->d_cart, p->d_T, cl.Sff[P.buf] + (size_t)s * np * np, p->n, mk(k.real(), k.imag()),
+                     p->N};
+    if(reqs[idx[P.b0 + s]].wave.sh) {
+      any_sh = true;
+      const cplx k2 = 2.0 * k;
+      hm[cl.B + s] = BatchMat{p->d_cart, p->d_Tsh, cl.Ssh[P.buf] + (size_t)s * np * np, p->n,
+                              mk(k2.real(), k2.imag()), p->N};
+    }
+  }
+  const int nmats = any_sh ? 2 * cl.B : cl.B;
+  BatchMat *dm = cl.mats + (size_t)2 * cl.B * P.buf;
+  cudaMemcpyAsync(dm, hm, sizeof(BatchMat) * nmats, cudaMemcpyHostToDevice, ctx->stream_lo);
+  const int L0 = ctx->last_launches;
+  launch_assemble_batch(ctx, key.nmax, key.precision, dm, nmats, (int)((long)key.Npad * (key.Npad + 1) / 2),
+                        ctx->stream_lo);
+  *launches += ctx->last_launches - L0;
+  cudaEventRecord(cl.ev_asm[P.buf], ctx->stream_lo);
+}
+
+// The FF solves, the SH sources, the SH solves and the cross sections of a
+// prepared batch.
+template <typename M, typename V>
+int finish_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::vector<int> &idx,
+                 const om_request *reqs, om_result *out, double t_call, Pending &P, long *launches) {
   const bool mixed = key.precision == OM_C64;
   const long np = cl.np;
-  const size_t per = Class<M, V>::slot_bytes(np, key.m);
-  const double t0 = now_ms();
-  int rc = OM_OK;
+  const size_t per = Class<M, V>::slot_bytes(np, key.m, cl.nbuf);
+  std::vector<om_problem *> &pr = P.pr;
+  const int nb = P.nb;
   auto actx = [&](int s) { return ctx->aux[s % kAux]; };
   auto tracked = [&](om_context *c, auto &&fn) {
     const int L0 = c->last_launches;
     fn();
     *launches += c->last_launches - L0;
   };
-  auto fail = [&](int s, int r) {
-    om_result &res = out[idx[b0 + s]];
-    if(res.status == OM_OK || res.status == OM_ERR_NOT_CONVERGED)
-      res.status = r;
-    ctx->err = actx(s)->err;
-  };
-  // set-up: per-sphere terms, incident coefficients, source vector
-  for(int s = 0; s < nb; ++s) {
-    const om_request &rq = reqs[idx[b0 + s]];
-    om_result &res = out[idx[b0 + s]];
-    res.slot = s;
-    res.queue_ms = t0 - t_call;
-    om_context *a = actx(s);
-    int r = om_problem_create(a, rq.spheres, rq.n_spheres, &rq.background, &rq.wave, &pr[s]);
-    *launches += a->last_launches;
-    if(r) {
-      fail(s, r);
-      pr[s] = nullptr;
-      continue;
-    }
-    tracked(a, [&] { launch_source(pr[s]); });
-    pr[s]->have_source = true;
-  }
-  join(ctx, cl.ev_main, cl.ev_aux, false);
-  // one assembly launch: FF matrices in entries 0 .. B-1, SH in B .. 2B-1
-  const long per_mat = (long)key.Npad * (key.Npad + 1) / 2;
-  bool any_sh = false;
-  for(int e = 0; e < 2 * cl.B; ++e)
-    cl.h_mats[e] = BatchMat{nullptr, nullptr, nullptr, 0, mk(0.0, 0.0), 0};
-  for(int s = 0; s < nb; ++s) {
-    if(!pr[s])
-      continue;
-    const cplx k = pr[s]->waveK;
-    cl.h_mats[s] = BatchMat{pr[s]->d_cart, pr[s]->d_T, cl.Sff + (size_t)s * np * np, pr[s]->n,
-                            mk(k.real(), k.imag()), pr[s]->N};
-    if(reqs[idx[b0 + s]].wave.sh) {
-      any_sh = true;
-      const cplx k2 = 2.0 * k;
-      cl.h_mats[cl.B + s] = BatchMat{pr[s]->d_cart, pr[s]->d_Tsh, cl.Ssh + (size_t)s * np * np,
-                                     pr[s]->n, mk(k2.real(), k2.imag()), pr[s]->N};
-    }
-  }
-  const int nmats = any_sh ? 2 * cl.B : cl.B;
-  cudaMemcpyAsync(cl.mats, cl.h_mats, sizeof(BatchMat) * nmats, cudaMemcpyHostToDevice, ctx->stream);
-  tracked(ctx, [&] {
-    launch_assemble_batch(ctx, key.nmax, key.precision, cl.mats, nmats, (int)per_mat, ctx->stream);
-  });
+  cudaStreamWaitEvent(ctx->stream, cl.ev_asm[P.buf], 0);
   // FF systems
   for(int s = 0; s < cl.B; ++s) {
     Slot z{};
@@ -931,7 +967,7 @@ int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::
     z.xzero = 1;
     if(s < nb && pr[s]) {
       z.n = pr[s]->n;
-      z.S = cl.Sff + (size_t)s * np * np;
+      z.S = cl.Sff[P.buf] + (size_t)s * np * np;
       z.outer = 1;
       cudaMemcpyAsync(cl.b + (size_t)s * np, pr[s]->d_Q, sizeof(double2) * z.n,
                       cudaMemcpyDeviceToDevice, ctx->stream);
@@ -939,7 +975,7 @@ int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::
     cl.h_st[s] = z;
   }
   const double ts = now_ms();
-  rc = cl.solve(launches);
+  int rc = cl.solve(launches);
   const double t_ff = (now_ms() - ts) * 1e-3;
   if(rc)
     return rc;
@@ -949,7 +985,7 @@ int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::
   for(int s = 0; s < nb; ++s) {
     if(!pr[s])
       continue;
-    om_result &res = out[idx[b0 + s]];
+    om_result &res = out[idx[P.b0 + s]];
     fill_stats(ff[s], mixed, t_ff, &res.ff);
     res.status = ff[s].status;
     om_context *a = actx(s);
@@ -960,10 +996,11 @@ int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::
       launch_cross_sections(pr[s]);
     });
     pr[s]->have_solution = true;
-    if(reqs[idx[b0 + s]].wave.sh) {
+    if(reqs[idx[P.b0 + s]].wave.sh) {
       int r = sh_alloc(pr[s]);
       if(r) {
-        fail(s, r);
+        res.status = r;
+        ctx->err = a->err;
         continue;
       }
       tracked(a, [&] { launch_sh_source(pr[s]); });
@@ -976,9 +1013,9 @@ int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::
     Slot z{};
     z.bnorm = -1.0;
     z.xzero = 1;
-    if(s < nb && pr[s] && reqs[idx[b0 + s]].wave.sh && pr[s]->d_K && pr[s]->d_acs) {
+    if(s < nb && pr[s] && reqs[idx[P.b0 + s]].wave.sh && pr[s]->d_K && pr[s]->d_acs) {
       z.n = pr[s]->n;
-      z.S = cl.Ssh + (size_t)s * np * np;
+      z.S = cl.Ssh[P.buf] + (size_t)s * np * np;
       z.outer = 1;
       run = true;
       cudaMemcpyAsync(cl.b + (size_t)s * np, pr[s]->d_K, sizeof(double2) * z.n,
@@ -1002,7 +1039,7 @@ int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::
       continue;
     om_context *a = actx(s);
     if(run && cl.h_st[s].n) {
-      om_result &res = out[idx[b0 + s]];
+      om_result &res = out[idx[P.b0 + s]];
       fill_stats(cl.h_st[s], mixed, t_sh, &res.sh);
       if(res.status == OM_OK)
         res.status = cl.h_st[s].status;
@@ -1026,15 +1063,15 @@ int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::
     e = cudaGetLastError();
   const double t_end = now_ms();
   for(int s = 0; s < nb; ++s) {
-    om_result &res = out[idx[b0 + s]];
+    om_result &res = out[idx[P.b0 + s]];
     if(pr[s]) {
       for(int q = 0; q < 4; ++q)
         res.xsec[q] = hx[8 * s + q];
-      if(reqs[idx[b0 + s]].wave.sh)
+      if(reqs[idx[P.b0 + s]].wave.sh)
         for(int q = 0; q < 2; ++q)
           res.xsec_sh[q] = hx[8 * s + 4 + q];
     }
-    res.service_ms = t_end - t0;
+    res.service_ms = t_end - P.t0;
     res.latency_ms = t_end - t_call;
     res.device_bytes = per;
   }
@@ -1045,11 +1082,13 @@ int run_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const std::
   return OM_OK;
 }
 
+// The requests idx of one size class, in batches of B slots; with more than
+// one batch, the next batch's set-up and assembly are issued before the
+// current batch's solves (two matrix buffers).
 template <typename M, typename V>
 int run_class(om_context *ctx, const ClassKey &key, const std::vector<int> &idx, const om_request *reqs,
               om_result *out, size_t arena, double t_call, long *launches) {
   const long np = (long)rup((size_t)2 * pmax(key.nmax) * key.Npad);
-  const size_t per = Class<M, V>::slot_bytes(np, key.m);
   // tables the auxiliary contexts share, ready before their streams use them
   int rc = aux_contexts(ctx);
   if(rc)
@@ -1057,32 +1096,65 @@ int run_class(om_context *ctx, const ClassKey &key, const std::vector<int> &idx,
   coef_tables(ctx, key.nmax);
   clg_tables_dev(ctx, key.nmax);
   cudaStreamSynchronize(ctx->stream);
-  int B = (int)std::min<size_t>({idx.size(), (size_t)kMaxSlots, std::max<size_t>(1, arena / per)});
+  const size_t count = idx.size();
+  auto slots_for = [&](int nbuf) {
+    return (int)std::min<size_t>({count, (size_t)kMaxSlots,
+                                  std::max<size_t>(1, arena / Class<M, V>::slot_bytes(np, key.m, nbuf))});
+  };
+  int nbuf = (size_t)slots_for(1) < count ? 2 : 1;
+  int B = slots_for(nbuf);
   Class<M, V> *cl = nullptr;
   for(;;) {
     cl = new Class<M, V>();
-    rc = cl->init(ctx, key, B);
+    rc = cl->init(ctx, key, B, nbuf);
     if(!rc)
       break;
     delete cl;
     cl = nullptr;
-    if(rc != OM_ERR_BUDGET || B == 1)
+    if(rc != OM_ERR_BUDGET || (B == 1 && nbuf == 1))
       break;
-    B = (B + 1) / 2;
+    if(B == 1)
+      nbuf = 1;
+    else
+      B = (B + 1) / 2;
   }
   if(!cl) {
     for(int i : idx)
       out[i].status = rc;
     return OM_OK;
   }
-  for(size_t b0 = 0; b0 < idx.size() && !rc; b0 += B) {
-    const int nb = (int)std::min<size_t>(B, idx.size() - b0);
-    std::vector<om_problem *> pr(nb, nullptr);
-    rc = run_batch(ctx, key, *cl, idx, b0, nb, reqs, out, t_call, pr, launches);
-    for(om_problem *p : pr)
+  std::vector<Pending> pend;
+  for(size_t b0 = 0; b0 < count; b0 += B) {
+    Pending P;
+    P.b0 = b0;
+    P.nb = (int)std::min<size_t>(B, count - b0);
+    P.buf = (int)(pend.size() % cl->nbuf);
+    pend.push_back(P);
+  }
+  auto destroy = [](Pending &P) {
+    for(om_problem *p : P.pr)
       if(p)
         om_problem_destroy(p);
+    P.pr.clear();
+  };
+  if(!pend.empty())
+    prepare_batch(ctx, key, *cl, idx, reqs, out, t_call, pend[0], launches);
+  for(size_t k = 0; k < pend.size(); ++k) {
+    if(!rc && k + 1 < pend.size() && cl->nbuf > 1)
+      prepare_batch(ctx, key, *cl, idx, reqs, out, t_call, pend[k + 1], launches);
+    if(!rc)
+      rc = finish_batch(ctx, key, *cl, idx, reqs, out, t_call, pend[k], launches);
+    if(rc) {  // device error: wait for what is in flight before freeing
+      cudaStreamSynchronize(ctx->stream_lo);
+      cudaStreamSynchronize(ctx->stream);
+    }
+    destroy(pend[k]);
+    if(!rc && k + 1 < pend.size() && cl->nbuf == 1)
+      prepare_batch(ctx, key, *cl, idx, reqs, out, t_call, pend[k + 1], launches);
   }
+  for(auto &P : pend)
+    destroy(P);
+  cudaStreamSynchronize(ctx->stream_lo);
   delete cl;
   return rc;
 }

@@ -569,6 +569,11 @@ void om_context_destroy(om_context *ctx) {
   }
   for(auto &t : ctx->clg)
     cudaFree(t.second);
+  for(auto &t : ctx->clgc) {
+    cudaFree(t.off);
+    cudaFree(t.pq);
+    cudaFree(t.val);
+  }
   if(ctx->mark)
     cudaEventDestroy(ctx->mark);
   cudaEventDestroy(ctx->ev_fork);

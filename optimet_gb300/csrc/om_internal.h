@@ -85,6 +85,18 @@ struct BatchMat {
 };
 struct BatchClass;
 
+// The SH coupling tables in compact form (sh.cu): for SH harmonic k the pairs
+// (p, q) with m_p + m_q = M_k, n_q >= |m_q|, in the order p ascending, n_q
+// ascending (entries off[k] .. off[k+1]-1 of pq), and the nine coefficients
+// of each pair (val[t * count + e], t = table).
+struct ClgCompact {
+  int nmax = -1;
+  long count = 0;
+  int *off = nullptr;
+  int2 *pq = nullptr;
+  double *val = nullptr;
+};
+
 }  // namespace om
 
 struct om_context {
@@ -106,6 +118,7 @@ struct om_context {
   std::string err;
   std::vector<om::CoefTables> tables;  // by nmax
   std::vector<std::pair<int, double *>> clg;  // SH coupling tables by nmax
+  std::vector<om::ClgCompact> clgc;           // their compact forms
   int last_launches = 0;               // kernels launched by the last API call
   // kernel timers (CUDA events on `stream`), reset by om_context_timers
   bool timing = false;

@@ -89,7 +89,7 @@ __device__ __noinline__ double Wf(const double *f, int L1, int J1, int M1, int L
          w6j(f, L1, L2, L, J2, J1, 1) * cg(f, L, 0, L1, 0, L2, 0) * cg(f, L, M, J1, M1, J2, M2);
 }
 
-__device__ __forceinline__ void nm_of(int p, int &n, int &m) {
+__host__ __device__ __forceinline__ void nm_of(int p, int &n, int &m) {
   n = (int)sqrtf((float)(p + 1));
   while(n * n > p + 1)
     --n;
@@ -195,48 +195,68 @@ __global__ void k_sh_vectors(const ShScalars *shs, const zd *Xint, int nmax, zd 
 }
 
 // u', v', u'' per (sphere, SH harmonic) and K, K1ana (source_vectorSH, K1ana).
-__global__ void __launch_bounds__(256) k_sh_source(const ShScalars *shs, const zd *vec,
-                                                   const double *tab, const zd *shf, int nmax,
-                                                   zd *K, zd *K1) {
+// One CTA per sphere, one warp per SH harmonic k at a time: the lanes walk
+// k's (p, q) pairs of the compact coupling table (coalesced), each keeping
+// partial sums of the bilinear forms, which a warp reduction combines.
+__global__ void __launch_bounds__(256) k_sh_source(const ShScalars *shs, const zd *vec, const int *off,
+                                                   const int2 *pq, const double *val, long count,
+                                                   const zd *shf, int nmax, zd *K, zd *K1) {
   extern __shared__ zd sv[];
   const int j = blockIdx.x, P = pmax(nmax);
-  const size_t sz = (size_t)P * P * P;
   for(int t = threadIdx.x; t < 3 * P; t += blockDim.x)
     sv[t] = vec[(size_t)j * 3 * P + t];
   __syncthreads();
   const zd *a0 = sv, *a1 = sv + P, *am1 = sv + 2 * P;
   const ShScalars c = shs[j];
-  for(int k = threadIdx.x; k < P; k += blockDim.x) {
-    int J, M;
-    nm_of(k, J, M);
+  const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  for(int k = threadIdx.x >> 5; k < P; k += warps) {
     zd up = mk(0, 0), vp = mk(0, 0), gmn = mk(0, 0), fmn = mk(0, 0);
-    for(int p = 0; p < P; ++p) {
-      int n1, m1;
-      nm_of(p, n1, m1);
-      const int m2 = M - m1;
-      if(m2 < -nmax || m2 > nmax)
-        continue;
-      for(int n2 = max(1, abs(m2)); n2 <= nmax; ++n2) {
-        const int q = flat(n2, m2);
-        const size_t at = ((size_t)k * P + p) * P + q;
-        const zd a1am = a1[p] * am1[q], a0am = a0[p] * am1[q];
-        up = up + a1am * tab[T_C10m1 * sz + at] + a0am * tab[T_C11m1 * sz + at];
-        vp = vp + a1am * tab[T_C00m1 * sz + at] + a0am * tab[T_C01m1 * sz + at];
-        gmn = gmn + am1[p] * am1[q] * tab[T_Wm1m1 * sz + at];
-        fmn = fmn + a1[p] * a1[q] * tab[T_W11 * sz + at] + a0[p] * a0[q] * tab[T_W00 * sz + at] +
-              a1[p] * a0[q] * tab[T_W10 * sz + at] + a0[p] * a1[q] * tab[T_W01 * sz + at];
-      }
+    for(int t = off[k] + lane; t < off[k + 1]; t += 32) {
+      const int p = pq[t].x, q = pq[t].y;
+      const double *v = val + t;
+      const zd a1am = a1[p] * am1[q], a0am = a0[p] * am1[q];
+      up = up + a1am * v[T_C10m1 * count] + a0am * v[T_C11m1 * count];
+      vp = vp + a1am * v[T_C00m1 * count] + a0am * v[T_C01m1 * count];
+      gmn = gmn + am1[p] * am1[q] * v[T_Wm1m1 * count];
+      fmn = fmn + a1[p] * a1[q] * v[T_W11 * count] + a0[p] * a0[q] * v[T_W00 * count] +
+            a1[p] * a0[q] * v[T_W10 * count] + a0[p] * a1[q] * v[T_W01 * count];
     }
-    const double snn = sqrt((double)(J * (J + 1)));
-    const zd u1 = up * c.c_up, v1 = vp * c.c_vp;
-    const zd u2 = (c.c_g1 * snn) * gmn + (c.c_g2 * snn) * (gmn + fmn);
-    const zd *f = shf + ((size_t)j * (nmax + 1) + J) * 8;
-    const size_t o = (size_t)j * 2 * P;
-    K[o + k] = f[0] * v1;               // + T2_TE * v'' (v'' = 0, Geometry.cpp:296)
-    K[o + P + k] = f[1] * u1 + f[3] * u2;
-    K1[o + k] = mk(0.0, 0.0);           // IauxSH2_TE * v''
-    K1[o + P + k] = f[7] * u2;
+    for(int o = 16; o > 0; o >>= 1) {
+      up.re += __shfl_down_sync(0xffffffffu, up.re, o);
+      up.im += __shfl_down_sync(0xffffffffu, up.im, o);
+      vp.re += __shfl_down_sync(0xffffffffu, vp.re, o);
+      vp.im += __shfl_down_sync(0xffffffffu, vp.im, o);
+      gmn.re += __shfl_down_sync(0xffffffffu, gmn.re, o);
+      gmn.im += __shfl_down_sync(0xffffffffu, gmn.im, o);
+      fmn.re += __shfl_down_sync(0xffffffffu, fmn.re, o);
+      fmn.im += __shfl_down_sync(0xffffffffu, fmn.im, o);
+    }
+    if(lane == 0) {
+      int J, M;
+      nm_of(k, J, M);
+      const double snn = sqrt((double)(J * (J + 1)));
+      const zd u1 = up * c.c_up, v1 = vp * c.c_vp;
+      const zd u2 = (c.c_g1 * snn) * gmn + (c.c_g2 * snn) * (gmn + fmn);
+      const zd *f = shf + ((size_t)j * (nmax + 1) + J) * 8;
+      const size_t o = (size_t)j * 2 * P;
+      K[o + k] = f[0] * v1;               // + T2_TE * v'' (v'' = 0, Geometry.cpp:296)
+      K[o + P + k] = f[1] * u1 + f[3] * u2;
+      K1[o + k] = mk(0.0, 0.0);           // IauxSH2_TE * v''
+      K1[o + P + k] = f[7] * u2;
+    }
   }
+}
+
+// Gathers the compact table's coefficients from the dense tables.
+__global__ void k_clg_compact(const double *tab, int P, const int2 *pq, const int *kof, long count,
+                              double *val) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(t >= count)
+    return;
+  const size_t sz = (size_t)P * P * P;
+  const size_t at = ((size_t)kof[t] * P + pq[t].x) * P + pq[t].y;
+  for(int e = 0; e < 9; ++e)
+    val[e * count + t] = tab[e * sz + at];
 }
 
 // convertInternal_SH (Solver.cpp:95-116)
@@ -552,14 +572,70 @@ const double *clg_tables_dev(om_context *ctx, int nmax) {
   return d;
 }
 
+// The compact form of the SH coupling tables for nmax (cached per context;
+// a context with a parent uses the parent's, finished before it returns).
+const ClgCompact &clg_compact_dev(om_context *ctx, int nmax) {
+  if(ctx->parent) {
+    bool cached = false;
+    for(auto &t : ctx->parent->clgc)
+      cached |= t.nmax == nmax;
+    const ClgCompact &c = clg_compact_dev(ctx->parent, nmax);
+    if(!cached)
+      cudaStreamSynchronize(ctx->parent->stream);
+    return c;
+  }
+  for(auto &t : ctx->clgc)
+    if(t.nmax == nmax)
+      return t;
+  const double *tab = clg_tables_dev(ctx, nmax);
+  const int P = pmax(nmax);
+  std::vector<int> off(P + 1, 0), kof;
+  std::vector<int2> pq;
+  for(int k = 0; k < P; ++k) {
+    int J, M;
+    nm_of(k, J, M);
+    off[k] = (int)pq.size();
+    for(int p = 0; p < P; ++p) {
+      int n1, m1;
+      nm_of(p, n1, m1);
+      const int m2 = M - m1;
+      if(m2 < -nmax || m2 > nmax)
+        continue;
+      for(int n2 = std::max(1, std::abs(m2)); n2 <= nmax; ++n2) {
+        pq.push_back(make_int2(p, flat(n2, m2)));
+        kof.push_back(k);
+      }
+    }
+  }
+  off[P] = (int)pq.size();
+  ClgCompact c;
+  c.nmax = nmax;
+  c.count = (long)pq.size();
+  int *d_kof = nullptr;
+  if(cudaMalloc(&c.off, sizeof(int) * (P + 1)) != cudaSuccess ||
+     cudaMalloc(&c.pq, sizeof(int2) * pq.size()) != cudaSuccess ||
+     cudaMalloc(&c.val, sizeof(double) * 9 * pq.size()) != cudaSuccess ||
+     cudaMalloc(&d_kof, sizeof(int) * kof.size()) != cudaSuccess)
+    throw std::runtime_error("cudaMalloc failed for the compact SH coupling tables");
+  cudaMemcpy(c.off, off.data(), sizeof(int) * (P + 1), cudaMemcpyHostToDevice);
+  cudaMemcpy(c.pq, pq.data(), sizeof(int2) * pq.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_kof, kof.data(), sizeof(int) * kof.size(), cudaMemcpyHostToDevice);
+  k_clg_compact<<<blocks_for(c.count, 256), 256, 0, ctx->stream>>>(tab, P, c.pq, d_kof, c.count, c.val);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_kof);
+  ctx->last_launches++;
+  ctx->clgc.push_back(c);
+  return ctx->clgc.back();
+}
+
 void launch_sh_source(om_problem *pr) {
   om_context *ctx = pr->ctx;
-  const double *tab = clg_tables_dev(ctx, pr->nmax);
+  const ClgCompact c = clg_compact_dev(ctx, pr->nmax);
   const int P = pr->P;
   k_sh_vectors<<<pr->N, 128, 0, ctx->stream>>>(pr->d_shs, pr->d_Xint, pr->nmax, pr->d_shvec);
-  k_sh_source<<<pr->N, 256, 3 * P * sizeof(zd), ctx->stream>>>(pr->d_shs, pr->d_shvec, tab,
-                                                               pr->d_shf, pr->nmax, pr->d_K,
-                                                               pr->d_K1);
+  k_sh_source<<<pr->N, 256, 3 * P * sizeof(zd), ctx->stream>>>(pr->d_shs, pr->d_shvec, c.off, c.pq,
+                                                               c.val, c.count, pr->d_shf, pr->nmax,
+                                                               pr->d_K, pr->d_K1);
   ctx->last_launches += 2;
 }
 

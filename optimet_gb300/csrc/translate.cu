@@ -785,71 +785,79 @@ __global__ void __launch_bounds__(256) k_coupling(CouplingArgs a, Layout y) {
 }
 
 // Per sphere and n: T-matrix (FF, SH), internal factors and the Mie
-// absorption factors (Scatterer.cpp:39-271, Geometry.cpp:86-145).
-__global__ void k_sphere_terms(const SphereScalars *sc, int N, int nmax, zd *T, zd *Tsh, zd *iaux,
-                               double *cabs_out, zd *shf) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// absorption factors (Scatterer.cpp:39-271, Geometry.cpp:86-145). One CTA
+// per sphere: six threads evaluate the Bessel sequences j(r0), j(rho r0),
+// h(r0) of both harmonics side by side, then one thread per (harmonic, n)
+// forms that order's factors.
+__global__ void __launch_bounds__(64) k_sphere_terms(const SphereScalars *sc, int N, int nmax, zd *T,
+                                                     zd *Tsh, zd *iaux, double *cabs_out, zd *shf) {
+  __shared__ zd Bv[2][3][kMaxNmax + 2], dBv[2][3][kMaxNmax + 2];
+  const int i = blockIdx.x;
   if(i >= N)
     return;
   const SphereScalars c = sc[i];
-  for(int h = 0; h < 2; ++h) {
-    const zd r0 = h ? c.r0_sh : c.r0, rho = h ? c.rho_sh : c.rho,
-             mu_sob = h ? c.mu_sob_sh : c.mu_sob;
-    zd J[kMaxNmax + 2], dJ[kMaxNmax + 2], Jr[kMaxNmax + 2], dJr[kMaxNmax + 2], H[kMaxNmax + 2],
-        dH[kMaxNmax + 2];
-    bessel_deriv(0, r0, nmax, J, dJ);
-    bessel_deriv(0, rho * r0, nmax, Jr, dJr);
-    bessel_deriv(1, r0, nmax, H, dH);
+  if(threadIdx.x < 6) {
+    const int h = threadIdx.x / 3, w = threadIdx.x % 3;
+    const zd r0 = h ? c.r0_sh : c.r0, rho = h ? c.rho_sh : c.rho;
+    bessel_deriv(w == 2 ? 1 : 0, w == 1 ? rho * r0 : r0, nmax, Bv[h][w], dBv[h][w]);
+  }
+  __syncthreads();
+  for(int t = threadIdx.x; t < 2 * (nmax + 1); t += blockDim.x) {
+    const int h = t / (nmax + 1), n = t % (nmax + 1);
     zd *Tout = (h ? Tsh : T) + (size_t)i * 2 * (nmax + 1);
-    Tout[0] = mk(0.0, 0.0);
-    Tout[1] = mk(0.0, 0.0);
-    for(int n = 1; n <= nmax; ++n) {
-      zd psi = r0 * J[n];
-      zd dpsi = r0 * dJ[n] + J[n];
-      zd ksi = r0 * H[n];
-      zd dksi = r0 * dH[n] + H[n];
-      zd psirho = r0 * rho * Jr[n];
-      zd dpsirho = r0 * rho * dJr[n] + Jr[n];
-      zd TE = (psi / ksi) * (mu_sob * dpsi / psi - rho * dpsirho / psirho) /
-              (rho * dpsirho / psirho - mu_sob * dksi / ksi);
-      zd TM = (psi / ksi) * (mu_sob * dpsirho / psirho - rho * dpsi / psi) /
-              (rho * dksi / ksi - mu_sob * dpsirho / psirho);
-      Tout[2 * n] = TE;
-      Tout[2 * n + 1] = TM;
-      if(h == 1 && shf) {
-        // getTLocalSH1_outer / SH2_outer / getIauxSH1 / getIauxSH2 (Scatterer.cpp:163-412)
-        const zd x_b2 = c.x_b2, x_i2 = c.x_i2, z = c.zeta;
-        zd *f = shf + ((size_t)i * (nmax + 1) + n) * 8;
-        const zd den_te = z * ksi * dpsirho - psirho * dksi;
-        const zd den_tm = z * psirho * dksi - ksi * dpsirho;
-        f[0] = -(x_b2 * psirho) / den_te;
-        f[1] = -(x_b2 * dpsirho) / den_tm;
-        f[2] = z * x_b2 * dpsirho / den_te;
-        f[3] = z * x_b2 * psirho / den_tm;
-        const zd i1te = (-x_i2 * ksi) / (x_b2 * psirho);
-        const zd i1tm = (-x_i2 * dksi) / (x_b2 * dpsirho);
-        f[4] = i1te;
-        f[5] = i1tm;
-        const zd bnpp = (z * x_b2 * dpsirho) / den_te;
-        const zd anpp = (z * x_b2 * psirho) / den_tm;
-        f[6] = bnpp * ((-x_i2 * ksi) / (x_b2 * psirho) + (x_i2 * dksi) / (z * x_b2 * dpsirho));
-        f[7] = anpp * ((-x_i2 * dksi) / (x_b2 * dpsirho) + (x_i2 * ksi) / (z * x_b2 * psirho));
-      }
-      if(h == 0) {
-        const zd mu_j = c.mu_j, mu_0 = c.mu_0, I = mk(0.0, 1.0);
-        zd ia_te = (mu_j * rho) / (mu_0 * rho * dpsirho * psi - mu_j * psirho * dpsi) * I;
-        zd ia_tm = (mu_j * rho) / (mu_j * psi * dpsirho - mu_0 * rho * psirho * dpsi) * I;
-        iaux[(size_t)i * 2 * (nmax + 1) + 2 * n] = ia_te;
-        iaux[(size_t)i * 2 * (nmax + 1) + 2 * n + 1] = ia_tm;
-        zd t1 = I * rho * mu_0 * conj(mu_j) * conj(psirho) * dpsirho;
-        double t2 = cabs(mu_j * psirho * dpsi - mu_0 * rho * dpsirho * psi);
-        t2 *= t2;
-        cabs_out[(size_t)i * 2 * (nmax + 1) + 2 * n] = t1.re / t2;
-        t1 = I * conj(rho) * mu_0 * mu_j * conj(psirho) * dpsirho;
-        t2 = cabs(mu_0 * rho * psirho * dpsi - mu_j * dpsirho * psi);
-        t2 *= t2;
-        cabs_out[(size_t)i * 2 * (nmax + 1) + 2 * n + 1] = t1.re / t2;
-      }
+    if(n == 0) {
+      Tout[0] = mk(0.0, 0.0);
+      Tout[1] = mk(0.0, 0.0);
+      continue;
+    }
+    const zd r0 = h ? c.r0_sh : c.r0, rho = h ? c.rho_sh : c.rho, mu_sob = h ? c.mu_sob_sh : c.mu_sob;
+    const zd *J = Bv[h][0], *dJ = dBv[h][0], *Jr = Bv[h][1], *dJr = dBv[h][1], *H = Bv[h][2],
+             *dH = dBv[h][2];
+    zd psi = r0 * J[n];
+    zd dpsi = r0 * dJ[n] + J[n];
+    zd ksi = r0 * H[n];
+    zd dksi = r0 * dH[n] + H[n];
+    zd psirho = r0 * rho * Jr[n];
+    zd dpsirho = r0 * rho * dJr[n] + Jr[n];
+    zd TE = (psi / ksi) * (mu_sob * dpsi / psi - rho * dpsirho / psirho) /
+            (rho * dpsirho / psirho - mu_sob * dksi / ksi);
+    zd TM = (psi / ksi) * (mu_sob * dpsirho / psirho - rho * dpsi / psi) /
+            (rho * dksi / ksi - mu_sob * dpsirho / psirho);
+    Tout[2 * n] = TE;
+    Tout[2 * n + 1] = TM;
+    if(h == 1 && shf) {
+      // getTLocalSH1_outer / SH2_outer / getIauxSH1 / getIauxSH2 (Scatterer.cpp:163-412)
+      const zd x_b2 = c.x_b2, x_i2 = c.x_i2, z = c.zeta;
+      zd *f = shf + ((size_t)i * (nmax + 1) + n) * 8;
+      const zd den_te = z * ksi * dpsirho - psirho * dksi;
+      const zd den_tm = z * psirho * dksi - ksi * dpsirho;
+      f[0] = -(x_b2 * psirho) / den_te;
+      f[1] = -(x_b2 * dpsirho) / den_tm;
+      f[2] = z * x_b2 * dpsirho / den_te;
+      f[3] = z * x_b2 * psirho / den_tm;
+      const zd i1te = (-x_i2 * ksi) / (x_b2 * psirho);
+      const zd i1tm = (-x_i2 * dksi) / (x_b2 * dpsirho);
+      f[4] = i1te;
+      f[5] = i1tm;
+      const zd bnpp = (z * x_b2 * dpsirho) / den_te;
+      const zd anpp = (z * x_b2 * psirho) / den_tm;
+      f[6] = bnpp * ((-x_i2 * ksi) / (x_b2 * psirho) + (x_i2 * dksi) / (z * x_b2 * dpsirho));
+      f[7] = anpp * ((-x_i2 * dksi) / (x_b2 * dpsirho) + (x_i2 * ksi) / (z * x_b2 * psirho));
+    }
+    if(h == 0) {
+      const zd mu_j = c.mu_j, mu_0 = c.mu_0, I = mk(0.0, 1.0);
+      zd ia_te = (mu_j * rho) / (mu_0 * rho * dpsirho * psi - mu_j * psirho * dpsi) * I;
+      zd ia_tm = (mu_j * rho) / (mu_j * psi * dpsirho - mu_0 * rho * psirho * dpsi) * I;
+      iaux[(size_t)i * 2 * (nmax + 1) + 2 * n] = ia_te;
+      iaux[(size_t)i * 2 * (nmax + 1) + 2 * n + 1] = ia_tm;
+      zd t1 = I * rho * mu_0 * conj(mu_j) * conj(psirho) * dpsirho;
+      double t2 = cabs(mu_j * psirho * dpsi - mu_0 * rho * dpsirho * psi);
+      t2 *= t2;
+      cabs_out[(size_t)i * 2 * (nmax + 1) + 2 * n] = t1.re / t2;
+      t1 = I * conj(rho) * mu_0 * mu_j * conj(psirho) * dpsirho;
+      t2 = cabs(mu_0 * rho * psirho * dpsi - mu_j * dpsirho * psi);
+      t2 *= t2;
+      cabs_out[(size_t)i * 2 * (nmax + 1) + 2 * n + 1] = t1.re / t2;
     }
   }
 }
@@ -1004,7 +1012,7 @@ const CoefTables &coef_tables(om_context *ctx, int nmax) {
 }
 
 void launch_sphere_terms(om_problem *pr) {
-  k_sphere_terms<<<blocks_for(pr->N, 64), 64, 0, pr->ctx->stream>>>(
+  k_sphere_terms<<<pr->N, 64, 0, pr->ctx->stream>>>(
       pr->d_scal, pr->N, pr->nmax, pr->d_T, pr->d_Tsh, pr->d_iaux, pr->d_cabs, pr->d_shf);
   pr->ctx->last_launches++;
 }
