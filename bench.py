@@ -585,6 +585,20 @@ def run_batch(G, ctx, cases, opts, precision, bg):
     return dev_s, res, ctx.last_launches
 
 
+def c3_profile_case(G, mixed, bg):
+    """The small c3 case the ncu captures use: 24 requests with N >= 40 of two
+    wavelengths per cluster, precision form, batch arena 6 GiB."""
+    cases = [c for c in c3_cases(64, 2) if c["N"] >= 40][:24]
+    ctx = G.Context(0)
+    t0 = time.perf_counter()
+    res = G.batch_solve(ctx, [(c["sp"], bg, c["wave"], mixed, G.C64) for c in cases],
+                        arena_bytes=6 << 30)
+    dt = time.perf_counter() - t0
+    ctx.close()
+    return {"workload": "c3 profiling case: 24 requests with N >= 40, precision form, 6 GiB arena",
+            "seconds": dt, "statuses": sorted({r["status"] for r in res})}
+
+
 def batch_arm(args):
     """c3: the ragged spectral sweep through the batching form
     (om_batch_solve), precision form against the FP64 form on the same cases;
@@ -592,10 +606,12 @@ def batch_arm(args):
     import optimet_gb300 as G
     from optimet_gb300 import build
     build.build()
-    cases = c3_cases(args.c3_clusters, args.c3_wavelengths)
     bg = G.medium(1.0)
     mixed = G.options(G.SOLVE_FGMRES_MIXED, tol=1e-8, max_iter=30, restarts=4, inner_iter=60,
                       inner_tol=1e-4)
+    if args.c3_profile:
+        return c3_profile_case(G, mixed, bg)
+    cases = c3_cases(args.c3_clusters, args.c3_wavelengths)
     fp64 = G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=300, restarts=6)
     ctx = G.Context(0)
     # warm-up: one request per nMax (coefficient and SH coupling tables, the
@@ -881,6 +897,8 @@ def main():
     ap.add_argument("--c4-seconds", type=float, default=60.0)
     ap.add_argument("--batch-slots", type=int, default=6, help="server slots for c3 / c4")
     ap.add_argument("--no-server", action="store_true", help="c3: skip the server comparison")
+    ap.add_argument("--c3-profile", action="store_true",
+                    help="c3: only the small batched case that the ncu captures use")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload == "aca":
