@@ -54,7 +54,8 @@ namespace {
 
 constexpr int kBT = 256;         // threads of the vector kernels; rows per matvec tile
 constexpr int kBCols = 1024;     // columns per split-K chunk
-constexpr int kBDotRows = 2048;  // rows per block of the dot products
+constexpr int kBDotRows = 2048;  // rows per block of the residual norm
+constexpr int kFRows = 512;      // rows per block of the Arnoldi vector kernels
 constexpr int kSegSteps = 8;     // Arnoldi steps per captured segment
 constexpr int kMaxSlots = 256;   // slots per batch (one thread per slot in the control kernels)
 
@@ -208,27 +209,6 @@ __global__ void __launch_bounds__(kBT) k_b_resid(const Slot *st, const int4 *til
   }
 }
 
-// basis column j + 1 = sum of the chunks' partials (fixed order)
-template <typename V>
-__global__ void k_b_reduce_w(const Slot *st, const Ctl *ctl, const V *part, long np, int nsm, V *Vb,
-                             long vslot) {
-  const int s = blockIdx.y;
-  if(!st[s].inner)
-    return;
-  const long n = st[s].n, i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if(i >= n)
-    return;
-  const int ns = (int)((n + kBCols - 1) / kBCols);
-  const V *p = part + (long)s * nsm * np + i;
-  V acc = p[0];
-  for(int c = 1; c < ns; ++c) {
-    const V v = p[(long)c * np];
-    acc.x += v.x;
-    acc.y += v.y;
-  }
-  Vb[s * vslot + (long)(ctl->j + 1) * np + i] = acc;
-}
-
 // r = b - S x (r = b while x = 0)
 __global__ void k_b_reduce_r(const Slot *st, const double2 *part, long np, int nsm, const double2 *b,
                              double2 *r) {
@@ -254,105 +234,169 @@ __global__ void k_b_reduce_r(const Slot *st, const double2 *part, long np, int n
   r[s * np + i] = make_double2(bv.x - acc.x, bv.y - acc.y);
 }
 
-// Block partial sums over rows [blockIdx.x kBDotRows, ...) of slot blockIdx.y:
-// norm = 0: conj(v_t) . w for t = 0 .. j, w = column j + 1 (Arnoldi slots);
-// norm = 1: |w|^2 with w = column j + 1 (use_j) or column 0 (residual, outer slots).
-// dpart[((s nblk) + block) m2 + t]
-template <typename V>
-__global__ void __launch_bounds__(kBT) k_b_dot(const Slot *st, const Ctl *ctl, const V *base,
-                                              long vslot, long np, int use_j, int norm, int outer,
-                                              int nblk, int m2, V *dpart) {
-  __shared__ V red[kBT];
+// ||r||^2 block partials of the residual: rows [blockIdx.x kBDotRows, ...)
+// of slot blockIdx.y (slots with outer set), into dpart[(s nblk + block) m2]
+__global__ void __launch_bounds__(kBT) k_b_rnorm(const Slot *st, const double2 *r, long np, int nblk,
+                                                int m2, double2 *dpart) {
+  __shared__ double red[kBT];
   const int s = blockIdx.y;
-  if(!(outer ? st[s].outer : st[s].inner))
+  if(!st[s].outer)
     return;
   const long n = st[s].n;
   const long r0 = (long)blockIdx.x * kBDotRows;
   if(r0 >= n)
     return;
   const long r1 = min(n, r0 + kBDotRows);
-  const int j = use_j ? ctl->j : -1;
-  const V *vs = base + s * vslot;
-  const V *w = vs + (long)(j + 1) * np;
-  const int cnt = norm ? 1 : j + 1;
-  V *out = dpart + ((long)s * nblk + blockIdx.x) * m2;
-  for(int t = 0; t < cnt; ++t) {
+  double acc = 0.0;
+  for(long i = r0 + threadIdx.x; i < r1; i += kBT) {
+    const double2 a = r[s * np + i];
+    acc = fma(a.x, a.x, acc);
+    acc = fma(a.y, a.y, acc);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for(int h = kBT / 2; h > 0; h >>= 1) {
+    if(threadIdx.x < h)
+      red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0)
+    dpart[((long)s * nblk + blockIdx.x) * m2] = make_double2(red[0], 0.0);
+}
+
+// The Arnoldi vector kernels work on row blocks of kFRows rows of one slot
+// (grid: row blocks x slots); a block's partial sums go to
+// dp[(s nbf + block) m2 + t] and the next kernel adds them in block order.
+template <typename V> __device__ __forceinline__ V warp_sum(V a) {
+  for(int o = 16; o > 0; o >>= 1) {
+    a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+    a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+  }
+  return a;
+}
+
+// out[t] = sum over rows [r0, r1) of conj(v_t) w, t < k: one warp per t
+template <typename V>
+__device__ __forceinline__ void block_proj(const V *vs, const V *w, long np, long r0, long r1, int k,
+                                           V *out) {
+  const int lane = threadIdx.x & 31;
+  for(int t = threadIdx.x >> 5; t < k; t += kBT / 32) {
+    const V *v = vs + (long)t * np;
     V acc;
     acc.x = acc.y = 0;
-    if(!norm) {
-      const V *v = vs + (long)t * np;
-      for(long i = r0 + threadIdx.x; i < r1; i += kBT)
-        acc = cfma_conj(v[i], w[i], acc);
-    } else {
-      for(long i = r0 + threadIdx.x; i < r1; i += kBT) {
-        const V a = w[i];
-        acc.x = fma(a.x, a.x, acc.x);
-        acc.x = fma(a.y, a.y, acc.x);
-      }
-    }
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for(int h = kBT / 2; h > 0; h >>= 1) {
-      if(threadIdx.x < h) {
-        red[threadIdx.x].x += red[threadIdx.x + h].x;
-        red[threadIdx.x].y += red[threadIdx.x + h].y;
-      }
-      __syncthreads();
-    }
-    if(threadIdx.x == 0)
-      out[t] = red[0];
-    __syncthreads();
+    for(long i = r0 + lane; i < r1; i += 32)
+      acc = cfma_conj(v[i], w[i], acc);
+    acc = warp_sum(acc);
+    if(lane == 0)
+      out[t] = acc;
   }
 }
 
-// h_t = sum over blocks (fixed order) for t = 0 .. j; hacc = h (pass 0) or hacc + h (pass 1)
+// h[t] = sum over the slot's nb blocks of dp (block order), t < k, in shared memory
 template <typename V>
-__global__ void k_b_hsum(const Slot *st, const Ctl *ctl, const V *dpart, int nblk, int m2, V *hs,
-                         double2 *hacc, int pass) {
-  const int s = blockIdx.x;
-  if(!st[s].inner)
-    return;
-  const int k = ctl->j + 1;
-  const int nb = (int)((st[s].n + kBDotRows - 1) / kBDotRows);
-  for(int t = threadIdx.x; t < k; t += blockDim.x) {
-    const V *p = dpart + (long)s * nblk * m2 + t;
-    V acc = p[0];
+__device__ __forceinline__ void gather_h(const V *dp, int nb, int m2, int k, V *h) {
+  for(int t = threadIdx.x; t < k; t += kBT) {
+    V acc = dp[t];
     for(int b = 1; b < nb; ++b) {
-      acc.x += p[(long)b * m2].x;
-      acc.y += p[(long)b * m2].y;
+      acc.x += dp[(long)b * m2 + t].x;
+      acc.y += dp[(long)b * m2 + t].y;
     }
-    hs[s * m2 + t] = acc;
-    const double2 a = to_d2(acc);
-    hacc[s * m2 + t] = pass ? cadd(hacc[s * m2 + t], a) : a;
+    h[t] = acc;
   }
+  __syncthreads();
 }
 
-// w -= V[:, 0..j] h (w = column j + 1)
+// w (basis column j + 1) = the split-K partials summed in chunk order; then
+// the first projection pass V[:, 0..j]^H w
 template <typename V>
-__global__ void k_b_sub(const Slot *st, const Ctl *ctl, const V *hs, int m2, V *Vb, long vslot, long np) {
+__global__ void __launch_bounds__(kBT) k_b_red_proj(const Slot *st, const Ctl *ctl, const V *part, long np,
+                                                   int nsm, V *Vb, long vslot, int nbf, int m2, V *dpA) {
   const int s = blockIdx.y;
   if(!st[s].inner)
     return;
-  const long n = st[s].n, i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if(i >= n)
+  const long n = st[s].n, r0 = (long)blockIdx.x * kFRows;
+  if(r0 >= n)
     return;
+  const long r1 = min(n, r0 + kFRows);
   const int k = ctl->j + 1;
-  V *vs = Vb + s * vslot;
-  V acc = vs[(long)k * np + i];
-  for(int t = 0; t < k; ++t) {
-    V c = hs[s * m2 + t];
-    c.x = -c.x;
-    c.y = -c.y;
-    acc = cfma(vs[(long)t * np + i], c, acc);
+  V *vs = Vb + s * vslot, *w = vs + (long)k * np;
+  const int ns = (int)((n + kBCols - 1) / kBCols);
+  for(long i = r0 + threadIdx.x; i < r1; i += kBT) {
+    const V *p = part + (long)s * nsm * np + i;
+    V acc = p[0];
+    for(int c = 1; c < ns; ++c) {
+      const V v = p[(long)c * np];
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+    w[i] = acc;
   }
-  vs[(long)k * np + i] = acc;
+  __syncthreads();
+  block_proj(vs, w, np, r0, r1, k, dpA + ((long)s * nbf + blockIdx.x) * m2);
+}
+
+// w -= V h with h the previous pass's projections (hacc = h on pass 0, += h
+// on pass 1, written by block 0); then the second projection pass (pass 0)
+// or |w|^2 into entry m2 - 1 of the block's partials (pass 1)
+template <typename V>
+__global__ void __launch_bounds__(kBT) k_b_sub_proj(const Slot *st, const Ctl *ctl, V *Vb, long vslot,
+                                                   long np, int nbf, int m2, const V *dp_in, V *dp_out,
+                                                   double2 *hacc, int pass) {
+  extern __shared__ unsigned char h_raw[];
+  V *h = reinterpret_cast<V *>(h_raw);
+  __shared__ double red[kBT / 32];
+  const int s = blockIdx.y;
+  if(!st[s].inner)
+    return;
+  const long n = st[s].n, r0 = (long)blockIdx.x * kFRows;
+  if(r0 >= n)
+    return;
+  const long r1 = min(n, r0 + kFRows);
+  const int k = ctl->j + 1;
+  const int nb = (int)((n + kFRows - 1) / kFRows);
+  gather_h(dp_in + (long)s * nbf * m2, nb, m2, k, h);
+  if(blockIdx.x == 0)
+    for(int t = threadIdx.x; t < k; t += kBT)
+      hacc[s * m2 + t] = pass ? cadd(hacc[s * m2 + t], to_d2(h[t])) : to_d2(h[t]);
+  V *vs = Vb + s * vslot, *w = vs + (long)k * np;
+  double nrm = 0.0;
+  for(long i = r0 + threadIdx.x; i < r1; i += kBT) {
+    V acc = w[i];
+    for(int t = 0; t < k; ++t) {
+      V c = h[t];
+      c.x = -c.x;
+      c.y = -c.y;
+      acc = cfma(vs[(long)t * np + i], c, acc);
+    }
+    w[i] = acc;
+    nrm = fma((double)acc.x, (double)acc.x, nrm);
+    nrm = fma((double)acc.y, (double)acc.y, nrm);
+  }
+  V *out = dp_out + ((long)s * nbf + blockIdx.x) * m2;
+  if(!pass) {
+    __syncthreads();
+    block_proj(vs, w, np, r0, r1, k, out);
+    return;
+  }
+  for(int o = 16; o > 0; o >>= 1)
+    nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
+  if((threadIdx.x & 31) == 0)
+    red[threadIdx.x >> 5] = nrm;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    double a = 0.0;
+    for(int q = 0; q < kBT / 32; ++q)
+      a += red[q];
+    out[m2 - 1].x = a;
+    out[m2 - 1].y = 0;
+  }
 }
 
 // Hessenberg column j of every Arnoldi slot: previous rotations, the new
 // rotation, the residual estimate |g_{j+1}| and the stop test; one thread
 // per slot. Then the step index advances (if any slot ran).
 template <typename V>
-__global__ void k_b_givens(Slot *st, Ctl *ctl, const V *dpart, int nblk, int m2, const double2 *hacc,
+__global__ void k_b_givens(Slot *st, Ctl *ctl, const V *dp, int nbf, int m2, const double2 *hacc,
                            double2 *Hm, double2 *cs, double2 *sn, double2 *g, double *inv, int m,
                            int B) {
   const int s = threadIdx.x;
@@ -362,14 +406,12 @@ __global__ void k_b_givens(Slot *st, Ctl *ctl, const V *dpart, int nblk, int m2,
   int still = 0;
   if(act) {
     Slot &sl = st[s];
-    const int nb = (int)((sl.n + kBDotRows - 1) / kBDotRows);
-    const V *p = dpart + (long)s * nblk * m2;
-    V acc = p[0];
-    for(int b = 1; b < nb; ++b) {
-      acc.x += p[(long)b * m2].x;
-      acc.y += p[(long)b * m2].y;
-    }
-    const double hn = sqrt((double)acc.x);
+    const int nb = (int)((sl.n + kFRows - 1) / kFRows);
+    const V *p = dp + (long)s * nbf * m2 + (m2 - 1);
+    double acc = p[0].x;
+    for(int b = 1; b < nb; ++b)
+      acc += p[(long)b * m2].x;
+    const double hn = sqrt(acc);
     double2 *col = Hm + ((long)s * m + j) * (m + 1);
     for(int t = 0; t <= j; ++t)
       col[t] = hacc[s * m2 + t];
@@ -547,7 +589,7 @@ inline size_t rup(size_t v) { return ((v + 255) / 256) * 256; }
 template <typename M, typename V> struct Class {
   om_context *ctx = nullptr;
   ClassKey key{};
-  int B = 0, m = 0, m2 = 0, nsm = 0, nblk = 0, max_tiles = 0;
+  int B = 0, m = 0, m2 = 0, nsm = 0, nblk = 0, nbf = 0, max_tiles = 0;
   long np = 0, vslot = 0;
   unsigned mv_grid = 1;
   void *buf = nullptr;
@@ -559,8 +601,8 @@ template <typename M, typename V> struct Class {
   BatchMat *mats = nullptr;           // nbuf x 2B entries
   M *Sff[2] = {nullptr, nullptr}, *Ssh[2] = {nullptr, nullptr};
   double2 *b = nullptr, *x = nullptr, *r = nullptr, *part = nullptr;
-  V *Vb = nullptr, *hs = nullptr;
-  void *dpart = nullptr;
+  V *Vb = nullptr;
+  double2 *dpA = nullptr, *dpB = nullptr;  // block partial sums (two passes; entries of V or double2)
   double2 *hacc = nullptr, *Hm = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr;
   double *inv = nullptr;
   unsigned long long *counter = nullptr;
@@ -578,10 +620,10 @@ template <typename M, typename V> struct Class {
 
   static size_t slot_bytes(long np, int m, int nbuf) {
     const int m2 = m + 2;
-    const long nsm = (np + kBCols - 1) / kBCols, nblk = (np + kBDotRows - 1) / kBDotRows;
+    const long nsm = (np + kBCols - 1) / kBCols, nbf = (np + kFRows - 1) / kFRows;
     return 2 * nbuf * rup(sizeof(M) * (size_t)np * np) + 3 * sizeof(double2) * np +
            sizeof(V) * (size_t)(m + 1) * np + sizeof(double2) * (size_t)nsm * np +
-           sizeof(double2) * (size_t)nblk * m2 + sizeof(V) * m2 +
+           2 * sizeof(double2) * (size_t)nbf * m2 +
            sizeof(double2) * ((size_t)m2 + (size_t)m * (m + 1) + 2 * (size_t)m + (m + 1) + m) +
            sizeof(int4) * (size_t)((np + kBT - 1) / kBT) * nsm + sizeof(Slot) +
            2 * nbuf * sizeof(BatchMat) + 64;
@@ -598,6 +640,7 @@ template <typename M, typename V> struct Class {
     vslot = (long)(m + 1) * np;
     nsm = (int)((np + kBCols - 1) / kBCols);
     nblk = (int)((np + kBDotRows - 1) / kBDotRows);
+    nbf = (int)((np + kFRows - 1) / kFRows);
     max_tiles = B * (int)((np + kBT - 1) / kBT) * nsm;
     // overlapping batches: half the SM's CTA slots, so that two CTAs of the
     // next batch's assembly (FP64-bound) fit beside the matvec (HBM-bound)
@@ -607,8 +650,9 @@ template <typename M, typename V> struct Class {
     size_t sz[] = {Bz * sizeof(Slot), sizeof(Ctl), sizeof(int4) * (size_t)max_tiles,
                    2 * Bz * nbuf * sizeof(BatchMat), mz, mz, nbuf > 1 ? mz : 0, nbuf > 1 ? mz : 0,
                    Bz * sizeof(double2) * np, Bz * sizeof(double2) * np, Bz * sizeof(double2) * np,
-                   Bz * sizeof(double2) * nsm * np, Bz * sizeof(V) * vslot, Bz * sizeof(V) * m2,
-                   Bz * sizeof(double2) * nblk * m2, Bz * sizeof(double2) * m2,
+                   Bz * sizeof(double2) * nsm * np, Bz * sizeof(V) * vslot,
+                   Bz * sizeof(double2) * nbf * m2, Bz * sizeof(double2) * nbf * m2,
+                   Bz * sizeof(double2) * m2,
                    Bz * sizeof(double2) * m * (m + 1), Bz * sizeof(double2) * m,
                    Bz * sizeof(double2) * m, Bz * sizeof(double2) * (m + 1), Bz * sizeof(double2) * m,
                    Bz * sizeof(double), sizeof(unsigned long long)};
@@ -638,8 +682,8 @@ template <typename M, typename V> struct Class {
     r = (double2 *)take(sz[i++]);
     part = (double2 *)take(sz[i++]);
     Vb = (V *)take(sz[i++]);
-    hs = (V *)take(sz[i++]);
-    dpart = take(sz[i++]);
+    dpA = (double2 *)take(sz[i++]);
+    dpB = (double2 *)take(sz[i++]);
     hacc = (double2 *)take(sz[i++]);
     Hm = (double2 *)take(sz[i++]);
     cs = (double2 *)take(sz[i++]);
@@ -694,28 +738,27 @@ template <typename M, typename V> struct Class {
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
     k_b_resid<M><<<mv_grid, kBT, 0, s>>>(st, tiles, ctl, x, np, nsm, part, counter);
     k_b_reduce_r<<<vgrid(), kBT, 0, s>>>(st, part, np, nsm, b, r);
-    k_b_dot<double2><<<dim3(nblk, B), kBT, 0, s>>>(st, ctl, r, np, np, 0, 1, 1, nblk, m2,
-                                                   (double2 *)dpart);
-    k_b_start<<<1, ctl_threads(), 0, s>>>(st, ctl, (const double2 *)dpart, nblk, m2, g, m, B,
-                                          key.tol, key.inner_rel, key.max_cycles);
+    k_b_rnorm<<<dim3(nblk, B), kBT, 0, s>>>(st, r, np, nblk, m2, dpA);
+    k_b_start<<<1, ctl_threads(), 0, s>>>(st, ctl, dpA, nblk, m2, g, m, B, key.tol, key.inner_rel,
+                                          key.max_cycles);
     k_b_v0<V><<<vgrid(), kBT, 0, s>>>(st, r, np, Vb, vslot);
     return 5;
   }
-  // one Arnoldi step with CGS2 (two projection passes), the rotation, the scaling
+  // one Arnoldi step with CGS2: the matvec; w and the first projections;
+  // subtraction and the second projections; subtraction and |w|^2; the
+  // rotation; the scaling
   int enqueue_step(cudaStream_t s) {
-    V *dp = (V *)dpart;
+    V *pA = (V *)dpA, *pB = (V *)dpB;
+    const dim3 fg((unsigned)nbf, (unsigned)B);
+    const size_t hsm = sizeof(V) * m2;
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
     k_b_mv<M, V><<<mv_grid, kBT, 0, s>>>(st, tiles, ctl, Vb, vslot, np, nsm, (V *)part, counter);
-    k_b_reduce_w<V><<<vgrid(), kBT, 0, s>>>(st, ctl, (const V *)part, np, nsm, Vb, vslot);
-    for(int pass = 0; pass < 2; ++pass) {
-      k_b_dot<V><<<dim3(nblk, B), kBT, 0, s>>>(st, ctl, Vb, vslot, np, 1, 0, 0, nblk, m2, dp);
-      k_b_hsum<V><<<B, 64, 0, s>>>(st, ctl, dp, nblk, m2, hs, hacc, pass);
-      k_b_sub<V><<<vgrid(), kBT, 0, s>>>(st, ctl, hs, m2, Vb, vslot, np);
-    }
-    k_b_dot<V><<<dim3(nblk, B), kBT, 0, s>>>(st, ctl, Vb, vslot, np, 1, 1, 0, nblk, m2, dp);
-    k_b_givens<V><<<1, ctl_threads(), 0, s>>>(st, ctl, dp, nblk, m2, hacc, Hm, cs, sn, g, inv, m, B);
+    k_b_red_proj<V><<<fg, kBT, 0, s>>>(st, ctl, (const V *)part, np, nsm, Vb, vslot, nbf, m2, pA);
+    k_b_sub_proj<V><<<fg, kBT, hsm, s>>>(st, ctl, Vb, vslot, np, nbf, m2, pA, pB, hacc, 0);
+    k_b_sub_proj<V><<<fg, kBT, hsm, s>>>(st, ctl, Vb, vslot, np, nbf, m2, pB, pA, hacc, 1);
+    k_b_givens<V><<<1, ctl_threads(), 0, s>>>(st, ctl, pA, nbf, m2, hacc, Hm, cs, sn, g, inv, m, B);
     k_b_scale<V><<<vgrid(), kBT, 0, s>>>(st, ctl, inv, Vb, vslot, np);
-    return 11;
+    return 6;
   }
   int enqueue_end(cudaStream_t s) {
     k_b_end<<<1, ctl_threads(), 0, s>>>(st, Hm, g, y, m, B);
