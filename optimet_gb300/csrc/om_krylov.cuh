@@ -23,15 +23,16 @@ template <typename V> __device__ __forceinline__ V cfma_conj(V a, V b, V c) {  /
   return c;
 }
 
-// sum_{u < cnt} S[u ld] xs[u] for the row that `col` points into (xs: the
-// column chunk staged in shared memory). Eight columns' loads are issued
-// before their FMAs; two accumulators take alternate columns.
+// sum_{j0 <= j < j1} S[(j - j0) ld] xs[j - j0] for the row that `col` points
+// into (xs: the column chunk j0 .. j1 - 1 staged in shared memory). Eight
+// columns' loads are issued before their FMAs; two accumulators take
+// alternate columns.
 template <typename M, typename V>
-__device__ __forceinline__ V mv_row(const M *col, long ld, const V *xs, int cnt) {
+__device__ __forceinline__ V mv_row(const M *col, long ld, const V *xs, long j0, long j1) {
   V acc0, acc1;
   acc0.x = acc0.y = acc1.x = acc1.y = 0;
-  int j = 0;
-  for(; j + 7 < cnt; j += 8) {
+  long j = j0;
+  for(; j + 7 < j1; j += 8) {
     M s[8];
 #pragma unroll
     for(int u = 0; u < 8; ++u)
@@ -40,17 +41,17 @@ __device__ __forceinline__ V mv_row(const M *col, long ld, const V *xs, int cnt)
     for(int u = 0; u < 8; u += 2) {
       V a0, a1;
       a0.x = s[u].x; a0.y = s[u].y; a1.x = s[u + 1].x; a1.y = s[u + 1].y;
-      acc0 = cfma(a0, xs[j + u], acc0);
-      acc1 = cfma(a1, xs[j + u + 1], acc1);
+      acc0 = cfma(a0, xs[j - j0 + u], acc0);
+      acc1 = cfma(a1, xs[j - j0 + u + 1], acc1);
     }
     col += 8 * ld;
   }
-  for(; j < cnt; ++j) {
+  for(; j < j1; ++j) {
     M s0 = col[0];
     V a0;
     a0.x = s0.x;
     a0.y = s0.y;
-    acc0 = cfma(a0, xs[j], acc0);
+    acc0 = cfma(a0, xs[j - j0], acc0);
     col += ld;
   }
   acc0.x += acc1.x;
@@ -80,21 +81,22 @@ __device__ __forceinline__ float4 df_split(double2 v) {
 // (TwoProduct) and summed in a float-float accumulator; the small terms
 // (product errors and s * x_lo) go to a separate float sum; the parts are
 // combined in FP64. Four columns' loads are in flight at a time.
-__device__ __forceinline__ double2 mv_row_df(const float2 *col, long ld, const float4 *xs, int cnt) {
+__device__ __forceinline__ double2 mv_row_df(const float2 *col, long ld, const float4 *xs, long j0,
+                                             long j1) {
   DF re{0.f, 0.f}, im{0.f, 0.f};
   float er = 0.f, ei = 0.f;
-  for(int j = 0; j < cnt; j += 4) {
+  for(long j = j0; j < j1; j += 4) {
     float2 av[4];
-    const int c4 = min(4, cnt - j);
+    const int cnt = (int)min(4L, j1 - j);
 #pragma unroll
     for(int u = 0; u < 4; ++u)
-      av[u] = u < c4 ? col[u * ld] : make_float2(0.f, 0.f);
+      av[u] = u < cnt ? col[u * ld] : make_float2(0.f, 0.f);
 #pragma unroll
     for(int u = 0; u < 4; ++u) {
-      if(u >= c4)
+      if(u >= cnt)
         break;
       const float2 a = av[u];
-      const float4 v = xs[j + u];
+      const float4 v = xs[j - j0 + u];
       // __fmul_rn keeps the products out of FMA contraction so that the
       // TwoProduct error terms below are exact
       float p = __fmul_rn(a.x, v.x);

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld,
     __syncthreads();
     if(i >= n)
       continue;
-    part[ct * n + i] = mv_row<M, V>(S + j0 * ld + i, ld, xs, (int)(j1 - j0));
+    part[ct * n + i] = mv_row<M, V>(S + j0 * ld + i, ld, xs, j0, j1);
   }
 }
 
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part_df(const float2 *S, 
     __syncthreads();
     if(i >= n)
       continue;
-    part[ct * n + i] = mv_row_df(S + j0 * ld + i, ld, xs, (int)(j1 - j0));
+    part[ct * n + i] = mv_row_df(S + j0 * ld + i, ld, xs, j0, j1);
   }
 }
 
