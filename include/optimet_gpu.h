@@ -318,6 +318,19 @@ int om_server_drain(om_server *srv);
  * the device time from the earliest event of the previous mark to the latest
  * of this one (0 for the first). */
 int om_server_mark(om_server *srv, double *ms);
+/* Batched service: with max_requests > 1, requests that om_batch_solve runs
+ * (OM_C128 with OM_SOLVE_GMRES, OM_C64 with OM_SOLVE_FGMRES_MIXED) whose
+ * batched footprint (FF and SH matrices together plus the slot's vectors) is
+ * at most max_request_bytes (0 = any) are batchable. A free slot serves the
+ * head of the queue on the single-request path when it is not batchable and
+ * fits; otherwise it takes the batchable requests of the queue in arrival
+ * order, at most max_requests and within the budget, and serves them in one
+ * om_batch_solve call (arena_bytes as there; 0 = the run's own footprint).
+ * max_requests <= 1 turns it off (the default). Each path's results are
+ * fixed-order reductions (bitwise reproducible); the two paths agree within
+ * the solver tolerance. */
+int om_server_batching(om_server *srv, int max_requests, size_t arena_bytes,
+                       size_t max_request_bytes);
 /* om_context_tune on every slot; only while no request is outstanding. */
 int om_server_tune(om_server *srv, const om_tuning *t);
 /* Autotuner of the launch tuning: runs `count` requests like *rq (its cluster

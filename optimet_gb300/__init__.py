@@ -152,6 +152,7 @@ def lib():
         L.om_server_last_error.argtypes = [vp]
         L.om_server_last_error.restype = C.c_char_p
         L.om_server_destroy.argtypes = [vp]
+        L.om_server_batching.argtypes = [vp, C.c_int, C.c_size_t, C.c_size_t]
         L.om_batch_solve.argtypes = [vp, C.POINTER(Request), C.c_int, C.c_size_t, C.POINTER(Result)]
         _lib = L
     return _lib
@@ -504,6 +505,14 @@ class Server:
 
     def drain(self):
         lib().om_server_drain(self.h)
+
+    def batching(self, max_requests=64, arena_bytes=0, max_request_bytes=0):
+        """Serve runs of up to max_requests batchable requests (footprint at
+        most max_request_bytes, 0 = any) through the batching form
+        (om_server_batching); max_requests <= 1 turns it off."""
+        rc = lib().om_server_batching(self.h, max_requests, arena_bytes, max_request_bytes)
+        if rc:
+            raise OptimetError(rc, "server batching")
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
              matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1):

@@ -40,6 +40,7 @@
 #include <chrono>
 #include <cmath>
 #include <map>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <type_traits>
@@ -597,9 +598,8 @@ template <typename M, typename V> struct Class {
   Slot *st = nullptr;
   Ctl *ctl = nullptr;
   int4 *tiles = nullptr;
-  int nbuf = 1;                       // matrix buffers: 2 when batches overlap
+  int nbuf = 1;                       // batches in flight: 2 when they overlap
   BatchMat *mats = nullptr;           // nbuf x 2B entries
-  M *Sff[2] = {nullptr, nullptr}, *Ssh[2] = {nullptr, nullptr};
   double2 *b = nullptr, *x = nullptr, *r = nullptr, *part = nullptr;
   V *Vb = nullptr;
   double2 *dpA = nullptr, *dpB = nullptr;  // block partial sums (two passes; entries of V or double2)
@@ -614,14 +614,17 @@ template <typename M, typename V> struct Class {
   double *h_xsec = nullptr;  // 8 per slot: the FF and SH cross sections
   cudaEvent_t ev_main = nullptr;        // main stream -> auxiliary streams
   std::vector<cudaEvent_t> ev_aux;      // auxiliary streams -> main / assembly stream
-  cudaEvent_t ev_asm[2] = {nullptr, nullptr};  // assembly of buffer i done
+  cudaEvent_t ev_asm[2] = {nullptr, nullptr};    // assembly of batch buffer i done
+  cudaEvent_t ev_alloc[2] = {nullptr, nullptr};  // matrix storage of batch buffer i allocated
   cudaGraphExec_t g_start = nullptr, g_seg = nullptr, g_end = nullptr;
   int k_start = 0, k_seg = 0, k_end = 0;  // kernels per replay
 
+  // device bytes of one slot's vectors and tables (the matrices are
+  // allocated per batch at the requests' own sizes)
   static size_t slot_bytes(long np, int m, int nbuf) {
     const int m2 = m + 2;
     const long nsm = (np + kBCols - 1) / kBCols, nbf = (np + kFRows - 1) / kFRows;
-    return 2 * nbuf * rup(sizeof(M) * (size_t)np * np) + 3 * sizeof(double2) * np +
+    return 3 * sizeof(double2) * np +
            sizeof(V) * (size_t)(m + 1) * np + sizeof(double2) * (size_t)nsm * np +
            2 * sizeof(double2) * (size_t)nbf * m2 +
            sizeof(double2) * ((size_t)m2 + (size_t)m * (m + 1) + 2 * (size_t)m + (m + 1) + m) +
@@ -646,9 +649,10 @@ template <typename M, typename V> struct Class {
     // next batch's assembly (FP64-bound) fit beside the matvec (HBM-bound)
     mv_grid = (unsigned)std::max(1L, std::min((long)max_tiles,
                                               (long)ctx->sm_count * (nbuf > 1 ? 4 : 8)));
-    const size_t Bz = (size_t)B, mz = Bz * sizeof(M) * np * np;
+    // the matrices are allocated per batch, at the requests' own sizes
+    const size_t Bz = (size_t)B;
     size_t sz[] = {Bz * sizeof(Slot), sizeof(Ctl), sizeof(int4) * (size_t)max_tiles,
-                   2 * Bz * nbuf * sizeof(BatchMat), mz, mz, nbuf > 1 ? mz : 0, nbuf > 1 ? mz : 0,
+                   2 * Bz * nbuf * sizeof(BatchMat),
                    Bz * sizeof(double2) * np, Bz * sizeof(double2) * np, Bz * sizeof(double2) * np,
                    Bz * sizeof(double2) * nsm * np, Bz * sizeof(V) * vslot,
                    Bz * sizeof(double2) * nbf * m2, Bz * sizeof(double2) * nbf * m2,
@@ -673,10 +677,6 @@ template <typename M, typename V> struct Class {
     ctl = (Ctl *)take(sz[i++]);
     tiles = (int4 *)take(sz[i++]);
     mats = (BatchMat *)take(sz[i++]);
-    Sff[0] = (M *)take(sz[i++]);
-    Ssh[0] = (M *)take(sz[i++]);
-    Sff[1] = (M *)take(sz[i++]);
-    Ssh[1] = (M *)take(sz[i++]);
     b = (double2 *)take(sz[i++]);
     x = (double2 *)take(sz[i++]);
     r = (double2 *)take(sz[i++]);
@@ -704,6 +704,8 @@ template <typename M, typename V> struct Class {
     cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&ev_asm[0], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&ev_asm[1], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_alloc[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_alloc[1], cudaEventDisableTiming);
     ev_aux.resize(ctx->aux.size());
     for(auto &e : ev_aux)
       cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
@@ -725,6 +727,8 @@ template <typename M, typename V> struct Class {
     if(h_xsec) cudaFreeHost(h_xsec);
     if(ev_main) cudaEventDestroy(ev_main);
     for(auto &e : ev_asm)
+      if(e) cudaEventDestroy(e);
+    for(auto &e : ev_alloc)
       if(e) cudaEventDestroy(e);
     for(auto &e : ev_aux)
       if(e) cudaEventDestroy(e);
@@ -919,8 +923,11 @@ struct Pending {
   std::vector<om_problem *> pr;  // per slot; null where set-up failed
   size_t b0 = 0;                 // first request (index into the class's list)
   int nb = 0;                    // requests
-  int buf = 0;                   // matrix buffer
+  int buf = 0;                   // mats table / event set
   double t0 = 0;                 // host time when its set-up started
+  void *mbuf = nullptr;          // the batch's FF and SH matrices
+  size_t mbytes = 0;
+  std::vector<size_t> off_ff, off_sh;  // per slot: element offsets into mbuf
 };
 
 // Set-up of a batch and its assembly: request s lives on auxiliary context
@@ -953,10 +960,38 @@ void prepare_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const 
     *launches += a->last_launches - L0;
     P.pr[s]->have_source = true;
   }
+  // matrix storage at the requests' own sizes (column-major, ld = n)
+  P.off_ff.assign(P.nb, 0);
+  P.off_sh.assign(P.nb, 0);
+  size_t elems = 0;
+  for(int s = 0; s < P.nb; ++s) {
+    if(!P.pr[s])
+      continue;
+    const size_t nn = (size_t)P.pr[s]->n * P.pr[s]->n;
+    P.off_ff[s] = elems;
+    elems += nn;
+    if(reqs[idx[P.b0 + s]].wave.sh) {
+      P.off_sh[s] = elems;
+      elems += nn;
+    }
+  }
+  P.mbytes = std::max<size_t>(elems, 1) * sizeof(M);
+  if(dev_malloc(ctx, &P.mbuf, P.mbytes)) {
+    P.mbuf = nullptr;
+    for(int s = 0; s < P.nb; ++s)
+      if(P.pr[s]) {
+        out[idx[P.b0 + s]].status = OM_ERR_BUDGET;
+        om_problem_destroy(P.pr[s]);
+        P.pr[s] = nullptr;
+      }
+  }
+  cudaEventRecord(cl.ev_alloc[P.buf], ctx->stream);
+  cudaStreamWaitEvent(ctx->stream_lo, cl.ev_alloc[P.buf], 0);
   for(size_t q = 0; q < ctx->aux.size(); ++q) {
     cudaEventRecord(cl.ev_aux[q], ctx->aux[q]->stream);
     cudaStreamWaitEvent(ctx->stream_lo, cl.ev_aux[q], 0);
   }
+  M *S = (M *)P.mbuf;
   // FF matrices in entries 0 .. B-1, SH in B .. 2B-1 of this buffer's table
   BatchMat *hm = cl.h_mats + (size_t)2 * cl.B * P.buf;
   for(int e = 0; e < 2 * cl.B; ++e)
@@ -967,13 +1002,12 @@ void prepare_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const 
     if(!p)
       continue;
     const cplx k = p->waveK;
-    hm[s] = BatchMat{p->d_cart, p->d_T, cl.Sff[P.buf] + (size_t)s * np * np, p->n, mk(k.real(), k.imag()),
-                     p->N};
+    hm[s] = BatchMat{p->d_cart, p->d_T, S + P.off_ff[s], p->n, mk(k.real(), k.imag()), p->N};
     if(reqs[idx[P.b0 + s]].wave.sh) {
       any_sh = true;
       const cplx k2 = 2.0 * k;
-      hm[cl.B + s] = BatchMat{p->d_cart, p->d_Tsh, cl.Ssh[P.buf] + (size_t)s * np * np, p->n,
-                              mk(k2.real(), k2.imag()), p->N};
+      hm[cl.B + s] = BatchMat{p->d_cart, p->d_Tsh, S + P.off_sh[s], p->n, mk(k2.real(), k2.imag()),
+                              p->N};
     }
   }
   const int nmats = any_sh ? 2 * cl.B : cl.B;
@@ -1010,7 +1044,7 @@ int finish_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const st
     z.xzero = 1;
     if(s < nb && pr[s]) {
       z.n = pr[s]->n;
-      z.S = cl.Sff[P.buf] + (size_t)s * np * np;
+      z.S = (const M *)P.mbuf + P.off_ff[s];
       z.outer = 1;
       cudaMemcpyAsync(cl.b + (size_t)s * np, pr[s]->d_Q, sizeof(double2) * z.n,
                       cudaMemcpyDeviceToDevice, ctx->stream);
@@ -1058,7 +1092,7 @@ int finish_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const st
     z.xzero = 1;
     if(s < nb && pr[s] && reqs[idx[P.b0 + s]].wave.sh && pr[s]->d_K && pr[s]->d_acs) {
       z.n = pr[s]->n;
-      z.S = cl.Ssh[P.buf] + (size_t)s * np * np;
+      z.S = (const M *)P.mbuf + P.off_sh[s];
       z.outer = 1;
       run = true;
       cudaMemcpyAsync(cl.b + (size_t)s * np, pr[s]->d_K, sizeof(double2) * z.n,
@@ -1125,6 +1159,65 @@ int finish_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const st
   return OM_OK;
 }
 
+// Class workspaces are kept between calls, per context, so that a serving
+// loop that calls om_batch_solve for small runs does not rebuild the arena,
+// the pinned staging and the graphs of a size class each time. Entries not
+// in use are evicted least recently used beyond kCacheBytes per context.
+struct CacheEntry {
+  om_context *ctx;
+  ClassKey key;
+  int B, nbuf;
+  void *cls;
+  void (*del)(void *);
+  size_t bytes;
+  unsigned long long last;
+};
+std::mutex g_cache_mu;
+std::vector<CacheEntry> g_cache;
+unsigned long long g_cache_clock = 0;
+constexpr size_t kCacheBytes = size_t(4) << 30;
+
+bool same_key(const ClassKey &a, const ClassKey &b) { return !(a < b) && !(b < a); }
+
+template <typename M, typename V> Class<M, V> *cache_take(om_context *ctx, const ClassKey &key, int B, int nbuf) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  for(size_t i = 0; i < g_cache.size(); ++i) {
+    CacheEntry &e = g_cache[i];
+    if(e.ctx == ctx && same_key(e.key, key) && e.B >= B && e.nbuf >= nbuf) {
+      Class<M, V> *cl = static_cast<Class<M, V> *>(e.cls);
+      g_cache.erase(g_cache.begin() + i);
+      return cl;
+    }
+  }
+  return nullptr;
+}
+
+template <typename M, typename V> void cache_put(om_context *ctx, Class<M, V> *cl) {
+  std::vector<CacheEntry> victims;
+  {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_cache.push_back(CacheEntry{ctx, cl->key, cl->B, cl->nbuf, cl,
+                                 [](void *p) { delete static_cast<Class<M, V> *>(p); }, cl->bytes,
+                                 ++g_cache_clock});
+    for(;;) {
+      size_t total = 0;
+      long oldest = -1;
+      for(size_t i = 0; i < g_cache.size(); ++i)
+        if(g_cache[i].ctx == ctx) {
+          total += g_cache[i].bytes;
+          if(oldest < 0 || g_cache[i].last < g_cache[oldest].last)
+            oldest = (long)i;
+        }
+      if(total <= kCacheBytes || oldest < 0)
+        break;
+      victims.push_back(g_cache[oldest]);
+      g_cache.erase(g_cache.begin() + oldest);
+    }
+  }
+  for(auto &v : victims)
+    v.del(v.cls);
+}
+
 // The requests idx of one size class, in batches of B slots; with more than
 // one batch, the next batch's set-up and assembly are issued before the
 // current batch's solves (two matrix buffers).
@@ -1140,14 +1233,22 @@ int run_class(om_context *ctx, const ClassKey &key, const std::vector<int> &idx,
   clg_tables_dev(ctx, key.nmax);
   cudaStreamSynchronize(ctx->stream);
   const size_t count = idx.size();
+  // a slot holds its vectors and, per batch in flight, the largest request's
+  // matrices
+  size_t maxmat = 0;
+  for(int i : idx) {
+    const size_t n = 2 * (size_t)pmax(key.nmax) * reqs[i].n_spheres;
+    maxmat = std::max(maxmat, sizeof(M) * n * n * (reqs[i].wave.sh ? 2 : 1));
+  }
   auto slots_for = [&](int nbuf) {
-    return (int)std::min<size_t>({count, (size_t)kMaxSlots,
-                                  std::max<size_t>(1, arena / Class<M, V>::slot_bytes(np, key.m, nbuf))});
+    const size_t per = Class<M, V>::slot_bytes(np, key.m, nbuf) + nbuf * maxmat;
+    return (int)std::min<size_t>({count, (size_t)kMaxSlots, std::max<size_t>(1, arena / per)});
   };
   int nbuf = (size_t)slots_for(1) < count ? 2 : 1;
   int B = slots_for(nbuf);
-  Class<M, V> *cl = nullptr;
-  for(;;) {
+  // a cached workspace with at least B slots serves (batches stay at B)
+  Class<M, V> *cl = cache_take<M, V>(ctx, key, B, nbuf);
+  while(!cl) {
     cl = new Class<M, V>();
     rc = cl->init(ctx, key, B, nbuf);
     if(!rc)
@@ -1174,11 +1275,14 @@ int run_class(om_context *ctx, const ClassKey &key, const std::vector<int> &idx,
     P.buf = (int)(pend.size() % cl->nbuf);
     pend.push_back(P);
   }
-  auto destroy = [](Pending &P) {
+  auto destroy = [ctx](Pending &P) {
     for(om_problem *p : P.pr)
       if(p)
         om_problem_destroy(p);
     P.pr.clear();
+    if(P.mbuf)
+      dev_release(ctx, P.mbuf, P.mbytes);
+    P.mbuf = nullptr;
   };
   if(!pend.empty())
     prepare_batch(ctx, key, *cl, idx, reqs, out, t_call, pend[0], launches);
@@ -1198,11 +1302,51 @@ int run_class(om_context *ctx, const ClassKey &key, const std::vector<int> &idx,
   for(auto &P : pend)
     destroy(P);
   cudaStreamSynchronize(ctx->stream_lo);
-  delete cl;
+  if(rc)
+    delete cl;
+  else
+    cache_put(ctx, cl);
   return rc;
 }
 
 }  // namespace
+
+// Drops the class workspaces cached for ctx (called by om_context_destroy).
+void batch_release(om_context *ctx) {
+  std::vector<CacheEntry> mine;
+  {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    for(size_t i = 0; i < g_cache.size();) {
+      if(g_cache[i].ctx == ctx) {
+        mine.push_back(g_cache[i]);
+        g_cache.erase(g_cache.begin() + i);
+      } else {
+        ++i;
+      }
+    }
+  }
+  for(auto &e : mine)
+    e.del(e.cls);
+}
+
+// Device bytes one request takes in a batch: its FF (and SH) matrices at its
+// own size, and its slot's vectors (padded to the class size); 0 for requests
+// the batching form does not run.
+size_t batch_request_bytes(const om_request &rq) {
+  const om_solve_options &o = rq.opts;
+  const bool plain = rq.precision == OM_C128 && o.method == OM_SOLVE_GMRES;
+  const bool mixed = rq.precision == OM_C64 && o.method == OM_SOLVE_FGMRES_MIXED;
+  if((!plain && !mixed) || !rq.spheres || rq.n_spheres < 1 || rq.spheres[0].nmax < 1 ||
+     rq.spheres[0].nmax > kMaxNmax)
+    return 0;
+  const size_t P = pmax(rq.spheres[0].nmax);
+  const size_t n = 2 * P * rq.n_spheres, np = rup(2 * P * pad_spheres(rq.n_spheres));
+  const size_t elem = mixed ? sizeof(float2) : sizeof(double2);
+  const size_t m = (size_t)std::max(1, mixed ? o.inner_iter : o.max_iter);
+  const size_t nsm = (np + kBCols - 1) / kBCols;
+  return elem * n * n * (rq.wave.sh ? 2 : 1) + elem * (m + 1) * np + sizeof(double2) * (3 + nsm) * np +
+         sizeof(double2) * (m + 2) * (m + 2) * 2 + (size_t(64) << 20);
+}
 
 }  // namespace om
 

@@ -554,6 +554,7 @@ void om_context_destroy(om_context *ctx) {
   if(!ctx)
     return;
   cudaSetDevice(ctx->device);
+  om::batch_release(ctx);
   for(om_context *a : ctx->aux)
     om_context_destroy(a);
   ctx->aux.clear();

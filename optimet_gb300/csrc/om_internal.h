@@ -245,6 +245,11 @@ AcaOp aca_op(const om_problem *pr, int harmonic);
 // y = S x, or y = b - S x when b is given
 void aca_matvec(om_context *ctx, const AcaOp &op, const double2 *x, double2 *y, const double2 *b);
 
+// batch.cu: device bytes of one request in the batching form (0: not batchable);
+// release of the class workspaces a context keeps between calls
+size_t batch_request_bytes(const om_request &rq);
+void batch_release(om_context *ctx);
+
 // tma_matvec.cu: complex64 matvec with TMA-staged matrix tiles; false when the
 // tensor map cannot be encoded
 bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const void *x, void *part, bool df,

@@ -29,7 +29,8 @@ struct Job {
   unsigned long long ticket = 0;
   om_request rq{};
   std::vector<om_sphere> spheres;
-  size_t bytes = 0;
+  size_t bytes = 0;        // admission estimate of the single-request path
+  size_t batch_bytes = 0;  // ... and of the batched path (0: not batchable)
   clock_type::time_point submitted;
 };
 
@@ -83,10 +84,18 @@ struct om_server {
   long launches = 0;
   bool stop = false;
   bool has_mark = false;
+  int batch_max = 0;        // > 1: slots take runs of batchable requests
+  size_t batch_arena = 0;   // om_batch_solve arena per run (0: its default)
+  size_t batch_limit = 0;   // batch only requests with a footprint up to this (0: any)
+
+  bool batchable(const Job &j) const {
+    return batch_max > 1 && j.batch_bytes && (!batch_limit || j.batch_bytes <= batch_limit);
+  }
   std::string err;
 
   void run_slot(Slot &s);
   int serve(Slot &s, Job &job, om_result &res);
+  void serve_batch(Slot &s, std::vector<Job> &jobs);
 };
 
 namespace {
@@ -166,6 +175,46 @@ int om_server::serve(Slot &s, Job &job, om_result &res) {
   return rc ? rc : conv;
 }
 
+// A run of requests on one slot through the batching form (om_batch_solve):
+// size classes, one assembly launch and graph-captured lockstep solves per
+// batch.
+void om_server::serve_batch(Slot &s, std::vector<Job> &jobs) {
+  om_context *ctx = s.ctx;
+  std::vector<om_request> rq(jobs.size());
+  for(size_t i = 0; i < jobs.size(); ++i) {
+    rq[i] = jobs[i].rq;
+    rq[i].spheres = jobs[i].spheres.data();
+  }
+  std::vector<om_result> res(jobs.size());
+  const auto t0 = clock_type::now();
+  size_t arena = batch_arena;
+  if(!arena)
+    for(const Job &j : jobs)
+      arena += j.batch_bytes;
+  int rc = om_batch_solve(ctx, rq.data(), (int)rq.size(), arena, res.data());
+  const auto t1 = clock_type::now();
+  std::lock_guard<std::mutex> lk(mu);
+  if(rc)
+    err = "slot " + std::to_string(s.index) + ": " + ctx->err;
+  launches += ctx->last_launches;
+  for(size_t i = 0; i < jobs.size(); ++i) {
+    om_result r = res[i];
+    if(rc && (r.status == OM_OK || r.status == OM_ERR_NOT_CONVERGED))
+      r.status = rc;
+    r.slot = s.index;
+    r.device_bytes = jobs[i].batch_bytes;
+    r.queue_ms = ms_between(jobs[i].submitted, t0);
+    r.service_ms = ms_between(t0, t1);
+    r.latency_ms = ms_between(jobs[i].submitted, t1);
+    reserved -= jobs[i].batch_bytes;
+    done[jobs[i].ticket] = r;
+    pending.erase(jobs[i].ticket);
+    --outstanding;
+  }
+  cv_done.notify_all();
+  cv_work.notify_all();
+}
+
 void om_server::run_slot(Slot &s) {
   cudaSetDevice(device);
   for(;;) {
@@ -185,7 +234,17 @@ void om_server::run_slot(Slot &s) {
           Job &head = queue.front();
           // the slot's own resident bytes are reused (same key) or released
           const size_t others = reserved - s.resident;
-          if(others + head.bytes <= budget)
+          // a batchable request anywhere in the queue that fits, or the head
+          bool batch_ready = false;
+          if(batch_max > 1)
+            for(const Job &j : queue)
+              if(batchable(j) && others + j.batch_bytes <= budget) {
+                batch_ready = true;
+                break;
+              }
+          if(batch_ready || (!batchable(head) && others + head.bytes <= budget))
+            break;
+          if(batchable(head) && others + head.bytes <= budget)
             break;
           if(head.bytes > budget) {
             // can never run: fail it here
@@ -218,6 +277,33 @@ void om_server::run_slot(Slot &s) {
       }
       if(stop && queue.empty())
         break;
+      const bool head_single =
+          !batchable(queue.front()) && reserved - s.resident + queue.front().bytes <= budget;
+      if(batch_max > 1 && !head_single) {
+        // the batchable requests of the queue, in arrival order, up to
+        // batch_max and within the budget; the slot's resident problem goes
+        // first
+        std::vector<Job> run;
+        size_t take = reserved - s.resident;
+        for(auto it = queue.begin(); it != queue.end() && (int)run.size() < batch_max;) {
+          if(batchable(*it) && take + it->batch_bytes <= budget) {
+            take += it->batch_bytes;
+            reserved += it->batch_bytes;
+            run.push_back(std::move(*it));
+            it = queue.erase(it);
+          } else {
+            ++it;
+          }
+        }
+        if(run.empty())  // only a batchable head that fits on its own path
+          goto single;
+        lk.unlock();
+        if(s.resident || s.pr)
+          drop_resident(this, s);
+        serve_batch(s, run);
+        continue;
+      }
+    single:
       job = std::move(queue.front());
       queue.pop_front();
       reserved -= s.resident;
@@ -328,6 +414,7 @@ int om_server_submit(om_server *srv, const om_request *rq, unsigned long long *t
   job.spheres.assign(rq->spheres, rq->spheres + rq->n_spheres);
   job.rq.spheres = nullptr;
   job.bytes = estimate_bytes(*rq, nmax);
+  job.batch_bytes = om::batch_request_bytes(*rq);
   job.submitted = clock_type::now();
   std::lock_guard<std::mutex> lk(srv->mu);
   if(srv->stop)
@@ -401,6 +488,18 @@ int om_server_mark(om_server *srv, double *ms) {
   srv->has_mark = true;
   if(ms)
     *ms = t;
+  return OM_OK;
+}
+
+int om_server_batching(om_server *srv, int max_requests, size_t arena_bytes,
+                       size_t max_request_bytes) {
+  if(!srv || max_requests < 0)
+    return OM_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  srv->batch_max = max_requests;
+  srv->batch_arena = arena_bytes;
+  srv->batch_limit = max_request_bytes;
+  srv->cv_work.notify_all();
   return OM_OK;
 }
 

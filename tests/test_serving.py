@@ -125,3 +125,26 @@ def test_memory_pressure_releases_resident_problems(G):
     for r, (sp, bg, wave, opts, prec, key) in zip(res, reqs):
         assert np.array_equal(G.wavelength_solve(ctx, sp, bg, wave, opts, prec)[0], r["xsec"])
     ctx.close()
+
+
+def test_batched_service(G):
+    """With batching on, runs of batchable requests go through om_batch_solve
+    (results bitwise equal to a direct om_batch_solve call on the same
+    requests) and the rest (an LU request) through the single-request path."""
+    reqs = [rq for rq in _requests(G) if rq[3].method != G.SOLVE_LU]
+    lu = next(rq for rq in _requests(G) if rq[3].method == G.SOLVE_LU)
+    srv = G.Server(0, 0, 2)
+    srv.batching(16)
+    tickets = [srv.submit(*rq) for rq in reqs] + [srv.submit(*lu)]
+    res = _wait_all(srv, tickets)
+    srv.close()
+    assert all(r["status"] == G.OK for r in res)
+    ctx = G.Context(0)
+    direct = G.batch_solve(ctx, [rq[:5] for rq in reqs])
+    for r, d in zip(res, direct):
+        assert np.array_equal(r["xsec"], d["xsec"])
+        assert np.array_equal(r["xsec_sh"], d["xsec_sh"])
+    sp, bg, wave, opts, prec, key = lu
+    xs, xsh, _ = G.wavelength_solve_sh(ctx, sp, bg, wave, opts, prec)
+    assert np.array_equal(res[-1]["xsec"], xs)
+    ctx.close()
