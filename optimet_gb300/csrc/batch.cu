@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kBT) k_b_mv(const Slot *st, const int4 *tiles,
       xs[j - j0] = x[j];
     __syncthreads();
     if(i < n)
-      part[((long)d.x * nsm + d.z) * np + i] = mv_row<M, V>(S + j0 * n + i, n, xs, j0, j1);
+      part[((long)d.x * nsm + d.z) * np + i] = mv_row<M, V>(S + j0 * n + i, n, xs, 0L, j1 - j0);
   }
 }
 
@@ -203,9 +203,9 @@ __global__ void __launch_bounds__(kBT) k_b_resid(const Slot *st, const int4 *til
       continue;
     double2 v;
     if constexpr(kDF)
-      v = mv_row_df(S + j0 * n + i, n, xs, j0, j1);
+      v = mv_row_df(S + j0 * n + i, n, xs, 0L, j1 - j0);
     else
-      v = mv_row<double2, double2>(S + j0 * n + i, n, xs, j0, j1);
+      v = mv_row<double2, double2>(S + j0 * n + i, n, xs, 0L, j1 - j0);
     part[((long)d.x * nsm + d.z) * np + i] = v;
   }
 }

@@ -136,3 +136,35 @@ def test_failures_stay_with_their_request(G, ctx):
     assert np.array_equal(res[0]["xsec"], res[4]["xsec"])
     # the unconverged request still reports its (approximate) cross sections
     assert res[3]["ff"]["iterations"] == 2 and np.all(np.isfinite(res[3]["xsec"]))
+
+
+@pytest.mark.parametrize("nmax", [1, 2, 12, 15])
+def test_batch_extreme_nmax(G, ctx, nmax):
+    """The batched assembly's table layouts at the ends of the nMax range
+    (global factor tables from nMax 14), with a single sphere and a pair,
+    FF + SH, against the single-request FP64 path (LU). The SH cross
+    sections are compared up to nMax 8: from nMax 10 the SH source reads
+    X_int = X_sca (.) Iaux, where |Iaux| reaches 1e20 on the high orders, so two
+    independent solves (GMRES to 1e-13 and LU) give different SH sources there,
+    in the reference as here; the same holds for the fourth cross section (the
+    absorption from the internal coefficients and the Mie factors). The
+    batch's GMRES stops at a residual of 1e-13; with the condition number the
+    system reaches at nMax 12-15 that leaves the FF cross sections within
+    5e-9 of LU (1e-10 up to nMax 8)."""
+    rng = np.random.default_rng(nmax)
+    reqs = []
+    for N in (1, 2, 2):
+        xyz, rad = random_cluster(rng, N, 600 * nm, 50 * nm, 70 * nm, 30 * nm)
+        sp = G.spheres_array(xyz, rad, (1.9 + 0.03j) ** 2, nmax, eps_sh=(2.0 + 0.05j) ** 2,
+                             ksippp=1.0, ksiparppar=0.25)
+        wave = G.plane_wave(rng.uniform(500, 800) * nm, theta=rng.uniform(0, np.pi),
+                            phi=rng.uniform(-np.pi, np.pi), e_theta=0.6, e_phi=0.8j, sh=True)
+        reqs.append((sp, G.medium(1.1), wave, plain(G), G.C128))
+    res = G.batch_solve(ctx, reqs)
+    for r, (sp, bg, wave, opts, prec) in zip(res, reqs):
+        assert r["status"] == G.OK
+        xs, xsh, _ = G.wavelength_solve_sh(ctx, sp, bg, wave, G.options(G.SOLVE_LU), prec)
+        assert rel(r["xsec"][:3], xs[:3]) < (1e-10 if nmax <= 8 else 5e-9)
+        if nmax <= 8:
+            assert rel(r["xsec"][3], xs[3]) < 1e-10
+            assert rel(r["xsec_sh"], xsh) < 1e-9
