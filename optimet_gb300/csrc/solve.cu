@@ -396,7 +396,7 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
   w.ctx = ctx;
   const int nsplit = mv_nsplit(ctx, n);
   const int nblk = (int)((n + kDotRows - 1) / kDotRows);
-  size_t bytes = sizeof(double2) * ((size_t)(m + 1) * n + (pc ? (size_t)m * n : 0) + 2 * n +
+  size_t bytes = sizeof(double2) * ((size_t)(m + 1) * n + (pc ? (size_t)m * n : 0) + n +
                                     (size_t)nsplit * n + (size_t)nblk * (m + 2) + 3 * (m + 2)) +
                  64 * 256;
   int rc = alloc_work(ctx, w, bytes);
@@ -406,7 +406,6 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
   double2 *Vb = w.take<double2>((size_t)(m + 1) * n, off);
   double2 *Zb = pc ? w.take<double2>((size_t)m * n, off) : nullptr;
   double2 *r = w.take<double2>(n, off);
-  double2 *t = w.take<double2>(n, off);
   double2 *part = w.take<double2>((size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)), off);
   double2 *hd = w.take<double2>(2 * (m + 2), off);
   double2 *yd = w.take<double2>(m + 2, off);
@@ -429,6 +428,9 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
     } else {
       op_apply(ctx, S, n, x, part, r, b);
       beta = vec_norm(ctx, r, n, part, hd);
+      err = beta / bnorm;
+      if(err <= tol)
+        break;
     }
     if(beta == 0.0) {
       err = 0.0;
@@ -494,10 +496,10 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
     k_add_combo<double2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(pc ? Zb : Vb, n, k,
                                                                                yd, x, n);
     ctx->last_launches++;
-    // true residual for the stopping test of the next cycle
-    op_apply(ctx, S, n, x, part, t, b);
-    err = vec_norm(ctx, t, n, part, hd) / bnorm;
-    cudaStreamSynchronize(ctx->stream);
+    // the stopping test of Gmres_Zcomp (PreconditionedMatrix.cpp:916-919,
+    // 962-964): the residual estimate |g_{k+1}| / ||b||; a further cycle starts
+    // from the true residual
+    err = cur;
   }
   *iters = total;
   *relres = err;
@@ -1090,7 +1092,6 @@ int gmres_on_workspace(om_context *ctx, const M *S, long n, const double2 *b, do
   w.buf = ws;
   double2 *Vb = w.take<double2>((size_t)(m + 1) * n, off);
   double2 *r = w.take<double2>(n, off);
-  double2 *t = w.take<double2>(n, off);
   double2 *part = w.take<double2>((size_t)std::max<long>((long)nsplit * n, (long)nblk * (m + 2)), off);
   double2 *hd = w.take<double2>(2 * (m + 2), off);
   double2 *yd = w.take<double2>(m + 2, off);
@@ -1113,6 +1114,9 @@ int gmres_on_workspace(om_context *ctx, const M *S, long n, const double2 *b, do
     } else {
       matvec<M, double2>(ctx, S, n, x, part, r, b);
       beta = vec_norm(ctx, r, n, part, hd);
+      err = beta / bnorm;
+      if(err <= tol)
+        break;
     }
     if(beta == 0.0) {
       err = 0.0;
@@ -1170,9 +1174,7 @@ int gmres_on_workspace(om_context *ctx, const M *S, long n, const double2 *b, do
     cudaMemcpyAsync(yd, yh.data(), sizeof(double2) * k, cudaMemcpyHostToDevice, ctx->stream);
     k_add_combo<double2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(Vb, n, k, yd, x, n);
     ctx->last_launches++;
-    matvec<M, double2>(ctx, S, n, x, part, t, b);
-    err = vec_norm(ctx, t, n, part, hd) / bnorm;
-    cudaStreamSynchronize(ctx->stream);
+    err = cur;  // the estimate, as gmres64
   }
   *iters = total;
   *relres = err;
@@ -1211,7 +1213,7 @@ extern "C" int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve
   const size_t nsplit = (size_t)mv_nsplit(ctx, n);
   const size_t nblk = (size_t)((n + kDotRows - 1) / kDotRows);
   const size_t z = sizeof(double2);
-  const size_t need = 2 * round(z * n) + round(z * (size_t)(m + 1) * n) + 2 * round(z * n) +
+  const size_t need = 2 * round(z * n) + round(z * (size_t)(m + 1) * n) + round(z * n) +
                       round(z * std::max(nsplit * n, nblk * (size_t)(m + 2))) +
                       round(z * 2 * (size_t)(m + 2)) + round(z * (size_t)(m + 2));
   if(need > kNoAllocBytes) {
