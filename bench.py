@@ -191,8 +191,11 @@ def gpu_arm(args, w):
     bg = G.medium(complex(w["host"]) ** 2)
     pr = G.Problem(ctx, sp, bg, G.plane_wave(w["lam"]))
     n = pr.n
-    mixed_opts = G.options(G.SOLVE_FGMRES_MIXED, tol=1e-8, max_iter=30, restarts=4, inner_iter=80,
-                           inner_tol=1e-4)
+    # outer tolerance 1e-7, inner 1e-3: two outer steps of 4 FP32 matvecs each.
+    # Q_ext then sits ~2e-9 from FP64, set by the complex64 rounding of S (the
+    # same as with tol 1e-8 / inner 1e-4, which takes 10 FP32 matvecs)
+    mixed_opts = G.options(G.SOLVE_FGMRES_MIXED, tol=1e-7, max_iter=30, restarts=4, inner_iter=80,
+                           inner_tol=1e-3)
     fp64_opts = G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=400, restarts=6)
 
     def step(i, mixed):
@@ -344,7 +347,7 @@ def gpu_arm(args, w):
         "config": {"workload": args.workload + ": " + w["desc"], "unknowns": n,
                    "parallelism": f"replicas x{world}, {args.slots} serving slots per GPU",
                    "l2": "inputs larger than L2 (no flush)",
-                   "solver": "FGMRES(FP64 outer, tol 1e-8) + GMRES(FP32 inner, 80 it, tol 1e-4)",
+                   "solver": "FGMRES(FP64 outer, tol 1e-7) + GMRES(FP32 inner, 80 it, tol 1e-3)",
                    "timing": "CUDA events on every slot's stream (om_server_mark) around the K requests",
                    "launch_tuning": {"mixed": tuning, "fp64": tuning64,
                                      "how": "om_server_autotune on warm-up requests"}},
