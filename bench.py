@@ -277,7 +277,7 @@ def gpu_arm(args, w):
     # solve. Same requests for both forms; a slot keeps its problem resident
     # across wavelengths (cluster_key) like the reference's scan keeps its
     # Geometry.
-    def served(opts, precision, k, key, tuning=None, tune_count=4):
+    def served(opts, precision, k, key, tuning=None, tune_count=6):
         srv = G.Server(local, 0, args.slots)
         lam = lambda i: G.plane_wave(w["lam"] + 0.25 * nm * i)
         # launch tuning: the server's autotuner on warm-up requests (untimed)

@@ -523,11 +523,11 @@ int om_server_autotune(om_server *srv, const om_request *rq, int count, double s
     return OM_ERR_INVALID;
   // the TMA matvec's 144 KB of stage buffers leave no room for another slot's
   // assembly on the SM, so the overlapping candidates use the plain kernel
-  static const om_tuning cands[] = {{8, 8, -1, -1, -1, 1},
-                                    {6, 3, 50, 50, -1, 0},
-                                    {4, 2, 50, 50, -1, 0},
-                                    {4, 2, -1, -1, -1, 0},
-                                    {3, 2, 50, 50, -1, 0}};
+  static const om_tuning cands[] = {{8, 8, -1, -1, -1, 1}, {6, 3, 50, 50, -1, 0},
+                                    {4, 2, 50, 50, -1, 0}, {4, 2, -1, -1, -1, 0},
+                                    {3, 2, 50, 50, -1, 0}, {3, 2, -1, -1, -1, 0},
+                                    {4, 1, -1, -1, -1, 0}, {5, 2, -1, -1, -1, 0},
+                                    {4, 3, -1, -1, -1, 0}, {6, 2, -1, -1, -1, 0}};
   const int nslots = (int)srv->slots.size();
   double best = 1e300;
   om_tuning pick = cands[0];
