@@ -279,11 +279,11 @@ void om_server::run_slot(Slot &s) {
         break;
       const bool head_single =
           !batchable(queue.front()) && reserved - s.resident + queue.front().bytes <= budget;
+      std::vector<Job> run;
       if(batch_max > 1 && !head_single) {
         // the batchable requests of the queue, in arrival order, up to
-        // batch_max and within the budget; the slot's resident problem goes
-        // first
-        std::vector<Job> run;
+        // batch_max and within the budget (none: a batchable head that fits
+        // only on the single-request path takes that path)
         size_t take = reserved - s.resident;
         for(auto it = queue.begin(); it != queue.end() && (int)run.size() < batch_max;) {
           if(batchable(*it) && take + it->batch_bytes <= budget) {
@@ -295,15 +295,15 @@ void om_server::run_slot(Slot &s) {
             ++it;
           }
         }
-        if(run.empty())  // only a batchable head that fits on its own path
-          goto single;
+      }
+      if(!run.empty()) {
+        // the slot's resident problem goes first
         lk.unlock();
         if(s.resident || s.pr)
           drop_resident(this, s);
         serve_batch(s, run);
         continue;
       }
-    single:
       job = std::move(queue.front());
       queue.pop_front();
       reserved -= s.resident;
