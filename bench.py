@@ -771,6 +771,50 @@ def fp64_gemm_tflops():
     return 2.0 * 8192 ** 3 / best / 1e12
 
 
+def lu_mixed_arm(args):
+    """c2 through the precision form's LU role: FP32 LU of the complex64
+    matrix (tensor-core trailing updates) as the preconditioner of FP64 outer
+    FGMRES with compensated residuals (GMRES-based iterative refinement), one
+    wavelength-solve per step, against the FP64 GMRES solve of the same
+    cluster."""
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    w = WORKLOADS["c2"]
+    xyz, rad = cluster(w)
+    ctx = G.Context(0)
+    sp = G.spheres_array(xyz, rad, complex(w["index"]) ** 2, w["nmax"])
+    pr = G.Problem(ctx, sp, G.medium(complex(w["host"]) ** 2), G.plane_wave(w["lam"]))
+    pr.source_vector(copy=False)
+    pr.assemble(G.FF, G.C128)
+    pr.solve(G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=400, restarts=6))
+    ref = pr.cross_sections()
+    pr.close()
+    pr = G.Problem(ctx, sp, G.medium(complex(w["host"]) ** 2), G.plane_wave(w["lam"]))
+    opts = G.options(G.SOLVE_LU_MIXED, tol=1e-9, max_iter=30, restarts=4)
+    times, st = [], None
+    with ClockSampler(0) as clk:
+        for _ in range(max(1, args.steps)):
+            ctx.synchronize()
+            ctx.mark()
+            pr.source_vector(copy=False)
+            pr.assemble(G.FF, G.C64)
+            st = pr.solve(opts)
+            xs = pr.cross_sections()
+            times.append(ctx.mark() * 1e-3)
+    t = float(np.median(times))
+    err = float(abs(xs[0] - ref[0]) / abs(ref[0]))
+    pr.close()
+    ctx.close()
+    return {"metric": METRIC, "value": 1.0 / t, "unit": UNIT, "n_gpus": 1, "steps": len(times),
+            "warmup": 0, "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 (FP32) LU + c128 (FP64) refinement",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "c2 LU role: " + w["desc"],
+                       "solver": "GMRES-based iterative refinement: FP64 residuals, GMRES on the system left-preconditioned by the FP32 LU (tensor-core trailing updates), tol 1e-9"},
+            "refinement_iterations": st.iterations, "qext_rel_err_vs_fp64": err, "clocks": clk.summary()}
+
+
 def near_field_arm(args):
     """c1 near field: |E|^2 on a 256 x 256 grid in the z = 0 plane (two z
     layers at +-0.1 nm, as the reference's grid needs two steps: 131,072
@@ -897,7 +941,8 @@ def main():
     ap.add_argument("--slots", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c1f", "c3", "c4", "aca"])
+    ap.add_argument("--workload", default="c2",
+                    choices=sorted(WORKLOADS) + ["c1f", "c2lu", "c3", "c4", "aca"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--single-stream", action="store_true",
                     help="only the single-stream measurement of both forms (profiling runs)")
@@ -920,6 +965,8 @@ def main():
         out = aca_arm(args) if args.impl != "reference" else None
     elif args.workload == "c1f":
         out = near_field_arm(args) if args.impl != "reference" else None
+    elif args.workload == "c2lu":
+        out = lu_mixed_arm(args) if args.impl != "reference" else None
     elif args.workload == "c3":
         out = batch_arm(args) if args.impl != "reference" else None
     elif args.workload == "c4":

@@ -498,8 +498,23 @@ int gmres64(om_context *ctx, const M *S, long n, const double2 *b, double2 *x, d
     ctx->last_launches++;
     // the stopping test of Gmres_Zcomp (PreconditionedMatrix.cpp:916-919,
     // 962-964): the residual estimate |g_{k+1}| / ||b||; a further cycle starts
-    // from the true residual
+    // from the true residual. The estimate assumes that y solves the small
+    // least-squares problem exactly; with a flexible preconditioner the basis
+    // Z can be ill-conditioned (an inaccurate LU), and so can R. Then the
+    // true residual decides (R's diagonal ratio, a lower bound on its
+    // condition number, above 1e6).
     err = cur;
+    if(pc && err <= tol && k > 0) {
+      double dmax = 0.0, dmin = 1e300;
+      for(int j = 0; j < k; ++j) {
+        dmax = std::max(dmax, std::abs(H[j][j]));
+        dmin = std::min(dmin, std::abs(H[j][j]));
+      }
+      if(!(dmax <= 1e6 * dmin)) {
+        op_apply(ctx, S, n, x, part, r, b);
+        err = vec_norm(ctx, r, n, part, hd) / bnorm;
+      }
+    }
   }
   *iters = total;
   *relres = err;
@@ -1019,26 +1034,102 @@ struct LuPrecond32 : PrecondFn {
   }
 };
 
+// GMRES-based iterative refinement (Carson & Higham 2018), the
+// mixed-precision LU refinement role: FP64 residuals r = b - S x of the
+// complex64 system (compensated products), each correction from GMRES on the
+// left-preconditioned system M^{-1} S d = M^{-1} r with M the FP32 LU. GMRES
+// on M^{-1} S (close to the identity) controls the correction's error, not
+// only its residual; right preconditioning with an inexact LU can leave
+// solution components along near-null directions of S that a small residual
+// does not reveal.
+struct LuLeftOp {
+  const float2 *S;
+  LuPrecond32 *lu;
+  double2 *t;  // n scratch
+};
+
+__global__ void k_sub_vec(const double2 *b, const double2 *t, double2 *y, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i < n)
+    y[i] = make_double2(b[i].x - t[i].x, b[i].y - t[i].y);
+}
+__global__ void k_add_vec(const double2 *d, double2 *x, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i < n)
+    x[i] = make_double2(x[i].x + d[i].x, x[i].y + d[i].y);
+}
+
+// y = M^{-1} S x, or y = b - M^{-1} S x when b is given
+inline void op_apply(om_context *ctx, const LuLeftOp *op, long n, const double2 *x, double2 *part,
+                     double2 *y, const double2 *b) {
+  double2 *t = b ? op->t : y;
+  matvec<float2, double2>(ctx, op->S, n, x, part, t, nullptr);
+  op->lu->apply(t, t);
+  if(b) {
+    k_sub_vec<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(b, t, y, n);
+    ctx->last_launches++;
+  }
+}
+
 int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
                        double2 *x, om_solve_stats *st) {
   om_context *ctx = pr->ctx;
+  const long n = pr->n;
   const float2 *S32 = (const float2 *)pr->d_S32[harmonic];
-  LuPrecond32 lu(ctx, pr->n);
+  LuPrecond32 lu(ctx, n);
   int rc = lu.init(S32);
   if(rc)
     return rc;
-  int it = 0;
-  double rr = 0;
-  const int outer_m = std::max(1, std::min(o->max_iter, 32));
-  rc = gmres64<float2>(ctx, S32, pr->n, b, x, o->tol, outer_m, o->restarts, &lu, &it, &rr);
+  Work w;
+  w.ctx = ctx;
+  const int nsplit = mv_nsplit(ctx, n);
+  const int nblk = (int)((n + kDotRows - 1) / kDotRows);
+  rc = alloc_work(ctx, w, sizeof(double2) * (4 * (size_t)n + (size_t)std::max<long>((long)nsplit * n, 2L * nblk) + 8) +
+                              16 * 256);
+  if(rc)
+    return rc;
+  size_t off = 0;
+  double2 *r = w.take<double2>(n, off), *c = w.take<double2>(n, off), *d = w.take<double2>(n, off);
+  double2 *t = w.take<double2>(n, off);
+  double2 *part = w.take<double2>((size_t)std::max<long>((long)nsplit * n, 2L * nblk), off);
+  double2 *hd = w.take<double2>(8, off);
+  LuLeftOp op{S32, &lu, t};
+  cudaMemsetAsync(x, 0, sizeof(double2) * n, ctx->stream);
+  const double bnorm = vec_norm(ctx, b, n, part, hd);
+  // at most 8 refinement steps per restart allowed by the options; each
+  // correction: GMRES(m) on M^{-1} S to 1e-4, two cycles at most
+  const int max_ref = 8 * std::max(1, o->restarts);
+  const int m = std::max(1, std::min(o->max_iter, 32));
+  int ref = 0, inner = 0;
+  double rr = bnorm > 0.0 ? 1.0 : 0.0;
+  for(; bnorm > 0.0; ++ref) {
+    if(ref == 0)
+      cudaMemcpyAsync(r, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    else
+      matvec<float2, double2>(ctx, S32, n, x, part, r, b);
+    rr = vec_norm(ctx, r, n, part, hd) / bnorm;
+    if(rr <= o->tol || ref == max_ref)
+      break;
+    lu.apply(r, c);
+    int it = 0;
+    double irr = 0.0;
+    const int e = gmres64<LuLeftOp>(ctx, &op, n, c, d, 1e-4, m, 2, nullptr, &it, &irr);
+    if(e && e != OM_ERR_NOT_CONVERGED)
+      return e;
+    inner += it;
+    k_add_vec<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(d, x, n);
+    ctx->last_launches++;
+  }
   if(st) {
-    st->iterations = it;
-    st->inner_iterations = lu.applied;
+    st->iterations = ref;
+    st->inner_iterations = inner;
     st->rel_residual = rr;
   }
-  if(rc == OM_ERR_NOT_CONVERGED)
+  if(rr > o->tol) {
     ctx->err = "LU-preconditioned refinement did not reach the requested tolerance";
-  return rc;
+    return OM_ERR_NOT_CONVERGED;
+  }
+  return OM_OK;
 }
 
 
