@@ -716,6 +716,151 @@ __global__ void __launch_bounds__(1024) k_lu_panel(V *A, long ld, long n, long k
   }
 }
 
+// Tall panels on many CTAs (rows >= kTallPanel). Per column c: a one-CTA
+// kernel takes the pivot from the per-CTA partial maxima (block order; the
+// larger magnitude, then the smaller row index, as k_lu_panel), swaps the two
+// rows inside the panel and publishes the pivot row; then a multi-CTA kernel
+// scales column c below the pivot, applies the rank-1 update to the panel's
+// later columns, and leaves the partial maxima of column c + 1. Each entry
+// takes the same operations as in k_lu_panel, so the factors are the same.
+constexpr long kTallPanel = 8192;
+constexpr int kPanThreads = 256;
+
+struct PanelScratch {
+  double *bestv;  // per CTA
+  long *besti;
+  void *prow;     // kNb entries of the element type: the pivot row
+  int nblk;
+};
+
+// partial maxima of |A[col, i]|^2, i >= col, one per CTA
+template <typename V>
+__global__ void __launch_bounds__(kPanThreads) k_pan_max(const V *A, long ld, long n, long col,
+                                                         PanelScratch ps) {
+  __shared__ double bv_s[kPanThreads];
+  __shared__ long bi_s[kPanThreads];
+  double bv = -1.0;
+  long bi = col;
+  for(long i = col + blockIdx.x * (long)kPanThreads + threadIdx.x; i < n;
+      i += (long)gridDim.x * kPanThreads) {
+    const double v = mag2(A[col * ld + i]);
+    if(v > bv) {
+      bv = v;
+      bi = i;
+    }
+  }
+  bv_s[threadIdx.x] = bv;
+  bi_s[threadIdx.x] = bi;
+  __syncthreads();
+  for(int h = kPanThreads / 2; h > 0; h >>= 1) {
+    if(threadIdx.x < h && (bv_s[threadIdx.x + h] > bv_s[threadIdx.x] ||
+                           (bv_s[threadIdx.x + h] == bv_s[threadIdx.x] &&
+                            bi_s[threadIdx.x + h] < bi_s[threadIdx.x]))) {
+      bv_s[threadIdx.x] = bv_s[threadIdx.x + h];
+      bi_s[threadIdx.x] = bi_s[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) {
+    ps.bestv[blockIdx.x] = bv_s[0];
+    ps.besti[blockIdx.x] = bi_s[0];
+  }
+}
+
+// the pivot of column col = k + c, the row swap inside the panel, the pivot row
+template <typename V>
+__global__ void k_pan_pivot(V *A, long ld, long k, int c, int nb, int *piv, int *info, PanelScratch ps) {
+  __shared__ long p_s;
+  const long col = k + c;
+  if(threadIdx.x == 0) {
+    double bv = ps.bestv[0];
+    long bi = ps.besti[0];
+    for(int b = 1; b < ps.nblk; ++b)
+      if(ps.bestv[b] > bv || (ps.bestv[b] == bv && ps.besti[b] < bi)) {
+        bv = ps.bestv[b];
+        bi = ps.besti[b];
+      }
+    piv[col] = (int)bi;
+    if(bv <= 0.0 && *info == 0)
+      *info = (int)col + 1;
+    p_s = bi;
+  }
+  __syncthreads();
+  const long p = p_s;
+  const int t = threadIdx.x;
+  V *prow = reinterpret_cast<V *>(ps.prow);
+  if(t < nb) {
+    V a = A[(k + t) * ld + col];
+    if(p != col) {
+      V q = A[(k + t) * ld + p];
+      A[(k + t) * ld + col] = q;
+      A[(k + t) * ld + p] = a;
+      a = q;
+    }
+    prow[t] = a;
+  }
+}
+
+// column c below the pivot scaled by 1 / pivot, the later panel columns
+// updated; partial maxima of column c + 1 (when there is one)
+template <typename V>
+__global__ void __launch_bounds__(kPanThreads) k_pan_update(V *A, long ld, long n, long k, int c, int nb,
+                                                            PanelScratch ps) {
+  __shared__ V u[kNb];
+  __shared__ double bv_s[kPanThreads];
+  __shared__ long bi_s[kPanThreads];
+  const long col = k + c;
+  const V *prow = reinterpret_cast<const V *>(ps.prow);
+  if(threadIdx.x < nb)
+    u[threadIdx.x] = prow[threadIdx.x];
+  __syncthreads();
+  const bool ok = mag2(u[c]) > 0.0;
+  const V inv = ok ? crecip(u[c]) : u[c];
+  const bool next = c + 1 < nb;
+  const long ncol = col + 1;
+  double bv = -1.0;
+  long bi = ncol;
+  for(long i = col + 1 + blockIdx.x * (long)kPanThreads + threadIdx.x; i < n;
+      i += (long)gridDim.x * kPanThreads) {
+    if(ok) {
+      V l = cmul(A[col * ld + i], inv);
+      A[col * ld + i] = l;
+      for(int j = c + 1; j < nb; ++j) {
+        V uu = u[j];
+        V a = A[(k + j) * ld + i];
+        a.x -= l.x * uu.x - l.y * uu.y;
+        a.y -= l.x * uu.y + l.y * uu.x;
+        A[(k + j) * ld + i] = a;
+      }
+    }
+    if(next && i >= ncol) {
+      const double v = mag2(A[ncol * ld + i]);
+      if(v > bv) {
+        bv = v;
+        bi = i;
+      }
+    }
+  }
+  if(!next)
+    return;
+  bv_s[threadIdx.x] = bv;
+  bi_s[threadIdx.x] = bi;
+  __syncthreads();
+  for(int h = kPanThreads / 2; h > 0; h >>= 1) {
+    if(threadIdx.x < h && (bv_s[threadIdx.x + h] > bv_s[threadIdx.x] ||
+                           (bv_s[threadIdx.x + h] == bv_s[threadIdx.x] &&
+                            bi_s[threadIdx.x + h] < bi_s[threadIdx.x]))) {
+      bv_s[threadIdx.x] = bv_s[threadIdx.x + h];
+      bi_s[threadIdx.x] = bi_s[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) {
+    ps.bestv[blockIdx.x] = bv_s[0];
+    ps.besti[blockIdx.x] = bi_s[0];
+  }
+}
+
 // Apply the panel's row interchanges to the columns outside the panel.
 template <typename V>
 __global__ void k_lu_swap(V *A, long ld, long n, long k, int nb, const int *piv) {
@@ -854,11 +999,36 @@ __global__ void k_tri_update(const V *A, long ld, long k, int nb, V *b, long lo,
 template <typename V>
 int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   cudaMemsetAsync(info, 0, 2 * sizeof(int), ctx->stream);
+  Work ws;
+  ws.ctx = ctx;
+  PanelScratch ps{};
+  const int maxblk = 4 * ctx->sm_count;
+  if(n >= kTallPanel) {
+    const int rc = alloc_work(ctx, ws, maxblk * (sizeof(double) + sizeof(long)) + kNb * sizeof(V) + 3 * 256);
+    if(rc)
+      return rc;
+    size_t off = 0;
+    ps.bestv = ws.take<double>(maxblk, off);
+    ps.besti = ws.take<long>(maxblk, off);
+    ps.prow = ws.take<V>(kNb, off);
+  }
   for(long k = 0; k < n; k += kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
-    k_lu_panel<V><<<1, 1024, 0, ctx->stream>>>(A, n, n, k, nb, piv, info);
+    const long rows = n - k;
+    if(rows >= kTallPanel) {
+      ps.nblk = (int)std::min<long>(maxblk, (rows + kPanThreads - 1) / kPanThreads);
+      k_pan_max<V><<<ps.nblk, kPanThreads, 0, ctx->stream>>>(A, n, n, k, ps);
+      for(int c = 0; c < nb; ++c) {
+        k_pan_pivot<V><<<1, kNb, 0, ctx->stream>>>(A, n, k, c, nb, piv, info, ps);
+        k_pan_update<V><<<ps.nblk, kPanThreads, 0, ctx->stream>>>(A, n, n, k, c, nb, ps);
+      }
+      ctx->last_launches += 1 + 2 * nb;
+    } else {
+      k_lu_panel<V><<<1, 1024, 0, ctx->stream>>>(A, n, n, k, nb, piv, info);
+      ctx->last_launches++;
+    }
     k_lu_swap<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, n, k, nb, piv);
-    ctx->last_launches += 2;
+    ctx->last_launches++;
     const long rest = n - k - nb;
     if(rest > 0) {
       k_lu_trsm<V><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, n, k, nb);
@@ -918,10 +1088,12 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   size_t off = 0;
   double2 *A = w.take<double2>((size_t)n * n, off);
   int *piv = w.take<int>(n, off);
-  int *info = w.take<int>(1, off);
+  int *info = w.take<int>(2, off);
   cudaMemcpyAsync(A, pr->d_S[harmonic], sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToDevice,
                   ctx->stream);
-  lu_factor<double2>(ctx, A, n, piv, info);
+  rc = lu_factor<double2>(ctx, A, n, piv, info);
+  if(rc)
+    return rc;
   cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
   lu_solve_vec<double2>(ctx, A, n, piv, x);
   int hinfo = 0;
@@ -1011,7 +1183,9 @@ struct LuPrecond32 : PrecondFn {
     piv = w.take<int>(n, off);
     info = w.take<int>(2, off);
     cudaMemcpyAsync(A, S32, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, ctx->stream);
-    lu_factor<float2>(ctx, A, n, piv, info);
+    rc = lu_factor<float2>(ctx, A, n, piv, info);
+    if(rc)
+      return rc;
     int hinfo[2] = {0, 0};
     cudaMemcpyAsync(hinfo, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     cudaStreamSynchronize(ctx->stream);

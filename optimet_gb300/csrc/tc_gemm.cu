@@ -6,15 +6,17 @@
 // Each FP32 component x is split into bf16 x_hi + x_lo (x_lo = bf16(x - x_hi));
 // a real product is x_hi y_hi + x_hi y_lo + x_lo y_hi (three bf16 MMAs with
 // FP32 accumulation, about 17 significant bits), so
-//   Re(AB) = Ar Br - Ai Bi,  Im(AB) = Ar Bi + Ai Br
-// takes 12 MMAs of M = 128, N = 64, K = 16 per 16 columns of k. One CTA of
-// 128 threads owns a 128 x 64 tile of C: the operands are split and stored in
-// shared memory in the canonical K-major layout without swizzle (8 x 16-byte
-// core matrices), thread 0 issues the MMAs into three TMEM accumulators
-// (Ar Br, Ai Bi, Ar Bi + Ai Br; 64 columns each), commits them to an
-// mbarrier, and the four warps read their 32 TMEM lanes back
-// (tcgen05.ld 32x32b) and subtract from C. Waits are bounded: on time-out
-// the kernel raises *err, still frees its TMEM and leaves C untouched.
+//   Re(AB) = Ar Br + Ai (-Bi),  Im(AB) = Ar Bi + Ai Br
+// takes 12 MMAs of M = 128, N = 64, K = 16 per 16 columns of k (B's imaginary
+// part is staged twice, with both signs; a sign flip is exact in bf16). One
+// CTA of 128 threads owns a 128 x 64 tile of C: the operands are split and
+// stored in shared memory in the canonical K-major layout without swizzle
+// (8 x 16-byte core matrices), thread 0 issues the MMAs into two TMEM
+// accumulators (Re, Im; 64 columns each: 128 TMEM columns, four CTAs per
+// SM), commits them to an mbarrier, and the four warps read their 32 TMEM
+// lanes back (tcgen05.ld 32x32b) and subtract from C, whose first 16 columns
+// are loaded while the MMAs run. Waits are bounded: on time-out the kernel
+// raises *err, still frees its TMEM and leaves C untouched.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -25,10 +27,11 @@ namespace om {
 namespace {
 
 constexpr int kTcM = 128, kTcN = 64, kTcK = 32;
-constexpr uint32_t kTmemCols = 256;  // 3 x 64 accumulator columns, rounded up to a power of 2
+constexpr uint32_t kTmemCols = 128;  // 2 x 64 accumulator columns
 // shared-memory operand tiles (bf16): A parts 128 x 32, B parts 64 x 32
+// (Ar, Ai, Br, Bi, -Bi: hi and lo each)
 constexpr int kAPart = kTcM * kTcK * 2, kBPart = kTcN * kTcK * 2;
-constexpr int kTcSmem = 4 * kAPart + 4 * kBPart + 64;
+constexpr int kTcSmem = 4 * kAPart + 6 * kBPart + 64;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -77,9 +80,9 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda,
   extern __shared__ __align__(1024) unsigned char tsm[];
   unsigned char *Arh = tsm, *Arl = tsm + kAPart, *Aih = tsm + 2 * kAPart, *Ail = tsm + 3 * kAPart;
   unsigned char *Brh = tsm + 4 * kAPart, *Brl = Brh + kBPart, *Bih = Brh + 2 * kBPart,
-                *Bil = Brh + 3 * kBPart;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(tsm + 4 * kAPart + 4 * kBPart);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tsm + 4 * kAPart + 4 * kBPart + 16);
+                *Bil = Brh + 3 * kBPart, *Bnh = Brh + 4 * kBPart, *Bnl = Brh + 5 * kBPart;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(tsm + 4 * kAPart + 6 * kBPart);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tsm + 4 * kAPart + 6 * kBPart + 16);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const long r0 = (long)blockIdx.x * kTcM, c0 = (long)blockIdx.y * kTcN;
 
@@ -117,6 +120,7 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda,
       const int off = kmajor_off(j, c);
       split_store(Brh, Brl, off, v.x);
       split_store(Bih, Bil, off, v.y);
+      split_store(Bnh, Bnl, off, -v.y);
     }
   }
   // generic-proxy stores -> visible to the tensor core (async proxy)
@@ -125,33 +129,40 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda,
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t d_rr = tmem, d_ii = tmem + kTcN, d_ri = tmem + 2 * kTcN;
+  const uint32_t d_re = tmem, d_im = tmem + kTcN;
 
   if(t == 0) {
     for(int s = 0; s < kTcK / 16; ++s) {
       const uint32_t ko = s * 256;  // two core matrices along K per MMA
       auto da = [&](unsigned char *p) { return umma_desc(smem_addr(p) + ko, 128, 512); };
       const uint32_t acc = s > 0;  // the first K step overwrites the accumulators
-      // Ar Br
-      mma_bf16(d_rr, da(Arh), da(Brh), acc);
-      mma_bf16(d_rr, da(Arh), da(Brl), 1);
-      mma_bf16(d_rr, da(Arl), da(Brh), 1);
-      // Ai Bi
-      mma_bf16(d_ii, da(Aih), da(Bih), acc);
-      mma_bf16(d_ii, da(Aih), da(Bil), 1);
-      mma_bf16(d_ii, da(Ail), da(Bih), 1);
-      // Ar Bi + Ai Br
-      mma_bf16(d_ri, da(Arh), da(Bih), acc);
-      mma_bf16(d_ri, da(Arh), da(Bil), 1);
-      mma_bf16(d_ri, da(Arl), da(Bih), 1);
-      mma_bf16(d_ri, da(Aih), da(Brh), 1);
-      mma_bf16(d_ri, da(Aih), da(Brl), 1);
-      mma_bf16(d_ri, da(Ail), da(Brh), 1);
+      // Re: Ar Br + Ai (-Bi)
+      mma_bf16(d_re, da(Arh), da(Brh), acc);
+      mma_bf16(d_re, da(Arh), da(Brl), 1);
+      mma_bf16(d_re, da(Arl), da(Brh), 1);
+      mma_bf16(d_re, da(Aih), da(Bnh), 1);
+      mma_bf16(d_re, da(Aih), da(Bnl), 1);
+      mma_bf16(d_re, da(Ail), da(Bnh), 1);
+      // Im: Ar Bi + Ai Br
+      mma_bf16(d_im, da(Arh), da(Bih), acc);
+      mma_bf16(d_im, da(Arh), da(Bil), 1);
+      mma_bf16(d_im, da(Arl), da(Bih), 1);
+      mma_bf16(d_im, da(Aih), da(Brh), 1);
+      mma_bf16(d_im, da(Aih), da(Brl), 1);
+      mma_bf16(d_im, da(Ail), da(Brh), 1);
     }
     asm volatile(
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
             smem_addr(mbar))
         : "memory");
+  }
+  // the first 16 columns of this thread's row of C, loaded while the MMAs run
+  const long r = r0 + warp * 32 + lane;
+  float2 cpre[16];
+#pragma unroll
+  for(int q = 0; q < 16; ++q) {
+    const long col = c0 + q;
+    cpre[q] = (r < m && col < n) ? C[col * ldc + r] : make_float2(0.f, 0.f);
   }
   // bounded wait for the MMAs (phase 0 of the mbarrier)
   uint32_t done = 0;
@@ -172,28 +183,27 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda,
       atomicExch(err, 1);
   } else {
     // warp w reads TMEM lanes 32 w .. 32 w + 31 = rows r0 + 32 w + lane
-    const long r = r0 + warp * 32 + lane;
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
     for(int cc = 0; cc < kTcN; cc += 16) {
-      uint32_t a[16], b[16], c[16];
+      uint32_t a[16], b[16];
 #define OM_TMEM_LD16(dst, addr)                                                                     \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
                : "=r"(dst[0]), "=r"(dst[1]), "=r"(dst[2]), "=r"(dst[3]), "=r"(dst[4]), "=r"(dst[5]),  \
                  "=r"(dst[6]), "=r"(dst[7]), "=r"(dst[8]), "=r"(dst[9]), "=r"(dst[10]),              \
                  "=r"(dst[11]), "=r"(dst[12]), "=r"(dst[13]), "=r"(dst[14]), "=r"(dst[15])           \
                : "r"(addr))
-      OM_TMEM_LD16(a, d_rr + lane_base + cc);
-      OM_TMEM_LD16(b, d_ii + lane_base + cc);
-      OM_TMEM_LD16(c, d_ri + lane_base + cc);
+      OM_TMEM_LD16(a, d_re + lane_base + cc);
+      OM_TMEM_LD16(b, d_im + lane_base + cc);
 #undef OM_TMEM_LD16
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if(r < m) {
+#pragma unroll
         for(int q = 0; q < 16; ++q) {
           const long col = c0 + cc + q;
           if(col < n) {
-            float2 v = C[col * ldc + r];
-            v.x -= __uint_as_float(a[q]) - __uint_as_float(b[q]);
-            v.y -= __uint_as_float(c[q]);
+            float2 v = cc == 0 ? cpre[q] : C[col * ldc + r];
+            v.x -= __uint_as_float(a[q]);
+            v.y -= __uint_as_float(b[q]);
             C[col * ldc + r] = v;
           }
         }

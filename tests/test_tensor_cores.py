@@ -67,3 +67,21 @@ def test_lu_mixed_with_and_without_tensor_cores(G, ctx):
         assert np.max(np.abs(xs - ref) / np.abs(ref)) < 1e-6, (tc, xs, ref)
     # the FP64 refinement absorbs the weaker factorisation in a few more steps
     assert out[1][1] <= out[0][1] + 10
+
+
+def test_lu_tall_panels(G, ctx):
+    """n = 8,208 unknowns: the LU panels run on many CTAs (tall-panel path,
+    from 8,192 rows). FP64 LU against FP64 GMRES, and the LU refinement role
+    (complex64 LU with tensor-core updates, GMRES-based refinement) against
+    FP64."""
+    rng = np.random.default_rng(33)
+    xyz, rad = random_cluster(rng, 171, 2400 * nm, 40 * nm, 60 * nm, 20 * nm)
+    sp = G.spheres_array(xyz, rad, (1.8 + 0.02j) ** 2, 4)     # P = 24: n = 8,208
+    bg, wave = G.medium(1.0), G.plane_wave(700 * nm)
+    ref = G.wavelength_solve(ctx, sp, bg, wave, G.options(G.SOLVE_GMRES, tol=1e-13, max_iter=300), G.C128)[0]
+    lu = G.wavelength_solve(ctx, sp, bg, wave, G.options(G.SOLVE_LU), G.C128)[0]
+    assert np.max(np.abs(lu - ref) / np.abs(ref)) < 1e-10
+    xs, _, _, st = G.wavelength_solve(ctx, sp, bg, wave,
+                                      G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4), G.C64)
+    assert st.rel_residual <= 1e-10
+    assert np.max(np.abs(xs - ref) / np.abs(ref)) < 1e-6
