@@ -959,39 +959,62 @@ template <typename V> __global__ void k_lu_permute(V *b, long n, const int *piv)
   }
 }
 
-// Triangular solves, one block of kNb rows at a time.
-template <typename V>
-__global__ void k_tri_diag(const V *A, long ld, long k, int nb, V *b, int upper) {
-  if(threadIdx.x != 0)
-    return;
-  if(!upper) {
-    for(int r = 0; r < nb; ++r) {
-      V v = b[k + r];
-      for(int s = 0; s < r; ++s)
-        v = cfma(A[(k + s) * ld + k + r], make_neg(b[k + s]), v);
-      b[k + r] = v;
-    }
-  } else {
-    for(int r = nb - 1; r >= 0; --r) {
-      V v = b[k + r];
-      for(int s = r + 1; s < nb; ++s)
-        v = cfma(A[(k + s) * ld + k + r], make_neg(b[k + s]), v);
-      V d = A[(k + r) * ld + k + r];
-      b[k + r] = cmul(v, crecip(d));
-    }
-  }
+// One block of kNb rows of a triangular solve in a single launch: every CTA
+// solves the diagonal block from src[k .. k+nb) in shared memory (warp 0, a
+// lane per row: forward with the unit lower factor, or backward with the upper
+// factor and its diagonal), then updates its rows [lo, hi) of src outside the
+// block; CTA 0 writes the block's solution to dst. The rows read and the rows
+// written are disjoint, so the CTAs need no ordering among themselves.
+template <typename V> __device__ __forceinline__ V shfl_v(V a, int src) {
+  a.x = __shfl_sync(0xffffffffu, a.x, src);
+  a.y = __shfl_sync(0xffffffffu, a.y, src);
+  return a;
 }
 
-// rows i outside [k, k+nb): b[i] -= A[i, k:k+nb) b[k:k+nb)  (below for L, above for U)
 template <typename V>
-__global__ void k_tri_update(const V *A, long ld, long k, int nb, V *b, long lo, long hi) {
+__global__ void __launch_bounds__(256) k_tri_block(const V *A, long ld, long k, int nb, V *src, V *dst,
+                                                   long lo, long hi, int upper) {
+  __shared__ V Ad[kNb][kNb + 1];
+  __shared__ V xs[kNb];
+  for(int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+    const int r = idx % nb, c = idx / nb;
+    Ad[r][c] = A[(k + c) * ld + k + r];
+  }
+  __syncthreads();
+  if(threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    V v;
+    v.x = v.y = 0;
+    if(lane < nb)
+      v = src[k + lane];
+    if(!upper) {
+      for(int c = 0; c < nb; ++c) {
+        const V xc = shfl_v(v, c);
+        if(lane > c && lane < nb)
+          v = cfma(Ad[lane][c], make_neg(xc), v);
+      }
+    } else {
+      for(int c = nb - 1; c >= 0; --c) {
+        if(lane == c)
+          v = cmul(v, crecip(Ad[c][c]));
+        const V xc = shfl_v(v, c);
+        if(lane < c)
+          v = cfma(Ad[lane][c], make_neg(xc), v);
+      }
+    }
+    if(lane < nb)
+      xs[lane] = v;
+  }
+  __syncthreads();
+  if(blockIdx.x == 0 && threadIdx.x < nb)
+    dst[k + threadIdx.x] = xs[threadIdx.x];
   const long i = lo + blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if(i >= hi)
-    return;
-  V v = b[i];
-  for(int s = 0; s < nb; ++s)
-    v = cfma(A[(k + s) * ld + i], make_neg(b[k + s]), v);
-  b[i] = v;
+  if(i < hi) {
+    V v = src[i];
+    for(int c = 0; c < nb; ++c)
+      v = cfma(A[(k + c) * ld + i], make_neg(xs[c]), v);
+    src[i] = v;
+  }
 }
 
 // info[0]: first zero pivot (1-based) or 0; info[1]: set when a tensor-core
@@ -1049,23 +1072,27 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   return OM_OK;
 }
 
-template <typename V> void lu_solve_vec(om_context *ctx, const V *A, long n, const int *piv, V *b) {
+// b := A^{-1} b with A = P^T L U from lu_factor; y: n entries of scratch.
+// 1 + 2 ceil(n / kNb) launches, all stream-ordered (capturable as a graph).
+template <typename V>
+int lu_solve_vec(om_context *ctx, const V *A, long n, const int *piv, V *b, V *y) {
   k_lu_permute<V><<<1, 32, 0, ctx->stream>>>(b, n, piv);
-  ctx->last_launches++;
+  int launches = 1;
   for(long k = 0; k < n; k += kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
-    k_tri_diag<V><<<1, 32, 0, ctx->stream>>>(A, n, k, nb, b, 0);
-    if(k + nb < n)
-      k_tri_update<V><<<blocks_for(n - k - nb, 256), 256, 0, ctx->stream>>>(A, n, k, nb, b, k + nb, n);
-    ctx->last_launches += 2;
+    const long rows = n - k - nb;
+    k_tri_block<V><<<(unsigned)std::max<long>(1, blocks_for(rows, 256)), 256, 0, ctx->stream>>>(
+        A, n, k, nb, b, y, k + nb, n, 0);
+    ++launches;
   }
   for(long k = ((n - 1) / kNb) * kNb; k >= 0; k -= kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
-    k_tri_diag<V><<<1, 32, 0, ctx->stream>>>(A, n, k, nb, b, 1);
-    if(k > 0)
-      k_tri_update<V><<<blocks_for(k, 256), 256, 0, ctx->stream>>>(A, n, k, nb, b, 0, k);
-    ctx->last_launches += 2;
+    k_tri_block<V><<<(unsigned)std::max<long>(1, blocks_for(k, 256)), 256, 0, ctx->stream>>>(
+        A, n, k, nb, y, b, 0, k, 1);
+    ++launches;
   }
+  ctx->last_launches += launches;
+  return launches;
 }
 
 }  // namespace
@@ -1081,12 +1108,13 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   }
   Work w;
   w.ctx = ctx;
-  size_t bytes = sizeof(double2) * (size_t)n * n + sizeof(int) * (n + 1) + 1024;
+  size_t bytes = sizeof(double2) * ((size_t)n * n + n) + sizeof(int) * (n + 2) + 1024;
   int rc = alloc_work(ctx, w, bytes);
   if(rc)
     return rc;
   size_t off = 0;
   double2 *A = w.take<double2>((size_t)n * n, off);
+  double2 *y = w.take<double2>(n, off);
   int *piv = w.take<int>(n, off);
   int *info = w.take<int>(2, off);
   cudaMemcpyAsync(A, pr->d_S[harmonic], sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToDevice,
@@ -1095,7 +1123,7 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   if(rc)
     return rc;
   cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
-  lu_solve_vec<double2>(ctx, A, n, piv, x);
+  lu_solve_vec<double2>(ctx, A, n, piv, x, y);
   int hinfo = 0;
   cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
@@ -1168,18 +1196,26 @@ struct LuPrecond32 : PrecondFn {
   om_context *ctx;
   long n;
   Work w;
-  float2 *A = nullptr, *v32 = nullptr;
+  float2 *A = nullptr, *v32 = nullptr, *y32 = nullptr;
   int *piv = nullptr, *info = nullptr;
   int applied = 0;
+  // the triangular solves on v32, captured once as a graph and replayed
+  cudaGraphExec_t solve_graph = nullptr;
+  int solve_launches = 0;
   LuPrecond32(om_context *c, long n_) : ctx(c), n(n_) { w.ctx = c; }
+  ~LuPrecond32() {
+    if(solve_graph)
+      cudaGraphExecDestroy(solve_graph);
+  }
   int init(const float2 *S32) {
-    size_t bytes = sizeof(float2) * ((size_t)n * n + n) + sizeof(int) * (n + 1) + 1024;
+    size_t bytes = sizeof(float2) * ((size_t)n * n + 2 * n) + sizeof(int) * (n + 2) + 1024;
     int rc = alloc_work(ctx, w, bytes);
     if(rc)
       return rc;
     size_t off = 0;
     A = w.take<float2>((size_t)n * n, off);
     v32 = w.take<float2>(n, off);
+    y32 = w.take<float2>(n, off);
     piv = w.take<int>(n, off);
     info = w.take<int>(2, off);
     cudaMemcpyAsync(A, S32, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, ctx->stream);
@@ -1197,11 +1233,30 @@ struct LuPrecond32 : PrecondFn {
       ctx->err = "singular complex64 matrix: zero pivot at column " + std::to_string(hinfo[0]);
       return OM_ERR_SINGULAR;
     }
+    // capture the solve sequence (its pointers are fixed); plain launches if
+    // capture is refused
+    cudaGraph_t g = nullptr;
+    if(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const int before = ctx->last_launches;
+      solve_launches = lu_solve_vec<float2>(ctx, A, n, piv, v32, y32);
+      ctx->last_launches = before;
+      if(cudaStreamEndCapture(ctx->stream, &g) != cudaSuccess ||
+         cudaGraphInstantiate(&solve_graph, g, 0) != cudaSuccess)
+        solve_graph = nullptr;
+      if(g)
+        cudaGraphDestroy(g);
+    }
+    cudaGetLastError();
     return OM_OK;
   }
   void apply(const double2 *v, double2 *z) override {
     k_scale_copy<double2, float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v, 1.0, v32, n);
-    lu_solve_vec<float2>(ctx, A, n, piv, v32);
+    if(solve_graph) {
+      cudaGraphLaunch(solve_graph, ctx->stream);
+      ctx->last_launches += solve_launches;
+    } else {
+      lu_solve_vec<float2>(ctx, A, n, piv, v32, y32);
+    }
     k_scale_copy<float2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v32, 1.0, z, n);
     ctx->last_launches += 2;
     ++applied;
