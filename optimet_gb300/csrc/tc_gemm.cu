@@ -97,30 +97,36 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda,
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
 
-  // A tile: thread t owns row r0 + t (coalesced down each column)
+  // A tile: thread t owns row r0 + t (coalesced down each column); all of a
+  // thread's loads are issued before the first split, so that they are in
+  // flight together
   {
     const long r = r0 + t;
+    float2 av[kTcK];
+#pragma unroll
+    for(int c = 0; c < kTcK; ++c)
+      av[c] = (c < k && r < m) ? A[(long)c * lda + r] : make_float2(0.f, 0.f);
+#pragma unroll
     for(int c = 0; c < kTcK; ++c) {
-      float2 v = make_float2(0.f, 0.f);
-      if(c < k && r < m)
-        v = A[(long)c * lda + r];
       const int off = kmajor_off(t, c);
-      split_store(Arh, Arl, off, v.x);
-      split_store(Aih, Ail, off, v.y);
+      split_store(Arh, Arl, off, av[c].x);
+      split_store(Aih, Ail, off, av[c].y);
     }
   }
   // B tile as N x K: thread t owns column c0 + t / 2, half of K (contiguous in memory)
   {
     const int j = t >> 1, cb = (t & 1) * 16;
     const long col = c0 + j;
-    for(int c = cb; c < cb + 16; ++c) {
-      float2 v = make_float2(0.f, 0.f);
-      if(c < k && col < n)
-        v = B[col * ldb + c];
-      const int off = kmajor_off(j, c);
-      split_store(Brh, Brl, off, v.x);
-      split_store(Bih, Bil, off, v.y);
-      split_store(Bnh, Bnl, off, -v.y);
+    float2 bv[16];
+#pragma unroll
+    for(int c = 0; c < 16; ++c)
+      bv[c] = (cb + c < k && col < n) ? B[col * ldb + cb + c] : make_float2(0.f, 0.f);
+#pragma unroll
+    for(int c = 0; c < 16; ++c) {
+      const int off = kmajor_off(j, cb + c);
+      split_store(Brh, Brl, off, bv[c].x);
+      split_store(Bih, Bil, off, bv[c].y);
+      split_store(Bnh, Bnl, off, -bv[c].y);
     }
   }
   // generic-proxy stores -> visible to the tensor core (async proxy)
