@@ -45,7 +45,8 @@ extern "C" {
 #define OM_SOLVE_LU 0             /* dense LU, partial pivoting: ScalapackSolver pzgesv role */
 #define OM_SOLVE_GMRES 1          /* restarted GMRES: MatrixBelosSolver / Gmres_Zcomp role */
 #define OM_SOLVE_FGMRES_MIXED 2   /* FP64 outer FGMRES around FP32 inner GMRES on the C64 matrix */
-#define OM_SOLVE_LU_MIXED 3       /* FP32 LU + FP64 iterative refinement */
+#define OM_SOLVE_LU_MIXED 3       /* FP32 LU + FP64 iterative refinement (GMRES-IR: GMRES on the system
+                                     left-preconditioned by the LU, FP64-accurate residuals) */
 
 typedef struct om_context om_context;
 typedef struct om_problem om_problem;
@@ -87,8 +88,10 @@ typedef struct {
 } om_solve_options;
 
 typedef struct {
-  int iterations;        /* Krylov iterations (outer for the mixed form) */
-  int inner_iterations;  /* total inner FP32 iterations (mixed) */
+  int iterations;        /* Krylov iterations; OM_SOLVE_FGMRES_MIXED: outer FGMRES steps;
+                            OM_SOLVE_LU_MIXED: refinement steps */
+  int inner_iterations;  /* OM_SOLVE_FGMRES_MIXED: inner FP32 GMRES iterations;
+                            OM_SOLVE_LU_MIXED: GMRES iterations on the LU-preconditioned system */
   double rel_residual;   /* final FP64 relative residual */
   double seconds;        /* device time of the solve */
 } om_solve_stats;
