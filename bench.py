@@ -373,12 +373,15 @@ def gpu_arm(args, w):
                 "d2h_bytes_per_step": d2h,
                 "path": "om_server_submit/om_server_poll (C ABI, host buffers, problem set-up "
                         "from the host every request, host wall clock)"},
-        "roofline": {"bound": "hbm", "kernel": "k_matvec_part<float2,float2> (FP32 inner matvec)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "k_matvec_tma<0> (FP32 inner matvec, TMA-staged; timed in the "
+                               "single-stream part, where a context uses it)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": how + " (MEASURED_PEAKS.json hbm_gbs)",
                      # DRAM bytes per launch from an ncu capture of the same kernel at
-                     # n = 6,400 (dram read + write): 1.0099 x the algorithmic bytes
-                     "traffic": bytes_mv * 1.0099,
+                     # n = 6,400 (dram read 327.75 MB + write 4.16 MB): 1.0129 x the
+                     # algorithmic 8 n^2 bytes
+                     "traffic": bytes_mv * 1.0129,
                      "algorithmic_bytes_per_launch": bytes_mv},
         "kernels": {
             "assemble_mixed": {"ms_avg": asm_ms / max(asm_n, 1), "launches": asm_n,
