@@ -405,7 +405,7 @@ def wavelength_solve(ctx: Context, spheres, bg, wave, opts=None, precision=C128,
 
 
 def cgemm_sub_c64(ctx: Context, A, B, C_):
-    """C - A B for complex64 A (m x k), B (k x n), C (m x n), k <= 32, on the
+    """C - A B for complex64 A (m x k), B (k x n), C (m x n), any k >= 1, on the
     tensor cores (om_cgemm_sub_c64); returns the new C."""
     A = np.asfortranarray(A, dtype=np.complex64)
     B = np.asfortranarray(B, dtype=np.complex64)

@@ -433,7 +433,7 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
 
 int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, long lda,
                      const float *B, long ldb, float *C, long ldc) {
-  if(!ctx || !A || !B || !C || m < 1 || n < 1 || k < 1 || k > 32 || lda < m || ldb < k || ldc < m)
+  if(!ctx || !A || !B || !C || m < 1 || n < 1 || k < 1 || lda < m || ldb < k || ldc < m)
     return OM_ERR_INVALID;
   cudaSetDevice(ctx->device);
   ctx->last_launches = 0;

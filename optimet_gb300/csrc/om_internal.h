@@ -232,7 +232,7 @@ int solve_fgmres_rhs(om_problem *pr, int harmonic, const om_solve_options *o, co
 int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, const double2 *b,
                        double2 *x, om_solve_stats *st);
 
-// tc_gemm.cu: C (m x n) -= A (m x k) B (k x n), k <= 32, complex64, column-major,
+// tc_gemm.cu: C (m x n) -= A (m x k) B (k x n), any k >= 1, complex64, column-major,
 // on the tensor cores (bf16 hi/lo split, FP32 accumulation); *d_err set on a
 // timed-out wait
 void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,

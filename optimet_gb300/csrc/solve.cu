@@ -861,11 +861,14 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_update(V *A, long ld, long 
   }
 }
 
-// Apply the panel's row interchanges to the columns outside the panel.
+// Apply the row interchanges of rows k .. k + nb - 1 (in order) to the
+// columns jlo .. jhi - 1 other than slo .. shi - 1 (the panel's own columns,
+// which the panel kernels swap themselves).
 template <typename V>
-__global__ void k_lu_swap(V *A, long ld, long n, long k, int nb, const int *piv) {
-  const long j = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if(j >= n || (j >= k && j < k + nb))
+__global__ void k_lu_swap(V *A, long ld, long jlo, long jhi, long slo, long shi, long k, int nb,
+                          const int *piv) {
+  const long j = jlo + blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(j >= jhi || (j >= slo && j < shi))
     return;
   V *col = A + j * ld;
   for(int c = 0; c < nb; ++c) {
@@ -878,17 +881,18 @@ __global__ void k_lu_swap(V *A, long ld, long n, long k, int nb, const int *piv)
   }
 }
 
-// U12 = L11^{-1} A12 (unit lower L11), one thread per column.
+// U12 = L11^{-1} A12 (unit lower L11: rows and columns k .. k + nb - 1) for
+// the columns jlo .. jhi - 1, one thread per column.
 template <typename V>
-__global__ void k_lu_trsm(V *A, long ld, long n, long k, int nb) {
+__global__ void k_lu_trsm(V *A, long ld, long jlo, long jhi, long k, int nb) {
   __shared__ V L[kNb][kNb];
   for(int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
     int r = idx % nb, c = idx / nb;
     L[r][c] = A[(k + c) * ld + k + r];
   }
   __syncthreads();
-  const long j = k + nb + blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if(j >= n)
+  const long j = jlo + blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(j >= jhi)
     return;
   V x[kNb];
   for(int r = 0; r < nb; ++r) {
@@ -945,18 +949,40 @@ __global__ void __launch_bounds__(256) k_lu_gemm(V *A, long ld, long n, long k, 
   }
 }
 
-// b := P b (row interchanges in order)
-template <typename V> __global__ void k_lu_permute(V *b, long n, const int *piv) {
-  if(threadIdx.x != 0 || blockIdx.x != 0)
-    return;
-  for(long r = 0; r < n; ++r) {
-    long p = piv[r];
-    if(p != r) {
-      V a = b[r];
-      b[r] = b[p];
-      b[p] = a;
-    }
+// y = P b, P the product of the row interchanges in order, as a gather:
+// perm[i] is the row of b that the interchanges bring to row i.
+template <typename V> __global__ void k_lu_gather(const V *b, V *y, const int *perm, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i < n)
+    y[i] = b[perm[i]];
+}
+
+// perm (device, n entries) from the pivots of lu_factor: the interchanges
+// applied in order to the row indices, on the host (one download of piv and
+// one upload, after the factorization).
+int lu_perm(om_context *ctx, const int *piv, long n, int *perm) {
+  std::vector<int> hp((size_t)n), idx((size_t)n);
+  cudaMemcpyAsync(hp.data(), piv, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream);
+  const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if(e != cudaSuccess) {
+    ctx->err = std::string("LU pivots: ") + cudaGetErrorString(e);
+    return OM_ERR_CUDA;
   }
+  for(long i = 0; i < n; ++i)
+    idx[i] = (int)i;
+  for(long r = 0; r < n; ++r) {
+    const long p = hp[r];
+    if(p > r && p < n)
+      std::swap(idx[r], idx[p]);
+  }
+  cudaMemcpyAsync(perm, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream);
+  // idx must outlive the copy
+  const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+  if(e2 != cudaSuccess) {
+    ctx->err = std::string("LU permutation: ") + cudaGetErrorString(e2);
+    return OM_ERR_CUDA;
+  }
+  return OM_OK;
 }
 
 // One block of kNb rows of a triangular solve in a single launch: every CTA
@@ -1017,6 +1043,57 @@ __global__ void __launch_bounds__(256) k_tri_block(const V *A, long ld, long k, 
   }
 }
 
+// Complex64 LU with tensor-core updates, blocked in two levels (the order of
+// LAPACK's blocked getrf): each block of kTcBlock columns is factored as a
+// tall panel, in panels of kNb columns whose interchanges and updates stay
+// inside the block; then the block's interchanges are applied to the columns
+// outside it, its rows of U to the right are solved (L11^{-1} A12, kNb rows
+// at a time), and the trailing matrix takes one rank-kTcBlock update, so that
+// it is read and written once per kTcBlock columns instead of once per kNb.
+// The pivots are those of the unblocked order (each panel's pivot search sees
+// fully updated columns); the roundings differ.
+constexpr long kTcBlock = 128;
+
+template <typename Panel>
+void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Panel &panel) {
+  for(long K = 0; K < n; K += kTcBlock) {
+    const long W = std::min<long>(kTcBlock, n - K), KE = K + W;
+    for(long k = K; k < KE; k += kNb) {
+      const int nb = (int)std::min<long>(kNb, KE - k);
+      const long kn = k + nb;
+      panel(k, nb);
+      if(W > nb) {  // the block's other columns
+        k_lu_swap<float2><<<blocks_for(W, 256), 256, 0, ctx->stream>>>(A, n, K, KE, k, kn, k, nb, piv);
+        ctx->last_launches++;
+      }
+      if(kn < KE) {  // the block's later columns: U rows, then all rows below
+        k_lu_trsm<float2><<<blocks_for(KE - kn, 128), 128, 0, ctx->stream>>>(A, n, kn, KE, k, nb);
+        ctx->last_launches++;
+        launch_cgemm_sub_tc(ctx, A + k * n + kn, n, A + kn * n + k, n, A + kn * n + kn, n, n - kn,
+                            KE - kn, nb, info + 1);
+      }
+    }
+    if(W < n) {  // the block's interchanges on the columns left and right of it
+      k_lu_swap<float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, 0, n, K, KE, K, (int)W, piv);
+      ctx->last_launches++;
+    }
+    const long rest = n - KE;
+    if(rest <= 0)
+      continue;
+    for(long k = K; k < KE; k += kNb) {  // U12 = L11^{-1} A12
+      const int nb = (int)std::min<long>(kNb, KE - k);
+      const long kn = k + nb;
+      k_lu_trsm<float2><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, KE, n, k, nb);
+      ctx->last_launches++;
+      if(kn < KE)
+        launch_cgemm_sub_tc(ctx, A + k * n + kn, n, A + KE * n + k, n, A + KE * n + kn, n, KE - kn,
+                            rest, nb, info + 1);
+    }
+    launch_cgemm_sub_tc(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest, rest,
+                        (int)W, info + 1);
+  }
+}
+
 // info[0]: first zero pivot (1-based) or 0; info[1]: set when a tensor-core
 // trailing update timed out (complex64 only).
 template <typename V>
@@ -1035,8 +1112,8 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
     ps.besti = ws.take<long>(maxblk, off);
     ps.prow = ws.take<V>(kNb, off);
   }
-  for(long k = 0; k < n; k += kNb) {
-    const int nb = (int)std::min<long>(kNb, n - k);
+  // LU of the panel A[k:n, k:k+nb) with its row interchanges inside the panel
+  auto panel = [&](long k, int nb) {
     const long rows = n - k;
     if(rows >= kTallPanel) {
       ps.nblk = (int)std::min<long>(maxblk, (rows + kPanThreads - 1) / kPanThreads);
@@ -1050,47 +1127,52 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
       k_lu_panel<V><<<1, 1024, 0, ctx->stream>>>(A, n, n, k, nb, piv, info);
       ctx->last_launches++;
     }
-    k_lu_swap<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, n, k, nb, piv);
+  };
+  if constexpr(std::is_same<V, float2>::value) {
+    if(ctx->lu_tc) {
+      lu_blocked_tc(ctx, A, n, piv, info, panel);
+      return OM_OK;
+    }
+  }
+  for(long k = 0; k < n; k += kNb) {
+    const int nb = (int)std::min<long>(kNb, n - k);
+    panel(k, nb);
+    k_lu_swap<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, 0, n, k, k + nb, k, nb, piv);
     ctx->last_launches++;
     const long rest = n - k - nb;
     if(rest > 0) {
-      k_lu_trsm<V><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, n, k, nb);
-      ctx->last_launches++;
-      if constexpr(std::is_same<V, float2>::value) {
-        if(ctx->lu_tc && rest >= 128) {
-          const long kn = k + nb;
-          launch_cgemm_sub_tc(ctx, A + k * n + kn, n, A + kn * n + k, n, A + kn * n + kn, n, rest,
-                              rest, nb, info + 1);
-          continue;
-        }
-      }
+      k_lu_trsm<V><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, k + nb, n, k, nb);
       dim3 g((unsigned)((rest + 31) / 32), (unsigned)((rest + 31) / 32));
       k_lu_gemm<V><<<g, 256, 0, ctx->stream>>>(A, n, n, k, nb);
-      ctx->last_launches++;
+      ctx->last_launches += 2;
     }
   }
   return OM_OK;
 }
 
-// b := A^{-1} b with A = P^T L U from lu_factor; y: n entries of scratch.
-// 1 + 2 ceil(n / kNb) launches, all stream-ordered (capturable as a graph).
+// b := A^{-1} b with A = P^T L U from lu_factor and perm from lu_perm; y: n
+// entries of scratch. 2 + 2 ceil(n / kNb) launches, all stream-ordered
+// (capturable as a graph): y = P b, the forward solve from y into b, the
+// backward solve from b into y, and y copied back to b.
 template <typename V>
-int lu_solve_vec(om_context *ctx, const V *A, long n, const int *piv, V *b, V *y) {
-  k_lu_permute<V><<<1, 32, 0, ctx->stream>>>(b, n, piv);
+int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, V *b, V *y) {
+  k_lu_gather<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(b, y, perm, n);
   int launches = 1;
   for(long k = 0; k < n; k += kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
     const long rows = n - k - nb;
     k_tri_block<V><<<(unsigned)std::max<long>(1, blocks_for(rows, 256)), 256, 0, ctx->stream>>>(
-        A, n, k, nb, b, y, k + nb, n, 0);
+        A, n, k, nb, y, b, k + nb, n, 0);
     ++launches;
   }
   for(long k = ((n - 1) / kNb) * kNb; k >= 0; k -= kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
     k_tri_block<V><<<(unsigned)std::max<long>(1, blocks_for(k, 256)), 256, 0, ctx->stream>>>(
-        A, n, k, nb, y, b, 0, k, 1);
+        A, n, k, nb, b, y, 0, k, 1);
     ++launches;
   }
+  k_scale_copy<V, V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(y, 1.0, b, n);
+  ++launches;
   ctx->last_launches += launches;
   return launches;
 }
@@ -1108,7 +1190,7 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   }
   Work w;
   w.ctx = ctx;
-  size_t bytes = sizeof(double2) * ((size_t)n * n + n) + sizeof(int) * (n + 2) + 1024;
+  size_t bytes = sizeof(double2) * ((size_t)n * n + n) + sizeof(int) * (2 * n + 2) + 2048;
   int rc = alloc_work(ctx, w, bytes);
   if(rc)
     return rc;
@@ -1117,13 +1199,16 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   double2 *y = w.take<double2>(n, off);
   int *piv = w.take<int>(n, off);
   int *info = w.take<int>(2, off);
+  int *perm = w.take<int>(n, off);
   cudaMemcpyAsync(A, pr->d_S[harmonic], sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToDevice,
                   ctx->stream);
   rc = lu_factor<double2>(ctx, A, n, piv, info);
+  if(!rc)
+    rc = lu_perm(ctx, piv, n, perm);
   if(rc)
     return rc;
   cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
-  lu_solve_vec<double2>(ctx, A, n, piv, x, y);
+  lu_solve_vec<double2>(ctx, A, n, perm, x, y);
   int hinfo = 0;
   cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
@@ -1197,7 +1282,7 @@ struct LuPrecond32 : PrecondFn {
   long n;
   Work w;
   float2 *A = nullptr, *v32 = nullptr, *y32 = nullptr;
-  int *piv = nullptr, *info = nullptr;
+  int *piv = nullptr, *info = nullptr, *perm = nullptr;
   int applied = 0;
   // the triangular solves on v32, captured once as a graph and replayed
   cudaGraphExec_t solve_graph = nullptr;
@@ -1208,7 +1293,7 @@ struct LuPrecond32 : PrecondFn {
       cudaGraphExecDestroy(solve_graph);
   }
   int init(const float2 *S32) {
-    size_t bytes = sizeof(float2) * ((size_t)n * n + 2 * n) + sizeof(int) * (n + 2) + 1024;
+    size_t bytes = sizeof(float2) * ((size_t)n * n + 2 * n) + sizeof(int) * (2 * n + 2) + 2048;
     int rc = alloc_work(ctx, w, bytes);
     if(rc)
       return rc;
@@ -1218,6 +1303,7 @@ struct LuPrecond32 : PrecondFn {
     y32 = w.take<float2>(n, off);
     piv = w.take<int>(n, off);
     info = w.take<int>(2, off);
+    perm = w.take<int>(n, off);
     cudaMemcpyAsync(A, S32, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, ctx->stream);
     rc = lu_factor<float2>(ctx, A, n, piv, info);
     if(rc)
@@ -1233,12 +1319,15 @@ struct LuPrecond32 : PrecondFn {
       ctx->err = "singular complex64 matrix: zero pivot at column " + std::to_string(hinfo[0]);
       return OM_ERR_SINGULAR;
     }
+    rc = lu_perm(ctx, piv, n, perm);
+    if(rc)
+      return rc;
     // capture the solve sequence (its pointers are fixed); plain launches if
     // capture is refused
     cudaGraph_t g = nullptr;
     if(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const int before = ctx->last_launches;
-      solve_launches = lu_solve_vec<float2>(ctx, A, n, piv, v32, y32);
+      solve_launches = lu_solve_vec<float2>(ctx, A, n, perm, v32, y32);
       ctx->last_launches = before;
       if(cudaStreamEndCapture(ctx->stream, &g) != cudaSuccess ||
          cudaGraphInstantiate(&solve_graph, g, 0) != cudaSuccess)
@@ -1255,7 +1344,7 @@ struct LuPrecond32 : PrecondFn {
       cudaGraphLaunch(solve_graph, ctx->stream);
       ctx->last_launches += solve_launches;
     } else {
-      lu_solve_vec<float2>(ctx, A, n, piv, v32, y32);
+      lu_solve_vec<float2>(ctx, A, n, perm, v32, y32);
     }
     k_scale_copy<float2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v32, 1.0, z, n);
     ctx->last_launches += 2;

@@ -1,5 +1,5 @@
 // Complex64 rank-k update on the 5th-generation tensor cores (tcgen05):
-//   C (m x n) -= A (m x k) B (k x n),  k <= 32, column-major complex64,
+//   C (m x n) -= A (m x k) B (k x n),  any k >= 1, column-major complex64,
 // the trailing update of the precision form's blocked LU (the role of the
 // pzgesv trailing pzgemm, ScalapackSolver.cpp:54-130 / LinearSystemSolver.hpp:55-65).
 //
@@ -9,14 +9,16 @@
 //   Re(AB) = Ar Br + Ai (-Bi),  Im(AB) = Ar Bi + Ai Br
 // takes 12 MMAs of M = 128, N = 64, K = 16 per 16 columns of k (B's imaginary
 // part is staged twice, with both signs; a sign flip is exact in bf16). One
-// CTA of 128 threads owns a 128 x 64 tile of C: the operands are split and
-// stored in shared memory in the canonical K-major layout without swizzle
-// (8 x 16-byte core matrices), thread 0 issues the MMAs into two TMEM
-// accumulators (Re, Im; 64 columns each: 128 TMEM columns, four CTAs per
-// SM), commits them to an mbarrier, and the four warps read their 32 TMEM
-// lanes back (tcgen05.ld 32x32b) and subtract from C, whose first 16 columns
-// are loaded while the MMAs run. Waits are bounded: on time-out the kernel
-// raises *err, still frees its TMEM and leaves C untouched.
+// CTA of 128 threads owns a 128 x 64 tile of C. k runs in chunks of 32: each
+// chunk's operands are split and stored in shared memory in the canonical
+// K-major layout without swizzle (8 x 16-byte core matrices), thread 0 issues
+// its MMAs into two TMEM accumulators (Re, Im; 64 columns each: 128 TMEM
+// columns) and commits them to an mbarrier, and the next chunk's operands are
+// loaded into registers while those MMAs run. After the last chunk the four
+// warps read their 32 TMEM lanes back (tcgen05.ld 32x32b) and subtract from
+// C, whose first 16 columns are loaded while the last MMAs run: C is read and
+// written once for the whole rank-k update. Waits are bounded: on time-out
+// the kernel raises *err, still frees its TMEM and leaves C untouched.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -67,14 +69,66 @@ __device__ __forceinline__ int kmajor_off(int r, int c) {
   return (r >> 3) * 512 + (c >> 3) * 128 + (r & 7) * 16 + (c & 7) * 2;
 }
 
-__device__ __forceinline__ void split_store(unsigned char *hi, unsigned char *lo, int off, float x) {
-  const __nv_bfloat16 h = __float2bfloat16_rn(x);
-  const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
-  *reinterpret_cast<__nv_bfloat16 *>(hi + off) = h;
-  *reinterpret_cast<__nv_bfloat16 *>(lo + off) = l;
+// Two FP32 values split into bf16 hi and lo parts, packed as bf16x2
+// (the first value in the low half): hi = bf16(x), lo = bf16(x - hi), both
+// rounded to nearest.
+__device__ __forceinline__ void split2(float a, float b, uint32_t &hi, uint32_t &lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<const uint32_t *>(&h);
+  lo = *reinterpret_cast<const uint32_t *>(&l);
 }
 
-__global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda, const float2 *B,
+__device__ __forceinline__ void st_shared_v4(unsigned char *p, uint32_t x, uint32_t y, uint32_t z,
+                                             uint32_t w) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(smem_addr(p)), "r"(x), "r"(y), "r"(z),
+               "r"(w)
+               : "memory");
+}
+
+// Eight K-consecutive complex values of one row (v[0..7]) into one 16-byte
+// core-matrix row of each part: the real parts' hi / lo, the imaginary parts'
+// hi / lo, and (for B) the negated imaginary parts' hi / lo, whose bf16 values
+// are those of the imaginary parts with the sign bit flipped (rounding to
+// nearest is symmetric).
+__device__ __forceinline__ void stage8(const float2 *v, int off, unsigned char *rh, unsigned char *rl,
+                                       unsigned char *ih, unsigned char *il, unsigned char *nh,
+                                       unsigned char *nl) {
+  uint32_t a[4], b[4], c[4], d[4];
+#pragma unroll
+  for(int p = 0; p < 4; ++p) {
+    split2(v[2 * p].x, v[2 * p + 1].x, a[p], b[p]);
+    split2(v[2 * p].y, v[2 * p + 1].y, c[p], d[p]);
+  }
+  st_shared_v4(rh + off, a[0], a[1], a[2], a[3]);
+  st_shared_v4(rl + off, b[0], b[1], b[2], b[3]);
+  st_shared_v4(ih + off, c[0], c[1], c[2], c[3]);
+  st_shared_v4(il + off, d[0], d[1], d[2], d[3]);
+  if(nh) {
+    constexpr uint32_t sgn = 0x80008000u;
+    st_shared_v4(nh + off, c[0] ^ sgn, c[1] ^ sgn, c[2] ^ sgn, c[3] ^ sgn);
+    st_shared_v4(nl + off, d[0] ^ sgn, d[1] ^ sgn, d[2] ^ sgn, d[3] ^ sgn);
+  }
+}
+
+// Bounded wait for the completion of the mbarrier phase of the given parity;
+// 1 when it completed, 0 on time-out.
+__device__ __forceinline__ uint32_t wait_phase(uint64_t *mbar, uint32_t parity) {
+  uint32_t done = 0;
+  for(long it = 0; it < (1L << 24) && !done; ++it) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(smem_addr(mbar)), "r"(parity)
+        : "memory");
+  }
+  return done;
+}
+
+__global__ void __launch_bounds__(128, 3) k_cgemm_sub_tc(const float2 *A, long lda, const float2 *B,
                                                       long ldb, float2 *C, long ldc, long m, long n,
                                                       int k, int *err) {
   extern __shared__ __align__(1024) unsigned char tsm[];
@@ -97,92 +151,121 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda,
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
 
-  // A tile: thread t owns row r0 + t (coalesced down each column); all of a
-  // thread's loads are issued before the first split, so that they are in
-  // flight together
+  // K runs in chunks of kTcK columns through the one set of operand tiles.
+  // Chunk q + 1 is loaded into registers while the MMAs of chunk q run, and
+  // is stored to shared memory once those MMAs have completed (mbarrier
+  // phase q). A tile: thread t owns row r0 + t (coalesced down each column);
+  // B tile as N x K: thread t owns column c0 + t / 2, half of the chunk
+  // (contiguous in memory).
+  // the C tile's lines requested into L2 now, so that its DRAM reads overlap
+  // the operand staging and the MMAs: thread t covers column t / 2, rows
+  // (t & 1) 64 .. (t & 1) 64 + 63 (four 128-byte lines)
   {
-    const long r = r0 + t;
-    float2 av[kTcK];
+    const long col = c0 + (t >> 1);
+    if(col < n) {
+#pragma unroll
+      for(int i = 0; i < 4; ++i) {
+        const long row = r0 + (t & 1) * 64 + 16 * i;
+        if(row < m)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(C + col * ldc + row));
+      }
+    }
+  }
+  const int nq = (k + kTcK - 1) / kTcK;
+  // B's chunks start at even offsets of 16-byte aligned columns when B is
+  // 16-byte aligned and ldb is even
+  const bool bvec = ((reinterpret_cast<uintptr_t>(B) & 15) == 0) && ((ldb & 1) == 0);
+  const long ra = r0 + t;
+  const int jb = t >> 1, cb = (t & 1) * 16;
+  const long colb = c0 + jb;
+  float2 av[kTcK], bv[16];
+  auto load_chunk = [&](int q) {
+    const int kq = q * kTcK;
 #pragma unroll
     for(int c = 0; c < kTcK; ++c)
-      av[c] = (c < k && r < m) ? A[(long)c * lda + r] : make_float2(0.f, 0.f);
+      av[c] = (kq + c < k && ra < m) ? A[(long)(kq + c) * lda + ra] : make_float2(0.f, 0.f);
+    if(bvec && kq + cb + 16 <= k && colb < n) {  // 16-byte loads
+      const float4 *src = reinterpret_cast<const float4 *>(B + colb * ldb + kq + cb);
 #pragma unroll
-    for(int c = 0; c < kTcK; ++c) {
-      const int off = kmajor_off(t, c);
-      split_store(Arh, Arl, off, av[c].x);
-      split_store(Aih, Ail, off, av[c].y);
+      for(int c = 0; c < 8; ++c) {
+        const float4 w = src[c];
+        bv[2 * c] = make_float2(w.x, w.y);
+        bv[2 * c + 1] = make_float2(w.z, w.w);
+      }
+    } else {
+#pragma unroll
+      for(int c = 0; c < 16; ++c)
+        bv[c] = (kq + cb + c < k && colb < n) ? B[colb * ldb + kq + cb + c] : make_float2(0.f, 0.f);
     }
-  }
-  // B tile as N x K: thread t owns column c0 + t / 2, half of K (contiguous in memory)
-  {
-    const int j = t >> 1, cb = (t & 1) * 16;
-    const long col = c0 + j;
-    float2 bv[16];
+  };
+  load_chunk(0);
+  uint32_t tmem = 0;
+  bool ok = true;
+  for(int q = 0; q < nq; ++q) {
+    uint32_t done = 1;
+    if(q > 0)  // the MMAs of chunk q - 1 have read the tiles
+      done = wait_phase(mbar, (uint32_t)(q - 1) & 1u);
 #pragma unroll
-    for(int c = 0; c < 16; ++c)
-      bv[c] = (cb + c < k && col < n) ? B[col * ldb + cb + c] : make_float2(0.f, 0.f);
+    for(int g = 0; g < kTcK / 8; ++g)
+      stage8(av + 8 * g, kmajor_off(t, 8 * g), Arh, Arl, Aih, Ail, nullptr, nullptr);
 #pragma unroll
-    for(int c = 0; c < 16; ++c) {
-      const int off = kmajor_off(j, cb + c);
-      split_store(Brh, Brl, off, bv[c].x);
-      split_store(Bih, Bil, off, bv[c].y);
-      split_store(Bnh, Bnl, off, -bv[c].y);
+    for(int g = 0; g < 2; ++g)
+      stage8(bv + 8 * g, kmajor_off(jb, cb + 8 * g), Brh, Brl, Bih, Bil, Bnh, Bnl);
+    // generic-proxy stores -> visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    done = __syncthreads_and(done);  // one decision for the whole CTA
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem = *tmem_slot;
+    if(!done) {
+      ok = false;
+      break;
     }
+    if(t == 0) {
+      const uint32_t d_re = tmem, d_im = tmem + kTcN;
+      for(int s = 0; s < kTcK / 16; ++s) {
+        const uint32_t ko = s * 256;  // two core matrices along K per MMA
+        auto da = [&](unsigned char *p) { return umma_desc(smem_addr(p) + ko, 128, 512); };
+        const uint32_t acc = q > 0 || s > 0;  // the first K step overwrites the accumulators
+        // Re: Ar Br + Ai (-Bi)
+        mma_bf16(d_re, da(Arh), da(Brh), acc);
+        mma_bf16(d_re, da(Arh), da(Brl), 1);
+        mma_bf16(d_re, da(Arl), da(Brh), 1);
+        mma_bf16(d_re, da(Aih), da(Bnh), 1);
+        mma_bf16(d_re, da(Aih), da(Bnl), 1);
+        mma_bf16(d_re, da(Ail), da(Bnh), 1);
+        // Im: Ar Bi + Ai Br
+        mma_bf16(d_im, da(Arh), da(Bih), acc);
+        mma_bf16(d_im, da(Arh), da(Bil), 1);
+        mma_bf16(d_im, da(Arl), da(Bih), 1);
+        mma_bf16(d_im, da(Aih), da(Brh), 1);
+        mma_bf16(d_im, da(Aih), da(Brl), 1);
+        mma_bf16(d_im, da(Ail), da(Brh), 1);
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_addr(mbar))
+          : "memory");
+    }
+    if(q + 1 < nq)
+      load_chunk(q + 1);
   }
-  // generic-proxy stores -> visible to the tensor core (async proxy)
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
   const uint32_t d_re = tmem, d_im = tmem + kTcN;
 
-  if(t == 0) {
-    for(int s = 0; s < kTcK / 16; ++s) {
-      const uint32_t ko = s * 256;  // two core matrices along K per MMA
-      auto da = [&](unsigned char *p) { return umma_desc(smem_addr(p) + ko, 128, 512); };
-      const uint32_t acc = s > 0;  // the first K step overwrites the accumulators
-      // Re: Ar Br + Ai (-Bi)
-      mma_bf16(d_re, da(Arh), da(Brh), acc);
-      mma_bf16(d_re, da(Arh), da(Brl), 1);
-      mma_bf16(d_re, da(Arl), da(Brh), 1);
-      mma_bf16(d_re, da(Aih), da(Bnh), 1);
-      mma_bf16(d_re, da(Aih), da(Bnl), 1);
-      mma_bf16(d_re, da(Ail), da(Bnh), 1);
-      // Im: Ar Bi + Ai Br
-      mma_bf16(d_im, da(Arh), da(Bih), acc);
-      mma_bf16(d_im, da(Arh), da(Bil), 1);
-      mma_bf16(d_im, da(Arl), da(Bih), 1);
-      mma_bf16(d_im, da(Aih), da(Brh), 1);
-      mma_bf16(d_im, da(Aih), da(Brl), 1);
-      mma_bf16(d_im, da(Ail), da(Brh), 1);
-    }
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_addr(mbar))
-        : "memory");
-  }
-  // the first 16 columns of this thread's row of C, loaded while the MMAs run
+  // columns 0 .. 31 of this thread's row of C, loaded while the last MMAs
+  // run; columns 32 .. 47 and 48 .. 63 follow into the registers of the
+  // 16 columns just done
   const long r = r0 + warp * 32 + lane;
-  float2 cpre[16];
+  float2 cv[32];
 #pragma unroll
-  for(int q = 0; q < 16; ++q) {
+  for(int q = 0; q < 32; ++q) {
     const long col = c0 + q;
-    cpre[q] = (r < m && col < n) ? C[col * ldc + r] : make_float2(0.f, 0.f);
+    cv[q] = (r < m && col < n) ? C[col * ldc + r] : make_float2(0.f, 0.f);
   }
-  // bounded wait for the MMAs (phase 0 of the mbarrier)
-  uint32_t done = 0;
-  for(long it = 0; it < (1L << 24) && !done; ++it) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(smem_addr(mbar)), "r"(0u)
-        : "memory");
-  }
+  // bounded wait for the last chunk's MMAs (phase nq - 1 of the mbarrier)
+  uint32_t done = ok ? wait_phase(mbar, (uint32_t)(nq - 1) & 1u) : 0u;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  done = __syncthreads_and(done);  // one decision for the whole CTA
+  done = __syncthreads_and(done);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if(!done) {
     if(t == 0)
@@ -190,7 +273,9 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda,
   } else {
     // warp w reads TMEM lanes 32 w .. 32 w + 31 = rows r0 + 32 w + lane
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-    for(int cc = 0; cc < kTcN; cc += 16) {
+#pragma unroll
+    for(int g = 0; g < kTcN / 16; ++g) {
+      const int cc = 16 * g, base = (g & 1) * 16;
       uint32_t a[16], b[16];
 #define OM_TMEM_LD16(dst, addr)                                                                     \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
@@ -207,11 +292,18 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc(const float2 *A, long lda,
         for(int q = 0; q < 16; ++q) {
           const long col = c0 + cc + q;
           if(col < n) {
-            float2 v = cc == 0 ? cpre[q] : C[col * ldc + r];
+            float2 v = cv[base + q];
             v.x -= __uint_as_float(a[q]);
             v.y -= __uint_as_float(b[q]);
             C[col * ldc + r] = v;
           }
+        }
+      }
+      if(g < 2) {
+#pragma unroll
+        for(int q = 0; q < 16; ++q) {
+          const long col = c0 + cc + 32 + q;
+          cv[base + q] = (r < m && col < n) ? C[col * ldc + r] : make_float2(0.f, 0.f);
         }
       }
     }

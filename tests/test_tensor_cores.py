@@ -25,7 +25,10 @@ def ctx(G):
     c.close()
 
 
-@pytest.mark.parametrize("m,n,k", [(128, 64, 32), (300, 200, 32), (257, 70, 17), (5, 3, 1)])
+# k > 32 runs in several chunks through the kernel's operand tiles (the
+# LU's rank-128 trailing updates), with a ragged last chunk for 80 and 33
+@pytest.mark.parametrize("m,n,k", [(128, 64, 32), (300, 200, 32), (257, 70, 17), (5, 3, 1),
+                                   (300, 200, 128), (257, 70, 80), (130, 65, 33)])
 def test_update_exact_on_bf16_values(G, ctx, m, n, k):
     rng = np.random.default_rng(m + n + k)
     A = (rng.integers(-8, 9, (m, k)) + 1j * rng.integers(-8, 9, (m, k))).astype(np.complex64)
@@ -36,9 +39,10 @@ def test_update_exact_on_bf16_values(G, ctx, m, n, k):
     assert np.array_equal(out.astype(np.complex128), ref)
 
 
-def test_update_accuracy_general(G, ctx):
+@pytest.mark.parametrize("k", [32, 128])
+def test_update_accuracy_general(G, ctx, k):
     rng = np.random.default_rng(3)
-    m, n, k = 600, 400, 32
+    m, n = 600, 400
     A = (rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))).astype(np.complex64)
     B = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))).astype(np.complex64)
     C = (rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))).astype(np.complex64)
@@ -50,10 +54,13 @@ def test_update_accuracy_general(G, ctx):
     assert err > 1e-9        # (and not an FP32 SIMT path in disguise)
 
 
-def test_lu_mixed_with_and_without_tensor_cores(G, ctx):
+# n = 1,152: nine blocks of 128 columns; n = 450: a last block of 66 columns
+# (inner panels of 32, 32 and 2)
+@pytest.mark.parametrize("N,nmax", [(12, 6), (15, 3)])
+def test_lu_mixed_with_and_without_tensor_cores(G, ctx, N, nmax):
     rng = np.random.default_rng(21)
-    xyz, rad = random_cluster(rng, 12, 900 * nm, 40 * nm, 70 * nm, 20 * nm)
-    sp = G.spheres_array(xyz, rad, (2.5 + 0.05j) ** 2, 6)   # n = 1,152
+    xyz, rad = random_cluster(rng, N, 900 * nm, 40 * nm, 70 * nm, 20 * nm)
+    sp = G.spheres_array(xyz, rad, (2.5 + 0.05j) ** 2, nmax)
     bg, wave = G.medium(1.0), G.plane_wave(600 * nm)
     ref = G.wavelength_solve(ctx, sp, bg, wave, G.options(G.SOLVE_LU), G.C128)[0]
     opts = G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4)
