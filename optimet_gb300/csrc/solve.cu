@@ -767,23 +767,40 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_max(const V *A, long ld, lo
   }
 }
 
-// the pivot of column col = k + c, the row swap inside the panel, the pivot row
+// the pivot of column col = k + c, the row swap inside the panel, the pivot
+// row. One warp (kNb = 32 threads): each lane scans every 32nd partial
+// maximum, then a butterfly leaves on every lane the largest magnitude, the
+// smaller row index among equal ones (the order of k_lu_panel).
 template <typename V>
 __global__ void k_pan_pivot(V *A, long ld, long k, int c, int nb, int *piv, int *info, PanelScratch ps) {
   __shared__ long p_s;
   const long col = k + c;
-  if(threadIdx.x == 0) {
-    double bv = ps.bestv[0];
-    long bi = ps.besti[0];
-    for(int b = 1; b < ps.nblk; ++b)
-      if(ps.bestv[b] > bv || (ps.bestv[b] == bv && ps.besti[b] < bi)) {
-        bv = ps.bestv[b];
-        bi = ps.besti[b];
+  {
+    double bv = -2.0;  // below every partial maximum (those are >= -1)
+    long bi = col;
+    for(int b = threadIdx.x; b < ps.nblk; b += 32) {
+      const double v = ps.bestv[b];
+      const long i = ps.besti[b];
+      if(v > bv || (v == bv && i < bi)) {
+        bv = v;
+        bi = i;
       }
-    piv[col] = (int)bi;
-    if(bv <= 0.0 && *info == 0)
-      *info = (int)col + 1;
-    p_s = bi;
+    }
+#pragma unroll
+    for(int h = 16; h > 0; h >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, bv, h);
+      const long oi = __shfl_xor_sync(0xffffffffu, bi, h);
+      if(ov > bv || (ov == bv && oi < bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if(threadIdx.x == 0) {
+      piv[col] = (int)bi;
+      if(bv <= 0.0 && *info == 0)
+        *info = (int)col + 1;
+      p_s = bi;
+    }
   }
   __syncthreads();
   const long p = p_s;
@@ -957,6 +974,13 @@ template <typename V> __global__ void k_lu_gather(const V *b, V *y, const int *p
     y[i] = b[perm[i]];
 }
 
+// dinv[i] = 1 / U[i][i] (the backward solve's divisions, done once)
+template <typename V> __global__ void k_lu_diag_inv(const V *A, long ld, long n, V *dinv) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if(i < n)
+    dinv[i] = crecip(A[i * ld + i]);
+}
+
 // perm (device, n entries) from the pivots of lu_factor: the interchanges
 // applied in order to the row indices, on the host (one download of piv and
 // one upload, after the factorization).
@@ -988,7 +1012,8 @@ int lu_perm(om_context *ctx, const int *piv, long n, int *perm) {
 // One block of kNb rows of a triangular solve in a single launch: every CTA
 // solves the diagonal block from src[k .. k+nb) in shared memory (warp 0, a
 // lane per row: forward with the unit lower factor, or backward with the upper
-// factor and its diagonal), then updates its rows [lo, hi) of src outside the
+// factor and the reciprocals of its diagonal, dinv, computed once per
+// factorization), then updates its rows [lo, hi) of src outside the
 // block; CTA 0 writes the block's solution to dst. The rows read and the rows
 // written are disjoint, so the CTAs need no ordering among themselves.
 template <typename V> __device__ __forceinline__ V shfl_v(V a, int src) {
@@ -999,7 +1024,7 @@ template <typename V> __device__ __forceinline__ V shfl_v(V a, int src) {
 
 template <typename V>
 __global__ void __launch_bounds__(256) k_tri_block(const V *A, long ld, long k, int nb, V *src, V *dst,
-                                                   long lo, long hi, int upper) {
+                                                   long lo, long hi, int upper, const V *dinv) {
   __shared__ V Ad[kNb][kNb + 1];
   __shared__ V xs[kNb];
   for(int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
@@ -1011,8 +1036,12 @@ __global__ void __launch_bounds__(256) k_tri_block(const V *A, long ld, long k, 
     const int lane = threadIdx.x;
     V v;
     v.x = v.y = 0;
-    if(lane < nb)
+    V dl = v;  // lane c: 1 / U[c][c] of this block (backward solve)
+    if(lane < nb) {
       v = src[k + lane];
+      if(upper)
+        dl = dinv[k + lane];
+    }
     if(!upper) {
       for(int c = 0; c < nb; ++c) {
         const V xc = shfl_v(v, c);
@@ -1022,7 +1051,7 @@ __global__ void __launch_bounds__(256) k_tri_block(const V *A, long ld, long k, 
     } else {
       for(int c = nb - 1; c >= 0; --c) {
         if(lane == c)
-          v = cmul(v, crecip(Ad[c][c]));
+          v = cmul(v, dl);
         const V xc = shfl_v(v, c);
         if(lane < c)
           v = cfma(Ad[lane][c], make_neg(xc), v);
@@ -1150,25 +1179,25 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   return OM_OK;
 }
 
-// b := A^{-1} b with A = P^T L U from lu_factor and perm from lu_perm; y: n
-// entries of scratch. 2 + 2 ceil(n / kNb) launches, all stream-ordered
-// (capturable as a graph): y = P b, the forward solve from y into b, the
-// backward solve from b into y, and y copied back to b.
+// b := A^{-1} b with A = P^T L U from lu_factor, perm from lu_perm and dinv
+// from k_lu_diag_inv; y: n entries of scratch. 2 + 2 ceil(n / kNb) launches,
+// all stream-ordered (capturable as a graph): y = P b, the forward solve from
+// y into b, the backward solve from b into y, and y copied back to b.
 template <typename V>
-int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, V *b, V *y) {
+int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, const V *dinv, V *b, V *y) {
   k_lu_gather<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(b, y, perm, n);
   int launches = 1;
   for(long k = 0; k < n; k += kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
     const long rows = n - k - nb;
     k_tri_block<V><<<(unsigned)std::max<long>(1, blocks_for(rows, 256)), 256, 0, ctx->stream>>>(
-        A, n, k, nb, y, b, k + nb, n, 0);
+        A, n, k, nb, y, b, k + nb, n, 0, dinv);
     ++launches;
   }
   for(long k = ((n - 1) / kNb) * kNb; k >= 0; k -= kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
     k_tri_block<V><<<(unsigned)std::max<long>(1, blocks_for(k, 256)), 256, 0, ctx->stream>>>(
-        A, n, k, nb, b, y, 0, k, 1);
+        A, n, k, nb, b, y, 0, k, 1, dinv);
     ++launches;
   }
   k_scale_copy<V, V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(y, 1.0, b, n);
@@ -1190,7 +1219,7 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   }
   Work w;
   w.ctx = ctx;
-  size_t bytes = sizeof(double2) * ((size_t)n * n + n) + sizeof(int) * (2 * n + 2) + 2048;
+  size_t bytes = sizeof(double2) * ((size_t)n * n + 2 * n) + sizeof(int) * (2 * n + 2) + 2048;
   int rc = alloc_work(ctx, w, bytes);
   if(rc)
     return rc;
@@ -1200,6 +1229,7 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   int *piv = w.take<int>(n, off);
   int *info = w.take<int>(2, off);
   int *perm = w.take<int>(n, off);
+  double2 *dinv = w.take<double2>(n, off);
   cudaMemcpyAsync(A, pr->d_S[harmonic], sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToDevice,
                   ctx->stream);
   rc = lu_factor<double2>(ctx, A, n, piv, info);
@@ -1207,8 +1237,10 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
     rc = lu_perm(ctx, piv, n, perm);
   if(rc)
     return rc;
+  k_lu_diag_inv<double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, n, dinv);
+  ctx->last_launches++;
   cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
-  lu_solve_vec<double2>(ctx, A, n, perm, x, y);
+  lu_solve_vec<double2>(ctx, A, n, perm, dinv, x, y);
   int hinfo = 0;
   cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
@@ -1281,7 +1313,7 @@ struct LuPrecond32 : PrecondFn {
   om_context *ctx;
   long n;
   Work w;
-  float2 *A = nullptr, *v32 = nullptr, *y32 = nullptr;
+  float2 *A = nullptr, *v32 = nullptr, *y32 = nullptr, *dinv = nullptr;
   int *piv = nullptr, *info = nullptr, *perm = nullptr;
   int applied = 0;
   // the triangular solves on v32, captured once as a graph and replayed
@@ -1293,7 +1325,7 @@ struct LuPrecond32 : PrecondFn {
       cudaGraphExecDestroy(solve_graph);
   }
   int init(const float2 *S32) {
-    size_t bytes = sizeof(float2) * ((size_t)n * n + 2 * n) + sizeof(int) * (2 * n + 2) + 2048;
+    size_t bytes = sizeof(float2) * ((size_t)n * n + 3 * n) + sizeof(int) * (2 * n + 2) + 2048;
     int rc = alloc_work(ctx, w, bytes);
     if(rc)
       return rc;
@@ -1304,6 +1336,7 @@ struct LuPrecond32 : PrecondFn {
     piv = w.take<int>(n, off);
     info = w.take<int>(2, off);
     perm = w.take<int>(n, off);
+    dinv = w.take<float2>(n, off);
     cudaMemcpyAsync(A, S32, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, ctx->stream);
     rc = lu_factor<float2>(ctx, A, n, piv, info);
     if(rc)
@@ -1322,12 +1355,14 @@ struct LuPrecond32 : PrecondFn {
     rc = lu_perm(ctx, piv, n, perm);
     if(rc)
       return rc;
+    k_lu_diag_inv<float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, n, dinv);
+    ctx->last_launches++;
     // capture the solve sequence (its pointers are fixed); plain launches if
     // capture is refused
     cudaGraph_t g = nullptr;
     if(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const int before = ctx->last_launches;
-      solve_launches = lu_solve_vec<float2>(ctx, A, n, perm, v32, y32);
+      solve_launches = lu_solve_vec<float2>(ctx, A, n, perm, dinv, v32, y32);
       ctx->last_launches = before;
       if(cudaStreamEndCapture(ctx->stream, &g) != cudaSuccess ||
          cudaGraphInstantiate(&solve_graph, g, 0) != cudaSuccess)
@@ -1344,7 +1379,7 @@ struct LuPrecond32 : PrecondFn {
       cudaGraphLaunch(solve_graph, ctx->stream);
       ctx->last_launches += solve_launches;
     } else {
-      lu_solve_vec<float2>(ctx, A, n, perm, v32, y32);
+      lu_solve_vec<float2>(ctx, A, n, perm, dinv, v32, y32);
     }
     k_scale_copy<float2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v32, 1.0, z, n);
     ctx->last_launches += 2;

