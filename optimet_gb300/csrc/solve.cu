@@ -651,6 +651,29 @@ template <typename V> __device__ __forceinline__ V crecip(V a) {
   return r;
 }
 
+// Row i of the panel's columns c + 1 .. nb - 1 minus l times the pivot row u:
+// eight columns' loads are issued before their stores (the loads of a group
+// cannot move above the previous group's stores, which may alias them).
+template <typename V>
+__device__ __forceinline__ void panel_row_update(V *A, long ld, long k, long i, int c, int nb, V l,
+                                                 const V *u) {
+  for(int j0 = c + 1; j0 < nb; j0 += 8) {
+    V a[8];
+#pragma unroll
+    for(int q = 0; q < 8; ++q)
+      if(j0 + q < nb)
+        a[q] = A[(k + j0 + q) * ld + i];
+#pragma unroll
+    for(int q = 0; q < 8; ++q)
+      if(j0 + q < nb) {
+        const V uu = u[j0 + q];
+        a[q].x -= l.x * uu.x - l.y * uu.y;
+        a[q].y -= l.x * uu.y + l.y * uu.x;
+        A[(k + j0 + q) * ld + i] = a[q];
+      }
+  }
+}
+
 // Unblocked LU of the panel A[k:n, k:k+nb) (one CTA); pivots to piv[k..k+nb).
 template <typename V>
 __global__ void __launch_bounds__(1024) k_lu_panel(V *A, long ld, long n, long k, int nb, int *piv,
@@ -703,13 +726,7 @@ __global__ void __launch_bounds__(1024) k_lu_panel(V *A, long ld, long n, long k
       for(long i = col + 1 + t; i < n; i += blockDim.x) {
         V l = cmul(A[col * ld + i], inv);
         A[col * ld + i] = l;
-        for(int j = c + 1; j < nb; ++j) {
-          V u = pivrow[j];
-          V a = A[(k + j) * ld + i];
-          a.x -= l.x * u.x - l.y * u.y;
-          a.y -= l.x * u.y + l.y * u.x;
-          A[(k + j) * ld + i] = a;
-        }
+        panel_row_update(A, ld, k, i, c, nb, l, pivrow);
       }
     }
     __syncthreads();
@@ -842,13 +859,7 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_update(V *A, long ld, long 
     if(ok) {
       V l = cmul(A[col * ld + i], inv);
       A[col * ld + i] = l;
-      for(int j = c + 1; j < nb; ++j) {
-        V uu = u[j];
-        V a = A[(k + j) * ld + i];
-        a.x -= l.x * uu.x - l.y * uu.y;
-        a.y -= l.x * uu.y + l.y * uu.x;
-        A[(k + j) * ld + i] = a;
-      }
+      panel_row_update(A, ld, k, i, c, nb, l, u);
     }
     if(next && i >= ncol) {
       const double v = mag2(A[ncol * ld + i]);
@@ -1066,8 +1077,18 @@ __global__ void __launch_bounds__(256) k_tri_block(const V *A, long ld, long k, 
   const long i = lo + blockIdx.x * (long)blockDim.x + threadIdx.x;
   if(i < hi) {
     V v = src[i];
-    for(int c = 0; c < nb; ++c)
-      v = cfma(A[(k + c) * ld + i], make_neg(xs[c]), v);
+    if(nb == kNb) {  // a full block: the row's kNb loads issued together
+      V a[kNb];
+#pragma unroll
+      for(int c = 0; c < kNb; ++c)
+        a[c] = A[(k + c) * ld + i];
+#pragma unroll
+      for(int c = 0; c < kNb; ++c)
+        v = cfma(a[c], make_neg(xs[c]), v);
+    } else {
+      for(int c = 0; c < nb; ++c)
+        v = cfma(A[(k + c) * ld + i], make_neg(xs[c]), v);
+    }
     src[i] = v;
   }
 }
