@@ -1,7 +1,9 @@
 // Dense solves of the OPTIMET scattering system on the device.
 //
 //  * LU with partial pivoting (the ScalapackSolver / pzgesv role,
-//    ScalapackSolver.cpp:54-130): right-looking, panels of kNb columns.
+//    ScalapackSolver.cpp:54-130): right-looking, panels of kNb columns; the
+//    complex64 LU with tensor cores in blocks of kTcBlock columns with one
+//    rank-kTcBlock trailing update per block.
 //  * Restarted GMRES (the MatrixBelosSolver / Gmres_Zcomp role,
 //    MatrixBelosSolver.cpp:26-104, PreconditionedMatrix.cpp:892-985): classical
 //    Gram-Schmidt with one re-orthogonalisation pass, Givens rotations of
