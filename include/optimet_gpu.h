@@ -138,8 +138,9 @@ int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any
  * k >= 1, host buffers: the tensor-core trailing update of the complex64 LU
  * (bf16 hi/lo split products accumulated in FP32 over all of k, about 17
- * significant bits). The role of the trailing pzgemm of pzgesv
- * (ScalapackSolver.cpp:54-130). */
+ * significant bits). From k = 64 the operands are split into bf16 tiles
+ * once and streamed by bulk copies (the LU's rank-128 path). The role of the
+ * trailing pzgemm of pzgesv (ScalapackSolver.cpp:54-130). */
 int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, long lda,
                      const float *B, long ldb, float *C, long ldc);
 /* Statistics of an ACA-compressed matrix (om_assemble with OM_ACA): device

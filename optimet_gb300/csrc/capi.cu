@@ -439,17 +439,24 @@ int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, lon
   ctx->last_launches = 0;
   float2 *dA = nullptr, *dB = nullptr, *dC = nullptr;
   int *derr = nullptr;
+  unsigned char *dS = nullptr;
   const size_t na = (size_t)lda * k, nbb = (size_t)ldb * n, nc = (size_t)ldc * n;
+  // from k = 64 the LU's path: operands split once, then streamed by bulk copies
+  const size_t ns = k >= 64 ? om::cgemm_sub_tc_split_bytes(m, n, k) : 0;
   int rc = dev_alloc(ctx, &dA, na);
   if(!rc) rc = dev_alloc(ctx, &dB, nbb);
   if(!rc) rc = dev_alloc(ctx, &dC, nc);
   if(!rc) rc = dev_alloc(ctx, &derr, 1);
+  if(!rc && ns) rc = dev_alloc(ctx, &dS, ns);
   if(!rc) {
     cudaMemcpyAsync(dA, A, sizeof(float2) * na, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(dB, B, sizeof(float2) * nbb, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(dC, C, sizeof(float2) * nc, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(derr, 0, sizeof(int), ctx->stream);
-    om::launch_cgemm_sub_tc(ctx, dA, lda, dB, ldb, dC, ldc, m, n, k, derr);
+    if(ns)
+      om::launch_cgemm_sub_tc_split(ctx, dA, lda, dB, ldb, dC, ldc, m, n, k, dS, derr);
+    else
+      om::launch_cgemm_sub_tc(ctx, dA, lda, dB, ldb, dC, ldc, m, n, k, derr);
     rc = check_launch(ctx, "tensor-core update");
     int herr = 0;
     if(!rc) {
@@ -469,6 +476,8 @@ int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, lon
   dev_free(ctx, dB, nbb);
   dev_free(ctx, dC, nc);
   dev_free(ctx, derr, 1);
+  if(dS)
+    dev_free(ctx, dS, ns);
   return rc;
 }
 

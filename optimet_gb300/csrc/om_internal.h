@@ -237,6 +237,12 @@ int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, 
 // timed-out wait
 void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
                          float2 *C, long ldc, long m, long n, int k, int *d_err);
+// The same update from operands split once into bf16 hi / lo tiles (three
+// launches: the two splits and the bulk-copy tensor-core kernel); scratch:
+// cgemm_sub_tc_split_bytes(m, n, k) bytes of device memory, 16-byte aligned.
+size_t cgemm_sub_tc_split_bytes(long m, long n, int k);
+void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
+                               float2 *C, long ldc, long m, long n, int k, void *scratch, int *d_err);
 
 // aca.cu
 int aca_build(om_problem *pr, int harmonic);

@@ -1107,7 +1107,7 @@ __global__ void __launch_bounds__(256) k_tri_block(const V *A, long ld, long k, 
 constexpr long kTcBlock = 128;
 
 template <typename Panel>
-void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Panel &panel) {
+void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Panel &panel, void *split) {
   for(long K = 0; K < n; K += kTcBlock) {
     const long W = std::min<long>(kTcBlock, n - K), KE = K + W;
     for(long k = K; k < KE; k += kNb) {
@@ -1141,8 +1141,12 @@ void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Pane
         launch_cgemm_sub_tc(ctx, A + k * n + kn, n, A + KE * n + k, n, A + KE * n + kn, n, KE - kn,
                             rest, nb, info + 1);
     }
-    launch_cgemm_sub_tc(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest, rest,
-                        (int)W, info + 1);
+    if(split && W >= 64)  // operands split once, streamed by bulk copies
+      launch_cgemm_sub_tc_split(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest,
+                                rest, (int)W, split, info + 1);
+    else
+      launch_cgemm_sub_tc(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest, rest,
+                          (int)W, info + 1);
   }
 }
 
@@ -1155,14 +1159,25 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   ws.ctx = ctx;
   PanelScratch ps{};
   const int maxblk = 4 * ctx->sm_count;
-  if(n >= kTallPanel) {
-    const int rc = alloc_work(ctx, ws, maxblk * (sizeof(double) + sizeof(long)) + kNb * sizeof(V) + 3 * 256);
+  size_t split_bytes = 0;  // the pre-split operands of the rank-128 updates
+  if constexpr(std::is_same<V, float2>::value)
+    if(ctx->lu_tc && n > kTcBlock)
+      split_bytes = cgemm_sub_tc_split_bytes(n, n, (int)kTcBlock);
+  const size_t pan_bytes =
+      n >= kTallPanel ? maxblk * (sizeof(double) + sizeof(long)) + kNb * sizeof(V) + 3 * 256 : 0;
+  void *split = nullptr;
+  if(pan_bytes + split_bytes) {
+    const int rc = alloc_work(ctx, ws, pan_bytes + split_bytes + 256);
     if(rc)
       return rc;
     size_t off = 0;
-    ps.bestv = ws.take<double>(maxblk, off);
-    ps.besti = ws.take<long>(maxblk, off);
-    ps.prow = ws.take<V>(kNb, off);
+    if(pan_bytes) {
+      ps.bestv = ws.take<double>(maxblk, off);
+      ps.besti = ws.take<long>(maxblk, off);
+      ps.prow = ws.take<V>(kNb, off);
+    }
+    if(split_bytes)
+      split = ws.take<unsigned char>(split_bytes, off);
   }
   // LU of the panel A[k:n, k:k+nb) with its row interchanges inside the panel
   auto panel = [&](long k, int nb) {
@@ -1182,7 +1197,7 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   };
   if constexpr(std::is_same<V, float2>::value) {
     if(ctx->lu_tc) {
-      lu_blocked_tc(ctx, A, n, piv, info, panel);
+      lu_blocked_tc(ctx, A, n, piv, info, panel, split);
       return OM_OK;
     }
   }

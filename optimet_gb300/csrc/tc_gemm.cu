@@ -316,6 +316,264 @@ __global__ void __launch_bounds__(128, 3) k_cgemm_sub_tc(const float2 *A, long l
   }
 }
 
+// --- pre-split operands, streamed by bulk copies --------------------------
+//
+// For the LU's rank-128 trailing updates the operands are split once, before
+// the update: L21 (m x k) and U12 (k x n) go to bf16 hi / lo parts laid out
+// exactly as the shared-memory tiles above (per 128-row tile of A or 64-column
+// tile of B and per 32-column chunk of k: the parts one after another, each
+// in the K-major core-matrix layout). The update kernel then copies each
+// chunk's tiles with one-dimensional bulk copies (cp.async.bulk, completion
+// counted on an mbarrier) into one of two shared-memory stages, so that no
+// thread converts or stores operands in the loop. The real part is kept as
+// two accumulators (Ar Br and Ai Bi, subtracted in the epilogue) instead of
+// staging -Bi, which leaves 48 KB a stage: two stages and two CTAs per SM.
+constexpr int kStageA = 4 * kAPart, kStageB = 4 * kBPart, kStage = kStageA + kStageB;
+constexpr int kTc2Smem = 2 * kStage + 128;
+constexpr uint32_t kTmem2Cols = 256;  // three 64-column accumulators
+
+// A (m x k, lda) -> per (row tile, chunk): Arh, Arl, Aih, Ail (8 KB each).
+// One CTA of 512 threads per (row tile, chunk): thread t takes row t % 128
+// and the chunk's K columns 8 (t / 128) .. 8 (t / 128) + 7.
+__global__ void __launch_bounds__(512) k_tc_split_a(const float2 *A, long lda, long m, int k, int nq,
+                                                    unsigned char *out) {
+  const int t = threadIdx.x, r = t & 127, g = t >> 7;
+  const long row = (long)blockIdx.x * kTcM + r;
+  const int q = blockIdx.y, k0 = q * kTcK + 8 * g;
+  float2 v[8];
+#pragma unroll
+  for(int j = 0; j < 8; ++j)
+    v[j] = (row < m && k0 + j < k) ? A[(long)(k0 + j) * lda + row] : make_float2(0.f, 0.f);
+  uint32_t a[4], b[4], c[4], d[4];
+#pragma unroll
+  for(int p = 0; p < 4; ++p) {
+    split2(v[2 * p].x, v[2 * p + 1].x, a[p], b[p]);
+    split2(v[2 * p].y, v[2 * p + 1].y, c[p], d[p]);
+  }
+  unsigned char *o = out + ((size_t)blockIdx.x * nq + q) * kStageA + kmajor_off(r, 8 * g);
+  *reinterpret_cast<uint4 *>(o) = make_uint4(a[0], a[1], a[2], a[3]);
+  *reinterpret_cast<uint4 *>(o + kAPart) = make_uint4(b[0], b[1], b[2], b[3]);
+  *reinterpret_cast<uint4 *>(o + 2 * kAPart) = make_uint4(c[0], c[1], c[2], c[3]);
+  *reinterpret_cast<uint4 *>(o + 3 * kAPart) = make_uint4(d[0], d[1], d[2], d[3]);
+}
+
+// B (k x n, ldb) -> per (column tile, chunk): Brh, Brl, Bih, Bil (4 KB each),
+// as N x K. One CTA of 256 threads per (column tile, chunk): thread t takes
+// column t % 64 and the chunk's K rows 8 (t / 64) .. 8 (t / 64) + 7.
+__global__ void __launch_bounds__(256) k_tc_split_b(const float2 *B, long ldb, long n, int k, int nq,
+                                                    unsigned char *out) {
+  const int t = threadIdx.x, j = t & 63, g = t >> 6;
+  const long col = (long)blockIdx.x * kTcN + j;
+  const int q = blockIdx.y, k0 = q * kTcK + 8 * g;
+  float2 v[8];
+#pragma unroll
+  for(int i = 0; i < 8; ++i)
+    v[i] = (col < n && k0 + i < k) ? B[col * ldb + k0 + i] : make_float2(0.f, 0.f);
+  uint32_t a[4], b[4], c[4], d[4];
+#pragma unroll
+  for(int p = 0; p < 4; ++p) {
+    split2(v[2 * p].x, v[2 * p + 1].x, a[p], b[p]);
+    split2(v[2 * p].y, v[2 * p + 1].y, c[p], d[p]);
+  }
+  unsigned char *o = out + ((size_t)blockIdx.x * nq + q) * kStageB + kmajor_off(j, 8 * g);
+  *reinterpret_cast<uint4 *>(o) = make_uint4(a[0], a[1], a[2], a[3]);
+  *reinterpret_cast<uint4 *>(o + kBPart) = make_uint4(b[0], b[1], b[2], b[3]);
+  *reinterpret_cast<uint4 *>(o + 2 * kBPart) = make_uint4(c[0], c[1], c[2], c[3]);
+  *reinterpret_cast<uint4 *>(o + 3 * kBPart) = make_uint4(d[0], d[1], d[2], d[3]);
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void arrive_expect(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+// C (m x n) -= A B from the pre-split tiles (nq chunks of 32 columns of k).
+// Thread 0 issues the bulk copies (two stages ahead) and the MMAs; the copy
+// of chunk q + 2 waits for the MMAs of chunk q (mbarrier `empty`), the MMAs of
+// chunk q for its copy (mbarrier `full`). The other threads load their rows
+// of C meanwhile; all wait for the last chunk's MMAs, then run the epilogue.
+// Waits are bounded: on time-out the kernel raises *err, frees its TMEM and
+// leaves C untouched.
+__global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, const unsigned char *Bs,
+                                                       int nq, float2 *C, long ldc, long m, long n,
+                                                       int *err) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  uint64_t *full = reinterpret_cast<uint64_t *>(tsm + 2 * kStage);  // [2]
+  uint64_t *empty = full + 2;                                        // [2]
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(full + 4);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const long r0 = (long)blockIdx.x * kTcM, c0 = (long)blockIdx.y * kTcN;
+  const unsigned char *Ab = As + (size_t)blockIdx.x * nq * kStageA;
+  const unsigned char *Bb = Bs + (size_t)blockIdx.y * nq * kStageB;
+
+  if(warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(tmem_slot)),
+                 "r"(kTmem2Cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if(t == 0) {
+    for(int i = 0; i < 4; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(full + i)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // the C tile's lines requested into L2 (as in k_cgemm_sub_tc)
+  {
+    const long col = c0 + (t >> 1);
+    if(col < n) {
+#pragma unroll
+      for(int i = 0; i < 4; ++i) {
+        const long row = r0 + (t & 1) * 64 + 16 * i;
+        if(row < m)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(C + col * ldc + row));
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t d_r1 = tmem, d_r2 = tmem + kTcN, d_im = tmem + 2 * kTcN;
+
+  uint32_t ok = 1;
+  if(t == 0) {
+    int issued = 0, landed = 0, committed = 0;  // chunks copied in / waited for / with MMAs issued
+    auto issue = [&](int q) {
+      const int s = q & 1;
+      arrive_expect(full + s, (uint32_t)kStage);
+      bulk_load(tsm + s * kStage, Ab + (size_t)q * kStageA, (uint32_t)kStageA, full + s);
+      bulk_load(tsm + s * kStage + kStageA, Bb + (size_t)q * kStageB, (uint32_t)kStageB, full + s);
+      issued = q + 1;
+    };
+    issue(0);
+    if(nq > 1)
+      issue(1);
+    for(int q = 0; q < nq; ++q) {
+      const int s = q & 1;
+      const uint32_t par = (uint32_t)(q >> 1) & 1u;
+      if(!wait_phase(full + s, par)) {
+        ok = 0;
+        break;
+      }
+      landed = q + 1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      unsigned char *Ar = tsm + s * kStage;
+      unsigned char *Arh = Ar, *Arl = Ar + kAPart, *Aih = Ar + 2 * kAPart, *Ail = Ar + 3 * kAPart;
+      unsigned char *Brh = Ar + kStageA, *Brl = Brh + kBPart, *Bih = Brh + 2 * kBPart,
+                    *Bil = Brh + 3 * kBPart;
+      for(int st = 0; st < kTcK / 16; ++st) {
+        const uint32_t ko = st * 256;  // two core matrices along K per MMA
+        auto da = [&](unsigned char *p) { return umma_desc(smem_addr(p) + ko, 128, 512); };
+        const uint32_t acc = q > 0 || st > 0;
+        // Ar Br
+        mma_bf16(d_r1, da(Arh), da(Brh), acc);
+        mma_bf16(d_r1, da(Arh), da(Brl), 1);
+        mma_bf16(d_r1, da(Arl), da(Brh), 1);
+        // Ai Bi
+        mma_bf16(d_r2, da(Aih), da(Bih), acc);
+        mma_bf16(d_r2, da(Aih), da(Bil), 1);
+        mma_bf16(d_r2, da(Ail), da(Bih), 1);
+        // Ar Bi + Ai Br
+        mma_bf16(d_im, da(Arh), da(Bih), acc);
+        mma_bf16(d_im, da(Arh), da(Bil), 1);
+        mma_bf16(d_im, da(Arl), da(Bih), 1);
+        mma_bf16(d_im, da(Aih), da(Brh), 1);
+        mma_bf16(d_im, da(Aih), da(Brl), 1);
+        mma_bf16(d_im, da(Ail), da(Brh), 1);
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_addr(empty + s))
+          : "memory");
+      committed = q + 1;
+      if(q + 2 < nq) {  // stage s is free once these MMAs have read it
+        if(!wait_phase(empty + s, par)) {
+          ok = 0;
+          break;
+        }
+        issue(q + 2);
+      }
+    }
+    if(!ok) {  // before leaving: the copies still in flight and the last MMAs (bounded)
+      for(int q = landed; q < issued; ++q)
+        wait_phase(full + (q & 1), (uint32_t)(q >> 1) & 1u);
+      if(committed > 0)
+        wait_phase(empty + ((committed - 1) & 1), (uint32_t)((committed - 1) >> 1) & 1u);
+    }
+  }
+  // columns 0 .. 31 of this thread's row of C, loaded while the MMAs run
+  const long r = r0 + warp * 32 + lane;
+  float2 cv[32];
+#pragma unroll
+  for(int q = 0; q < 32; ++q) {
+    const long col = c0 + q;
+    cv[q] = (r < m && col < n) ? C[col * ldc + r] : make_float2(0.f, 0.f);
+  }
+  // bounded wait for the last chunk's MMAs (they complete after all earlier ones)
+  const int last = nq - 1;
+  uint32_t done = __syncthreads_and(ok);
+  if(done)
+    done = wait_phase(empty + (last & 1), (uint32_t)(last >> 1) & 1u);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  done = __syncthreads_and(done);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if(!done) {
+    if(t == 0)
+      atomicExch(err, 1);
+  } else {
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll
+    for(int g = 0; g < kTcN / 16; ++g) {
+      const int cc = 16 * g, base = (g & 1) * 16;
+      uint32_t a[16], b[16], c[16];
+#define OM_TMEM_LD16(dst, addr)                                                                     \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
+               : "=r"(dst[0]), "=r"(dst[1]), "=r"(dst[2]), "=r"(dst[3]), "=r"(dst[4]), "=r"(dst[5]),  \
+                 "=r"(dst[6]), "=r"(dst[7]), "=r"(dst[8]), "=r"(dst[9]), "=r"(dst[10]),              \
+                 "=r"(dst[11]), "=r"(dst[12]), "=r"(dst[13]), "=r"(dst[14]), "=r"(dst[15])           \
+               : "r"(addr))
+      OM_TMEM_LD16(a, d_r1 + lane_base + cc);
+      OM_TMEM_LD16(b, d_r2 + lane_base + cc);
+      OM_TMEM_LD16(c, d_im + lane_base + cc);
+#undef OM_TMEM_LD16
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if(r < m) {
+#pragma unroll
+        for(int q = 0; q < 16; ++q) {
+          const long col = c0 + cc + q;
+          if(col < n) {
+            float2 v = cv[base + q];
+            v.x -= __uint_as_float(a[q]) - __uint_as_float(b[q]);
+            v.y -= __uint_as_float(c[q]);
+            C[col * ldc + r] = v;
+          }
+        }
+      }
+      if(g < 2) {
+#pragma unroll
+        for(int q = 0; q < 16; ++q) {
+          const long col = c0 + cc + 32 + q;
+          cv[base + q] = (r < m && col < n) ? C[col * ldc + r] : make_float2(0.f, 0.f);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if(warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmem2Cols));
+  }
+}
+
 }  // namespace
 
 void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
@@ -324,6 +582,24 @@ void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float
   dim3 grid((unsigned)((m + kTcM - 1) / kTcM), (unsigned)((n + kTcN - 1) / kTcN));
   k_cgemm_sub_tc<<<grid, 128, kTcSmem, ctx->stream>>>(A, lda, B, ldb, C, ldc, m, n, k, d_err);
   ctx->last_launches++;
+}
+
+size_t cgemm_sub_tc_split_bytes(long m, long n, int k) {
+  const size_t nq = (size_t)((k + kTcK - 1) / kTcK);
+  return (size_t)((m + kTcM - 1) / kTcM) * nq * kStageA + (size_t)((n + kTcN - 1) / kTcN) * nq * kStageB;
+}
+
+void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
+                               float2 *C, long ldc, long m, long n, int k, void *scratch, int *d_err) {
+  const int nq = (k + kTcK - 1) / kTcK;
+  const unsigned mt = (unsigned)((m + kTcM - 1) / kTcM), nt = (unsigned)((n + kTcN - 1) / kTcN);
+  unsigned char *As = static_cast<unsigned char *>(scratch);
+  unsigned char *Bs = As + (size_t)mt * nq * kStageA;
+  k_tc_split_a<<<dim3(mt, (unsigned)nq), 512, 0, ctx->stream>>>(A, lda, m, k, nq, As);
+  k_tc_split_b<<<dim3(nt, (unsigned)nq), 256, 0, ctx->stream>>>(B, ldb, n, k, nq, Bs);
+  cudaFuncSetAttribute(k_cgemm_sub_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, kTc2Smem);
+  k_cgemm_sub_tc2<<<dim3(mt, nt), 128, kTc2Smem, ctx->stream>>>(As, Bs, nq, C, ldc, m, n, d_err);
+  ctx->last_launches += 3;
 }
 
 }  // namespace om
