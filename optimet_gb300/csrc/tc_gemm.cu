@@ -19,6 +19,10 @@
 // C, whose first 16 columns are loaded while the last MMAs run: C is read and
 // written once for the whole rank-k update. Waits are bounded: on time-out
 // the kernel raises *err, still frees its TMEM and leaves C untouched.
+//
+// From k = 64 (the LU's rank-128 updates) a second path splits the operands
+// once and streams them by bulk copies (k_tc_split_a/b, k_cgemm_sub_tc2,
+// below).
 #include <cuda_bf16.h>
 #include <stdint.h>
 
