@@ -144,6 +144,51 @@ def test_rotation_invariance_of_extinction(oracle):
     assert abs(rot[3] - base[3]) / abs(base[3]) < 1e-12
 
 
+def _wigner_small_d(n, theta):
+    """d^n_{m' m}(theta) from the explicit sum (Wigner's formula), m', m = -n..n."""
+    from math import factorial as f
+    c, s = np.cos(theta / 2), np.sin(theta / 2)
+    d = np.zeros((2 * n + 1, 2 * n + 1))
+    for mp in range(-n, n + 1):
+        for m in range(-n, n + 1):
+            tot = 0.0
+            for k in range(0, 2 * n + 1):
+                a, b, cc, dd = n + m - k, k, n - k - mp, k - m + mp
+                if min(a, b, cc, dd) < 0:
+                    continue
+                tot += ((-1) ** (k - m + mp) * c ** (2 * n + m - mp - 2 * k) * s ** (2 * k - m + mp)
+                        / (f(a) * f(b) * f(cc) * f(dd)))
+            d[mp + n, m + n] = tot * np.sqrt(float(f(n + mp) * f(n - mp) * f(n + m) * f(n - m)))
+    return d
+
+
+@pytest.mark.parametrize("nmax,R", [(4, (300 * nm, 1.1, 0.7)), (6, (450 * nm, 2.6, -2.2)),
+                                    (8, (260 * nm, 0.35, 4.0))])
+def test_coupling_is_a_rotated_z_axis_translation(oracle, nmax, R):
+    """A(R) = U A(|R| z) U^H and B(R) = U B(|R| z) U^H, U block-diagonal over
+    the degree n with U[p(n, m'), p(n, m)] = d^n_{m' m}(theta) e^{i m' phi},
+    and the z-axis blocks diagonal in m: an identity independent of the
+    Stout recurrences, for both Bessel kinds (the rotation-based form of the
+    translation, point-and-shoot)."""
+    k = complex(2 * np.pi / 600e-9)
+    P = nmax * (nmax + 2)
+    U = np.zeros((P, P), complex)
+    for n in range(1, nmax + 1):
+        d = _wigner_small_d(n, R[1])
+        for mp in range(-n, n + 1):
+            for m in range(-n, n + 1):
+                U[n * (n + 1) - mp - 1, n * (n + 1) - m - 1] = d[mp + n, m + n] * np.exp(1j * mp * R[2])
+    mof = np.array([m for n in range(1, nmax + 1) for m in range(n, -n - 1, -1)])
+    for regular in (False, True):
+        A, B = oracle.coupling(R, k, nmax, regular)
+        Az, Bz = oracle.coupling((R[0], 0.0, 0.0), k, nmax, regular)
+        assert np.max(np.abs(Az[mof[:, None] != mof[None, :]])) == 0.0
+        assert np.max(np.abs(Bz[mof[:, None] != mof[None, :]])) == 0.0
+        scale = np.max(np.abs(A))
+        assert np.max(np.abs(U @ Az @ U.conj().T - A)) / scale < 1e-12
+        assert np.max(np.abs(U @ Bz @ U.conj().T - B)) / scale < 1e-12
+
+
 def test_translation_convergence_single_sphere(oracle):
     k0 = np.array([0.3, -0.5, 0.8])
     k0 /= np.linalg.norm(k0)
