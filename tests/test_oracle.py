@@ -189,6 +189,39 @@ def test_coupling_is_a_rotated_z_axis_translation(oracle, nmax, R):
         assert np.max(np.abs(U @ Bz @ U.conj().T - B)) / scale < 1e-12
 
 
+def test_scattering_matrix_from_rotated_translations(oracle):
+    """The oracle's S (PreconditionedMatrix.cpp:369-397) block by block from
+    the rotated form: S_ij = -T_i [A^T B^T; B^T A^T] with A, B the coupling of
+    r_i - r_j (the reference's inverted `regular` flag set) and
+    A = U A(|R| z) U^H, B = U B(|R| z) U^H. Pins the layout, the transposes
+    and the T scaling that a rotation-based assembly has to reproduce."""
+    nmax = 4
+    P = nmax * (nmax + 2)
+    xyz = np.array([[0, 0, 0], [220, 30, -40], [-60, 210, 90]]) * nm
+    cl = oracle.Cluster(xyz=xyz, radius=np.array([60, 50, 70]) * nm, eps=(2.0 + 0.05j) ** 2, nmax=nmax,
+                        wavelength=650 * nm)
+    pr = oracle.Problem(cl)
+    S = pr.scattering_matrix()
+    k0, _ = pr.wave_numbers()
+    for i in range(3):
+        for j in range(3):
+            blk = S[2 * P * i:2 * P * (i + 1), 2 * P * j:2 * P * (j + 1)]
+            if i == j:
+                assert np.array_equal(blk, np.eye(2 * P))
+                continue
+            r, th, ph = oracle.to_spherical(*(xyz[i] - xyz[j]))
+            U = np.zeros((P, P), complex)
+            for n in range(1, nmax + 1):
+                d = _wigner_small_d(n, th)
+                for mp in range(-n, n + 1):
+                    for m in range(-n, n + 1):
+                        U[n * (n + 1) - mp - 1, n * (n + 1) - m - 1] = d[mp + n, m + n] * np.exp(1j * mp * ph)
+            Az, Bz = oracle.coupling((r, 0.0, 0.0), k0, nmax, True)
+            A, B = U @ Az @ U.conj().T, U @ Bz @ U.conj().T
+            got = -pr.tmatrix(i)[:, None] * np.block([[A.T, B.T], [B.T, A.T]])
+            assert np.max(np.abs(got - blk)) / np.max(np.abs(blk)) < 1e-12
+
+
 def test_translation_convergence_single_sphere(oracle):
     k0 = np.array([0.3, -0.5, 0.8])
     k0 /= np.linalg.norm(k0)
