@@ -326,7 +326,10 @@ def max_threads() -> int:
 
 
 def assemble_pairs(pr: Problem, pairs):
-    """Blocks S_ij for the given (i, j) pairs (timing sample of the assembly)."""
+    """Off-diagonal blocks S_ij (i != j) for the given (i, j) pairs: the
+    assembly's timing sample, and sampled parity at sizes where the full S is
+    too large. The library writes each block column-major, so the C-ordered
+    buffer is returned transposed back to S's orientation."""
     pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
     n2 = 2 * pr.cl.P
     out = np.zeros((pairs.shape[0], n2, n2), np.complex128)
@@ -334,7 +337,7 @@ def assemble_pairs(pr: Problem, pairs):
                                   _p(out))
     if rc:
         raise RuntimeError(lib().orc_last_error().decode())
-    return out
+    return out.transpose(0, 2, 1)
 
 
 def matvec(A, x):

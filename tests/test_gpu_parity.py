@@ -302,3 +302,36 @@ def test_tma_matvec_bitwise_equal(G, ctx, N, nmax):
     ctx.tune(matvec_tma=1)
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
     assert out[0][2:] == out[1][2:]
+
+
+def test_c1_scale_sampled_blocks_and_residual(G, ctx, oracle):
+    """N = 100 spheres at nMax = 8 (16,000 unknowns, the C1 size), where the
+    oracle's dense solve would take minutes on the host: the GPU's S against
+    the oracle's blocks on a sample of pairs (1e-10), the FP64 GMRES
+    solution's true residual recomputed in FP64 on the host, and the precision
+    form's cross sections against FP64 (1e-6)."""
+    rng = np.random.default_rng(100)
+    xyz, rad = random_cluster(rng, 100, 2000 * nm, 50 * nm, 80 * nm, 20 * nm)
+    cl = oracle.Cluster(xyz=xyz, radius=rad, eps=(0.3 + 3.0j) ** 2, nmax=8, wavelength=650 * nm,
+                        bg_eps=1.33 ** 2)
+    pr = make(G, ctx, cl)
+    Q = pr.source_vector()
+    pr.assemble(G.FF, G.C128)
+    S = pr.matrix()
+    P2 = 2 * cl.P
+    pairs = np.concatenate([rng.integers(0, 100, size=(24, 2)), [[0, 99], [99, 0], [41, 57]]])
+    pairs = pairs[pairs[:, 0] != pairs[:, 1]]  # off-diagonal blocks (S_ii is the identity)
+    blocks = oracle.assemble_pairs(oracle.Problem(cl), pairs)
+    for (i, j), b in zip(pairs, blocks):
+        assert rel(S[P2 * i:P2 * (i + 1), P2 * j:P2 * (j + 1)], b) < 1e-10, (i, j)
+    pr.solve(G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=400, restarts=6))
+    x, _ = pr.coefficients()
+    assert np.linalg.norm(Q - S @ x) / np.linalg.norm(Q) < 1e-9
+    ref = pr.cross_sections()
+    del S
+    mixed = make(G, ctx, cl)
+    mixed.source_vector(copy=False)
+    mixed.assemble(G.FF, G.C64)
+    mixed.solve(G.options(G.SOLVE_FGMRES_MIXED, tol=1e-8, max_iter=30, restarts=8, inner_iter=80,
+                          inner_tol=1e-4))
+    assert np.max(np.abs(mixed.cross_sections() - ref) / np.abs(ref)) < 1e-6
