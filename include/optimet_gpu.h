@@ -133,6 +133,9 @@ typedef struct {
   int lu_tensor_cores;   /* complex64 LU trailing updates on the tensor cores: 1 (default) / 0 */
   int matvec_tma;        /* complex64 x complex64 matvec with TMA-staged matrix tiles: 1 (default for
                             a context) / 0 (default for the slots of a server with several slots) */
+  int assemble_rotation; /* complex64 assembly by rotated z-axis translations (one recurrence
+                            chain per pair, FP32 rotation products): 1 (default) / 0 (the general
+                            translation's 3 nMax + 1 chains per pair, FP32 block forming) */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any

@@ -428,6 +428,8 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
     ctx->lu_tc = t->lu_tensor_cores ? 1 : 0;
   if(t->matvec_tma >= 0)
     ctx->mv_tma = t->matvec_tma ? 1 : 0;
+  if(t->assemble_rotation >= 0)
+    ctx->asm_rot = t->assemble_rotation ? 1 : 0;
   return OM_OK;
 }
 

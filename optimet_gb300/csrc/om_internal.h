@@ -30,6 +30,7 @@ struct CoefTables {
   double *qf = nullptr;
   double *pf = nullptr;
   double *legc = nullptr;  // normalised-Legendre recurrence coefficients for l <= 2 nMax
+  double *wig = nullptr;   // Wigner d recurrence coefficients for n <= nMax (wigner_tables)
 };
 constexpr int kQfacStride = 6;
 constexpr int kPfacStride = 8;
@@ -113,6 +114,7 @@ struct om_context {
   int mv_tma = 1;                                // complex64 matvecs staged by TMA
   int carve_asm = -1, carve_mv = -1;  // preferred smem carveout (percent), -1 = driver's choice
   int lu_tc = 1;  // complex64 LU trailing updates on the tensor cores
+  int asm_rot = 1;  // precision-form assembly by rotated z-axis translations (assemble_rot.cu)
   size_t budget = 0;
   size_t used = 0;
   std::string err;
@@ -203,6 +205,14 @@ void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, 
 void launch_assemble_batch(om_context *ctx, int nmax, int precision, const BatchMat *d_mats,
                            int nmats, int per_mat, cudaStream_t stream);
 void launch_source(om_problem *pr);
+
+// assemble_rot.cu: the precision-form (complex64) assembly by rotations;
+// wigner_tables(nmax) are the host-built coefficients of its Wigner d recurrence
+std::vector<double> wigner_tables(int nmax);
+int rot_smem_bytes(int nmax);
+void launch_assemble_rot(om_problem *pr, int harmonic);
+void launch_assemble_rot_batch(om_context *ctx, int nmax, const BatchMat *d_mats, int nmats, int per_mat,
+                               cudaStream_t stream);
 void launch_sh_weights(om_problem *pr);
 int launch_coupling(om_context *ctx, const double *d_rel, int count, zd waveK, int nmax,
                     int hankel, zd *d_A, zd *d_B);

@@ -1007,6 +1007,7 @@ const CoefTables &coef_tables(om_context *ctx, int nmax) {
   t.qf = up(qf);
   t.pf = up(pf);
   t.legc = up(legc);
+  t.wig = up(wigner_tables(nmax));
   ctx->tables.push_back(t);
   return ctx->tables.back();
 }
@@ -1028,8 +1029,12 @@ void launch_incident(om_problem *pr, const double einc[6]) {
 
 void launch_assemble(om_problem *pr, int harmonic, int precision) {
   om_context *ctx = pr->ctx;
-  const CoefTables &ct = coef_tables(ctx, pr->nmax);
   const bool mixed = precision == OM_C64;
+  if(mixed && ctx->asm_rot) {
+    launch_assemble_rot(pr, harmonic);
+    return;
+  }
+  const CoefTables &ct = coef_tables(ctx, pr->nmax);
   Layout y = make_layout(pr->nmax, smem_limit(), mixed);
   AssembleArgs a;
   a.cart = pr->d_cart;
@@ -1093,8 +1098,12 @@ void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, 
 
 void launch_assemble_batch(om_context *ctx, int nmax, int precision, const BatchMat *d_mats,
                            int nmats, int per_mat, cudaStream_t stream) {
-  const CoefTables &ct = coef_tables(ctx, nmax);
   const bool mixed = precision == OM_C64;
+  if(mixed && ctx->asm_rot) {
+    launch_assemble_rot_batch(ctx, nmax, d_mats, nmats, per_mat, stream);
+    return;
+  }
+  const CoefTables &ct = coef_tables(ctx, nmax);
   Layout y = make_layout(nmax, smem_limit(), mixed);
   AssembleArgs a{};
   a.rec = ct.rec;
