@@ -578,6 +578,9 @@ void om_context_destroy(om_context *ctx) {
     cudaFree(t.qf);
     cudaFree(t.pf);
     cudaFree(t.legc);
+    cudaFree(t.rot_i);
+    cudaFree(t.rot_d);
+    cudaFree(t.rot_z);
   }
   for(auto &t : ctx->clg)
     cudaFree(t.second);

@@ -30,7 +30,12 @@ struct CoefTables {
   double *qf = nullptr;
   double *pf = nullptr;
   double *legc = nullptr;  // normalised-Legendre recurrence coefficients for l <= 2 nMax
-  double *wig = nullptr;   // Wigner d recurrence coefficients for n <= nMax (wigner_tables)
+  // rotation assembly (assemble_rot.cu, rotation_tables): Wigner d step
+  // coefficients and lane schedule, the z-axis translation map, the Az / Bz table
+  int *rot_i = nullptr;
+  double *rot_d = nullptr;
+  float *rot_z = nullptr;
+  int rot_nent = 0, rot_ent_base = 0, rot_onl_base = 0;
 };
 constexpr int kQfacStride = 6;
 constexpr int kPfacStride = 8;
@@ -206,9 +211,10 @@ void launch_assemble_batch(om_context *ctx, int nmax, int precision, const Batch
                            int nmats, int per_mat, cudaStream_t stream);
 void launch_source(om_problem *pr);
 
-// assemble_rot.cu: the precision-form (complex64) assembly by rotations;
-// wigner_tables(nmax) are the host-built coefficients of its Wigner d recurrence
-std::vector<double> wigner_tables(int nmax);
+// assemble_rot.cu: the precision-form (complex64) assembly by rotations and
+// its host-built tables for one nMax
+void rotation_tables(int nmax, std::vector<int> &ti, std::vector<double> &td, std::vector<float> &tz, int &nent,
+                     int &ent_base, int &onl_base);
 int rot_smem_bytes(int nmax);
 void launch_assemble_rot(om_problem *pr, int harmonic);
 void launch_assemble_rot_batch(om_context *ctx, int nmax, const BatchMat *d_mats, int nmats, int per_mat,

@@ -1007,7 +1007,18 @@ const CoefTables &coef_tables(om_context *ctx, int nmax) {
   t.qf = up(qf);
   t.pf = up(pf);
   t.legc = up(legc);
-  t.wig = up(wigner_tables(nmax));
+  {
+    std::vector<int> ti;
+    std::vector<double> td;
+    std::vector<float> tz;
+    rotation_tables(nmax, ti, td, tz, t.rot_nent, t.rot_ent_base, t.rot_onl_base);
+    t.rot_d = up(td);
+    if(cudaMalloc(&t.rot_i, ti.size() * sizeof(int)) != cudaSuccess ||
+       cudaMalloc(&t.rot_z, tz.size() * sizeof(float)) != cudaSuccess)
+      throw std::runtime_error("cudaMalloc failed for rotation tables");
+    cudaMemcpy(t.rot_i, ti.data(), ti.size() * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(t.rot_z, tz.data(), tz.size() * sizeof(float), cudaMemcpyHostToDevice);
+  }
   ctx->tables.push_back(t);
   return ctx->tables.back();
 }
