@@ -19,7 +19,7 @@ x-polarised. Synthetic data. Inputs exceed L2 (S alone is 32.8 GB complex64 +
 
 The headline number is the batched/served form: om_server with two slots
 (device contexts with their own streams and host threads) takes the scan's
-wavelengths in order, so one wavelength's FP64-bound assembly overlaps the
+wavelengths in order, so one wavelength's assembly overlaps the
 previous wavelength's HBM-bound solve; the FP64 form is served the same way.
 The single-stream numbers of both forms are reported beside it.
 
@@ -55,6 +55,10 @@ WORKLOADS = {
                   nmax=8, lam=650 * nm, seed=20260403,
                   desc="profiling case: N=40 spheres, nMax=8 (6,400 unknowns), 1.5 um cube, "
                        "radii U[40,70] nm, index 2.0+0.05i in vacuum"),
+    "mid": dict(N=120, edge=4000 * nm * (120 / 400) ** (1 / 3), rmin=40 * nm, rmax=70 * nm, index=2.0 + 0.05j,
+                host=1.0, nmax=8, lam=650 * nm, seed=20260402,
+                desc="profiling case: N=120 spheres at the c2 number density, nMax=8 (19,200 unknowns, "
+                     "complex64 S 2.95 GB)"),
     "c1": dict(N=100, edge=2000 * nm, rmin=50 * nm, rmax=80 * nm, index=0.3 + 3.0j, host=1.33,
                nmax=8, lam=650 * nm, seed=20260401,
                desc="N=100 spheres, nMax=8 (16,000 unknowns), 2 um cube, radii U[50,80] nm, "
@@ -273,8 +277,8 @@ def gpu_arm(args, w):
 
     # ---- batched / served form: om_server with `slots` contexts on the GPU ----
     # Successive wavelengths of the scan run on alternating slots, so one
-    # wavelength's FP64-bound assembly overlaps the previous one's HBM-bound
-    # solve. Same requests for both forms; a slot keeps its problem resident
+    # wavelength's assembly overlaps the previous one's solve (both
+    # HBM-bound). Same requests for both forms; a slot keeps its problem resident
     # across wavelengths (cluster_key) like the reference's scan keeps its
     # Geometry.
     def served(opts, precision, k, key, tuning=None, tune_count=6):
@@ -386,7 +390,11 @@ def gpu_arm(args, w):
         "kernels": {
             "assemble_mixed": {"ms_avg": asm_ms / max(asm_n, 1), "launches": asm_n,
                                "written_GBps": bytes_asm / (asm_ms / max(asm_n, 1) * 1e-3) / 1e9
-                               if asm_n else None, "bound": "fp64 ALU"},
+                               if asm_n else None,
+                               "frac_of_hbm_peak": bytes_asm / (asm_ms / max(asm_n, 1) * 1e-3) / 1e9 / hbm
+                               if asm_n else None,
+                               "kernel": "k_assemble_rot (rotated z-axis translations)",
+                               "bound": "hbm write (8 n^2 B per assembly)"},
             "matvec_c64": {"ms_avg": mv_ms / max(mv_n, 1), "launches": mv_n,
                            "GBps": achieved, "bound": "hbm"},
             "matvec_c64_compensated": {"ms_avg": kt["matvec_c64_df"][0] / max(kt["matvec_c64_df"][1], 1),
@@ -937,6 +945,30 @@ def aca_arm(args):
             "cases": out}
 
 
+def assemble_arm(args, w):
+    """Precision-form assemblies only (profiling): warm-up then `steps` timed
+    om_assemble(FF, C64) calls of the workload's cluster, CUDA-event timers."""
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    ctx = G.Context(0)
+    xyz, rad = cluster(w)
+    sp = G.spheres_array(xyz, rad, complex(w["index"]) ** 2, w["nmax"])
+    pr = G.Problem(ctx, sp, G.medium(complex(w["host"]) ** 2), G.plane_wave(w["lam"]))
+    for _ in range(args.warmup):
+        pr.assemble(G.FF, G.C64)
+    ctx.timers(True)
+    for _ in range(args.steps):
+        pr.assemble(G.FF, G.C64)
+    ms, launches = ctx.timers(False)["assemble"]
+    n = pr.n
+    pr.close()
+    ctx.close()
+    per = ms / max(launches, 1)
+    return {"workload": w["desc"], "unknowns": n, "ms_per_assembly": per, "launches": launches,
+            "written_GB": 8.0 * n * n / 1e9, "written_GBps": 8.0 * n * n / 1e6 / per}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -947,6 +979,8 @@ def main():
     ap.add_argument("--workload", default="c2",
                     choices=sorted(WORKLOADS) + ["c1f", "c2lu", "c3", "c4", "aca"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--assemble-only", action="store_true",
+                    help="only timed precision-form assemblies of the workload (profiling runs)")
     ap.add_argument("--single-stream", action="store_true",
                     help="only the single-stream measurement of both forms (profiling runs)")
     ap.add_argument("--c3-clusters", type=int, default=64)
@@ -974,6 +1008,8 @@ def main():
         out = batch_arm(args) if args.impl != "reference" else None
     elif args.workload == "c4":
         out = serve_arm(args) if args.impl != "reference" else None
+    elif args.assemble_only:
+        out = assemble_arm(args, WORKLOADS[args.workload]) if args.impl != "reference" else None
     else:
         w = WORKLOADS[args.workload]
         out = reference_arm(args, w) if args.impl == "reference" else gpu_arm(args, w)
