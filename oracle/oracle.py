@@ -23,9 +23,20 @@ _lib = None
 _dp = C.POINTER(C.c_double)
 
 
+def reference_tree():
+    """The OPTIMET source tree named by $OPTIMET_REFERENCE when it holds the
+    vendored AMOS sources (srcAna/amos.c), else None."""
+    root = os.environ.get("OPTIMET_REFERENCE")
+    if root and os.path.exists(os.path.join(root, "srcAna", "amos.c")):
+        return root
+    return None
+
+
 def build(ref: bool = False) -> None:
-    """Compile the oracle (and, when the reference tree exists, its AMOS)."""
-    targets = ["port"] + (["ref"] if ref else [])
+    """Compile the oracle and, with ref and a reference tree in
+    $OPTIMET_REFERENCE, the reference's own AMOS Bessel code."""
+    root = reference_tree() if ref else None
+    targets = ["port"] + (["ref", f"REFERENCE={root}"] if root else [])
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
 

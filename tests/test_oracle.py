@@ -36,8 +36,9 @@ def test_bessel_against_reference_amos_table(oracle):
         assert np.max(np.abs(dH[1:] - g["dH"][i][1:]) / np.abs(g["dH"][i][1:])) < 1e-12, z
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/srcAna/amos.c"),
-                    reason="reference tree absent (GPU box): AMOS pin runs where it exists")
+@pytest.mark.skipif(not os.environ.get("OPTIMET_REFERENCE")
+                    or not os.path.exists(os.path.join(os.environ["OPTIMET_REFERENCE"], "srcAna", "amos.c")),
+                    reason="OPTIMET_REFERENCE unset: the live AMOS pin runs where a reference tree is given")
 def test_bessel_against_live_amos(oracle):
     oracle.build(ref=True)
     rng = np.random.default_rng(3)
