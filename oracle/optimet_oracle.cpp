@@ -755,6 +755,78 @@ void source_vector(const Problem &pr, cplx *Q) {
   }
 }
 
+// Householder QR with column pivoting, then R x = Q^H b: the serial solver of
+// PreconditionedMatrix::solve (PreconditionedMatrixSolver.h:45-79, Eigen's
+// colPivHouseholderQr().solve). At step k the remaining column of largest
+// norm is swapped in (norms recomputed exactly), a reflector
+// H = I - tau v v^H with v_0 = 1 zeroes it below the diagonal, and H is applied
+// to the trailing columns and to b.
+int qr_solve(int n, const cplx *A_in, const cplx *b, cplx *x) {
+  std::vector<cplx> A(A_in, A_in + size_t(n) * n), y(b, b + n);
+  std::vector<int> perm(n);
+  for(int j = 0; j < n; ++j)
+    perm[j] = j;
+  std::vector<double> cn(n);
+  for(int k = 0; k < n; ++k) {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for(int j = k; j < n; ++j) {
+      double s = 0.0;
+      const cplx *c = &A[size_t(j) * n];
+      for(int i = k; i < n; ++i)
+        s += std::norm(c[i]);
+      cn[j] = s;
+    }
+    int jm = k;
+    for(int j = k + 1; j < n; ++j)
+      if(cn[j] > cn[jm])
+        jm = j;
+    if(jm != k) {
+      std::swap_ranges(A.begin() + size_t(k) * n, A.begin() + size_t(k + 1) * n, A.begin() + size_t(jm) * n);
+      std::swap(perm[k], perm[jm]);
+    }
+    cplx *ck = &A[size_t(k) * n];
+    const double xn = std::sqrt(cn[jm]);
+    if(xn == 0.0)
+      return k + 1;
+    const cplx x0 = ck[k];
+    const cplx ph = std::abs(x0) > 0.0 ? x0 / std::abs(x0) : cplx(1.0, 0.0);
+    const cplx alpha = -ph * xn;  // R_kk
+    const cplx v0 = x0 - alpha;
+    for(int i = k + 1; i < n; ++i)
+      ck[i] /= v0;  // v = (1, ck[k+1..] )
+    const cplx tau = (alpha - x0) / alpha;
+    ck[k] = alpha;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for(int j = k + 1; j < n; ++j) {
+      cplx *cj = &A[size_t(j) * n];
+      cplx d = cj[k];
+      for(int i = k + 1; i < n; ++i)
+        d += std::conj(ck[i]) * cj[i];
+      d *= std::conj(tau);
+      cj[k] -= d;
+      for(int i = k + 1; i < n; ++i)
+        cj[i] -= d * ck[i];
+    }
+    cplx d = y[k];
+    for(int i = k + 1; i < n; ++i)
+      d += std::conj(ck[i]) * y[i];
+    d *= std::conj(tau);
+    y[k] -= d;
+    for(int i = k + 1; i < n; ++i)
+      y[i] -= d * ck[i];
+  }
+  std::vector<cplx> z(n);
+  for(int k = n - 1; k >= 0; --k) {
+    cplx v = y[k];
+    for(int j = k + 1; j < n; ++j)
+      v -= A[size_t(j) * n + k] * z[j];
+    z[k] = v / A[size_t(k) * n + k];
+  }
+  for(int k = 0; k < n; ++k)
+    x[perm[k]] = z[k];
+  return 0;
+}
+
 // Dense LU with partial pivoting (the pzgesv role, ScalapackSolver.cpp:54-130).
 int lu_solve(int n, const cplx *A_in, const cplx *b, cplx *x) {
   std::vector<cplx> A(A_in, A_in + size_t(n) * n);
@@ -1880,6 +1952,10 @@ int orc_lu_solve(int n, const double *A, const double *b, double *x) {
   return lu_solve(n, C(A), C(b), C(x));
 }
 
+int orc_qr_solve(int n, const double *A, const double *b, double *x) {
+  return qr_solve(n, C(A), C(b), C(x));
+}
+
 int orc_gmres(int n, const double *S, const double *b, double *x, double tol, int maxit,
               int restarts, int *iters, double *relres) {
   return gmres(n, C(S), C(b), C(x), tol, maxit, restarts, iters, relres);
@@ -2102,7 +2178,7 @@ void orc_matvec(int rows, int cols, const double *A, const double *x, double *y)
 }
 
 // One full wavelength-solve (the unit the CPU baseline times): source vector,
-// FF assembly, solve (0 = LU, 1 = GMRES), internal coefficients, cross
+// FF assembly, solve (0 = LU, 1 = GMRES, 2 = column-pivoted QR), internal coefficients, cross
 // sections. X_sca / X_int may be null.
 int orc_wavelength_solve(void *h, int method, double tol, int maxit, int restarts, double *xsec,
                          double *X_sca, double *X_int, int *iters) {
@@ -2115,6 +2191,9 @@ int orc_wavelength_solve(void *h, int method, double tol, int maxit, int restart
     int rc;
     if(method == 0) {
       rc = lu_solve(n, S.data(), Q.data(), X.data());
+      *iters = 0;
+    } else if(method == 2) {
+      rc = qr_solve(n, S.data(), Q.data(), X.data());
       *iters = 0;
     } else {
       double rr;

@@ -325,7 +325,7 @@ class Problem:
         xs = np.zeros(self.n, np.complex128)
         xi = np.zeros(self.n, np.complex128)
         it = C.c_int(0)
-        rc = lib().orc_wavelength_solve(self.h, 0 if method == "lu" else 1, tol, maxit, restarts,
+        rc = lib().orc_wavelength_solve(self.h, {"lu": 0, "gmres": 1, "qr": 2}[method], tol, maxit, restarts,
                                         _p(xsec), _p(xs), _p(xi), C.byref(it))
         if rc < 0:
             raise RuntimeError(lib().orc_last_error().decode())
@@ -380,6 +380,17 @@ def lu_solve(A, b):
     rc = lib().orc_lu_solve(A.shape[0], _p(A), _p(b), _p(x))
     if rc:
         raise RuntimeError(f"singular matrix at column {rc}")
+    return x
+
+
+def qr_solve(A, b):
+    """Column-pivoted Householder QR solve (the serial PreconditionedMatrix::solve role)."""
+    A = np.asfortranarray(A, dtype=np.complex128)
+    b = _c(b)
+    x = np.zeros_like(b)
+    rc = lib().orc_qr_solve(A.shape[0], _p(A), _p(b), _p(x))
+    if rc:
+        raise RuntimeError(f"rank-deficient matrix at column {rc}")
     return x
 
 

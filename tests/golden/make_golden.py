@@ -2,7 +2,9 @@
 the reference tree, so the oracle can route its Bessel layer through the
 reference's own AMOS build in oracle/_ref).
 
-    python tests/golden/make_golden.py
+    OPTIMET_REFERENCE=<OPTIMET source tree> python tests/golden/make_golden.py [c1]
+
+(`c1` writes only the full-size C1 fixture, a few minutes of host work.)
 
 Each fixture is an .npz holding the inputs (cluster description) and the
 oracle's outputs computed with the reference's AMOS Bessel arithmetic. The GPU
@@ -137,10 +139,58 @@ def bessel_table():
     np.savez_compressed(os.path.join(HERE, "bessel_amos.npz"), z=zs, J=J, dJ=dJ, H=Hk, dH=dH)
 
 
+def make_c1():
+    """c1.npz: the C1 configuration at full size (bench.py's seeded N = 100
+    cluster, nMax = 8, 16,000 unknowns, metal-like spheres in water), solved by
+    the oracle's GMRES to a relative residual of 1e-13 on its own assembled S,
+    once through each Bessel route: the reference's AMOS (`_amos`) and the
+    oracle's recurrences (`_rec`, the route the GPU kernels also take). Near
+    field at 2,048 points of the C1 grid (256 x 256 x 2 over [-1, 1] um^2 at
+    z = +-0.1 nm), 64 of them inside spheres."""
+    sys.path.insert(0, ROOT)
+    import bench
+    w = bench.WORKLOADS["c1"]
+    xyz, rad = bench.cluster(w)
+    cl = O.Cluster(xyz=xyz, radius=rad, eps=complex(w["index"]) ** 2, nmax=w["nmax"],
+                   wavelength=w["lam"], bg_eps=complex(w["host"]) ** 2)
+    grid = O.grid_points([-1000 * nm, 1000 * nm, 256, -1000 * nm, 1000 * nm, 256, -0.1 * nm, 0.1 * nm, 2])
+    inside = np.zeros(len(grid), bool)
+    for c, r in zip(xyz, rad):
+        inside |= np.linalg.norm(grid - c, axis=1) <= r
+    rng = np.random.default_rng(2026)
+    pick = np.concatenate([rng.choice(np.nonzero(inside)[0], 64, replace=False),
+                           rng.choice(np.nonzero(~inside)[0], 2048 - 64, replace=False)])
+    pts = grid[np.sort(pick)]
+    out = {}
+    for route, amos in (("rec", False), ("amos", True)):
+        if not O.use_amos(amos):
+            raise SystemExit("the reference's AMOS build (oracle/_ref) is required")
+        pr = O.Problem(cl)
+        S = pr.scattering_matrix()
+        Q = pr.source_vector()
+        X, it, rr = O.gmres(S, Q, tol=1e-13, maxit=400, restarts=6)
+        del S
+        Xi = pr.internal(X)
+        E, H = pr.near_field(X, Xi, pts)
+        out.update({f"X_sca_{route}": X, f"xsec_{route}": pr.cross_sections(X), f"E_{route}": E,
+                    f"H_{route}": H, f"Q_{route}": Q, f"gmres_{route}": np.array([it, rr])})
+        print("c1", route, "iterations", it, "residual", rr, "xsec", out[f"xsec_{route}"])
+    O.use_amos(False)
+    np.savez_compressed(
+        os.path.join(HERE, "c1.npz"), **out,
+        xyz=cl.xyz, radius=cl.radius, eps=cl.eps, mu=cl.mu, eps_sh=cl.eps_sh,
+        bg=np.array([cl.bg_eps, cl.bg_mu], np.complex128), nmax=cl.nmax,
+        wavelength=cl.wavelength, angles=np.array([cl.theta, cl.phi]),
+        pol=np.array([cl.e_theta, cl.e_phi], np.complex128), points=pts, inside=inside[np.sort(pick)])
+
+
 def main():
     O.build(ref=True)
     if not O.use_amos(True):
         raise SystemExit("the reference's AMOS build (oracle/_ref) is required")
+    if sys.argv[1:] == ["c1"]:
+        make_c1()
+        return
     bessel_table()
     for name, cl in cases().items():
         make(name, cl)

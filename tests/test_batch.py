@@ -3,7 +3,7 @@ vectors of the oracle and with the single-request entry points, a request's
 results are bitwise the same alone and in any batch, and failures stay with
 the request that caused them.
 
-Tolerances: the plain form (complex128 GMRES to 1e-13) within 5e-10 of the
+Tolerances: the plain form (complex128 GMRES to 1e-13) within 1e-10 of the
 golden cross sections, as the single-request entry point; both forms against
 the single-request FP64 path within 1e-10 (plain) and 1e-6 (precision form)."""
 import numpy as np
@@ -70,9 +70,9 @@ def test_golden_vectors_through_the_batch(G, ctx, oracle):
     res = G.batch_solve(ctx, reqs)
     for name, g, r in zip(names, gs, res):
         assert r["status"] == G.OK, name
-        assert np.max(np.abs(r["xsec"] - g["xsec"]) / np.abs(g["xsec"])) < 5e-10, name
+        assert np.max(np.abs(r["xsec"] - g["xsec"]) / np.abs(g["xsec"])) < 1e-10, name
         if "xsec_sh" in g.files:
-            assert np.max(np.abs(r["xsec_sh"] - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10, name
+            assert np.max(np.abs(r["xsec_sh"] - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 1e-10, name
 
 
 def test_plain_batch_matches_single_requests(G, ctx):

@@ -58,4 +58,4 @@ def test_c0_through_the_cpp_interface(tmp_path):
     assert run.returncode == 0, run.stderr
     out = run.stdout
     xsec = np.array([float(v) for v in next(l for l in out.splitlines() if l.startswith("xsec")).split()[1:]])
-    assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 5e-10
+    assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 1e-10

@@ -88,8 +88,11 @@ def test_fixture_pipeline(G, ctx, oracle, name):
     xsec = pr.cross_sections()
     xo_sec = pr_o.cross_sections(xo)
     assert np.max(np.abs(xsec - xo_sec) / np.abs(xo_sec)) < 1e-10, (xsec, xo_sec)
-    # golden fixture (reference AMOS Bessel arithmetic), see test_oracle for the 5e-10
-    assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 5e-10
+    # golden fixture (the reference's AMOS Bessel arithmetic): the oracle's own
+    # route sits 4e-15 to 2e-14 from it (test_oracle), so the GPU is held to
+    # the same 1e-10 as against the oracle
+    assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 1e-10
+    assert rel(xs, g["X_sca"]) < 1e-10
     # near field at the fixture's points, including one interior point
     E, H = pr.near_field(g["points"])
     Eo, Ho = pr_o.near_field(xo, pr_o.internal(xo), g["points"])
@@ -221,11 +224,11 @@ def test_sh_pipeline(G, ctx, oracle, name, method):
     xs = pr.sh_cross_sections()
     xso = pr_o.sh_cross_sections(tab, xio, Xso, Xiso)
     assert np.max(np.abs(xs - xso) / np.abs(xso)) < 1e-10
-    assert np.max(np.abs(xs - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10
+    assert np.max(np.abs(xs - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 1e-10
     E, H = pr.near_field_sh(g["points"])
     Eo, Ho = pr_o.near_field_sh(tab, xio, Xso, Xiso, g["points"])
     assert rel(E, Eo) < 1e-10 and rel(H, Ho) < 1e-10
-    assert rel(E, g["E_sh"]) < 5e-10 and rel(H, g["H_sh"]) < 5e-10
+    assert rel(E, g["E_sh"]) < 1e-10 and rel(H, g["H_sh"]) < 1e-10
 
 
 def test_wavelength_solve_sh_entry_point(G, ctx, oracle):
@@ -234,8 +237,8 @@ def test_wavelength_solve_sh_entry_point(G, ctx, oracle):
     sp, bg, wave = gpu_inputs(G, cl)
     wave.sh = 1
     xsec, xsh, st = G.wavelength_solve_sh(ctx, sp, bg, wave, G.options(G.SOLVE_LU))
-    assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 5e-10
-    assert np.max(np.abs(xsh - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 5e-10
+    assert np.max(np.abs(xsec - g["xsec"]) / np.abs(g["xsec"])) < 1e-10
+    assert np.max(np.abs(xsh - g["xsec_sh"]) / np.abs(g["xsec_sh"])) < 1e-10
 
 
 @pytest.mark.parametrize("nmax", [10, 14, 15])
