@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kBT) k_b_resid(const Slot *st, const int4 *til
                                                 const double2 *x, long np, int nsm, double2 *part,
                                                 unsigned long long *next) {
   constexpr bool kDF = std::is_same<M, float2>::value;
-  typedef typename std::conditional<kDF, float4, double2>::type XS;
+  typedef typename std::conditional<kDF, DFX, double2>::type XS;
   __shared__ XS xs[kBCols];
   __shared__ int tile;
   const int ntiles = ctl->ntiles;

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part_df(const float2 *S, 
                                                                const double2 *x, double2 *part,
                                                                int row_tiles, long tiles,
                                                                unsigned long long *next, int cols) {
-  __shared__ float4 xs[kMvCols];
+  __shared__ DFX xs[kMvCols];
   __shared__ long tile;
   for(;;) {
     __syncthreads();
