@@ -1102,6 +1102,44 @@ def assemble_arm(args, w):
             "written_GB": 8.0 * n * n / 1e9, "written_GBps": 8.0 * n * n / 1e6 / per}
 
 
+def spawn_ranks(n):
+    """`bench.py --gpus N` without a launcher: start N copies of this command,
+    one per GPU, with RANK / LOCAL_RANK / WORLD_SIZE and a local rendezvous
+    (what `torch.distributed.run --nproc-per-node N` sets); rank 0 prints the
+    line. Returns the largest exit code."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__)] + sys.argv[1:], env=env))
+    return max(p.wait() for p in procs)
+
+
+def dry_arm(args):
+    """The multi-rank plumbing without GPU work (gloo): rank r reports r + 1
+    units in 0.5 (r + 1) seconds; the line aggregates them as the real arms do
+    (summed units over the slowest rank's time)."""
+    import torch.distributed as dist
+    rank, world, _ = dist_env()
+    if world > 1:
+        dist.init_process_group("gloo")
+    units, seconds = rank + 1, 0.5 * (rank + 1)
+    t = max_over_ranks([seconds], world)[0]
+    value = replica_value(units, seconds, world)
+    if world > 1:
+        dist.destroy_process_group()
+    if rank != 0:
+        return None
+    return {"metric": "dry run (no GPU work)", "value": value, "unit": "units/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "none", "data": "none",
+            "config": {"workload": "dry"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1129,8 +1167,16 @@ def main():
     ap.add_argument("--no-server", action="store_true", help="c3: skip the server comparison")
     ap.add_argument("--c3-profile", action="store_true",
                     help="c3: only the small batched case that the ncu captures use")
+    ap.add_argument("--dry", action="store_true", help="multi-rank plumbing only (gloo, no GPU work)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(spawn_ranks(args.gpus))
+    if args.dry:
+        out = dry_arm(args)
+        if out is not None:
+            print(json.dumps(out))
+        return
     if args.workload == "c0":
         out = c0_arm(args) if args.impl != "reference" else {"impl": "reference", **c0_cpu(1000)}
     elif args.workload == "c1full":

@@ -220,6 +220,20 @@ int om_solve_rhs(om_problem *pr, int harmonic, const om_solve_options *opts, con
  *   on the GPU, from any context on the same device, race. */
 int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve_options *opts,
                          const double *b, double *x, om_solve_stats *stats);
+/* Block rows of S for a solve sharded over several GPUs: the rows of spheres
+ * sphere0 .. sphere1 - 1 (complex128, 2P (sphere1 - sphere0) x n, kept on the
+ * device in place of a previous row block). The role of one MPI rank's rows
+ * in the reference's distributed product (matvec_parallel,
+ * PreconditionedMatrix.cpp:989-1054, rank r owning spheres gran1 .. gran2 - 1,
+ * :1001-1007). Synchronous. */
+int om_assemble_rows(om_problem *pr, int harmonic, int sphere0, int sphere1);
+/* y = S_rows x for the row block of om_assemble_rows: x is n complex128 values
+ * and y 2P (sphere1 - sphere0) values, both in DEVICE memory of the context's
+ * GPU (e.g. tensors of the framework that runs the collective). The partial
+ * product one rank contributes before the all-gather of the full vector
+ * (MPI_Gatherv + MPI_Bcast, PreconditionedMatrix.cpp:1044-1051). Each row's sum
+ * is formed in an order that does not depend on the row split. Synchronous. */
+int om_matvec_rows(om_problem *pr, int harmonic, const double *x, double *y);
 /* Scattered and internal coefficients (n each; either may be NULL). */
 int om_get_coefficients(om_problem *pr, double *X_sca, double *X_int);
 /* Result::getExtinctionCrossSection, getScatteringCrossSection,

@@ -126,6 +126,8 @@ def lib():
         L.om_solve_rhs.argtypes = [vp, C.c_int, C.POINTER(SolveOptions), _dp, _dp,
                                    C.POINTER(SolveStats)]
         L.om_get_coefficients.argtypes = [vp, _dp, _dp]
+        L.om_assemble_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.om_matvec_rows.argtypes = [vp, C.c_int, vp, vp]
         L.om_cross_sections.argtypes = [vp, _dp]
         L.om_near_field.argtypes = [vp, _dp, C.c_int, _dp, _dp]
         L.om_near_field_sh.argtypes = [vp, _dp, C.c_int, _dp, _dp]
@@ -323,6 +325,17 @@ class Problem:
         self.ctx.check(lib().om_solve_rhs(self.h, harmonic, C.byref(opts or options()), _p(b),
                                           _p(x), C.byref(st)))
         return x, st
+
+    def assemble_rows(self, sphere0, sphere1, harmonic=FF):
+        """Block rows of S for spheres sphere0 .. sphere1 - 1 (complex128, on
+        the device; om_assemble_rows)."""
+        self.ctx.check(lib().om_assemble_rows(self.h, harmonic, int(sphere0), int(sphere1)))
+
+    def matvec_rows(self, x_device_ptr, y_device_ptr, harmonic=FF):
+        """y = S_rows x with x (n) and y (the block's rows) complex128 device
+        buffers given by address (om_matvec_rows)."""
+        self.ctx.check(lib().om_matvec_rows(self.h, harmonic, C.c_void_p(x_device_ptr),
+                                            C.c_void_p(y_device_ptr)))
 
     def coefficients(self):
         xs = np.zeros(self.n, np.complex128)

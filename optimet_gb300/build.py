@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboptimet_gpu.so")
 SOURCES = ["translate.cu", "field.cu", "solve.cu", "sh.cu", "capi.cu", "serve.cu", "tc_gemm.cu", "aca.cu", "tma_matvec.cu",
-           "batch.cu", "assemble_rot.cu"]
+           "batch.cu", "assemble_rot.cu", "shard.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-pthread", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]

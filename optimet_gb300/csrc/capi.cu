@@ -163,6 +163,9 @@ void free_problem(om_problem *pr) {
   dev_free(ctx, pr->d_K1, n);
   dev_free(ctx, pr->d_Xsh, n);
   dev_free(ctx, pr->d_Xish, n);
+  if(pr->d_Srows)
+    om::dev_release(ctx, pr->d_Srows, pr->rows_bytes);
+  pr->d_Srows = nullptr;
   dev_free(ctx, pr->d_wsh, N * P);
   dev_free(ctx, pr->d_acs, N * P);
   for(int h = 0; h < 2; ++h) {

@@ -171,6 +171,9 @@ struct om_problem {
   double *d_wsca = nullptr;   // N x P: sum_p |T^reg_pq|^2 (Result.cpp:563-631)
   om::zd *d_Q = nullptr;      // n
   void *d_S[2] = {nullptr, nullptr};    // complex128 matrix per harmonic (plain form)
+  void *d_Srows = nullptr;              // a block of sphere rows (om_assemble_rows), complex128
+  int rows0 = 0, rows1 = 0, rows_harmonic = -1;
+  size_t rows_bytes = 0;
   void *d_S32[2] = {nullptr, nullptr};  // complex64 matrix per harmonic (precision form)
   int S_prec[2] = {-1, -1};             // which of the two holds the current assembly
   om::zd *d_X = nullptr, *d_Xint = nullptr;
@@ -207,6 +210,9 @@ void launch_assemble(om_problem *pr, int harmonic, int precision);
 void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, double2 *scratch);
 // batched assembly: matrix e of the table d_mats (device) is assembled by CTAs
 // e per_mat .. (e + 1) per_mat - 1; per_mat >= N (N + 1) / 2 for every entry
+// the block rows of spheres sphere0 .. sphere1 - 1 of S (complex128), into a
+// (2P (sphere1 - sphere0)) x 2PN column-major block
+void launch_assemble_rows(om_problem *pr, int harmonic, int sphere0, int sphere1, double2 *Srows);
 void launch_assemble_batch(om_context *ctx, int nmax, int precision, const BatchMat *d_mats,
                            int nmats, int per_mat, cudaStream_t stream);
 void launch_source(om_problem *pr);

@@ -513,6 +513,10 @@ struct AssembleArgs {
   // N, waveK, ld and S
   const BatchMat *batch;
   int per_mat;
+  // row-block mode (row1 > row0): the rows of spheres row0 .. row1 - 1 only,
+  // into a (2P (row1 - row0)) x 2PN column-major block (ld = its rows);
+  // CTA b handles the ordered pair (row0 + b / N, b % N)
+  int row0, row1;
 };
 
 template <typename O> __device__ __forceinline__ void put_out(O *S, size_t at, double re, double im);
@@ -560,23 +564,38 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
   }
   const long npairs = (long)N * (N - 1) / 2;
   const int P = y.P;
-  if(!a.scratch && b >= npairs) {
-    const int i = (int)(b - npairs);
-    const long x0 = 2L * P * i;
-    for(int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) {
-      int c = idx / (2 * P), r = idx - c * 2 * P;
-      put_out<OutT>(S, (x0 + c) * ld + x0 + r, r == c ? 1.0 : 0.0, 0.0);
+  const bool rowblk = a.row1 > a.row0;
+  int i, j;
+  if(rowblk) {
+    i = a.row0 + (int)(b / N);
+    j = (int)(b % N);
+    if(i == j) {
+      const long r0 = 2L * P * (i - a.row0), c0 = 2L * P * i;
+      for(int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) {
+        int c = idx / (2 * P), r = idx - c * 2 * P;
+        put_out<OutT>(S, (c0 + c) * ld + r0 + r, r == c ? 1.0 : 0.0, 0.0);
+      }
+      return;
     }
-    return;
+  } else {
+    if(!a.scratch && b >= npairs) {
+      const int d = (int)(b - npairs);
+      const long x0 = 2L * P * d;
+      for(int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) {
+        int c = idx / (2 * P), r = idx - c * 2 * P;
+        put_out<OutT>(S, (x0 + c) * ld + x0 + r, r == c ? 1.0 : 0.0, 0.0);
+      }
+      return;
+    }
+    // b -> (i, j), i < j: b = j (j - 1) / 2 + i
+    j = (int)((1.0 + sqrt(1.0 + 8.0 * (double)b)) * 0.5);
+    while((long)j * (j - 1) / 2 > b)
+      --j;
+    while((long)(j + 1) * j / 2 <= b)
+      ++j;
+    i = (int)(b - (long)j * (j - 1) / 2);
   }
-  // b -> (i, j), i < j: b = j (j - 1) / 2 + i
-  int j = (int)((1.0 + sqrt(1.0 + 8.0 * (double)b)) * 0.5);
-  while((long)j * (j - 1) / 2 > b)
-    --j;
-  while((long)(j + 1) * j / 2 <= b)
-    ++j;
-  const int i = (int)(b - (long)j * (j - 1) / 2);
-  const long xi = a.scratch ? 0 : 2L * P * i, xj = a.scratch ? 0 : 2L * P * j;
+  const long xi = a.scratch ? 0 : 2L * P * (rowblk ? i - a.row0 : i), xj = a.scratch ? 0 : 2L * P * j;
   OutT *Sij = S, *Sji = S;
   if(a.scratch) {
     Sij = S + (size_t)(2 * blockIdx.x) * (4L * P * P);
@@ -639,6 +658,8 @@ __global__ void __launch_bounds__(256) k_assemble(AssembleArgs a, Layout y,
       put_out<OutT>(Sij, col_tm + p, v.re, v.im);
       v = neg_mul(tmi, B);
       put_out<OutT>(Sij, col_te + P + p, v.re, v.im);
+      if(rowblk)
+        continue;
       // S_ji, translation r_j - r_i
       if((n + l) & 1) {
         A.re = -A.re;
@@ -1047,7 +1068,7 @@ void launch_assemble(om_problem *pr, int harmonic, int precision) {
   }
   const CoefTables &ct = coef_tables(ctx, pr->nmax);
   Layout y = make_layout(pr->nmax, smem_limit(), mixed);
-  AssembleArgs a;
+  AssembleArgs a{};
   a.cart = pr->d_cart;
   a.T = harmonic == OM_SH ? pr->d_Tsh : pr->d_T;
   a.rec = ct.rec;
@@ -1086,7 +1107,7 @@ void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, 
   om_context *ctx = pr->ctx;
   const CoefTables &ct = coef_tables(ctx, pr->nmax);
   Layout y = make_layout(pr->nmax, smem_limit(), false);
-  AssembleArgs a;
+  AssembleArgs a{};
   a.cart = pr->d_cart;
   a.T = harmonic == OM_SH ? pr->d_Tsh : pr->d_T;
   a.rec = ct.rec;
@@ -1104,6 +1125,30 @@ void launch_assemble_pairs(om_problem *pr, int harmonic, long pair0, int count, 
   fill_chunks(a, y);
   set_smem(k_assemble<false>, y.bytes, ctx->carve_asm);
   k_assemble<false><<<count, 256, y.bytes, ctx->stream>>>(a, y, scratch);
+  ctx->last_launches++;
+}
+
+void launch_assemble_rows(om_problem *pr, int harmonic, int sphere0, int sphere1, double2 *Srows) {
+  om_context *ctx = pr->ctx;
+  const CoefTables &ct = coef_tables(ctx, pr->nmax);
+  Layout y = make_layout(pr->nmax, smem_limit(), false);
+  AssembleArgs a{};
+  a.cart = pr->d_cart;
+  a.T = harmonic == OM_SH ? pr->d_Tsh : pr->d_T;
+  a.rec = ct.rec;
+  a.qf = ct.qf;
+  a.pf = ct.pf;
+  a.legc = ct.legc;
+  a.N = pr->N;
+  cplx k = harmonic == OM_SH ? 2.0 * pr->waveK : pr->waveK;
+  a.waveK = mk(k.real(), k.imag());
+  a.ld = 2L * pr->P * (sphere1 - sphere0);
+  a.per_mat = 1;
+  a.row0 = sphere0;
+  a.row1 = sphere1;
+  fill_chunks(a, y);
+  set_smem(k_assemble<false>, y.bytes, ctx->carve_asm);
+  k_assemble<false><<<(unsigned)((long)(sphere1 - sphere0) * pr->N), 256, y.bytes, ctx->stream>>>(a, y, Srows);
   ctx->last_launches++;
 }
 

@@ -43,3 +43,25 @@ def test_replica_aggregation_two_gloo_ranks():
     for rank, times, value in res:
         assert times == [2.0, 10.0]          # MAX over ranks
         assert value == pytest.approx(5.0 / 2.0)  # (2 + 3) solves / slowest 2 s
+
+
+@pytest.mark.parametrize("n,value", [(2, 3.0), (3, 4.0)])
+def test_bench_spawns_its_ranks(n, value):
+    """`bench.py --gpus N` with no launcher starts N ranks itself (RANK,
+    LOCAL_RANK, WORLD_SIZE, local rendezvous); the dry mode runs the ranks'
+    gloo aggregation without GPU work: rank r reports r + 1 units in 0.5 (r + 1)
+    seconds, so the line carries (1 + .. + N) units over the slowest N / 2 s."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", str(n), "--dry"],
+                       capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1  # rank 0 alone prints
+    out = json.loads(lines[0])
+    assert out["n_gpus"] == n
+    assert out["value"] == pytest.approx(value)
+    assert out["ms_per_step"] == pytest.approx(500.0 * n)
