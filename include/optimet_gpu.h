@@ -217,7 +217,8 @@ int om_solve_rhs(om_problem *pr, int harmonic, const om_solve_options *opts, con
  *   before any stream capture on that device.
  *   All calls share the array and it keeps the previous call's contents (the
  *   solution vector is cleared at the start of every call); calls that overlap
- *   on the GPU, from any context on the same device, race. */
+ *   on the GPU, from any context on the same device, race.
+ *   stats->seconds is the host wall-clock time of the call, copies included. */
 int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve_options *opts,
                          const double *b, double *x, om_solve_stats *stats);
 /* Block rows of S for a solve sharded over several GPUs: the rows of spheres

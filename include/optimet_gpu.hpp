@@ -15,7 +15,9 @@
 #ifndef OPTIMET_GPU_HPP
 #define OPTIMET_GPU_HPP
 
+#include <algorithm>
 #include <array>
+#include <cmath>
 #include <complex>
 #include <stdexcept>
 #include <string>
@@ -58,11 +60,88 @@ private:
   om_context *ctx_ = nullptr;
 };
 
+// How the reference was built, which decides its solver (solver::factory,
+// Solver.cpp:30-54): Serial (no MPI) -> PreconditionedMatrix; Scalapack (MPI
+// with ScaLAPACK, no Belos) -> Scalapack; Belos (MPI with Belos and
+// ScaLAPACK) -> by the parameter list's "Solver": "eigen" ->
+// PreconditionedMatrix, "scalapack" -> Scalapack, otherwise MatrixBelos.
+enum class Build { Serial, Scalapack, Belos };
+
+// The run's solver inputs: the build, the <ParameterList> entries the
+// reference reads (read_parameter_list, Reader.cpp:909-921; defaults of
+// gmres_linear_system, LinearSystemSolver.hpp:149-160) and the <ACA
+// compression="yes"> flag (Geometry::ACA_cond_).
+struct SolverChoice {
+  Build build = Build::Serial;
+  std::string solver = "GMRES";   // "Solver": "GMRES" | "scalapack" | "eigen"
+  double tolerance = 1e-10;       // "Convergence Tolerance"
+  int max_iterations = 4000;      // "Maximum Iterations"
+  int num_blocks = 1000;          // "Num Blocks" (the restart length)
+  bool aca = false;
+};
+
+// What the GPU runs for a SolverChoice: the matrix form and the solve.
+//  - direct solvers (PreconditionedMatrix's colPivHouseholderQr,
+//    PreconditionedMatrixSolver.h:45-79; Scalapack's pzgesv,
+//    ScalapackSolver.cpp:54-130): OM_C128 with OM_SOLVE_LU;
+//  - MatrixBelos (MatrixBelosSolver.cpp:26-104): OM_C128 with OM_SOLVE_GMRES,
+//    restart length "Num Blocks" (at most 1000), "Maximum Iterations" in total,
+//    "Convergence Tolerance";
+//  - with ACA each class runs Gmres_Zcomp on the compressed operator with its
+//    own constants (tolerance, iterations per cycle, cycles):
+//    PreconditionedMatrix 1e-6, 240, 2 (PreconditionedMatrixSolver.h:48-51),
+//    Scalapack 1e-7, 250, 3 (ScalapackSolver.cpp:58-60), MatrixBelos 1e-6,
+//    340, 1 (MatrixBelosSolver.cpp:35-37): OM_ACA with OM_SOLVE_GMRES.
+struct Plan {
+  int precision;
+  om_solve_options opts;
+};
+
+inline Plan plan(const SolverChoice &c) {
+  enum { PM, SC, MB } role = PM;
+  if(c.build == Build::Scalapack)
+    role = SC;
+  else if(c.build == Build::Belos)
+    role = c.solver == "eigen" ? PM : (c.solver == "scalapack" ? SC : MB);
+  Plan p{OM_C128, om_solve_options{OM_SOLVE_LU, 0, 0, 0, 0.0, 0.0}};
+  if(c.aca) {
+    p.precision = OM_ACA;
+    p.opts.method = OM_SOLVE_GMRES;
+    if(role == PM)
+      p.opts = om_solve_options{OM_SOLVE_GMRES, 240, 2, 0, 1e-6, 0.0};
+    else if(role == SC)
+      p.opts = om_solve_options{OM_SOLVE_GMRES, 250, 3, 0, 1e-7, 0.0};
+    else
+      p.opts = om_solve_options{OM_SOLVE_GMRES, 340, 1, 0, 1e-6, 0.0};
+    return p;
+  }
+  if(role != MB)
+    return p;
+  const int m = std::max(1, std::min(c.num_blocks, 1000));
+  p.opts = om_solve_options{OM_SOLVE_GMRES, m, std::max(1, (c.max_iterations + m - 1) / m), 0, c.tolerance, 0.0};
+  return p;
+}
+
+// (E_theta, E_phi) of a plane wave from the Cartesian field the reference's
+// Excitation keeps (Excitation::Einc = Tools::toProjection of (0, E_theta,
+// E_phi), Reader.cpp:818-827): Tools::fromProjection's theta and phi rows
+// (Tools.cpp:290-301) at the propagation direction (theta, phi).
+inline std::pair<cplx, cplx> polarisation(double theta, double phi, cplx ex, cplx ey, cplx ez) {
+  const double st = std::sin(theta), ct = std::cos(theta), sp = std::sin(phi), cp = std::cos(phi);
+  return {ct * cp * ex + ct * sp * ey - st * ez, cp * ey - sp * ex};
+}
+
 // A cluster of spheres, a background medium and a plane wave, with the
-// solver options and the precision form (OM_C128 plain FP64, OM_C64 the
-// precision form with OM_SOLVE_FGMRES_MIXED or OM_SOLVE_LU_MIXED).
+// solver options and the matrix form (OM_C128 plain FP64; OM_ACA the
+// compressed FP64 operator, GMRES only; OM_C64 the precision form with
+// OM_SOLVE_FGMRES_MIXED or OM_SOLVE_LU_MIXED).
 class Solver {
 public:
+  // the solver the reference would pick for `choice` (plan())
+  Solver(Context &ctx, std::vector<om_sphere> spheres, om_medium background, om_plane_wave wave,
+         const SolverChoice &choice)
+      : Solver(ctx, std::move(spheres), background, wave, plan(choice).opts, plan(choice).precision) {}
+
   Solver(Context &ctx, std::vector<om_sphere> spheres, om_medium background, om_plane_wave wave,
          om_solve_options opts, int precision = OM_C128)
       : ctx_(ctx), spheres_(std::move(spheres)), bg_(background), wave_(wave), opts_(opts),

@@ -280,8 +280,8 @@ void batch_release(om_context *ctx);
 
 // tma_matvec.cu: complex64 matvec with TMA-staged matrix tiles; false when the
 // tensor map cannot be encoded
-bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const void *x, void *part, bool df,
-                       int row_tiles, long tiles, int cols, unsigned grid);
+bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *part, int row_tiles,
+                       long tiles, int cols, unsigned grid);
 
 // capi.cu: stream-ordered device memory counted against the context budget
 int dev_malloc(om_context *ctx, void **p, size_t bytes);

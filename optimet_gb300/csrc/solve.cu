@@ -285,7 +285,7 @@ void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, cons
   bool done = false;
   if constexpr(sizeof(M) == sizeof(float2) && !df)
     if(ctx->mv_tma)
-      done = launch_matvec_tma(ctx, (const float2 *)S, n, x, part, false, row_tiles, tiles,
+      done = launch_matvec_tma(ctx, (const float2 *)S, n, (const float2 *)x, (float2 *)part, row_tiles, tiles,
                                mv_cols(ctx, n), grid);
   if(done) {
   } else if constexpr(df)
@@ -1707,6 +1707,7 @@ extern "C" int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve
   char *ws = static_cast<char *>(noalloc_scratch(ctx));
   if(!ws)
     return OM_ERR_CUDA;
+  const auto t0 = std::chrono::steady_clock::now();
   double2 *db = reinterpret_cast<double2 *>(ws);
   double2 *dx = reinterpret_cast<double2 *>(ws + round(z * n));
   char *rest = ws + 2 * round(z * n);
@@ -1722,6 +1723,8 @@ extern "C" int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve
                                     m, opts->restarts, rest, &it, &rr);
   cudaMemcpyAsync(x, dx, z * n, cudaMemcpyDeviceToHost, ctx->stream);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if(e == cudaSuccess)
+    e = cudaGetLastError();  // launch-configuration errors, which the synchronisation does not return
   if(e != cudaSuccess) {
     ctx->err = std::string("om_solve_rhs_noalloc: ") + cudaGetErrorString(e);
     return OM_ERR_CUDA;
@@ -1730,7 +1733,7 @@ extern "C" int om_solve_rhs_noalloc(om_problem *pr, int harmonic, const om_solve
     stats->iterations = it;
     stats->inner_iterations = 0;
     stats->rel_residual = rr;
-    stats->seconds = 0.0;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
   if(rc == OM_ERR_NOT_CONVERGED)
     ctx->err = "GMRES did not reach the requested tolerance";

@@ -1,6 +1,5 @@
-// Complex64 matrix-vector products with the matrix staged by the Tensor
-// Memory Accelerator: the GMRES matvecs of the precision form (the inner FP32
-// one and the compensated FP64-accurate residual one).
+// Complex64 matrix-vector product with the matrix staged by the Tensor
+// Memory Accelerator: the inner FP32 GMRES matvec of the precision form.
 //
 // Same decomposition as the plain kernels: tiles of 256 rows x `cols` columns
 // taken from a counter by a capped grid, x chunk in shared memory, one row
@@ -9,12 +8,15 @@
 // column-major matrix) through a 4-deep ring of shared-memory buffers, each
 // with an mbarrier that the TMA completes by transaction bytes. Thread 0
 // issues the copies; after all threads have consumed a buffer it refills it
-// with the stage four ahead. Waits are bounded (error flag, no hang). The
-// arithmetic and its order per thread are those of the plain kernels, so
-// the results are bitwise the same. The solver dispatches the complex64 x
-// complex64 variant; the compensated variant (kDF) measured slower than the
-// register-prefetching plain kernel (its FP32 work needs more resident warps
-// than the 144 KB of buffers leave) and is kept for the tuning experiments.
+// with the stage four ahead. The arithmetic and its order per thread are those
+// of the plain kernel, so the results are bitwise the same.
+//
+// Waits are bounded: every thread polls the stage's barrier a bounded number
+// of times and the CTA decides together (a barrier with an OR reduction)
+// whether the stage arrived. If not, thread 0 records the failure in the
+// error flag the solver reads back, waits (bounded again) for the stages it
+// has already issued so that no copy lands in this CTA's shared memory after
+// it exits, and the CTA stops taking tiles.
 #include <cuda.h>
 
 #include <mutex>
@@ -62,33 +64,13 @@ __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity) {
   return false;
 }
 
-struct DF {
-  float hi, lo;
-};
-__device__ __forceinline__ void df_add(DF &a, float p) {
-  const float s = a.hi + p;
-  const float bb = s - a.hi;
-  a.lo += (a.hi - (s - bb)) + (p - bb);
-  a.hi = s;
-}
-
-template <bool kDF> struct XT;
-template <> struct XT<false> { typedef float2 type; };
-template <> struct XT<true> { typedef float4 type; };
-
-// kDF = false: part = S x (complex64 x complex64, two alternating FP32
-// accumulators as k_matvec_part); kDF = true: the compensated product of
-// k_matvec_part_df (x split into hi + lo floats, TwoProduct / TwoSum).
-template <bool kDF>
 __global__ void __launch_bounds__(kTmaRows) k_matvec_tma(const __grid_constant__ CUtensorMap tm, long n,
-                                                      const typename std::conditional<kDF, double2, float2>::type *x,
-                                                      typename std::conditional<kDF, double2, float2>::type *part,
-                                                      int row_tiles, long tiles, unsigned long long *next,
-                                                      int cols, int *err) {
+                                                          const float2 *x, float2 *part, int row_tiles,
+                                                          long tiles, unsigned long long *next, int cols,
+                                                          int *err) {
   extern __shared__ __align__(128) unsigned char tsm_[];
   float2 *stage = reinterpret_cast<float2 *>(tsm_);  // [kTmaStages][kTmaStageCols][kTmaRows]
-  typename XT<kDF>::type *xs =
-      reinterpret_cast<typename XT<kDF>::type *>(tsm_ + kTmaStages * kStageBytes);
+  float2 *xs = reinterpret_cast<float2 *>(tsm_ + kTmaStages * kStageBytes);
   __shared__ __align__(8) uint64_t bar[kTmaStages];
   __shared__ long tile;
   __shared__ int fail;
@@ -121,86 +103,61 @@ __global__ void __launch_bounds__(kTmaRows) k_matvec_tma(const __grid_constant__
                  (int)(j0 + s * kTmaStageCols), &bar[s]);
       }
     }
-    for(long j = j0 + t; j < j1; j += kTmaRows) {
-      if constexpr(kDF) {
-        const double2 v = x[j];
-        const float hr = (float)v.x, hi = (float)v.y;
-        xs[j - j0] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
-      } else {
-        xs[j - j0] = x[j];
-      }
-    }
+    for(long j = j0 + t; j < j1; j += kTmaRows)
+      xs[j - j0] = x[j];
     __syncthreads();
-    // accumulators (the plain kernels' order: columns in groups of eight,
+    // accumulators (the plain kernel's order: columns in groups of eight,
     // alternating accumulators, a tail of fewer than eight into acc0)
     float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
-    DF re{0.f, 0.f}, im{0.f, 0.f};
-    float er = 0.f, ei = 0.f;
     const long full8 = j0 + ((j1 - j0) / 8) * 8;
     for(int s = 0; s < nst; ++s) {
       const int slot = s % kTmaStages;
-      if(!fail && !wait_phase(&bar[slot], (parity >> slot) & 1u)) {
-        fail = 1;
-        if(t == 0)
-          atomicExch(err, 1);
-      }
+      const bool arrived = wait_phase(&bar[slot], (parity >> slot) & 1u);
       parity ^= 1u << slot;
+      if(__syncthreads_or(!arrived)) {
+        if(t == 0) {
+          atomicExch(err, 1);
+          for(int q = s + 1; q < nst && q < s + kTmaStages; ++q) {  // issued, not yet waited for
+            const int sl = q % kTmaStages;
+            wait_phase(&bar[sl], (parity >> sl) & 1u);
+            parity ^= 1u << sl;
+          }
+          fail = 1;
+        }
+        break;
+      }
       const float2 *sb = stage + (size_t)slot * kTmaStageCols * kTmaRows;
       const long cb = j0 + (long)s * kTmaStageCols;
       const int ccount = (int)min((long)kTmaStageCols, j1 - cb);
-      if(i < n && !fail) {
+      if(i < n) {
         for(int c = 0; c < ccount; ++c) {
           const float2 a = sb[c * kTmaRows + t];
           const long j = cb + c;
-          if constexpr(kDF) {
-            const float4 v = xs[j - j0];
-            float p = __fmul_rn(a.x, v.x);
-            er += fmaf(a.x, v.x, -p);
-            df_add(re, p);
-            p = __fmul_rn(-a.y, v.y);
-            er += fmaf(-a.y, v.y, -p);
-            df_add(re, p);
-            er = fmaf(a.x, v.z, er);
-            er = fmaf(-a.y, v.w, er);
-            p = __fmul_rn(a.x, v.y);
-            ei += fmaf(a.x, v.y, -p);
-            df_add(im, p);
-            p = __fmul_rn(a.y, v.x);
-            ei += fmaf(a.y, v.x, -p);
-            df_add(im, p);
-            ei = fmaf(a.x, v.w, ei);
-            ei = fmaf(a.y, v.z, ei);
-          } else {
-            const float2 xv = xs[j - j0];
-            const bool alt = j < full8 && ((j - j0) & 1);
-            float2 acc = alt ? acc1 : acc0;
-            acc.x = fmaf(a.x, xv.x, acc.x);
-            acc.x = fmaf(-a.y, xv.y, acc.x);
-            acc.y = fmaf(a.x, xv.y, acc.y);
-            acc.y = fmaf(a.y, xv.x, acc.y);
-            if(alt)
-              acc1 = acc;
-            else
-              acc0 = acc;
-          }
+          const float2 xv = xs[j - j0];
+          const bool alt = j < full8 && ((j - j0) & 1);
+          float2 acc = alt ? acc1 : acc0;
+          acc.x = fmaf(a.x, xv.x, acc.x);
+          acc.x = fmaf(-a.y, xv.y, acc.x);
+          acc.y = fmaf(a.x, xv.y, acc.y);
+          acc.y = fmaf(a.y, xv.x, acc.y);
+          if(alt)
+            acc1 = acc;
+          else
+            acc0 = acc;
         }
       }
       __syncthreads();  // the buffer is free again
-      if(t == 0 && s + kTmaStages < nst && !fail) {
+      if(t == 0 && s + kTmaStages < nst) {
         arm(&bar[slot], kStageBytes);
         tma_load(stage + (size_t)slot * kTmaStageCols * kTmaRows, &tm, (int)(rt * kTmaRows),
                  (int)(j0 + (long)(s + kTmaStages) * kTmaStageCols), &bar[slot]);
       }
     }
+    __syncthreads();  // `fail` as thread 0 left it
     if(i < n && !fail) {
-      if constexpr(kDF) {
-        part[ct * n + i] = make_double2((double)re.hi + ((double)re.lo + (double)er),
-                                        (double)im.hi + ((double)im.lo + (double)ei));
-      } else {
-        acc0.x += acc1.x;
-        acc0.y += acc1.y;
-        part[ct * n + i] = acc0;
-      }
+      acc0.x += acc1.x;
+      acc0.y += acc1.y;
+      part[ct * n + i] = acc0;
     }
   }
 }
@@ -229,8 +186,8 @@ EncodeFn encode_fn() {
 
 // Launches the TMA matvec (false when the tensor map cannot be made: the
 // caller then runs the plain kernel).
-bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const void *x, void *part, bool df,
-                       int row_tiles, long tiles, int cols, unsigned grid) {
+bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *part, int row_tiles,
+                       long tiles, int cols, unsigned grid) {
   EncodeFn enc = encode_fn();
   if(!enc || (reinterpret_cast<uintptr_t>(S) & 15) || (n & 1))
     return false;
@@ -243,19 +200,10 @@ bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const void *x, 
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return false;
-  const size_t xbytes = (size_t)cols * (df ? sizeof(float4) : sizeof(float2));
-  const size_t smem = kTmaStages * kStageBytes + xbytes;
-  if(df) {
-    cudaFuncSetAttribute(k_matvec_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_matvec_tma<true><<<grid, kTmaRows, smem, ctx->stream>>>(
-        tm, n, (const double2 *)x, (double2 *)part, row_tiles, tiles, ctx->d_tile_counter, cols,
-        ctx->d_tma_err);
-  } else {
-    cudaFuncSetAttribute(k_matvec_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_matvec_tma<false><<<grid, kTmaRows, smem, ctx->stream>>>(
-        tm, n, (const float2 *)x, (float2 *)part, row_tiles, tiles, ctx->d_tile_counter, cols,
-        ctx->d_tma_err);
-  }
+  const size_t smem = kTmaStages * kStageBytes + (size_t)cols * sizeof(float2);
+  cudaFuncSetAttribute(k_matvec_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_matvec_tma<<<grid, kTmaRows, smem, ctx->stream>>>(tm, n, x, part, row_tiles, tiles, ctx->d_tile_counter,
+                                                      cols, ctx->d_tma_err);
   return true;
 }
 

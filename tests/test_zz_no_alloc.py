@@ -54,6 +54,24 @@ def test_no_alloc_solve_matches_allocating_solve():
         assert rc == G.OK, G.lib().om_context_last_error(ctx.h)
         assert st.rel_residual <= 1e-12
         assert rel(x, x_ref) < 1e-10
+    # independent of om_solve_rhs: the fixture's scattering coefficients
+    # (the oracle's solution, through the reference's AMOS Bessel route)
+    g = load_golden("metal5")
+    assert rel(x, g["X_sca"]) < 1e-10
+    # the complex64 matrix (the precision form's storage): the same GMRES over
+    # the compensated complex64 x complex128 product, against om_solve_rhs on
+    # that matrix; the complex64 rounding of S keeps it within 1e-6 of FP64
+    pr.assemble(G.FF, G.C64)
+    x64_ref, _ = pr.solve_rhs(b, G.FF, opts)
+    for _ in range(2):
+        x = np.zeros_like(b)
+        st = G.SolveStats()
+        rc = solve_noalloc(pr.h, G.FF, C.byref(opts), b.ctypes.data_as(dp), x.ctypes.data_as(dp),
+                           C.byref(st))
+        assert rc == G.OK, G.lib().om_context_last_error(ctx.h)
+        assert st.rel_residual <= 1e-12 and st.seconds > 0
+        assert rel(x, x64_ref) < 1e-10
+        assert rel(x, g["X_sca"]) < 1e-6
     # a request larger than the fixed array is refused before any GPU work
     big = G.options(G.SOLVE_GMRES, tol=1e-12, max_iter=200000, restarts=1)
     x = np.zeros_like(b)
