@@ -177,6 +177,63 @@ def _read_scatterer(node, nmax: int) -> Scatterer:
     return Scatterer(vR=vR, radius=radius, elmag=em, nMax=nmax)
 
 
+# The zincblende (GaAs) cell of the structure generators, in units of the
+# cell size: 14 large sites, then 4 small ones (Reader.cpp:209-213, 341-345).
+_ZB = ((1, 0, 0), (1, .5, .5), (.5, .5, 0), (.5, 0, .5), (0, .5, .5), (0, 1, 0), (.5, 1, .5), (1, 1, 1),
+       (.5, .5, 1), (0, 0, 1), (0, 0, 0), (1, 0, 1), (1, 1, 0), (0, 1, 1), (.75, .25, .25), (.25, .75, .25),
+       (.75, .75, .75), (.25, .25, .75))
+
+
+def _structure(st, nmax: int):
+    """The structure generators of read_structure (Reader.cpp:103-574): "cube"
+    (points^3 copies on a cubic lattice, a corner at the origin), "surface"
+    (points^2 in the xy plane), "GaAssurf" (No_cells^2 zincblende cells in the
+    xy plane; the 4 small sites have radius R / 2) and "GaAscube" (No_cells^3
+    cells; small radius R / 1.7). Sites shared with an earlier cell are not
+    repeated (the reference's X1 > 0 / Y1 > 0 / Z1 > 0 tests). The objects come
+    out in the reference's order: it writes each generated site (the origin
+    skipped in the zincblende ones) into the last object pushed and then pushes
+    a fresh copy of the prototype, so object k holds site k + 1 (k + 1-th
+    non-origin site) and the prototype with its own position and radius comes
+    last."""
+    kind = st.get("type")
+    props = st.find("properties")
+    proto = _read_scatterer(st.find("object"), nmax)
+    sites, radii = [], []
+    if kind in ("cube", "surface"):
+        no, d = int(props.get("points")), float(props.get("distance")) * FRNM_TO_M
+        layers = range(no) if kind == "cube" else [0]
+        for k in layers:
+            for j in range(no):
+                for i in range(no):
+                    sites.append((d * i, d * j, d * k))
+                    radii.append(proto.radius)
+        sites, radii = sites[1:], radii[1:]  # site 0 is the prototype's own slot
+    elif kind in ("GaAssurf", "GaAscube"):
+        no = int(props.get("No_cells"))
+        a = float(props.get("cell_size")) * FRNM_TO_M
+        R = proto.radius
+        small = R / 2.0 if kind == "GaAssurf" else R / 1.7
+        cell = [(a * x, a * y, a * z) for x, y, z in _ZB]
+        for t in (range(no) if kind == "GaAscube" else [0]):
+            for i in range(no):
+                for j in range(no):
+                    for k, (x, y, z) in enumerate(cell):
+                        if (i > 0 and x <= 0.0) or (j > 0 and y <= 0.0) or (t > 0 and z <= 0.0):
+                            continue
+                        p = (x + a * i if i else x, y + a * j if j else y, z + a * t if t else z)
+                        if p == (0.0, 0.0, 0.0):
+                            continue
+                        sites.append(p)
+                        radii.append(R if k < 14 else small)
+    else:
+        raise NotImplementedError(f"structure type {kind!r}")
+    out = [Scatterer(vR=np.array(p, dtype=float), radius=r, elmag=proto.elmag, nMax=nmax)
+           for p, r in zip(sites, radii)]
+    out.append(proto)
+    return out
+
+
 def simulation_input(source) -> Run:
     """Parse an Optimet3D case (path or XML text). The case file holds several
     top-level elements, so it is wrapped in one root before parsing."""
@@ -198,18 +255,8 @@ def simulation_input(source) -> Run:
     g = Geometry(ACA_cond=aca)
     st = geo.find("structure")
     if st is not None:
-        if st.get("type") != "cube":
-            raise NotImplementedError(f"structure type {st.get('type')!r}: only the cubic "
-                                      "lattice generator (Reader.cpp:123-178) is provided")
-        # points^3 copies of the object on a cubic lattice with a corner at the origin
-        props = st.find("properties")
-        no, d = int(props.get("points")), float(props.get("distance")) * FRNM_TO_M
-        proto = _read_scatterer(st.find("object"), nmax)
-        for k in range(no):
-            for j in range(no):
-                for i in range(no):
-                    g.pushObject(Scatterer(vR=np.array([d * i, d * j, d * k]), radius=proto.radius,
-                                           elmag=proto.elmag, nMax=nmax))
+        for o in _structure(st, nmax):
+            g.pushObject(o)
     for node in geo.findall("object"):
         g.pushObject(_read_scatterer(node, nmax))
     bg = geo.find("background")

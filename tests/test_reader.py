@@ -51,7 +51,7 @@ def test_reader_rejections():
     with pytest.raises(RuntimeError, match="overlap"):
         O.simulation_input(base.replace('z="90.0"', 'z="50.0"'))
     with pytest.raises(NotImplementedError):
-        O.simulation_input(base.replace('<object type="sphere">', '<structure type="GaAscube"><object type="sphere">', 1)
+        O.simulation_input(base.replace('<object type="sphere">', '<structure type="hexagonal"><object type="sphere">', 1)
                            .replace('</object>', '</object></structure>', 1))
     with pytest.raises(RuntimeError, match="Unknown type"):
         O.simulation_input(base.replace('type="relative" value.real="-17.0"', 'type="Drude" value.real="-17.0"', 1))
@@ -155,5 +155,58 @@ def test_material_models_and_cube_structure():
                         '<object type="sphere">\n    <cartesian x="-300.0" y="0.0" z="0.0" />')
     run = O.simulation_input(cube)
     assert len(run.geometry.objects) == 28
-    assert np.allclose(run.geometry.objects[26].vR, [400e-9, 400e-9, 400e-9])
-    assert np.allclose(run.geometry.objects[1].vR, [200e-9, 0.0, 0.0])
+    # the reference's order: object k holds lattice site k + 1, the prototype
+    # (its own position, the origin here) comes last, then the other objects
+    assert np.allclose(run.geometry.objects[0].vR, [200e-9, 0.0, 0.0])
+    assert np.allclose(run.geometry.objects[25].vR, [400e-9, 400e-9, 400e-9])
+    assert np.allclose(run.geometry.objects[26].vR, [0.0, 0.0, 0.0])
+    assert np.allclose(run.geometry.objects[27].vR, [-300e-9, 0.0, 0.0])
+
+
+def _structure_case(kind, props, radius=20.0):
+    head = open(os.path.join(CASES, "field_map.xml")).read()
+    i, j = head.index("<geometry>"), head.index("</geometry>")
+    geo = ('<geometry>\n<structure type="%s"><properties %s />\n<object type="sphere">\n'
+           '<properties radius="%g" />\n<epsilon type="relative" value.real="12.0" value.imag="0.1" />\n'
+           '<mu type="relative" value.real="1.0" value.imag="0.0" />\n</object></structure>\n'
+           % (kind, props, radius))
+    return head[:i] + geo + head[j:]
+
+
+@pytest.mark.parametrize("kind,no,count", [("GaAssurf", 1, 18), ("GaAssurf", 2, 54), ("GaAssurf", 3, 110),
+                                           ("GaAscube", 1, 18), ("GaAscube", 2, 95), ("surface", 3, 9)])
+def test_structure_generators(kind, no, count):
+    """read_structure's generators (Reader.cpp:103-574). Zincblende cells of
+    size a: 14 large sites (radius R) and 4 small ones (R / 2 on a surface,
+    R / 1.7 in a cube); sites on a face shared with an earlier cell are not
+    repeated, so No x No cells hold 18 + 26 (No - 1) + 10 (No - 1)^2 sites and
+    No^3 cells 18 + 39 (No - 1) + 30 (No - 1)^2 + 8 (No - 1)^3 (the origin is
+    the prototype's own slot). Object k holds the (k + 1)-th non-origin site;
+    the prototype comes last at its own position (the origin)."""
+    from optimet_gb300 import optimet as O
+    a = 200.0
+    props = ('No_cells="%d" cell_size="%g"' % (no, a)) if kind.startswith("GaAs") else \
+        ('points="%d" distance="%g"' % (no, a))
+    run = O.simulation_input(_structure_case(kind, props))
+    obj = run.geometry.objects
+    m = no - 1
+    want = {"GaAssurf": 18 + 26 * m + 10 * m * m, "GaAscube": 18 + 39 * m + 30 * m * m + 8 * m ** 3,
+            "surface": no * no}[kind]
+    assert len(obj) == want == count
+    xyz = np.array([o.vR for o in obj]) / 1e-9
+    assert np.allclose(xyz[-1], 0.0)
+    assert len({tuple(np.round(p, 6)) for p in xyz}) == len(obj)  # no site twice
+    r = np.array([o.radius for o in obj]) / 1e-9
+    if kind == "surface":
+        assert np.allclose(xyz[0], [a, 0, 0]) and np.allclose(xyz[:, 2], 0.0) and np.allclose(r, 20.0)
+        return
+    assert np.allclose(xyz[0], [a, 0, 0]) and r[0] == pytest.approx(20.0)
+    small = 20.0 / (2.0 if kind == "GaAssurf" else 1.7)
+    assert set(np.round(r, 9)) == {20.0, round(small, 9)}
+    # the small sites sit at the quarter positions of each cell
+    frac = np.mod(xyz[r < 20.0] / a, 1.0)
+    assert np.all(np.isin(np.round(frac, 9), [0.25, 0.75]))
+    assert xyz.min() >= 0.0 and xyz.max() <= a * no + 1e-9
+    if kind == "GaAssurf":
+        assert xyz[:, 2].max() <= a + 1e-9
+
