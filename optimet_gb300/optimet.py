@@ -178,14 +178,14 @@ def _read_scatterer(node, nmax: int) -> Scatterer:
 
 
 # The zincblende (GaAs) cell of the structure generators, in units of the
-# cell size: 14 large sites, then 4 small ones (Reader.cpp:209-213, 341-345).
+# cell size: 14 large sites, then 4 small ones (Reader.cpp:205-209, 341-345).
 _ZB = ((1, 0, 0), (1, .5, .5), (.5, .5, 0), (.5, 0, .5), (0, .5, .5), (0, 1, 0), (.5, 1, .5), (1, 1, 1),
        (.5, .5, 1), (0, 0, 1), (0, 0, 0), (1, 0, 1), (1, 1, 0), (0, 1, 1), (.75, .25, .25), (.25, .75, .25),
        (.75, .75, .75), (.25, .25, .75))
 
 
 def _structure(st, nmax: int):
-    """The structure generators of read_structure (Reader.cpp:103-574): "cube"
+    """The structure generators of read_structure (Reader.cpp:120-573): "cube"
     (points^3 copies on a cubic lattice, a corner at the origin), "surface"
     (points^2 in the xy plane), "GaAssurf" (No_cells^2 zincblende cells in the
     xy plane; the 4 small sites have radius R / 2) and "GaAscube" (No_cells^3

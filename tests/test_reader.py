@@ -176,7 +176,7 @@ def _structure_case(kind, props, radius=20.0):
 @pytest.mark.parametrize("kind,no,count", [("GaAssurf", 1, 18), ("GaAssurf", 2, 54), ("GaAssurf", 3, 110),
                                            ("GaAscube", 1, 18), ("GaAscube", 2, 95), ("surface", 3, 9)])
 def test_structure_generators(kind, no, count):
-    """read_structure's generators (Reader.cpp:103-574). Zincblende cells of
+    """read_structure's generators (Reader.cpp:120-573). Zincblende cells of
     size a: 14 large sites (radius R) and 4 small ones (R / 2 on a surface,
     R / 1.7 in a cube); sites on a face shared with an earlier cell are not
     repeated, so No x No cells hold 18 + 26 (No - 1) + 10 (No - 1)^2 sites and
