@@ -843,6 +843,7 @@ def lu_mixed_arm(args):
     ref = pr.cross_sections()
     pr.close()
     pr = G.Problem(ctx, sp, G.medium(complex(w["host"]) ** 2), G.plane_wave(w["lam"]))
+    ctx.tune(lu_tensor_cores=args.lu_update)
     opts = G.options(G.SOLVE_LU_MIXED, tol=1e-9, max_iter=30, restarts=4)
     times, st = [], None
     with ClockSampler(0) as clk:
@@ -854,17 +855,33 @@ def lu_mixed_arm(args):
             st = pr.solve(opts)
             xs = pr.cross_sections()
             times.append(ctx.mark() * 1e-3)
+    # one more solve, untimed, with the phase timers on (an event pair per
+    # panel, trailing update and triangular solve)
+    ctx.timers(True)
+    ctx.lu_timers()
+    pr.solve(opts)
+    ph = ctx.lu_timers()
+    ctx.timers(False)
     t = float(np.median(times))
     err = float(abs(xs[0] - ref[0]) / abs(ref[0]))
+    n = pr.n
     pr.close()
     ctx.close()
+    upd_bytes = 16.0 * sum((n - K) ** 2 for K in range(128, n, 128))  # C read + written, complex64
+    phases = {"factor_ms": ph["factor"][0], "panel_ms": ph["panel"][0], "panels": ph["panel"][1],
+              "update_ms": ph["update"][0], "updates": ph["update"][1],
+              "update_hbm_frac_of_measured": upd_bytes / (ph["update"][0] * 1e-3) / 1e9 / peaks()[0]
+              if ph["update"][0] > 0 else None,
+              "tri_solve_ms": ph["tri_solve"][0], "tri_solves": ph["tri_solve"][1]}
     return {"metric": METRIC, "value": 1.0 / t, "unit": UNIT, "n_gpus": 1, "steps": len(times),
             "warmup": 0, "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64 (FP32) LU + c128 (FP64) refinement",
             "data": "synthetic (seeded)",
             "config": {"workload": "c2 LU role: " + w["desc"],
-                       "solver": "GMRES-based iterative refinement: FP64 residuals, GMRES on the system left-preconditioned by the FP32 LU (tensor-core trailing updates), tol 1e-9"},
-            "refinement_iterations": st.iterations, "qext_rel_err_vs_fp64": err, "clocks": clk.summary()}
+                       "solver": "GMRES-based iterative refinement: FP64 residuals, GMRES on the system left-preconditioned by the FP32 LU (tensor-core trailing updates), tol 1e-9",
+                       "trailing_update": {1: "persistent", 2: "one CTA per tile"}[args.lu_update]},
+            "refinement_iterations": st.iterations, "qext_rel_err_vs_fp64": err, "phases": phases,
+            "clocks": clk.summary()}
 
 
 def near_field_arm(args):
@@ -1160,6 +1177,8 @@ def main():
     ap.add_argument("--c4-seconds", type=float, default=60.0)
     ap.add_argument("--batch-slots", type=int, default=6, help="server slots for c3 / c4")
     ap.add_argument("--c4-forms", default="mixed,fp64", help="c4: forms to run (comma-separated)")
+    ap.add_argument("--lu-update", type=int, default=1, choices=[1, 2],
+                    help="c2lu: trailing-update kernel (1 persistent, 2 one CTA per tile)")
     ap.add_argument("--c4-batch-limit-gb", type=float, default=1.0,
                     help="c4: largest batched footprint of a request that is batched")
     ap.add_argument("--c4-batching", type=int, default=64,

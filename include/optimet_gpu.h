@@ -115,6 +115,12 @@ int om_context_synchronize(om_context *ctx);
  * complex128 (compensated) matvec ms, launches} (out may be NULL), resets
  * them and switches timing on or off. */
 int om_context_timers(om_context *ctx, int enable, double *out);
+/* LU phase timers, recorded while om_context_timers has switched timing on:
+ * out[8] = {factorization ms, factorizations, panel ms, panels, trailing-
+ * update ms, trailing updates, triangular-solve ms, solves (one forward and
+ * one backward sweep each)} accumulated since the previous call (out may be
+ * NULL); resets them. */
+int om_context_lu_timers(om_context *ctx, double *out);
 /* Launch tuning of a context (no counterpart in the reference). Fields below
  * zero keep the current value.
  *   matvec_ctas_per_sm / matvec_df_ctas_per_sm: grid caps of the complex64 /
@@ -130,12 +136,16 @@ typedef struct {
   int matvec_df_ctas_per_sm;
   int assemble_carveout;
   int matvec_carveout;
-  int lu_tensor_cores;   /* complex64 LU trailing updates on the tensor cores: 1 (default) / 0 */
+  int lu_tensor_cores;   /* complex64 LU trailing updates on the tensor cores: 1 (default,
+                            persistent: one CTA per SM), 2 (one CTA per 128 x 64 tile), 0 off */
   int matvec_tma;        /* complex64 x complex64 matvec with TMA-staged matrix tiles: 1 (default for
                             a context) / 0 (default for the slots of a server with several slots) */
   int assemble_rotation; /* complex64 assembly by rotated z-axis translations (one recurrence
                             chain per pair, FP32 rotation products): 1 (default) / 0 (the general
                             translation's 3 nMax + 1 chains per pair, FP32 block forming) */
+  int lu_panel;          /* LU panels of 8,192 rows or more: 1 (default) one cooperative launch
+                            per panel (a grid-wide barrier per column), 2 a pivot launch and an
+                            update launch per column */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any

@@ -68,7 +68,7 @@ class Tuning(C.Structure):
     _fields_ = [("matvec_ctas_per_sm", C.c_int), ("matvec_df_ctas_per_sm", C.c_int),
                 ("assemble_carveout", C.c_int), ("matvec_carveout", C.c_int),
                 ("lu_tensor_cores", C.c_int), ("matvec_tma", C.c_int),
-                ("assemble_rotation", C.c_int)]
+                ("assemble_rotation", C.c_int), ("lu_panel", C.c_int)]
 
 
 class Request(C.Structure):
@@ -104,6 +104,7 @@ def lib():
         L.om_context_last_launches.argtypes = [vp]
         L.om_context_synchronize.argtypes = [vp]
         L.om_context_timers.argtypes = [vp, C.c_int, _dp]
+        L.om_context_lu_timers.argtypes = [vp, _dp]
         L.om_context_mark.argtypes = [vp, _dp]
         L.om_context_tune.argtypes = [vp, C.POINTER(Tuning)]
         L.om_aca_info.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp,
@@ -203,10 +204,10 @@ class Context:
         return float(out[0])
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
-             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1):
+             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_panel=-1):
         """Launch tuning (om_context_tune); 0 / -1 keep the current value."""
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
-                   lu_tensor_cores, matvec_tma, assemble_rotation)
+                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_panel)
         self.check(lib().om_context_tune(self.h, C.byref(t)))
 
     def timers(self, enable=True):
@@ -215,6 +216,15 @@ class Context:
         self.check(lib().om_context_timers(self.h, int(enable), _p(out)))
         return {"assemble": (out[0], int(out[1])), "matvec_c128": (out[2], int(out[3])),
                 "matvec_c64": (out[4], int(out[5])), "matvec_c64_df": (out[6], int(out[7]))}
+
+    def lu_timers(self):
+        """LU phase times since the last call (recorded while timers() is on):
+        dict of (milliseconds, count) for factorizations, panels, trailing
+        updates and triangular solves."""
+        out = np.zeros(8)
+        self.check(lib().om_context_lu_timers(self.h, _p(out)))
+        return {"factor": (out[0], int(out[1])), "panel": (out[2], int(out[3])),
+                "update": (out[4], int(out[5])), "tri_solve": (out[6], int(out[7]))}
 
     @property
     def last_launches(self) -> int:
@@ -529,9 +539,9 @@ class Server:
             raise OptimetError(rc, "server batching")
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
-             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1):
+             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_panel=-1):
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
-                   lu_tensor_cores, matvec_tma, assemble_rotation)
+                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_panel)
         rc = lib().om_server_tune(self.h, C.byref(t))
         if rc:
             raise OptimetError(rc, "server tune")

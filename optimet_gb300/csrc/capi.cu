@@ -388,6 +388,10 @@ void collect_timers(om_context *ctx) {
   fold(ctx->ev_mv32, ctx->t_mv32, ctx->n_mv32);
   fold(ctx->ev_asm, ctx->t_asm, ctx->n_asm);
   fold(ctx->ev_mvdf, ctx->t_mvdf, ctx->n_mvdf);
+  fold(ctx->ev_luf, ctx->t_luf, ctx->n_luf);
+  fold(ctx->ev_lup, ctx->t_lup, ctx->n_lup);
+  fold(ctx->ev_luu, ctx->t_luu, ctx->n_luu);
+  fold(ctx->ev_lus, ctx->t_lus, ctx->n_lus);
 }
 }  // namespace om
 
@@ -428,11 +432,13 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
   if(t->matvec_carveout >= 0)
     ctx->carve_mv = t->matvec_carveout;
   if(t->lu_tensor_cores >= 0)
-    ctx->lu_tc = t->lu_tensor_cores ? 1 : 0;
+    ctx->lu_tc = std::min(t->lu_tensor_cores, 2);
   if(t->matvec_tma >= 0)
     ctx->mv_tma = t->matvec_tma ? 1 : 0;
   if(t->assemble_rotation >= 0)
     ctx->asm_rot = t->assemble_rotation ? 1 : 0;
+  if(t->lu_panel > 0)
+    ctx->lu_panel = std::min(t->lu_panel, 2);
   return OM_OK;
 }
 
@@ -504,6 +510,26 @@ int om_context_timers(om_context *ctx, int enable, double *out) {
   ctx->t_asm = ctx->t_mv64 = ctx->t_mv32 = ctx->t_mvdf = 0;
   ctx->n_asm = ctx->n_mv64 = ctx->n_mv32 = ctx->n_mvdf = 0;
   ctx->timing = enable != 0;
+  return OM_OK;
+}
+
+int om_context_lu_timers(om_context *ctx, double *out) {
+  if(!ctx)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  om::collect_timers(ctx);
+  if(out) {
+    out[0] = ctx->t_luf;
+    out[1] = (double)ctx->n_luf;
+    out[2] = ctx->t_lup;
+    out[3] = (double)ctx->n_lup;
+    out[4] = ctx->t_luu;
+    out[5] = (double)ctx->n_luu;
+    out[6] = ctx->t_lus;
+    out[7] = (double)ctx->n_lus;
+  }
+  ctx->t_luf = ctx->t_lup = ctx->t_luu = ctx->t_lus = 0;
+  ctx->n_luf = ctx->n_lup = ctx->n_luu = ctx->n_lus = 0;
   return OM_OK;
 }
 

@@ -118,7 +118,12 @@ struct om_context {
   int *d_tma_err = nullptr;                      // set by a TMA matvec whose wait timed out
   int mv_tma = 1;                                // complex64 matvecs staged by TMA
   int carve_asm = -1, carve_mv = -1;  // preferred smem carveout (percent), -1 = driver's choice
-  int lu_tc = 1;  // complex64 LU trailing updates on the tensor cores
+  // complex64 LU trailing updates on the tensor cores: 1 persistent kernel,
+  // 2 one CTA per tile, 0 off (FP32 CUDA cores)
+  int lu_tc = 1;
+  // LU panels of kTallPanel rows or more: 1 one cooperative launch per panel,
+  // 2 a pivot launch and an update launch per column
+  int lu_panel = 1;
   int asm_rot = 1;  // precision-form assembly by rotated z-axis translations (assemble_rot.cu)
   size_t budget = 0;
   size_t used = 0;
@@ -133,6 +138,10 @@ struct om_context {
   double t_mv64 = 0, t_mv32 = 0, t_mvdf = 0, t_asm = 0;  // accumulated milliseconds
   cudaEvent_t mark = nullptr;                // last om_context_mark event
   long n_mv64 = 0, n_mv32 = 0, n_mvdf = 0, n_asm = 0;
+  // LU phases: whole factorizations, panels, trailing updates, triangular solves
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_luf, ev_lup, ev_luu, ev_lus;
+  double t_luf = 0, t_lup = 0, t_luu = 0, t_lus = 0;
+  long n_luf = 0, n_lup = 0, n_luu = 0, n_lus = 0;
   std::vector<om_problem *> problems;  // live problems, destroyed with the context
   // auxiliary contexts of the batched solver (streams for per-request work);
   // a context with a parent takes its coefficient tables from the parent

@@ -891,6 +891,230 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_update(V *A, long ld, long 
   }
 }
 
+// A tall panel in one cooperative launch (all CTAs resident), one grid-wide
+// barrier per column instead of a pivot kernel and an update kernel. The row
+// interchanges are kept as a small permutation table (the positions a swap
+// has touched and the physical row at each) instead of being carried out at
+// once: a CTA updates the physical rows of its grid-stride range that are not
+// yet pivot rows, and the pivot row of column c is read from its physical
+// row, which no CTA writes during that step. Every CTA reduces the per-CTA
+// partial maxima itself (larger magnitude, then the smaller position, the
+// order of k_lu_panel) and applies the same table updates, so no CTA waits for
+// another's pivot. After the last column CTA 0 moves the touched rows of the
+// panel's columns to their final positions. Each entry takes the operations
+// of k_lu_panel, so the factors are the same. Barrier waits are bounded; on
+// time-out the kernel raises *err and returns.
+struct PanelPerm {
+  long pos[2 * kNb], row[2 * kNb];
+  int cnt;
+};
+
+__device__ __forceinline__ long perm_row(const PanelPerm &pm, long pos) {
+  for(int e = 0; e < pm.cnt; ++e)
+    if(pm.pos[e] == pos)
+      return pm.row[e];
+  return pos;
+}
+__device__ __forceinline__ long perm_pos(const PanelPerm &pm, long row) {
+  for(int e = 0; e < pm.cnt; ++e)
+    if(pm.row[e] == row)
+      return pm.pos[e];
+  return row;
+}
+__device__ __forceinline__ void perm_set(PanelPerm &pm, long pos, long row) {
+  for(int e = 0; e < pm.cnt; ++e)
+    if(pm.pos[e] == pos) {
+      pm.row[e] = row;
+      return;
+    }
+  pm.pos[pm.cnt] = pos;
+  pm.row[pm.cnt] = row;
+  ++pm.cnt;
+}
+
+// grid-wide barrier on a counter that only grows: this CTA's arrival, then a
+// bounded wait for `target` arrivals
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target, int *err) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    int ok = 0;
+    for(long it = 0; it < (1L << 22); ++it) {
+      if(*(volatile unsigned *)bar >= target) {
+        ok = 1;
+        break;
+      }
+      if((it & 63) == 63 && *(volatile int *)err)
+        break;  // another CTA (or an earlier launch) gave up
+    }
+    if(!ok)
+      atomicExch(err, 1);
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kPanThreads) k_pan_coop(V *A, long ld, long n, long k, int nb, int *piv,
+                                                          int *info, PanelScratch ps, unsigned *bar,
+                                                          unsigned bar_base, int *err) {
+  __shared__ V u[kNb];
+  __shared__ PanelPerm pm;
+  __shared__ long piv_row[kNb];  // physical rows of the pivots so far
+  __shared__ double wv[kPanThreads / 32];
+  __shared__ long wi[kPanThreads / 32];
+  __shared__ long p_s;
+  __shared__ double pv_s;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const unsigned G = gridDim.x;
+  if(*(volatile int *)err)  // an earlier wait timed out: the factorization is void
+    return;
+  if(t == 0)
+    pm.cnt = 0;
+  // partial maximum of |A[col, r]|^2 over the active physical rows r of this
+  // CTA (positions for ties), reduced over the CTA into ps.bestv / besti
+  auto partial_max = [&](long col, int npiv) {
+    double bv = -1.0;
+    long bp = col;
+    for(long r = k + blockIdx.x * (long)kPanThreads + t; r < n; r += (long)G * kPanThreads) {
+      bool retired = false;
+      for(int e = 0; e < npiv; ++e)
+        retired |= piv_row[e] == r;
+      if(retired)
+        continue;
+      const double v = mag2(A[col * ld + r]);
+      if(v >= bv) {
+        const long pos = perm_pos(pm, r);
+        if(v > bv || pos < bp) {
+          bv = v;
+          bp = pos;
+        }
+      }
+    }
+#pragma unroll
+    for(int h = 16; h > 0; h >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, bv, h);
+      const long op = __shfl_xor_sync(0xffffffffu, bp, h);
+      if(ov > bv || (ov == bv && op < bp)) {
+        bv = ov;
+        bp = op;
+      }
+    }
+    if(lane == 0) {
+      wv[wid] = bv;
+      wi[wid] = bp;
+    }
+    __syncthreads();
+    if(t == 0) {
+      for(int w = 1; w < kPanThreads / 32; ++w)
+        if(wv[w] > bv || (wv[w] == bv && wi[w] < bp)) {
+          bv = wv[w];
+          bp = wi[w];
+        }
+      ps.bestv[blockIdx.x] = bv;
+      ps.besti[blockIdx.x] = bp;
+    }
+  };
+  __syncthreads();
+  partial_max(k, 0);
+  unsigned target = bar_base;
+  for(int c = 0; c < nb; ++c) {
+    const long col = k + c;
+    target += G;
+    if(!grid_barrier(bar, target, err))
+      return;
+    // the pivot: every CTA reduces all partial maxima (in CTA order)
+    {
+      double bv = -2.0;
+      long bp = col;
+      for(unsigned b = t; b < G; b += kPanThreads) {
+        const double v = ps.bestv[b];
+        const long i = ps.besti[b];
+        if(v > bv || (v == bv && i < bp)) {
+          bv = v;
+          bp = i;
+        }
+      }
+#pragma unroll
+      for(int h = 16; h > 0; h >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, bv, h);
+        const long op = __shfl_xor_sync(0xffffffffu, bp, h);
+        if(ov > bv || (ov == bv && op < bp)) {
+          bv = ov;
+          bp = op;
+        }
+      }
+      if(lane == 0) {
+        wv[wid] = bv;
+        wi[wid] = bp;
+      }
+      __syncthreads();
+      if(t == 0) {
+        for(int w = 1; w < kPanThreads / 32; ++w)
+          if(wv[w] > bv || (wv[w] == bv && wi[w] < bp)) {
+            bv = wv[w];
+            bp = wi[w];
+          }
+        if(blockIdx.x == 0) {
+          piv[col] = (int)bp;
+          if(bv <= 0.0 && *info == 0)
+            *info = (int)col + 1;
+        }
+        // interchange positions col and bp in the table
+        const long a = perm_row(pm, col), b = perm_row(pm, bp);
+        if(bp != col) {
+          perm_set(pm, col, b);
+          perm_set(pm, bp, a);
+        }
+        piv_row[c] = b;
+        p_s = b;
+        pv_s = bv;
+      }
+      __syncthreads();
+    }
+    const long prow = p_s;
+    if(t < nb)
+      u[t] = A[(k + t) * ld + prow];
+    __syncthreads();
+    if(pv_s > 0.0) {
+      const V inv = crecip(u[c]);
+      for(long r = k + blockIdx.x * (long)kPanThreads + t; r < n; r += (long)G * kPanThreads) {
+        bool retired = false;
+        for(int e = 0; e <= c; ++e)
+          retired |= piv_row[e] == r;
+        if(retired)
+          continue;
+        V l = cmul(A[col * ld + r], inv);
+        A[col * ld + r] = l;
+        panel_row_update(A, ld, k, r, c, nb, l, u);
+      }
+    }
+    if(c + 1 < nb) {
+      __syncthreads();
+      partial_max(col + 1, c + 1);
+    }
+  }
+  target += G;
+  if(!grid_barrier(bar, target, err) || blockIdx.x != 0)
+    return;
+  // CTA 0: the touched rows of the panel's columns to their final positions
+  __shared__ V tmp[2 * kNb][kNb];
+  const int cnt = pm.cnt;
+  for(int idx = t; idx < cnt * nb; idx += kPanThreads) {
+    const int e = idx / nb, j = idx - e * nb;
+    tmp[e][j] = A[(k + j) * ld + pm.row[e]];
+  }
+  __syncthreads();
+  for(int idx = t; idx < cnt * nb; idx += kPanThreads) {
+    const int e = idx / nb, j = idx - e * nb;
+    A[(k + j) * ld + pm.pos[e]] = tmp[e][j];
+  }
+}
+
 // Apply the row interchanges of rows k .. k + nb - 1 (in order) to the
 // columns jlo .. jhi - 1 other than slo .. shi - 1 (the panel's own columns,
 // which the panel kernels swap themselves).
@@ -1141,17 +1365,19 @@ void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Pane
         launch_cgemm_sub_tc(ctx, A + k * n + kn, n, A + KE * n + k, n, A + KE * n + kn, n, KE - kn,
                             rest, nb, info + 1);
     }
+    timer_begin(ctx, ctx->ev_luu);
     if(split && W >= 64)  // operands split once, streamed by bulk copies
       launch_cgemm_sub_tc_split(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest,
                                 rest, (int)W, split, info + 1);
     else
       launch_cgemm_sub_tc(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest, rest,
                           (int)W, info + 1);
+    timer_end(ctx, ctx->ev_luu);
   }
 }
 
-// info[0]: first zero pivot (1-based) or 0; info[1]: set when a tensor-core
-// trailing update timed out (complex64 only).
+// info[0]: first zero pivot (1-based) or 0; info[1]: set when a wait timed
+// out (a tensor-core trailing update or a cooperative panel's barrier).
 template <typename V>
 int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   cudaMemsetAsync(info, 0, 2 * sizeof(int), ctx->stream);
@@ -1164,8 +1390,20 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
     if(ctx->lu_tc && n > kTcBlock)
       split_bytes = cgemm_sub_tc_split_bytes(n, n, (int)kTcBlock);
   const size_t pan_bytes =
-      n >= kTallPanel ? maxblk * (sizeof(double) + sizeof(long)) + kNb * sizeof(V) + 3 * 256 : 0;
+      n >= kTallPanel ? maxblk * (sizeof(double) + sizeof(long)) + kNb * sizeof(V) + 4 * 256 : 0;
   void *split = nullptr;
+  unsigned *bar = nullptr, bar_base = 0;  // the cooperative panels' barrier counter
+  // CTAs of one cooperative panel launch: one per SM, as many as can be
+  // resident at once
+  int coop_grid = 0;
+  if(ctx->lu_panel == 1 && n >= kTallPanel) {
+    int per_sm = 0, coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+    if(coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pan_coop<V>, kPanThreads, 0) ==
+                   cudaSuccess)
+      coop_grid = std::min(per_sm, 1) * ctx->sm_count;
+    cudaGetLastError();
+  }
   if(pan_bytes + split_bytes) {
     const int rc = alloc_work(ctx, ws, pan_bytes + split_bytes + 256);
     if(rc)
@@ -1175,13 +1413,32 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
       ps.bestv = ws.take<double>(maxblk, off);
       ps.besti = ws.take<long>(maxblk, off);
       ps.prow = ws.take<V>(kNb, off);
+      bar = ws.take<unsigned>(1, off);
+      cudaMemsetAsync(bar, 0, sizeof(unsigned), ctx->stream);
     }
     if(split_bytes)
       split = ws.take<unsigned char>(split_bytes, off);
   }
+  timer_begin(ctx, ctx->ev_luf);
   // LU of the panel A[k:n, k:k+nb) with its row interchanges inside the panel
   auto panel = [&](long k, int nb) {
+    timer_begin(ctx, ctx->ev_lup);
     const long rows = n - k;
+    if(rows >= kTallPanel && coop_grid > 0) {
+      ps.nblk = (int)std::min<long>(coop_grid, (rows + kPanThreads - 1) / kPanThreads);
+      int *err = info + 1;
+      void *args[] = {&A, (void *)&n, (void *)&n, (void *)&k, (void *)&nb, &piv, &info, &ps, &bar, &bar_base, &err};
+      const cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_pan_coop<V>, dim3(ps.nblk),
+                                                        dim3(kPanThreads), args, 0, ctx->stream);
+      if(e == cudaSuccess) {
+        bar_base += (unsigned)(nb + 1) * (unsigned)ps.nblk;
+        ctx->last_launches++;
+        timer_end(ctx, ctx->ev_lup);
+        return;
+      }
+      cudaGetLastError();  // refused: the per-column kernels below
+      coop_grid = 0;
+    }
     if(rows >= kTallPanel) {
       ps.nblk = (int)std::min<long>(maxblk, (rows + kPanThreads - 1) / kPanThreads);
       k_pan_max<V><<<ps.nblk, kPanThreads, 0, ctx->stream>>>(A, n, n, k, ps);
@@ -1194,10 +1451,12 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
       k_lu_panel<V><<<1, 1024, 0, ctx->stream>>>(A, n, n, k, nb, piv, info);
       ctx->last_launches++;
     }
+    timer_end(ctx, ctx->ev_lup);
   };
   if constexpr(std::is_same<V, float2>::value) {
     if(ctx->lu_tc) {
       lu_blocked_tc(ctx, A, n, piv, info, panel, split);
+      timer_end(ctx, ctx->ev_luf);
       return OM_OK;
     }
   }
@@ -1210,10 +1469,13 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
     if(rest > 0) {
       k_lu_trsm<V><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, k + nb, n, k, nb);
       dim3 g((unsigned)((rest + 31) / 32), (unsigned)((rest + 31) / 32));
+      timer_begin(ctx, ctx->ev_luu);
       k_lu_gemm<V><<<g, 256, 0, ctx->stream>>>(A, n, n, k, nb);
+      timer_end(ctx, ctx->ev_luu);
       ctx->last_launches += 2;
     }
   }
+  timer_end(ctx, ctx->ev_luf);
   return OM_OK;
 }
 
@@ -1278,12 +1540,18 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   k_lu_diag_inv<double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, n, dinv);
   ctx->last_launches++;
   cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+  timer_begin(ctx, ctx->ev_lus);
   lu_solve_vec<double2>(ctx, A, n, perm, dinv, x, y);
-  int hinfo = 0;
-  cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  timer_end(ctx, ctx->ev_lus);
+  int hinfo[2] = {0, 0};
+  cudaMemcpyAsync(hinfo, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
-  if(hinfo) {
-    ctx->err = "singular matrix: zero pivot at column " + std::to_string(hinfo);
+  if(hinfo[1]) {
+    ctx->err = "LU panel barrier timed out";
+    return OM_ERR_CUDA;
+  }
+  if(hinfo[0]) {
+    ctx->err = "singular matrix: zero pivot at column " + std::to_string(hinfo[0]);
     return OM_ERR_SINGULAR;
   }
   if(st) {
@@ -1383,7 +1651,7 @@ struct LuPrecond32 : PrecondFn {
     cudaMemcpyAsync(hinfo, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     if(hinfo[1]) {
-      ctx->err = "tensor-core LU update timed out";
+      ctx->err = "LU kernel wait timed out (tensor-core trailing update or panel barrier)";
       return OM_ERR_CUDA;
     }
     if(hinfo[0]) {
@@ -1413,12 +1681,14 @@ struct LuPrecond32 : PrecondFn {
   }
   void apply(const double2 *v, double2 *z) override {
     k_scale_copy<double2, float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v, 1.0, v32, n);
+    timer_begin(ctx, ctx->ev_lus);
     if(solve_graph) {
       cudaGraphLaunch(solve_graph, ctx->stream);
       ctx->last_launches += solve_launches;
     } else {
       lu_solve_vec<float2>(ctx, A, n, perm, dinv, v32, y32);
     }
+    timer_end(ctx, ctx->ev_lus);
     k_scale_copy<float2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v32, 1.0, z, n);
     ctx->last_launches += 2;
     ++applied;

@@ -23,6 +23,8 @@
 // From k = 64 (the LU's rank-128 updates) a second path splits the operands
 // once and streams them by bulk copies (k_tc_split_a/b, k_cgemm_sub_tc2,
 // below).
+#include <algorithm>
+
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -578,6 +580,312 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent form of the split-operand update, one CTA per SM. The CTA takes a
+// contiguous range of the 128 x 64 tiles in row-tile-major order, so its A
+// tiles (all nq <= 4 chunks: up to 128 KB) stay resident in shared memory
+// while it walks the column tiles of a row tile; only B's chunks (16 KB) are
+// streamed, through a ring of three stages. The roles are split by warp:
+//   warps 0-3  epilogue: TMEM lanes 32 w .. 32 w + 31 (rows of the tile), C
+//              read from a shared-memory ring, C - AB stored to global;
+//   warp 4     operand copies (A when the row tile changes, B chunks);
+//   warp 5     TMEM allocation and the MMAs (one elected thread);
+//   warp 6     C copies: each tile's columns in groups of 16 (16 KB; one
+//              bulk copy per column) through a ring of three slots.
+// The accumulators (Ar Br, Ai Bi, Im: 3 x 64 TMEM columns) are double
+// buffered, so the epilogue of one tile runs under the MMAs of the next, and
+// the C ring keeps up to 48 KB of C reads in flight per SM. Every wait is
+// bounded; a time-out raises *err and a shared abort flag that the other
+// roles poll, after which each role waits (bounded) for its own copies and
+// MMAs in flight, and the TMEM is freed.
+constexpr int kPThreads = 224;
+constexpr int kPMaxQ = 4;                      // k <= 128
+constexpr int kPBStages = 3, kPCSlots = 3;
+constexpr int kPCSlot = 16 * kTcM * 8;         // 16 columns of 128 complex64
+constexpr int kPOffB = kPMaxQ * kStageA;       // 128 KB of resident A
+constexpr int kPOffC = kPOffB + kPBStages * kStageB;
+constexpr int kPOffBar = kPOffC + kPCSlots * kPCSlot;
+constexpr int kPSmem = kPOffBar + 256;
+constexpr uint32_t kPTmemCols = 512;           // two sets of three 64-column accumulators
+static_assert(kPSmem <= 227 * 1024, "persistent update: shared memory");
+
+struct PBars {
+  uint64_t a_full, a_empty, drain;
+  uint64_t b_full[kPBStages], b_empty[kPBStages];
+  uint64_t c_full[kPCSlots], c_empty[kPCSlots];
+  uint64_t t_full[2], t_empty[2];
+  uint32_t tmem;
+  int abort;
+};
+static_assert(sizeof(PBars) <= 256, "persistent update: barrier block");
+
+__device__ __forceinline__ uint32_t try_phase(uint64_t *bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done;
+}
+
+// Bounded wait that also gives up when another role has aborted; a time-out
+// raises the abort flag and *err.
+__device__ __forceinline__ uint32_t pwait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                          int *err) {
+  for(long it = 0; it < (1L << 24); ++it) {
+    if(try_phase(bar, parity))
+      return 1;
+    if((it & 63) == 63 && *abort_flag)
+      return 0;
+  }
+  *abort_flag = 1;
+  atomicExch(err, 1);
+  return 0;
+}
+
+__device__ __forceinline__ void arrive1(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_addr(bar))
+               : "memory");
+}
+
+__global__ void __launch_bounds__(kPThreads, 1)
+    k_cgemm_sub_tc3(const unsigned char *As, const unsigned char *Bs, int nq, float2 *C, long ldc,
+                    long m, long n, int *err) {
+  extern __shared__ __align__(1024) unsigned char psm[];
+  PBars *bars = reinterpret_cast<PBars *>(psm + kPOffBar);
+  volatile int *abort_flag = &bars->abort;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const long mt = (m + kTcM - 1) / kTcM, nt = (n + kTcN - 1) / kTcN, T = mt * nt;
+  const long t0 = T * blockIdx.x / gridDim.x, t1 = T * (blockIdx.x + 1) / gridDim.x;
+
+  if(warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(&bars->tmem)),
+                 "r"(kPTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if(t == 0) {
+    auto init = [](uint64_t *b, int c) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(c));
+    };
+    init(&bars->a_full, 1);
+    init(&bars->a_empty, 1);
+    init(&bars->drain, 1);
+    for(int i = 0; i < kPBStages; ++i) {
+      init(bars->b_full + i, 1);
+      init(bars->b_empty + i, 1);
+    }
+    for(int i = 0; i < kPCSlots; ++i) {
+      init(bars->c_full + i, 1);
+      init(bars->c_empty + i, 4);
+    }
+    for(int i = 0; i < 2; ++i) {
+      init(bars->t_full + i, 1);
+      init(bars->t_empty + i, 4);
+    }
+    bars->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = bars->tmem;
+
+  if(warp == 4 && lane == 0) {
+    // operand copies
+    long prev_rt = -1, bq = 0;
+    int a_loads = 0;
+    for(long tile = t0; tile < t1 && !*abort_flag; ++tile) {
+      const long rt = tile / nt, ct = tile - rt * nt;
+      if(rt != prev_rt) {
+        if(a_loads > 0 && !pwait(&bars->a_empty, (uint32_t)(a_loads - 1) & 1u, abort_flag, err))
+          break;
+        arrive_expect(&bars->a_full, (uint32_t)(nq * kStageA));
+        for(int q = 0; q < nq; ++q)
+          bulk_load(psm + q * kStageA, As + ((size_t)rt * nq + q) * kStageA, (uint32_t)kStageA,
+                    &bars->a_full);
+        ++a_loads;
+        prev_rt = rt;
+      }
+      bool stop = false;
+      for(int q = 0; q < nq; ++q, ++bq) {
+        const int s = (int)(bq % kPBStages);
+        if(bq >= kPBStages &&
+           !pwait(bars->b_empty + s, (uint32_t)(bq / kPBStages - 1) & 1u, abort_flag, err)) {
+          stop = true;
+          break;
+        }
+        arrive_expect(bars->b_full + s, (uint32_t)kStageB);
+        bulk_load(psm + kPOffB + s * kStageB, Bs + ((size_t)ct * nq + q) * kStageB, (uint32_t)kStageB,
+                  bars->b_full + s);
+      }
+      if(stop)
+        break;
+    }
+    // the copies still in flight land before the CTA may exit (bounded)
+    if(a_loads > 0)
+      wait_phase(&bars->a_full, (uint32_t)(a_loads - 1) & 1u);
+    for(long q = bq - 1; q >= 0 && q >= bq - kPBStages; --q)
+      wait_phase(bars->b_full + q % kPBStages, (uint32_t)(q / kPBStages) & 1u);
+  } else if(warp == 5 && lane == 0) {
+    // MMAs
+    long prev_rt = -1, bq = 0;
+    int a_loaded = 0;
+    for(long tile = t0, j = 0; tile < t1 && !*abort_flag; ++tile, ++j) {
+      const long rt = tile / nt;
+      if(rt != prev_rt) {
+        if(prev_rt >= 0)
+          mma_commit(&bars->a_empty);  // the previous row tile's MMAs have read A
+        if(!pwait(&bars->a_full, (uint32_t)a_loaded & 1u, abort_flag, err))
+          break;
+        ++a_loaded;
+        prev_rt = rt;
+      }
+      const int as = (int)(j & 1);
+      if(j >= 2 && !pwait(bars->t_empty + as, (uint32_t)(j / 2 - 1) & 1u, abort_flag, err))
+        break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t d_r1 = tmem + as * 3 * kTcN, d_r2 = d_r1 + kTcN, d_im = d_r1 + 2 * kTcN;
+      bool stop = false;
+      for(int q = 0; q < nq; ++q, ++bq) {
+        const int s = (int)(bq % kPBStages);
+        if(!pwait(bars->b_full + s, (uint32_t)(bq / kPBStages) & 1u, abort_flag, err)) {
+          stop = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        unsigned char *Aq = psm + q * kStageA;
+        unsigned char *Arh = Aq, *Arl = Aq + kAPart, *Aih = Aq + 2 * kAPart, *Ail = Aq + 3 * kAPart;
+        unsigned char *Brh = psm + kPOffB + s * kStageB, *Brl = Brh + kBPart, *Bih = Brh + 2 * kBPart,
+                      *Bil = Brh + 3 * kBPart;
+        for(int st = 0; st < kTcK / 16; ++st) {
+          const uint32_t ko = st * 256;
+          auto da = [&](unsigned char *p) { return umma_desc(smem_addr(p) + ko, 128, 512); };
+          const uint32_t acc = q > 0 || st > 0;
+          mma_bf16(d_r1, da(Arh), da(Brh), acc);
+          mma_bf16(d_r1, da(Arh), da(Brl), 1);
+          mma_bf16(d_r1, da(Arl), da(Brh), 1);
+          mma_bf16(d_r2, da(Aih), da(Bih), acc);
+          mma_bf16(d_r2, da(Aih), da(Bil), 1);
+          mma_bf16(d_r2, da(Ail), da(Bih), 1);
+          mma_bf16(d_im, da(Arh), da(Bih), acc);
+          mma_bf16(d_im, da(Arh), da(Bil), 1);
+          mma_bf16(d_im, da(Arl), da(Bih), 1);
+          mma_bf16(d_im, da(Aih), da(Brh), 1);
+          mma_bf16(d_im, da(Aih), da(Brl), 1);
+          mma_bf16(d_im, da(Ail), da(Brh), 1);
+        }
+        mma_commit(bars->b_empty + s);
+      }
+      if(stop)
+        break;
+      mma_commit(bars->t_full + as);
+    }
+    // every MMA issued has completed before the TMEM is freed (bounded)
+    mma_commit(&bars->drain);
+    wait_phase(&bars->drain, 0u);
+  } else if(warp == 6 && lane == 0) {
+    // C copies
+    long cq = 0;
+    for(long tile = t0; tile < t1 && !*abort_flag; ++tile) {
+      const long rt = tile / nt, ct = tile - rt * nt;
+      const long r0 = rt * kTcM, c0 = ct * kTcN;
+      const uint32_t rows = (uint32_t)min((long)kTcM, m - r0);
+      bool stop = false;
+      for(int g = 0; g < kTcN / 16; ++g, ++cq) {
+        const int s = (int)(cq % kPCSlots);
+        if(cq >= kPCSlots &&
+           !pwait(bars->c_empty + s, (uint32_t)(cq / kPCSlots - 1) & 1u, abort_flag, err)) {
+          stop = true;
+          break;
+        }
+        const long cg = c0 + 16 * g;
+        const int cols = (int)max(0L, min(16L, n - cg));
+        arrive_expect(bars->c_full + s, (uint32_t)cols * rows * 8u);
+        for(int c = 0; c < cols; ++c)
+          bulk_load(psm + kPOffC + s * kPCSlot + c * (kTcM * 8), C + (cg + c) * ldc + r0, rows * 8u,
+                    bars->c_full + s);
+      }
+      if(stop)
+        break;
+    }
+    for(long q = cq - 1; q >= 0 && q >= cq - kPCSlots; --q)
+      wait_phase(bars->c_full + q % kPCSlots, (uint32_t)(q / kPCSlots) & 1u);
+  } else if(warp < 4) {
+    // epilogue: thread (warp, lane) owns row 32 warp + lane of each tile
+    // (decisions are made per warp: tcgen05.ld needs the whole warp)
+    long cq = 0;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    for(long tile = t0, j = 0; tile < t1; ++tile, ++j) {
+      if(__any_sync(0xffffffffu, *abort_flag))
+        break;
+      const long rt = tile / nt, ct = tile - rt * nt;
+      const long r = rt * kTcM + warp * 32 + lane, c0 = ct * kTcN;
+      const int as = (int)(j & 1);
+      if(!__all_sync(0xffffffffu, pwait(bars->t_full + as, (uint32_t)(j / 2) & 1u, abort_flag, err)))
+        break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t d_r1 = tmem + lane_base + as * 3 * kTcN, d_r2 = d_r1 + kTcN, d_im = d_r1 + 2 * kTcN;
+      bool stop = false;
+      for(int g = 0; g < kTcN / 16; ++g, ++cq) {
+        const int s = (int)(cq % kPCSlots);
+        uint32_t a[16], b[16], c[16];
+#define OM_TMEM_LD16(dst, addr)                                                                     \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
+               : "=r"(dst[0]), "=r"(dst[1]), "=r"(dst[2]), "=r"(dst[3]), "=r"(dst[4]), "=r"(dst[5]),  \
+                 "=r"(dst[6]), "=r"(dst[7]), "=r"(dst[8]), "=r"(dst[9]), "=r"(dst[10]),              \
+                 "=r"(dst[11]), "=r"(dst[12]), "=r"(dst[13]), "=r"(dst[14]), "=r"(dst[15])           \
+               : "r"(addr))
+        OM_TMEM_LD16(a, d_r1 + 16 * g);
+        OM_TMEM_LD16(b, d_r2 + 16 * g);
+        OM_TMEM_LD16(c, d_im + 16 * g);
+#undef OM_TMEM_LD16
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if(!__all_sync(0xffffffffu, pwait(bars->c_full + s, (uint32_t)(cq / kPCSlots) & 1u, abort_flag, err))) {
+          stop = true;
+          break;
+        }
+        const float2 *cs = reinterpret_cast<const float2 *>(psm + kPOffC + s * kPCSlot) + warp * 32 + lane;
+        if(r < m) {
+#pragma unroll
+          for(int q = 0; q < 16; ++q) {
+            const long col = c0 + 16 * g + q;
+            if(col < n) {
+              float2 v = cs[q * kTcM];
+              v.x -= __uint_as_float(a[q]) - __uint_as_float(b[q]);
+              v.y -= __uint_as_float(c[q]);
+              C[col * ldc + r] = v;
+            }
+          }
+        }
+        __syncwarp();
+        if(lane == 0)
+          arrive1(bars->c_empty + s);
+      }
+      if(stop)
+        break;
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if(lane == 0)
+        arrive1(bars->t_empty + as);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if(warp == 5) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPTmemCols));
+  }
+}
+
 }  // namespace
 
 void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
@@ -601,8 +909,19 @@ void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const
   unsigned char *Bs = As + (size_t)mt * nq * kStageA;
   k_tc_split_a<<<dim3(mt, (unsigned)nq), 512, 0, ctx->stream>>>(A, lda, m, k, nq, As);
   k_tc_split_b<<<dim3(nt, (unsigned)nq), 256, 0, ctx->stream>>>(B, ldb, n, k, nq, Bs);
-  cudaFuncSetAttribute(k_cgemm_sub_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, kTc2Smem);
-  k_cgemm_sub_tc2<<<dim3(mt, nt), 128, kTc2Smem, ctx->stream>>>(As, Bs, nq, C, ldc, m, n, d_err);
+  // the persistent form copies C's columns (m rows each) by bulk copies:
+  // 16-byte aligned starts and sizes
+  const bool persistent = ctx->lu_tc == 1 && nq <= kPMaxQ &&
+                          (reinterpret_cast<uintptr_t>(C) & 15) == 0 && (ldc & 1) == 0 && (m & 1) == 0;
+  if(persistent) {
+    cudaFuncSetAttribute(k_cgemm_sub_tc3, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem);
+    const long tiles = (long)mt * nt;
+    const unsigned grid = (unsigned)std::min<long>(tiles, ctx->sm_count);
+    k_cgemm_sub_tc3<<<grid, kPThreads, kPSmem, ctx->stream>>>(As, Bs, nq, C, ldc, m, n, d_err);
+  } else {
+    cudaFuncSetAttribute(k_cgemm_sub_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, kTc2Smem);
+    k_cgemm_sub_tc2<<<dim3(mt, nt), 128, kTc2Smem, ctx->stream>>>(As, Bs, nq, C, ldc, m, n, d_err);
+  }
   ctx->last_launches += 3;
 }
 

@@ -28,7 +28,8 @@ def ctx(G):
 # k > 32 runs in several chunks through the kernel's operand tiles (the
 # LU's rank-128 trailing updates), with a ragged last chunk for 80 and 33
 @pytest.mark.parametrize("m,n,k", [(128, 64, 32), (300, 200, 32), (257, 70, 17), (5, 3, 1),
-                                   (300, 200, 128), (257, 70, 80), (130, 65, 33)])
+                                   (300, 200, 128), (257, 70, 80), (130, 65, 33), (258, 70, 80),
+                                   (1000, 1030, 128), (130, 66, 64)])
 def test_update_exact_on_bf16_values(G, ctx, m, n, k):
     rng = np.random.default_rng(m + n + k)
     A = (rng.integers(-8, 9, (m, k)) + 1j * rng.integers(-8, 9, (m, k))).astype(np.complex64)
@@ -54,6 +55,29 @@ def test_update_accuracy_general(G, ctx, k):
     assert err > 1e-9        # (and not an FP32 SIMT path in disguise)
 
 
+# The persistent update (one CTA per SM walking its range of tiles, A resident,
+# B and C streamed through rings, double-buffered accumulators) issues the same
+# MMAs in the same order as the one-CTA-per-tile kernel and rounds the same
+# epilogue, so the two agree bit for bit: a grid with fewer tiles than SMs,
+# ranges that cross row tiles, and long ranges that wrap every ring many times.
+@pytest.mark.parametrize("m,n,k", [(256, 192, 128), (2050, 1500, 128), (4000, 4001, 128), (1998, 700, 96)])
+def test_persistent_update_matches_tile_grid(G, ctx, m, n, k):
+    rng = np.random.default_rng(m + 7 * n + k)
+    A = (rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))).astype(np.complex64)
+    B = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))).astype(np.complex64)
+    C = (rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))).astype(np.complex64)
+    out = {}
+    for tc in (1, 2):
+        ctx.tune(lu_tensor_cores=tc)
+        out[tc] = G.cgemm_sub_c64(ctx, A, B, C)
+    ctx.tune(lu_tensor_cores=1)
+    assert np.array_equal(np.ascontiguousarray(out[1]).view(np.float32),
+                          np.ascontiguousarray(out[2]).view(np.float32))
+    ref = C.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
+    scale = np.abs(A.astype(np.complex128)) @ np.abs(B.astype(np.complex128))
+    assert np.max(np.abs(out[1] - ref) / scale) < 4e-5
+
+
 # n = 1,152: nine blocks of 128 columns; n = 450: a last block of 66 columns
 # (inner panels of 32, 32 and 2)
 @pytest.mark.parametrize("N,nmax", [(12, 6), (15, 3)])
@@ -65,7 +89,7 @@ def test_lu_mixed_with_and_without_tensor_cores(G, ctx, N, nmax):
     ref = G.wavelength_solve(ctx, sp, bg, wave, G.options(G.SOLVE_LU), G.C128)[0]
     opts = G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4)
     out = {}
-    for tc in (1, 0):
+    for tc in (1, 2, 0):
         ctx.tune(lu_tensor_cores=tc)
         xs, _, _, st = G.wavelength_solve(ctx, sp, bg, wave, opts, G.C64)
         out[tc] = (xs, st.iterations)
@@ -96,3 +120,33 @@ def test_lu_tall_panels(G, ctx):
                                       G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4), G.C64)
     assert st.rel_residual <= 1e-10
     assert np.max(np.abs(xs - ref) / np.abs(ref)) < 1e-6
+
+
+def test_cooperative_panels_give_the_same_factors(G, ctx):
+    """n = 9,600 (44 panels of 8,192 rows or more): the one-launch cooperative
+    panel (a grid-wide barrier per column, row interchanges kept in a table and
+    applied after the last column) takes the same operations per entry as the
+    two-launches-per-column panel, so both LU roles give bit-identical
+    solutions; and the persistent trailing update with cooperative panels
+    matches the one-CTA-per-tile update with per-column panels bit for bit."""
+    rng = np.random.default_rng(35)
+    xyz, rad = random_cluster(rng, 200, 2600 * nm, 40 * nm, 60 * nm, 20 * nm)
+    sp = G.spheres_array(xyz, rad, (1.8 + 0.02j) ** 2, 4)     # P = 24: n = 9,600
+    bg, wave = G.medium(1.0), G.plane_wave(700 * nm)
+    out = {}
+    for mode in (1, 2):
+        ctx.tune(lu_tensor_cores=mode, lu_panel=mode)
+        pr = G.Problem(ctx, sp, bg, wave)
+        pr.source_vector(copy=False)
+        pr.assemble(G.FF, G.C128)
+        pr.solve(G.options(G.SOLVE_LU))
+        x64 = pr.coefficients()[0].copy()
+        pr.assemble(G.FF, G.C64)
+        st = pr.solve(G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4))
+        out[mode] = (x64, pr.coefficients()[0].copy(), st.iterations)
+        pr.close()
+    ctx.tune(lu_tensor_cores=1, lu_panel=1)
+    assert np.array_equal(out[1][0], out[2][0])
+    assert np.array_equal(out[1][1], out[2][1]) and out[1][2] == out[2][2]
+    assert np.max(np.abs(out[1][1] - out[1][0])) / np.max(np.abs(out[1][0])) < 1e-8
+
