@@ -843,7 +843,7 @@ def lu_mixed_arm(args):
     ref = pr.cross_sections()
     pr.close()
     pr = G.Problem(ctx, sp, G.medium(complex(w["host"]) ** 2), G.plane_wave(w["lam"]))
-    ctx.tune(lu_tensor_cores=args.lu_update)
+    ctx.tune(lu_tensor_cores=args.lu_update, lu_persistent=args.lu_persistent)
     opts = G.options(G.SOLVE_LU_MIXED, tol=1e-9, max_iter=30, restarts=4)
     times, st = [], None
     with ClockSampler(0) as clk:
@@ -867,7 +867,8 @@ def lu_mixed_arm(args):
     n = pr.n
     pr.close()
     ctx.close()
-    upd_bytes = 16.0 * sum((n - K) ** 2 for K in range(128, n, 128))  # C read + written, complex64
+    blk = 128 if args.lu_update else 32  # rank of the trailing updates
+    upd_bytes = 16.0 * sum((n - K) ** 2 for K in range(blk, n, blk))  # C read + written, complex64
     phases = {"factor_ms": ph["factor"][0], "panel_ms": ph["panel"][0], "panels": ph["panel"][1],
               "update_ms": ph["update"][0], "updates": ph["update"][1],
               "update_hbm_frac_of_measured": upd_bytes / (ph["update"][0] * 1e-3) / 1e9 / peaks()[0]
@@ -879,7 +880,10 @@ def lu_mixed_arm(args):
             "data": "synthetic (seeded)",
             "config": {"workload": "c2 LU role: " + w["desc"],
                        "solver": "GMRES-based iterative refinement: FP64 residuals, GMRES on the system left-preconditioned by the FP32 LU (tensor-core trailing updates), tol 1e-9",
-                       "trailing_update": {1: "persistent", 2: "one CTA per tile"}[args.lu_update]},
+                       "trailing_update": {1: "persistent", 2: "one CTA per tile",
+                                           0: "FP32 CUDA cores, rank 32"}[args.lu_update],
+                       "panels_and_sweeps": {1: "one launch per panel / sweep",
+                                             2: "per-column panel launches, per-block sweep launches"}[args.lu_persistent]},
             "refinement_iterations": st.iterations, "qext_rel_err_vs_fp64": err, "phases": phases,
             "clocks": clk.summary()}
 
@@ -1177,8 +1181,10 @@ def main():
     ap.add_argument("--c4-seconds", type=float, default=60.0)
     ap.add_argument("--batch-slots", type=int, default=6, help="server slots for c3 / c4")
     ap.add_argument("--c4-forms", default="mixed,fp64", help="c4: forms to run (comma-separated)")
-    ap.add_argument("--lu-update", type=int, default=1, choices=[1, 2],
-                    help="c2lu: trailing-update kernel (1 persistent, 2 one CTA per tile)")
+    ap.add_argument("--lu-update", type=int, default=1, choices=[0, 1, 2],
+                    help="c2lu: trailing-update kernel (1 persistent, 2 one CTA per tile, 0 FP32 CUDA cores)")
+    ap.add_argument("--lu-persistent", type=int, default=1, choices=[1, 2],
+                    help="c2lu: panels and triangular sweeps (1 one launch each, 2 per column / per block)")
     ap.add_argument("--c4-batch-limit-gb", type=float, default=1.0,
                     help="c4: largest batched footprint of a request that is batched")
     ap.add_argument("--c4-batching", type=int, default=64,

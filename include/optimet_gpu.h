@@ -143,9 +143,11 @@ typedef struct {
   int assemble_rotation; /* complex64 assembly by rotated z-axis translations (one recurrence
                             chain per pair, FP32 rotation products): 1 (default) / 0 (the general
                             translation's 3 nMax + 1 chains per pair, FP32 block forming) */
-  int lu_panel;          /* LU panels of 8,192 rows or more: 1 (default) one cooperative launch
-                            per panel (a grid-wide barrier per column), 2 a pivot launch and an
-                            update launch per column */
+  int lu_persistent;     /* LU kernels: 1 (default) one cooperative launch per panel of 8,192
+                            rows or more (a grid-wide barrier per column) and one launch per
+                            triangular sweep (solved blocks published through flags); 2 a pivot
+                            launch and an update launch per panel column, one launch per
+                            32-row block of a triangular sweep */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any

@@ -437,8 +437,8 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
     ctx->mv_tma = t->matvec_tma ? 1 : 0;
   if(t->assemble_rotation >= 0)
     ctx->asm_rot = t->assemble_rotation ? 1 : 0;
-  if(t->lu_panel > 0)
-    ctx->lu_panel = std::min(t->lu_panel, 2);
+  if(t->lu_persistent > 0)
+    ctx->lu_persist = std::min(t->lu_persistent, 2);
   return OM_OK;
 }
 

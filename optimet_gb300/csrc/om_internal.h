@@ -121,9 +121,9 @@ struct om_context {
   // complex64 LU trailing updates on the tensor cores: 1 persistent kernel,
   // 2 one CTA per tile, 0 off (FP32 CUDA cores)
   int lu_tc = 1;
-  // LU panels of kTallPanel rows or more: 1 one cooperative launch per panel,
-  // 2 a pivot launch and an update launch per column
-  int lu_panel = 1;
+  // LU kernels: 1 one cooperative launch per tall panel and one launch per
+  // triangular sweep, 2 per-column panel launches and per-block sweep launches
+  int lu_persist = 1;
   int asm_rot = 1;  // precision-form assembly by rotated z-axis translations (assemble_rot.cu)
   size_t budget = 0;
   size_t used = 0;

@@ -631,13 +631,22 @@ struct InnerGmres32 : PrecondFn {
 // ---------------------------------------------------------------------------
 constexpr int kNb = 32;
 
+// The LU's complex products are written with explicit fused and unfused
+// operations, so that every kernel that forms the same entry rounds it the
+// same way (an expression such as a b - c d leaves the compiler free to fuse
+// either product, and it may choose differently in different kernels).
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
 template <typename V> __device__ __forceinline__ double mag2(V a) {
-  return (double)a.x * a.x + (double)a.y * a.y;
+  return fma((double)a.x, (double)a.x, __dmul_rn((double)a.y, (double)a.y));
 }
 template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
   V r;
-  r.x = a.x * b.x - a.y * b.y;
-  r.y = a.x * b.y + a.y * b.x;
+  r.x = fma(a.x, b.x, -mul_rn(a.y, b.y));
+  r.y = fma(a.x, b.y, mul_rn(a.y, b.x));
   return r;
 }
 template <typename V> __device__ __forceinline__ V make_neg(V a) {
@@ -646,7 +655,7 @@ template <typename V> __device__ __forceinline__ V make_neg(V a) {
   return a;
 }
 template <typename V> __device__ __forceinline__ V crecip(V a) {
-  double d = (double)a.x * a.x + (double)a.y * a.y;
+  const double d = mag2(a);
   V r;
   r.x = a.x / d;
   r.y = -a.y / d;
@@ -669,8 +678,8 @@ __device__ __forceinline__ void panel_row_update(V *A, long ld, long k, long i, 
     for(int q = 0; q < 8; ++q)
       if(j0 + q < nb) {
         const V uu = u[j0 + q];
-        a[q].x -= l.x * uu.x - l.y * uu.y;
-        a[q].y -= l.x * uu.y + l.y * uu.x;
+        a[q].x = sub_rn(a[q].x, fma(l.x, uu.x, -mul_rn(l.y, uu.y)));
+        a[q].y = sub_rn(a[q].y, fma(l.x, uu.y, mul_rn(l.y, uu.x)));
         A[(k + j0 + q) * ld + i] = a[q];
       }
   }
@@ -1319,6 +1328,203 @@ __global__ void __launch_bounds__(256) k_tri_block(const V *A, long ld, long k, 
   }
 }
 
+// A whole triangular sweep in one launch. CTA b owns the 32-row blocks
+// r = b, b + G, b + 2G, ... (G CTAs); its seven compute warps take the owned
+// blocks in turn (local block q to warp q % 8) and keep their running values
+// in shared memory. A warp walks the sweep's column blocks in order: once
+// block j's solution is published it applies that block's columns to each of
+// its rows still to be solved (the next one to be solved first), and when a
+// block has received every column it needs, the warp solves its diagonal
+// block and publishes the solution (the values to dst, then flags[j] = this
+// sweep's epoch). An eighth warp polls the flags in sweep order and counts the
+// published blocks in shared memory for the others. Every row takes the same
+// operations in the same order as with k_tri_block (one launch per block),
+// so the results are the same bits. The epoch (sync[0]) is read at the start
+// and moved on by the last CTA to finish, so a captured sweep replays. Waits
+// are bounded by a clock budget; on time-out the kernel raises *err, and a
+// sweep that starts with *err raised does nothing.
+constexpr int kSweepWarps = 7;
+constexpr int kSweepThreads = 32 * (kSweepWarps + 1);
+
+__device__ __forceinline__ bool clock_wait_expired(long long t0) {
+  return clock64() - t0 > (1LL << 32);  // about two seconds
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long ld, long n, const V *src, V *dst,
+                                                             int upper, const V *dinv, unsigned *flags,
+                                                             unsigned *sync, int *err) {
+  extern __shared__ __align__(16) unsigned char sweep_sm[];
+  V *vals = reinterpret_cast<V *>(sweep_sm);
+  __shared__ volatile int ready;    // sweep steps whose solution is published
+  __shared__ volatile int abort_s;
+  __shared__ unsigned epoch_s;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long nblk = (n + kNb - 1) / kNb;
+  const long G = gridDim.x, b = blockIdx.x;
+  const int ob = (int)((nblk - b + G - 1) / G);  // owned blocks r = b + q G, q < ob
+  if(threadIdx.x == 0) {
+    ready = 0;
+    abort_s = *(volatile int *)err;
+    epoch_s = *(volatile unsigned *)sync;
+  }
+  __syncthreads();
+  const unsigned epoch = epoch_s;
+  // sweep step of column block j, and the block solved at step s
+  auto step_of = [&](long j) { return upper ? nblk - 1 - j : j; };
+  auto solve_publish = [&](int q) {
+    const long r = b + q * G, kk = r * kNb;
+    const int nbr = (int)min((long)kNb, n - kk);
+    V v = vals[q * kNb + lane];
+    V a[kNb];
+#pragma unroll
+    for(int c = 0; c < kNb; ++c)
+      if(c < nbr && lane < nbr)
+        a[c] = A[(kk + c) * ld + kk + lane];
+    // (fully unrolled over kNb columns so that a[] stays in registers; the
+    // columns past nbr change nothing)
+    if(!upper) {
+#pragma unroll
+      for(int c = 0; c < kNb; ++c) {
+        const V xc = shfl_v(v, c);
+        if(lane > c && lane < nbr)
+          v = cfma(a[c], make_neg(xc), v);
+      }
+    } else {
+      V dl;
+      dl.x = dl.y = 0;
+      if(lane < nbr)
+        dl = dinv[kk + lane];
+#pragma unroll
+      for(int c = kNb - 1; c >= 0; --c) {
+        if(lane == c && c < nbr)
+          v = cmul(v, dl);
+        const V xc = shfl_v(v, c);
+        if(lane < c && c < nbr)
+          v = cfma(a[c], make_neg(xc), v);
+      }
+    }
+    if(lane < nbr)
+      dst[kk + lane] = v;
+    __threadfence();
+    __syncwarp();
+    if(lane == 0)
+      atomicExch(flags + r, epoch);
+  };
+  if(!abort_s && warp == kSweepWarps) {
+    // the poller: steps this CTA still needs (forward: the columns left of its
+    // last block; backward: those right of its first block)
+    const long need = upper ? nblk - 1 - b : b + (long)(ob - 1) * G;
+    if(lane == 0) {
+      for(long st = 0; st < need; ++st) {
+        const long j = upper ? nblk - 1 - st : st;
+        const long long t0 = clock64();
+        bool ok = true;
+        while(*(volatile unsigned *)(flags + j) != epoch) {
+          if(abort_s || *(volatile int *)err || clock_wait_expired(t0)) {
+            ok = false;
+            break;
+          }
+        }
+        if(!ok) {
+          atomicExch(err, 1);
+          abort_s = 1;
+          break;
+        }
+        __threadfence();
+        ready = (int)(st + 1);
+      }
+    }
+  } else if(!abort_s && warp < kSweepWarps) {
+    for(int q = warp; q < ob; q += kSweepWarps) {
+      const long row = (b + q * G) * kNb + lane;
+      V v;
+      v.x = v.y = 0;
+      if(row < n)
+        v = src[row];
+      vals[q * kNb + lane] = v;
+    }
+    __syncwarp();
+    // this warp's blocks in the order they become ready
+    const int nq = ob > warp ? (ob - warp + kSweepWarps - 1) / kSweepWarps : 0;
+    auto qi = [&](int t) { return upper ? warp + (nq - 1 - t) * kSweepWarps : warp + t * kSweepWarps; };
+    int first = 0;  // the warp's blocks before `first` are solved
+    if(nq > 0 && step_of(b + qi(0) * G) == 0) {  // the sweep's first block
+      solve_publish(qi(0));
+      first = 1;
+    }
+    for(long st = 0; first < nq; ++st) {
+      const long j = upper ? nblk - 1 - st : st;
+      // wait for block j's solution
+      const long long t0 = clock64();
+      bool ok = true;
+      while(ready <= st) {
+        if(abort_s || clock_wait_expired(t0)) {
+          ok = false;
+          break;
+        }
+        __nanosleep(20);
+      }
+      if(!__all_sync(0xffffffffu, ok)) {
+        if(lane == 0) {
+          atomicExch(err, 1);
+          abort_s = 1;
+        }
+        break;
+      }
+      __threadfence_block();
+      const long k = j * kNb;
+      const int nbj = (int)min((long)kNb, n - k);
+      V xl;
+      xl.x = xl.y = 0;
+      if(lane < nbj)
+        xl = __ldcg(dst + k + lane);
+      for(int t = first; t < nq; ++t) {
+        const int q = qi(t);
+        const long r = b + q * G, i = r * kNb + lane;
+        // (every lane takes part in the shuffles; rows past n stay unused)
+        V v = vals[q * kNb + lane];
+        if(nbj == kNb) {  // two halves of 16 loads issued together
+#pragma unroll
+          for(int h = 0; h < kNb; h += kNb / 2) {
+            V a[kNb / 2];
+#pragma unroll
+            for(int c = 0; c < kNb / 2; ++c) {
+              a[c].x = a[c].y = 0;
+              if(i < n)
+                a[c] = A[(k + h + c) * ld + i];
+            }
+#pragma unroll
+            for(int c = 0; c < kNb / 2; ++c)
+              v = cfma(a[c], make_neg(shfl_v(xl, h + c)), v);
+          }
+        } else {
+          for(int c = 0; c < nbj; ++c) {
+            const V xc = shfl_v(xl, c);
+            if(i < n)
+              v = cfma(A[(k + c) * ld + i], make_neg(xc), v);
+          }
+        }
+        vals[q * kNb + lane] = v;
+        __syncwarp();
+        if(step_of(r) == st + 1) {  // every column this block needs is in
+          solve_publish(q);
+          ++first;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if(threadIdx.x == 0) {  // the last CTA out moves the epoch on
+    __threadfence();
+    if(atomicAdd(sync + 1, 1u) == (unsigned)G - 1) {
+      sync[1] = 0;
+      __threadfence();
+      atomicAdd(sync, 1u);
+    }
+  }
+}
+
 // Complex64 LU with tensor-core updates, blocked in two levels (the order of
 // LAPACK's blocked getrf): each block of kTcBlock columns is factored as a
 // tall panel, in panels of kNb columns whose interchanges and updates stay
@@ -1396,7 +1602,7 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   // CTAs of one cooperative panel launch: one per SM, as many as can be
   // resident at once
   int coop_grid = 0;
-  if(ctx->lu_panel == 1 && n >= kTallPanel) {
+  if(ctx->lu_persist == 1 && n >= kTallPanel) {
     int per_sm = 0, coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
     if(coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pan_coop<V>, kPanThreads, 0) ==
@@ -1483,10 +1689,34 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
 // from k_lu_diag_inv; y: n entries of scratch. 2 + 2 ceil(n / kNb) launches,
 // all stream-ordered (capturable as a graph): y = P b, the forward solve from
 // y into b, the backward solve from b into y, and y copied back to b.
+// Workspace of the one-launch sweeps: flags (one per 32-row block, set to
+// all ones) and the epoch / finished-CTA pair.
+inline size_t sweep_ws_words(long n) { return (size_t)((n + kNb - 1) / kNb) + 2; }
+inline void sweep_ws_init(om_context *ctx, unsigned *ws, long n) {
+  const size_t nblk = (size_t)((n + kNb - 1) / kNb);
+  cudaMemsetAsync(ws, 0xFF, nblk * sizeof(unsigned), ctx->stream);
+  cudaMemsetAsync(ws + nblk, 0, 2 * sizeof(unsigned), ctx->stream);
+}
+
 template <typename V>
-int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, const V *dinv, V *b, V *y) {
+int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, const V *dinv, V *b, V *y,
+                 unsigned *sweep_ws = nullptr, int *err = nullptr) {
   k_lu_gather<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(b, y, perm, n);
   int launches = 1;
+  if(ctx->lu_persist == 1 && sweep_ws && err) {
+    const long nblk = (n + kNb - 1) / kNb;
+    const long G = std::min<long>(ctx->sm_count, nblk);
+    const size_t smem = sizeof(V) * kNb * (size_t)((nblk + G - 1) / G);
+    unsigned *flags = sweep_ws, *sync = sweep_ws + nblk;
+    if(smem > 48 * 1024)
+      cudaFuncSetAttribute(k_tri_sweep<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_tri_sweep<V><<<(unsigned)G, kSweepThreads, smem, ctx->stream>>>(A, n, n, y, b, 0, dinv, flags, sync, err);
+    k_tri_sweep<V><<<(unsigned)G, kSweepThreads, smem, ctx->stream>>>(A, n, n, b, y, 1, dinv, flags, sync, err);
+    k_scale_copy<V, V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(y, 1.0, b, n);
+    launches += 3;
+    ctx->last_launches += launches;
+    return launches;
+  }
   for(long k = 0; k < n; k += kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
     const long rows = n - k - nb;
@@ -1519,7 +1749,8 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   }
   Work w;
   w.ctx = ctx;
-  size_t bytes = sizeof(double2) * ((size_t)n * n + 2 * n) + sizeof(int) * (2 * n + 2) + 2048;
+  size_t bytes = sizeof(double2) * ((size_t)n * n + 2 * n) + sizeof(int) * (2 * n + 2) +
+                 sizeof(unsigned) * sweep_ws_words(n) + 2048;
   int rc = alloc_work(ctx, w, bytes);
   if(rc)
     return rc;
@@ -1530,6 +1761,8 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   int *info = w.take<int>(2, off);
   int *perm = w.take<int>(n, off);
   double2 *dinv = w.take<double2>(n, off);
+  unsigned *sweep = w.take<unsigned>(sweep_ws_words(n), off);
+  sweep_ws_init(ctx, sweep, n);
   cudaMemcpyAsync(A, pr->d_S[harmonic], sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToDevice,
                   ctx->stream);
   rc = lu_factor<double2>(ctx, A, n, piv, info);
@@ -1541,13 +1774,13 @@ int solve_lu_rhs(om_problem *pr, int harmonic, const double2 *b, double2 *x, om_
   ctx->last_launches++;
   cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->stream);
   timer_begin(ctx, ctx->ev_lus);
-  lu_solve_vec<double2>(ctx, A, n, perm, dinv, x, y);
+  lu_solve_vec<double2>(ctx, A, n, perm, dinv, x, y, sweep, info + 1);
   timer_end(ctx, ctx->ev_lus);
   int hinfo[2] = {0, 0};
   cudaMemcpyAsync(hinfo, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
   if(hinfo[1]) {
-    ctx->err = "LU panel barrier timed out";
+    ctx->err = "LU kernel wait timed out (panel barrier or triangular sweep)";
     return OM_ERR_CUDA;
   }
   if(hinfo[0]) {
@@ -1621,6 +1854,7 @@ struct LuPrecond32 : PrecondFn {
   Work w;
   float2 *A = nullptr, *v32 = nullptr, *y32 = nullptr, *dinv = nullptr;
   int *piv = nullptr, *info = nullptr, *perm = nullptr;
+  unsigned *sweep = nullptr;  // flags and epoch of the one-launch triangular sweeps
   int applied = 0;
   // the triangular solves on v32, captured once as a graph and replayed
   cudaGraphExec_t solve_graph = nullptr;
@@ -1631,7 +1865,8 @@ struct LuPrecond32 : PrecondFn {
       cudaGraphExecDestroy(solve_graph);
   }
   int init(const float2 *S32) {
-    size_t bytes = sizeof(float2) * ((size_t)n * n + 3 * n) + sizeof(int) * (2 * n + 2) + 2048;
+    size_t bytes = sizeof(float2) * ((size_t)n * n + 3 * n) + sizeof(int) * (2 * n + 2) +
+                   sizeof(unsigned) * sweep_ws_words(n) + 2048;
     int rc = alloc_work(ctx, w, bytes);
     if(rc)
       return rc;
@@ -1643,6 +1878,8 @@ struct LuPrecond32 : PrecondFn {
     info = w.take<int>(2, off);
     perm = w.take<int>(n, off);
     dinv = w.take<float2>(n, off);
+    sweep = w.take<unsigned>(sweep_ws_words(n), off);
+    sweep_ws_init(ctx, sweep, n);
     cudaMemcpyAsync(A, S32, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, ctx->stream);
     rc = lu_factor<float2>(ctx, A, n, piv, info);
     if(rc)
@@ -1668,7 +1905,7 @@ struct LuPrecond32 : PrecondFn {
     cudaGraph_t g = nullptr;
     if(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const int before = ctx->last_launches;
-      solve_launches = lu_solve_vec<float2>(ctx, A, n, perm, dinv, v32, y32);
+      solve_launches = lu_solve_vec<float2>(ctx, A, n, perm, dinv, v32, y32, sweep, info + 1);
       ctx->last_launches = before;
       if(cudaStreamEndCapture(ctx->stream, &g) != cudaSuccess ||
          cudaGraphInstantiate(&solve_graph, g, 0) != cudaSuccess)
@@ -1686,7 +1923,7 @@ struct LuPrecond32 : PrecondFn {
       cudaGraphLaunch(solve_graph, ctx->stream);
       ctx->last_launches += solve_launches;
     } else {
-      lu_solve_vec<float2>(ctx, A, n, perm, dinv, v32, y32);
+      lu_solve_vec<float2>(ctx, A, n, perm, dinv, v32, y32, sweep, info + 1);
     }
     timer_end(ctx, ctx->ev_lus);
     k_scale_copy<float2, double2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(v32, 1.0, z, n);
@@ -1785,6 +2022,13 @@ int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, 
     st->iterations = ref;
     st->inner_iterations = inner;
     st->rel_residual = rr;
+  }
+  int sweep_err = 0;  // a triangular sweep's wait timed out
+  cudaMemcpyAsync(&sweep_err, lu.info + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  if(sweep_err) {
+    ctx->err = "LU triangular sweep wait timed out";
+    return OM_ERR_CUDA;
   }
   if(rr > o->tol) {
     ctx->err = "LU-preconditioned refinement did not reach the requested tolerance";

@@ -122,6 +122,35 @@ def test_lu_tall_panels(G, ctx):
     assert np.max(np.abs(xs - ref) / np.abs(ref)) < 1e-6
 
 
+@pytest.mark.parametrize("N,nmax", [(15, 3), (12, 6), (40, 5)])
+def test_one_launch_sweeps_match_block_launches(G, ctx, N, nmax):
+    """The one-launch triangular sweeps (blocks published through flags)
+    against one launch per 32-row block: the same bits for the FP64 LU role
+    and the LU refinement role; n = 450 ends in a partial block, n = 1,152
+    leaves most CTAs one block, n = 2,800 (88 blocks) gives some CTAs two."""
+    rng = np.random.default_rng(N + nmax)
+    xyz, rad = random_cluster(rng, N, 900 * nm * max(1, N // 15), 40 * nm, 70 * nm, 20 * nm)
+    sp = G.spheres_array(xyz, rad, (2.5 + 0.05j) ** 2, nmax)
+    bg, wave = G.medium(1.0), G.plane_wave(600 * nm)
+    out = {}
+    for mode in (1, 2):
+        ctx.tune(lu_persistent=mode)
+        pr = G.Problem(ctx, sp, bg, wave)
+        pr.source_vector(copy=False)
+        pr.assemble(G.FF, G.C128)
+        pr.solve(G.options(G.SOLVE_LU))
+        x64 = pr.coefficients()[0].copy()
+        pr.assemble(G.FF, G.C64)
+        # twice, so that the captured sweeps replay with a new epoch
+        for _ in range(2):
+            st = pr.solve(G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4))
+        out[mode] = (x64, pr.coefficients()[0].copy(), st.iterations)
+        pr.close()
+    ctx.tune(lu_persistent=1)
+    assert np.array_equal(out[1][0], out[2][0])
+    assert np.array_equal(out[1][1], out[2][1]) and out[1][2] == out[2][2]
+
+
 def test_cooperative_panels_give_the_same_factors(G, ctx):
     """n = 9,600 (44 panels of 8,192 rows or more): the one-launch cooperative
     panel (a grid-wide barrier per column, row interchanges kept in a table and
@@ -135,7 +164,7 @@ def test_cooperative_panels_give_the_same_factors(G, ctx):
     bg, wave = G.medium(1.0), G.plane_wave(700 * nm)
     out = {}
     for mode in (1, 2):
-        ctx.tune(lu_tensor_cores=mode, lu_panel=mode)
+        ctx.tune(lu_tensor_cores=mode, lu_persistent=mode)
         pr = G.Problem(ctx, sp, bg, wave)
         pr.source_vector(copy=False)
         pr.assemble(G.FF, G.C128)
@@ -145,7 +174,7 @@ def test_cooperative_panels_give_the_same_factors(G, ctx):
         st = pr.solve(G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4))
         out[mode] = (x64, pr.coefficients()[0].copy(), st.iterations)
         pr.close()
-    ctx.tune(lu_tensor_cores=1, lu_panel=1)
+    ctx.tune(lu_tensor_cores=1, lu_persistent=1)
     assert np.array_equal(out[1][0], out[2][0])
     assert np.array_equal(out[1][1], out[2][1]) and out[1][2] == out[2][2]
     assert np.max(np.abs(out[1][1] - out[1][0])) / np.max(np.abs(out[1][0])) < 1e-8
