@@ -147,7 +147,8 @@ typedef struct {
                             rows or more (a grid-wide barrier per column) and one launch per
                             triangular sweep (solved blocks published through flags); 2 a pivot
                             launch and an update launch per panel column, one launch per
-                            32-row block of a triangular sweep */
+                            32-row block of a triangular sweep; 3 as 1 with the panel's rows
+                            kept in global memory rather than shared memory */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any

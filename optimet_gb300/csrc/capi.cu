@@ -438,7 +438,7 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
   if(t->assemble_rotation >= 0)
     ctx->asm_rot = t->assemble_rotation ? 1 : 0;
   if(t->lu_persistent > 0)
-    ctx->lu_persist = std::min(t->lu_persistent, 2);
+    ctx->lu_persist = std::min(t->lu_persistent, 3);
   return OM_OK;
 }
 

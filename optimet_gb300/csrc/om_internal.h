@@ -121,8 +121,10 @@ struct om_context {
   // complex64 LU trailing updates on the tensor cores: 1 persistent kernel,
   // 2 one CTA per tile, 0 off (FP32 CUDA cores)
   int lu_tc = 1;
-  // LU kernels: 1 one cooperative launch per tall panel and one launch per
-  // triangular sweep, 2 per-column panel launches and per-block sweep launches
+  // LU kernels: 1 one cooperative launch per tall panel (its rows in shared
+  // memory when they fit) and one launch per triangular sweep, 2 per-column
+  // panel launches and per-block sweep launches, 3 as 1 with the panel rows
+  // always in global memory
   int lu_persist = 1;
   int asm_rot = 1;  // precision-form assembly by rotated z-axis translations (assemble_rot.cu)
   size_t budget = 0;
@@ -289,6 +291,9 @@ void batch_release(om_context *ctx);
 
 // tma_matvec.cu: complex64 matvec with TMA-staged matrix tiles; false when the
 // tensor map cannot be encoded
+// cuTensorMapEncodeTiled through the runtime's driver entry point (nullptr
+// when the driver does not provide it)
+void *tensor_map_encoder();
 bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *part, int row_tiles,
                        long tiles, int cols, unsigned grid);
 

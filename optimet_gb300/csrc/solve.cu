@@ -1124,6 +1124,201 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop(V *A, long ld, long n,
   }
 }
 
+// The cooperative panel with each CTA's rows held in shared memory for the
+// whole panel: CTA b takes the contiguous rows k + b R .. k + (b + 1) R - 1
+// (R = ceil((n - k) / G)), all nb columns of them, and writes them back after
+// the last column. Besides its partial maximum a CTA publishes the row that
+// holds it (its current values, all nb columns) in cand[b], so that after the
+// barrier every CTA takes the pivot row from the winning CTA's slot: one
+// grid-wide barrier and two small reads per column, no global traffic on the
+// panel itself. The entries take the operations of k_lu_panel, in the same
+// order, so the factors are the same bits.
+template <typename V>
+__global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long n, long k, int nb, int *piv,
+                                                             int *info, PanelScratch ps, V *cand,
+                                                             unsigned *bar, unsigned bar_base, int *err) {
+  extern __shared__ __align__(16) unsigned char pan_sm[];
+  __shared__ V u[kNb];
+  __shared__ PanelPerm pm;
+  __shared__ double wv[kPanThreads / 32];
+  __shared__ long wi[kPanThreads / 32];
+  __shared__ int wl[kPanThreads / 32];
+  __shared__ long p_s;
+  __shared__ double pv_s;
+  __shared__ int rl_s, wb_s;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const long G = gridDim.x, b = blockIdx.x;
+  const long R = (n - k + G - 1) / G, r0 = k + b * R, r1 = min(n, r0 + R);
+  const int nr = (int)max(0L, r1 - r0);
+  V *P = reinterpret_cast<V *>(pan_sm);                              // P[c R + rl]
+  unsigned char *retired = pan_sm + sizeof(V) * (size_t)nb * R;    // per local row
+  if(*(volatile int *)err)
+    return;
+  if(t == 0)
+    pm.cnt = 0;
+  for(int c = 0; c < nb; ++c)
+    for(int rl = t; rl < nr; rl += kPanThreads)
+      P[c * R + rl] = A[(k + c) * ld + r0 + rl];
+  for(int rl = t; rl < nr; rl += kPanThreads)
+    retired[rl] = 0;
+  __syncthreads();
+  // partial maximum of column c over the active local rows (positions for
+  // ties), and the row holding it published in cand[b]
+  auto partial_max = [&](int c) {
+    double bv = -1.0;
+    long bp = k + c;
+    int bl = -1;
+    for(int rl = t; rl < nr; rl += kPanThreads) {
+      if(retired[rl])
+        continue;
+      const double v = mag2(P[c * R + rl]);
+      if(v >= bv) {
+        const long pos = perm_pos(pm, r0 + rl);
+        if(v > bv || pos < bp) {
+          bv = v;
+          bp = pos;
+          bl = rl;
+        }
+      }
+    }
+#pragma unroll
+    for(int h = 16; h > 0; h >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, bv, h);
+      const long op = __shfl_xor_sync(0xffffffffu, bp, h);
+      const int ol = __shfl_xor_sync(0xffffffffu, bl, h);
+      if(ov > bv || (ov == bv && op < bp)) {
+        bv = ov;
+        bp = op;
+        bl = ol;
+      }
+    }
+    if(lane == 0) {
+      wv[wid] = bv;
+      wi[wid] = bp;
+      wl[wid] = bl;
+    }
+    __syncthreads();
+    if(t == 0) {
+      for(int w = 1; w < kPanThreads / 32; ++w)
+        if(wv[w] > bv || (wv[w] == bv && wi[w] < bp)) {
+          bv = wv[w];
+          bp = wi[w];
+          bl = wl[w];
+        }
+      ps.bestv[b] = bv;
+      ps.besti[b] = bp;
+      rl_s = bl;
+    }
+    __syncthreads();
+    if(t < nb && rl_s >= 0)
+      cand[b * kNb + t] = P[t * R + rl_s];
+  };
+  partial_max(0);
+  unsigned target = bar_base;
+  for(int c = 0; c < nb; ++c) {
+    const long col = k + c;
+    target += (unsigned)G;
+    if(!grid_barrier(bar, target, err))
+      return;
+    {
+      double bv = -2.0;
+      long bp = col;
+      int bw = 0;
+      for(long w = t; w < G; w += kPanThreads) {
+        const double v = __ldcg(ps.bestv + w);
+        const long i = __ldcg(ps.besti + w);
+        if(v > bv || (v == bv && i < bp)) {
+          bv = v;
+          bp = i;
+          bw = (int)w;
+        }
+      }
+#pragma unroll
+      for(int h = 16; h > 0; h >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, bv, h);
+        const long op = __shfl_xor_sync(0xffffffffu, bp, h);
+        const int ow = __shfl_xor_sync(0xffffffffu, bw, h);
+        if(ov > bv || (ov == bv && op < bp)) {
+          bv = ov;
+          bp = op;
+          bw = ow;
+        }
+      }
+      if(lane == 0) {
+        wv[wid] = bv;
+        wi[wid] = bp;
+        wl[wid] = bw;
+      }
+      __syncthreads();
+      if(t == 0) {
+        for(int w = 1; w < kPanThreads / 32; ++w)
+          if(wv[w] > bv || (wv[w] == bv && wi[w] < bp)) {
+            bv = wv[w];
+            bp = wi[w];
+            bw = wl[w];
+          }
+        if(b == 0) {
+          piv[col] = (int)bp;
+          if(bv <= 0.0 && *info == 0)
+            *info = (int)col + 1;
+        }
+        const long a = perm_row(pm, col), pr = perm_row(pm, bp);
+        if(bp != col) {
+          perm_set(pm, col, pr);
+          perm_set(pm, bp, a);
+        }
+        if(pr >= r0 && pr < r1)
+          retired[pr - r0] = 1;
+        p_s = pr;
+        pv_s = bv;
+        wb_s = bw;
+      }
+      __syncthreads();
+    }
+    if(t < nb)
+      u[t] = __ldcg(cand + (long)wb_s * kNb + t);
+    __syncthreads();
+    if(pv_s > 0.0) {
+      const V inv = crecip(u[c]);
+      for(int rl = t; rl < nr; rl += kPanThreads) {
+        if(retired[rl])
+          continue;
+        const V l = cmul(P[c * R + rl], inv);
+        P[c * R + rl] = l;
+        for(int j = c + 1; j < nb; ++j) {
+          const V uu = u[j];
+          V a = P[j * R + rl];
+          a.x = sub_rn(a.x, fma(l.x, uu.x, -mul_rn(l.y, uu.y)));
+          a.y = sub_rn(a.y, fma(l.x, uu.y, mul_rn(l.y, uu.x)));
+          P[j * R + rl] = a;
+        }
+      }
+    }
+    __syncthreads();
+    if(c + 1 < nb)
+      partial_max(c + 1);
+  }
+  // the rows back in place, then (CTA 0, after every CTA's rows are out) the
+  // touched rows of the panel's columns to their final positions
+  for(int c = 0; c < nb; ++c)
+    for(int rl = t; rl < nr; rl += kPanThreads)
+      A[(k + c) * ld + r0 + rl] = P[c * R + rl];
+  target += (unsigned)G;
+  if(!grid_barrier(bar, target, err) || b != 0)
+    return;
+  V *tmp = P;  // [2 kNb][kNb], the shared rows are written back
+  const int cnt = pm.cnt;
+  for(int idx = t; idx < cnt * nb; idx += kPanThreads) {
+    const int e = idx / nb, j = idx - e * nb;
+    tmp[e * kNb + j] = __ldcg(A + (k + j) * ld + pm.row[e]);
+  }
+  __syncthreads();
+  for(int idx = t; idx < cnt * nb; idx += kPanThreads) {
+    const int e = idx / nb, j = idx - e * nb;
+    A[(k + j) * ld + pm.pos[e]] = tmp[e * kNb + j];
+  }
+}
+
 // Apply the row interchanges of rows k .. k + nb - 1 (in order) to the
 // columns jlo .. jhi - 1 other than slo .. shi - 1 (the panel's own columns,
 // which the panel kernels swap themselves).
@@ -1372,15 +1567,21 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
   const unsigned epoch = epoch_s;
   // sweep step of column block j, and the block solved at step s
   auto step_of = [&](long j) { return upper ? nblk - 1 - j : j; };
-  auto solve_publish = [&](int q) {
-    const long r = b + q * G, kk = r * kNb;
+  // the diagonal block of local block q (lane: its row), loaded into a[]
+  auto load_diag = [&](int q, V(&a)[kNb]) {
+    const long kk = (b + q * G) * kNb;
     const int nbr = (int)min((long)kNb, n - kk);
-    V v = vals[q * kNb + lane];
-    V a[kNb];
 #pragma unroll
     for(int c = 0; c < kNb; ++c)
       if(c < nbr && lane < nbr)
         a[c] = A[(kk + c) * ld + kk + lane];
+  };
+  auto solve_publish = [&](int q, V(&a)[kNb], bool loaded) {
+    const long r = b + q * G, kk = r * kNb;
+    const int nbr = (int)min((long)kNb, n - kk);
+    V v = vals[q * kNb + lane];
+    if(!loaded)
+      load_diag(q, a);
     // (fully unrolled over kNb columns so that a[] stays in registers; the
     // columns past nbr change nothing)
     if(!upper) {
@@ -1450,16 +1651,36 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
     auto qi = [&](int t) { return upper ? warp + (nq - 1 - t) * kSweepWarps : warp + t * kSweepWarps; };
     int first = 0;  // the warp's blocks before `first` are solved
     if(nq > 0 && step_of(b + qi(0) * G) == 0) {  // the sweep's first block
-      solve_publish(qi(0));
+      V dg[kNb];
+      solve_publish(qi(0), dg, false);
       first = 1;
     }
     for(long st = 0; first < nq; ++st) {
       const long j = upper ? nblk - 1 - st : st;
+      const long k = j * kNb;
+      const int nbj = (int)min((long)kNb, n - k);
+      // The next block to be solved (the first unsolved one) is on the
+      // critical path: its tile of column block j, and its diagonal block
+      // when it is solved at this step (complex64: registers allow both), are
+      // loaded before block j's solution is in.
+      const int t0 = first, q0 = qi(t0);
+      const long r0c = b + q0 * G, i0 = r0c * kNb + lane;
+      const bool solve0 = step_of(r0c) == st + 1;
+      V a0[kNb], dg[kNb];
+#pragma unroll
+      for(int c = 0; c < kNb; ++c) {
+        a0[c].x = a0[c].y = 0;
+        if(c < nbj && i0 < n)
+          a0[c] = A[(k + c) * ld + i0];
+      }
+      constexpr bool kPreDiag = sizeof(V) == 8;
+      if(kPreDiag && solve0)
+        load_diag(q0, dg);
       // wait for block j's solution
-      const long long t0 = clock64();
+      const long long w0 = clock64();
       bool ok = true;
       while(ready <= st) {
-        if(abort_s || clock_wait_expired(t0)) {
+        if(abort_s || clock_wait_expired(w0)) {
           ok = false;
           break;
         }
@@ -1473,13 +1694,27 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
         break;
       }
       __threadfence_block();
-      const long k = j * kNb;
-      const int nbj = (int)min((long)kNb, n - k);
       V xl;
       xl.x = xl.y = 0;
       if(lane < nbj)
         xl = __ldcg(dst + k + lane);
-      for(int t = first; t < nq; ++t) {
+      {
+        V v = vals[q0 * kNb + lane];
+#pragma unroll
+        for(int c = 0; c < kNb; ++c) {
+          const V xc = shfl_v(xl, c);
+          if(c < nbj && i0 < n)
+            v = cfma(a0[c], make_neg(xc), v);
+        }
+        vals[q0 * kNb + lane] = v;
+        __syncwarp();
+        if(solve0) {  // every column this block needs is in
+          solve_publish(q0, dg, kPreDiag);
+          ++first;
+        }
+      }
+      // the warp's other blocks (none of them is complete at this step)
+      for(int t = t0 + 1; t < nq; ++t) {
         const int q = qi(t);
         const long r = b + q * G, i = r * kNb + lane;
         // (every lane takes part in the shuffles; rows past n stay unused)
@@ -1507,10 +1742,6 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
         }
         vals[q * kNb + lane] = v;
         __syncwarp();
-        if(step_of(r) == st + 1) {  // every column this block needs is in
-          solve_publish(q);
-          ++first;
-        }
       }
     }
   }
@@ -1596,18 +1827,32 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
     if(ctx->lu_tc && n > kTcBlock)
       split_bytes = cgemm_sub_tc_split_bytes(n, n, (int)kTcBlock);
   const size_t pan_bytes =
-      n >= kTallPanel ? maxblk * (sizeof(double) + sizeof(long)) + kNb * sizeof(V) + 4 * 256 : 0;
+      n >= kTallPanel ? maxblk * (sizeof(double) + sizeof(long) + kNb * sizeof(V)) + kNb * sizeof(V) + 5 * 256
+                      : 0;
   void *split = nullptr;
   unsigned *bar = nullptr, bar_base = 0;  // the cooperative panels' barrier counter
-  // CTAs of one cooperative panel launch: one per SM, as many as can be
-  // resident at once
+  V *cand = nullptr;                       // their per-CTA candidate pivot rows
+  // CTAs of one cooperative panel launch: one per SM. The panel's rows stay
+  // in shared memory when the tallest panel's share fits (coop_smem bytes).
   int coop_grid = 0;
-  if(ctx->lu_persist == 1 && n >= kTallPanel) {
+  size_t coop_smem = 0;
+  if(ctx->lu_persist != 2 && n >= kTallPanel) {
     int per_sm = 0, coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
-    if(coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pan_coop<V>, kPanThreads, 0) ==
-                   cudaSuccess)
+    const long R = (n + ctx->sm_count - 1) / ctx->sm_count;
+    const size_t sm = std::max(sizeof(V) * kNb * (size_t)R + (size_t)R, sizeof(V) * 2 * kNb * kNb);
+    if(coop && ctx->lu_persist == 1 && sm <= 220 * 1024 &&
+       cudaFuncSetAttribute(k_pan_coop_sm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
+           cudaSuccess &&
+       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pan_coop_sm<V>, kPanThreads, sm) ==
+           cudaSuccess &&
+       per_sm >= 1) {
+      coop_grid = ctx->sm_count;
+      coop_smem = sm;
+    } else if(coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pan_coop<V>, kPanThreads, 0) ==
+                          cudaSuccess) {
       coop_grid = std::min(per_sm, 1) * ctx->sm_count;
+    }
     cudaGetLastError();
   }
   if(pan_bytes + split_bytes) {
@@ -1620,6 +1865,7 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
       ps.besti = ws.take<long>(maxblk, off);
       ps.prow = ws.take<V>(kNb, off);
       bar = ws.take<unsigned>(1, off);
+      cand = ws.take<V>((size_t)maxblk * kNb, off);
       cudaMemsetAsync(bar, 0, sizeof(unsigned), ctx->stream);
     }
     if(split_bytes)
@@ -1631,11 +1877,23 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
     timer_begin(ctx, ctx->ev_lup);
     const long rows = n - k;
     if(rows >= kTallPanel && coop_grid > 0) {
-      ps.nblk = (int)std::min<long>(coop_grid, (rows + kPanThreads - 1) / kPanThreads);
       int *err = info + 1;
-      void *args[] = {&A, (void *)&n, (void *)&n, (void *)&k, (void *)&nb, &piv, &info, &ps, &bar, &bar_base, &err};
-      const cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_pan_coop<V>, dim3(ps.nblk),
-                                                        dim3(kPanThreads), args, 0, ctx->stream);
+      cudaError_t e;
+      if(coop_smem) {  // rows in shared memory
+        ps.nblk = coop_grid;
+        const long R = (rows + coop_grid - 1) / coop_grid;
+        const size_t sm = std::max(sizeof(V) * nb * (size_t)R + (size_t)R, sizeof(V) * 2 * kNb * kNb);
+        void *args[] = {&A, (void *)&n, (void *)&n, (void *)&k, (void *)&nb, &piv, &info, &ps, &cand, &bar,
+                        &bar_base, &err};
+        e = cudaLaunchCooperativeKernel((const void *)k_pan_coop_sm<V>, dim3(ps.nblk), dim3(kPanThreads), args,
+                                        sm, ctx->stream);
+      } else {
+        ps.nblk = (int)std::min<long>(coop_grid, (rows + kPanThreads - 1) / kPanThreads);
+        void *args[] = {&A, (void *)&n, (void *)&n, (void *)&k, (void *)&nb, &piv, &info, &ps, &bar, &bar_base,
+                        &err};
+        e = cudaLaunchCooperativeKernel((const void *)k_pan_coop<V>, dim3(ps.nblk), dim3(kPanThreads), args, 0,
+                                        ctx->stream);
+      }
       if(e == cudaSuccess) {
         bar_base += (unsigned)(nb + 1) * (unsigned)ps.nblk;
         ctx->last_launches++;
@@ -1703,7 +1961,7 @@ int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, const V *
                  unsigned *sweep_ws = nullptr, int *err = nullptr) {
   k_lu_gather<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(b, y, perm, n);
   int launches = 1;
-  if(ctx->lu_persist == 1 && sweep_ws && err) {
+  if(ctx->lu_persist != 2 && sweep_ws && err) {
     const long nblk = (n + kNb - 1) / kNb;
     const long G = std::min<long>(ctx->sm_count, nblk);
     const size_t smem = sizeof(V) * kNb * (size_t)((nblk + G - 1) / G);

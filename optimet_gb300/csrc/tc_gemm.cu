@@ -25,6 +25,7 @@
 // below).
 #include <algorithm>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -590,8 +591,8 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, 
 //              read from a shared-memory ring, C - AB stored to global;
 //   warp 4     operand copies (A when the row tile changes, B chunks);
 //   warp 5     TMEM allocation and the MMAs (one elected thread);
-//   warp 6     C copies: each tile's columns in groups of 16 (16 KB; one
-//              bulk copy per column) through a ring of three slots.
+//   warp 6     C copies: each tile's columns in groups of 16 (16 KB, one
+//              two-dimensional tensor copy) through a ring of three slots.
 // The accumulators (Ar Br, Ai Bi, Im: 3 x 64 TMEM columns) are double
 // buffered, so the epilogue of one tile runs under the MMAs of the next, and
 // the C ring keeps up to 48 KB of C reads in flight per SM. Every wait is
@@ -656,9 +657,17 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
                : "memory");
 }
 
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_addr(dst)),
+      "l"(tm), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
 __global__ void __launch_bounds__(kPThreads, 1)
-    k_cgemm_sub_tc3(const unsigned char *As, const unsigned char *Bs, int nq, float2 *C, long ldc,
-                    long m, long n, int *err) {
+    k_cgemm_sub_tc3(const unsigned char *As, const unsigned char *Bs, int nq,
+                    const __grid_constant__ CUtensorMap cmap, float2 *C, long ldc, long m, long n, int *err) {
   extern __shared__ __align__(1024) unsigned char psm[];
   PBars *bars = reinterpret_cast<PBars *>(psm + kPOffBar);
   volatile int *abort_flag = &bars->abort;
@@ -793,12 +802,12 @@ __global__ void __launch_bounds__(kPThreads, 1)
     mma_commit(&bars->drain);
     wait_phase(&bars->drain, 0u);
   } else if(warp == 6 && lane == 0) {
-    // C copies
+    // C copies: a 128 x 16 box per group (rows and columns past C's edge
+    // read as zeros and are not used)
     long cq = 0;
     for(long tile = t0; tile < t1 && !*abort_flag; ++tile) {
       const long rt = tile / nt, ct = tile - rt * nt;
       const long r0 = rt * kTcM, c0 = ct * kTcN;
-      const uint32_t rows = (uint32_t)min((long)kTcM, m - r0);
       bool stop = false;
       for(int g = 0; g < kTcN / 16; ++g, ++cq) {
         const int s = (int)(cq % kPCSlots);
@@ -807,12 +816,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
           stop = true;
           break;
         }
-        const long cg = c0 + 16 * g;
-        const int cols = (int)max(0L, min(16L, n - cg));
-        arrive_expect(bars->c_full + s, (uint32_t)cols * rows * 8u);
-        for(int c = 0; c < cols; ++c)
-          bulk_load(psm + kPOffC + s * kPCSlot + c * (kTcM * 8), C + (cg + c) * ldc + r0, rows * 8u,
-                    bars->c_full + s);
+        arrive_expect(bars->c_full + s, (uint32_t)kPCSlot);
+        tma_load_2d(psm + kPOffC + s * kPCSlot, &cmap, (int)r0, (int)(c0 + 16 * g), bars->c_full + s);
       }
       if(stop)
         break;
@@ -909,15 +914,30 @@ void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const
   unsigned char *Bs = As + (size_t)mt * nq * kStageA;
   k_tc_split_a<<<dim3(mt, (unsigned)nq), 512, 0, ctx->stream>>>(A, lda, m, k, nq, As);
   k_tc_split_b<<<dim3(nt, (unsigned)nq), 256, 0, ctx->stream>>>(B, ldb, n, k, nq, Bs);
-  // the persistent form copies C's columns (m rows each) by bulk copies:
-  // 16-byte aligned starts and sizes
-  const bool persistent = ctx->lu_tc == 1 && nq <= kPMaxQ &&
-                          (reinterpret_cast<uintptr_t>(C) & 15) == 0 && (ldc & 1) == 0 && (m & 1) == 0;
+  // the persistent form reads C by tensor copies: a 16-byte aligned base and
+  // an even leading dimension (column stride a multiple of 16 bytes)
+  alignas(64) CUtensorMap cmap;
+  bool persistent = ctx->lu_tc == 1 && nq <= kPMaxQ && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
+                    (ldc & 1) == 0;
+  if(persistent) {
+    typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                 CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                 CUtensorMapFloatOOBfill);
+    EncodeFn enc = reinterpret_cast<EncodeFn>(tensor_map_encoder());
+    const cuuint64_t dims[2] = {(cuuint64_t)m, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {(cuuint64_t)ldc * sizeof(float2)};
+    const cuuint32_t box[2] = {(cuuint32_t)kTcM, 16};
+    const cuuint32_t estr[2] = {1, 1};
+    persistent = enc && enc(&cmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, C, dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  }
   if(persistent) {
     cudaFuncSetAttribute(k_cgemm_sub_tc3, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem);
     const long tiles = (long)mt * nt;
     const unsigned grid = (unsigned)std::min<long>(tiles, ctx->sm_count);
-    k_cgemm_sub_tc3<<<grid, kPThreads, kPSmem, ctx->stream>>>(As, Bs, nq, C, ldc, m, n, d_err);
+    k_cgemm_sub_tc3<<<grid, kPThreads, kPSmem, ctx->stream>>>(As, Bs, nq, cmap, C, ldc, m, n, d_err);
   } else {
     cudaFuncSetAttribute(k_cgemm_sub_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, kTc2Smem);
     k_cgemm_sub_tc2<<<dim3(mt, nt), 128, kTc2Smem, ctx->stream>>>(As, Bs, nq, C, ldc, m, n, d_err);

@@ -184,6 +184,8 @@ EncodeFn encode_fn() {
 
 }  // namespace
 
+void *tensor_map_encoder() { return reinterpret_cast<void *>(encode_fn()); }
+
 // Launches the TMA matvec (false when the tensor map cannot be made: the
 // caller then runs the plain kernel).
 bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *part, int row_tiles,

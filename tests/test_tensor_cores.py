@@ -154,7 +154,8 @@ def test_one_launch_sweeps_match_block_launches(G, ctx, N, nmax):
 def test_cooperative_panels_give_the_same_factors(G, ctx):
     """n = 9,600 (44 panels of 8,192 rows or more): the one-launch cooperative
     panel (a grid-wide barrier per column, row interchanges kept in a table and
-    applied after the last column) takes the same operations per entry as the
+    applied after the last column; the rows in shared memory, mode 1, or in
+    global memory, mode 3) takes the same operations per entry as the
     two-launches-per-column panel, so both LU roles give bit-identical
     solutions; and the persistent trailing update with cooperative panels
     matches the one-CTA-per-tile update with per-column panels bit for bit."""
@@ -163,8 +164,8 @@ def test_cooperative_panels_give_the_same_factors(G, ctx):
     sp = G.spheres_array(xyz, rad, (1.8 + 0.02j) ** 2, 4)     # P = 24: n = 9,600
     bg, wave = G.medium(1.0), G.plane_wave(700 * nm)
     out = {}
-    for mode in (1, 2):
-        ctx.tune(lu_tensor_cores=mode, lu_persistent=mode)
+    for mode in (1, 2, 3):
+        ctx.tune(lu_tensor_cores=min(mode, 2), lu_persistent=mode)
         pr = G.Problem(ctx, sp, bg, wave)
         pr.source_vector(copy=False)
         pr.assemble(G.FF, G.C128)
@@ -175,7 +176,8 @@ def test_cooperative_panels_give_the_same_factors(G, ctx):
         out[mode] = (x64, pr.coefficients()[0].copy(), st.iterations)
         pr.close()
     ctx.tune(lu_tensor_cores=1, lu_persistent=1)
-    assert np.array_equal(out[1][0], out[2][0])
-    assert np.array_equal(out[1][1], out[2][1]) and out[1][2] == out[2][2]
+    for mode in (2, 3):
+        assert np.array_equal(out[1][0], out[mode][0])
+        assert np.array_equal(out[1][1], out[mode][1]) and out[1][2] == out[mode][2]
     assert np.max(np.abs(out[1][1] - out[1][0])) / np.max(np.abs(out[1][0])) < 1e-8
 
