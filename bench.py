@@ -867,7 +867,7 @@ def lu_mixed_arm(args):
     n = pr.n
     pr.close()
     ctx.close()
-    blk = 128 if args.lu_update else 32  # rank of the trailing updates
+    blk = 256 if args.lu_update else 32  # rank of the trailing updates
     upd_bytes = 16.0 * sum((n - K) ** 2 for K in range(blk, n, blk))  # C read + written, complex64
     phases = {"factor_ms": ph["factor"][0], "panel_ms": ph["panel"][0], "panels": ph["panel"][1],
               "update_ms": ph["update"][0], "updates": ph["update"][1],

@@ -149,14 +149,18 @@ typedef struct {
                             launch and an update launch per panel column, one launch per
                             32-row block of a triangular sweep; 3 as 1 with the panel's rows
                             kept in global memory rather than shared memory */
+  int batch_tiles;       /* tiles and schedule of the batched matvecs (om_batch_solve): 0 (default)
+                            autotuned per size class at its first batch, 1..8 a fixed candidate
+                            (rows per tile, tile order, CTAs per SM; see om_batch_tiles) */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any
- * k >= 1, host buffers: the tensor-core trailing update of the complex64 LU
- * (bf16 hi/lo split products accumulated in FP32 over all of k, about 17
- * significant bits). From k = 64 the operands are split into bf16 tiles
- * once and streamed by bulk copies (the LU's rank-128 path). The role of the
- * trailing pzgemm of pzgesv (ScalapackSolver.cpp:54-130). */
+ * k >= 1, host buffers: the tensor-core trailing update of the complex64 LU.
+ * A's rows and B's columns are scaled by powers of two and split into fp16
+ * hi / lo parts once; the products hi hi + hi lo + lo hi accumulate in FP32
+ * over all of k (about 21 significant bits relative to the rows' and
+ * columns' magnitudes). The role of the trailing pzgemm of pzgesv
+ * (ScalapackSolver.cpp:54-130). */
 int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, long lda,
                      const float *B, long ldb, float *C, long ldc);
 /* Statistics of an ACA-compressed matrix (om_assemble with OM_ACA): device
@@ -402,6 +406,13 @@ void om_server_destroy(om_server *srv);
  * (overlap, not converged, budget) are in results[i].status. */
 int om_batch_solve(om_context *ctx, const om_request *reqs, int count, size_t arena_bytes,
                    om_result *results);
+/* The batched matvecs' tile configurations chosen so far on this context,
+ * one per size class (the autotuner times each candidate on the class's
+ * first batch and keeps the fastest): out[7 i .. 7 i + 6] = {precision,
+ * nMax, padded N, rows per tile, tile order (0 slot by slot, 1 interleaved
+ * across slots), CTAs per SM, microseconds of one Arnoldi matvec of that
+ * batch}. Returns the number of classes (at most max_entries are written). */
+int om_batch_tiles(om_context *ctx, int *out, int max_entries);
 
 #ifdef __cplusplus
 }

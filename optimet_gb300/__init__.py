@@ -68,7 +68,7 @@ class Tuning(C.Structure):
     _fields_ = [("matvec_ctas_per_sm", C.c_int), ("matvec_df_ctas_per_sm", C.c_int),
                 ("assemble_carveout", C.c_int), ("matvec_carveout", C.c_int),
                 ("lu_tensor_cores", C.c_int), ("matvec_tma", C.c_int),
-                ("assemble_rotation", C.c_int), ("lu_persistent", C.c_int)]
+                ("assemble_rotation", C.c_int), ("lu_persistent", C.c_int), ("batch_tiles", C.c_int)]
 
 
 class Request(C.Structure):
@@ -105,6 +105,7 @@ def lib():
         L.om_context_synchronize.argtypes = [vp]
         L.om_context_timers.argtypes = [vp, C.c_int, _dp]
         L.om_context_lu_timers.argtypes = [vp, _dp]
+        L.om_batch_tiles.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
         L.om_context_mark.argtypes = [vp, _dp]
         L.om_context_tune.argtypes = [vp, C.POINTER(Tuning)]
         L.om_aca_info.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp,
@@ -204,10 +205,10 @@ class Context:
         return float(out[0])
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
-             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1):
+             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1):
         """Launch tuning (om_context_tune); 0 / -1 keep the current value."""
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
-                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent)
+                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles)
         self.check(lib().om_context_tune(self.h, C.byref(t)))
 
     def timers(self, enable=True):
@@ -487,6 +488,18 @@ def batch_solve(ctx: Context, requests, arena_bytes: int = 0):
     return [_result_dict(out[i]) for i in range(n)]
 
 
+def batch_tiles(ctx: Context):
+    """The batched matvec configurations the autotuner chose on this context
+    (om_batch_tiles): one dict per size class."""
+    k = lib().om_batch_tiles(ctx.h, None, 0)
+    if k < 0:
+        ctx.check(k)
+    buf = (C.c_int * max(7 * k, 1))()
+    lib().om_batch_tiles(ctx.h, buf, k)
+    keys = ("precision", "nmax", "Npad", "rows", "order", "ctas_per_sm", "matvec_us")
+    return [dict(zip(keys, buf[7 * i:7 * i + 7])) for i in range(k)]
+
+
 class Server:
     """Serving / batching runtime (om_server_*): `slots` contexts on one GPU
     taking wavelength-solve requests in arrival order, admitted against an HBM
@@ -539,9 +552,9 @@ class Server:
             raise OptimetError(rc, "server batching")
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
-             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1):
+             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1):
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
-                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent)
+                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles)
         rc = lib().om_server_tune(self.h, C.byref(t))
         if rc:
             raise OptimetError(rc, "server tune")

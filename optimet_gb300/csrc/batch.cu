@@ -132,11 +132,12 @@ template <typename V> __device__ __forceinline__ double2 to_d2(V v) { return mak
 // launch). part[(s nsm + chunk) np + i] holds a chunk's partial sum.
 // ---------------------------------------------------------------------------
 
-// Arnoldi product: S_s times basis column j of slot s (slots with inner set)
-template <typename M, typename V>
-__global__ void __launch_bounds__(kBT) k_b_mv(const Slot *st, const int4 *tiles, const Ctl *ctl,
-                                             const V *Vb, long vslot, long np, int nsm, V *part,
-                                             unsigned long long *next) {
+// Arnoldi product: S_s times basis column j of slot s (slots with inner set).
+// R rows per tile (one thread each): the row sums do not depend on R.
+template <typename M, typename V, int R>
+__global__ void __launch_bounds__(R) k_b_mv(const Slot *st, const int4 *tiles, const Ctl *ctl,
+                                           const V *Vb, long vslot, long np, int nsm, V *part,
+                                           unsigned long long *next) {
   __shared__ V xs[kBCols];
   __shared__ int tile;
   const int ntiles = ctl->ntiles;
@@ -155,9 +156,9 @@ __global__ void __launch_bounds__(kBT) k_b_mv(const Slot *st, const int4 *tiles,
     const long n = st[d.x].n;
     const M *S = (const M *)st[d.x].S;
     const V *x = Vb + d.x * vslot + (long)jcol * np;
-    const long i = (long)d.y * kBT + threadIdx.x;
+    const long i = (long)d.y * R + threadIdx.x;
     const long j0 = (long)d.z * kBCols, j1 = min(n, j0 + kBCols);
-    for(long j = j0 + threadIdx.x; j < j1; j += kBT)
+    for(long j = j0 + threadIdx.x; j < j1; j += R)
       xs[j - j0] = x[j];
     __syncthreads();
     if(i < n)
@@ -167,10 +168,10 @@ __global__ void __launch_bounds__(kBT) k_b_mv(const Slot *st, const int4 *tiles,
 
 // Residual product: S_s x_s with x in FP64 (slots with outer set and x != 0);
 // a complex64 matrix takes the compensated FP64-accurate sums
-template <typename M>
-__global__ void __launch_bounds__(kBT) k_b_resid(const Slot *st, const int4 *tiles, const Ctl *ctl,
-                                                const double2 *x, long np, int nsm, double2 *part,
-                                                unsigned long long *next) {
+template <typename M, int R>
+__global__ void __launch_bounds__(R) k_b_resid(const Slot *st, const int4 *tiles, const Ctl *ctl,
+                                              const double2 *x, long np, int nsm, double2 *part,
+                                              unsigned long long *next) {
   constexpr bool kDF = std::is_same<M, float2>::value;
   typedef typename std::conditional<kDF, DFX, double2>::type XS;
   __shared__ XS xs[kBCols];
@@ -190,9 +191,9 @@ __global__ void __launch_bounds__(kBT) k_b_resid(const Slot *st, const int4 *til
     const long n = st[d.x].n;
     const M *S = (const M *)st[d.x].S;
     const double2 *xv = x + d.x * np;
-    const long i = (long)d.y * kBT + threadIdx.x;
+    const long i = (long)d.y * R + threadIdx.x;
     const long j0 = (long)d.z * kBCols, j1 = min(n, j0 + kBCols);
-    for(long j = j0 + threadIdx.x; j < j1; j += kBT) {
+    for(long j = j0 + threadIdx.x; j < j1; j += R) {
       if constexpr(kDF)
         xs[j - j0] = df_split(xv[j]);
       else
@@ -586,6 +587,31 @@ struct ClassKey {
 
 inline size_t rup(size_t v) { return ((v + 255) / 256) * 256; }
 
+// Tile shapes and schedules of the batched matvecs (k_b_mv, k_b_resid) that
+// the autotuner chooses among, per size class: rows per tile (threads per
+// CTA), the tile order (slot by slot, or interleaved across slots so that the
+// counter spreads every slot over the SMs) and the grid (CTAs per SM; halved
+// when the next batch's assembly runs beside the solves). None of them
+// changes a row's sum (the 1,024-column chunks and their order are fixed), so
+// a request's bits do not depend on the choice.
+struct MvCfg {
+  int rows, order, cap;
+};
+constexpr MvCfg kMvCands[] = {{256, 0, 8},  {256, 1, 8},  {128, 0, 8}, {128, 1, 8},
+                              {256, 0, 16}, {128, 1, 16}, {256, 1, 4}, {128, 0, 4}};
+constexpr int kNumMvCands = (int)(sizeof(kMvCands) / sizeof(kMvCands[0]));
+
+// the autotuner's choices, per context and size class, kept beyond the
+// class's buffers (which the cache may evict)
+struct TunedEntry {
+  om_context *ctx;
+  int precision, nmax, Npad, m;
+  int cand;
+  double us;
+};
+std::mutex g_tuned_mu;
+std::vector<TunedEntry> g_tuned;
+
 // Device and pinned host buffers of one size class, and its graphs.
 template <typename M, typename V> struct Class {
   om_context *ctx = nullptr;
@@ -618,6 +644,8 @@ template <typename M, typename V> struct Class {
   cudaEvent_t ev_alloc[2] = {nullptr, nullptr};  // matrix storage of batch buffer i allocated
   cudaGraphExec_t g_start = nullptr, g_seg = nullptr, g_end = nullptr;
   int k_start = 0, k_seg = 0, k_end = 0;  // kernels per replay
+  MvCfg mv = kMvCands[0];  // the matvec tiles and schedule (autotuned at the first solve)
+  bool tuned = false;
 
   // device bytes of one slot's vectors and tables (the matrices are
   // allocated per batch at the requests' own sizes)
@@ -628,7 +656,7 @@ template <typename M, typename V> struct Class {
            sizeof(V) * (size_t)(m + 1) * np + sizeof(double2) * (size_t)nsm * np +
            2 * sizeof(double2) * (size_t)nbf * m2 +
            sizeof(double2) * ((size_t)m2 + (size_t)m * (m + 1) + 2 * (size_t)m + (m + 1) + m) +
-           sizeof(int4) * (size_t)((np + kBT - 1) / kBT) * nsm + sizeof(Slot) +
+           sizeof(int4) * (size_t)((np + 127) / 128) * nsm + sizeof(Slot) +
            2 * nbuf * sizeof(BatchMat) + 64;
   }
 
@@ -644,11 +672,7 @@ template <typename M, typename V> struct Class {
     nsm = (int)((np + kBCols - 1) / kBCols);
     nblk = (int)((np + kBDotRows - 1) / kBDotRows);
     nbf = (int)((np + kFRows - 1) / kFRows);
-    max_tiles = B * (int)((np + kBT - 1) / kBT) * nsm;
-    // overlapping batches: half the SM's CTA slots, so that two CTAs of the
-    // next batch's assembly (FP64-bound) fit beside the matvec (HBM-bound)
-    mv_grid = (unsigned)std::max(1L, std::min((long)max_tiles,
-                                              (long)ctx->sm_count * (nbuf > 1 ? 4 : 8)));
+    max_tiles = B * (int)((np + 127) / 128) * nsm;  // (the smallest tiles)
     // the matrices are allocated per batch, at the requests' own sizes
     const size_t Bz = (size_t)B;
     size_t sz[] = {Bz * sizeof(Slot), sizeof(Ctl), sizeof(int4) * (size_t)max_tiles,
@@ -709,6 +733,126 @@ template <typename M, typename V> struct Class {
     ev_aux.resize(ctx->aux.size());
     for(auto &e : ev_aux)
       cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    // a choice made for this class before (the graphs are captured once the
+    // matvec configuration is known: here, or after the autotuning)
+    {
+      std::lock_guard<std::mutex> lk(g_tuned_mu);
+      for(const TunedEntry &e : g_tuned)
+        if(e.ctx == ctx && e.precision == key.precision && e.nmax == key.nmax && e.Npad == key.Npad &&
+           e.m == key.m) {
+          set_mv(e.cand);
+          tuned = true;
+        }
+    }
+    if(!tuned && ctx->batch_tiles > 0) {  // a configuration fixed by om_context_tune
+      set_mv(std::min(ctx->batch_tiles, kNumMvCands) - 1);
+      tuned = true;
+    }
+    return tuned ? capture() : OM_OK;
+  }
+
+  void set_mv(int cand) {
+    mv = kMvCands[cand];
+    // overlapping batches: half the SM's CTA slots, so that two CTAs of the
+    // next batch's assembly (FP64-bound) fit beside the matvec (HBM-bound)
+    const int cap = nbuf > 1 ? std::max(2, mv.cap / 2) : mv.cap;
+    mv_grid = (unsigned)std::max(1L, std::min((long)max_tiles, (long)ctx->sm_count * cap));
+  }
+
+  // the tiles of the slots whose h_st entries have outer set, in the order of
+  // configuration c; returns their count
+  int build_tiles(const MvCfg &c) {
+    int nt = 0;
+    if(c.order == 0) {
+      for(int s = 0; s < B; ++s) {
+        const long n = h_st[s].outer ? h_st[s].n : 0;
+        const int rt = (int)((n + c.rows - 1) / c.rows), ct = (int)((n + kBCols - 1) / kBCols);
+        for(int cc = 0; cc < ct; ++cc)
+          for(int q = 0; q < rt; ++q)
+            h_tiles[nt++] = make_int4(s, q, cc, 0);
+      }
+    } else {
+      int most = 0;
+      for(int s = 0; s < B; ++s) {
+        const long n = h_st[s].outer ? h_st[s].n : 0;
+        most = std::max(most, (int)(((n + c.rows - 1) / c.rows) * ((n + kBCols - 1) / kBCols)));
+      }
+      for(int p = 0; p < most; ++p)
+        for(int s = 0; s < B; ++s) {
+          const long n = h_st[s].outer ? h_st[s].n : 0;
+          const int rt = (int)((n + c.rows - 1) / c.rows), ct = (int)((n + kBCols - 1) / kBCols);
+          if(p < rt * ct)
+            h_tiles[nt++] = make_int4(s, p % rt, p / rt, 0);
+        }
+    }
+    return nt;
+  }
+
+  void launch_mv(cudaStream_t s) {
+    if(mv.rows == 128)
+      k_b_mv<M, V, 128><<<mv_grid, 128, 0, s>>>(st, tiles, ctl, Vb, vslot, np, nsm, (V *)part, counter);
+    else
+      k_b_mv<M, V, 256><<<mv_grid, 256, 0, s>>>(st, tiles, ctl, Vb, vslot, np, nsm, (V *)part, counter);
+  }
+  void launch_resid(cudaStream_t s) {
+    if(mv.rows == 128)
+      k_b_resid<M, 128><<<mv_grid, 128, 0, s>>>(st, tiles, ctl, x, np, nsm, part, counter);
+    else
+      k_b_resid<M, 256><<<mv_grid, 256, 0, s>>>(st, tiles, ctl, x, np, nsm, part, counter);
+  }
+
+  // The autotuner: times the Arnoldi matvec of this batch's matrices (every
+  // slot with a system) under each candidate configuration (best of three
+  // launches; the product lands in scratch), keeps the fastest for the class,
+  // and captures the graphs with it.
+  int autotune() {
+    std::vector<Slot> probe(h_st, h_st + B);
+    for(Slot &sl : probe)
+      sl.inner = sl.outer && sl.n > 0;
+    cudaMemcpyAsync(st, probe.data(), sizeof(Slot) * B, cudaMemcpyHostToDevice, ctx->stream);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = 0;
+    float best_ms = 1e30f;
+    for(int c = 0; c < kNumMvCands; ++c) {
+      set_mv(c);
+      h_ctl->j = 0;
+      h_ctl->n_inner = h_ctl->n_outer = 0;
+      h_ctl->ntiles = build_tiles(mv);
+      cudaMemcpyAsync(ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, ctx->stream);
+      if(h_ctl->ntiles)
+        cudaMemcpyAsync(tiles, h_tiles, sizeof(int4) * h_ctl->ntiles, cudaMemcpyHostToDevice, ctx->stream);
+      float ms_min = 1e30f;
+      for(int rep = 0; rep < 3; ++rep) {
+        cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream);
+        cudaEventRecord(e0, ctx->stream);
+        launch_mv(ctx->stream);
+        cudaEventRecord(e1, ctx->stream);
+        if(cudaEventSynchronize(e1) != cudaSuccess)
+          break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms_min = std::min(ms_min, ms);
+      }
+      if(ms_min < best_ms) {
+        best_ms = ms_min;
+        best = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) {
+      ctx->err = std::string("batch autotuning: ") + cudaGetErrorString(e);
+      return OM_ERR_CUDA;
+    }
+    set_mv(best);
+    tuned = true;
+    {
+      std::lock_guard<std::mutex> lk(g_tuned_mu);
+      g_tuned.push_back(TunedEntry{ctx, key.precision, key.nmax, key.Npad, key.m, best, 1e3 * best_ms});
+    }
     return capture();
   }
 
@@ -740,7 +884,7 @@ template <typename M, typename V> struct Class {
   // cycle start: r = b - S x, ||r||, the test, v_0
   int enqueue_start(cudaStream_t s) {
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
-    k_b_resid<M><<<mv_grid, kBT, 0, s>>>(st, tiles, ctl, x, np, nsm, part, counter);
+    launch_resid(s);
     k_b_reduce_r<<<vgrid(), kBT, 0, s>>>(st, part, np, nsm, b, r);
     k_b_rnorm<<<dim3(nblk, B), kBT, 0, s>>>(st, r, np, nblk, m2, dpA);
     k_b_start<<<1, ctl_threads(), 0, s>>>(st, ctl, dpA, nblk, m2, g, m, B, key.tol, key.inner_rel,
@@ -756,7 +900,7 @@ template <typename M, typename V> struct Class {
     const dim3 fg((unsigned)nbf, (unsigned)B);
     const size_t hsm = sizeof(V) * m2;
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
-    k_b_mv<M, V><<<mv_grid, kBT, 0, s>>>(st, tiles, ctl, Vb, vslot, np, nsm, (V *)part, counter);
+    launch_mv(s);
     k_b_red_proj<V><<<fg, kBT, 0, s>>>(st, ctl, (const V *)part, np, nsm, Vb, vslot, nbf, m2, pA);
     k_b_sub_proj<V><<<fg, kBT, hsm, s>>>(st, ctl, Vb, vslot, np, nbf, m2, pA, pB, hacc, 0);
     k_b_sub_proj<V><<<fg, kBT, hsm, s>>>(st, ctl, Vb, vslot, np, nbf, m2, pB, pA, hacc, 1);
@@ -816,14 +960,12 @@ template <typename M, typename V> struct Class {
   // Solve the systems of the slots whose h_st entries are set (uploaded here):
   // replays the graphs until no slot needs another cycle.
   int solve(long *launches) {
-    int nt = 0;
-    for(int s = 0; s < B; ++s) {
-      const long n = h_st[s].outer ? h_st[s].n : 0;
-      const int rt = (int)((n + kBT - 1) / kBT), ct = (int)((n + kBCols - 1) / kBCols);
-      for(int c = 0; c < ct; ++c)
-        for(int q = 0; q < rt; ++q)
-          h_tiles[nt++] = make_int4(s, q, c, 0);
+    if(!tuned) {
+      const int rc = autotune();
+      if(rc)
+        return rc;
     }
+    const int nt = build_tiles(mv);
     h_ctl->j = 0;
     h_ctl->n_inner = 0;
     h_ctl->n_outer = 0;
@@ -1313,6 +1455,12 @@ int run_class(om_context *ctx, const ClassKey &key, const std::vector<int> &idx,
 
 // Drops the class workspaces cached for ctx (called by om_context_destroy).
 void batch_release(om_context *ctx) {
+  {
+    std::lock_guard<std::mutex> lk(g_tuned_mu);
+    g_tuned.erase(std::remove_if(g_tuned.begin(), g_tuned.end(),
+                                 [ctx](const TunedEntry &e) { return e.ctx == ctx; }),
+                  g_tuned.end());
+  }
   std::vector<CacheEntry> mine;
   {
     std::lock_guard<std::mutex> lk(g_cache_mu);
@@ -1349,6 +1497,31 @@ size_t batch_request_bytes(const om_request &rq) {
 }
 
 }  // namespace om
+
+extern "C" int om_batch_tiles(om_context *ctx, int *out, int max_entries) {
+  using namespace om;
+  if(!ctx || max_entries < 0 || (max_entries > 0 && !out))
+    return OM_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
+  int k = 0;
+  for(const TunedEntry &e : g_tuned) {
+    if(e.ctx != ctx)
+      continue;
+    if(k < max_entries) {
+      const MvCfg &c = kMvCands[e.cand];
+      int *o = out + 7 * k;
+      o[0] = e.precision;
+      o[1] = e.nmax;
+      o[2] = e.Npad;
+      o[3] = c.rows;
+      o[4] = c.order;
+      o[5] = c.cap;
+      o[6] = (int)e.us;
+    }
+    ++k;
+  }
+  return k;
+}
 
 extern "C" int om_batch_solve(om_context *ctx, const om_request *reqs, int count, size_t arena_bytes,
                               om_result *results) {

@@ -439,6 +439,8 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
     ctx->asm_rot = t->assemble_rotation ? 1 : 0;
   if(t->lu_persistent > 0)
     ctx->lu_persist = std::min(t->lu_persistent, 3);
+  if(t->batch_tiles >= 0)
+    ctx->batch_tiles = std::min(t->batch_tiles, 8);
   return OM_OK;
 }
 
@@ -452,22 +454,19 @@ int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, lon
   int *derr = nullptr;
   unsigned char *dS = nullptr;
   const size_t na = (size_t)lda * k, nbb = (size_t)ldb * n, nc = (size_t)ldc * n;
-  // from k = 64 the LU's path: operands split once, then streamed by bulk copies
-  const size_t ns = k >= 64 ? om::cgemm_sub_tc_split_bytes(m, n, k) : 0;
+  // operands split once, then streamed by bulk copies (the LU's path)
+  const size_t ns = om::cgemm_sub_tc_split_bytes(m, n, k);
   int rc = dev_alloc(ctx, &dA, na);
   if(!rc) rc = dev_alloc(ctx, &dB, nbb);
   if(!rc) rc = dev_alloc(ctx, &dC, nc);
   if(!rc) rc = dev_alloc(ctx, &derr, 1);
-  if(!rc && ns) rc = dev_alloc(ctx, &dS, ns);
+  if(!rc) rc = dev_alloc(ctx, &dS, ns);
   if(!rc) {
     cudaMemcpyAsync(dA, A, sizeof(float2) * na, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(dB, B, sizeof(float2) * nbb, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(dC, C, sizeof(float2) * nc, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(derr, 0, sizeof(int), ctx->stream);
-    if(ns)
-      om::launch_cgemm_sub_tc_split(ctx, dA, lda, dB, ldb, dC, ldc, m, n, k, dS, derr);
-    else
-      om::launch_cgemm_sub_tc(ctx, dA, lda, dB, ldb, dC, ldc, m, n, k, derr);
+    om::launch_cgemm_sub_tc_split(ctx, dA, lda, dB, ldb, dC, ldc, m, n, k, dS, derr);
     rc = check_launch(ctx, "tensor-core update");
     int herr = 0;
     if(!rc) {

@@ -126,6 +126,8 @@ struct om_context {
   // panel launches and per-block sweep launches, 3 as 1 with the panel rows
   // always in global memory
   int lu_persist = 1;
+  // batched matvec tiles: 0 autotuned per size class, k > 0 candidate k - 1
+  int batch_tiles = 0;
   int asm_rot = 1;  // precision-form assembly by rotated z-axis translations (assemble_rot.cu)
   size_t budget = 0;
   size_t used = 0;
@@ -266,13 +268,11 @@ int solve_lu_mixed_rhs(om_problem *pr, int harmonic, const om_solve_options *o, 
                        double2 *x, om_solve_stats *st);
 
 // tc_gemm.cu: C (m x n) -= A (m x k) B (k x n), any k >= 1, complex64, column-major,
-// on the tensor cores (bf16 hi/lo split, FP32 accumulation); *d_err set on a
-// timed-out wait
-void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
-                         float2 *C, long ldc, long m, long n, int k, int *d_err);
-// The same update from operands split once into bf16 hi / lo tiles (three
-// launches: the two splits and the bulk-copy tensor-core kernel); scratch:
-// cgemm_sub_tc_split_bytes(m, n, k) bytes of device memory, 16-byte aligned.
+// on the tensor cores from operands split once into fp16 hi / lo parts of
+// power-of-two scaled rows and columns (FP32 accumulation); three launches:
+// the two splits and the update kernel; *d_err set on a timed-out wait;
+// scratch: cgemm_sub_tc_split_bytes(m, n, k) bytes of device memory, 16-byte
+// aligned.
 size_t cgemm_sub_tc_split_bytes(long m, long n, int k);
 void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
                                float2 *C, long ldc, long m, long n, int k, void *scratch, int *d_err);

@@ -752,11 +752,13 @@ __global__ void __launch_bounds__(1024) k_lu_panel(V *A, long ld, long n, long k
 // later columns, and leaves the partial maxima of column c + 1. Each entry
 // takes the same operations as in k_lu_panel, so the factors are the same.
 constexpr long kTallPanel = 8192;
+constexpr long kCoopPanel = 512;  // the shared-memory cooperative panel from here
 constexpr int kPanThreads = 256;
 
 struct PanelScratch {
   double *bestv;  // per CTA
   long *besti;
+  long *bestr;    // per CTA: the physical row of the partial maximum (shared-memory panel)
   void *prow;     // kNb entries of the element type: the pivot row
   int nblk;
 };
@@ -941,26 +943,29 @@ __device__ __forceinline__ void perm_set(PanelPerm &pm, long pos, long row) {
   ++pm.cnt;
 }
 
-// grid-wide barrier on a counter that only grows: this CTA's arrival, then a
-// bounded wait for `target` arrivals
+// grid-wide barrier on a counter that only grows: this CTA's arrival (a
+// release add: the CTA's earlier writes, ordered before it by the CTA
+// barrier, become visible with it), then a bounded wait with acquire loads
+// for `target` arrivals
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target, int *err) {
   __shared__ int ok_s;
   __syncthreads();
   if(threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(bar, 1u);
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(bar), "r"(1u) : "memory");
     int ok = 0;
     for(long it = 0; it < (1L << 22); ++it) {
-      if(*(volatile unsigned *)bar >= target) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+      if(v >= target) {
         ok = 1;
         break;
       }
       if((it & 63) == 63 && *(volatile int *)err)
         break;  // another CTA (or an earlier launch) gave up
+      __nanosleep(32);  // fewer polls of the counter's line while the arrivals land
     }
     if(!ok)
       atomicExch(err, 1);
-    __threadfence();
     ok_s = ok;
   }
   __syncthreads();
@@ -1139,28 +1144,36 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
                                                              unsigned *bar, unsigned bar_base, int *err) {
   extern __shared__ __align__(16) unsigned char pan_sm[];
   __shared__ V u[kNb];
-  __shared__ PanelPerm pm;
+  // the interchanges so far: the physical row at each position of the
+  // panel's diagonal range (row_at), and the rows moved below it (position,
+  // row; a later entry for the same position replaces an earlier one)
+  __shared__ long row_at[kNb], ext_pos[kNb], ext_row[kNb];
+  __shared__ int ext_cnt;
   __shared__ double wv[kPanThreads / 32];
   __shared__ long wi[kPanThreads / 32];
   __shared__ int wl[kPanThreads / 32];
-  __shared__ long p_s;
   __shared__ double pv_s;
   __shared__ int rl_s, wb_s;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const long G = gridDim.x, b = blockIdx.x;
   const long R = (n - k + G - 1) / G, r0 = k + b * R, r1 = min(n, r0 + R);
   const int nr = (int)max(0L, r1 - r0);
-  V *P = reinterpret_cast<V *>(pan_sm);                              // P[c R + rl]
-  unsigned char *retired = pan_sm + sizeof(V) * (size_t)nb * R;    // per local row
+  V *P = reinterpret_cast<V *>(pan_sm);                                 // P[c R + rl]
+  long *posl = reinterpret_cast<long *>(pan_sm + sizeof(V) * (size_t)nb * R);  // position of local row rl
+  unsigned char *retired = reinterpret_cast<unsigned char *>(posl + R);         // per local row
   if(*(volatile int *)err)
     return;
+  if(t < nb)
+    row_at[t] = k + t;
   if(t == 0)
-    pm.cnt = 0;
+    ext_cnt = 0;
   for(int c = 0; c < nb; ++c)
     for(int rl = t; rl < nr; rl += kPanThreads)
       P[c * R + rl] = A[(k + c) * ld + r0 + rl];
-  for(int rl = t; rl < nr; rl += kPanThreads)
+  for(int rl = t; rl < nr; rl += kPanThreads) {
     retired[rl] = 0;
+    posl[rl] = r0 + rl;
+  }
   __syncthreads();
   // partial maximum of column c over the active local rows (positions for
   // ties), and the row holding it published in cand[b]
@@ -1172,13 +1185,11 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
       if(retired[rl])
         continue;
       const double v = mag2(P[c * R + rl]);
-      if(v >= bv) {
-        const long pos = perm_pos(pm, r0 + rl);
-        if(v > bv || pos < bp) {
-          bv = v;
-          bp = pos;
-          bl = rl;
-        }
+      const long pos = posl[rl];
+      if(v > bv || (v == bv && pos < bp)) {
+        bv = v;
+        bp = pos;
+        bl = rl;
       }
     }
 #pragma unroll
@@ -1207,6 +1218,7 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
         }
       ps.bestv[b] = bv;
       ps.besti[b] = bp;
+      ps.bestr[b] = bl >= 0 ? r0 + bl : -1;
       rl_s = bl;
     }
     __syncthreads();
@@ -1262,14 +1274,25 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
           if(bv <= 0.0 && *info == 0)
             *info = (int)col + 1;
         }
-        const long a = perm_row(pm, col), pr = perm_row(pm, bp);
+        // interchange positions col and bp: the pivot row pr (published by
+        // the winning CTA) comes to col, the row at col goes to bp
+        const long pr = __ldcg(ps.bestr + bw), a = row_at[c];
         if(bp != col) {
-          perm_set(pm, col, pr);
-          perm_set(pm, bp, a);
+          row_at[c] = pr;
+          if(bp - k < nb) {
+            row_at[bp - k] = a;
+          } else {
+            ext_pos[ext_cnt] = bp;
+            ext_row[ext_cnt] = a;
+            ++ext_cnt;
+          }
+          if(a >= r0 && a < r1)
+            posl[a - r0] = bp;
         }
-        if(pr >= r0 && pr < r1)
+        if(pr >= r0 && pr < r1) {
           retired[pr - r0] = 1;
-        p_s = pr;
+          posl[pr - r0] = col;
+        }
         pv_s = bv;
         wb_s = bw;
       }
@@ -1306,16 +1329,41 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
   target += (unsigned)G;
   if(!grid_barrier(bar, target, err) || b != 0)
     return;
+  // (position, row) pairs: the diagonal range, then the moved rows below it
+  // (the last entry of each position)
+  __shared__ long fpos[2 * kNb], frow[2 * kNb];
+  __shared__ int fcnt;
+  if(t == 0) {
+    int cnt = 0;
+    for(int c = 0; c < nb; ++c)
+      if(row_at[c] != k + c) {
+        fpos[cnt] = k + c;
+        frow[cnt] = row_at[c];
+        ++cnt;
+      }
+    for(int e = ext_cnt - 1; e >= 0; --e) {
+      bool later = false;
+      for(int f = e + 1; f < ext_cnt; ++f)
+        later |= ext_pos[f] == ext_pos[e];
+      if(!later) {
+        fpos[cnt] = ext_pos[e];
+        frow[cnt] = ext_row[e];
+        ++cnt;
+      }
+    }
+    fcnt = cnt;
+  }
+  __syncthreads();
   V *tmp = P;  // [2 kNb][kNb], the shared rows are written back
-  const int cnt = pm.cnt;
+  const int cnt = fcnt;
   for(int idx = t; idx < cnt * nb; idx += kPanThreads) {
     const int e = idx / nb, j = idx - e * nb;
-    tmp[e * kNb + j] = __ldcg(A + (k + j) * ld + pm.row[e]);
+    tmp[e * kNb + j] = __ldcg(A + (k + j) * ld + frow[e]);
   }
   __syncthreads();
   for(int idx = t; idx < cnt * nb; idx += kPanThreads) {
     const int e = idx / nb, j = idx - e * nb;
-    A[(k + j) * ld + pm.pos[e]] = tmp[e * kNb + j];
+    A[(k + j) * ld + fpos[e]] = tmp[e * kNb + j];
   }
 }
 
@@ -1548,7 +1596,16 @@ __device__ __forceinline__ bool clock_wait_expired(long long t0) {
 template <typename V>
 __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long ld, long n, const V *src, V *dst,
                                                              int upper, const V *dinv, unsigned *flags,
-                                                             unsigned *sync, int *err) {
+                                                             unsigned long long *msg, unsigned *sync, int *err) {
+  // complex64: a solved block travels as 64 words (epoch << 32 | the bits of
+  // one real or imaginary part; single-copy atomic 64-bit stores), so a
+  // reader that sees the epoch in both of a lane's words has that lane's
+  // value, with no flag and no fence. complex128 publishes flags[j] after a
+  // fence and readers take the values from dst.
+  constexpr bool kPacked = sizeof(V) == 8;
+  constexpr int kRing = 64;  // steps of solved values held in shared memory (complex64)
+  __shared__ V xring[kPacked ? kRing * kNb : 1];
+  __shared__ volatile int prog[kSweepWarps];  // steps each compute warp has finished
   extern __shared__ __align__(16) unsigned char sweep_sm[];
   V *vals = reinterpret_cast<V *>(sweep_sm);
   __shared__ volatile int ready;    // sweep steps whose solution is published
@@ -1563,6 +1620,10 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
     abort_s = *(volatile int *)err;
     epoch_s = *(volatile unsigned *)sync;
   }
+  // a compute warp's progress starts at 0 when it has blocks (set before the
+  // poller can start, so that it never runs the ring past a warp's steps)
+  if(threadIdx.x < kSweepWarps)
+    prog[threadIdx.x] = ob > (int)threadIdx.x ? 0 : 0x7fffffff;
   __syncthreads();
   const unsigned epoch = epoch_s;
   // sweep step of column block j, and the block solved at step s
@@ -1607,16 +1668,70 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
     }
     if(lane < nbr)
       dst[kk + lane] = v;
-    __threadfence();
-    __syncwarp();
-    if(lane == 0)
-      atomicExch(flags + r, epoch);
+    if constexpr(kPacked) {
+      const unsigned long long tag = (unsigned long long)epoch << 32;
+      volatile unsigned long long *mm = msg + (r * kNb + lane) * 2;
+      mm[0] = tag | __float_as_uint((float)v.x);
+      mm[1] = tag | __float_as_uint((float)v.y);
+    } else {
+      __threadfence();
+      __syncwarp();
+      if(lane == 0)
+        atomicExch(flags + r, epoch);
+    }
   };
   if(!abort_s && warp == kSweepWarps) {
     // the poller: steps this CTA still needs (forward: the columns left of its
     // last block; backward: those right of its first block)
     const long need = upper ? nblk - 1 - b : b + (long)(ob - 1) * G;
-    if(lane == 0) {
+    if constexpr(kPacked) {
+      // the whole warp polls block j's 64 words, then stores the values in
+      // the ring once every compute warp is done with the step kRing back
+      for(long st = 0; st < need; ++st) {
+        const long j = upper ? nblk - 1 - st : st;
+        const long long t0 = clock64();
+        bool ok = true;
+        for(;;) {
+          int lag = 0x7fffffff;
+#pragma unroll
+          for(int w = 0; w < kSweepWarps; ++w)
+            lag = min(lag, prog[w]);
+          if(lag > st - kRing)
+            break;
+          if(abort_s || clock_wait_expired(t0)) {
+            ok = false;
+            break;
+          }
+          __nanosleep(20);
+        }
+        unsigned long long m0 = 0, m1 = 0;
+        const volatile unsigned long long *mm = msg + (j * kNb + lane) * 2;
+        while(ok) {
+          m0 = mm[0];
+          m1 = mm[1];
+          if(__all_sync(0xffffffffu, (unsigned)(m0 >> 32) == epoch && (unsigned)(m1 >> 32) == epoch))
+            break;
+          if(abort_s || *(volatile int *)err || clock_wait_expired(t0))
+            ok = false;
+          __nanosleep(16);
+        }
+        if(!__all_sync(0xffffffffu, ok)) {
+          if(lane == 0) {
+            atomicExch(err, 1);
+            abort_s = 1;
+          }
+          break;
+        }
+        V x;
+        x.x = __uint_as_float((unsigned)m0);
+        x.y = __uint_as_float((unsigned)m1);
+        xring[(st % kRing) * kNb + lane] = x;
+        __syncwarp();
+        __threadfence_block();
+        if(lane == 0)
+          ready = (int)(st + 1);
+      }
+    } else if(lane == 0) {
       for(long st = 0; st < need; ++st) {
         const long j = upper ? nblk - 1 - st : st;
         const long long t0 = clock64();
@@ -1696,8 +1811,12 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
       __threadfence_block();
       V xl;
       xl.x = xl.y = 0;
-      if(lane < nbj)
-        xl = __ldcg(dst + k + lane);
+      if(lane < nbj) {
+        if constexpr(kPacked)
+          xl = xring[(st % kRing) * kNb + lane];
+        else
+          xl = __ldcg(dst + k + lane);
+      }
       {
         V v = vals[q0 * kNb + lane];
 #pragma unroll
@@ -1743,7 +1862,11 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
         vals[q * kNb + lane] = v;
         __syncwarp();
       }
+      if(lane == 0)
+        prog[warp] = first < nq ? (int)(st + 1) : 0x7fffffff;
     }
+    if(lane == 0)  // (done, or given up)
+      prog[warp] = 0x7fffffff;
   }
   __syncthreads();
   if(threadIdx.x == 0) {  // the last CTA out moves the epoch on
@@ -1765,7 +1888,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
 // it is read and written once per kTcBlock columns instead of once per kNb.
 // The pivots are those of the unblocked order (each panel's pivot search sees
 // fully updated columns); the roundings differ.
-constexpr long kTcBlock = 128;
+constexpr long kTcBlock = 256;
 
 template <typename Panel>
 void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Panel &panel, void *split) {
@@ -1782,8 +1905,8 @@ void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Pane
       if(kn < KE) {  // the block's later columns: U rows, then all rows below
         k_lu_trsm<float2><<<blocks_for(KE - kn, 128), 128, 0, ctx->stream>>>(A, n, kn, KE, k, nb);
         ctx->last_launches++;
-        launch_cgemm_sub_tc(ctx, A + k * n + kn, n, A + kn * n + k, n, A + kn * n + kn, n, n - kn,
-                            KE - kn, nb, info + 1);
+        launch_cgemm_sub_tc_split(ctx, A + k * n + kn, n, A + kn * n + k, n, A + kn * n + kn, n, n - kn,
+                                  KE - kn, nb, split, info + 1);
       }
     }
     if(W < n) {  // the block's interchanges on the columns left and right of it
@@ -1799,16 +1922,12 @@ void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Pane
       k_lu_trsm<float2><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, KE, n, k, nb);
       ctx->last_launches++;
       if(kn < KE)
-        launch_cgemm_sub_tc(ctx, A + k * n + kn, n, A + KE * n + k, n, A + KE * n + kn, n, KE - kn,
-                            rest, nb, info + 1);
+        launch_cgemm_sub_tc_split(ctx, A + k * n + kn, n, A + KE * n + k, n, A + KE * n + kn, n, KE - kn,
+                                  rest, nb, split, info + 1);
     }
     timer_begin(ctx, ctx->ev_luu);
-    if(split && W >= 64)  // operands split once, streamed by bulk copies
-      launch_cgemm_sub_tc_split(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest,
-                                rest, (int)W, split, info + 1);
-    else
-      launch_cgemm_sub_tc(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest, rest,
-                          (int)W, info + 1);
+    launch_cgemm_sub_tc_split(ctx, A + K * n + KE, n, A + KE * n + K, n, A + KE * n + KE, n, rest, rest,
+                              (int)W, split, info + 1);
     timer_end(ctx, ctx->ev_luu);
   }
 }
@@ -1822,12 +1941,12 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   ws.ctx = ctx;
   PanelScratch ps{};
   const int maxblk = 4 * ctx->sm_count;
-  size_t split_bytes = 0;  // the pre-split operands of the rank-128 updates
+  size_t split_bytes = 0;  // the pre-split operands of the tensor-core updates (the largest)
   if constexpr(std::is_same<V, float2>::value)
-    if(ctx->lu_tc && n > kTcBlock)
+    if(ctx->lu_tc)
       split_bytes = cgemm_sub_tc_split_bytes(n, n, (int)kTcBlock);
   const size_t pan_bytes =
-      n >= kTallPanel ? maxblk * (sizeof(double) + sizeof(long) + kNb * sizeof(V)) + kNb * sizeof(V) + 5 * 256
+      n >= kCoopPanel ? maxblk * (sizeof(double) + 2 * sizeof(long) + kNb * sizeof(V)) + kNb * sizeof(V) + 6 * 256
                       : 0;
   void *split = nullptr;
   unsigned *bar = nullptr, bar_base = 0;  // the cooperative panels' barrier counter
@@ -1836,11 +1955,12 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   // in shared memory when the tallest panel's share fits (coop_smem bytes).
   int coop_grid = 0;
   size_t coop_smem = 0;
-  if(ctx->lu_persist != 2 && n >= kTallPanel) {
+  if(ctx->lu_persist != 2 && n >= kCoopPanel) {
     int per_sm = 0, coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
-    const long R = (n + ctx->sm_count - 1) / ctx->sm_count;
-    const size_t sm = std::max(sizeof(V) * kNb * (size_t)R + (size_t)R, sizeof(V) * 2 * kNb * kNb);
+    // rows a CTA holds: n / G for the tallest panel, at least 64 (see below)
+    const long R = std::max<long>((n + ctx->sm_count - 1) / ctx->sm_count, 64);
+    const size_t sm = std::max((sizeof(V) * kNb + sizeof(long) + 1) * (size_t)R, sizeof(V) * 2 * kNb * kNb);
     if(coop && ctx->lu_persist == 1 && sm <= 220 * 1024 &&
        cudaFuncSetAttribute(k_pan_coop_sm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
            cudaSuccess &&
@@ -1863,6 +1983,7 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
     if(pan_bytes) {
       ps.bestv = ws.take<double>(maxblk, off);
       ps.besti = ws.take<long>(maxblk, off);
+      ps.bestr = ws.take<long>(maxblk, off);
       ps.prow = ws.take<V>(kNb, off);
       bar = ws.take<unsigned>(1, off);
       cand = ws.take<V>((size_t)maxblk * kNb, off);
@@ -1876,13 +1997,13 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   auto panel = [&](long k, int nb) {
     timer_begin(ctx, ctx->ev_lup);
     const long rows = n - k;
-    if(rows >= kTallPanel && coop_grid > 0) {
+    if((rows >= kTallPanel || (coop_smem && rows >= kCoopPanel)) && coop_grid > 0) {
       int *err = info + 1;
       cudaError_t e;
-      if(coop_smem) {  // rows in shared memory
-        ps.nblk = coop_grid;
-        const long R = (rows + coop_grid - 1) / coop_grid;
-        const size_t sm = std::max(sizeof(V) * nb * (size_t)R + (size_t)R, sizeof(V) * 2 * kNb * kNb);
+      if(coop_smem) {  // rows in shared memory, 64 rows a CTA at least
+        ps.nblk = (int)std::min<long>(coop_grid, (rows + 63) / 64);
+        const long R = (rows + ps.nblk - 1) / ps.nblk;
+        const size_t sm = std::max((sizeof(V) * nb + sizeof(long) + 1) * (size_t)R, sizeof(V) * 2 * kNb * kNb);
         void *args[] = {&A, (void *)&n, (void *)&n, (void *)&k, (void *)&nb, &piv, &info, &ps, &cand, &bar,
                         &bar_base, &err};
         e = cudaLaunchCooperativeKernel((const void *)k_pan_coop_sm<V>, dim3(ps.nblk), dim3(kPanThreads), args,
@@ -1949,11 +2070,17 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
 // y into b, the backward solve from b into y, and y copied back to b.
 // Workspace of the one-launch sweeps: flags (one per 32-row block, set to
 // all ones) and the epoch / finished-CTA pair.
-inline size_t sweep_ws_words(long n) { return (size_t)((n + kNb - 1) / kNb) + 2; }
+// Workspace of the one-launch sweeps: the complex64 messages (64 words of 8
+// bytes per 32-row block), flags (one per block) and the epoch / finished-CTA
+// pair; messages and flags start as all ones (an epoch never reached).
+inline size_t sweep_ws_words(long n) {
+  const size_t nblk = (size_t)((n + kNb - 1) / kNb);
+  return nblk * 2 * kNb * 2 + nblk + 2;
+}
 inline void sweep_ws_init(om_context *ctx, unsigned *ws, long n) {
   const size_t nblk = (size_t)((n + kNb - 1) / kNb);
-  cudaMemsetAsync(ws, 0xFF, nblk * sizeof(unsigned), ctx->stream);
-  cudaMemsetAsync(ws + nblk, 0, 2 * sizeof(unsigned), ctx->stream);
+  cudaMemsetAsync(ws, 0xFF, (nblk * 2 * kNb * 2 + nblk) * sizeof(unsigned), ctx->stream);
+  cudaMemsetAsync(ws + nblk * 2 * kNb * 2 + nblk, 0, 2 * sizeof(unsigned), ctx->stream);
 }
 
 template <typename V>
@@ -1965,11 +2092,14 @@ int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, const V *
     const long nblk = (n + kNb - 1) / kNb;
     const long G = std::min<long>(ctx->sm_count, nblk);
     const size_t smem = sizeof(V) * kNb * (size_t)((nblk + G - 1) / G);
-    unsigned *flags = sweep_ws, *sync = sweep_ws + nblk;
+    unsigned long long *msg = reinterpret_cast<unsigned long long *>(sweep_ws);
+    unsigned *flags = sweep_ws + nblk * 2 * kNb * 2, *sync = flags + nblk;
     if(smem > 48 * 1024)
       cudaFuncSetAttribute(k_tri_sweep<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_tri_sweep<V><<<(unsigned)G, kSweepThreads, smem, ctx->stream>>>(A, n, n, y, b, 0, dinv, flags, sync, err);
-    k_tri_sweep<V><<<(unsigned)G, kSweepThreads, smem, ctx->stream>>>(A, n, n, b, y, 1, dinv, flags, sync, err);
+    k_tri_sweep<V><<<(unsigned)G, kSweepThreads, smem, ctx->stream>>>(A, n, n, y, b, 0, dinv, flags, msg, sync,
+                                                                      err);
+    k_tri_sweep<V><<<(unsigned)G, kSweepThreads, smem, ctx->stream>>>(A, n, n, b, y, 1, dinv, flags, msg, sync,
+                                                                      err);
     k_scale_copy<V, V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(y, 1.0, b, n);
     launches += 3;
     ctx->last_launches += launches;

@@ -1,32 +1,26 @@
 // Complex64 rank-k update on the 5th-generation tensor cores (tcgen05):
 //   C (m x n) -= A (m x k) B (k x n),  any k >= 1, column-major complex64,
-// the trailing update of the precision form's blocked LU (the role of the
+// the trailing updates of the precision form's blocked LU (the role of the
 // pzgesv trailing pzgemm, ScalapackSolver.cpp:54-130 / LinearSystemSolver.hpp:55-65).
 //
-// Each FP32 component x is split into bf16 x_hi + x_lo (x_lo = bf16(x - x_hi));
-// a real product is x_hi y_hi + x_hi y_lo + x_lo y_hi (three bf16 MMAs with
-// FP32 accumulation, about 17 significant bits), so
-//   Re(AB) = Ar Br + Ai (-Bi),  Im(AB) = Ar Bi + Ai Br
-// takes 12 MMAs of M = 128, N = 64, K = 16 per 16 columns of k (B's imaginary
-// part is staged twice, with both signs; a sign flip is exact in bf16). One
-// CTA of 128 threads owns a 128 x 64 tile of C. k runs in chunks of 32: each
-// chunk's operands are split and stored in shared memory in the canonical
-// K-major layout without swizzle (8 x 16-byte core matrices), thread 0 issues
-// its MMAs into two TMEM accumulators (Re, Im; 64 columns each: 128 TMEM
-// columns) and commits them to an mbarrier, and the next chunk's operands are
-// loaded into registers while those MMAs run. After the last chunk the four
-// warps read their 32 TMEM lanes back (tcgen05.ld 32x32b) and subtract from
-// C, whose first 16 columns are loaded while the last MMAs run: C is read and
-// written once for the whole rank-k update. Waits are bounded: on time-out
-// the kernel raises *err, still frees its TMEM and leaves C untouched.
-//
-// From k = 64 (the LU's rank-128 updates) a second path splits the operands
-// once and streams them by bulk copies (k_tc_split_a/b, k_cgemm_sub_tc2,
-// below).
+// The operands are split once into fp16 hi / lo parts of power-of-two scaled
+// rows (A) and columns (B) (k_tc_split_a/b), laid out as the tensor cores'
+// shared-memory operand tiles: K-major, no swizzle, 8 x 16-byte core
+// matrices. A real product is hi hi + hi lo + lo hi (FP32 accumulation in
+// TMEM), and B's tile holds its parts in the order -Bi, Br, Bi (hi, then lo),
+// so that [Br | Bi] and [-Bi | Br] are each one 128-row operand: with
+//   Re + i Im = Ar [Br | Bi] + Ai [-Bi | Br]
+// the 128 x 64 tile of C takes 6 MMAs of M = 128, N = 128, K = 16 per 16
+// columns of k into one 128-column accumulator (Re, Im side by side): half
+// the MMAs, and a third less shared-memory operand traffic, than separate
+// 64-column products. Two update kernels share the layout and the epilogue
+// arithmetic, so they give the same bits: k_cgemm_sub_tc2, one CTA per
+// 128 x 64 tile of C, and k_cgemm_sub_tc3, one persistent CTA per SM with its
+// row tile's A resident and the roles split by warp.
 #include <algorithm>
 
 #include <cuda.h>
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 #include "om_internal.h"
@@ -36,11 +30,9 @@ namespace om {
 namespace {
 
 constexpr int kTcM = 128, kTcN = 64, kTcK = 32;
-constexpr uint32_t kTmemCols = 128;  // 2 x 64 accumulator columns
-// shared-memory operand tiles (bf16): A parts 128 x 32, B parts 64 x 32
-// (Ar, Ai, Br, Bi, -Bi: hi and lo each)
+// shared-memory operand tiles (fp16): A parts 128 x 32 (Ar, Ai: hi and lo),
+// B parts 64 x 32 (-Bi, Br, Bi: hi, then lo)
 constexpr int kAPart = kTcM * kTcK * 2, kBPart = kTcN * kTcK * 2;
-constexpr int kTcSmem = 4 * kAPart + 6 * kBPart + 64;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -57,66 +49,49 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-// Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
-                            ((uint32_t)(kTcM >> 4) << 24);
+// Instruction descriptor, kind::f16: D F32, A and B F16, both K-major (the
+// pre-split operands below).
+constexpr uint32_t kIdescF16 = (1u << 4) | ((uint32_t)((2 * kTcN) >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(acc));
+      "l"(adesc), "l"(bdesc), "r"(kIdescF16), "r"(acc));
+}
+
+// The 12 MMAs (N = 128) of one 32-column chunk of k (two K-steps of 16) into
+// the accumulator d (Re: columns 0-63, Im: 64-127), from the chunk's operand
+// tiles at shared addresses a (Arh, Arl, Aih, Ail, kAPart bytes apart) and b
+// (-Bih, Brh, Bih, -Bil, Brl, Bil, kBPart apart). A descriptor is a fixed
+// template plus the address / 16: the address field takes the low 14 bits and
+// cannot carry into the next field below 256 KB, so the issuing thread spends
+// one add per operand.
+constexpr int kAPartB = kTcM * kTcK * 2, kBPartB = kTcN * kTcK * 2;  // (= kAPart, kBPart)
+__device__ __forceinline__ void mma_chunk(uint32_t d, uint32_t a, uint32_t b, bool first) {
+  const uint64_t tmpl = umma_desc(0, 128, 512);
+  constexpr uint32_t dA = kAPartB >> 4, dB = kBPartB >> 4;
+#pragma unroll
+  for(int st = 0; st < kTcK / 16; ++st) {
+    const uint64_t A0 = tmpl + ((a >> 4) + 16u * st), B0 = tmpl + ((b >> 4) + 16u * st);
+    const uint64_t Arh = A0, Arl = A0 + dA, Aih = A0 + 2 * dA, Ail = A0 + 3 * dA;
+    const uint64_t NBh = B0, BRh = B0 + dB, NBl = B0 + 3 * dB, BRl = B0 + 4 * dB;  // [-Bi | Br], [Br | Bi]
+    const uint32_t acc = !first || st > 0;
+    mma_f16(d, Arh, BRh, acc);  // Ar [Br | Bi]
+    mma_f16(d, Arh, BRl, 1);
+    mma_f16(d, Arl, BRh, 1);
+    mma_f16(d, Aih, NBh, 1);    // Ai [-Bi | Br]
+    mma_f16(d, Aih, NBl, 1);
+    mma_f16(d, Ail, NBh, 1);
+  }
 }
 
 // byte offset of element (row r, k index c) in a K-major no-swizzle tile with
-// 32 columns of K: core matrices of 8 rows x 8 bf16, K-adjacent ones 128 B
+// 32 columns of K: core matrices of 8 rows x 8 fp16, K-adjacent ones 128 B
 // apart (LBO), row-adjacent ones 512 B apart (SBO)
 __device__ __forceinline__ int kmajor_off(int r, int c) {
   return (r >> 3) * 512 + (c >> 3) * 128 + (r & 7) * 16 + (c & 7) * 2;
-}
-
-// Two FP32 values split into bf16 hi and lo parts, packed as bf16x2
-// (the first value in the low half): hi = bf16(x), lo = bf16(x - hi), both
-// rounded to nearest.
-__device__ __forceinline__ void split2(float a, float b, uint32_t &hi, uint32_t &lo) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  const float2 hf = __bfloat1622float2(h);
-  const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
-  hi = *reinterpret_cast<const uint32_t *>(&h);
-  lo = *reinterpret_cast<const uint32_t *>(&l);
-}
-
-__device__ __forceinline__ void st_shared_v4(unsigned char *p, uint32_t x, uint32_t y, uint32_t z,
-                                             uint32_t w) {
-  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(smem_addr(p)), "r"(x), "r"(y), "r"(z),
-               "r"(w)
-               : "memory");
-}
-
-// Eight K-consecutive complex values of one row (v[0..7]) into one 16-byte
-// core-matrix row of each part: the real parts' hi / lo, the imaginary parts'
-// hi / lo, and (for B) the negated imaginary parts' hi / lo, whose bf16 values
-// are those of the imaginary parts with the sign bit flipped (rounding to
-// nearest is symmetric).
-__device__ __forceinline__ void stage8(const float2 *v, int off, unsigned char *rh, unsigned char *rl,
-                                       unsigned char *ih, unsigned char *il, unsigned char *nh,
-                                       unsigned char *nl) {
-  uint32_t a[4], b[4], c[4], d[4];
-#pragma unroll
-  for(int p = 0; p < 4; ++p) {
-    split2(v[2 * p].x, v[2 * p + 1].x, a[p], b[p]);
-    split2(v[2 * p].y, v[2 * p + 1].y, c[p], d[p]);
-  }
-  st_shared_v4(rh + off, a[0], a[1], a[2], a[3]);
-  st_shared_v4(rl + off, b[0], b[1], b[2], b[3]);
-  st_shared_v4(ih + off, c[0], c[1], c[2], c[3]);
-  st_shared_v4(il + off, d[0], d[1], d[2], d[3]);
-  if(nh) {
-    constexpr uint32_t sgn = 0x80008000u;
-    st_shared_v4(nh + off, c[0] ^ sgn, c[1] ^ sgn, c[2] ^ sgn, c[3] ^ sgn);
-    st_shared_v4(nl + off, d[0] ^ sgn, d[1] ^ sgn, d[2] ^ sgn, d[3] ^ sgn);
-  }
 }
 
 // Bounded wait for the completion of the mbarrier phase of the given parity;
@@ -135,258 +110,169 @@ __device__ __forceinline__ uint32_t wait_phase(uint64_t *mbar, uint32_t parity) 
   return done;
 }
 
-__global__ void __launch_bounds__(128, 3) k_cgemm_sub_tc(const float2 *A, long lda, const float2 *B,
-                                                      long ldb, float2 *C, long ldc, long m, long n,
-                                                      int k, int *err) {
-  extern __shared__ __align__(1024) unsigned char tsm[];
-  unsigned char *Arh = tsm, *Arl = tsm + kAPart, *Aih = tsm + 2 * kAPart, *Ail = tsm + 3 * kAPart;
-  unsigned char *Brh = tsm + 4 * kAPart, *Brl = Brh + kBPart, *Bih = Brh + 2 * kBPart,
-                *Bil = Brh + 3 * kBPart, *Bnh = Brh + 4 * kBPart, *Bnl = Brh + 5 * kBPart;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(tsm + 4 * kAPart + 6 * kBPart);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tsm + 4 * kAPart + 6 * kBPart + 16);
-  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const long r0 = (long)blockIdx.x * kTcM, c0 = (long)blockIdx.y * kTcN;
-
-  if(warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_addr(tmem_slot)),
-                 "r"(kTmemCols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  if(t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(1));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-
-  // K runs in chunks of kTcK columns through the one set of operand tiles.
-  // Chunk q + 1 is loaded into registers while the MMAs of chunk q run, and
-  // is stored to shared memory once those MMAs have completed (mbarrier
-  // phase q). A tile: thread t owns row r0 + t (coalesced down each column);
-  // B tile as N x K: thread t owns column c0 + t / 2, half of the chunk
-  // (contiguous in memory).
-  // the C tile's lines requested into L2 now, so that its DRAM reads overlap
-  // the operand staging and the MMAs: thread t covers column t / 2, rows
-  // (t & 1) 64 .. (t & 1) 64 + 63 (four 128-byte lines)
-  {
-    const long col = c0 + (t >> 1);
-    if(col < n) {
-#pragma unroll
-      for(int i = 0; i < 4; ++i) {
-        const long row = r0 + (t & 1) * 64 + 16 * i;
-        if(row < m)
-          asm volatile("prefetch.global.L2 [%0];" ::"l"(C + col * ldc + row));
-      }
-    }
-  }
-  const int nq = (k + kTcK - 1) / kTcK;
-  // B's chunks start at even offsets of 16-byte aligned columns when B is
-  // 16-byte aligned and ldb is even
-  const bool bvec = ((reinterpret_cast<uintptr_t>(B) & 15) == 0) && ((ldb & 1) == 0);
-  const long ra = r0 + t;
-  const int jb = t >> 1, cb = (t & 1) * 16;
-  const long colb = c0 + jb;
-  float2 av[kTcK], bv[16];
-  auto load_chunk = [&](int q) {
-    const int kq = q * kTcK;
-#pragma unroll
-    for(int c = 0; c < kTcK; ++c)
-      av[c] = (kq + c < k && ra < m) ? A[(long)(kq + c) * lda + ra] : make_float2(0.f, 0.f);
-    if(bvec && kq + cb + 16 <= k && colb < n) {  // 16-byte loads
-      const float4 *src = reinterpret_cast<const float4 *>(B + colb * ldb + kq + cb);
-#pragma unroll
-      for(int c = 0; c < 8; ++c) {
-        const float4 w = src[c];
-        bv[2 * c] = make_float2(w.x, w.y);
-        bv[2 * c + 1] = make_float2(w.z, w.w);
-      }
-    } else {
-#pragma unroll
-      for(int c = 0; c < 16; ++c)
-        bv[c] = (kq + cb + c < k && colb < n) ? B[colb * ldb + kq + cb + c] : make_float2(0.f, 0.f);
-    }
-  };
-  load_chunk(0);
-  uint32_t tmem = 0;
-  bool ok = true;
-  for(int q = 0; q < nq; ++q) {
-    uint32_t done = 1;
-    if(q > 0)  // the MMAs of chunk q - 1 have read the tiles
-      done = wait_phase(mbar, (uint32_t)(q - 1) & 1u);
-#pragma unroll
-    for(int g = 0; g < kTcK / 8; ++g)
-      stage8(av + 8 * g, kmajor_off(t, 8 * g), Arh, Arl, Aih, Ail, nullptr, nullptr);
-#pragma unroll
-    for(int g = 0; g < 2; ++g)
-      stage8(bv + 8 * g, kmajor_off(jb, cb + 8 * g), Brh, Brl, Bih, Bil, Bnh, Bnl);
-    // generic-proxy stores -> visible to the tensor core (async proxy)
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    done = __syncthreads_and(done);  // one decision for the whole CTA
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    tmem = *tmem_slot;
-    if(!done) {
-      ok = false;
-      break;
-    }
-    if(t == 0) {
-      const uint32_t d_re = tmem, d_im = tmem + kTcN;
-      for(int s = 0; s < kTcK / 16; ++s) {
-        const uint32_t ko = s * 256;  // two core matrices along K per MMA
-        auto da = [&](unsigned char *p) { return umma_desc(smem_addr(p) + ko, 128, 512); };
-        const uint32_t acc = q > 0 || s > 0;  // the first K step overwrites the accumulators
-        // Re: Ar Br + Ai (-Bi)
-        mma_bf16(d_re, da(Arh), da(Brh), acc);
-        mma_bf16(d_re, da(Arh), da(Brl), 1);
-        mma_bf16(d_re, da(Arl), da(Brh), 1);
-        mma_bf16(d_re, da(Aih), da(Bnh), 1);
-        mma_bf16(d_re, da(Aih), da(Bnl), 1);
-        mma_bf16(d_re, da(Ail), da(Bnh), 1);
-        // Im: Ar Bi + Ai Br
-        mma_bf16(d_im, da(Arh), da(Bih), acc);
-        mma_bf16(d_im, da(Arh), da(Bil), 1);
-        mma_bf16(d_im, da(Arl), da(Bih), 1);
-        mma_bf16(d_im, da(Aih), da(Brh), 1);
-        mma_bf16(d_im, da(Aih), da(Brl), 1);
-        mma_bf16(d_im, da(Ail), da(Brh), 1);
-      }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_addr(mbar))
-          : "memory");
-    }
-    if(q + 1 < nq)
-      load_chunk(q + 1);
-  }
-  const uint32_t d_re = tmem, d_im = tmem + kTcN;
-
-  // columns 0 .. 31 of this thread's row of C, loaded while the last MMAs
-  // run; columns 32 .. 47 and 48 .. 63 follow into the registers of the
-  // 16 columns just done
-  const long r = r0 + warp * 32 + lane;
-  float2 cv[32];
-#pragma unroll
-  for(int q = 0; q < 32; ++q) {
-    const long col = c0 + q;
-    cv[q] = (r < m && col < n) ? C[col * ldc + r] : make_float2(0.f, 0.f);
-  }
-  // bounded wait for the last chunk's MMAs (phase nq - 1 of the mbarrier)
-  uint32_t done = ok ? wait_phase(mbar, (uint32_t)(nq - 1) & 1u) : 0u;
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  done = __syncthreads_and(done);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if(!done) {
-    if(t == 0)
-      atomicExch(err, 1);
-  } else {
-    // warp w reads TMEM lanes 32 w .. 32 w + 31 = rows r0 + 32 w + lane
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-#pragma unroll
-    for(int g = 0; g < kTcN / 16; ++g) {
-      const int cc = 16 * g, base = (g & 1) * 16;
-      uint32_t a[16], b[16];
-#define OM_TMEM_LD16(dst, addr)                                                                     \
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
-               : "=r"(dst[0]), "=r"(dst[1]), "=r"(dst[2]), "=r"(dst[3]), "=r"(dst[4]), "=r"(dst[5]),  \
-                 "=r"(dst[6]), "=r"(dst[7]), "=r"(dst[8]), "=r"(dst[9]), "=r"(dst[10]),              \
-                 "=r"(dst[11]), "=r"(dst[12]), "=r"(dst[13]), "=r"(dst[14]), "=r"(dst[15])           \
-               : "r"(addr))
-      OM_TMEM_LD16(a, d_re + lane_base + cc);
-      OM_TMEM_LD16(b, d_im + lane_base + cc);
-#undef OM_TMEM_LD16
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if(r < m) {
-#pragma unroll
-        for(int q = 0; q < 16; ++q) {
-          const long col = c0 + cc + q;
-          if(col < n) {
-            float2 v = cv[base + q];
-            v.x -= __uint_as_float(a[q]);
-            v.y -= __uint_as_float(b[q]);
-            C[col * ldc + r] = v;
-          }
-        }
-      }
-      if(g < 2) {
-#pragma unroll
-        for(int q = 0; q < 16; ++q) {
-          const long col = c0 + cc + 32 + q;
-          cv[base + q] = (r < m && col < n) ? C[col * ldc + r] : make_float2(0.f, 0.f);
-        }
-      }
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if(warp == 0) {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
-  }
-}
-
 // --- pre-split operands, streamed by bulk copies --------------------------
 //
-// For the LU's rank-128 trailing updates the operands are split once, before
-// the update: L21 (m x k) and U12 (k x n) go to bf16 hi / lo parts laid out
-// exactly as the shared-memory tiles above (per 128-row tile of A or 64-column
-// tile of B and per 32-column chunk of k: the parts one after another, each
-// in the K-major core-matrix layout). The update kernel then copies each
-// chunk's tiles with one-dimensional bulk copies (cp.async.bulk, completion
-// counted on an mbarrier) into one of two shared-memory stages, so that no
-// thread converts or stores operands in the loop. The real part is kept as
-// two accumulators (Ar Br and Ai Bi, subtracted in the epilogue) instead of
-// staging -Bi, which leaves 48 KB a stage: two stages and two CTAs per SM.
-constexpr int kStageA = 4 * kAPart, kStageB = 4 * kBPart, kStage = kStageA + kStageB;
+// For the LU's trailing updates the operands are split once, before the
+// update, into fp16 hi / lo parts of power-of-two scaled values: each row of
+// L21 (m x k) is scaled by sa = 2^e so that its largest component lies in
+// [2^14, 2^15), each column of U12 (k x n) likewise by sb, and x sa = hi + lo
+// with hi = fp16(x sa), lo = fp16(x sa - hi). The scaled values keep 22
+// significant bits (11 in each part); lo stays a normal fp16 number for every
+// entry within 2^-17 of its row's (column's) largest, and below that its
+// absolute error is under 2^-39 of the largest. A real product is
+// hi hi + hi lo + lo hi (three MMAs, FP32 accumulation), so the update carries
+// about 21 significant bits relative to the rows' and columns' magnitudes,
+// against about 17 for bf16 parts without scaling. The epilogue takes the
+// accumulators times 1 / (sa sb), exactly (powers of two). The parts are laid
+// out exactly as the shared-memory tiles above (per 128-row tile of A or
+// 64-column tile of B and per 32-column chunk of k: the parts one after
+// another, each in the K-major core-matrix layout), followed by the inverse
+// scales (float per row of A, then per column of B). The update kernels copy
+// each chunk's tiles with one-dimensional bulk copies (cp.async.bulk,
+// completion counted on an mbarrier), so that no thread converts or stores
+// operands in the loop. The real part is kept as two accumulators (Ar Br and
+// Ai Bi, subtracted in the epilogue) instead of staging -Bi.
+constexpr int kStageA = 4 * kAPart, kStageB = 6 * kBPart, kStage = kStageA + kStageB;
 constexpr int kTc2Smem = 2 * kStage + 128;
-constexpr uint32_t kTmem2Cols = 256;  // three 64-column accumulators
+constexpr uint32_t kTmem2Cols = 128;  // one 128-column accumulator (Re, Im)
 
-// A (m x k, lda) -> per (row tile, chunk): Arh, Arl, Aih, Ail (8 KB each).
-// One CTA of 512 threads per (row tile, chunk): thread t takes row t % 128
-// and the chunk's K columns 8 (t / 128) .. 8 (t / 128) + 7.
+// Two scaled FP32 values split into fp16 hi and lo parts, packed as half2
+// (the first value in the low half).
+__device__ __forceinline__ void split2_f16(float a, float b, uint32_t &hi, uint32_t &lo) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 hf = __half22float2(h);
+  const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<const uint32_t *>(&h);
+  lo = *reinterpret_cast<const uint32_t *>(&l);
+}
+
+// 2^e with max |x| 2^e in [2^14, 2^15) (1 for a zero row or column)
+__device__ __forceinline__ float split_scale(float amax) {
+  if(!(amax > 0.f))
+    return 1.f;
+  int e;
+  frexpf(amax, &e);  // amax = f 2^e, f in [0.5, 1)
+  return ldexpf(1.f, 15 - e);
+}
+
+// A (m x k, lda) -> per (row tile, chunk): Arh, Arl, Aih, Ail (8 KB each),
+// and 1 / sa per row (inv_a). One CTA of 512 threads per row tile: thread t
+// takes row t % 128 and, in every chunk, the K columns 8 (t / 128) ..
+// 8 (t / 128) + 7; a first pass finds the row's largest component.
 __global__ void __launch_bounds__(512) k_tc_split_a(const float2 *A, long lda, long m, int k, int nq,
-                                                    unsigned char *out) {
+                                                    unsigned char *out, float *inv_a) {
+  __shared__ float part_max[4][kTcM];
+  __shared__ float scale_s[kTcM];
   const int t = threadIdx.x, r = t & 127, g = t >> 7;
   const long row = (long)blockIdx.x * kTcM + r;
-  const int q = blockIdx.y, k0 = q * kTcK + 8 * g;
-  float2 v[8];
+  float amax = 0.f;
+  for(int q = 0; q < nq; ++q) {
+    const int k0 = q * kTcK + 8 * g;
 #pragma unroll
-  for(int j = 0; j < 8; ++j)
-    v[j] = (row < m && k0 + j < k) ? A[(long)(k0 + j) * lda + row] : make_float2(0.f, 0.f);
-  uint32_t a[4], b[4], c[4], d[4];
-#pragma unroll
-  for(int p = 0; p < 4; ++p) {
-    split2(v[2 * p].x, v[2 * p + 1].x, a[p], b[p]);
-    split2(v[2 * p].y, v[2 * p + 1].y, c[p], d[p]);
+    for(int j = 0; j < 8; ++j)
+      if(row < m && k0 + j < k) {
+        const float2 v = A[(long)(k0 + j) * lda + row];
+        amax = fmaxf(amax, fmaxf(fabsf(v.x), fabsf(v.y)));
+      }
   }
-  unsigned char *o = out + ((size_t)blockIdx.x * nq + q) * kStageA + kmajor_off(r, 8 * g);
-  *reinterpret_cast<uint4 *>(o) = make_uint4(a[0], a[1], a[2], a[3]);
-  *reinterpret_cast<uint4 *>(o + kAPart) = make_uint4(b[0], b[1], b[2], b[3]);
-  *reinterpret_cast<uint4 *>(o + 2 * kAPart) = make_uint4(c[0], c[1], c[2], c[3]);
-  *reinterpret_cast<uint4 *>(o + 3 * kAPart) = make_uint4(d[0], d[1], d[2], d[3]);
+  part_max[g][r] = amax;
+  __syncthreads();
+  if(g == 0) {
+    const float sc = split_scale(fmaxf(fmaxf(part_max[0][r], part_max[1][r]), fmaxf(part_max[2][r], part_max[3][r])));
+    scale_s[r] = sc;
+    if(row < m)
+      inv_a[row] = 1.f / sc;
+  }
+  __syncthreads();
+  const float sc = scale_s[r];
+  for(int q = 0; q < nq; ++q) {
+    const int k0 = q * kTcK + 8 * g;
+    float2 v[8];
+#pragma unroll
+    for(int j = 0; j < 8; ++j) {
+      v[j] = (row < m && k0 + j < k) ? A[(long)(k0 + j) * lda + row] : make_float2(0.f, 0.f);
+      v[j].x *= sc;
+      v[j].y *= sc;
+    }
+    uint32_t a[4], b[4], c[4], d[4];
+#pragma unroll
+    for(int p = 0; p < 4; ++p) {
+      split2_f16(v[2 * p].x, v[2 * p + 1].x, a[p], b[p]);
+      split2_f16(v[2 * p].y, v[2 * p + 1].y, c[p], d[p]);
+    }
+    unsigned char *o = out + ((size_t)blockIdx.x * nq + q) * kStageA + kmajor_off(r, 8 * g);
+    *reinterpret_cast<uint4 *>(o) = make_uint4(a[0], a[1], a[2], a[3]);
+    *reinterpret_cast<uint4 *>(o + kAPart) = make_uint4(b[0], b[1], b[2], b[3]);
+    *reinterpret_cast<uint4 *>(o + 2 * kAPart) = make_uint4(c[0], c[1], c[2], c[3]);
+    *reinterpret_cast<uint4 *>(o + 3 * kAPart) = make_uint4(d[0], d[1], d[2], d[3]);
+  }
 }
 
 // B (k x n, ldb) -> per (column tile, chunk): Brh, Brl, Bih, Bil (4 KB each),
-// as N x K. One CTA of 256 threads per (column tile, chunk): thread t takes
-// column t % 64 and the chunk's K rows 8 (t / 64) .. 8 (t / 64) + 7.
+// as N x K, and 1 / sb per column (inv_b). One CTA of 256 threads per column
+// tile: thread t takes column t % 64 and, in every chunk, the K rows
+// 8 (t / 64) .. 8 (t / 64) + 7.
 __global__ void __launch_bounds__(256) k_tc_split_b(const float2 *B, long ldb, long n, int k, int nq,
-                                                    unsigned char *out) {
+                                                    unsigned char *out, float *inv_b) {
+  __shared__ float part_max[4][kTcN];
+  __shared__ float scale_s[kTcN];
   const int t = threadIdx.x, j = t & 63, g = t >> 6;
   const long col = (long)blockIdx.x * kTcN + j;
-  const int q = blockIdx.y, k0 = q * kTcK + 8 * g;
-  float2 v[8];
+  float amax = 0.f;
+  for(int q = 0; q < nq; ++q) {
+    const int k0 = q * kTcK + 8 * g;
 #pragma unroll
-  for(int i = 0; i < 8; ++i)
-    v[i] = (col < n && k0 + i < k) ? B[col * ldb + k0 + i] : make_float2(0.f, 0.f);
-  uint32_t a[4], b[4], c[4], d[4];
-#pragma unroll
-  for(int p = 0; p < 4; ++p) {
-    split2(v[2 * p].x, v[2 * p + 1].x, a[p], b[p]);
-    split2(v[2 * p].y, v[2 * p + 1].y, c[p], d[p]);
+    for(int i = 0; i < 8; ++i)
+      if(col < n && k0 + i < k) {
+        const float2 v = B[col * ldb + k0 + i];
+        amax = fmaxf(amax, fmaxf(fabsf(v.x), fabsf(v.y)));
+      }
   }
-  unsigned char *o = out + ((size_t)blockIdx.x * nq + q) * kStageB + kmajor_off(j, 8 * g);
-  *reinterpret_cast<uint4 *>(o) = make_uint4(a[0], a[1], a[2], a[3]);
-  *reinterpret_cast<uint4 *>(o + kBPart) = make_uint4(b[0], b[1], b[2], b[3]);
-  *reinterpret_cast<uint4 *>(o + 2 * kBPart) = make_uint4(c[0], c[1], c[2], c[3]);
-  *reinterpret_cast<uint4 *>(o + 3 * kBPart) = make_uint4(d[0], d[1], d[2], d[3]);
+  part_max[g][j] = amax;
+  __syncthreads();
+  if(g == 0) {
+    const float sc = split_scale(fmaxf(fmaxf(part_max[0][j], part_max[1][j]), fmaxf(part_max[2][j], part_max[3][j])));
+    scale_s[j] = sc;
+    if(col < n)
+      inv_b[col] = 1.f / sc;
+  }
+  __syncthreads();
+  const float sc = scale_s[j];
+  for(int q = 0; q < nq; ++q) {
+    const int k0 = q * kTcK + 8 * g;
+    float2 v[8];
+#pragma unroll
+    for(int i = 0; i < 8; ++i) {
+      v[i] = (col < n && k0 + i < k) ? B[col * ldb + k0 + i] : make_float2(0.f, 0.f);
+      v[i].x *= sc;
+      v[i].y *= sc;
+    }
+    uint32_t a[4], b[4], c[4], d[4];
+#pragma unroll
+    for(int p = 0; p < 4; ++p) {
+      split2_f16(v[2 * p].x, v[2 * p + 1].x, a[p], b[p]);
+      split2_f16(v[2 * p].y, v[2 * p + 1].y, c[p], d[p]);
+    }
+    // parts -Bih, Brh, Bih, -Bil, Brl, Bil (a sign flip is exact in fp16)
+    constexpr uint32_t sgn = 0x80008000u;
+    unsigned char *o = out + ((size_t)blockIdx.x * nq + q) * kStageB + kmajor_off(j, 8 * g);
+    *reinterpret_cast<uint4 *>(o) = make_uint4(c[0] ^ sgn, c[1] ^ sgn, c[2] ^ sgn, c[3] ^ sgn);
+    *reinterpret_cast<uint4 *>(o + kBPart) = make_uint4(a[0], a[1], a[2], a[3]);
+    *reinterpret_cast<uint4 *>(o + 2 * kBPart) = make_uint4(c[0], c[1], c[2], c[3]);
+    *reinterpret_cast<uint4 *>(o + 3 * kBPart) = make_uint4(d[0] ^ sgn, d[1] ^ sgn, d[2] ^ sgn, d[3] ^ sgn);
+    *reinterpret_cast<uint4 *>(o + 4 * kBPart) = make_uint4(b[0], b[1], b[2], b[3]);
+    *reinterpret_cast<uint4 *>(o + 5 * kBPart) = make_uint4(d[0], d[1], d[2], d[3]);
+  }
+}
+
+// C entry minus the unscaled accumulators (re, im) / (sa sb), with the
+// inverse scales applied one after the other (each product exact unless the
+// result itself leaves FP32's range) and every operation written out, so that
+// both update kernels round alike.
+__device__ __forceinline__ float2 unscale_sub(float2 v, uint32_t re, uint32_t im, float sa, float sb) {
+  const float rv = __fmul_rn(__fmul_rn(__uint_as_float(re), sa), sb);
+  const float iv = __fmul_rn(__fmul_rn(__uint_as_float(im), sa), sb);
+  return make_float2(__fsub_rn(v.x, rv), __fsub_rn(v.y, iv));
 }
 
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
@@ -410,8 +296,8 @@ __device__ __forceinline__ void arrive_expect(uint64_t *bar, uint32_t bytes) {
 // Waits are bounded: on time-out the kernel raises *err, frees its TMEM and
 // leaves C untouched.
 __global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, const unsigned char *Bs,
-                                                       int nq, float2 *C, long ldc, long m, long n,
-                                                       int *err) {
+                                                       const float *inv_a, const float *inv_b, int nq,
+                                                       float2 *C, long ldc, long m, long n, int *err) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   uint64_t *full = reinterpret_cast<uint64_t *>(tsm + 2 * kStage);  // [2]
   uint64_t *empty = full + 2;                                        // [2]
@@ -448,7 +334,7 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, 
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t d_r1 = tmem, d_r2 = tmem + kTcN, d_im = tmem + 2 * kTcN;
+  const uint32_t d_re = tmem, d_im = tmem + kTcN;
 
   uint32_t ok = 1;
   if(t == 0) {
@@ -472,30 +358,7 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, 
       }
       landed = q + 1;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      unsigned char *Ar = tsm + s * kStage;
-      unsigned char *Arh = Ar, *Arl = Ar + kAPart, *Aih = Ar + 2 * kAPart, *Ail = Ar + 3 * kAPart;
-      unsigned char *Brh = Ar + kStageA, *Brl = Brh + kBPart, *Bih = Brh + 2 * kBPart,
-                    *Bil = Brh + 3 * kBPart;
-      for(int st = 0; st < kTcK / 16; ++st) {
-        const uint32_t ko = st * 256;  // two core matrices along K per MMA
-        auto da = [&](unsigned char *p) { return umma_desc(smem_addr(p) + ko, 128, 512); };
-        const uint32_t acc = q > 0 || st > 0;
-        // Ar Br
-        mma_bf16(d_r1, da(Arh), da(Brh), acc);
-        mma_bf16(d_r1, da(Arh), da(Brl), 1);
-        mma_bf16(d_r1, da(Arl), da(Brh), 1);
-        // Ai Bi
-        mma_bf16(d_r2, da(Aih), da(Bih), acc);
-        mma_bf16(d_r2, da(Aih), da(Bil), 1);
-        mma_bf16(d_r2, da(Ail), da(Bih), 1);
-        // Ar Bi + Ai Br
-        mma_bf16(d_im, da(Arh), da(Bih), acc);
-        mma_bf16(d_im, da(Arh), da(Bil), 1);
-        mma_bf16(d_im, da(Arl), da(Bih), 1);
-        mma_bf16(d_im, da(Aih), da(Brh), 1);
-        mma_bf16(d_im, da(Aih), da(Brl), 1);
-        mma_bf16(d_im, da(Ail), da(Brh), 1);
-      }
+      mma_chunk(d_re, smem_addr(tsm + s * kStage), smem_addr(tsm + s * kStage + kStageA), q == 0);
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
               smem_addr(empty + s))
@@ -518,6 +381,7 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, 
   }
   // columns 0 .. 31 of this thread's row of C, loaded while the MMAs run
   const long r = r0 + warp * 32 + lane;
+  const float sa = r < m ? inv_a[r] : 0.f;
   float2 cv[32];
 #pragma unroll
   for(int q = 0; q < 32; ++q) {
@@ -540,28 +404,26 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, 
 #pragma unroll
     for(int g = 0; g < kTcN / 16; ++g) {
       const int cc = 16 * g, base = (g & 1) * 16;
-      uint32_t a[16], b[16], c[16];
+      uint32_t a[16], c[16];
 #define OM_TMEM_LD16(dst, addr)                                                                     \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
                : "=r"(dst[0]), "=r"(dst[1]), "=r"(dst[2]), "=r"(dst[3]), "=r"(dst[4]), "=r"(dst[5]),  \
                  "=r"(dst[6]), "=r"(dst[7]), "=r"(dst[8]), "=r"(dst[9]), "=r"(dst[10]),              \
                  "=r"(dst[11]), "=r"(dst[12]), "=r"(dst[13]), "=r"(dst[14]), "=r"(dst[15])           \
                : "r"(addr))
-      OM_TMEM_LD16(a, d_r1 + lane_base + cc);
-      OM_TMEM_LD16(b, d_r2 + lane_base + cc);
+      OM_TMEM_LD16(a, d_re + lane_base + cc);
       OM_TMEM_LD16(c, d_im + lane_base + cc);
 #undef OM_TMEM_LD16
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if(r < m) {
+      {
+        const long lcol = c0 + cc + (lane & 15);
+        const float sbl = lcol < n ? inv_b[lcol] : 0.f;
 #pragma unroll
         for(int q = 0; q < 16; ++q) {
+          const float sb = __shfl_sync(0xffffffffu, sbl, q);
           const long col = c0 + cc + q;
-          if(col < n) {
-            float2 v = cv[base + q];
-            v.x -= __uint_as_float(a[q]) - __uint_as_float(b[q]);
-            v.y -= __uint_as_float(c[q]);
-            C[col * ldc + r] = v;
-          }
+          if(r < m && col < n)
+            C[col * ldc + r] = unscale_sub(cv[base + q], a[q], c[q], sa, sb);
         }
       }
       if(g < 2) {
@@ -585,30 +447,44 @@ __global__ void __launch_bounds__(128) k_cgemm_sub_tc2(const unsigned char *As, 
 // Persistent form of the split-operand update, one CTA per SM. The CTA takes a
 // contiguous range of the 128 x 64 tiles in row-tile-major order, so its A
 // tiles (all nq <= 4 chunks: up to 128 KB) stay resident in shared memory
-// while it walks the column tiles of a row tile; only B's chunks (16 KB) are
-// streamed, through a ring of three stages. The roles are split by warp:
+// while it walks the column tiles of a row tile; only B's chunks (24 KB) are
+// streamed, through a ring of two stages. The roles are split by warp:
 //   warps 0-3  epilogue: TMEM lanes 32 w .. 32 w + 31 (rows of the tile), C
-//              read from a shared-memory ring, C - AB stored to global;
+//              read from a shared-memory ring, C - AB stored to global (one
+//              consumer group, so that the ring's slots are consumed in the
+//              order they are filled: a second group working ahead on other
+//              columns could see a slot's previous fill as its own, since an
+//              mbarrier's phase parity only tells two phases apart);
 //   warp 4     operand copies (A when the row tile changes, B chunks);
 //   warp 5     TMEM allocation and the MMAs (one elected thread);
 //   warp 6     C copies: each tile's columns in groups of 16 (16 KB, one
 //              two-dimensional tensor copy) through a ring of three slots.
-// The accumulators (Ar Br, Ai Bi, Im: 3 x 64 TMEM columns) are double
+// The accumulator (Re, Im: 2 x 64 TMEM columns) is double
 // buffered, so the epilogue of one tile runs under the MMAs of the next, and
 // the C ring keeps up to 48 KB of C reads in flight per SM. Every wait is
 // bounded; a time-out raises *err and a shared abort flag that the other
 // roles poll, after which each role waits (bounded) for its own copies and
 // MMAs in flight, and the TMEM is freed.
 constexpr int kPThreads = 224;
-constexpr int kPMaxQ = 4;                      // k <= 128
-constexpr int kPBStages = 3, kPCSlots = 3;
+constexpr int kPProd = 4, kPMma = 5, kPCLoad = 6;  // the warps' roles (0-3: epilogue)
+constexpr int kPMaxQ = 4;                      // k <= 128 with A resident
+constexpr int kPBStages = 3, kPCSlots = 3;     // (stages: 2 with A resident, 3 streaming A)
+constexpr int kPCAhead = 2;                    // C tiles requested into L2 ahead of the ring
 constexpr int kPCSlot = 16 * kTcM * 8;         // 16 columns of 128 complex64
-constexpr int kPOffB = kPMaxQ * kStageA;       // 128 KB of resident A
-constexpr int kPOffC = kPOffB + kPBStages * kStageB;
-constexpr int kPOffBar = kPOffC + kPCSlots * kPCSlot;
-constexpr int kPSmem = kPOffBar + 256;
-constexpr uint32_t kPTmemCols = 512;           // two sets of three 64-column accumulators
-static_assert(kPSmem <= 227 * 1024, "persistent update: shared memory");
+// Shared-memory layout: with A resident (k <= 128), 128 KB of A, then two
+// stages of B chunks (24 KB); for larger k, three stages of an A chunk and a
+// B chunk (56 KB) each. Then the C ring and the barriers.
+template <bool kResA> struct PLayout {
+  static constexpr int stages = kResA ? 2 : 3;
+  static constexpr int offB = kResA ? kPMaxQ * kStageA : 0;
+  static constexpr int stage = kResA ? kStageB : kStageA + kStageB;
+  static constexpr int offC = offB + stages * stage;
+  static constexpr int offBar = offC + kPCSlots * kPCSlot;
+  static constexpr int smem = offBar + 256;
+};
+static_assert(PLayout<true>::smem <= 227 * 1024 && PLayout<false>::smem <= 227 * 1024,
+              "persistent update: shared memory");
+constexpr uint32_t kPTmemCols = 256;           // two 128-column accumulators (Re, Im)
 
 struct PBars {
   uint64_t a_full, a_empty, drain;
@@ -665,17 +541,25 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, in
       : "memory");
 }
 
+__device__ __forceinline__ void tma_prefetch_l2(const CUtensorMap *tm, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(tm), "r"(x), "r"(y)
+               : "memory");
+}
+
+template <bool kResA>
 __global__ void __launch_bounds__(kPThreads, 1)
-    k_cgemm_sub_tc3(const unsigned char *As, const unsigned char *Bs, int nq,
-                    const __grid_constant__ CUtensorMap cmap, float2 *C, long ldc, long m, long n, int *err) {
+    k_cgemm_sub_tc3(const unsigned char *As, const unsigned char *Bs, const float *inv_a, const float *inv_b,
+                    int nq, const __grid_constant__ CUtensorMap cmap, float2 *C, long ldc, long m, long n,
+                    int *err) {
   extern __shared__ __align__(1024) unsigned char psm[];
-  PBars *bars = reinterpret_cast<PBars *>(psm + kPOffBar);
+  typedef PLayout<kResA> L;
+  PBars *bars = reinterpret_cast<PBars *>(psm + L::offBar);
   volatile int *abort_flag = &bars->abort;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const long mt = (m + kTcM - 1) / kTcM, nt = (n + kTcN - 1) / kTcN, T = mt * nt;
   const long t0 = T * blockIdx.x / gridDim.x, t1 = T * (blockIdx.x + 1) / gridDim.x;
 
-  if(warp == 5) {
+  if(warp == kPMma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_addr(&bars->tmem)),
                  "r"(kPTmemCols));
@@ -688,7 +572,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
     init(&bars->a_full, 1);
     init(&bars->a_empty, 1);
     init(&bars->drain, 1);
-    for(int i = 0; i < kPBStages; ++i) {
+    for(int i = 0; i < L::stages; ++i) {
       init(bars->b_full + i, 1);
       init(bars->b_empty + i, 1);
     }
@@ -708,13 +592,13 @@ __global__ void __launch_bounds__(kPThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = bars->tmem;
 
-  if(warp == 4 && lane == 0) {
+  if(warp == kPProd && lane == 0) {
     // operand copies
     long prev_rt = -1, bq = 0;
     int a_loads = 0;
     for(long tile = t0; tile < t1 && !*abort_flag; ++tile) {
       const long rt = tile / nt, ct = tile - rt * nt;
-      if(rt != prev_rt) {
+      if(kResA && rt != prev_rt) {
         if(a_loads > 0 && !pwait(&bars->a_empty, (uint32_t)(a_loads - 1) & 1u, abort_flag, err))
           break;
         arrive_expect(&bars->a_full, (uint32_t)(nq * kStageA));
@@ -726,15 +610,21 @@ __global__ void __launch_bounds__(kPThreads, 1)
       }
       bool stop = false;
       for(int q = 0; q < nq; ++q, ++bq) {
-        const int s = (int)(bq % kPBStages);
-        if(bq >= kPBStages &&
-           !pwait(bars->b_empty + s, (uint32_t)(bq / kPBStages - 1) & 1u, abort_flag, err)) {
+        const int s = (int)(bq % L::stages);
+        if(bq >= L::stages &&
+           !pwait(bars->b_empty + s, (uint32_t)(bq / L::stages - 1) & 1u, abort_flag, err)) {
           stop = true;
           break;
         }
-        arrive_expect(bars->b_full + s, (uint32_t)kStageB);
-        bulk_load(psm + kPOffB + s * kStageB, Bs + ((size_t)ct * nq + q) * kStageB, (uint32_t)kStageB,
-                  bars->b_full + s);
+        unsigned char *dst = psm + L::offB + s * L::stage;
+        if(kResA) {
+          arrive_expect(bars->b_full + s, (uint32_t)kStageB);
+        } else {  // the A chunk too, ahead of B in the stage
+          arrive_expect(bars->b_full + s, (uint32_t)(kStageA + kStageB));
+          bulk_load(dst, As + ((size_t)rt * nq + q) * kStageA, (uint32_t)kStageA, bars->b_full + s);
+          dst += kStageA;
+        }
+        bulk_load(dst, Bs + ((size_t)ct * nq + q) * kStageB, (uint32_t)kStageB, bars->b_full + s);
       }
       if(stop)
         break;
@@ -742,15 +632,15 @@ __global__ void __launch_bounds__(kPThreads, 1)
     // the copies still in flight land before the CTA may exit (bounded)
     if(a_loads > 0)
       wait_phase(&bars->a_full, (uint32_t)(a_loads - 1) & 1u);
-    for(long q = bq - 1; q >= 0 && q >= bq - kPBStages; --q)
-      wait_phase(bars->b_full + q % kPBStages, (uint32_t)(q / kPBStages) & 1u);
-  } else if(warp == 5 && lane == 0) {
+    for(long q = bq - 1; q >= 0 && q >= bq - L::stages; --q)
+      wait_phase(bars->b_full + q % L::stages, (uint32_t)(q / L::stages) & 1u);
+  } else if(warp == kPMma && lane == 0) {
     // MMAs
     long prev_rt = -1, bq = 0;
     int a_loaded = 0;
     for(long tile = t0, j = 0; tile < t1 && !*abort_flag; ++tile, ++j) {
       const long rt = tile / nt;
-      if(rt != prev_rt) {
+      if(kResA && rt != prev_rt) {
         if(prev_rt >= 0)
           mma_commit(&bars->a_empty);  // the previous row tile's MMAs have read A
         if(!pwait(&bars->a_full, (uint32_t)a_loaded & 1u, abort_flag, err))
@@ -762,36 +652,20 @@ __global__ void __launch_bounds__(kPThreads, 1)
       if(j >= 2 && !pwait(bars->t_empty + as, (uint32_t)(j / 2 - 1) & 1u, abort_flag, err))
         break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t d_r1 = tmem + as * 3 * kTcN, d_r2 = d_r1 + kTcN, d_im = d_r1 + 2 * kTcN;
+      const uint32_t d_acc = tmem + as * 2 * kTcN;
       bool stop = false;
       for(int q = 0; q < nq; ++q, ++bq) {
-        const int s = (int)(bq % kPBStages);
-        if(!pwait(bars->b_full + s, (uint32_t)(bq / kPBStages) & 1u, abort_flag, err)) {
+        const int s = (int)(bq % L::stages);
+        if(!pwait(bars->b_full + s, (uint32_t)(bq / L::stages) & 1u, abort_flag, err)) {
           stop = true;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        unsigned char *Aq = psm + q * kStageA;
-        unsigned char *Arh = Aq, *Arl = Aq + kAPart, *Aih = Aq + 2 * kAPart, *Ail = Aq + 3 * kAPart;
-        unsigned char *Brh = psm + kPOffB + s * kStageB, *Brl = Brh + kBPart, *Bih = Brh + 2 * kBPart,
-                      *Bil = Brh + 3 * kBPart;
-        for(int st = 0; st < kTcK / 16; ++st) {
-          const uint32_t ko = st * 256;
-          auto da = [&](unsigned char *p) { return umma_desc(smem_addr(p) + ko, 128, 512); };
-          const uint32_t acc = q > 0 || st > 0;
-          mma_bf16(d_r1, da(Arh), da(Brh), acc);
-          mma_bf16(d_r1, da(Arh), da(Brl), 1);
-          mma_bf16(d_r1, da(Arl), da(Brh), 1);
-          mma_bf16(d_r2, da(Aih), da(Bih), acc);
-          mma_bf16(d_r2, da(Aih), da(Bil), 1);
-          mma_bf16(d_r2, da(Ail), da(Bih), 1);
-          mma_bf16(d_im, da(Arh), da(Bih), acc);
-          mma_bf16(d_im, da(Arh), da(Bil), 1);
-          mma_bf16(d_im, da(Arl), da(Bih), 1);
-          mma_bf16(d_im, da(Aih), da(Brh), 1);
-          mma_bf16(d_im, da(Aih), da(Brl), 1);
-          mma_bf16(d_im, da(Ail), da(Brh), 1);
-        }
+        const uint32_t stg = smem_addr(psm + L::offB + s * L::stage);
+        if(kResA)
+          mma_chunk(d_acc, smem_addr(psm + q * kStageA), stg, q == 0);
+        else
+          mma_chunk(d_acc, stg, stg + kStageA, q == 0);
         mma_commit(bars->b_empty + s);
       }
       if(stop)
@@ -801,13 +675,25 @@ __global__ void __launch_bounds__(kPThreads, 1)
     // every MMA issued has completed before the TMEM is freed (bounded)
     mma_commit(&bars->drain);
     wait_phase(&bars->drain, 0u);
-  } else if(warp == 6 && lane == 0) {
+  } else if(warp == kPCLoad && lane == 0) {
     // C copies: a 128 x 16 box per group (rows and columns past C's edge
-    // read as zeros and are not used)
+    // read as zeros and are not used). The tiles kPCAhead ahead are requested
+    // into L2 first, so that the shared-memory ring (three quarters of a
+    // tile) refills from L2 and the DRAM reads run ahead of the epilogue.
     long cq = 0;
+    auto prefetch_tile = [&](long tile) {
+      const long rt = tile / nt, ct = tile - rt * nt;
+      for(int g = 0; g < kTcN / 16; ++g)
+        if(ct * kTcN + 16 * g < n)
+          tma_prefetch_l2(&cmap, (int)(rt * kTcM), (int)(ct * kTcN + 16 * g));
+    };
+    for(long tile = t0; tile < t1 && tile < t0 + kPCAhead; ++tile)
+      prefetch_tile(tile);
     for(long tile = t0; tile < t1 && !*abort_flag; ++tile) {
       const long rt = tile / nt, ct = tile - rt * nt;
       const long r0 = rt * kTcM, c0 = ct * kTcN;
+      if(tile + kPCAhead < t1)
+        prefetch_tile(tile + kPCAhead);
       bool stop = false;
       for(int g = 0; g < kTcN / 16; ++g, ++cq) {
         const int s = (int)(cq % kPCSlots);
@@ -817,7 +703,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
           break;
         }
         arrive_expect(bars->c_full + s, (uint32_t)kPCSlot);
-        tma_load_2d(psm + kPOffC + s * kPCSlot, &cmap, (int)r0, (int)(c0 + 16 * g), bars->c_full + s);
+        tma_load_2d(psm + L::offC + s * kPCSlot, &cmap, (int)r0, (int)(c0 + 16 * g), bars->c_full + s);
       }
       if(stop)
         break;
@@ -827,30 +713,31 @@ __global__ void __launch_bounds__(kPThreads, 1)
   } else if(warp < 4) {
     // epilogue: thread (warp, lane) owns row 32 warp + lane of each tile
     // (decisions are made per warp: tcgen05.ld needs the whole warp)
-    long cq = 0;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const int quarter = warp;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     for(long tile = t0, j = 0; tile < t1; ++tile, ++j) {
       if(__any_sync(0xffffffffu, *abort_flag))
         break;
       const long rt = tile / nt, ct = tile - rt * nt;
-      const long r = rt * kTcM + warp * 32 + lane, c0 = ct * kTcN;
+      const long r = rt * kTcM + quarter * 32 + lane, c0 = ct * kTcN;
       const int as = (int)(j & 1);
       if(!__all_sync(0xffffffffu, pwait(bars->t_full + as, (uint32_t)(j / 2) & 1u, abort_flag, err)))
         break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t d_r1 = tmem + lane_base + as * 3 * kTcN, d_r2 = d_r1 + kTcN, d_im = d_r1 + 2 * kTcN;
+      const uint32_t d_re = tmem + lane_base + as * 2 * kTcN, d_im = d_re + kTcN;
+      const float sa = r < m ? inv_a[r] : 0.f;
       bool stop = false;
-      for(int g = 0; g < kTcN / 16; ++g, ++cq) {
+      for(int g = 0; g < kTcN / 16; ++g) {
+        const long cq = 4 * j + g;  // the C loader's group counter
         const int s = (int)(cq % kPCSlots);
-        uint32_t a[16], b[16], c[16];
+        uint32_t a[16], c[16];
 #define OM_TMEM_LD16(dst, addr)                                                                     \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
                : "=r"(dst[0]), "=r"(dst[1]), "=r"(dst[2]), "=r"(dst[3]), "=r"(dst[4]), "=r"(dst[5]),  \
                  "=r"(dst[6]), "=r"(dst[7]), "=r"(dst[8]), "=r"(dst[9]), "=r"(dst[10]),              \
                  "=r"(dst[11]), "=r"(dst[12]), "=r"(dst[13]), "=r"(dst[14]), "=r"(dst[15])           \
                : "r"(addr))
-        OM_TMEM_LD16(a, d_r1 + 16 * g);
-        OM_TMEM_LD16(b, d_r2 + 16 * g);
+        OM_TMEM_LD16(a, d_re + 16 * g);
         OM_TMEM_LD16(c, d_im + 16 * g);
 #undef OM_TMEM_LD16
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -858,18 +745,16 @@ __global__ void __launch_bounds__(kPThreads, 1)
           stop = true;
           break;
         }
-        const float2 *cs = reinterpret_cast<const float2 *>(psm + kPOffC + s * kPCSlot) + warp * 32 + lane;
-        if(r < m) {
+        const float2 *cs = reinterpret_cast<const float2 *>(psm + L::offC + s * kPCSlot) + quarter * 32 + lane;
+        // the group's 16 column scales: lane q % 16 loads column q's, shuffled
+        const long lcol = c0 + 16 * g + (lane & 15);
+        const float sbl = lcol < n ? inv_b[lcol] : 0.f;
 #pragma unroll
-          for(int q = 0; q < 16; ++q) {
-            const long col = c0 + 16 * g + q;
-            if(col < n) {
-              float2 v = cs[q * kTcM];
-              v.x -= __uint_as_float(a[q]) - __uint_as_float(b[q]);
-              v.y -= __uint_as_float(c[q]);
-              C[col * ldc + r] = v;
-            }
-          }
+        for(int q = 0; q < 16; ++q) {
+          const float sb = __shfl_sync(0xffffffffu, sbl, q);
+          const long col = c0 + 16 * g + q;
+          if(r < m && col < n)
+            C[col * ldc + r] = unscale_sub(cs[q * kTcM], a[q], c[q], sa, sb);
         }
         __syncwarp();
         if(lane == 0)
@@ -885,7 +770,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if(warp == 5) {
+  if(warp == kPMma) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPTmemCols));
   }
@@ -893,17 +778,10 @@ __global__ void __launch_bounds__(kPThreads, 1)
 
 }  // namespace
 
-void launch_cgemm_sub_tc(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
-                         float2 *C, long ldc, long m, long n, int k, int *d_err) {
-  cudaFuncSetAttribute(k_cgemm_sub_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-  dim3 grid((unsigned)((m + kTcM - 1) / kTcM), (unsigned)((n + kTcN - 1) / kTcN));
-  k_cgemm_sub_tc<<<grid, 128, kTcSmem, ctx->stream>>>(A, lda, B, ldb, C, ldc, m, n, k, d_err);
-  ctx->last_launches++;
-}
-
 size_t cgemm_sub_tc_split_bytes(long m, long n, int k) {
   const size_t nq = (size_t)((k + kTcK - 1) / kTcK);
-  return (size_t)((m + kTcM - 1) / kTcM) * nq * kStageA + (size_t)((n + kTcN - 1) / kTcN) * nq * kStageB;
+  const size_t mt = (size_t)((m + kTcM - 1) / kTcM), nt = (size_t)((n + kTcN - 1) / kTcN);
+  return mt * nq * kStageA + nt * nq * kStageB + sizeof(float) * (mt * kTcM + nt * kTcN);
 }
 
 void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const float2 *B, long ldb,
@@ -912,12 +790,14 @@ void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const
   const unsigned mt = (unsigned)((m + kTcM - 1) / kTcM), nt = (unsigned)((n + kTcN - 1) / kTcN);
   unsigned char *As = static_cast<unsigned char *>(scratch);
   unsigned char *Bs = As + (size_t)mt * nq * kStageA;
-  k_tc_split_a<<<dim3(mt, (unsigned)nq), 512, 0, ctx->stream>>>(A, lda, m, k, nq, As);
-  k_tc_split_b<<<dim3(nt, (unsigned)nq), 256, 0, ctx->stream>>>(B, ldb, n, k, nq, Bs);
+  float *inv_a = reinterpret_cast<float *>(Bs + (size_t)nt * nq * kStageB);
+  float *inv_b = inv_a + (size_t)mt * kTcM;
+  k_tc_split_a<<<mt, 512, 0, ctx->stream>>>(A, lda, m, k, nq, As, inv_a);
+  k_tc_split_b<<<nt, 256, 0, ctx->stream>>>(B, ldb, n, k, nq, Bs, inv_b);
   // the persistent form reads C by tensor copies: a 16-byte aligned base and
   // an even leading dimension (column stride a multiple of 16 bytes)
   alignas(64) CUtensorMap cmap;
-  bool persistent = ctx->lu_tc == 1 && nq <= kPMaxQ && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
+  bool persistent = ctx->lu_tc == 1 && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
                     (ldc & 1) == 0;
   if(persistent) {
     typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -934,13 +814,23 @@ void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   }
   if(persistent) {
-    cudaFuncSetAttribute(k_cgemm_sub_tc3, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem);
     const long tiles = (long)mt * nt;
     const unsigned grid = (unsigned)std::min<long>(tiles, ctx->sm_count);
-    k_cgemm_sub_tc3<<<grid, kPThreads, kPSmem, ctx->stream>>>(As, Bs, nq, cmap, C, ldc, m, n, d_err);
+    if(nq <= kPMaxQ) {  // A resident
+      cudaFuncSetAttribute(k_cgemm_sub_tc3<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           PLayout<true>::smem);
+      k_cgemm_sub_tc3<true><<<grid, kPThreads, PLayout<true>::smem, ctx->stream>>>(As, Bs, inv_a, inv_b, nq,
+                                                                                   cmap, C, ldc, m, n, d_err);
+    } else {  // A streamed with B
+      cudaFuncSetAttribute(k_cgemm_sub_tc3<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           PLayout<false>::smem);
+      k_cgemm_sub_tc3<false><<<grid, kPThreads, PLayout<false>::smem, ctx->stream>>>(
+          As, Bs, inv_a, inv_b, nq, cmap, C, ldc, m, n, d_err);
+    }
   } else {
     cudaFuncSetAttribute(k_cgemm_sub_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, kTc2Smem);
-    k_cgemm_sub_tc2<<<dim3(mt, nt), 128, kTc2Smem, ctx->stream>>>(As, Bs, nq, C, ldc, m, n, d_err);
+    k_cgemm_sub_tc2<<<dim3(mt, nt), 128, kTc2Smem, ctx->stream>>>(As, Bs, inv_a, inv_b, nq, C, ldc, m, n,
+                                                                  d_err);
   }
   ctx->last_launches += 3;
 }

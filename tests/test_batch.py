@@ -118,6 +118,34 @@ def test_alone_equals_in_the_batch(G, ctx, form):
     assert len({r["slot"] for r in together}) > 1
 
 
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_autotuned_tiles_do_not_change_the_bits(G, form):
+    """The batched matvecs' tile configurations (rows per tile, tile order,
+    CTAs per SM) fixed one at a time, and chosen by the autotuner: the same
+    bits, and the autotuner reports one choice per size class."""
+    reqs = ragged_requests(G, plain(G) if form == "plain" else mixed(G),
+                           G.C128 if form == "plain" else G.C64, seed=9)
+    runs = []
+    for cand in [0] + list(range(1, 9)):
+        c = G.Context(0)
+        c.tune(batch_tiles=cand)
+        runs.append(G.batch_solve(c, reqs))
+        if cand == 0:
+            chosen = G.batch_tiles(c)
+            assert len(chosen) >= 3  # the ragged requests span several size classes
+            assert len({(t["precision"], t["nmax"], t["Npad"]) for t in chosen}) == len(chosen)
+            assert all(t["rows"] in (128, 256) and t["ctas_per_sm"] in (2, 4, 8, 16) and t["matvec_us"] >= 0
+                       for t in chosen)
+        else:
+            assert G.batch_tiles(c) == []
+        c.close()
+    for other in runs[1:]:
+        for a, b in zip(runs[0], other):
+            assert a["status"] == b["status"] == G.OK
+            assert np.array_equal(a["xsec"], b["xsec"]) and np.array_equal(a["xsec_sh"], b["xsec_sh"])
+            assert a["ff"]["iterations"] == b["ff"]["iterations"]
+
+
 def test_failures_stay_with_their_request(G, ctx):
     rng = np.random.default_rng(3)
     xyz, rad = random_cluster(rng, 4, 800 * nm, 40 * nm, 60 * nm, 20 * nm)
