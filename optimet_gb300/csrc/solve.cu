@@ -1367,23 +1367,91 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
   }
 }
 
-// Apply the row interchanges of rows k .. k + nb - 1 (in order) to the
-// columns jlo .. jhi - 1 other than slo .. shi - 1 (the panel's own columns,
-// which the panel kernels swap themselves).
+// The row interchanges of rows k .. k + nb - 1 (pivots piv[k .. k + nb), in
+// order) as one permutation: (position, row) pairs, the new row at each
+// position they move; pos_row[0] = the count, then the pairs. One thread
+// (nb <= 256 steps): the rows at positions k .. k + nb - 1 in a table, the
+// rows moved below them in a list whose last entry for a position counts.
+constexpr int kPermMax = 256;  // interchanges per table
+__global__ void k_lu_perm_table(const int *piv, long k, int nb, long *pos_row) {
+  __shared__ long row_at[kPermMax], ext_pos[kPermMax], ext_row[kPermMax];
+  if(threadIdx.x != 0)
+    return;
+  for(int c = 0; c < nb; ++c)
+    row_at[c] = k + c;
+  int ext = 0;
+  for(int c = 0; c < nb; ++c) {
+    const long p = piv[k + c];
+    if(p == k + c)
+      continue;
+    const long a = row_at[c];
+    long b;
+    if(p - k < nb) {
+      b = row_at[p - k];
+      row_at[p - k] = a;
+    } else {
+      b = p;  // the row now at p: the latest entry for p, else p itself
+      for(int e = ext - 1; e >= 0; --e)
+        if(ext_pos[e] == p) {
+          b = ext_row[e];
+          break;
+        }
+      ext_pos[ext] = p;
+      ext_row[ext] = a;
+      ++ext;
+    }
+    row_at[c] = b;
+  }
+  long cnt = 0;
+  for(int c = 0; c < nb; ++c)
+    if(row_at[c] != k + c) {
+      pos_row[1 + 2 * cnt] = k + c;
+      pos_row[2 + 2 * cnt] = row_at[c];
+      ++cnt;
+    }
+  for(int e = ext - 1; e >= 0; --e) {
+    bool later = false;
+    for(int f = e + 1; f < ext; ++f)
+      later |= ext_pos[f] == ext_pos[e];
+    if(!later) {
+      pos_row[1 + 2 * cnt] = ext_pos[e];
+      pos_row[2 + 2 * cnt] = ext_row[e];
+      ++cnt;
+    }
+  }
+  pos_row[0] = cnt;
+}
+
+// The permutation of k_lu_perm_table applied to the columns jlo .. jhi - 1
+// other than slo .. shi - 1: a warp per column, each lane gathering its
+// pairs' rows (loads issued together; consecutive positions on consecutive
+// lanes) before any store.
 template <typename V>
-__global__ void k_lu_swap(V *A, long ld, long jlo, long jhi, long slo, long shi, long k, int nb,
-                          const int *piv) {
-  const long j = jlo + blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if(j >= jhi || (j >= slo && j < shi))
+__global__ void __launch_bounds__(256) k_lu_permute(V *A, long ld, long jlo, long jhi, long slo, long shi,
+                                                    const long *pos_row) {
+  const long cnt = pos_row[0];
+  const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  long j = jlo + warp;
+  if(j >= slo)
+    j += shi - slo;  // skip the panel's own columns
+  if(j >= jhi)
     return;
   V *col = A + j * ld;
-  for(int c = 0; c < nb; ++c) {
-    const long r = k + c, p = piv[r];
-    if(p != r) {
-      V a = col[r];
-      col[r] = col[p];
-      col[p] = a;
-    }
+  constexpr int kPer = 2 * kPermMax / 32;
+  V v[kPer];
+#pragma unroll
+  for(int i = 0; i < kPer; ++i) {
+    const long e = lane + 32L * i;
+    if(e < cnt)
+      v[i] = col[pos_row[2 + 2 * e]];
+  }
+  __syncwarp();
+#pragma unroll
+  for(int i = 0; i < kPer; ++i) {
+    const long e = lane + 32L * i;
+    if(e < cnt)
+      col[pos_row[1 + 2 * e]] = v[i];
   }
 }
 
@@ -1889,9 +1957,24 @@ __global__ void __launch_bounds__(kSweepThreads, 1) k_tri_sweep(const V *A, long
 // The pivots are those of the unblocked order (each panel's pivot search sees
 // fully updated columns); the roundings differ.
 constexpr long kTcBlock = 256;
+static_assert(kTcBlock <= kPermMax, "a block's interchanges fit one permutation table");
+
+// The interchanges of rows k .. k + nb - 1 on the columns jlo .. jhi - 1
+// other than slo .. shi - 1 (inside that range): one permutation, gathered
+// before it is stored, instead of nb dependent swaps per column.
+template <typename V>
+void lu_interchange(om_context *ctx, V *A, long n, long jlo, long jhi, long slo, long shi, long k, int nb,
+                    const int *piv, long *ptab) {
+  const long cols = (jhi - jlo) - (shi - slo);
+  if(cols <= 0)
+    return;
+  k_lu_perm_table<<<1, 32, 0, ctx->stream>>>(piv, k, nb, ptab);
+  k_lu_permute<V><<<blocks_for(cols, 8), 256, 0, ctx->stream>>>(A, n, jlo, jhi, slo, shi, ptab);
+  ctx->last_launches += 2;
+}
 
 template <typename Panel>
-void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Panel &panel, void *split) {
+void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Panel &panel, void *split, long *ptab) {
   for(long K = 0; K < n; K += kTcBlock) {
     const long W = std::min<long>(kTcBlock, n - K), KE = K + W;
     for(long k = K; k < KE; k += kNb) {
@@ -1899,8 +1982,7 @@ void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Pane
       const long kn = k + nb;
       panel(k, nb);
       if(W > nb) {  // the block's other columns
-        k_lu_swap<float2><<<blocks_for(W, 256), 256, 0, ctx->stream>>>(A, n, K, KE, k, kn, k, nb, piv);
-        ctx->last_launches++;
+        lu_interchange<float2>(ctx, A, n, K, KE, k, kn, k, nb, piv, ptab);
       }
       if(kn < KE) {  // the block's later columns: U rows, then all rows below
         k_lu_trsm<float2><<<blocks_for(KE - kn, 128), 128, 0, ctx->stream>>>(A, n, kn, KE, k, nb);
@@ -1910,8 +1992,7 @@ void lu_blocked_tc(om_context *ctx, float2 *A, long n, int *piv, int *info, Pane
       }
     }
     if(W < n) {  // the block's interchanges on the columns left and right of it
-      k_lu_swap<float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, 0, n, K, KE, K, (int)W, piv);
-      ctx->last_launches++;
+      lu_interchange<float2>(ctx, A, n, 0, n, K, KE, K, (int)W, piv, ptab);
     }
     const long rest = n - KE;
     if(rest <= 0)
@@ -1975,11 +2056,14 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
     }
     cudaGetLastError();
   }
-  if(pan_bytes + split_bytes) {
-    const int rc = alloc_work(ctx, ws, pan_bytes + split_bytes + 256);
+  long *ptab = nullptr;  // the row-interchange permutation table
+  {
+    const size_t ptab_bytes = sizeof(long) * (1 + 4 * kPermMax);
+    const int rc = alloc_work(ctx, ws, pan_bytes + split_bytes + ptab_bytes + 512);
     if(rc)
       return rc;
     size_t off = 0;
+    ptab = ws.take<long>(1 + 4 * kPermMax, off);
     if(pan_bytes) {
       ps.bestv = ws.take<double>(maxblk, off);
       ps.besti = ws.take<long>(maxblk, off);
@@ -2040,7 +2124,7 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   };
   if constexpr(std::is_same<V, float2>::value) {
     if(ctx->lu_tc) {
-      lu_blocked_tc(ctx, A, n, piv, info, panel, split);
+      lu_blocked_tc(ctx, A, n, piv, info, panel, split, ptab);
       timer_end(ctx, ctx->ev_luf);
       return OM_OK;
     }
@@ -2048,8 +2132,7 @@ int lu_factor(om_context *ctx, V *A, long n, int *piv, int *info) {
   for(long k = 0; k < n; k += kNb) {
     const int nb = (int)std::min<long>(kNb, n - k);
     panel(k, nb);
-    k_lu_swap<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(A, n, 0, n, k, k + nb, k, nb, piv);
-    ctx->last_launches++;
+    lu_interchange<V>(ctx, A, n, 0, n, k, k + nb, k, nb, piv, ptab);
     const long rest = n - k - nb;
     if(rest > 0) {
       k_lu_trsm<V><<<blocks_for(rest, 128), 128, 0, ctx->stream>>>(A, n, k + nb, n, k, nb);
