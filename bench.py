@@ -669,16 +669,15 @@ def batch_arm(args):
     cases = c3_cases(args.c3_clusters, args.c3_wavelengths)
     fp64 = G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=300, restarts=6)
     ctx = G.Context(0)
-    # warm-up: one request per nMax (coefficient and SH coupling tables, the
-    # auxiliary contexts) in both forms
-    warm = {}
-    for cs in cases:
-        warm.setdefault(cs["nmax"], cs)
+    # warm-up: the whole sweep once in both forms (coefficient and SH coupling
+    # tables, the auxiliary contexts, and the autotuner's choice of matvec
+    # tiles for every size class, made at a class's first batch)
     for opts, prec in ((mixed, G.C64), (fp64, G.C128)):
-        G.batch_solve(ctx, [(cs["sp"], bg, cs["wave"], opts, prec) for cs in warm.values()])
+        run_batch(G, ctx, cases, opts, prec, bg)
     with ClockSampler(0) as clk:
         t_mx, res_mx, launches = run_batch(G, ctx, cases, mixed, G.C64, bg)
     t_64, res_64, _ = run_batch(G, ctx, cases, fp64, G.C128, bg)
+    tiles = G.batch_tiles(ctx)
     ctx.close()
     ok = [i for i in range(len(cases)) if res_mx[i]["status"] == G.OK and res_64[i]["status"] == G.OK]
     err = max(abs(res_mx[i]["xsec"][0] - res_64[i]["xsec"][0]) / abs(res_64[i]["xsec"][0]) for i in ok)
@@ -698,7 +697,7 @@ def batch_arm(args):
     count = lambda res: {str(k): v for k, v in sorted(
         __import__("collections").Counter(r["status"] for r in res).items())}
     return {"metric": METRIC, "value": len(cases) / t_mx, "unit": UNIT + " (FF + SH per case)",
-            "n_gpus": 1, "steps": len(cases), "warmup": len(warm), "ms_per_step": 1e3 * t_mx / len(cases),
+            "n_gpus": 1, "steps": len(cases), "warmup": len(cases), "ms_per_step": 1e3 * t_mx / len(cases),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c64 (FP32) inner + c128 (FP64) outer/assembly", "data": "synthetic (seeded)",
             "config": {"workload": f"c3: {args.c3_clusters} clusters x {args.c3_wavelengths} of the "
@@ -715,7 +714,7 @@ def batch_arm(args):
             "qext_rel_err_vs_fp64": err, "sh_xsec_rel_err_vs_fp64": err_sh,
             "statuses": {"mixed": count(res_mx), "fp64": count(res_64)},
             "served": served,
-            "gpu_launches": launches, "clocks": clk.summary()}
+            "gpu_launches": launches, "matvec_tiles_autotuned": tiles, "clocks": clk.summary()}
 
 
 def c4_requests(rate, duration, seed=20260405):
@@ -821,6 +820,30 @@ def fp64_gemm_tflops():
         torch.cuda.synchronize()
         best = min(best, e0.elapsed_time(e1) * 1e-3)
     return 2.0 * 8192 ** 3 / best / 1e12
+
+
+def tc_update_arm(args):
+    """One tensor-core trailing update C (m x m) -= A (m x k) B (k x m), complex64
+    (om_cgemm_sub_c64: host buffers in and out), m = --tc-m, k = --tc-k: the
+    kernel the LU role's rank-k updates run, as a stand-alone case for ncu."""
+    import optimet_gb300 as G
+    from optimet_gb300 import build
+    build.build()
+    m, k = args.tc_m, args.tc_k
+    rng = np.random.default_rng(1)
+    A = (rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))).astype(np.complex64)
+    B = (rng.standard_normal((k, m)) + 1j * rng.standard_normal((k, m))).astype(np.complex64)
+    Cm = (rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))).astype(np.complex64)
+    ctx = G.Context(0)
+    ctx.tune(lu_tensor_cores=args.lu_update)
+    t0 = time.perf_counter()
+    out = G.cgemm_sub_c64(ctx, A, B, Cm)
+    wall = time.perf_counter() - t0
+    ctx.close()
+    return {"workload": f"tensor-core rank-{k} update, {m} x {m} complex64",
+            "kernel": {1: "k_cgemm_sub_tc3 (persistent)", 2: "k_cgemm_sub_tc2 (one CTA per tile)"}.get(
+                args.lu_update, "none"),
+            "wall_s_with_copies": wall, "checksum": float(np.abs(out[:4, :4]).sum())}
 
 
 def lu_mixed_arm(args):
@@ -1169,7 +1192,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2",
-                    choices=sorted(WORKLOADS) + ["c0", "c1f", "c1full", "c2lu", "c3", "c4", "aca"])
+                    choices=sorted(WORKLOADS) + ["c0", "c1f", "c1full", "c2lu", "c3", "c4", "aca", "tcupd"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--assemble-only", action="store_true",
                     help="only timed precision-form assemblies of the workload (profiling runs)")
@@ -1183,6 +1206,8 @@ def main():
     ap.add_argument("--c4-forms", default="mixed,fp64", help="c4: forms to run (comma-separated)")
     ap.add_argument("--lu-update", type=int, default=1, choices=[0, 1, 2],
                     help="c2lu: trailing-update kernel (1 persistent, 2 one CTA per tile, 0 FP32 CUDA cores)")
+    ap.add_argument("--tc-m", type=int, default=8192, help="tcupd: rows and columns of C")
+    ap.add_argument("--tc-k", type=int, default=128, help="tcupd: rank of the update")
     ap.add_argument("--lu-persistent", type=int, default=1, choices=[1, 2],
                     help="c2lu: panels and triangular sweeps (1 one launch each, 2 per column / per block)")
     ap.add_argument("--c4-batch-limit-gb", type=float, default=1.0,
@@ -1210,6 +1235,8 @@ def main():
         out = aca_arm(args) if args.impl != "reference" else None
     elif args.workload == "c1f":
         out = near_field_arm(args) if args.impl != "reference" else None
+    elif args.workload == "tcupd":
+        out = tc_update_arm(args) if args.impl != "reference" else None
     elif args.workload == "c2lu":
         out = lu_mixed_arm(args) if args.impl != "reference" else None
     elif args.workload == "c3":
