@@ -376,7 +376,10 @@ def gpu_arm(args, w):
         "e2e": {"value": world * args.steps / e2e_all, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "path": "om_server_submit/om_server_poll (C ABI, host buffers, problem set-up "
-                        "from the host every request, host wall clock)"},
+                        "from the host every request, host wall clock)",
+                "service_ms": {"p50": float(np.percentile([r["service_ms"] for r in res_e2e], 50)),
+                               "max": float(max(r["service_ms"] for r in res_e2e))},
+                "queue_ms_max": float(max(r["queue_ms"] for r in res_e2e))},
         "roofline": {"bound": "hbm",
                      "kernel": "k_matvec_tma<0> (FP32 inner matvec, TMA-staged; timed in the "
                                "single-stream part, where a context uses it)",
