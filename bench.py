@@ -289,12 +289,15 @@ def gpu_arm(args, w):
             tuning = srv.autotune(sp, bg, lam(0), opts, precision, 1, tune_count)
         else:
             srv.tune(**tuning)
-        for t in [srv.submit(sp, bg, lam(i), opts, precision, key) for i in range(args.warmup)]:
+        # warm-up: at least two requests per slot, so that every slot's
+        # problem buffers are in the memory pool before the timed requests
+        nwarm = max(args.warmup, 2 * args.slots)
+        for t in [srv.submit(sp, bg, lam(i), opts, precision, key) for i in range(nwarm)]:
             srv.poll(t)
         srv.launches()
         srv.mark()
         s0 = time.perf_counter()
-        tickets = [srv.submit(sp, bg, lam(args.warmup + i), opts, precision, key) for i in range(k)]
+        tickets = [srv.submit(sp, bg, lam(nwarm + i), opts, precision, key) for i in range(k)]
         res = [srv.poll(t) for t in tickets]
         wall = time.perf_counter() - s0
         dev_ms = srv.mark()

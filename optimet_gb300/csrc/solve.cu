@@ -1152,8 +1152,8 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
   __shared__ double wv[kPanThreads / 32];
   __shared__ long wi[kPanThreads / 32];
   __shared__ int wl[kPanThreads / 32];
-  __shared__ double pv_s;
-  __shared__ int rl_s, wb_s;
+  __shared__ long wr[kPanThreads / 32];
+  __shared__ int rl_s;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const long G = gridDim.x, b = blockIdx.x;
   const long R = (n - k + G - 1) / G, r0 = k + b * R, r1 = min(n, r0 + R);
@@ -1227,21 +1227,26 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
   };
   partial_max(0);
   unsigned target = bar_base;
+  double pv_s_local = 0.0;  // the pivot's |value|^2 (every thread reduces it)
   for(int c = 0; c < nb; ++c) {
     const long col = k + c;
     target += (unsigned)G;
     if(!grid_barrier(bar, target, err))
       return;
     {
+      // every thread reduces the per-CTA maxima (the physical row rides
+      // along), so the pivot row's load starts while thread 0 updates the
+      // interchange tables
       double bv = -2.0;
-      long bp = col;
+      long bp = col, br = -1;
       int bw = 0;
       for(long w = t; w < G; w += kPanThreads) {
         const double v = __ldcg(ps.bestv + w);
-        const long i = __ldcg(ps.besti + w);
+        const long i = __ldcg(ps.besti + w), r = __ldcg(ps.bestr + w);
         if(v > bv || (v == bv && i < bp)) {
           bv = v;
           bp = i;
+          br = r;
           bw = (int)w;
         }
       }
@@ -1249,34 +1254,44 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
       for(int h = 16; h > 0; h >>= 1) {
         const double ov = __shfl_xor_sync(0xffffffffu, bv, h);
         const long op = __shfl_xor_sync(0xffffffffu, bp, h);
+        const long orw = __shfl_xor_sync(0xffffffffu, br, h);
         const int ow = __shfl_xor_sync(0xffffffffu, bw, h);
         if(ov > bv || (ov == bv && op < bp)) {
           bv = ov;
           bp = op;
+          br = orw;
           bw = ow;
         }
       }
       if(lane == 0) {
         wv[wid] = bv;
         wi[wid] = bp;
+        wr[wid] = br;
         wl[wid] = bw;
       }
       __syncthreads();
+      bv = wv[0];
+      bp = wi[0];
+      br = wr[0];
+      bw = wl[0];
+      for(int w = 1; w < kPanThreads / 32; ++w)
+        if(wv[w] > bv || (wv[w] == bv && wi[w] < bp)) {
+          bv = wv[w];
+          bp = wi[w];
+          br = wr[w];
+          bw = wl[w];
+        }
+      if(t < nb)
+        u[t] = __ldcg(cand + (long)bw * kNb + t);
       if(t == 0) {
-        for(int w = 1; w < kPanThreads / 32; ++w)
-          if(wv[w] > bv || (wv[w] == bv && wi[w] < bp)) {
-            bv = wv[w];
-            bp = wi[w];
-            bw = wl[w];
-          }
         if(b == 0) {
           piv[col] = (int)bp;
           if(bv <= 0.0 && *info == 0)
             *info = (int)col + 1;
         }
-        // interchange positions col and bp: the pivot row pr (published by
+        // interchange positions col and bp: the pivot row br (published by
         // the winning CTA) comes to col, the row at col goes to bp
-        const long pr = __ldcg(ps.bestr + bw), a = row_at[c];
+        const long pr = br, a = row_at[c];
         if(bp != col) {
           row_at[c] = pr;
           if(bp - k < nb) {
@@ -1293,15 +1308,11 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
           retired[pr - r0] = 1;
           posl[pr - r0] = col;
         }
-        pv_s = bv;
-        wb_s = bw;
       }
+      pv_s_local = bv;
       __syncthreads();
     }
-    if(t < nb)
-      u[t] = __ldcg(cand + (long)wb_s * kNb + t);
-    __syncthreads();
-    if(pv_s > 0.0) {
+    if(pv_s_local > 0.0) {
       const V inv = crecip(u[c]);
       for(int rl = t; rl < nr; rl += kPanThreads) {
         if(retired[rl])
