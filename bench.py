@@ -324,7 +324,8 @@ def gpu_arm(args, w):
     # ---- end to end through the C ABI with host buffers: every request
     # copies its spheres and wave from the host, sets its problem up from
     # scratch (cluster_key 0), and returns its cross sections to the host ----
-    _, wall_e2e, res_e2e, _, _ = served(mixed_opts, G.C64, args.steps, 0, tuning=tuning)
+    with ClockSampler(local) as clk_e2e:
+        _, wall_e2e, res_e2e, _, _ = served(mixed_opts, G.C64, args.steps, 0, tuning=tuning)
     import ctypes
     h2d = ctypes.sizeof(G.Sphere) * len(sp) + ctypes.sizeof(G.Medium) + \
         ctypes.sizeof(G.PlaneWave) + ctypes.sizeof(G.SolveOptions)
@@ -382,7 +383,8 @@ def gpu_arm(args, w):
                         "from the host every request, host wall clock)",
                 "service_ms": {"p50": float(np.percentile([r["service_ms"] for r in res_e2e], 50)),
                                "max": float(max(r["service_ms"] for r in res_e2e))},
-                "queue_ms_max": float(max(r["queue_ms"] for r in res_e2e))},
+                "queue_ms_max": float(max(r["queue_ms"] for r in res_e2e)),
+                "clocks": clk_e2e.summary()},
         "roofline": {"bound": "hbm",
                      "kernel": "k_matvec_tma<0> (FP32 inner matvec, TMA-staged; timed in the "
                                "single-stream part, where a context uses it)",
