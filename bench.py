@@ -863,7 +863,7 @@ def lu_mixed_arm(args):
     import optimet_gb300 as G
     from optimet_gb300 import build
     build.build()
-    w = WORKLOADS["c2"]
+    w = WORKLOADS[args.lu_case]
     xyz, rad = cluster(w)
     ctx = G.Context(0)
     sp = G.spheres_array(xyz, rad, complex(w["index"]) ** 2, w["nmax"])
@@ -909,7 +909,7 @@ def lu_mixed_arm(args):
             "warmup": 0, "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64 (FP32) LU + c128 (FP64) refinement",
             "data": "synthetic (seeded)",
-            "config": {"workload": "c2 LU role: " + w["desc"],
+            "config": {"workload": args.lu_case + " LU role: " + w["desc"],
                        "solver": "GMRES-based iterative refinement: FP64 residuals, GMRES on the system left-preconditioned by the FP32 LU (tensor-core trailing updates), tol 1e-9",
                        "trailing_update": {1: "persistent", 2: "one CTA per tile",
                                            0: "FP32 CUDA cores, rank 32"}[args.lu_update],
@@ -1214,6 +1214,8 @@ def main():
     ap.add_argument("--c4-forms", default="mixed,fp64", help="c4: forms to run (comma-separated)")
     ap.add_argument("--lu-update", type=int, default=1, choices=[0, 1, 2],
                     help="c2lu: trailing-update kernel (1 persistent, 2 one CTA per tile, 0 FP32 CUDA cores)")
+    ap.add_argument("--lu-case", default="c2", choices=sorted(WORKLOADS),
+                    help="c2lu: the cluster of the LU role's solve (c2 by default)")
     ap.add_argument("--tc-m", type=int, default=8192, help="tcupd: rows and columns of C")
     ap.add_argument("--tc-k", type=int, default=128, help="tcupd: rank of the update")
     ap.add_argument("--lu-persistent", type=int, default=1, choices=[1, 2],
