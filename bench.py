@@ -877,6 +877,12 @@ def lu_mixed_arm(args):
     ctx.tune(lu_tensor_cores=args.lu_update, lu_persistent=args.lu_persistent)
     opts = G.options(G.SOLVE_LU_MIXED, tol=1e-9, max_iter=30, restarts=4)
     times, st = [], None
+    # one untimed solve first: the LU kernels' first launches (module loading,
+    # shared-memory attributes, the memory pool growing to the LU's workspace)
+    pr.source_vector(copy=False)
+    pr.assemble(G.FF, G.C64)
+    pr.solve(opts)
+    ctx.synchronize()
     with ClockSampler(0) as clk:
         for _ in range(max(1, args.steps)):
             ctx.synchronize()
@@ -906,7 +912,7 @@ def lu_mixed_arm(args):
               if ph["update"][0] > 0 else None,
               "tri_solve_ms": ph["tri_solve"][0], "tri_solves": ph["tri_solve"][1]}
     return {"metric": METRIC, "value": 1.0 / t, "unit": UNIT, "n_gpus": 1, "steps": len(times),
-            "warmup": 0, "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
+            "warmup": 1, "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64 (FP32) LU + c128 (FP64) refinement",
             "data": "synthetic (seeded)",
             "config": {"workload": args.lu_case + " LU role: " + w["desc"],
