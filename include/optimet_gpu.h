@@ -152,6 +152,12 @@ typedef struct {
   int batch_tiles;       /* tiles and schedule of the batched matvecs (om_batch_solve): 0 (default)
                             autotuned per size class at its first batch, 1..8 a fixed candidate
                             (rows per tile, tile order, CTAs per SM; see om_batch_tiles) */
+  int batch_fused;       /* batched solves of the small size classes in one cooperative launch
+                            per solve that runs every slot's cycles to the end (a group of one
+                            CTA per 512 rows for each slot): 1 (default) for the classes of at
+                            most 1,024 padded unknowns, 2 for those of at most 4,096, 0 never
+                            (the lockstep Arnoldi steps of all slots as captured graphs); the
+                            same bits either way */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any

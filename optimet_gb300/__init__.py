@@ -68,7 +68,8 @@ class Tuning(C.Structure):
     _fields_ = [("matvec_ctas_per_sm", C.c_int), ("matvec_df_ctas_per_sm", C.c_int),
                 ("assemble_carveout", C.c_int), ("matvec_carveout", C.c_int),
                 ("lu_tensor_cores", C.c_int), ("matvec_tma", C.c_int),
-                ("assemble_rotation", C.c_int), ("lu_persistent", C.c_int), ("batch_tiles", C.c_int)]
+                ("assemble_rotation", C.c_int), ("lu_persistent", C.c_int), ("batch_tiles", C.c_int),
+                ("batch_fused", C.c_int)]
 
 
 class Request(C.Structure):
@@ -205,10 +206,12 @@ class Context:
         return float(out[0])
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
-             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1):
+             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1,
+             batch_fused=-1):
         """Launch tuning (om_context_tune); 0 / -1 keep the current value."""
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
-                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles)
+                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles,
+                   batch_fused)
         self.check(lib().om_context_tune(self.h, C.byref(t)))
 
     def timers(self, enable=True):
@@ -552,9 +555,11 @@ class Server:
             raise OptimetError(rc, "server batching")
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
-             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1):
+             matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1,
+             batch_fused=-1):
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
-                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles)
+                   lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles,
+                   batch_fused)
         rc = lib().om_server_tune(self.h, C.byref(t))
         if rc:
             raise OptimetError(rc, "server tune")

@@ -563,6 +563,443 @@ __global__ void k_b_update(const Slot *st, const V *Vb, long vslot, long np, con
 }
 
 // ---------------------------------------------------------------------------
+// Fused solves of the small size classes (at most kFusedRows padded
+// unknowns): one cooperative launch runs every slot's restarted GMRES /
+// GMRES-IR to the end. A group of C = ceil(np / kFRows) CTAs serves one slot
+// at a time (group g of G takes slots g, g + G, ...); CTA c of the group owns
+// rows [c kFRows, (c + 1) kFRows) of the slot's vectors, so its matvec rows,
+// its Arnoldi vector work and its block partial sums are the row block the
+// lockstep kernels give CTA c. The CTAs of a group meet at a bounded barrier
+// in global memory three times per Arnoldi step (after the first
+// projections, after the second, after |w|^2) and twice per cycle. Every CTA
+// forms the residual norm, the projections, the Hessenberg column, the
+// rotation and the stop test itself from the same partial sums, so the CTAs
+// take the same branches without further exchange; CTA 0 keeps the
+// Hessenberg columns for the back substitution. Each value is formed by the
+// same inline functions, over the same rows and in the same order as in the
+// lockstep kernels above, so a slot's bits do not depend on the form that
+// solved it.
+// ---------------------------------------------------------------------------
+constexpr int kFusedBlocks = 8;                    // CTAs per slot at most
+constexpr int kFusedRows = kFusedBlocks * kFRows;  // 4,096 padded unknowns
+// By default the fused form takes the classes of at most kFusedAuto padded
+// unknowns (groups of one or two CTAs, one column chunk). Per size class of
+// the c3 sweep it measured 8-20 % faster there than the lockstep graphs, and
+// up to two times slower from about 1,300 unknowns on: the CTAs of a group then
+// run matvec rows of several chunks each one after the other, where the
+// lockstep matvec spreads a slot's tiles over the whole GPU.
+constexpr int kFusedAuto = 2 * kFRows;
+constexpr long kFusedSpin = 1L << 24;              // polls before a group barrier gives up
+constexpr int kFusedSmemMax = 200 * 1024;          // dynamic shared memory of k_b_fused at most
+static_assert(kFRows == 2 * kBT, "a fused CTA's thread takes two rows of its block");
+
+template <typename V> struct FusedArgs {
+  Slot *st;
+  int B;
+  const double2 *b;
+  double2 *x, *r;
+  V *Vb;
+  long vslot, np;
+  V *wbuf;        // 2 np per slot: w after its second pass, read by the next step's product
+  V *dpA, *dpB;   // [slot][nbf][m2] block partials (entry m2 - 1 of dpA: the block's |w|^2)
+  double2 *Hm;    // [slot][m][m + 1] (CTA 0 of the group)
+  int m, m2, nbf, C;
+  double tol, inner_rel;
+  int max_cycles;
+  unsigned *bar;  // one arrival counter per group, 32 words apart
+  int *err;       // set when a barrier gave up
+};
+
+// Dynamic shared memory of k_b_fused: the staged column chunk (the residual's
+// split x or the basis column), the CTA's w rows, the projections and the
+// Hessenberg / rotation state.
+template <typename V> struct FusedSmem {
+  int m2, m;
+  size_t xs, w, h, hacc, col, cs, sn, g, y, bytes;
+  __host__ __device__ FusedSmem(int m_, int m2_) : m2(m2_), m(m_) {
+    auto up = [](size_t v) { return (v + 15) / 16 * 16; };
+    size_t o = 0;
+    xs = o;
+    o += up(kBCols * (sizeof(DFX) > sizeof(double2) ? sizeof(DFX) : sizeof(double2)));
+    w = o;
+    o += up(kFRows * sizeof(V));
+    h = o;
+    o += up(m2 * sizeof(V));
+    hacc = o;
+    o += up(m2 * sizeof(double2));
+    col = o;
+    o += up((m + 1) * sizeof(double2));
+    cs = o;
+    o += up(m * sizeof(double2));
+    sn = o;
+    o += up(m * sizeof(double2));
+    g = o;
+    o += up((m + 1) * sizeof(double2));
+    y = o;
+    o += up(m * sizeof(double2));
+    bytes = o;
+  }
+};
+
+// The group's barrier: every CTA adds one arrival with release semantics
+// (its threads' writes, ordered before thread 0 by the CTA barrier, become
+// visible with it) and waits, with acquire loads and a bounded number of
+// polls, until the counter reaches `target`.
+__device__ __forceinline__ bool group_barrier(unsigned *ctr, unsigned target, int C, int *err) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if(C == 1)
+    return true;
+  if(threadIdx.x == 0) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(ctr), "r"(1u) : "memory");
+    int ok = 0;
+    for(long it = 0; it < kFusedSpin; ++it) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+      if((int)(v - target) >= 0) {
+        ok = 1;
+        break;
+      }
+      if((it & 63) == 63 && *(volatile int *)err)
+        break;  // another group's CTA gave up
+      __nanosleep(32);
+    }
+    if(!ok)
+      atomicExch(err, 1);
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// block_proj with the block's w rows in shared memory (ws[i - r0])
+template <typename V>
+__device__ __forceinline__ void block_proj_sm(const V *vs, const V *ws, long np, long r0, long r1, int k,
+                                              V *out) {
+  const int lane = threadIdx.x & 31;
+  for(int t = threadIdx.x >> 5; t < k; t += kBT / 32) {
+    const V *v = vs + (long)t * np;
+    V acc;
+    acc.x = acc.y = 0;
+    for(long i = r0 + lane; i < r1; i += 32)
+      acc = cfma_conj(v[i], ws[i - r0], acc);
+    acc = warp_sum(acc);
+    if(lane == 0)
+      out[t] = acc;
+  }
+}
+
+template <typename M, typename V>
+__global__ void __launch_bounds__(kBT) k_b_fused(FusedArgs<V> a) {
+  constexpr bool kDF = std::is_same<M, float2>::value;
+  typedef typename std::conditional<kDF, DFX, double2>::type XS;
+  extern __shared__ __align__(16) unsigned char fsm[];
+  const FusedSmem<V> L(a.m, a.m2);
+  XS *xr = reinterpret_cast<XS *>(fsm + L.xs);
+  V *xs = reinterpret_cast<V *>(fsm + L.xs);
+  V *w = reinterpret_cast<V *>(fsm + L.w);
+  V *h = reinterpret_cast<V *>(fsm + L.h);
+  double2 *hacc = reinterpret_cast<double2 *>(fsm + L.hacc);
+  double2 *col = reinterpret_cast<double2 *>(fsm + L.col);
+  double2 *c_s = reinterpret_cast<double2 *>(fsm + L.cs);
+  double2 *s_s = reinterpret_cast<double2 *>(fsm + L.sn);
+  double2 *gs = reinterpret_cast<double2 *>(fsm + L.g);
+  double2 *ys = reinterpret_cast<double2 *>(fsm + L.y);
+  __shared__ Slot sl;
+  __shared__ double red[kBT];
+  __shared__ double inv_s;
+  const int tid = threadIdx.x;
+  const int C = a.C, c = blockIdx.x % C, grp = blockIdx.x / C, G = gridDim.x / C;
+  const int m = a.m, m2 = a.m2;
+  const long np = a.np;
+  unsigned *ctr = a.bar + 32 * grp;
+  unsigned target = 0;
+  for(int s = grp; s < a.B; s += G) {
+    __syncthreads();
+    if(tid == 0)
+      sl = a.st[s];
+    __syncthreads();
+    if(sl.n == 0 || !sl.outer)
+      continue;
+    const long n = sl.n;
+    const M *S = (const M *)sl.S;
+    const long r0 = (long)c * kFRows, r1 = min(n, r0 + kFRows);  // r1 <= r0: no rows of this slot
+    const int nb = (int)((n + kFRows - 1) / kFRows);
+    const int ns = (int)((n + kBCols - 1) / kBCols);
+    V *vs = a.Vb + s * a.vslot;
+    const double2 *bs = a.b + s * np;
+    double2 *xv = a.x + s * np, *rv = a.r + s * np;
+    V *dA = a.dpA + (long)s * a.nbf * m2, *dB = a.dpB + (long)s * a.nbf * m2;
+    V *wb = a.wbuf + (long)s * 2 * np;
+    double2 *H = a.Hm + (long)s * m * (m + 1);
+    for(;;) {
+      // r = b - S x over the CTA's rows (k_b_resid, k_b_reduce_r)
+      if(sl.xzero) {
+        for(long i = r0 + tid; i < r1; i += kBT)
+          rv[i] = bs[i];
+      } else {
+        double2 acc[2];
+        for(int cc = 0; cc < ns; ++cc) {
+          const long j0 = (long)cc * kBCols, j1 = min(n, j0 + kBCols);
+          __syncthreads();
+          for(long j = j0 + tid; j < j1; j += kBT) {
+            if constexpr(kDF)
+              xr[j - j0] = df_split(xv[j]);
+            else
+              xr[j - j0] = xv[j];
+          }
+          __syncthreads();
+#pragma unroll
+          for(int q = 0; q < 2; ++q) {
+            const long i = r0 + q * kBT + tid;
+            if(i >= r1)
+              continue;
+            double2 v;
+            if constexpr(kDF)
+              v = mv_row_df(S + j0 * n + i, n, xr, 0L, j1 - j0);
+            else
+              v = mv_row<double2, double2>(S + j0 * n + i, n, xr, 0L, j1 - j0);
+            if(cc == 0) {
+              acc[q] = v;
+            } else {
+              acc[q].x += v.x;
+              acc[q].y += v.y;
+            }
+          }
+        }
+#pragma unroll
+        for(int q = 0; q < 2; ++q) {
+          const long i = r0 + q * kBT + tid;
+          if(i < r1)
+            rv[i] = make_double2(bs[i].x - acc[q].x, bs[i].y - acc[q].y);
+        }
+      }
+      if(!group_barrier(ctr, target += C, C, a.err))
+        return;
+      // ||r|| over kBDotRows-row blocks in block order (k_b_rnorm, k_b_start)
+      double tot = 0.0;
+      for(long q0 = 0; q0 < n; q0 += kBDotRows) {
+        const long q1 = min(n, q0 + kBDotRows);
+        double acc = 0.0;
+        for(long i = q0 + tid; i < q1; i += kBT) {
+          const double2 v = rv[i];
+          acc = fma(v.x, v.x, acc);
+          acc = fma(v.y, v.y, acc);
+        }
+        red[tid] = acc;
+        __syncthreads();
+        for(int hh = kBT / 2; hh > 0; hh >>= 1) {
+          if(tid < hh)
+            red[tid] += red[tid + hh];
+          __syncthreads();
+        }
+        tot = q0 == 0 ? red[0] : tot + red[0];
+        __syncthreads();
+      }
+      if(tid == 0) {
+        sl.k = 0;
+        sl.inner = 0;
+        const double rho = sqrt(tot);
+        if(sl.bnorm < 0.0)
+          sl.bnorm = rho;
+        sl.rho = rho;
+        if(sl.bnorm == 0.0 || rho <= a.tol * sl.bnorm) {
+          sl.outer = 0;
+          sl.status = OM_OK;
+        } else if(sl.cycles >= a.max_cycles) {
+          sl.outer = 0;
+          sl.status = OM_ERR_NOT_CONVERGED;
+        } else {
+          sl.inner = 1;
+          sl.thr = fmax(a.inner_rel * rho, a.tol * sl.bnorm);
+          gs[0] = make_double2(rho, 0.0);
+        }
+      }
+      __syncthreads();
+      if(!sl.outer)
+        break;
+      // v_0 = r / rho (k_b_v0); the first product stages it from r
+      const double f0 = 1.0 / sl.rho;
+      for(long i = r0 + tid; i < r1; i += kBT) {
+        const double2 v = rv[i];
+        V o;
+        o.x = v.x * f0;
+        o.y = v.y * f0;
+        vs[i] = o;
+      }
+      for(int j = 0;; ++j) {
+        const int k = j + 1;
+        // w = S v_j over the CTA's rows, chunk sums in chunk order (k_b_mv,
+        // k_b_red_proj); v_j is staged from r / rho or from the previous
+        // step's w times 1 / h_{j,j-1}, the values k_b_v0 / k_b_scale store
+        const V *wp = wb + (long)((j + 1) & 1) * np;
+        V acc[2];
+        for(int cc = 0; cc < ns; ++cc) {
+          const long j0 = (long)cc * kBCols, j1 = min(n, j0 + kBCols);
+          __syncthreads();
+          for(long jj = j0 + tid; jj < j1; jj += kBT) {
+            V o;
+            if(j == 0) {
+              const double2 v = rv[jj];
+              o.x = v.x * f0;
+              o.y = v.y * f0;
+            } else {
+              const V v = wp[jj];
+              o.x = v.x * inv_s;
+              o.y = v.y * inv_s;
+            }
+            xs[jj - j0] = o;
+          }
+          __syncthreads();
+#pragma unroll
+          for(int q = 0; q < 2; ++q) {
+            const long i = r0 + q * kBT + tid;
+            if(i >= r1)
+              continue;
+            const V v = mv_row<M, V>(S + j0 * n + i, n, xs, 0L, j1 - j0);
+            if(cc == 0) {
+              acc[q] = v;
+            } else {
+              acc[q].x += v.x;
+              acc[q].y += v.y;
+            }
+          }
+        }
+#pragma unroll
+        for(int q = 0; q < 2; ++q)
+          if(r0 + q * kBT + tid < r1)
+            w[q * kBT + tid] = acc[q];
+        __syncthreads();
+        if(r0 < r1)
+          block_proj_sm(vs, w, np, r0, r1, k, dA + (long)c * m2);
+        if(!group_barrier(ctr, target += C, C, a.err))
+          return;
+        // w -= V h, then the second projections (k_b_sub_proj, pass 0)
+        gather_h(dA, nb, m2, k, h);
+        for(int t = tid; t < k; t += kBT)
+          hacc[t] = to_d2(h[t]);
+        for(long i = r0 + tid; i < r1; i += kBT) {
+          V v = w[i - r0];
+          for(int t = 0; t < k; ++t) {
+            V cf = h[t];
+            cf.x = -cf.x;
+            cf.y = -cf.y;
+            v = cfma(vs[(long)t * np + i], cf, v);
+          }
+          w[i - r0] = v;
+        }
+        __syncthreads();
+        if(r0 < r1)
+          block_proj_sm(vs, w, np, r0, r1, k, dB + (long)c * m2);
+        if(!group_barrier(ctr, target += C, C, a.err))
+          return;
+        // w -= V h and |w|^2 (k_b_sub_proj, pass 1); w kept for the next product
+        gather_h(dB, nb, m2, k, h);
+        for(int t = tid; t < k; t += kBT)
+          hacc[t] = cadd(hacc[t], to_d2(h[t]));
+        double nrm = 0.0;
+        V *wn = wb + (long)(j & 1) * np;
+        for(long i = r0 + tid; i < r1; i += kBT) {
+          V v = w[i - r0];
+          for(int t = 0; t < k; ++t) {
+            V cf = h[t];
+            cf.x = -cf.x;
+            cf.y = -cf.y;
+            v = cfma(vs[(long)t * np + i], cf, v);
+          }
+          w[i - r0] = v;
+          wn[i] = v;
+          nrm = fma((double)v.x, (double)v.x, nrm);
+          nrm = fma((double)v.y, (double)v.y, nrm);
+        }
+        for(int o = 16; o > 0; o >>= 1)
+          nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
+        if((tid & 31) == 0)
+          red[tid >> 5] = nrm;
+        __syncthreads();
+        if(tid == 0 && r0 < r1) {
+          double sum = 0.0;
+          for(int q = 0; q < kBT / 32; ++q)
+            sum += red[q];
+          V *out = dA + (long)c * m2;
+          out[m2 - 1].x = sum;
+          out[m2 - 1].y = 0;
+        }
+        if(!group_barrier(ctr, target += C, C, a.err))
+          return;
+        // Hessenberg column j, rotations, |g_{j+1}| and the stop test (k_b_givens)
+        if(tid == 0) {
+          double accn = dA[m2 - 1].x;
+          for(int q = 1; q < nb; ++q)
+            accn += dA[(long)q * m2 + m2 - 1].x;
+          const double hn = sqrt(accn);
+          for(int t = 0; t <= j; ++t)
+            col[t] = hacc[t];
+          for(int i = 0; i < j; ++i) {
+            const double2 p = col[i], q = col[i + 1];
+            col[i] = cadd(cmul(cconj(c_s[i]), p), cmul(cconj(cneg(s_s[i])), q));
+            col[i + 1] = cadd(cmul(s_s[i], p), cmul(c_s[i], q));
+          }
+          double2 cr, sr;
+          const double2 hk1 = make_double2(hn, 0.0);
+          givens_dev(col[j], hk1, cr, sr);
+          c_s[j] = cr;
+          s_s[j] = sr;
+          const double2 hk = col[j];
+          col[j] = cadd(cmul(cconj(cr), hk), cmul(cconj(cneg(sr)), hk1));
+          const double2 g0 = gs[j];
+          gs[j] = cmul(cconj(cr), g0);
+          gs[j + 1] = cmul(sr, g0);
+          inv_s = hn > 0.0 ? 1.0 / hn : 0.0;
+          sl.k = j + 1;
+          sl.steps++;
+          sl.inner = !(cabs2(gs[j + 1]) <= sl.thr || hn == 0.0 || j + 1 >= m);
+          if(c == 0)
+            for(int t = 0; t <= j; ++t)
+              H[(long)j * (m + 1) + t] = col[t];
+        }
+        __syncthreads();
+        if(!sl.inner)
+          break;
+        // v_{j+1} = w / h_{j+1,j} (k_b_scale)
+        for(long i = r0 + tid; i < r1; i += kBT) {
+          const V v = w[i - r0];
+          V o;
+          o.x = v.x * inv_s;
+          o.y = v.y * inv_s;
+          vs[(long)(j + 1) * np + i] = o;
+        }
+      }
+      // end of the cycle: y = R^{-1} g from CTA 0's columns (k_b_end), x += V y
+      if(!group_barrier(ctr, target += C, C, a.err))
+        return;
+      if(tid == 0) {
+        const int k = sl.k;
+        for(int j = k - 1; j >= 0; --j) {
+          double2 v = gs[j];
+          for(int q = j + 1; q < k; ++q)
+            v = cadd(v, cneg(cmul(H[(long)q * (m + 1) + j], ys[q])));
+          ys[j] = cdiv(v, H[(long)j * (m + 1) + j]);
+        }
+        sl.cycles++;
+        sl.xzero = 0;
+      }
+      __syncthreads();
+      for(long i = r0 + tid; i < r1; i += kBT) {
+        double2 v = xv[i];
+        for(int t = 0; t < sl.k; ++t)
+          v = cfma(to_d2(vs[(long)t * np + i]), ys[t], v);
+        xv[i] = v;
+      }
+      if(!group_barrier(ctr, target += C, C, a.err))
+        return;
+    }
+    if(tid == 0 && c == 0)
+      a.st[s] = sl;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Size classes
 // ---------------------------------------------------------------------------
 
@@ -632,6 +1069,15 @@ template <typename M, typename V> struct Class {
   double2 *hacc = nullptr, *Hm = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr;
   double *inv = nullptr;
   unsigned long long *counter = nullptr;
+  // the fused solve (np <= kFusedRows): w of the last two steps per slot, the
+  // groups' barrier counters and the give-up flag
+  bool fused_ok = false;
+  V *wbuf = nullptr;
+  unsigned *fbar = nullptr;
+  int *ferr = nullptr;
+  int *h_ferr = nullptr;
+  size_t fsmem = 0;
+  int fcap = 0;  // CTAs of k_b_fused resident on the device
   // pinned host mirrors
   Slot *h_st = nullptr;
   Ctl *h_ctl = nullptr;
@@ -657,7 +1103,7 @@ template <typename M, typename V> struct Class {
            2 * sizeof(double2) * (size_t)nbf * m2 +
            sizeof(double2) * ((size_t)m2 + (size_t)m * (m + 1) + 2 * (size_t)m + (m + 1) + m) +
            sizeof(int4) * (size_t)((np + 127) / 128) * nsm + sizeof(Slot) +
-           2 * nbuf * sizeof(BatchMat) + 64;
+           2 * nbuf * sizeof(BatchMat) + 64 + (np <= kFusedRows ? 2 * sizeof(V) * np + 128 : 0);
   }
 
   int init(om_context *c, const ClassKey &k, int slots, int buffers) {
@@ -683,7 +1129,8 @@ template <typename M, typename V> struct Class {
                    Bz * sizeof(double2) * m2,
                    Bz * sizeof(double2) * m * (m + 1), Bz * sizeof(double2) * m,
                    Bz * sizeof(double2) * m, Bz * sizeof(double2) * (m + 1), Bz * sizeof(double2) * m,
-                   Bz * sizeof(double), sizeof(unsigned long long)};
+                   Bz * sizeof(double), sizeof(unsigned long long),
+                   np <= kFusedRows ? Bz * 2 * sizeof(V) * np : 0, Bz * 32 * sizeof(unsigned) + 16};
     bytes = 0;
     for(size_t v : sz)
       bytes += rup(v);
@@ -716,7 +1163,11 @@ template <typename M, typename V> struct Class {
     y = (double2 *)take(sz[i++]);
     inv = (double *)take(sz[i++]);
     counter = (unsigned long long *)take(sz[i++]);
+    wbuf = (V *)take(sz[i++]);
+    fbar = (unsigned *)take(sz[i++]);
+    ferr = (int *)(fbar + 32 * Bz);
     if(cudaMallocHost(&h_st, Bz * sizeof(Slot)) != cudaSuccess ||
+       cudaMallocHost(&h_ferr, sizeof(int)) != cudaSuccess ||
        cudaMallocHost(&h_ctl, sizeof(Ctl)) != cudaSuccess ||
        cudaMallocHost(&h_tiles, sizeof(int4) * (size_t)max_tiles) != cudaSuccess ||
        cudaMallocHost(&h_mats, 2 * Bz * nbuf * sizeof(BatchMat)) != cudaSuccess ||
@@ -733,6 +1184,23 @@ template <typename M, typename V> struct Class {
     ev_aux.resize(ctx->aux.size());
     for(auto &e : ev_aux)
       cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if(np <= kFusedRows) {
+      // the fused solve: its shared memory and how many of its CTAs fit
+      fsmem = FusedSmem<V>(m, m2).bytes;
+      int coop = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+      // (the attribute is the largest any class asks for, so that classes on
+      // other host threads never launch below a smaller setting)
+      if(coop && fsmem <= kFusedSmemMax &&
+         cudaFuncSetAttribute(k_b_fused<M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFusedSmemMax) ==
+             cudaSuccess &&
+         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_b_fused<M, V>, kBT, fsmem) == cudaSuccess &&
+         per_sm >= 1) {
+        fcap = per_sm * ctx->sm_count;
+        fused_ok = fcap >= nbf;
+      }
+      cudaGetLastError();
+    }
     // a choice made for this class before (the graphs are captured once the
     // matvec configuration is known: here, or after the autotuning)
     {
@@ -869,6 +1337,7 @@ template <typename M, typename V> struct Class {
     if(h_tiles) cudaFreeHost(h_tiles);
     if(h_mats) cudaFreeHost(h_mats);
     if(h_xsec) cudaFreeHost(h_xsec);
+    if(h_ferr) cudaFreeHost(h_ferr);
     if(ev_main) cudaEventDestroy(ev_main);
     for(auto &e : ev_asm)
       if(e) cudaEventDestroy(e);
@@ -957,9 +1426,48 @@ template <typename M, typename V> struct Class {
     return OM_OK;
   }
 
+  // The fused form of solve(): one cooperative launch of k_b_fused, a group of
+  // nbf CTAs per slot, as many groups as fit (at most one per slot with a
+  // system).
+  int solve_fused(long *launches) {
+    int active = 0;
+    for(int s = 0; s < B; ++s)
+      active += h_st[s].n > 0 && h_st[s].outer;
+    cudaMemcpyAsync(st, h_st, sizeof(Slot) * B, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(x, 0, sizeof(double2) * B * np, ctx->stream);
+    cudaMemsetAsync(fbar, 0, sizeof(unsigned) * 32 * B + 16, ctx->stream);
+    if(active) {
+      const int groups = std::max(1, std::min(active, fcap / nbf));
+      FusedArgs<V> fa{st, B, b, x, r, Vb, vslot, np, wbuf, (V *)dpA, (V *)dpB, Hm, m, m2, nbf, nbf,
+                      key.tol, key.inner_rel, key.max_cycles, fbar, ferr};
+      void *args[] = {&fa};
+      cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_b_fused<M, V>, dim3((unsigned)(groups * nbf)),
+                                                  dim3(kBT), args, fsmem, ctx->stream);
+      if(e != cudaSuccess) {
+        ctx->err = std::string("fused batched solve: ") + cudaGetErrorString(e);
+        return OM_ERR_CUDA;
+      }
+      ++*launches;
+    }
+    cudaMemcpyAsync(h_st, st, sizeof(Slot) * B, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(h_ferr, ferr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if(e != cudaSuccess) {
+      ctx->err = std::string("fused batched solve: ") + cudaGetErrorString(e);
+      return OM_ERR_CUDA;
+    }
+    if(*h_ferr) {
+      ctx->err = "fused batched solve: a group barrier wait timed out";
+      return OM_ERR_CUDA;
+    }
+    return OM_OK;
+  }
+
   // Solve the systems of the slots whose h_st entries are set (uploaded here):
   // replays the graphs until no slot needs another cycle.
   int solve(long *launches) {
+    if(fused_ok && (ctx->batch_fused == 2 || (ctx->batch_fused == 1 && np <= kFusedAuto)))
+      return solve_fused(launches);
     if(!tuned) {
       const int rc = autotune();
       if(rc)

@@ -441,6 +441,8 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
     ctx->lu_persist = std::min(t->lu_persistent, 3);
   if(t->batch_tiles >= 0)
     ctx->batch_tiles = std::min(t->batch_tiles, 8);
+  if(t->batch_fused >= 0)
+    ctx->batch_fused = std::min(t->batch_fused, 2);
   return OM_OK;
 }
 

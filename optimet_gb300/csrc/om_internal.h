@@ -128,6 +128,10 @@ struct om_context {
   int lu_persist = 1;
   // batched matvec tiles: 0 autotuned per size class, k > 0 candidate k - 1
   int batch_tiles = 0;
+  // batched solves: 1 one cooperative launch per solve (k_b_fused) for the
+  // classes of at most 1,024 padded unknowns, 2 for those of at most 4,096,
+  // 0 the lockstep graphs for every class
+  int batch_fused = 1;
   int asm_rot = 1;  // precision-form assembly by rotated z-axis translations (assemble_rot.cu)
   size_t budget = 0;
   size_t used = 0;

@@ -392,7 +392,7 @@ int om_server_create(int device, size_t hbm_budget, int slots, om_server **out) 
   if(slots > 1) {
     // side by side, the matvec kernels leave room for another slot's assembly
     // (plain matvec: the TMA one's stage buffers would fill the SM)
-    const om_tuning t{4, 2, 50, 50, -1, 0, -1, -1, -1};
+    const om_tuning t{4, 2, 50, 50, -1, 0, -1, -1, -1, -1};
     for(auto &s : srv->slots)
       om_context_tune(s.ctx, &t);
   }
@@ -523,11 +523,11 @@ int om_server_autotune(om_server *srv, const om_request *rq, int count, double s
     return OM_ERR_INVALID;
   // the TMA matvec's 144 KB of stage buffers leave no room for another slot's
   // assembly on the SM, so the overlapping candidates use the plain kernel
-  static const om_tuning cands[] = {{8, 8, -1, -1, -1, 1, -1, -1, -1}, {6, 3, 50, 50, -1, 0, -1, -1, -1},
-                                    {4, 2, 50, 50, -1, 0, -1, -1, -1}, {4, 2, -1, -1, -1, 0, -1, -1, -1},
-                                    {3, 2, 50, 50, -1, 0, -1, -1, -1}, {3, 2, -1, -1, -1, 0, -1, -1, -1},
-                                    {4, 1, -1, -1, -1, 0, -1, -1, -1}, {5, 2, -1, -1, -1, 0, -1, -1, -1},
-                                    {4, 3, -1, -1, -1, 0, -1, -1, -1}, {6, 2, -1, -1, -1, 0, -1, -1, -1}};
+  static const om_tuning cands[] = {{8, 8, -1, -1, -1, 1, -1, -1, -1, -1}, {6, 3, 50, 50, -1, 0, -1, -1, -1, -1},
+                                    {4, 2, 50, 50, -1, 0, -1, -1, -1, -1}, {4, 2, -1, -1, -1, 0, -1, -1, -1, -1},
+                                    {3, 2, 50, 50, -1, 0, -1, -1, -1, -1}, {3, 2, -1, -1, -1, 0, -1, -1, -1, -1},
+                                    {4, 1, -1, -1, -1, 0, -1, -1, -1, -1}, {5, 2, -1, -1, -1, 0, -1, -1, -1, -1},
+                                    {4, 3, -1, -1, -1, 0, -1, -1, -1, -1}, {6, 2, -1, -1, -1, 0, -1, -1, -1, -1}};
   const int nslots = (int)srv->slots.size();
   double best = 1e300;
   om_tuning pick = cands[0];

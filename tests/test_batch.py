@@ -128,7 +128,7 @@ def test_autotuned_tiles_do_not_change_the_bits(G, form):
     runs = []
     for cand in [0] + list(range(1, 9)):
         c = G.Context(0)
-        c.tune(batch_tiles=cand)
+        c.tune(batch_tiles=cand, batch_fused=0)  # the lockstep form (the fused solve has no tiles)
         runs.append(G.batch_solve(c, reqs))
         if cand == 0:
             chosen = G.batch_tiles(c)
@@ -144,6 +144,45 @@ def test_autotuned_tiles_do_not_change_the_bits(G, form):
             assert a["status"] == b["status"] == G.OK
             assert np.array_equal(a["xsec"], b["xsec"]) and np.array_equal(a["xsec_sh"], b["xsec_sh"])
             assert a["ff"]["iterations"] == b["ff"]["iterations"]
+
+
+def blocky_requests(G, opts, prec, seed=13):
+    """Size classes whose slots span several 512-row blocks (fused groups of
+    2 to 7 CTAs) and several 1,024-column chunks."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, (N, nmax) in enumerate([(12, 8), (16, 9), (10, 6), (3, 12), (12, 8)]):
+        xyz, rad = random_cluster(rng, N, 1400 * nm, 40 * nm, 80 * nm, 20 * nm)
+        sh = i % 2 == 1
+        sp = G.spheres_array(xyz, rad, (2.0 + 0.04j) ** 2, nmax, eps_sh=(2.2 + 0.06j) ** 2,
+                             ksippp=1.0 if sh else 0.0, ksiparppar=0.25 if sh else 0.0)
+        wave = G.plane_wave(rng.uniform(500, 800) * nm, theta=rng.uniform(0, np.pi),
+                            phi=rng.uniform(-np.pi, np.pi), sh=sh)
+        out.append((sp, G.medium(1.0), wave, opts, prec))
+    return out
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_fused_solve_matches_the_lockstep_graphs(G, form):
+    """The fused solve (one cooperative launch per solve, a group of CTAs per
+    slot) against the lockstep Arnoldi steps replayed as graphs: the same
+    bits, statistics included, in far fewer launches."""
+    opts, prec = (plain(G), G.C128) if form == "plain" else (mixed(G), G.C64)
+    reqs = ragged_requests(G, opts, prec, seed=21) + blocky_requests(G, opts, prec)
+    runs, launches = [], []
+    for fused in (2, 0):  # 2: every class of these requests through the fused solve
+        c = G.Context(0)
+        c.tune(batch_fused=fused)
+        runs.append(G.batch_solve(c, reqs))
+        launches.append(c.last_launches)
+        c.close()
+    for a, b in zip(*runs):
+        assert a["status"] == b["status"] == G.OK
+        assert np.array_equal(a["xsec"], b["xsec"]) and np.array_equal(a["xsec_sh"], b["xsec_sh"])
+        for h in ("ff", "sh"):
+            for f in ("iterations", "inner_iterations", "rel_residual"):
+                assert a[h][f] == b[h][f]
+    assert launches[0] < launches[1]
 
 
 def test_failures_stay_with_their_request(G, ctx):
