@@ -43,6 +43,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "wavelength-solves/sec mixed vs FP64 on 1 GB300 at 1e-6 Qext err; p50/p99 latency"
+
+# DRAM bytes read per launch of k_matvec_tma<true> over its algorithmic
+# 4 n^2 bytes: 163.912 MB / 163.840 MB in an ncu capture at n = 6,400 (the
+# reads grow with n^2; the writes are the split-K partial sums, 8 bytes per
+# row and 1,024-column chunk at the c2 size)
+BF16_READ_RATIO = 163.912 / 163.840
 UNIT = "wavelength-solves/s"
 nm = 1e-9
 
@@ -239,6 +245,7 @@ def gpu_arm(args, w):
         barrier()
         t_mixed = float(np.sum(lat))
     kt = ctx.timers(False)
+    kin = ctx.inner_timers()
     clocks = clk.summary()
 
     # ---- plain FP64 form on the same wavelengths ----
@@ -273,6 +280,9 @@ def gpu_arm(args, w):
                 "data": "synthetic (seeded random clusters)",
                 "config": {"workload": args.workload + ": " + w["desc"], "unknowns": n},
                 "fp64": {"value": k64 / t_fp64}, "kernels_ms": {k: v[0] / max(v[1], 1) for k, v in kt.items()},
+                "inner_products": {k: {"ms_avg": v[0] / max(v[1], 1), "launches": v[1]} for k, v in kin.items()},
+                "iterations": {"outer": outer / args.steps, "inner": inner / args.steps},
+                "qext_rel_err_vs_fp64": err,
                 "gpu_launches": total_launches, "clocks": clocks}
 
     # ---- batched / served form: om_server with `slots` contexts on the GPU ----
@@ -341,8 +351,14 @@ def gpu_arm(args, w):
 
     hbm, how = peaks()
     mv_ms, mv_n = kt["matvec_c64"]
-    bytes_mv = 8.0 * n * n  # complex64 matrix streamed once per inner matvec
-    achieved = bytes_mv / (mv_ms / mv_n * 1e-3) / 1e9 if mv_n else 0.0
+    bytes_mv = 8.0 * n * n  # complex64 matrix streamed once per product
+    achieved_c64 = bytes_mv / (mv_ms / mv_n * 1e-3) / 1e9 if mv_n else None
+    # the inner products on the bf16 copy (4 bytes per entry), and the one
+    # complex64 product per solve that writes the copy (8 bytes read, 4 written)
+    b16_ms, b16_n = kin["bf16"]
+    cp_ms, cp_n = kin["copy"]
+    bytes_b16 = 4.0 * n * n
+    achieved = bytes_b16 / (b16_ms / b16_n * 1e-3) / 1e9 if b16_n else 0.0
     asm_ms, asm_n = kt["assemble"]
     bytes_asm = 8.0 * n * n  # complex64 matrix written
     mv64_ms, mv64_n = kt64["matvec_c128"]
@@ -350,12 +366,14 @@ def gpu_arm(args, w):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_srv_all / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64 (FP32) inner + c128 (FP64) outer/assembly",
+        "dtype": "c64 (FP32) matrix; inner FP32 GMRES on its bf16 copy (FP32 accumulation); "
+                 "c128 (FP64) outer residuals (compensated) and assembly",
         "data": "synthetic (seeded random clusters)",
         "config": {"workload": args.workload + ": " + w["desc"], "unknowns": n,
                    "parallelism": f"replicas x{world}, {args.slots} serving slots per GPU",
                    "l2": "inputs larger than L2 (no flush)",
-                   "solver": "FGMRES(FP64 outer, tol 1e-7) + GMRES(FP32 inner, 80 it, tol 1e-3)",
+                   "solver": "FGMRES(FP64 outer, tol 1e-7) + GMRES(FP32 inner, 80 it, tol 1e-3; its "
+                             "products on a bf16 copy of the complex64 matrix, written by the first)",
                    "timing": "CUDA events on every slot's stream (om_server_mark) around the K requests",
                    "launch_tuning": {"mixed": tuning, "fp64": tuning64,
                                      "how": "om_server_autotune on warm-up requests"}},
@@ -386,15 +404,12 @@ def gpu_arm(args, w):
                 "queue_ms_max": float(max(r["queue_ms"] for r in res_e2e)),
                 "clocks": clk_e2e.summary()},
         "roofline": {"bound": "hbm",
-                     "kernel": "k_matvec_tma<0> (FP32 inner matvec, TMA-staged; timed in the "
-                               "single-stream part, where a context uses it)",
+                     "kernel": "k_matvec_tma<true> (inner FP32 product on the bf16 copy, TMA-staged; "
+                               "timed in the single-stream part, where a context uses it)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": how + " (MEASURED_PEAKS.json hbm_gbs)",
-                     # DRAM bytes per launch from an ncu capture of the same kernel at
-                     # n = 6,400 (dram read 327.75 MB + write 4.16 MB): 1.0129 x the
-                     # algorithmic 8 n^2 bytes
-                     "traffic": bytes_mv * 1.0129,
-                     "algorithmic_bytes_per_launch": bytes_mv},
+                     "traffic": bytes_b16 * BF16_READ_RATIO + 8.0 * n * -(-n // 1024),
+                     "algorithmic_bytes_per_launch": bytes_b16},
         "kernels": {
             "assemble_mixed": {"ms_avg": asm_ms / max(asm_n, 1), "launches": asm_n,
                                "written_GBps": bytes_asm / (asm_ms / max(asm_n, 1) * 1e-3) / 1e9
@@ -403,8 +418,13 @@ def gpu_arm(args, w):
                                if asm_n else None,
                                "kernel": "k_assemble_rot (rotated z-axis translations)",
                                "bound": "hbm write (8 n^2 B per assembly)"},
+            "matvec_bf16_inner": {"ms_avg": b16_ms / max(b16_n, 1), "launches": b16_n,
+                                  "GBps": achieved, "bound": "hbm (4 n^2 B read)"},
+            "matvec_c64_writing_copy": {"ms_avg": cp_ms / max(cp_n, 1), "launches": cp_n,
+                                        "GBps": 12.0 * n * n / (cp_ms / cp_n * 1e-3) / 1e9 if cp_n else None,
+                                        "bound": "hbm (8 n^2 B read + 4 n^2 B written)"},
             "matvec_c64": {"ms_avg": mv_ms / max(mv_n, 1), "launches": mv_n,
-                           "GBps": achieved, "bound": "hbm"},
+                           "GBps": achieved_c64, "bound": "hbm"},
             "matvec_c64_compensated": {"ms_avg": kt["matvec_c64_df"][0] / max(kt["matvec_c64_df"][1], 1),
                                        "launches": kt["matvec_c64_df"][1],
                                        "GBps": bytes_mv / (kt["matvec_c64_df"][0] / max(kt["matvec_c64_df"][1], 1) * 1e-3) / 1e9 if kt["matvec_c64_df"][1] else None},

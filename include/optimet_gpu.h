@@ -115,6 +115,11 @@ int om_context_synchronize(om_context *ctx);
  * complex128 (compensated) matvec ms, launches} (out may be NULL), resets
  * them and switches timing on or off. */
 int om_context_timers(om_context *ctx, int enable, double *out);
+/* Timers of the inner FP32 GMRES products of OM_SOLVE_FGMRES_MIXED on the
+ * bf16 copy (recorded while om_context_timers has switched timing on):
+ * out[4] = {products on the bf16 copy ms, launches, complex64 products that
+ * write the copy ms, launches}; resets them. */
+int om_context_inner_timers(om_context *ctx, double *out);
 /* LU phase timers, recorded while om_context_timers has switched timing on:
  * out[8] = {factorization ms, factorizations, panel ms, panels, trailing-
  * update ms, trailing updates, triangular-solve ms, solves (one forward and
@@ -158,6 +163,11 @@ typedef struct {
                             most 1,024 padded unknowns, 2 for those of at most 4,096, 0 never
                             (the lockstep Arnoldi steps of all slots as captured graphs); the
                             same bits either way */
+  int inner_bf16;        /* OM_SOLVE_FGMRES_MIXED: the inner FP32 GMRES reads a bf16 copy of the
+                            complex64 matrix (4 bytes per entry; its first product writes the copy
+                            while it reads the complex64 matrix) when 1 (default), the complex64
+                            matrix itself when 0; the outer FP64 residuals always use the
+                            complex64 matrix */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any
@@ -167,6 +177,13 @@ int om_context_tune(om_context *ctx, const om_tuning *t);
  * over all of k (about 21 significant bits relative to the rows' and
  * columns' magnitudes). The role of the trailing pzgemm of pzgesv
  * (ScalapackSolver.cpp:54-130). */
+/* y = S x, complex64 interleaved (S column-major n x n, host buffers), by the
+ * inner FP32 GMRES product of OM_SOLVE_FGMRES_MIXED repeated `products`
+ * times: the first on the complex64 matrix (writing its bf16 copy when the
+ * context's inner_bf16 tuning is on), the later ones on the copy; y is the
+ * last product. The role of the FP32 matvecs inside the reference's GMRES
+ * iterations (PreconditionedMatrix.cpp:892-1133). */
+int om_matvec_inner_c64(om_context *ctx, long n, const float *S, const float *x, float *y, int products);
 int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, long lda,
                      const float *B, long ldb, float *C, long ldc);
 /* Statistics of an ACA-compressed matrix (om_assemble with OM_ACA): device

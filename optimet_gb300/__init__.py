@@ -69,7 +69,7 @@ class Tuning(C.Structure):
                 ("assemble_carveout", C.c_int), ("matvec_carveout", C.c_int),
                 ("lu_tensor_cores", C.c_int), ("matvec_tma", C.c_int),
                 ("assemble_rotation", C.c_int), ("lu_persistent", C.c_int), ("batch_tiles", C.c_int),
-                ("batch_fused", C.c_int)]
+                ("batch_fused", C.c_int), ("inner_bf16", C.c_int)]
 
 
 class Request(C.Structure):
@@ -106,11 +106,13 @@ def lib():
         L.om_context_synchronize.argtypes = [vp]
         L.om_context_timers.argtypes = [vp, C.c_int, _dp]
         L.om_context_lu_timers.argtypes = [vp, _dp]
+        L.om_context_inner_timers.argtypes = [vp, _dp]
         L.om_batch_tiles.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
         L.om_context_mark.argtypes = [vp, _dp]
         L.om_context_tune.argtypes = [vp, C.POINTER(Tuning)]
         L.om_aca_info.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp,
                                   C.POINTER(C.c_int)]
+        L.om_matvec_inner_c64.argtypes = [vp, C.c_long, _fp, _fp, _fp, C.c_int]
         L.om_cgemm_sub_c64.argtypes = [vp, C.c_long, C.c_long, C.c_int, _fp, C.c_long, _fp,
                                        C.c_long, _fp, C.c_long]
         L.om_problem_create.argtypes = [vp, C.POINTER(Sphere), C.c_int, C.POINTER(Medium),
@@ -207,11 +209,11 @@ class Context:
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
              matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1,
-             batch_fused=-1):
+             batch_fused=-1, inner_bf16=-1):
         """Launch tuning (om_context_tune); 0 / -1 keep the current value."""
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
                    lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles,
-                   batch_fused)
+                   batch_fused, inner_bf16)
         self.check(lib().om_context_tune(self.h, C.byref(t)))
 
     def timers(self, enable=True):
@@ -220,6 +222,14 @@ class Context:
         self.check(lib().om_context_timers(self.h, int(enable), _p(out)))
         return {"assemble": (out[0], int(out[1])), "matvec_c128": (out[2], int(out[3])),
                 "matvec_c64": (out[4], int(out[5])), "matvec_c64_df": (out[6], int(out[7]))}
+
+    def inner_timers(self):
+        """Inner FP32 GMRES products of the precision form since the last
+        call (recorded while timers() is on): dict of (milliseconds, launches)
+        for the products on the bf16 copy and those that write it."""
+        out = np.zeros(4)
+        self.check(lib().om_context_inner_timers(self.h, _p(out)))
+        return {"bf16": (out[0], int(out[1])), "copy": (out[2], int(out[3]))}
 
     def lu_timers(self):
         """LU phase times since the last call (recorded while timers() is on):
@@ -445,6 +455,19 @@ def cgemm_sub_c64(ctx: Context, A, B, C_):
     return out
 
 
+def matvec_inner(ctx: Context, S, x, products: int = 1) -> np.ndarray:
+    """y = S x by the precision form's inner FP32 product, `products` times
+    (om_matvec_inner_c64): the first on the complex64 matrix (it writes the
+    bf16 copy when inner_bf16 is on), the later ones on the copy."""
+    S = np.asfortranarray(S, dtype=np.complex64)
+    x = np.ascontiguousarray(x, dtype=np.complex64)
+    n = S.shape[0]
+    y = np.zeros(n, dtype=np.complex64)
+    fp = lambda a: a.ctypes.data_as(_fp)
+    ctx.check(lib().om_matvec_inner_c64(ctx.h, n, fp(S), fp(x), fp(y), products))
+    return y
+
+
 def clg_tables(ctx: Context, nmax: int) -> np.ndarray:
     """The nine SH coupling tables computed on the device, flattened (9 P^3)."""
     P = nmax * (nmax + 2)
@@ -556,10 +579,10 @@ class Server:
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
              matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1,
-             batch_fused=-1):
+             batch_fused=-1, inner_bf16=-1):
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
                    lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles,
-                   batch_fused)
+                   batch_fused, inner_bf16)
         rc = lib().om_server_tune(self.h, C.byref(t))
         if rc:
             raise OptimetError(rc, "server tune")

@@ -388,6 +388,8 @@ void collect_timers(om_context *ctx) {
   fold(ctx->ev_mv32, ctx->t_mv32, ctx->n_mv32);
   fold(ctx->ev_asm, ctx->t_asm, ctx->n_asm);
   fold(ctx->ev_mvdf, ctx->t_mvdf, ctx->n_mvdf);
+  fold(ctx->ev_mv16, ctx->t_mv16, ctx->n_mv16);
+  fold(ctx->ev_mvcp, ctx->t_mvcp, ctx->n_mvcp);
   fold(ctx->ev_luf, ctx->t_luf, ctx->n_luf);
   fold(ctx->ev_lup, ctx->t_lup, ctx->n_lup);
   fold(ctx->ev_luu, ctx->t_luu, ctx->n_luu);
@@ -443,7 +445,37 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
     ctx->batch_tiles = std::min(t->batch_tiles, 8);
   if(t->batch_fused >= 0)
     ctx->batch_fused = std::min(t->batch_fused, 2);
+  if(t->inner_bf16 >= 0)
+    ctx->inner_bf16 = t->inner_bf16 ? 1 : 0;
   return OM_OK;
+}
+
+int om_matvec_inner_c64(om_context *ctx, long n, const float *S, const float *x, float *y, int products) {
+  if(!ctx || !S || !x || !y || n < 1 || products < 1)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  float2 *dS = nullptr, *dx = nullptr, *dy = nullptr;
+  const size_t nn = (size_t)n * n;
+  int rc = dev_alloc(ctx, &dS, nn);
+  if(!rc) rc = dev_alloc(ctx, &dx, (size_t)n);
+  if(!rc) rc = dev_alloc(ctx, &dy, (size_t)n);
+  if(!rc) {
+    cudaMemcpyAsync(dS, S, sizeof(float2) * nn, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dx, x, sizeof(float2) * n, cudaMemcpyHostToDevice, ctx->stream);
+    rc = om::inner_products(ctx, dS, n, dx, dy, products);
+    if(!rc) {
+      cudaMemcpyAsync(y, dy, sizeof(float2) * n, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if(e != cudaSuccess)
+        rc = cuda_fail(ctx, e, "inner product");
+    }
+  }
+  cudaStreamSynchronize(ctx->stream);
+  dev_free(ctx, dS, nn);
+  dev_free(ctx, dx, (size_t)n);
+  dev_free(ctx, dy, (size_t)n);
+  return rc;
 }
 
 int om_cgemm_sub_c64(om_context *ctx, long m, long n, int k, const float *A, long lda,
@@ -511,6 +543,22 @@ int om_context_timers(om_context *ctx, int enable, double *out) {
   ctx->t_asm = ctx->t_mv64 = ctx->t_mv32 = ctx->t_mvdf = 0;
   ctx->n_asm = ctx->n_mv64 = ctx->n_mv32 = ctx->n_mvdf = 0;
   ctx->timing = enable != 0;
+  return OM_OK;
+}
+
+int om_context_inner_timers(om_context *ctx, double *out) {
+  if(!ctx)
+    return OM_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  om::collect_timers(ctx);
+  if(out) {
+    out[0] = ctx->t_mv16;
+    out[1] = (double)ctx->n_mv16;
+    out[2] = ctx->t_mvcp;
+    out[3] = (double)ctx->n_mvcp;
+  }
+  ctx->t_mv16 = ctx->t_mvcp = 0;
+  ctx->n_mv16 = ctx->n_mvcp = 0;
   return OM_OK;
 }
 

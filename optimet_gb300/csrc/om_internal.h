@@ -132,6 +132,9 @@ struct om_context {
   // classes of at most 1,024 padded unknowns, 2 for those of at most 4,096,
   // 0 the lockstep graphs for every class
   int batch_fused = 1;
+  // precision-form FGMRES: the inner FP32 GMRES reads a bf16 copy of the
+  // complex64 matrix (written by its first product) when 1
+  int inner_bf16 = 1;
   int asm_rot = 1;  // precision-form assembly by rotated z-axis translations (assemble_rot.cu)
   size_t budget = 0;
   size_t used = 0;
@@ -146,6 +149,10 @@ struct om_context {
   double t_mv64 = 0, t_mv32 = 0, t_mvdf = 0, t_asm = 0;  // accumulated milliseconds
   cudaEvent_t mark = nullptr;                // last om_context_mark event
   long n_mv64 = 0, n_mv32 = 0, n_mvdf = 0, n_asm = 0;
+  // inner products on the bf16 copy, and the complex64 products that write it
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_mv16, ev_mvcp;
+  double t_mv16 = 0, t_mvcp = 0;
+  long n_mv16 = 0, n_mvcp = 0;
   // LU phases: whole factorizations, panels, trailing updates, triangular solves
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_luf, ev_lup, ev_luu, ev_lus;
   double t_luf = 0, t_lup = 0, t_luu = 0, t_lus = 0;
@@ -298,8 +305,15 @@ void batch_release(om_context *ctx);
 // cuTensorMapEncodeTiled through the runtime's driver entry point (nullptr
 // when the driver does not provide it)
 void *tensor_map_encoder();
+// (writing the bf16 copy of S into `copy`, ld ldc, when that is not null)
 bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *part, int row_tiles,
-                       long tiles, int cols, unsigned grid);
+                       long tiles, int cols, unsigned grid, void *copy, long ldc);
+// solve.cu: `products` inner FP32 GMRES products on device buffers (the first
+// writes the bf16 copy when ctx->inner_bf16 is set, the later ones read it)
+int inner_products(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *y, int products);
+// the same product on the bf16 copy (Bf16c entries, ld ldh a multiple of 4)
+bool launch_matvec_bf16(om_context *ctx, const void *H, long n, long ldh, const float2 *x, float2 *part,
+                        int row_tiles, long tiles, int cols, unsigned grid);
 
 // capi.cu: stream-ordered device memory counted against the context budget
 int dev_malloc(om_context *ctx, void **p, size_t bytes);

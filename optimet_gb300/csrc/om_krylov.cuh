@@ -4,9 +4,34 @@
 // same, whichever solver runs it.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace om {
+
+// An entry of the precision form's bf16 copy of a complex64 matrix (the inner
+// FP32 GMRES reads it): the real part rounded to bf16 in the low 16 bits, the
+// imaginary part in the high 16 bits. bf16 is the high half of an FP32 word,
+// so each part unpacks by one bit operation.
+struct Bf16c {
+  unsigned v;
+};
+__device__ __forceinline__ Bf16c pack_bf16c(float2 a) {  // round to nearest even
+  const unsigned re = __bfloat16_as_ushort(__float2bfloat16_rn(a.x));
+  const unsigned im = __bfloat16_as_ushort(__float2bfloat16_rn(a.y));
+  return Bf16c{re | (im << 16)};
+}
+
+// a matrix entry as the vector type of a product
+template <typename V, typename M> __device__ __forceinline__ V mv_entry(const M &s) {
+  V a;
+  a.x = s.x;
+  a.y = s.y;
+  return a;
+}
+template <> __device__ __forceinline__ float2 mv_entry<float2, Bf16c>(const Bf16c &s) {
+  return make_float2(__uint_as_float(s.v << 16), __uint_as_float(s.v & 0xffff0000u));
+}
 
 template <typename V> __device__ __forceinline__ V cfma(V a, V b, V c) {  // c + a*b
   c.x = fma(a.x, b.x, c.x);
@@ -39,20 +64,50 @@ __device__ __forceinline__ V mv_row(const M *col, long ld, const V *xs, long j0,
       s[u] = col[u * ld];
 #pragma unroll
     for(int u = 0; u < 8; u += 2) {
-      V a0, a1;
-      a0.x = s[u].x; a0.y = s[u].y; a1.x = s[u + 1].x; a1.y = s[u + 1].y;
+      const V a0 = mv_entry<V>(s[u]), a1 = mv_entry<V>(s[u + 1]);
       acc0 = cfma(a0, xs[j - j0 + u], acc0);
       acc1 = cfma(a1, xs[j - j0 + u + 1], acc1);
     }
     col += 8 * ld;
   }
   for(; j < j1; ++j) {
-    M s0 = col[0];
-    V a0;
-    a0.x = s0.x;
-    a0.y = s0.y;
+    const V a0 = mv_entry<V>(col[0]);
     acc0 = cfma(a0, xs[j - j0], acc0);
     col += ld;
+  }
+  acc0.x += acc1.x;
+  acc0.y += acc1.y;
+  return acc0;
+}
+
+// mv_row on a complex64 row that also writes the row's entries into the bf16
+// copy (`copy` points at this row's entry of column j0, ld ldc)
+__device__ __forceinline__ float2 mv_row_copy(const float2 *col, long ld, const float2 *xs, long j0, long j1,
+                                              Bf16c *copy, long ldc) {
+  float2 acc0 = make_float2(0.f, 0.f), acc1 = acc0;
+  long j = j0;
+  for(; j + 7 < j1; j += 8) {
+    float2 s[8];
+#pragma unroll
+    for(int u = 0; u < 8; ++u)
+      s[u] = col[u * ld];
+#pragma unroll
+    for(int u = 0; u < 8; ++u)
+      copy[u * ldc] = pack_bf16c(s[u]);
+#pragma unroll
+    for(int u = 0; u < 8; u += 2) {
+      acc0 = cfma(s[u], xs[j - j0 + u], acc0);
+      acc1 = cfma(s[u + 1], xs[j - j0 + u + 1], acc1);
+    }
+    col += 8 * ld;
+    copy += 8 * ldc;
+  }
+  for(; j < j1; ++j) {
+    const float2 a0 = col[0];
+    copy[0] = pack_bf16c(a0);
+    acc0 = cfma(a0, xs[j - j0], acc0);
+    col += ld;
+    copy += ldc;
   }
   acc0.x += acc1.x;
   acc0.y += acc1.y;

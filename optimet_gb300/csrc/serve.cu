@@ -60,6 +60,8 @@ size_t estimate_bytes(const om_request &rq, int nmax) {
     b += n * n * 16;
   if(o.method == OM_SOLVE_LU_MIXED)
     b += n * n * 8;
+  if(o.method == OM_SOLVE_FGMRES_MIXED && rq.precision == OM_C64)
+    b += n * n * 4;  // the inner GMRES's bf16 copy of the matrix
   const size_t m = (size_t)std::max(o.max_iter, 1), mi = (size_t)std::max(o.inner_iter, 1);
   b += (2 * (m + 2) + (mi + 2) + 16) * n * 16;
   b += 2 * ((n + 1023) / 1024) * n * 16;
@@ -392,7 +394,7 @@ int om_server_create(int device, size_t hbm_budget, int slots, om_server **out) 
   if(slots > 1) {
     // side by side, the matvec kernels leave room for another slot's assembly
     // (plain matvec: the TMA one's stage buffers would fill the SM)
-    const om_tuning t{4, 2, 50, 50, -1, 0, -1, -1, -1, -1};
+    const om_tuning t{4, 2, 50, 50, -1, 0, -1, -1, -1, -1, -1};
     for(auto &s : srv->slots)
       om_context_tune(s.ctx, &t);
   }
@@ -523,11 +525,11 @@ int om_server_autotune(om_server *srv, const om_request *rq, int count, double s
     return OM_ERR_INVALID;
   // the TMA matvec's 144 KB of stage buffers leave no room for another slot's
   // assembly on the SM, so the overlapping candidates use the plain kernel
-  static const om_tuning cands[] = {{8, 8, -1, -1, -1, 1, -1, -1, -1, -1}, {6, 3, 50, 50, -1, 0, -1, -1, -1, -1},
-                                    {4, 2, 50, 50, -1, 0, -1, -1, -1, -1}, {4, 2, -1, -1, -1, 0, -1, -1, -1, -1},
-                                    {3, 2, 50, 50, -1, 0, -1, -1, -1, -1}, {3, 2, -1, -1, -1, 0, -1, -1, -1, -1},
-                                    {4, 1, -1, -1, -1, 0, -1, -1, -1, -1}, {5, 2, -1, -1, -1, 0, -1, -1, -1, -1},
-                                    {4, 3, -1, -1, -1, 0, -1, -1, -1, -1}, {6, 2, -1, -1, -1, 0, -1, -1, -1, -1}};
+  static const om_tuning cands[] = {{8, 8, -1, -1, -1, 1, -1, -1, -1, -1, -1}, {6, 3, 50, 50, -1, 0, -1, -1, -1, -1, -1},
+                                    {4, 2, 50, 50, -1, 0, -1, -1, -1, -1, -1}, {4, 2, -1, -1, -1, 0, -1, -1, -1, -1, -1},
+                                    {3, 2, 50, 50, -1, 0, -1, -1, -1, -1, -1}, {3, 2, -1, -1, -1, 0, -1, -1, -1, -1, -1},
+                                    {4, 1, -1, -1, -1, 0, -1, -1, -1, -1, -1}, {5, 2, -1, -1, -1, 0, -1, -1, -1, -1, -1},
+                                    {4, 3, -1, -1, -1, 0, -1, -1, -1, -1, -1}, {6, 2, -1, -1, -1, 0, -1, -1, -1, -1, -1}};
   const int nslots = (int)srv->slots.size();
   double best = 1e300;
   om_tuning pick = cands[0];

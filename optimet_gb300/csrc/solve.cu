@@ -87,6 +87,34 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec_part(const M *S, long ld,
   }
 }
 
+// k_matvec_part<float2, float2> that also writes the bf16 copy of S (ld ldc)
+__global__ void __launch_bounds__(kMvThreads) k_matvec_part_copy(const float2 *S, long ld, long n,
+                                                                const float2 *x, float2 *part, int row_tiles,
+                                                                long tiles, unsigned long long *next, int cols,
+                                                                Bf16c *copy, long ldc) {
+  __shared__ float2 xs[kMvCols];
+  __shared__ long tile;
+  for(;;) {
+    __syncthreads();
+    if(threadIdx.x == 0)
+      tile = (long)atomicAdd(next, 1ull);
+    __syncthreads();
+    const long t = tile;
+    if(t >= tiles)
+      break;
+    const long ct = t / row_tiles, rt = t - ct * row_tiles;
+    const long i = rt * kMvThreads + threadIdx.x;
+    const long j0 = ct * cols;
+    const long j1 = min(n, j0 + cols);
+    for(long j = j0 + threadIdx.x; j < j1; j += kMvThreads)
+      xs[j - j0] = x[j];
+    __syncthreads();
+    if(i >= n)
+      continue;
+    part[ct * n + i] = mv_row_copy(S + j0 * ld + i, ld, xs, j0, j1, copy + j0 * ldc + i, ldc);
+  }
+}
+
 // Complex64 matrix times a complex128 vector with FP64-accurate results from
 // FP32 arithmetic (the precision form's refinement residuals): x is split as
 // x_hi + x_lo (floats); the products s * x_hi are made error-free with FMA
@@ -286,7 +314,7 @@ void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, cons
   if constexpr(sizeof(M) == sizeof(float2) && !df)
     if(ctx->mv_tma)
       done = launch_matvec_tma(ctx, (const float2 *)S, n, (const float2 *)x, (float2 *)part, row_tiles, tiles,
-                               mv_cols(ctx, n), grid);
+                               mv_cols(ctx, n), grid, nullptr, 0);
   if(done) {
   } else if constexpr(df)
     k_matvec_part_df<<<grid, kMvThreads, 0, ctx->stream>>>((const float2 *)S, n, n,
@@ -298,6 +326,53 @@ void matvec(om_context *ctx, const M *S, long n, const V *x, V *part, V *y, cons
                                                               ctx->d_tile_counter, mv_cols(ctx, n));
   timer_end(ctx, ev);
   k_matvec_reduce<V><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(part, nsplit, n, b, y);
+  ctx->last_launches += 2;
+}
+
+// The bf16 copy of a complex64 matrix for the inner FP32 GMRES (ld a
+// multiple of 4, so that a column starts on a 16-byte boundary).
+struct Bf16Copy {
+  Bf16c *H = nullptr;
+  long ld = 0;
+  bool ready = false;  // written by an earlier product of this solve
+};
+
+// y = S x for the inner FP32 GMRES of the precision form. With a copy: the
+// first product runs on the complex64 matrix and writes the copy as it reads
+// S; the later ones read the copy (4 bytes per entry instead of 8). TMA-staged
+// kernels where the context uses them, else the register-prefetching ones.
+void matvec_inner(om_context *ctx, const float2 *S, long n, Bf16Copy *hc, const float2 *x, float2 *part,
+                  float2 *y) {
+  if(!hc || !hc->H) {
+    matvec<float2, float2>(ctx, S, n, x, part, y, nullptr);
+    return;
+  }
+  const int nsplit = mv_nsplit(ctx, n);
+  const int row_tiles = (int)((n + kMvThreads - 1) / kMvThreads);
+  const long tiles = (long)row_tiles * nsplit;
+  const unsigned grid = (unsigned)std::max(1L, std::min(tiles, (long)ctx->sm_count * ctx->mv_ctas));
+  const int cols = mv_cols(ctx, n);
+  const bool first = !hc->ready;
+  auto &ev = first ? ctx->ev_mvcp : ctx->ev_mv16;
+  timer_begin(ctx, ev);
+  cudaMemsetAsync(ctx->d_tile_counter, 0, sizeof(unsigned long long), ctx->stream);
+  bool done = false;
+  if(first) {
+    if(ctx->mv_tma)
+      done = launch_matvec_tma(ctx, S, n, x, part, row_tiles, tiles, cols, grid, hc->H, hc->ld);
+    if(!done)
+      k_matvec_part_copy<<<grid, kMvThreads, 0, ctx->stream>>>(S, n, n, x, part, row_tiles, tiles,
+                                                               ctx->d_tile_counter, cols, hc->H, hc->ld);
+    hc->ready = true;
+  } else {
+    if(ctx->mv_tma)
+      done = launch_matvec_bf16(ctx, hc->H, n, hc->ld, x, part, row_tiles, tiles, cols, grid);
+    if(!done)
+      k_matvec_part<Bf16c, float2><<<grid, kMvThreads, 0, ctx->stream>>>(hc->H, hc->ld, n, x, part, row_tiles,
+                                                                        tiles, ctx->d_tile_counter, cols);
+  }
+  timer_end(ctx, ev);
+  k_matvec_reduce<float2><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(part, nsplit, n, nullptr, y);
   ctx->last_launches += 2;
 }
 
@@ -534,11 +609,24 @@ struct InnerGmres32 : PrecondFn {
   Work w;
   float2 *Vb, *r, *part, *hd, *yd, *xz;
   int total = 0;
+  Work hw;       // the bf16 copy of S (inner_bf16), made by the first product
+  Bf16Copy hc;
   InnerGmres32(om_context *c, const float2 *S_, long n_, int m_, double tol_)
       : ctx(c), S(S_), n(n_), m(m_), tol(tol_) {
     w.ctx = c;
+    hw.ctx = c;
   }
   int init() {
+    if(ctx->inner_bf16) {
+      // within the budget, else the products stay on the complex64 matrix
+      const long ld = (n + 3) / 4 * 4;
+      if(alloc_work(ctx, hw, sizeof(Bf16c) * (size_t)ld * n + 256) == OM_OK) {
+        hc.H = static_cast<Bf16c *>(hw.buf);
+        hc.ld = ld;
+      } else {
+        ctx->err.clear();
+      }
+    }
     const int nsplit = mv_nsplit(ctx, n);
     const int nblk = (int)((n + kDotRows - 1) / kDotRows);
     size_t bytes = sizeof(float2) * ((size_t)(m + 1) * n + 2 * n +
@@ -567,7 +655,7 @@ struct InnerGmres32 : PrecondFn {
     double cur = 1.0;
     while(k < m && cur > tol) {
       float2 *wv = Vb + (size_t)(k + 1) * n;
-      matvec<float2, float2>(ctx, S, n, Vb + (size_t)k * n, part, wv, nullptr);
+      matvec_inner(ctx, S, n, &hc, Vb + (size_t)k * n, part, wv);
       std::vector<std::complex<double>> h;
       arnoldi_orth<float2>(ctx, Vb, n, k + 1, wv, part, hd, h);
       const double hn = h[k + 1].real();
@@ -2219,6 +2307,36 @@ int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, const V *
 }
 
 }  // namespace
+
+// `products` inner FP32 GMRES products y = S x on device buffers, the bf16
+// copy made by the first one when the context's inner_bf16 is set (the test
+// entry point om_matvec_inner_c64).
+int inner_products(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *y, int products) {
+  Work w;
+  w.ctx = ctx;
+  const size_t ld = (size_t)(n + 3) / 4 * 4;
+  const size_t part = (size_t)mv_nsplit(ctx, n) * n;
+  int rc = alloc_work(ctx, w, sizeof(float2) * part + sizeof(Bf16c) * ld * n + 1024);
+  if(rc)
+    return rc;
+  size_t off = 0;
+  float2 *pt = w.take<float2>(part, off);
+  Bf16Copy hc;
+  if(ctx->inner_bf16) {
+    hc.H = w.take<Bf16c>(ld * n, off);
+    hc.ld = (long)ld;
+  }
+  for(int p = 0; p < products; ++p)
+    matvec_inner(ctx, S, n, &hc, x, pt, y);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if(e == cudaSuccess)
+    e = cudaGetLastError();
+  if(e != cudaSuccess) {
+    ctx->err = std::string("inner product: ") + cudaGetErrorString(e);
+    return OM_ERR_CUDA;
+  }
+  return OM_OK;
+}
 
 // Direct solve of S X = Q for the given harmonic. The FP64 matrix is factored
 // in a copy (S stays available for residuals and repeated solves).

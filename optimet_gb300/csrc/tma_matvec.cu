@@ -5,11 +5,19 @@
 // taken from a counter by a capped grid, x chunk in shared memory, one row
 // per thread, partial sums per column chunk. Here the tile's columns arrive
 // in stages of 16 columns (256 x 16 complex64 = 32 KB, one 2-D TMA box of the
-// column-major matrix) through a 4-deep ring of shared-memory buffers, each
+// column-major matrix) through a ring of shared-memory buffers, each
 // with an mbarrier that the TMA completes by transaction bytes. Thread 0
 // issues the copies; after all threads have consumed a buffer it refills it
 // with the stage four ahead. The arithmetic and its order per thread are those
 // of the plain kernel, so the results are bitwise the same.
+//
+// The same kernel serves the precision form's bf16 copy of the matrix
+// (kBf16): 4-byte entries (real part in the low 16 bits, imaginary in the
+// high), 32 columns per 32 KB stage, unpacked to FP32 by two bit operations and
+// accumulated in FP32 in the same order. The first inner product of a solve
+// runs on the complex64 matrix and writes that copy as it goes (`copy`: each
+// entry rounded to nearest even, coalesced 4-byte stores), so the copy costs
+// one extra write of 4 bytes per entry and no extra read.
 //
 // Waits are bounded: every thread polls the stage's barrier a bounded number
 // of times and the CTA decides together (a barrier with an OR reduction)
@@ -23,13 +31,30 @@
 #include <type_traits>
 
 #include "om_internal.h"
+#include "om_krylov.cuh"
 
 namespace om {
 
 namespace {
 
-constexpr int kTmaRows = 256, kTmaStageCols = 16, kTmaStages = 4;
-constexpr uint32_t kStageBytes = kTmaRows * kTmaStageCols * sizeof(float2);
+constexpr int kTmaRows = 256;
+constexpr uint32_t kStageBytes = 32768;  // 256 rows x 16 complex64 or 32 bf16 columns
+// Stages in the ring: four for the complex64 matrix (one CTA per SM); two for
+// the bf16 copy, whose product does twice the arithmetic per byte and
+// measured 0.66 of the copy peak with four stages (one CTA of eight warps per
+// SM) and 0.90 with two (three CTAs per SM) at n = 16,000.
+template <bool kBf16> struct TmaEntry {
+  typedef float2 T;
+  static constexpr int kCols = 16;
+  static constexpr int kStages = 4;
+  static __device__ __forceinline__ float2 load(const T &v) { return v; }
+};
+template <> struct TmaEntry<true> {
+  typedef Bf16c T;
+  static constexpr int kCols = 32;
+  static constexpr int kStages = 2;
+  static __device__ __forceinline__ float2 load(const T &v) { return mv_entry<float2>(v); }
+};
 
 __device__ __forceinline__ uint32_t sa(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -64,12 +89,16 @@ __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity) {
   return false;
 }
 
+template <bool kBf16>
 __global__ void __launch_bounds__(kTmaRows) k_matvec_tma(const __grid_constant__ CUtensorMap tm, long n,
                                                           const float2 *x, float2 *part, int row_tiles,
                                                           long tiles, unsigned long long *next, int cols,
-                                                          int *err) {
+                                                          int *err, Bf16c *copy, long ldc) {
+  typedef typename TmaEntry<kBf16>::T E;
+  constexpr int kTmaStageCols = TmaEntry<kBf16>::kCols;
+  constexpr int kTmaStages = TmaEntry<kBf16>::kStages;
   extern __shared__ __align__(128) unsigned char tsm_[];
-  float2 *stage = reinterpret_cast<float2 *>(tsm_);  // [kTmaStages][kTmaStageCols][kTmaRows]
+  E *stage = reinterpret_cast<E *>(tsm_);  // [kTmaStages][kTmaStageCols][kTmaRows]
   float2 *xs = reinterpret_cast<float2 *>(tsm_ + kTmaStages * kStageBytes);
   __shared__ __align__(8) uint64_t bar[kTmaStages];
   __shared__ long tile;
@@ -126,12 +155,14 @@ __global__ void __launch_bounds__(kTmaRows) k_matvec_tma(const __grid_constant__
         }
         break;
       }
-      const float2 *sb = stage + (size_t)slot * kTmaStageCols * kTmaRows;
+      const E *sb = stage + (size_t)slot * kTmaStageCols * kTmaRows;
       const long cb = j0 + (long)s * kTmaStageCols;
       const int ccount = (int)min((long)kTmaStageCols, j1 - cb);
       if(i < n) {
         for(int c = 0; c < ccount; ++c) {
-          const float2 a = sb[c * kTmaRows + t];
+          const float2 a = TmaEntry<kBf16>::load(sb[c * kTmaRows + t]);
+          if(!kBf16 && copy)
+            copy[(cb + c) * ldc + i] = pack_bf16c(a);
           const long j = cb + c;
           const float2 xv = xs[j - j0];
           const bool alt = j < full8 && ((j - j0) & 1);
@@ -186,26 +217,53 @@ EncodeFn encode_fn() {
 
 void *tensor_map_encoder() { return reinterpret_cast<void *>(encode_fn()); }
 
-// Launches the TMA matvec (false when the tensor map cannot be made: the
-// caller then runs the plain kernel).
+// Launches the TMA matvec on the complex64 matrix S (ld n), writing its bf16
+// copy into `copy` (ld ldc) when that is not null; false when the tensor map
+// cannot be made (the caller then runs the plain kernel).
 bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *part, int row_tiles,
-                       long tiles, int cols, unsigned grid) {
+                       long tiles, int cols, unsigned grid, void *copy, long ldc) {
   EncodeFn enc = encode_fn();
   if(!enc || (reinterpret_cast<uintptr_t>(S) & 15) || (n & 1))
     return false;
   alignas(64) CUtensorMap tm;
   const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
   const cuuint64_t strides[1] = {(cuuint64_t)n * sizeof(float2)};
-  const cuuint32_t box[2] = {kTmaRows, kTmaStageCols};
+  const cuuint32_t box[2] = {kTmaRows, (cuuint32_t)TmaEntry<false>::kCols};
   const cuuint32_t estr[2] = {1, 1};
   if(enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<float2 *>(S), dims, strides, box, estr,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return false;
-  const size_t smem = kTmaStages * kStageBytes + (size_t)cols * sizeof(float2);
-  cudaFuncSetAttribute(k_matvec_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_matvec_tma<<<grid, kTmaRows, smem, ctx->stream>>>(tm, n, x, part, row_tiles, tiles, ctx->d_tile_counter,
-                                                      cols, ctx->d_tma_err);
+  const size_t smem = TmaEntry<false>::kStages * kStageBytes + (size_t)cols * sizeof(float2);
+  cudaFuncSetAttribute(k_matvec_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_matvec_tma<false><<<grid, kTmaRows, smem, ctx->stream>>>(tm, n, x, part, row_tiles, tiles,
+                                                             ctx->d_tile_counter, cols, ctx->d_tma_err,
+                                                             static_cast<Bf16c *>(copy), ldc);
+  return true;
+}
+
+// The same product on the bf16 copy H (n x n, ld ldh, ldh a multiple of 4 so
+// that its column stride is a multiple of 16 bytes); false when the tensor map
+// cannot be made.
+bool launch_matvec_bf16(om_context *ctx, const void *H, long n, long ldh, const float2 *x, float2 *part,
+                        int row_tiles, long tiles, int cols, unsigned grid) {
+  EncodeFn enc = encode_fn();
+  if(!enc || (reinterpret_cast<uintptr_t>(H) & 15) || (ldh & 3))
+    return false;
+  alignas(64) CUtensorMap tm;
+  const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)ldh * sizeof(uint32_t)};
+  const cuuint32_t box[2] = {kTmaRows, (cuuint32_t)TmaEntry<true>::kCols};
+  const cuuint32_t estr[2] = {1, 1};
+  if(enc(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void *>(H), dims, strides, box, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  const size_t smem = TmaEntry<true>::kStages * kStageBytes + (size_t)cols * sizeof(float2);
+  cudaFuncSetAttribute(k_matvec_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_matvec_tma<true><<<grid, kTmaRows, smem, ctx->stream>>>(tm, n, x, part, row_tiles, tiles,
+                                                            ctx->d_tile_counter, cols, ctx->d_tma_err, nullptr,
+                                                            0);
   return true;
 }
 
