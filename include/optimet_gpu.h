@@ -163,11 +163,13 @@ typedef struct {
                             most 1,024 padded unknowns, 2 for those of at most 4,096, 0 never
                             (the lockstep Arnoldi steps of all slots as captured graphs); the
                             same bits either way */
-  int inner_bf16;        /* OM_SOLVE_FGMRES_MIXED: the inner FP32 GMRES reads a bf16 copy of the
-                            complex64 matrix (4 bytes per entry; its first product writes the copy
-                            while it reads the complex64 matrix) when 1 (default), the complex64
-                            matrix itself when 0; the outer FP64 residuals always use the
-                            complex64 matrix */
+  int inner_half;        /* the inner FP32 products of the precision form read a 4-byte copy of the
+                            complex64 matrix when 1 (default), the complex64 matrix itself when 0;
+                            the FP64 residuals always use the complex64 matrix. OM_SOLVE_FGMRES_MIXED:
+                            a bf16 copy, written by the first inner product while it reads the
+                            complex64 matrix. om_batch_solve (GMRES-based refinement): an fp16 copy
+                            with a power-of-two scale per 256-row block and column, written by one
+                            launch after the batch's assembly */
 } om_tuning;
 int om_context_tune(om_context *ctx, const om_tuning *t);
 /* C (m x n) -= A (m x k) B (k x n), complex64 interleaved, column-major, any
@@ -180,7 +182,7 @@ int om_context_tune(om_context *ctx, const om_tuning *t);
 /* y = S x, complex64 interleaved (S column-major n x n, host buffers), by the
  * inner FP32 GMRES product of OM_SOLVE_FGMRES_MIXED repeated `products`
  * times: the first on the complex64 matrix (writing its bf16 copy when the
- * context's inner_bf16 tuning is on), the later ones on the copy; y is the
+ * context's inner_half tuning is on), the later ones on the copy; y is the
  * last product. The role of the FP32 matvecs inside the reference's GMRES
  * iterations (PreconditionedMatrix.cpp:892-1133). */
 int om_matvec_inner_c64(om_context *ctx, long n, const float *S, const float *x, float *y, int products);

@@ -69,7 +69,7 @@ class Tuning(C.Structure):
                 ("assemble_carveout", C.c_int), ("matvec_carveout", C.c_int),
                 ("lu_tensor_cores", C.c_int), ("matvec_tma", C.c_int),
                 ("assemble_rotation", C.c_int), ("lu_persistent", C.c_int), ("batch_tiles", C.c_int),
-                ("batch_fused", C.c_int), ("inner_bf16", C.c_int)]
+                ("batch_fused", C.c_int), ("inner_half", C.c_int)]
 
 
 class Request(C.Structure):
@@ -209,11 +209,11 @@ class Context:
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
              matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1,
-             batch_fused=-1, inner_bf16=-1):
+             batch_fused=-1, inner_half=-1):
         """Launch tuning (om_context_tune); 0 / -1 keep the current value."""
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
                    lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles,
-                   batch_fused, inner_bf16)
+                   batch_fused, inner_half)
         self.check(lib().om_context_tune(self.h, C.byref(t)))
 
     def timers(self, enable=True):
@@ -458,7 +458,7 @@ def cgemm_sub_c64(ctx: Context, A, B, C_):
 def matvec_inner(ctx: Context, S, x, products: int = 1) -> np.ndarray:
     """y = S x by the precision form's inner FP32 product, `products` times
     (om_matvec_inner_c64): the first on the complex64 matrix (it writes the
-    bf16 copy when inner_bf16 is on), the later ones on the copy."""
+    bf16 copy when inner_half is on), the later ones on the copy."""
     S = np.asfortranarray(S, dtype=np.complex64)
     x = np.ascontiguousarray(x, dtype=np.complex64)
     n = S.shape[0]
@@ -579,10 +579,10 @@ class Server:
 
     def tune(self, matvec_ctas_per_sm=0, matvec_df_ctas_per_sm=0, assemble_carveout=-1,
              matvec_carveout=-1, lu_tensor_cores=-1, matvec_tma=-1, assemble_rotation=-1, lu_persistent=-1, batch_tiles=-1,
-             batch_fused=-1, inner_bf16=-1):
+             batch_fused=-1, inner_half=-1):
         t = Tuning(matvec_ctas_per_sm, matvec_df_ctas_per_sm, assemble_carveout, matvec_carveout,
                    lu_tensor_cores, matvec_tma, assemble_rotation, lu_persistent, batch_tiles,
-                   batch_fused, inner_bf16)
+                   batch_fused, inner_half)
         rc = lib().om_server_tune(self.h, C.byref(t))
         if rc:
             raise OptimetError(rc, "server tune")

@@ -64,6 +64,8 @@ constexpr int kMaxSlots = 256;   // slots per batch (one thread per slot in the 
 struct Slot {
   long n;          // unknowns; 0 = empty slot
   const void *S;   // matrix, column-major, ld = n
+  const F16c *H;   // precision form: the Arnoldi products' fp16 copy (ld = n), or null
+  const float *D;  // its scales: D[b n + j] for rows [256 b, 256 b + 256) of column j
   double bnorm;    // ||b||; negative until the first cycle
   double rho;      // ||b - S x|| at the start of the latest cycle
   double thr;      // this cycle's stop threshold on |g_{j+1}|
@@ -154,12 +156,24 @@ __global__ void __launch_bounds__(R) k_b_mv(const Slot *st, const int4 *tiles, c
     if(!st[d.x].inner)
       continue;
     const long n = st[d.x].n;
-    const M *S = (const M *)st[d.x].S;
+    const M *S = (const M *)(std::is_same<M, F16c>::value ? (const void *)st[d.x].H : st[d.x].S);
     const V *x = Vb + d.x * vslot + (long)jcol * np;
     const long i = (long)d.y * R + threadIdx.x;
     const long j0 = (long)d.z * kBCols, j1 = min(n, j0 + kBCols);
-    for(long j = j0 + threadIdx.x; j < j1; j += R)
-      xs[j - j0] = x[j];
+    if constexpr(std::is_same<M, F16c>::value) {
+      // x times the scales of the tile's 256-row block
+      const float *Dc = st[d.x].D + ((long)d.y * R / 256) * n;
+      for(long j = j0 + threadIdx.x; j < j1; j += R) {
+        V v = x[j];
+        const float f = Dc[j];
+        v.x = v.x * f;
+        v.y = v.y * f;
+        xs[j - j0] = v;
+      }
+    } else {
+      for(long j = j0 + threadIdx.x; j < j1; j += R)
+        xs[j - j0] = x[j];
+    }
     __syncthreads();
     if(i < n)
       part[((long)d.x * nsm + d.z) * np + i] = mv_row<M, V>(S + j0 * n + i, n, xs, 0L, j1 - j0);
@@ -562,6 +576,57 @@ __global__ void k_b_update(const Slot *st, const V *Vb, long vslot, long np, con
   x[s * np + i] = acc;
 }
 
+// The fp16 copies of a batch's complex64 matrices (precision form): per
+// matrix, column j and 256-row block b, the scale d = 2^(e - 15) with e the
+// exponent of the block column's largest part (frexp), D[b n + j] = d and
+// H = fp16(S / d), round to nearest even. One warp per (matrix, column,
+// block) item; items numbered matrix by matrix (first[m] = the matrix's
+// first item).
+struct CvMat {
+  const float2 *S;
+  F16c *H;
+  float *D;
+  long n, first;
+};
+__global__ void __launch_bounds__(256) k_b_tof16(const CvMat *mats, int nmats, long items) {
+  const int lane = threadIdx.x & 31;
+  const long warps = (long)gridDim.x * (blockDim.x / 32);
+  for(long q = (long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); q < items; q += warps) {
+    int lo = 0, hi = nmats - 1;  // the matrix whose items hold q
+    while(lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if(mats[mid].first <= q)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const CvMat mt = mats[lo];
+    const long nb = (mt.n + 255) / 256, r = q - mt.first, j = r / nb, b = r - j * nb;
+    float2 v[8];
+    float mx = 0.f;
+#pragma unroll
+    for(int u = 0; u < 8; ++u) {
+      const long i = b * 256 + lane + 32 * u;
+      v[u] = i < mt.n ? mt.S[j * mt.n + i] : make_float2(0.f, 0.f);
+      mx = fmaxf(mx, fmaxf(fabsf(v[u].x), fabsf(v[u].y)));
+    }
+    for(int o = 16; o > 0; o >>= 1)
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if(mx > 0.f)
+      frexpf(mx, &e);
+    const float up = ldexpf(1.f, 15 - e);
+#pragma unroll
+    for(int u = 0; u < 8; ++u) {
+      const long i = b * 256 + lane + 32 * u;
+      if(i < mt.n)
+        mt.H[j * mt.n + i] = F16c{__floats2half2_rn(v[u].x * up, v[u].y * up)};
+    }
+    if(lane == 0)
+      mt.D[b * mt.n + j] = ldexpf(1.f, e - 15);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Fused solves of the small size classes (at most kFusedRows padded
 // unknowns): one cooperative launch runs every slot's restarted GMRES /
@@ -723,6 +788,7 @@ __global__ void __launch_bounds__(kBT) k_b_fused(FusedArgs<V> a) {
       continue;
     const long n = sl.n;
     const M *S = (const M *)sl.S;
+    const F16c *Hf = sl.H;  // precision form: the Arnoldi products read the fp16 copy when set
     const long r0 = (long)c * kFRows, r1 = min(n, r0 + kFRows);  // r1 <= r0: no rows of this slot
     const int nb = (int)((n + kFRows - 1) / kFRows);
     const int ns = (int)((n + kBCols - 1) / kBCols);
@@ -848,6 +914,19 @@ __global__ void __launch_bounds__(kBT) k_b_fused(FusedArgs<V> a) {
               o.x = v.x * inv_s;
               o.y = v.y * inv_s;
             }
+            if constexpr(kDF) {
+              if(Hf) {  // the values k_b_mv stages: v_j times each 256-row block's scales
+#pragma unroll
+                for(int q = 0; q < 2; ++q) {
+                  const float f = sl.D[(2L * c + q) * n + jj];
+                  V t;
+                  t.x = o.x * f;
+                  t.y = o.y * f;
+                  xs[q * kBCols + jj - j0] = t;
+                }
+                continue;
+              }
+            }
             xs[jj - j0] = o;
           }
           __syncthreads();
@@ -856,7 +935,15 @@ __global__ void __launch_bounds__(kBT) k_b_fused(FusedArgs<V> a) {
             const long i = r0 + q * kBT + tid;
             if(i >= r1)
               continue;
-            const V v = mv_row<M, V>(S + j0 * n + i, n, xs, 0L, j1 - j0);
+            V v;
+            if constexpr(kDF) {
+              if(Hf)
+                v = mv_row<F16c, V>(Hf + j0 * n + i, n, xs + q * kBCols, 0L, j1 - j0);
+              else
+                v = mv_row<M, V>(S + j0 * n + i, n, xs, 0L, j1 - j0);
+            } else {
+              v = mv_row<M, V>(S + j0 * n + i, n, xs, 0L, j1 - j0);
+            }
             if(cc == 0) {
               acc[q] = v;
             } else {
@@ -1016,9 +1103,10 @@ int pad_spheres(int N) {
 struct ClassKey {
   int precision, nmax, Npad, m, max_cycles;
   double tol, inner_rel;
+  int f16;  // precision form: the Arnoldi products read scaled fp16 copies of the matrices
   bool operator<(const ClassKey &o) const {
-    return std::tie(precision, nmax, Npad, m, max_cycles, tol, inner_rel) <
-           std::tie(o.precision, o.nmax, o.Npad, o.m, o.max_cycles, o.tol, o.inner_rel);
+    return std::tie(precision, nmax, Npad, m, max_cycles, tol, inner_rel, f16) <
+           std::tie(o.precision, o.nmax, o.Npad, o.m, o.max_cycles, o.tol, o.inner_rel, o.f16);
   }
 };
 
@@ -1083,6 +1171,8 @@ template <typename M, typename V> struct Class {
   Ctl *h_ctl = nullptr;
   int4 *h_tiles = nullptr;
   BatchMat *h_mats = nullptr;
+  CvMat *h_cv = nullptr;  // nbuf x 2B: the fp16 conversion's matrix table
+  CvMat *cv = nullptr;
   double *h_xsec = nullptr;  // 8 per slot: the FF and SH cross sections
   cudaEvent_t ev_main = nullptr;        // main stream -> auxiliary streams
   std::vector<cudaEvent_t> ev_aux;      // auxiliary streams -> main / assembly stream
@@ -1130,7 +1220,8 @@ template <typename M, typename V> struct Class {
                    Bz * sizeof(double2) * m * (m + 1), Bz * sizeof(double2) * m,
                    Bz * sizeof(double2) * m, Bz * sizeof(double2) * (m + 1), Bz * sizeof(double2) * m,
                    Bz * sizeof(double), sizeof(unsigned long long),
-                   np <= kFusedRows ? Bz * 2 * sizeof(V) * np : 0, Bz * 32 * sizeof(unsigned) + 16};
+                   np <= kFusedRows ? Bz * 2 * sizeof(V) * np : 0, Bz * 32 * sizeof(unsigned) + 16,
+                   2 * Bz * nbuf * sizeof(CvMat)};
     bytes = 0;
     for(size_t v : sz)
       bytes += rup(v);
@@ -1166,11 +1257,13 @@ template <typename M, typename V> struct Class {
     wbuf = (V *)take(sz[i++]);
     fbar = (unsigned *)take(sz[i++]);
     ferr = (int *)(fbar + 32 * Bz);
+    cv = (CvMat *)take(sz[i++]);
     if(cudaMallocHost(&h_st, Bz * sizeof(Slot)) != cudaSuccess ||
        cudaMallocHost(&h_ferr, sizeof(int)) != cudaSuccess ||
        cudaMallocHost(&h_ctl, sizeof(Ctl)) != cudaSuccess ||
        cudaMallocHost(&h_tiles, sizeof(int4) * (size_t)max_tiles) != cudaSuccess ||
        cudaMallocHost(&h_mats, 2 * Bz * nbuf * sizeof(BatchMat)) != cudaSuccess ||
+       cudaMallocHost(&h_cv, 2 * Bz * nbuf * sizeof(CvMat)) != cudaSuccess ||
        cudaMallocHost(&h_xsec, 8 * Bz * sizeof(double)) != cudaSuccess) {
       cudaGetLastError();
       ctx->err = "pinned host staging for the batch";
@@ -1257,6 +1350,15 @@ template <typename M, typename V> struct Class {
   }
 
   void launch_mv(cudaStream_t s) {
+    if constexpr(std::is_same<M, float2>::value) {
+      if(key.f16) {
+        if(mv.rows == 128)
+          k_b_mv<F16c, V, 128><<<mv_grid, 128, 0, s>>>(st, tiles, ctl, Vb, vslot, np, nsm, (V *)part, counter);
+        else
+          k_b_mv<F16c, V, 256><<<mv_grid, 256, 0, s>>>(st, tiles, ctl, Vb, vslot, np, nsm, (V *)part, counter);
+        return;
+      }
+    }
     if(mv.rows == 128)
       k_b_mv<M, V, 128><<<mv_grid, 128, 0, s>>>(st, tiles, ctl, Vb, vslot, np, nsm, (V *)part, counter);
     else
@@ -1336,6 +1438,7 @@ template <typename M, typename V> struct Class {
     if(h_ctl) cudaFreeHost(h_ctl);
     if(h_tiles) cudaFreeHost(h_tiles);
     if(h_mats) cudaFreeHost(h_mats);
+    if(h_cv) cudaFreeHost(h_cv);
     if(h_xsec) cudaFreeHost(h_xsec);
     if(h_ferr) cudaFreeHost(h_ferr);
     if(ev_main) cudaEventDestroy(ev_main);
@@ -1578,6 +1681,12 @@ struct Pending {
   void *mbuf = nullptr;          // the batch's FF and SH matrices
   size_t mbytes = 0;
   std::vector<size_t> off_ff, off_sh;  // per slot: element offsets into mbuf
+  // precision form with fp16 copies: mbuf = [complex64 matrices][their fp16
+  // copies at the same offsets][scales]; scale offsets per slot
+  size_t elems = 0, scales = 0;
+  std::vector<size_t> soff_ff, soff_sh;
+  F16c *copies() const { return reinterpret_cast<F16c *>(static_cast<float2 *>(mbuf) + elems); }
+  float *scale_base() const { return reinterpret_cast<float *>(copies() + elems); }
 };
 
 // Set-up of a batch and its assembly: request s lives on auxiliary context
@@ -1625,7 +1734,25 @@ void prepare_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const 
       elems += nn;
     }
   }
-  P.mbytes = std::max<size_t>(elems, 1) * sizeof(M);
+  // the fp16 copies and their scales (ceil(n / 256) x n per matrix)
+  P.elems = elems;
+  P.scales = 0;
+  P.soff_ff.assign(P.nb, 0);
+  P.soff_sh.assign(P.nb, 0);
+  if(key.f16)
+    for(int s = 0; s < P.nb; ++s) {
+      if(!P.pr[s])
+        continue;
+      const size_t n = (size_t)P.pr[s]->n, ns = (n + 255) / 256 * n;
+      P.soff_ff[s] = P.scales;
+      P.scales += ns;
+      if(reqs[idx[P.b0 + s]].wave.sh) {
+        P.soff_sh[s] = P.scales;
+        P.scales += ns;
+      }
+    }
+  P.mbytes = std::max<size_t>(elems, 1) * sizeof(M) +
+             (key.f16 ? elems * sizeof(F16c) + P.scales * sizeof(float) : 0);
   if(dev_malloc(ctx, &P.mbuf, P.mbytes)) {
     P.mbuf = nullptr;
     for(int s = 0; s < P.nb; ++s)
@@ -1667,6 +1794,31 @@ void prepare_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const 
   launch_assemble_batch(ctx, key.nmax, key.precision, dm, nmats, (int)((long)key.Npad * (key.Npad + 1) / 2),
                         ctx->stream_lo);
   *launches += ctx->last_launches - L0;
+  if constexpr(std::is_same<M, float2>::value) {
+    if(key.f16 && P.mbuf) {  // the fp16 copies, on the same stream after the assembly
+      CvMat *hc = cl.h_cv + (size_t)2 * cl.B * P.buf;
+      int nc = 0;
+      long items = 0;
+      for(int s = 0; s < P.nb; ++s) {
+        if(!P.pr[s])
+          continue;
+        const long n = P.pr[s]->n, per = (n + 255) / 256 * n;
+        hc[nc++] = CvMat{S + P.off_ff[s], P.copies() + P.off_ff[s], P.scale_base() + P.soff_ff[s], n, items};
+        items += per;
+        if(reqs[idx[P.b0 + s]].wave.sh) {
+          hc[nc++] = CvMat{S + P.off_sh[s], P.copies() + P.off_sh[s], P.scale_base() + P.soff_sh[s], n, items};
+          items += per;
+        }
+      }
+      if(nc) {
+        CvMat *dc = cl.cv + (size_t)2 * cl.B * P.buf;
+        cudaMemcpyAsync(dc, hc, sizeof(CvMat) * nc, cudaMemcpyHostToDevice, ctx->stream_lo);
+        const long blocks = std::min<long>((items + 7) / 8, 8L * ctx->sm_count);
+        k_b_tof16<<<(unsigned)blocks, 256, 0, ctx->stream_lo>>>(dc, nc, items);
+        ++*launches;
+      }
+    }
+  }
   cudaEventRecord(cl.ev_asm[P.buf], ctx->stream_lo);
 }
 
@@ -1695,6 +1847,10 @@ int finish_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const st
     if(s < nb && pr[s]) {
       z.n = pr[s]->n;
       z.S = (const M *)P.mbuf + P.off_ff[s];
+      if(key.f16) {
+        z.H = P.copies() + P.off_ff[s];
+        z.D = P.scale_base() + P.soff_ff[s];
+      }
       z.outer = 1;
       cudaMemcpyAsync(cl.b + (size_t)s * np, pr[s]->d_Q, sizeof(double2) * z.n,
                       cudaMemcpyDeviceToDevice, ctx->stream);
@@ -1743,6 +1899,10 @@ int finish_batch(om_context *ctx, const ClassKey &key, Class<M, V> &cl, const st
     if(s < nb && pr[s] && reqs[idx[P.b0 + s]].wave.sh && pr[s]->d_K && pr[s]->d_acs) {
       z.n = pr[s]->n;
       z.S = (const M *)P.mbuf + P.off_sh[s];
+      if(key.f16) {
+        z.H = P.copies() + P.off_sh[s];
+        z.D = P.scale_base() + P.soff_sh[s];
+      }
       z.outer = 1;
       run = true;
       cudaMemcpyAsync(cl.b + (size_t)s * np, pr[s]->d_K, sizeof(double2) * z.n,
@@ -1888,7 +2048,8 @@ int run_class(om_context *ctx, const ClassKey &key, const std::vector<int> &idx,
   size_t maxmat = 0;
   for(int i : idx) {
     const size_t n = 2 * (size_t)pmax(key.nmax) * reqs[i].n_spheres;
-    maxmat = std::max(maxmat, sizeof(M) * n * n * (reqs[i].wave.sh ? 2 : 1));
+    maxmat = std::max(maxmat, (sizeof(M) * n * n + (key.f16 ? sizeof(F16c) * n * n + 4 * n * ((n + 255) / 256) : 0)) *
+                                  (reqs[i].wave.sh ? 2 : 1));
   }
   auto slots_for = [&](int nbuf) {
     const size_t per = Class<M, V>::slot_bytes(np, key.m, nbuf) + nbuf * maxmat;
@@ -2000,7 +2161,9 @@ size_t batch_request_bytes(const om_request &rq) {
   const size_t elem = mixed ? sizeof(float2) : sizeof(double2);
   const size_t m = (size_t)std::max(1, mixed ? o.inner_iter : o.max_iter);
   const size_t nsm = (np + kBCols - 1) / kBCols;
-  return elem * n * n * (rq.wave.sh ? 2 : 1) + elem * (m + 1) * np + sizeof(double2) * (3 + nsm) * np +
+  // (the precision form's matrices with their fp16 copies and scales)
+  const size_t mat = elem * n * n + (mixed ? sizeof(F16c) * n * n + 4 * n * ((n + 255) / 256) : 0);
+  return mat * (rq.wave.sh ? 2 : 1) + elem * (m + 1) * np + sizeof(double2) * (3 + nsm) * np +
          sizeof(double2) * (m + 2) * (m + 2) * 2 + (size_t(64) << 20);
 }
 
@@ -2065,6 +2228,7 @@ extern "C" int om_batch_solve(om_context *ctx, const om_request *reqs, int count
     k.max_cycles = mixed ? std::min(o.max_iter, 32) * o.restarts : o.restarts;
     k.tol = o.tol;
     k.inner_rel = mixed ? o.inner_tol : 0.0;
+    k.f16 = mixed && ctx->inner_half ? 1 : 0;
     classes[k].push_back(i);
   }
   bool bad = false;

@@ -445,8 +445,8 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
     ctx->batch_tiles = std::min(t->batch_tiles, 8);
   if(t->batch_fused >= 0)
     ctx->batch_fused = std::min(t->batch_fused, 2);
-  if(t->inner_bf16 >= 0)
-    ctx->inner_bf16 = t->inner_bf16 ? 1 : 0;
+  if(t->inner_half >= 0)
+    ctx->inner_half = t->inner_half ? 1 : 0;
   return OM_OK;
 }
 

@@ -132,9 +132,10 @@ struct om_context {
   // classes of at most 1,024 padded unknowns, 2 for those of at most 4,096,
   // 0 the lockstep graphs for every class
   int batch_fused = 1;
-  // precision-form FGMRES: the inner FP32 GMRES reads a bf16 copy of the
-  // complex64 matrix (written by its first product) when 1
-  int inner_bf16 = 1;
+  // precision form: the inner FP32 products read a 4-byte copy of the
+  // complex64 matrix when 1 (FGMRES: bf16, written by the first product; the
+  // batching form: scaled fp16, written after the batch's assembly)
+  int inner_half = 1;
   int asm_rot = 1;  // precision-form assembly by rotated z-axis translations (assemble_rot.cu)
   size_t budget = 0;
   size_t used = 0;
@@ -309,7 +310,7 @@ void *tensor_map_encoder();
 bool launch_matvec_tma(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *part, int row_tiles,
                        long tiles, int cols, unsigned grid, void *copy, long ldc);
 // solve.cu: `products` inner FP32 GMRES products on device buffers (the first
-// writes the bf16 copy when ctx->inner_bf16 is set, the later ones read it)
+// writes the bf16 copy when ctx->inner_half is set, the later ones read it)
 int inner_products(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *y, int products);
 // the same product on the bf16 copy (Bf16c entries, ld ldh a multiple of 4)
 bool launch_matvec_bf16(om_context *ctx, const void *H, long n, long ldh, const float2 *x, float2 *part,

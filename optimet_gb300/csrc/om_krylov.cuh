@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace om {
@@ -22,12 +23,24 @@ __device__ __forceinline__ Bf16c pack_bf16c(float2 a) {  // round to nearest eve
   return Bf16c{re | (im << 16)};
 }
 
+// An entry of the batching form's fp16 copy of a complex64 matrix: both parts
+// as fp16 after the entry's column in its 256-row block was scaled by a power
+// of two (the block column's largest part lands in [2^14, 2^15)); the
+// products take x times that scale's inverse, so that h (x d) = (h d) x with d
+// exact.
+struct F16c {
+  __half2 v;
+};
+
 // a matrix entry as the vector type of a product
 template <typename V, typename M> __device__ __forceinline__ V mv_entry(const M &s) {
   V a;
   a.x = s.x;
   a.y = s.y;
   return a;
+}
+template <> __device__ __forceinline__ float2 mv_entry<float2, F16c>(const F16c &s) {
+  return __half22float2(s.v);
 }
 template <> __device__ __forceinline__ float2 mv_entry<float2, Bf16c>(const Bf16c &s) {
   return make_float2(__uint_as_float(s.v << 16), __uint_as_float(s.v & 0xffff0000u));

@@ -609,7 +609,7 @@ struct InnerGmres32 : PrecondFn {
   Work w;
   float2 *Vb, *r, *part, *hd, *yd, *xz;
   int total = 0;
-  Work hw;       // the bf16 copy of S (inner_bf16), made by the first product
+  Work hw;       // the bf16 copy of S (inner_half), made by the first product
   Bf16Copy hc;
   InnerGmres32(om_context *c, const float2 *S_, long n_, int m_, double tol_)
       : ctx(c), S(S_), n(n_), m(m_), tol(tol_) {
@@ -617,7 +617,7 @@ struct InnerGmres32 : PrecondFn {
     hw.ctx = c;
   }
   int init() {
-    if(ctx->inner_bf16) {
+    if(ctx->inner_half) {
       // within the budget, else the products stay on the complex64 matrix
       const long ld = (n + 3) / 4 * 4;
       if(alloc_work(ctx, hw, sizeof(Bf16c) * (size_t)ld * n + 256) == OM_OK) {
@@ -2309,7 +2309,7 @@ int lu_solve_vec(om_context *ctx, const V *A, long n, const int *perm, const V *
 }  // namespace
 
 // `products` inner FP32 GMRES products y = S x on device buffers, the bf16
-// copy made by the first one when the context's inner_bf16 is set (the test
+// copy made by the first one when the context's inner_half is set (the test
 // entry point om_matvec_inner_c64).
 int inner_products(om_context *ctx, const float2 *S, long n, const float2 *x, float2 *y, int products) {
   Work w;
@@ -2322,7 +2322,7 @@ int inner_products(om_context *ctx, const float2 *S, long n, const float2 *x, fl
   size_t off = 0;
   float2 *pt = w.take<float2>(part, off);
   Bf16Copy hc;
-  if(ctx->inner_bf16) {
+  if(ctx->inner_half) {
     hc.H = w.take<Bf16c>(ld * n, off);
     hc.ld = (long)ld;
   }

@@ -185,6 +185,30 @@ def test_fused_solve_matches_the_lockstep_graphs(G, form):
     assert launches[0] < launches[1]
 
 
+def test_fp16_copies_in_the_batch(G):
+    """The precision form's Arnoldi products on the scaled fp16 copies
+    (inner_half = 1, the default) and on the complex64 matrices (0): both
+    within 1e-6 of the FP64 single-request path, a few refinement cycles
+    each."""
+    reqs = ragged_requests(G, mixed(G), G.C64, seed=31) + blocky_requests(G, mixed(G), G.C64, seed=32)
+    runs = {}
+    for half in (1, 0):
+        c = G.Context(0)
+        c.tune(inner_half=half)
+        runs[half] = G.batch_solve(c, reqs)
+        c.close()
+    c = G.Context(0)
+    for i, (sp, bg, wave, opts, prec) in enumerate(reqs):
+        xs, xsh, _ = G.wavelength_solve_sh(c, sp, bg, wave, plain(G), G.C128)
+        for half in (1, 0):
+            r = runs[half][i]
+            assert r["status"] == G.OK and 1 <= r["ff"]["iterations"] <= 8
+            assert rel(r["xsec"], xs) < 1e-6
+            if wave.sh:
+                assert rel(r["xsec_sh"], xsh) < 1e-6
+    c.close()
+
+
 def test_failures_stay_with_their_request(G, ctx):
     rng = np.random.default_rng(3)
     xyz, rad = random_cluster(rng, 4, 800 * nm, 40 * nm, 60 * nm, 20 * nm)

@@ -49,7 +49,7 @@ def test_bf16_copy_products(G, n):
     out = {}
     for tma in (1, 0):
         c = G.Context(0)
-        c.tune(matvec_tma=tma, inner_bf16=1)
+        c.tune(matvec_tma=tma, inner_half=1)
         out[tma] = [G.matvec_inner(c, S, x, p) for p in (1, 2, 3)]
         c.close()
     y1, y2, y3 = out[1]
@@ -60,7 +60,7 @@ def test_bf16_copy_products(G, n):
     for a, b in zip(out[1], out[0]):
         assert np.array_equal(a, b)       # TMA-staged and plain kernels: the same bits
     c = G.Context(0)
-    c.tune(inner_bf16=0)
+    c.tune(inner_half=0)
     assert np.array_equal(G.matvec_inner(c, S, x, 2), y1)
     c.close()
 
@@ -85,7 +85,7 @@ def test_fgmres_with_bf16_inner(G, oracle):
                      inner_tol=1e-4)
     res = {}
     for on in (1, 0):
-        c.tune(inner_bf16=on)
+        c.tune(inner_half=on)
         c.timers(True)
         st = pr.solve(opts)
         c.timers(False)
