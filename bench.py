@@ -809,6 +809,10 @@ def serve_arm(args):
                      "completed": int(len(lat)),
                      "refused_budget": int(sum(r["status"] == G.ERR_BUDGET for r in res)),
                      "other_failures": int(sum(r["status"] not in (G.OK, G.ERR_BUDGET) for r in res)),
+                     "failed": [{"request": i, "status": r["status"], "N": q["N"], "nmax": q["nmax"],
+                                 "sh": int(q["wave"].sh)}
+                                for i, (r, q) in enumerate(zip(res, reqs))
+                                if r["status"] not in (G.OK, G.ERR_BUDGET)][:20],
                      "service_ms_by_N": {f"{lo}-{hi}": float(np.median([r["service_ms"] for r, q in zip(res, reqs)
                                                                         if lo <= q["N"] <= hi] or [0]))
                                          for lo, hi in ((1, 10), (11, 30), (31, 100), (101, 300))},

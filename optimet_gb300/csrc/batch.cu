@@ -578,7 +578,7 @@ __global__ void k_b_update(const Slot *st, const V *Vb, long vslot, long np, con
 
 // The fp16 copies of a batch's complex64 matrices (precision form): per
 // matrix, column j and 256-row block b, the scale d = 2^(e - 15) with e the
-// exponent of the block column's largest part (frexp), D[b n + j] = d and
+// exponent of the block column's largest part (frexp, at least -100), D[b n + j] = d and
 // H = fp16(S / d), round to nearest even. One warp per (matrix, column,
 // block) item; items numbered matrix by matrix (first[m] = the matrix's
 // first item).
@@ -615,6 +615,10 @@ __global__ void __launch_bounds__(256) k_b_tof16(const CvMat *mats, int nmats, l
     int e = 0;
     if(mx > 0.f)
       frexpf(mx, &e);
+    // block columns of tiny entries (high orders of small spheres reach 1e-35
+    // and below) keep finite, normal scales: e >= -100 bounds 2^(15 - e) by
+    // 2^115 and d by 2^-115 (their entries then stay below 2^15 as well)
+    e = max(e, -100);
     const float up = ldexpf(1.f, 15 - e);
 #pragma unroll
     for(int u = 0; u < 8; ++u) {

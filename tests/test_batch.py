@@ -209,6 +209,29 @@ def test_fp16_copies_in_the_batch(G):
     c.close()
 
 
+def test_fp16_copies_with_tiny_block_columns(G):
+    """Small spheres at long wavelengths with a large nMax: the high-order
+    block columns of S fall to 1e-35 and below, where an unclamped fp16 scale
+    overflows (its zero entries then turned into NaN). The batched precision
+    form must converge to the same cross sections with and without the
+    copies."""
+    rng = np.random.default_rng(41)
+    reqs = []
+    for N, nmax in [(20, 9), (12, 11), (30, 7)]:
+        xyz, rad = random_cluster(rng, N, 900 * nm, 30 * nm, 34 * nm, 20 * nm)
+        sp = G.spheres_array(xyz, rad, (1.6 + 0.002j) ** 2, nmax)
+        reqs.append((sp, G.medium(1.0), G.plane_wave(890 * nm), mixed(G), G.C64))
+    runs = {}
+    for half in (1, 0):
+        c = G.Context(0)
+        c.tune(inner_half=half)
+        runs[half] = G.batch_solve(c, reqs)
+        c.close()
+    for a, b in zip(runs[1], runs[0]):
+        assert a["status"] == b["status"] == G.OK
+        assert np.all(np.isfinite(a["xsec"])) and rel(a["xsec"], b["xsec"]) < 1e-6
+
+
 def test_failures_stay_with_their_request(G, ctx):
     rng = np.random.default_rng(3)
     xyz, rad = random_cluster(rng, 4, 800 * nm, 40 * nm, 60 * nm, 20 * nm)
