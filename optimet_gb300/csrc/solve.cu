@@ -1468,57 +1468,80 @@ __global__ void __launch_bounds__(kPanThreads) k_pan_coop_sm(V *A, long ld, long
 
 // The row interchanges of rows k .. k + nb - 1 (pivots piv[k .. k + nb), in
 // order) as one permutation: (position, row) pairs, the new row at each
-// position they move; pos_row[0] = the count, then the pairs. One thread
-// (nb <= 256 steps): the rows at positions k .. k + nb - 1 in a table, the
-// rows moved below them in a list whose last entry for a position counts.
+// position they move; pos_row[0] = the count, then the pairs. One warp: the
+// interchanges are applied in order (nb <= 256 steps) to a table of the rows
+// at positions k .. k + nb - 1 and to a list of the rows moved below them,
+// whose last entry for a position counts; the lanes search that list
+// together and emit the pairs in order (the table's positions ascending, then
+// the list's live entries from the last one back).
 constexpr int kPermMax = 256;  // interchanges per table
 __global__ void k_lu_perm_table(const int *piv, long k, int nb, long *pos_row) {
   __shared__ long row_at[kPermMax], ext_pos[kPermMax], ext_row[kPermMax];
-  if(threadIdx.x != 0)
-    return;
-  for(int c = 0; c < nb; ++c)
+  __shared__ unsigned char live[kPermMax];
+  const int lane = threadIdx.x;
+  for(int c = lane; c < nb; c += 32)
     row_at[c] = k + c;
+  __syncwarp();
   int ext = 0;
   for(int c = 0; c < nb; ++c) {
     const long p = piv[k + c];
     if(p == k + c)
       continue;
-    const long a = row_at[c];
-    long b;
     if(p - k < nb) {
-      b = row_at[p - k];
-      row_at[p - k] = a;
+      if(lane == 0) {
+        const long a = row_at[c];
+        row_at[c] = row_at[p - k];
+        row_at[p - k] = a;
+      }
     } else {
-      b = p;  // the row now at p: the latest entry for p, else p itself
-      for(int e = ext - 1; e >= 0; --e)
-        if(ext_pos[e] == p) {
-          b = ext_row[e];
-          break;
-        }
-      ext_pos[ext] = p;
-      ext_row[ext] = a;
+      int last = -1;  // the latest list entry for position p
+      for(int e = lane; e < ext; e += 32)
+        if(ext_pos[e] == p)
+          last = e;
+      last = __reduce_max_sync(0xffffffffu, last);
+      if(lane == 0) {
+        const long a = row_at[c];
+        row_at[c] = last >= 0 ? ext_row[last] : p;
+        ext_pos[ext] = p;
+        ext_row[ext] = a;
+      }
       ++ext;
     }
-    row_at[c] = b;
+    __syncwarp();
   }
-  long cnt = 0;
-  for(int c = 0; c < nb; ++c)
-    if(row_at[c] != k + c) {
-      pos_row[1 + 2 * cnt] = k + c;
-      pos_row[2 + 2 * cnt] = row_at[c];
-      ++cnt;
-    }
-  for(int e = ext - 1; e >= 0; --e) {
+  // list entries that no later entry for the same position overrides
+  for(int e = lane; e < ext; e += 32) {
     bool later = false;
     for(int f = e + 1; f < ext; ++f)
       later |= ext_pos[f] == ext_pos[e];
-    if(!later) {
-      pos_row[1 + 2 * cnt] = ext_pos[e];
-      pos_row[2 + 2 * cnt] = ext_row[e];
-      ++cnt;
-    }
+    live[e] = !later;
   }
-  pos_row[0] = cnt;
+  __syncwarp();
+  long cnt = 0;
+  for(int c0 = 0; c0 < nb; c0 += 32) {  // table positions, ascending
+    const int c = c0 + lane;
+    const bool moved = c < nb && row_at[c] != k + c;
+    const unsigned m = __ballot_sync(0xffffffffu, moved);
+    if(moved) {
+      const long at = cnt + __popc(m & ((1u << lane) - 1u));
+      pos_row[1 + 2 * at] = k + c;
+      pos_row[2 + 2 * at] = row_at[c];
+    }
+    cnt += __popc(m);
+  }
+  for(int e0 = ext - 1; e0 >= 0; e0 -= 32) {  // list entries, from the last one back
+    const int e = e0 - lane;
+    const bool take = e >= 0 && live[e];
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    if(take) {
+      const long at = cnt + __popc(m & ((1u << lane) - 1u));
+      pos_row[1 + 2 * at] = ext_pos[e];
+      pos_row[2 + 2 * at] = ext_row[e];
+    }
+    cnt += __popc(m);
+  }
+  if(lane == 0)
+    pos_row[0] = cnt;
 }
 
 // The permutation of k_lu_perm_table applied to the columns jlo .. jhi - 1
