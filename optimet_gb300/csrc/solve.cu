@@ -1578,7 +1578,9 @@ __global__ void __launch_bounds__(256) k_lu_permute(V *A, long ld, long jlo, lon
 }
 
 // U12 = L11^{-1} A12 (unit lower L11: rows and columns k .. k + nb - 1) for
-// the columns jlo .. jhi - 1, one thread per column.
+// the columns jlo .. jhi - 1, one thread per column; products and
+// differences written with explicit fused and unfused operations, as in the
+// panels.
 template <typename V>
 __global__ void k_lu_trsm(V *A, long ld, long jlo, long jhi, long k, int nb) {
   __shared__ V L[kNb][kNb];
@@ -1590,16 +1592,40 @@ __global__ void k_lu_trsm(V *A, long ld, long jlo, long jhi, long k, int nb) {
   const long j = jlo + blockIdx.x * (long)blockDim.x + threadIdx.x;
   if(j >= jhi)
     return;
+  V *col = A + j * ld + k;
+  if(nb == kNb) {
+    // the full block: the column's 32 loads issued together, the
+    // substitution in registers, then the stores
+    V xr[kNb];
+#pragma unroll
+    for(int r = 0; r < kNb; ++r)
+      xr[r] = col[r];
+#pragma unroll
+    for(int r = 1; r < kNb; ++r) {
+      V v = xr[r];
+#pragma unroll
+      for(int s = 0; s < r; ++s) {
+        const V p = cmul(L[r][s], xr[s]);
+        v.x = sub_rn(v.x, p.x);
+        v.y = sub_rn(v.y, p.y);
+      }
+      xr[r] = v;
+    }
+#pragma unroll
+    for(int r = 0; r < kNb; ++r)
+      col[r] = xr[r];
+    return;
+  }
   V x[kNb];
   for(int r = 0; r < nb; ++r) {
-    V v = A[j * ld + k + r];
+    V v = col[r];
     for(int s = 0; s < r; ++s) {
-      V l = L[r][s];
-      v.x -= l.x * x[s].x - l.y * x[s].y;
-      v.y -= l.x * x[s].y + l.y * x[s].x;
+      const V p = cmul(L[r][s], x[s]);
+      v.x = sub_rn(v.x, p.x);
+      v.y = sub_rn(v.y, p.y);
     }
     x[r] = v;
-    A[j * ld + k + r] = v;
+    col[r] = v;
   }
 }
 
