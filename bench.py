@@ -873,7 +873,8 @@ def tc_update_arm(args):
     wall = time.perf_counter() - t0
     ctx.close()
     return {"workload": f"tensor-core rank-{k} update, {m} x {m} complex64",
-            "kernel": {1: "k_cgemm_sub_tc3 (persistent)", 2: "k_cgemm_sub_tc2 (one CTA per tile)"}.get(
+            "kernel": {1: "k_cgemm_sub_tc3 (persistent)", 2: "k_cgemm_sub_tc2 (one CTA per tile)",
+                       3: "k_cgemm_sub_tc3 (persistent) for k > 64, else k_cgemm_sub_tc2"}.get(
                 args.lu_update, "none"),
             "wall_s_with_copies": wall, "checksum": float(np.abs(out[:4, :4]).sum())}
 
@@ -946,6 +947,8 @@ def lu_mixed_arm(args):
             "config": {"workload": args.lu_case + " LU role: " + w["desc"],
                        "solver": "GMRES-based iterative refinement: FP64 residuals, GMRES on the system left-preconditioned by the FP32 LU (tensor-core trailing updates), tol 1e-9",
                        "trailing_update": {1: "persistent", 2: "one CTA per tile",
+                                           3: "persistent for the trailing updates, one CTA per tile "
+                                              "for the rank-32 in-block and U12 updates",
                                            0: "FP32 CUDA cores, rank 32"}[args.lu_update],
                        "panels_and_sweeps": {1: "one launch per panel / sweep",
                                              2: "per-column panel launches, per-block sweep launches"}[args.lu_persistent]},
@@ -1247,8 +1250,9 @@ def main():
     ap.add_argument("--c4-seconds", type=float, default=60.0)
     ap.add_argument("--batch-slots", type=int, default=6, help="server slots for c3 / c4")
     ap.add_argument("--c4-forms", default="mixed,fp64", help="c4: forms to run (comma-separated)")
-    ap.add_argument("--lu-update", type=int, default=1, choices=[0, 1, 2],
-                    help="c2lu: trailing-update kernel (1 persistent, 2 one CTA per tile, 0 FP32 CUDA cores)")
+    ap.add_argument("--lu-update", type=int, default=3, choices=[0, 1, 2, 3],
+                    help="c2lu: trailing-update kernel (1 persistent, 2 one CTA per tile, 3 persistent for "
+                         "rank 256 and one CTA per tile for rank 32, 0 FP32 CUDA cores)")
     ap.add_argument("--lu-case", default="c2", choices=sorted(WORKLOADS),
                     help="c2lu: the cluster of the LU role's solve (c2 by default)")
     ap.add_argument("--tc-m", type=int, default=8192, help="tcupd: rows and columns of C")

@@ -141,8 +141,11 @@ typedef struct {
   int matvec_df_ctas_per_sm;
   int assemble_carveout;
   int matvec_carveout;
-  int lu_tensor_cores;   /* complex64 LU trailing updates on the tensor cores: 1 (default,
-                            persistent: one CTA per SM), 2 (one CTA per 128 x 64 tile), 0 off */
+  int lu_tensor_cores;   /* complex64 LU updates on the tensor cores: 3 (default) the persistent
+                            kernel (one CTA per SM) for the rank-256 trailing updates and one CTA
+                            per 128 x 64 tile for the rank-32 in-block and U12 updates, 1 the
+                            persistent kernel for all, 2 one CTA per tile for all (the same bits
+                            in all three), 0 off */
   int matvec_tma;        /* complex64 x complex64 matvec with TMA-staged matrix tiles: 1 (default for
                             a context) / 0 (default for the slots of a server with several slots) */
   int assemble_rotation; /* complex64 assembly by rotated z-axis translations (one recurrence

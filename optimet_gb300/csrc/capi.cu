@@ -434,7 +434,7 @@ int om_context_tune(om_context *ctx, const om_tuning *t) {
   if(t->matvec_carveout >= 0)
     ctx->carve_mv = t->matvec_carveout;
   if(t->lu_tensor_cores >= 0)
-    ctx->lu_tc = std::min(t->lu_tensor_cores, 2);
+    ctx->lu_tc = std::min(t->lu_tensor_cores, 3);
   if(t->matvec_tma >= 0)
     ctx->mv_tma = t->matvec_tma ? 1 : 0;
   if(t->assemble_rotation >= 0)

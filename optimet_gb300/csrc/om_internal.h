@@ -118,9 +118,10 @@ struct om_context {
   int *d_tma_err = nullptr;                      // set by a TMA matvec whose wait timed out
   int mv_tma = 1;                                // complex64 matvecs staged by TMA
   int carve_asm = -1, carve_mv = -1;  // preferred smem carveout (percent), -1 = driver's choice
-  // complex64 LU trailing updates on the tensor cores: 1 persistent kernel,
-  // 2 one CTA per tile, 0 off (FP32 CUDA cores)
-  int lu_tc = 1;
+  // complex64 LU updates on the tensor cores: 3 the persistent kernel for the
+  // rank-256 trailing updates and one CTA per tile for the rank-32 ones,
+  // 1 persistent for all, 2 one CTA per tile for all, 0 off (FP32 CUDA cores)
+  int lu_tc = 3;
   // LU kernels: 1 one cooperative launch per tall panel (its rows in shared
   // memory when they fit) and one launch per triangular sweep, 2 per-column
   // panel launches and per-block sweep launches, 3 as 1 with the panel rows

@@ -797,8 +797,11 @@ void launch_cgemm_sub_tc_split(om_context *ctx, const float2 *A, long lda, const
   // the persistent form reads C by tensor copies: a 16-byte aligned base and
   // an even leading dimension (column stride a multiple of 16 bytes)
   alignas(64) CUtensorMap cmap;
-  bool persistent = ctx->lu_tc == 1 && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
-                    (ldc & 1) == 0;
+  // (lu_tc 3: the one-CTA-per-tile kernel for the rank-32 in-block and U12
+  // updates, whose few MMA steps per tile leave the persistent kernel waiting
+  // on its C ring; the same bits either way)
+  bool persistent = (ctx->lu_tc == 1 || (ctx->lu_tc == 3 && k > 64)) &&
+                    (reinterpret_cast<uintptr_t>(C) & 15) == 0 && (ldc & 1) == 0;
   if(persistent) {
     typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,

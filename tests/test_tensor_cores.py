@@ -73,7 +73,7 @@ def test_persistent_update_matches_tile_grid(G, ctx, m, n, k):
     for tc in (1, 2):
         ctx.tune(lu_tensor_cores=tc)
         out[tc] = G.cgemm_sub_c64(ctx, A, B, C)
-    ctx.tune(lu_tensor_cores=1)
+    ctx.tune(lu_tensor_cores=3)
     assert np.array_equal(np.ascontiguousarray(out[1]).view(np.float32),
                           np.ascontiguousarray(out[2]).view(np.float32))
     ref = C.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
@@ -92,11 +92,13 @@ def test_lu_mixed_with_and_without_tensor_cores(G, ctx, N, nmax):
     ref = G.wavelength_solve(ctx, sp, bg, wave, G.options(G.SOLVE_LU), G.C128)[0]
     opts = G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4)
     out = {}
-    for tc in (1, 2, 0):
+    for tc in (3, 1, 2, 0):
         ctx.tune(lu_tensor_cores=tc)
         xs, _, _, st = G.wavelength_solve(ctx, sp, bg, wave, opts, G.C64)
         out[tc] = (xs, st.iterations)
-    ctx.tune(lu_tensor_cores=1)
+    # the hybrid (3) takes the same bits as both single-kernel forms
+    assert np.array_equal(out[3][0], out[1][0]) and np.array_equal(out[3][0], out[2][0])
+    ctx.tune(lu_tensor_cores=3)
     for tc, (xs, it) in out.items():
         err = np.abs(xs - ref) / np.abs(ref)
         # C_ext, C_sca and C_ext - C_sca to 1e-6; C_abs comes from the internal
@@ -178,7 +180,7 @@ def test_cooperative_panels_give_the_same_factors(G, ctx):
         st = pr.solve(G.options(G.SOLVE_LU_MIXED, tol=1e-10, max_iter=30, restarts=4))
         out[mode] = (x64, pr.coefficients()[0].copy(), st.iterations)
         pr.close()
-    ctx.tune(lu_tensor_cores=1, lu_persistent=1)
+    ctx.tune(lu_tensor_cores=3, lu_persistent=1)
     for mode in (2, 3):
         assert np.array_equal(out[1][0], out[mode][0])
         assert np.array_equal(out[1][1], out[mode][1]) and out[1][2] == out[mode][2]
