@@ -783,7 +783,7 @@ def serve_arm(args):
     reqs = c4_requests(args.c4_rate, args.c4_seconds)
     bg = G.medium(1.0)
     forms = {"mixed": (G.options(G.SOLVE_FGMRES_MIXED, tol=1e-8, max_iter=30, restarts=4,
-                                 inner_iter=60, inner_tol=1e-4), G.C64),
+                                 inner_iter=60, inner_tol=args.c3_inner_tol), G.C64),
              "fp64": (G.options(G.SOLVE_GMRES, tol=1e-10, max_iter=300, restarts=6), G.C128)}
     forms = {k: v for k, v in forms.items() if k in args.c4_forms.split(",")}
     out = {}
