@@ -922,6 +922,8 @@ __global__ void __launch_bounds__(kBT) k_b_fused(FusedArgs<V> a) {
               if(Hf) {  // the values k_b_mv stages: v_j times each 256-row block's scales
 #pragma unroll
                 for(int q = 0; q < 2; ++q) {
+                  if((2L * c + q) * 256 >= n)
+                    break;  // no rows of the slot in this block (nor a scale column)
                   const float f = sl.D[(2L * c + q) * n + jj];
                   V t;
                   t.x = o.x * f;
